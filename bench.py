@@ -1,0 +1,342 @@
+"""Throughput benchmark of the GB300 transport path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload c2|c1]
+
+A step is one full render of the workload: every pixel of the film at the
+configured samples per pixel (c2: 1024x1024 x 256 spp over the 512^3 CT-like
+shell volume; c1: 256x256 x 64 spp over the 128^3 blob volume).  Inputs are
+seeded synthetic volumes (the reference ships no dataset).
+
+value : samples/s of the transport kernel with the scene resident in HBM,
+        CUDA events on the launching stream, max over ranks.
+e2e   : the same metric through the C ABI a user calls, with host buffers:
+        per step the volume and tracer descriptor are copied host->device
+        (BindVolume / BindTracer), the render runs (RenderSpp) and the RGBA8
+        estimate is read back (GetEstimate).
+--impl reference : the reference's transport code on the host cores (the
+        reference build in oracle/_ref when it exists for this machine, else
+        the C restatement of oracle/), all threads, each step a bounded
+        sample (a film crop at 1 spp) of the same workload.
+Multi-GPU (torchrun): independent replicas, one view per rank, no data-path
+collective; value = all ranks' samples / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "c2": dict(name="c2-ct-shells-512^3-1024^2-256spp", res=512, film=(1024, 1024), spp=256),
+    "c1": dict(name="c1-blobs-128^3-256^2-64spp", res=128, film=(256, 256), spp=64),
+}
+# algorithmic bytes per sample: 16 bytes per reference volume lookup (8 corners
+# x uint16) plus one float4 accumulate read+write, with the mean lookups per
+# sample of the reference estimator measured by the oracle on the workload
+BYTES_PER_LOOKUP = 16.0
+BYTES_PER_SAMPLE_FIXED = 32.0
+
+
+def make_scene(wl):
+    S = importlib.import_module("exposure-render_gb300.scenes")
+    if wl == "c2":
+        return S.scene_c2(res=512, film=WORKLOADS[wl]["film"], spp=WORKLOADS[wl]["spp"])
+    return S.scene_c1(res=128, film=WORKLOADS[wl]["film"], spp=WORKLOADS[wl]["spp"])
+
+
+def reference_shading(scene):
+    """Settings the current kernels implement for every workload: the live
+    reference shading (BRDF volume shader, light-sampling estimator)."""
+    s = scene.tracer.settings
+    s.apply_shading_type = 0
+    s.mis = 0
+    s.free_flight = 0
+    return "brdf-light-sampling (reference live path)"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = "clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+            "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 7:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[3:7]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return json.load(open(p)), "measured"
+    return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def profile_traffic(wl):
+    """DRAM bytes per sample of the transport kernel from a committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"traffic_{wl}.json")
+    if os.path.exists(p):
+        return json.load(open(p))
+    return None
+
+
+def lookups_per_sample(scene, nthreads, crop=24):
+    """Mean reference-estimator volume lookups per sample on a centre crop (oracle)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as OL
+    orc = OL.load_oracle()
+    h = OL.SceneHandle(orc, scene)
+    W, H = scene.width, scene.height
+    x0, y0 = W // 2 - crop // 2, H // 2 - crop // 2
+    h.render_sum(1, rect=(x0, y0, crop, crop), nthreads=nthreads)
+    L = orc.lookups_per_sample()
+    h.close()
+    return L
+
+
+def cpu_reference_rate(scene, seconds_target=12.0, nthreads=None, steps=1):
+    """Samples/s of the reference transport on the host cores (all threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as OL
+    nthreads = nthreads or os.cpu_count() or 1
+    kind = "port"
+    lib = OL.load_oracle()
+    ref = OL.load_ref()
+    if ref is not None:
+        lib, kind = ref, "reference"
+    h = OL.SceneHandle(lib, scene)
+    W, H = scene.width, scene.height
+    # calibrate a crop that takes about seconds_target / steps
+    side = 16
+    t0 = time.perf_counter()
+    h.render_sum(1, rect=(W // 2 - side // 2, H // 2 - side // 2, side, side), nthreads=nthreads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    rate = side * side / dt
+    want = rate * seconds_target / max(steps, 1)
+    side = int(max(16, min(min(W, H), np.sqrt(want))))
+    x0, y0 = W // 2 - side // 2, H // 2 - side // 2
+    rates = []
+    for s in range(steps):
+        t0 = time.perf_counter()
+        h.render_sum(1, first=s, rect=(x0, y0, side, side), nthreads=nthreads)
+        rates.append(side * side / (time.perf_counter() - t0))
+    h.close()
+    return float(np.median(rates)), kind, nthreads, f"{side}x{side} centre crop x 1 spp per step"
+
+
+def run_reference(args, wl, rank, world):
+    if rank != 0:
+        return
+    scene = make_scene(wl)
+    shading = reference_shading(scene)
+    W = WORKLOADS[wl]
+    for _ in range(args.warmup):
+        cpu_reference_rate(scene, seconds_target=2.0, steps=1)
+    rate, kind, cores, sample = cpu_reference_rate(scene, seconds_target=10.0 * max(1, args.steps) / 3.0, steps=args.steps)
+    line = {
+        "impl": "reference", "metric": "Msamples/s", "value": rate / 1e6, "unit": "Msamples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": W["name"], "film": list(W["film"]), "spp": W["spp"], "shading": shading},
+        "cpu_baseline": {"value": rate / 1e6, "unit": "Msamples/s", "cores": cores, "kind": kind, "sample": sample},
+        "e2e": {"value": rate / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, wl, rank, world, local_rank):
+    import torch
+    torch.cuda.set_device(local_rank)
+    pkg = importlib.import_module("exposure-render_gb300")
+    runtime = importlib.import_module("exposure-render_gb300.runtime")
+    C = pkg.capi
+    lib = C.load_library()
+    C.check(lib.er_set_device(local_rank))
+    W = WORKLOADS[wl]
+    scene = make_scene(wl)
+    shading = reference_shading(scene)
+    scene.tracer.settings.seed = 1 + rank                # one replica view per rank
+    r = runtime.Renderer(scene, lib)
+    spp = W["spp"]
+    width, height = scene.width, scene.height
+    stream = torch.cuda.current_stream()
+    C.check(lib.er_set_stream(ctypes.c_void_p(stream.cuda_stream)))
+    d_sum = torch.zeros((height, width, 4), dtype=torch.float32, device="cuda")
+
+    def step(k):
+        r.trace_sum_device(d_sum.data_ptr(), spp, rank, k * spp, 0, ctypes.c_void_p(stream.cuda_stream))
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        ev0.record(stream)
+        for k in range(args.steps):
+            step(args.warmup + k)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    samples_per_step = width * height * spp
+    value = world * samples_per_step * args.steps / (ms / 1e3) / 1e6
+
+    # end to end through the C ABI with host buffers
+    vd = scene.volume_desc()
+    vol_bytes = scene.volume.nbytes
+    tr_bytes = ctypes.sizeof(r.tracer_desc)
+    out = np.empty((height, width, 4), dtype=np.uint8)
+    e2e_steps = max(1, min(args.steps, 3))
+
+    def e2e_step():
+        vid = ctypes.c_int32(r.volume_id)
+        C.check(lib.er_bind_volume(ctypes.byref(vd), ctypes.byref(vid)))
+        tid = ctypes.c_int32(r.tracer_id)
+        C.check(lib.er_bind_tracer(ctypes.byref(r.tracer_desc), ctypes.byref(tid)))
+        C.check(lib.er_reset_accumulation(r.tracer_id))
+        C.check(lib.er_render_spp(r.tracer_id, spp))
+        C.check(lib.er_get_estimate(r.tracer_id, out.ctypes.data))
+
+    e2e_step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * samples_per_step * e2e_steps / e2e_s / 1e6
+
+    if rank != 0:
+        return
+    peaks, peak_kind = measured_peaks()
+    nthreads = os.cpu_count() or 1
+    L = lookups_per_sample(scene, nthreads)
+    bytes_per_sample = BYTES_PER_LOOKUP * L + BYTES_PER_SAMPLE_FIXED
+    achieved = bytes_per_sample * samples_per_step * args.steps / (ms / 1e3) / 1e9
+    traffic = profile_traffic(wl)
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+        "peak_source": peak_kind, "kernel": "k_trace_sum",
+        "algorithmic_bytes_per_sample": bytes_per_sample, "reference_lookups_per_sample": L,
+        "traffic": (traffic["dram_bytes_per_launch"] if traffic else None),
+    }
+    cpu_rate, kind, cores, sample = (None, None, None, None)
+    if world == 1:
+        cpu_rate, kind, cores, sample = cpu_reference_rate(scene, seconds_target=12.0, steps=1)
+    line = {
+        "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": W["name"], "film": list(W["film"]), "spp": W["spp"], "shading": shading,
+                   "free_flight": "fixed-step march (reference)", "kernel": "k_trace_sum (reference-order, bit-exact)",
+                   "l2": "inputs larger than L2 (volume %d MiB)" % (vol_bytes >> 20) if vol_bytes > (129 << 20) else
+                   "volume fits in L2 (%d MiB); transport re-reads it from L2" % (vol_bytes >> 20),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "roofline": roofline,
+        "cpu_baseline": ({"value": cpu_rate / 1e6, "unit": "Msamples/s", "cores": cores, "kind": kind, "sample": sample}
+                         if cpu_rate else None),
+        "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(vol_bytes + tr_bytes),
+                "d2h_bytes_per_step": int(out.nbytes)},
+        "clocks": clk.summary(),
+        "gpu_launches": args.steps,
+    }
+    print(json.dumps(line), flush=True)
+    r.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, args.workload, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    run_ours(args, args.workload, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

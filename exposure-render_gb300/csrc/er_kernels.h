@@ -1,0 +1,36 @@
+/*
+ * er_kernels.h - launch functions of the CUDA kernels, called by the host
+ * runtime (er_runtime.cpp).
+ */
+#ifndef ER_KERNELS_H
+#define ER_KERNELS_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "er_device.cuh"
+
+/* spatial (KernelD) and range (GaussSimilarity) weights of the bilateral
+   filter (Source/filter.h:34-40), passed by value */
+struct BilateralTables {
+    int radius;
+    float spatial[256];
+    float range[256];
+};
+
+cudaError_t er_launch_trace_frame(const erd::Params& P, uint32_t* lanes, float4* frame, cudaStream_t s);
+cudaError_t er_launch_trace_sum(const erd::Params& P, int spp, uint32_t view, uint32_t first, float4* sum, int accumulate,
+                                cudaStream_t s);
+cudaError_t er_launch_sigma_table(const erd::Plf* opacity, float density_scale, float* table, int n, cudaStream_t s);
+
+cudaError_t er_launch_post_frame(const float4* frame, float4* running, uchar4* rgba, int W, int H, int n_iter, float exposure,
+                                 int filter, cudaStream_t s);
+cudaError_t er_launch_post_mean(const float4* sum, float n, float4* running, uchar4* rgba, int W, int H, float exposure, int filter,
+                                cudaStream_t s);
+cudaError_t er_launch_tonemap(const float4* xyza, float scale, uchar4* rgba, int n, float exposure, cudaStream_t s);
+cudaError_t er_launch_bilateral(const uchar4* in, uchar4* tmp, uchar4* out, int W, int H, const BilateralTables& T,
+                                cudaStream_t s);
+cudaError_t er_launch_gradient_magnitude(const erd::Params& P, uint16_t* gm, unsigned int* max_bits, cudaStream_t s);
+cudaError_t er_launch_math_eval(int fn, int n, const float* x, const float* y, float* out, cudaStream_t s);
+
+#endif

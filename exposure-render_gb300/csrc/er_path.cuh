@@ -1,0 +1,771 @@
+/*
+ * er_path.cuh - one camera path of Exposure Render's single-scattering
+ * estimator on the GPU, in the reference's evaluation order.
+ *
+ * Function-by-function counterpart of the reference transport code
+ * (Source/singlescattering.h, Source/transport.h, Source/raymarching.h,
+ * Source/lights.h, Source/shader.h, Source/volumes.h, Source/buffer3d.h).
+ * Include only from translation units compiled with --fmad=false.
+ */
+#ifndef ER_PATH_CUH
+#define ER_PATH_CUH
+
+#include <float.h>
+
+#include "er_device.cuh"
+
+namespace erd {
+
+#define ER_PI_F 3.141592654f
+#define ER_INV_PI_F 0.31830988618379067154f
+#define ER_INV_TWO_PI_F 0.15915494309189533577f
+#define ER_RAY_EPS 0.0001f
+#define ER_INV_FOUR_PI_EXPANDED (1.0f / 4.0f * ER_PI_F)   /* INV_FOUR_PI_F as the macro expands */
+
+/* ---- volume access: Source/buffer3d.h:210-242, Source/volume.h:131-138 ---- */
+
+ER_D float voxel(const Params& P, int x, int y, int z)
+{
+    const int cx = iclamp(x, 0, P.res[0] - 1);
+    const int cy = iclamp(y, 0, P.res[1] - 1);
+    const int cz = iclamp(z, 0, P.res[2] - 1);
+    const size_t idx = (size_t)cz * (size_t)P.res[0] * (size_t)P.res[1] + (size_t)cy * (size_t)P.res[0] + (size_t)cx;
+    return (float)__ldg(P.vox + idx);
+}
+
+/* Lerp (Source/geometry.h:87-90) stored into unsigned short: truncation of a
+   non-negative value below 65536 */
+ER_D float lerp_u16(float t, float a, float b)
+{
+    const float r = (1.0f - t) * a + t * b;
+    return truncf(r);
+}
+
+ER_D float get_intensity(const Params& P, v3 p)
+{
+    const v3 off = V3(p.x - P.minp[0], p.y - P.minp[1], p.z - P.minp[2]);
+    const float Lx = off.x * P.inv_size[0] * (float)P.res[0];
+    const float Ly = off.y * P.inv_size[1] * (float)P.res[1];
+    const float Lz = off.z * P.inv_size[2] * (float)P.res[2];
+    const int vx = (int)floorf(Lx);
+    const int vy = (int)floorf(Ly);
+    const int vz = (int)floorf(Lz);
+    const float dx = Lx - (float)vx;
+    const float dy = Ly - (float)vy;
+    const float dz = Lz - (float)vz;
+    const float d00 = lerp_u16(dx, voxel(P, vx, vy, vz), voxel(P, vx + 1, vy, vz));
+    const float d10 = lerp_u16(dx, voxel(P, vx, vy + 1, vz), voxel(P, vx + 1, vy + 1, vz));
+    const float d01 = lerp_u16(dx, voxel(P, vx, vy, vz + 1), voxel(P, vx + 1, vy, vz + 1));
+    const float d11 = lerp_u16(dx, voxel(P, vx, vy + 1, vz + 1), voxel(P, vx + 1, vy + 1, vz + 1));
+    const float d0 = lerp_u16(dy, d00, d10);
+    const float d1 = lerp_u16(dy, d01, d11);
+    return lerp_u16(dz, d0, d1);
+}
+
+/* DensityScale * Opacity1D.Evaluate(I) from the integer-intensity table */
+ER_D float sigma_at(const Params& P, float I)
+{
+    int i = (int)I;
+    i = i < 0 ? 0 : (i >= P.sigma_n ? P.sigma_n - 1 : i);
+    return __ldg(P.sigma + i);
+}
+
+/* ---- gradients: Source/volumes.h:31-114 ---- */
+
+ER_D v3 gdelta(const Params& P, int axis) { return V3(axis == 0 ? P.min_step : 0.0f, axis == 1 ? P.min_step : 0.0f, axis == 2 ? P.min_step : 0.0f); }
+
+ER_D v3 gradient_cd(const Params& P, v3 p)
+{
+    const v3 dx = gdelta(P, 0), dy = gdelta(P, 1), dz = gdelta(P, 2);
+    const float i00 = get_intensity(P, vadd(p, dx)), i01 = get_intensity(P, vsub(p, dx));
+    const float i10 = get_intensity(P, vadd(p, dy)), i11 = get_intensity(P, vsub(p, dy));
+    const float i20 = get_intensity(P, vadd(p, dz)), i21 = get_intensity(P, vsub(p, dz));
+    return V3(i01 - i00, i11 - i10, i21 - i20);
+}
+
+ER_D v3 gradient_fd(const Params& P, v3 p)
+{
+    const float i0 = get_intensity(P, p);
+    const float i1 = get_intensity(P, vadd(p, gdelta(P, 0)));
+    const float i2 = get_intensity(P, vadd(p, gdelta(P, 1)));
+    const float i3 = get_intensity(P, vadd(p, gdelta(P, 2)));
+    return V3(i0 - i1, i0 - i2, i0 - i3);
+}
+
+ER_D v3 vlerp(v3 a, v3 b, float c) { return vadd(a, vscale(vsub(b, a), c)); }
+
+static __device__ __noinline__ v3 gradient_filtered(const Params& P, v3 p)
+{
+    const float o = P.min_step;
+    const v3 G0 = gradient_cd(P, p);
+    const v3 G1 = gradient_cd(P, vadd(p, V3(-o, -o, -o)));
+    const v3 G2 = gradient_cd(P, vadd(p, V3(o, o, o)));
+    const v3 G3 = gradient_cd(P, vadd(p, V3(-o, o, -o)));
+    const v3 G4 = gradient_cd(P, vadd(p, V3(o, -o, o)));
+    const v3 G5 = gradient_cd(P, vadd(p, V3(-o, -o, o)));
+    const v3 G6 = gradient_cd(P, vadd(p, V3(o, o, -o)));
+    const v3 G7 = gradient_cd(P, vadd(p, V3(-o, o, o)));
+    const v3 G8 = gradient_cd(P, vadd(p, V3(o, -o, -o)));
+    const v3 L0 = vlerp(vlerp(G1, G2, 0.5f), vlerp(G3, G4, 0.5f), 0.5f);
+    const v3 L1 = vlerp(vlerp(G5, G6, 0.5f), vlerp(G7, G8, 0.5f), 0.5f);
+    return vlerp(G0, vlerp(L0, L1, 0.5f), 0.75f);
+}
+
+ER_D v3 normalized_gradient(const Params& P, v3 p)
+{
+    v3 g;
+    if (P.gradient_mode == 1) g = gradient_cd(P, p);
+    else if (P.gradient_mode == 2) g = gradient_filtered(P, p);
+    else g = gradient_fd(P, p);
+    return vnorm(g);
+}
+
+ER_D float gradient_magnitude(const Params& P, v3 p)
+{
+    float sum = 0.0f;
+    for (int i = 0; i < 3; i++) {
+        const v3 d = gdelta(P, i);
+        float D = get_intensity(P, vsub(p, d)) - get_intensity(P, vadd(p, d));
+        D *= 0.5f / P.spacing[i];
+        sum += D * D;
+    }
+    return sqrtf(sum);
+}
+
+/* ---- geometry ---- */
+
+struct Ray { v3 O, D; float MinT, MaxT; };
+
+ER_D v3 ray_at(const Ray& r, float t) { return vadd(r.O, vscale(vnorm(r.D), t)); }
+
+struct Isect {
+    bool valid, front;
+    float near_t, far_t;
+    v3 P, N;
+    v2 UV;
+    ER_D void invalid()
+    {
+        valid = false; front = true; near_t = 0.0f; far_t = FLT_MAX;
+        P = V3(0, 0, 0); N = V3(0, 0, 0); UV.x = 0.0f; UV.y = 0.0f;
+    }
+};
+
+ER_D v3 xform_point(const float m[3][4], v3 p)
+{
+    return V3(m[0][0] * p.x + m[0][1] * p.y + m[0][2] * p.z + m[0][3],
+              m[1][0] * p.x + m[1][1] * p.y + m[1][2] * p.z + m[1][3],
+              m[2][0] * p.x + m[2][1] * p.y + m[2][2] * p.z + m[2][3]);
+}
+ER_D v3 xform_vector(const float m[3][4], v3 v)
+{
+    return V3(m[0][0] * v.x + m[0][1] * v.y + m[0][2] * v.z,
+              m[1][0] * v.x + m[1][1] * v.y + m[1][2] * v.z,
+              m[2][0] * v.x + m[2][1] * v.y + m[2][2] * v.z);
+}
+ER_D Ray xform_ray(const float m[3][4], const Ray& r)
+{
+    Ray t;
+    const v3 Pp = xform_point(m, r.O);
+    const v3 MinP = xform_point(m, ray_at(r, r.MinT));
+    const v3 MaxP = xform_point(m, ray_at(r, r.MaxT));
+    t.O = Pp;
+    t.D = vnorm(vsub(MaxP, t.O));
+    t.MinT = vlen(vsub(MinP, t.O));
+    t.MaxT = vlen(vsub(MaxP, t.O));
+    return t;
+}
+
+ER_D float spherical_theta(v3 w) { return er_acosf(eclamp(w.y, -1.0f, 1.0f)); }
+ER_D float spherical_phi(v3 w)
+{
+    const float p = er_atan2f(w.z, w.x);
+    return (p < 0.0f) ? p + 2.0f * ER_PI_F : p;
+}
+
+/* IntersectBox (Source/box.h:51-83); `full` also fills P and N */
+ER_D void intersect_box(const Ray& R, v3 mn, v3 mx, Isect& I, bool full)
+{
+    const v3 InvR = V3(1.0f / R.D.x, 1.0f / R.D.y, 1.0f / R.D.z);
+    const v3 B = vmul(InvR, vsub(mn, R.O));
+    const v3 T = vmul(InvR, vsub(mx, R.O));
+    const v3 MinT = V3(smin(T.x, B.x), smin(T.y, B.y), smin(T.z, B.z));
+    const v3 MaxT = V3(smax(T.x, B.x), smax(T.y, B.y), smax(T.z, B.z));
+    const float LargestMinT = fmaxf(fmaxf(MinT.x, MinT.y), fmaxf(MinT.x, MinT.z));
+    const float LargestMaxT = fminf(fminf(MaxT.x, MaxT.y), fminf(MaxT.x, MaxT.z));
+    if (LargestMaxT < LargestMinT) return;
+    I.near_t = LargestMinT > 0.0f ? LargestMinT : 0.0f;
+    I.far_t = LargestMaxT;
+    if (I.near_t < R.MinT || I.near_t > R.MaxT) return;
+    I.valid = true;
+    if (full) {
+        I.P = ray_at(R, I.near_t);
+        float n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
+        if (I.P.x <= mn.x + 0.0001f) n0 = -1.0f;
+        if (I.P.x >= mx.x - 0.0001f) n0 = 1.0f;
+        if (I.P.y <= mn.y + 0.0001f) n1 = -1.0f;
+        if (I.P.y >= mx.y - 0.0001f) n1 = 1.0f;
+        if (I.P.z <= mn.z + 0.0001f) n2 = -1.0f;
+        if (I.P.z >= mx.z - 0.0001f) n2 = 1.0f;
+        I.N = V3(n0, n1, n2);
+        I.UV.x = 0.0f; I.UV.y = 0.0f;
+    }
+}
+
+/* IntersectPlane(R, OneSided, Int) - Source/plane.h:41-62 */
+ER_D void intersect_plane_inf(const Ray& R, int one_sided, Isect& I)
+{
+    if (fabsf(R.O.z - R.D.z) < ER_RAY_EPS) return;
+    I.near_t = (0.0f - R.O.z) / R.D.z;
+    if (I.near_t < R.MinT || I.near_t > R.MaxT) return;
+    I.P = ray_at(R, I.near_t);
+    I.UV.x = I.P.x; I.UV.y = I.P.y;
+    I.N = V3(0.0f, 0.0f, 1.0f);
+    if (one_sided && R.D.z >= 0.0f) {
+        I.front = false;
+        I.N = V3(0.0f, 0.0f, -1.0f);
+    }
+    I.valid = true;
+}
+
+ER_D float v2len(v2 a) { return sqrtf(a.x * a.x + a.y * a.y); }
+
+ER_D void intersect_shape(const Light& L, const Ray& R, Isect& I)
+{
+    switch (L.type) {
+    case 0: {   /* Source/plane.h:76-88 */
+        intersect_plane_inf(R, L.one_sided, I);
+        const float sx = L.size[0], sy = L.size[1];
+        if (I.valid && (I.UV.x < -0.5f * sx || I.UV.x > 0.5f * sx || I.UV.y < -0.5f * sy || I.UV.y > 0.5f * sy)) I.valid = false;
+        I.UV.x /= sx; I.UV.y /= sy;
+        I.UV.x = I.UV.x + 0.5f; I.UV.y = I.UV.y + 0.5f;
+        I.UV.x = 1.0f - I.UV.x;
+        break;
+    }
+    case 1: {   /* Source/disk.h:37-49 */
+        intersect_plane_inf(R, L.one_sided, I);
+        if (I.valid && v2len(I.UV) > L.outer_radius) I.valid = false;
+        const float dia = 2.0f * L.outer_radius;
+        I.UV.x /= dia; I.UV.y /= dia;
+        I.UV.x = I.UV.x + 0.5f; I.UV.y = I.UV.y + 0.5f;
+        I.UV.x = 1.0f - I.UV.x;
+        break;
+    }
+    case 2: {   /* Source/ring.h:45-57 */
+        intersect_plane_inf(R, L.one_sided, I);
+        if (I.valid && (v2len(I.UV) < L.inner_radius || v2len(I.UV) > L.outer_radius)) I.valid = false;
+        const float dia = 2.0f * L.outer_radius;
+        I.UV.x /= dia; I.UV.y /= dia;
+        I.UV.x = I.UV.x + 0.5f; I.UV.y = I.UV.y + 0.5f;
+        I.UV.x = 1.0f - I.UV.x;
+        break;
+    }
+    case 3: {   /* Source/box.h:85-88 */
+        const v3 s = V3(L.size[0], L.size[1], L.size[2]);
+        intersect_box(R, vscale(s, -0.5f), vscale(s, 0.5f), I, true);
+        break;
+    }
+    case 4: {   /* Source/sphere.h:84-140 */
+        const float r = L.outer_radius;
+        const float a = vdot(R.D, R.D);
+        const float b = 2 * vdot(R.D, R.O);
+        const float c = vdot(R.O, R.O) - (r * r);
+        const float disc = b * b - 4 * a * c;
+        if (disc < 0) return;
+        const float ds = sqrtf(disc);
+        float q;
+        if (b < 0) q = (-b - ds) / 2.0f;
+        else q = (-b + ds) / 2.0f;
+        float t0 = q / a;
+        float t1 = c / q;
+        if (t0 > t1) { const float tmp = t0; t0 = t1; t1 = tmp; }
+        if (t0 >= R.MinT && t0 < R.MaxT) I.near_t = t0;
+        else {
+            if (t1 >= R.MinT && t1 < R.MaxT) I.near_t = t1;
+            else return;
+        }
+        if (I.near_t < R.MinT || I.near_t > R.MaxT) return;
+        I.valid = true;
+        I.P = ray_at(R, I.near_t);
+        I.N = vnorm(I.P);
+        const v3 Vn = vnorm(I.P);
+        I.UV.x = ER_INV_TWO_PI_F * spherical_phi(Vn);
+        I.UV.y = 1.0f - (ER_INV_PI_F * spherical_theta(Vn));
+        break;
+    }
+    default: break;
+    }
+}
+
+/* ---- sampling ---- */
+
+ER_D v2 concentric_sample_disk(v2 U)   /* Source/montecarlo.h:86-137 */
+{
+    float r, theta;
+    const float sx = 2 * U.x - 1;
+    const float sy = 2 * U.y - 1;
+    v2 out;
+    if (sx == 0.0f && sy == 0.0f) { out.x = 0.0f; out.y = 0.0f; return out; }
+    if (sx >= -sy) {
+        if (sx > sy) { r = sx; theta = (sy > 0.0f) ? sy / r : 8.0f + sy / r; }
+        else { r = sy; theta = 2.0f - sx / r; }
+    } else {
+        if (sx <= sy) { r = -sx; theta = 4.0f - sy / r; }
+        else { r = -sy; theta = 6.0f + sx / r; }
+    }
+    theta *= ER_PI_F / 4.f;
+    float sn, cs;
+    er_sincosf(theta, &sn, &cs);
+    out.x = r * cs;
+    out.y = r * sn;
+    return out;
+}
+
+struct Surf { v3 P, N; v2 UV; };
+
+/* SampleLightSurface - Source/lights.h:28-42 and the shape samplers */
+ER_D void sample_light_surface(const Light& L, v3 UVW, Surf& SS)
+{
+    SS.P = V3(0, 0, 0); SS.N = V3(0.0f, 0.0f, 1.0f); SS.UV.x = 0.0f; SS.UV.y = 0.0f;
+    switch (L.type) {
+    case 0:
+        SS.P = V3(-0.5f + UVW.x, -0.5f + UVW.y, 0.0f);
+        SS.UV.x = UVW.x; SS.UV.y = UVW.y;
+        SS.P = vmul(SS.P, V3(L.size[0], L.size[1], 0.0f));
+        break;
+    case 1: {
+        const float r = sqrtf(UVW.x);
+        const float theta = 2.0f * ER_PI_F * UVW.y;
+        float sn, cs; er_sincosf(theta, &sn, &cs);
+        SS.P = V3(r * cs, r * sn, 0.0f);
+        SS.UV.x = UVW.x; SS.UV.y = UVW.y;
+        SS.P = vscale(SS.P, L.outer_radius);
+        break;
+    }
+    case 2: {
+        const float inner = L.inner_radius / L.outer_radius;
+        const float r = inner + (1.0f - inner) * sqrtf(UVW.x);
+        const float theta = 2.0f * ER_PI_F * UVW.y;
+        float sn, cs; er_sincosf(theta, &sn, &cs);
+        SS.P = V3(r * cs, r * sn, 0.0f);
+        SS.P = vscale(SS.P, L.outer_radius);
+        SS.UV.x = SS.P.x; SS.UV.y = SS.P.y;
+        break;
+    }
+    case 3: {
+        const int side = (int)floorf(UVW.x * 6.0f);
+        v3 p = V3(0, 0, 0), n = SS.N;
+        switch (side) {
+        case 0: p = V3(0.5f, -0.5f + UVW.z, -0.5f + UVW.y); n = V3(1.0f, 0.0f, 0.0f); break;
+        case 1: p = V3(-0.5f, -0.5f + UVW.z, -0.5f + UVW.y); n = V3(-1.0f, 0.0f, 0.0f); break;
+        case 2: p = V3(-0.5f + UVW.y, 0.5f, -0.5f + UVW.z); n = V3(0.0f, 1.0f, 0.0f); break;
+        case 3: p = V3(-0.5f + UVW.y, -0.5f, -0.5f + UVW.z); n = V3(0.0f, -1.0f, 0.0f); break;
+        case 4: p = V3(-0.5f + UVW.y, -0.5f + UVW.z, 0.5f); n = V3(0.0f, 0.0f, 1.0f); break;
+        case 5: p = V3(-0.5f + UVW.y, -0.5f + UVW.z, -0.5f); n = V3(0.0f, 0.0f, -1.0f); break;
+        default: break;
+        }
+        SS.P = p; SS.N = n;
+        SS.UV.x = UVW.y; SS.UV.y = UVW.z;
+        SS.P = vmul(SS.P, V3(L.size[0], L.size[1], L.size[2]));
+        break;
+    }
+    case 4: {
+        const float z = 1.0f - 2.0f * UVW.x;
+        const float r = sqrtf(smax(0.0f, 1.0f - z * z));
+        const float phi = 2.0f * ER_PI_F * UVW.y;
+        float sn, cs; er_sincosf(phi, &sn, &cs);
+        SS.P = V3(r * cs, r * sn, z);
+        SS.N = SS.P;
+        SS.UV.x = spherical_theta(SS.P);
+        SS.UV.y = spherical_phi(SS.P);
+        SS.P = vscale(SS.P, L.outer_radius);
+        break;
+    }
+    default: break;
+    }
+    SS.P = xform_point(L.tm, SS.P);
+    SS.N = xform_vector(L.tm, SS.N);
+}
+
+/* EvaluateTexture - Source/textures.h:26-111 (procedural textures) */
+ER_D c3 evaluate_texture(const Params& P, int id, v2 UV)
+{
+    if (id < 0 || id >= P.n_textures) return C3(0, 0, 0);
+    const Texture& T = P.textures[id];
+    c3 L = C3(0, 0, 0);
+    v2 t = UV;
+    t.x *= T.repeat[0];
+    t.y *= T.repeat[1];
+    t.x += T.offset[0];
+    t.y += 1.0f - T.offset[1];
+    t.x = t.x - floorf(t.x);
+    t.y = t.y - floorf(t.y);
+    t.x = eclamp(t.x, 0.0f, 1.0f);
+    t.y = eclamp(t.y, 0.0f, 1.0f);
+    if (T.flip[0]) t.x = 1.0f - t.x;
+    if (T.flip[1]) t.y = 1.0f - t.y;
+    if (T.type == 0) {
+        switch (T.proc_type) {
+        case 0: L = C3(T.uniform[0], T.uniform[1], T.uniform[2]); break;
+        case 1: {
+            const int u = (int)(t.x * 2.0f), v = (int)(t.y * 2.0f);
+            const bool first = (u % 2 == 0) ? (v % 2 == 0) : (v % 2 != 0);
+            L = first ? C3(T.checker1[0], T.checker1[1], T.checker1[2]) : C3(T.checker2[0], T.checker2[1], T.checker2[2]);
+            break;
+        }
+        case 2: L = ctf_eval(T.gradient, t.y); break;
+        default: break;
+        }
+    }
+    return cscale(L, T.output_level);
+}
+
+/* ---- shading: Source/shader.h ---- */
+
+struct Shader {
+    int type;            /* 0 BRDF, 1 isotropic phase */
+    v3 Nn, Nu, Nv;
+    c3 Kd, Ks;
+    float ior, exponent;
+};
+
+ER_D void shader_init(Shader& sh, int type, v3 N, v3 Wo, c3 Kd, c3 Ks, float ior, float exponent)
+{
+    sh.type = type;
+    sh.Nn = vnorm(N);
+    sh.Nu = vnorm(vcross(N, Wo));
+    sh.Nv = vnorm(vcross(N, sh.Nu));
+    sh.Kd = Kd; sh.Ks = Ks; sh.ior = ior; sh.exponent = exponent;
+}
+
+ER_D v3 world_to_local(const Shader& sh, v3 W) { return V3(vdot(W, sh.Nu), vdot(W, sh.Nv), vdot(W, sh.Nn)); }
+ER_D v3 local_to_world(const Shader& sh, v3 W)
+{
+    return V3(sh.Nu.x * W.x + sh.Nv.x * W.y + sh.Nn.x * W.z,
+              sh.Nu.y * W.x + sh.Nv.y * W.y + sh.Nn.y * W.z,
+              sh.Nu.z * W.x + sh.Nv.z * W.y + sh.Nn.z * W.z);
+}
+
+ER_D float fresnel_eval(float ei_, float et_, float cosi)
+{
+    cosi = eclamp(cosi, -1.0f, 1.0f);
+    const bool entering = cosi > 0.0f;
+    float ei = ei_, et = et_;
+    if (!entering) { const float t = ei; ei = et; et = t; }
+    const float sint = ei / et * sqrtf(smax(0.f, 1.f - cosi * cosi));
+    if (sint >= 1.0f) return 1.0f;
+    const float cost = sqrtf(smax(0.f, 1.0f - sint * sint));
+    const float ci = fabsf(cosi);
+    const float Rparl = ((et * ci) - (ei * cost)) / ((et * ci) + (ei * cost));
+    const float Rperp = ((ei * ci) - (et * cost)) / ((ei * ci) + (et * cost));
+    return (Rparl * Rparl + Rperp * Rperp) / 2.f;
+}
+
+ER_D float blinn_d(float e, v3 Wh) { return (e + 2) * ER_INV_TWO_PI_F * er_powf(fabsf(Wh.z), e); }
+
+ER_D float blinn_pdf(float e, v3 Wo, v3 Wi)
+{
+    const v3 Wh = vnorm(vadd(Wo, Wi));
+    const float ct = fabsf(Wh.z);
+    float pdf = ((e + 1.0f) * er_powf(ct, e)) / (2.0f * ER_PI_F * 4.0f * vdot(Wo, Wh));
+    if (vdot(Wo, Wh) <= 0.0f) pdf = 0.0f;
+    return pdf;
+}
+
+ER_D c3 microfacet_f(const Shader& sh, v3 Wo, v3 Wi)
+{
+    const float co = fabsf(Wo.z), ci = fabsf(Wi.z);
+    if (ci == 0.f || co == 0.f) return C3(0, 0, 0);
+    v3 Wh = vadd(Wi, Wo);
+    if (Wh.x == 0.f && Wh.y == 0.f && Wh.z == 0.f) return C3(0, 0, 0);
+    Wh = vnorm(Wh);
+    const float F = fresnel_eval(1.0f, sh.ior, vdot(Wi, Wh));
+    const float NdotWh = fabsf(Wh.z), NdotWo = fabsf(Wo.z), NdotWi = fabsf(Wi.z);
+    const float WOdotWh = vabsdot(Wo, Wh);
+    const float G = smin(1.0f, smin((2.0f * NdotWh * NdotWo / WOdotWh), (2.0f * NdotWh * NdotWi / WOdotWh)));
+    const float D = blinn_d(sh.exponent, Wh);
+    const float den = 4.0f * ci * co;
+    c3 r = cscale(sh.Ks, D);
+    r = cscale(r, G);
+    r = cscale(r, F);
+    return cdivs(r, den);
+}
+
+ER_D bool same_hemisphere(v3 a, v3 b) { return (a.z * b.z) > 0.0f; }
+
+ER_D c3 shader_f(const Shader& sh, v3 Wo, v3 Wi)
+{
+    if (sh.type == 0) {
+        const v3 Wol = world_to_local(sh, Wo);
+        const v3 Wil = world_to_local(sh, Wi);
+        c3 R = C3(0, 0, 0);
+        R = cadd(R, cscale(sh.Kd, ER_INV_PI_F));
+        R = cadd(R, microfacet_f(sh, Wol, Wil));
+        return R;
+    }
+    return cscale(sh.Kd, ER_INV_PI_F);
+}
+
+ER_D float shader_pdf(const Shader& sh, v3 Wo, v3 Wi)
+{
+    if (sh.type == 0) {
+        const v3 Wol = world_to_local(sh, Wo);
+        const v3 Wil = world_to_local(sh, Wi);
+        float pdf = 0.0f;
+        pdf += same_hemisphere(Wol, Wil) ? fabsf(Wil.z) * ER_INV_PI_F : 0.0f;
+        pdf += same_hemisphere(Wol, Wil) ? blinn_pdf(sh.exponent, Wol, Wil) : 0.0f;
+        return pdf;
+    }
+    return ER_INV_FOUR_PI_EXPANDED;
+}
+
+ER_D float power_heuristic(float fPdf, float gPdf)
+{
+    const float f = 1 * fPdf, g = 1 * gPdf;
+    return (f * f) / (f * f + g * g);
+}
+
+/* ---- events ---- */
+
+struct Event {
+    int type;            /* 0 volume, 1 light */
+    bool valid;
+    float T;
+    v3 P, N, Wo;
+    c3 Le;
+};
+
+/* step budget of a fixed-step march: the loop ends after at most
+   (MaxT - MinT)/StepSize steps; a budget of twice that plus slack only trips
+   when float accumulation stalls (a step below the ulp of t) */
+ER_D long long march_budget(float t0, float t1, float step)
+{
+    const float n = (t1 - t0) / step;
+    if (!(n < 1.0e9f)) return 2000000000LL;
+    return (long long)(2.0f * n) + 64;
+}
+
+/* SampleVolume - Source/raymarching.h:30-71 */
+ER_D void sample_volume(const Params& P, const Ray& R, Rng& rng, Event& SE)
+{
+    Isect Int; Int.invalid();
+    intersect_box(R, vload(P.minp), vload(P.half_size), Int, false);
+    if (!Int.valid) return;
+    float MinT = smax(Int.near_t, R.MinT);
+    const float MaxT = smin(Int.far_t, R.MaxT);
+    const float S = -er_logf(rng.get1()) / P.density_scale;
+    float Sum = 0.0f;
+    v3 Ps = V3(0, 0, 0);
+    const float StepSize = P.step_primary * P.min_step;
+    MinT += rng.get1() * StepSize;
+    long long budget = march_budget(MinT, MaxT, StepSize);
+    while (Sum < S) {
+        Ps = vadd(R.O, vscale(R.D, MinT));
+        if (MinT >= MaxT) return;
+        if (--budget < 0) { atomicOr(P.err, 1); return; }
+        const float I = get_intensity(P, Ps);
+        const float SigmaT = sigma_at(P, I);
+        Sum += SigmaT * StepSize;
+        MinT += StepSize;
+    }
+    SE.valid = true;
+    SE.T = MinT;
+    SE.P = Ps;
+    SE.N = normalized_gradient(P, Ps);
+    SE.Wo = vneg(R.D);
+    SE.Le = C3(0, 0, 0);
+}
+
+/* ScatterEventInVolume - Source/raymarching.h:73-113 */
+ER_D bool scatter_event_in_volume(const Params& P, const Ray& R, Rng& rng)
+{
+    Isect Int; Int.invalid();
+    intersect_box(R, vload(P.minp), vload(P.half_size), Int, false);
+    if (!Int.valid) return false;
+    float MinT = smax(Int.near_t, R.MinT);
+    const float MaxT = smin(Int.far_t, R.MaxT);
+    const float S = -er_logf(rng.get1()) / P.density_scale;
+    float Sum = 0.0f;
+    const float StepSize = P.step_shadow * P.min_step;
+    MinT += rng.get1() * StepSize;
+    long long budget = march_budget(MinT, MaxT, StepSize);
+    while (Sum < S) {
+        const v3 Ps = vadd(R.O, vscale(R.D, MinT));
+        if (MinT > MaxT) return false;
+        if (--budget < 0) { atomicOr(P.err, 1); return false; }
+        const float I = get_intensity(P, Ps);
+        Sum += sigma_at(P, I) * StepSize;
+        MinT += StepSize;
+    }
+    return true;
+}
+
+/* IntersectLight - Source/lights.h:59-88 */
+ER_D void intersect_light(const Params& P, const Light& L, const Ray& R, Event& SE)
+{
+    const Ray Rt = xform_ray(L.inv_tm, R);
+    Isect Int; Int.invalid();
+    intersect_shape(L, Rt, Int);
+    if (Int.valid) {
+        SE.valid = true;
+        SE.P = xform_point(L.tm, Int.P);
+        SE.N = xform_vector(L.tm, Int.N);
+        SE.T = vlen(vsub(SE.P, R.O));
+        SE.Wo = vneg(R.D);
+        SE.Le = Int.front ? cscale(evaluate_texture(P, L.texture_id, Int.UV), L.multiplier) : C3(0, 0, 0);
+        if (L.unit == 1) SE.Le = cdivs(SE.Le, L.area);
+    }
+}
+
+/* IntersectLights - Source/lights.h:90-113 */
+ER_D void intersect_lights(const Params& P, const Ray& R, Event& RS, bool respect_visibility)
+{
+    float T = FLT_MAX;
+    for (int i = 0; i < P.light_count; i++) {
+        if (!P.light_valid[i]) continue;
+        const Light& L = P.lights[i];
+        if (respect_visibility && !L.visible) continue;
+        Event local;
+        local.type = 1; local.valid = false; local.T = 0.0f;
+        local.P = V3(0, 0, 0); local.N = V3(0, 0, 0); local.Wo = V3(0, 0, 0); local.Le = C3(0, 0, 0);
+        intersect_light(P, L, R, local);
+        if (local.valid && local.T < T) { RS = local; T = local.T; }
+    }
+}
+
+/* IntersectsLight - Source/lights.h:115-131 */
+ER_D bool intersects_light(const Params& P, const Ray& R)
+{
+    for (int i = 0; i < P.light_count; i++) {
+        if (!P.light_valid[i]) continue;
+        const Light& L = P.lights[i];
+        const Ray Rt = xform_ray(L.inv_tm, R);
+        Isect Int; Int.invalid();
+        intersect_shape(L, Rt, Int);
+        if (Int.valid) return true;
+    }
+    return false;
+}
+
+/* Visible / Intersect - Source/transport.h:30-56 */
+ER_D bool visible(const Params& P, v3 P1, v3 P2, Rng& rng)
+{
+    if (!P.shadows) return true;
+    const v3 W = vnorm(vsub(P2, P1));
+    Ray R;
+    R.O = vadd(P1, vscale(W, ER_RAY_EPS));
+    R.D = W;
+    R.MinT = 0.0f;
+    R.MaxT = smin(vlen(vsub(P2, P1)) - 2.0f * ER_RAY_EPS, P.max_shadow_distance);
+    if (intersects_light(P, R)) return false;
+    if (scatter_event_in_volume(P, R, rng)) return false;
+    return true;
+}
+
+/* SampleLight - Source/lights.h:44-57 */
+ER_D void sample_light(const Params& P, const Light& L, v3 uvw, Surf& SS, const Event& SE, v3& Wi, c3& Le)
+{
+    sample_light_surface(L, uvw, SS);
+    Wi = vnorm(vsub(SS.P, SE.P));
+    Le = cscale(evaluate_texture(P, L.texture_id, SS.UV), L.multiplier);
+    if (L.one_sided && vdot(vsub(SE.P, SS.P), SS.N) < 0.0f) Le = C3(0, 0, 0);
+    if (L.unit == 1) Le = cdivs(Le, L.area);
+}
+
+struct Metro {               /* MetroSample::LargeStep - Source/sample.h:258-262 */
+    float brdf_component;
+    v2 brdf_dir;
+    v3 light_uvw;
+    float light_num;
+    v2 film_uv;
+    v2 lens_uv;
+    ER_D void large_step(Rng& r)
+    {
+        brdf_component = r.get1();
+        brdf_dir = r.get2();
+        light_uvw = r.get3();
+        light_num = r.get1();
+        film_uv = r.get2();
+        lens_uv = r.get2();
+    }
+};
+
+/* EstimateDirectLight - Source/transport.h:58-84 */
+ER_D c3 estimate_direct_light(const Params& P, const Light& L, const Metro& ms, const Event& SE, Rng& rng, const Shader& sh)
+{
+    v3 Wi;
+    c3 Li, Ld = C3(0, 0, 0);
+    Surf SS;
+    sample_light(P, L, ms.light_uvw, SS, SE, Wi, Li);
+    const c3 F = shader_f(sh, SE.Wo, Wi);
+    const float BsdfPdf = shader_pdf(sh, SE.Wo, Wi);
+    if (!cblack(Li) && !cblack(F) && BsdfPdf > 0.0f && visible(P, SE.P, SS.P, rng)) {
+        const float LightPdf = vlen2(vsub(SE.P, SS.P)) / (vabsdot(SS.N, vneg(Wi)) * L.area);
+        const float Weight = power_heuristic(LightPdf, BsdfPdf);
+        if (sh.type == 0) Ld = cadd(Ld, cscale(cmul(F, Li), vabsdot(Wi, SE.N) * Weight / LightPdf));
+        else Ld = cadd(Ld, cdivs(cmul(F, Li), LightPdf));
+    }
+    return Ld;
+}
+
+/* UniformSampleOneLight - Source/transport.h:115-156 (volume events) */
+ER_D c3 uniform_sample_one_light(const Params& P, const Event& SE, Rng& rng, const Metro& ms)
+{
+    c3 Ld = C3(0, 0, 0);
+    const float I = get_intensity(P, SE.P);
+    Ld = cadd(Ld, ctf_eval(P.tfs->emission, I));
+    if (P.light_count <= 0) return Ld;
+    const int idx = (int)floorf(ms.light_num * (float)P.light_count);
+    if (idx < 0 || idx >= P.light_count || !P.light_valid[idx]) return Ld;
+    const Light& L = P.lights[idx];
+    Shader sh;
+    shader_init(sh, 0, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
+                1000000.0f * er_powf(plf_eval(P.tfs->glossiness, I), 7.0f));
+    Ld = cadd(Ld, estimate_direct_light(P, L, ms, SE, rng, sh));
+    return cscale(Ld, (float)P.light_count);
+}
+
+/* SampleCamera - Source/singlescattering.h:29-50 */
+ER_D Ray sample_camera(const Params& P, int u, int v, v2 film_uv, v2 lens_uv)
+{
+    Ray R;
+    const float sp0 = P.screen00 + (P.inv_screen0 * ((float)u + film_uv.x * 1.0f / (float)P.film[0]));
+    const float sp1 = P.screen10 + (P.inv_screen1 * ((float)v + film_uv.y * 1.0f / (float)P.film[1]));
+    R.O = vload(P.pos);
+    R.D = vnorm(vsub(vadd(vload(P.N), vscale(vload(P.U), sp0)), vscale(vload(P.V), sp1)));
+    R.MinT = P.clip_near;
+    R.MaxT = P.clip_far;
+    if (P.aperture != 0.0f) {
+        const v2 d = concentric_sample_disk(lens_uv);
+        const float lx = d.x * P.aperture, ly = d.y * P.aperture;
+        const v3 LI = vadd(vscale(vload(P.U), lx), vscale(vload(P.V), ly));
+        R.O = vadd(R.O, LI);
+        R.D = vnorm(vsub(vscale(R.D, P.focal_distance), LI));
+    }
+    return R;
+}
+
+/* SingleScattering - Source/singlescattering.h:76-102 */
+ER_D float4 single_scattering(const Params& P, int x, int y, Rng& rng)
+{
+    c3 Lv = C3(0, 0, 0);
+    Metro ms;
+    ms.large_step(rng);
+    const Ray R = sample_camera(P, x, y, ms.film_uv, ms.lens_uv);
+    Event se0, se1, SE;
+    se0.type = 0; se0.valid = false; se0.T = 0.0f; se0.Le = C3(0, 0, 0);
+    se0.P = V3(0, 0, 0); se0.N = V3(0, 0, 0); se0.Wo = V3(0, 0, 0);
+    se1 = se0; se1.type = 1;
+    sample_volume(P, R, rng, se0);
+    intersect_lights(P, R, se1, true);
+    SE = se0; SE.valid = false; SE.type = 0;
+    float T = FLT_MAX;
+    if (se0.valid && se0.T < T) { SE = se0; T = se0.T; }
+    if (se1.valid && se1.T < T) { SE = se1; T = se1.T; }
+    if (SE.valid && SE.type == 0) Lv = cadd(Lv, uniform_sample_one_light(P, SE, rng, ms));
+    if (SE.valid && SE.type == 1) Lv = cadd(Lv, SE.Le);
+    return make_float4(Lv.r, Lv.g, Lv.b, SE.valid ? 1.0f : 0.0f);
+}
+
+}  // namespace erd
+
+#endif

@@ -1,0 +1,85 @@
+/*
+ * er_render.cu - reference-order transport kernels (compiled with --fmad=false).
+ *
+ *   k_trace_frame : KrnlSingleScattering (Source/singlescattering.cuh:27-32):
+ *                   one sample per pixel with the RNG lanes read from and
+ *                   written back to per-pixel buffers.
+ *   k_trace_sum   : `spp` counter-seeded samples per pixel in one launch,
+ *                   summed in registers (one HBM write per pixel).
+ *   k_sigma_table : DensityScale * Opacity1D(I) for every integer I.
+ */
+#include "er_kernels.h"
+#include "er_path.cuh"
+
+using namespace erd;
+
+__global__ void __launch_bounds__(128) k_trace_frame(const Params P, uint32_t* __restrict__ lanes, float4* __restrict__ frame)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int W = P.film[0], H = P.film[1];
+    if (x >= W || y >= H) return;
+    const size_t p = (size_t)y * (size_t)W + (size_t)x;
+    const size_t n = (size_t)W * (size_t)H;
+    Rng rng;
+    rng.s0 = lanes[p];
+    rng.s1 = lanes[n + p];
+    frame[p] = single_scattering(P, x, y, rng);
+    lanes[p] = rng.s0;
+    lanes[n + p] = rng.s1;
+}
+
+__global__ void __launch_bounds__(128) k_trace_sum(const Params P, int spp, uint32_t view, uint32_t first, float4* __restrict__ sum,
+                                                   int accumulate)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int W = P.film[0], H = P.film[1];
+    if (x >= W || y >= H) return;
+    const uint32_t pix = (uint32_t)y * (uint32_t)W + (uint32_t)x;
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+    for (int k = 0; k < spp; k++) {
+        Rng rng;
+        er_seed_lanes(P.seed, view, pix, first + (uint32_t)k, &rng.s0, &rng.s1);
+        const float4 o = single_scattering(P, x, y, rng);
+        a0 += o.x; a1 += o.y; a2 += o.z; a3 += o.w;
+    }
+    float4 r = make_float4(a0, a1, a2, a3);
+    if (accumulate) {
+        const float4 q = sum[pix];
+        r = make_float4(q.x + a0, q.y + a1, q.z + a2, q.w + a3);
+    }
+    sum[pix] = r;
+}
+
+__global__ void k_sigma_table(const Plf* __restrict__ opacity, float density_scale, float* __restrict__ table, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    table[i] = density_scale * plf_eval(*opacity, (float)i);
+}
+
+/* ---- launchers ---- */
+
+cudaError_t er_launch_trace_frame(const Params& P, uint32_t* lanes, float4* frame, cudaStream_t s)
+{
+    const dim3 b(16, 8);
+    const dim3 g((P.film[0] + 15) / 16, (P.film[1] + 7) / 8);
+    k_trace_frame<<<g, b, 0, s>>>(P, lanes, frame);
+    return cudaGetLastError();
+}
+
+cudaError_t er_launch_trace_sum(const Params& P, int spp, uint32_t view, uint32_t first, float4* sum, int accumulate,
+                                cudaStream_t s)
+{
+    const dim3 b(16, 8);
+    const dim3 g((P.film[0] + 15) / 16, (P.film[1] + 7) / 8);
+    k_trace_sum<<<g, b, 0, s>>>(P, spp, view, first, sum, accumulate);
+    return cudaGetLastError();
+}
+
+cudaError_t er_launch_sigma_table(const Plf* opacity, float density_scale, float* table, int n, cudaStream_t s)
+{
+    k_sigma_table<<<(n + 255) / 256, 256, 0, s>>>(opacity, density_scale, table, n);
+    return cudaGetLastError();
+}

@@ -1,0 +1,948 @@
+/*
+ * er_runtime.cu - host runtime behind the C ABI of include/er_capi.h.
+ *
+ * Replaces the reference's List<D,H> bind lists and RenderEstimate pipeline
+ * (Source/list.cuh:27-173, Source/core.cu:50-155) with:
+ *   - std::map registries with the same ID semantics (ID = counter++, update
+ *     in place, no reuse, at most 31 items per list checked before the
+ *     update-or-insert decision as Source/list.cuh:63-83 does);
+ *   - per-tracer device blocks (transfer functions, resolved lights,
+ *     textures, sigma table, film buffers) rebuilt only when an item the
+ *     tracer depends on changed, instead of re-uploading every list every
+ *     frame (Source/core.cu:128, Source/list.cuh:108-148);
+ *   - asynchronous, stream-ordered launches (the reference synchronises
+ *     around every call, Source/wrapper.cuh:53-141).
+ *
+ * Host arithmetic that feeds the kernels (camera frame, volume geometry,
+ * light areas) follows Source/camera.h:61-96, Source/volume.h:100-129 and
+ * Source/shape.h:92-103 operation for operation; this file is compiled with
+ * -ffp-contract=off so the host never fuses those multiply-adds.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "er_capi.h"
+#include "er_kernels.h"
+#include "er_math.h"
+
+namespace {
+
+thread_local std::string g_last_error = "";
+
+er_status fail(er_status st, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return st;
+}
+
+#define ER_CUDA(call)                                                                                 \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) {                                                                      \
+            if (e_ == cudaErrorMemoryAllocation)                                                      \
+                return fail(ER_ERR_OUT_OF_MEMORY, "%s: %s", #call, cudaGetErrorString(e_));           \
+            return fail(ER_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));                        \
+        }                                                                                             \
+    } while (0)
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t ensure(size_t count)
+    {
+        if (count <= n && p) return cudaSuccess;
+        release();
+        if (count == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc((void**)&p, count * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        else p = nullptr;
+        return e;
+    }
+};
+
+float smin_h(float a, float b) { return (b < a) ? b : a; }
+float smax_h(float a, float b) { return (a < b) ? b : a; }
+
+struct V3h { float x, y, z; };
+V3h v3h(float x, float y, float z) { V3h r = {x, y, z}; return r; }
+V3h sub(V3h a, V3h b) { return v3h(a.x - b.x, a.y - b.y, a.z - b.z); }
+float len(V3h a) { return sqrtf(a.x * a.x + a.y * a.y + a.z * a.z); }
+V3h norm(V3h a) { const float L = len(a); return v3h(a.x / L, a.y / L, a.z / L); }
+V3h cross(V3h a, V3h b) { return v3h((a.y * b.z) - (a.z * b.y), (a.z * b.x) - (a.x * b.z), (a.x * b.y) - (a.y * b.x)); }
+
+/* Shape::Update (Source/shape.h:92-103) */
+float shape_area(const er_shape& s)
+{
+    const float PI = 3.141592654f;
+    switch (s.type) {
+    case ER_SHAPE_PLANE: return s.size[0] * s.size[1];
+    case ER_SHAPE_DISK: return PI * (s.outer_radius * s.outer_radius);
+    case ER_SHAPE_RING: return PI * (s.outer_radius * s.outer_radius) - PI * (s.inner_radius * s.inner_radius);
+    case ER_SHAPE_BOX: return (2.0f * s.size[0] * s.size[1]) + (2.0f * s.size[0] * s.size[2]) + (2.0f * s.size[1] * s.size[2]);
+    case ER_SHAPE_SPHERE: return 4.0f * PI * (s.outer_radius * s.outer_radius);
+    case ER_SHAPE_CYLINDER: return (2.0f * PI * (s.outer_radius * s.outer_radius)) + (2.0f * PI * s.outer_radius * s.size[2]);
+    default: return s.area;
+    }
+}
+
+struct VolumeItem {
+    int res[3];
+    float spacing[3];
+    int normalize;
+    uint16_t vmax = 0;
+    DevBuf<uint16_t> vox;
+    DevBuf<unsigned int> gm_max_bits;
+    float gm_max = -1.0f;          /* lazily computed maximum gradient magnitude */
+};
+
+struct BitmapItem {
+    int res[2];
+    DevBuf<uchar4> pixels;
+};
+
+struct TracerItem {
+    er_tracer_desc d;
+    int W = 0, H = 0;
+    int no_iterations = 0;
+    double n_samples = 0.0;        /* samples per pixel accumulated by er_render_spp */
+    DevBuf<float4> frame, running, sum;
+    DevBuf<uchar4> display, display_tmp, display_filtered;
+    DevBuf<uint32_t> lanes;
+    DevBuf<erd::Tfs> tfs;
+    DevBuf<erd::Plf> opacity;
+    DevBuf<erd::Light> lights;
+    DevBuf<int> light_valid;
+    DevBuf<erd::Texture> textures;
+    DevBuf<float> sigma;
+    DevBuf<int> err;
+    erd::Params P;
+    uint64_t built_version = 0;
+    bool built = false;
+};
+
+template <class T>
+struct Registry {
+    std::map<int, std::unique_ptr<T>> items;
+    int counter = 0;
+};
+
+struct Context {
+    std::recursive_mutex m;
+    cudaStream_t stream = 0;
+    int device = 0;
+    uint64_t version = 1;          /* bumped by every bind/unbind */
+    Registry<TracerItem> tracers;
+    Registry<VolumeItem> volumes;
+    Registry<er_light_desc> lights;
+    Registry<er_texture_desc> textures;
+    Registry<BitmapItem> bitmaps;
+    Registry<er_object_desc> objects;
+    Registry<er_clipping_object_desc> clipping;
+};
+
+Context& ctx()
+{
+    static Context* c = new Context();
+    return *c;
+}
+
+/* List::Bind capacity rule (Source/list.cuh:63-67): refused when
+   Map.size() + 1 >= 32, before the update-or-insert decision */
+template <class T>
+er_status reserve_id(Registry<T>& r, int32_t* id, bool* is_new)
+{
+    if (!id) return fail(ER_ERR_INVALID_ARGUMENT, "id pointer is NULL");
+    if (r.items.size() + 1 >= (size_t)(ER_MAX_ITEMS_PER_LIST + 1)) return fail(ER_ERR_LIST_FULL, "bind list is full (%d items)", ER_MAX_ITEMS_PER_LIST);
+    const bool exists = *id >= 0 && r.items.count(*id) != 0;
+    *is_new = !exists;
+    if (!exists) *id = r.counter++;
+    return ER_OK;
+}
+
+template <class T>
+er_status unbind(Registry<T>& r, int32_t id)
+{
+    auto it = r.items.find(id);
+    if (id < 0 || it == r.items.end()) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", id);
+    r.items.erase(it);
+    ctx().version++;
+    return ER_OK;
+}
+
+void to_plf(erd::Plf& o, const er_plf& s)
+{
+    o.count = s.count;
+    o.range0 = s.node_range[0];
+    o.range1 = s.node_range[1];
+    for (int i = 0; i < 128; i++) { o.pos[i] = s.position[i]; o.val[i] = s.value[i]; }
+}
+
+void to_light(erd::Light& o, const er_light_desc& s)
+{
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 4; j++) { o.tm[i][j] = s.shape.tm[i][j]; o.inv_tm[i][j] = s.shape.inv_tm[i][j]; }
+    o.one_sided = s.shape.one_sided;
+    o.type = s.shape.type;
+    for (int i = 0; i < 3; i++) o.size[i] = s.shape.size[i];
+    o.area = shape_area(s.shape);
+    o.inner_radius = s.shape.inner_radius;
+    o.outer_radius = s.shape.outer_radius;
+    o.visible = s.visible;
+    o.texture_id = s.texture_id;
+    o.multiplier = s.multiplier;
+    o.unit = s.unit;
+}
+
+void to_texture(erd::Texture& o, const er_texture_desc& s)
+{
+    o.type = s.type;
+    o.output_level = s.output_level;
+    o.bitmap_id = s.bitmap_id;
+    o.proc_type = s.procedural.type;
+    for (int i = 0; i < 3; i++) {
+        o.uniform[i] = s.procedural.uniform_color[i];
+        o.checker1[i] = s.procedural.checker_color1[i];
+        o.checker2[i] = s.procedural.checker_color2[i];
+        to_plf(o.gradient[i], s.procedural.gradient.plf[i]);
+    }
+    o.offset[0] = s.offset[0]; o.offset[1] = s.offset[1];
+    o.repeat[0] = s.repeat[0]; o.repeat[1] = s.repeat[1];
+    o.flip[0] = s.flip[0]; o.flip[1] = s.flip[1];
+}
+
+/* Volume::operator=(const ErVolume&) - Source/volume.h:100-129 */
+void volume_geometry(const VolumeItem& v, erd::Params& P)
+{
+    float scale = 0.0f;
+    if (v.normalize) {
+        const float p0 = (float)v.res[0] * v.spacing[0], p1 = (float)v.res[1] * v.spacing[1], p2 = (float)v.res[2] * v.spacing[2];
+        scale = 1.0f / smax_h(p0, smax_h(p1, p2));
+    }
+    float sp[3], size[3];
+    for (int i = 0; i < 3; i++) sp[i] = v.spacing[i] * scale;
+    for (int i = 0; i < 3; i++) size[i] = (float)v.res[i] * sp[i];
+    for (int i = 0; i < 3; i++) {
+        P.res[i] = v.res[i];
+        P.spacing[i] = sp[i];
+        P.inv_size[i] = 1.0f / size[i];
+        P.minp[i] = size[i] * -0.5f;
+        P.half_size[i] = size[i] * 0.5f;
+    }
+    P.min_step = smin_h(sp[0], smin_h(sp[1], sp[2]));
+    P.vox = v.vox.p;
+}
+
+/* Camera::Update - Source/camera.h:61-96 */
+void camera_frame(const er_camera_desc& c, erd::Params& P)
+{
+    const V3h pos = v3h(c.pos[0], c.pos[1], c.pos[2]);
+    const V3h target = v3h(c.target[0], c.target[1], c.target[2]);
+    const V3h up = v3h(c.up[0], c.up[1], c.up[2]);
+    const V3h N = norm(sub(target, pos));
+    const V3h U = norm(cross(N, up));
+    const V3h V = norm(cross(N, U));
+    float fd = c.focal_distance;
+    if (fd == -1.0f) fd = len(sub(target, pos));
+    const float sc = er_tanf((0.5f * c.fov / 57.29577951308232f));
+    const float aspect = (float)c.film_size[1] / (float)c.film_size[0];
+    float s00, s01, s10, s11;
+    if (aspect > 1.0f) { s00 = -sc; s01 = sc; s10 = -sc * aspect; s11 = sc * aspect; }
+    else { s00 = -sc / aspect; s01 = sc / aspect; s10 = -sc; s11 = sc; }
+    P.film[0] = c.film_size[0];
+    P.film[1] = c.film_size[1];
+    P.pos[0] = pos.x; P.pos[1] = pos.y; P.pos[2] = pos.z;
+    P.N[0] = N.x; P.N[1] = N.y; P.N[2] = N.z;
+    P.U[0] = U.x; P.U[1] = U.y; P.U[2] = U.z;
+    P.V[0] = V.x; P.V[1] = V.y; P.V[2] = V.z;
+    P.screen00 = s00;
+    P.screen10 = s10;
+    P.inv_screen0 = (s01 - s00) / (float)c.film_size[0];
+    P.inv_screen1 = (s11 - s10) / (float)c.film_size[1];
+    P.clip_near = c.clip_near;
+    P.clip_far = c.clip_far;
+    P.aperture = c.aperture_size;
+    P.focal_distance = fd;
+}
+
+er_status check_settings(const er_tracer_desc& d)
+{
+    const er_render_settings& s = d.settings;
+    if (!(s.step_factor_primary > 0.0f) || !(s.step_factor_shadow > 0.0f) || !std::isfinite(s.step_factor_primary) ||
+        !std::isfinite(s.step_factor_shadow))
+        return fail(ER_ERR_INVALID_ARGUMENT, "step factors must be finite and positive");
+    if (!(s.density_scale > 0.0f) || !std::isfinite(s.density_scale)) return fail(ER_ERR_INVALID_ARGUMENT, "density_scale must be finite and positive");
+    if (d.camera.film_size[0] <= 0 || d.camera.film_size[1] <= 0 || d.camera.film_size[0] > 32768 || d.camera.film_size[1] > 32768)
+        return fail(ER_ERR_INVALID_ARGUMENT, "film size %d x %d out of range", d.camera.film_size[0], d.camera.film_size[1]);
+    if (d.light_count < 0 || d.light_count > ER_MAX_INDICES) return fail(ER_ERR_INVALID_ARGUMENT, "light_count %d out of range", d.light_count);
+    return ER_OK;
+}
+
+er_status init_lanes(TracerItem& t)
+{
+    const size_t n = (size_t)t.W * t.H;
+    std::vector<uint32_t> h(2 * n);
+    for (size_t p = 0; p < n; p++) er_seed_lanes(t.d.settings.seed, 0u, (uint32_t)p, 0xffffffffu, &h[p], &h[n + p]);
+    ER_CUDA(cudaMemcpyAsync(t.lanes.p, h.data(), 2 * n * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx().stream));
+    ER_CUDA(cudaStreamSynchronize(ctx().stream));
+    return ER_OK;
+}
+
+er_status reset_tracer_buffers(TracerItem& t)
+{
+    const size_t n = (size_t)t.W * t.H;
+    cudaStream_t s = ctx().stream;
+    ER_CUDA(cudaMemsetAsync(t.running.p, 0, n * sizeof(float4), s));
+    ER_CUDA(cudaMemsetAsync(t.sum.p, 0, n * sizeof(float4), s));
+    ER_CUDA(cudaMemsetAsync(t.frame.p, 0, n * sizeof(float4), s));
+    ER_CUDA(cudaMemsetAsync(t.display.p, 0, n * sizeof(uchar4), s));
+    ER_CUDA(cudaMemsetAsync(t.display_filtered.p, 0, n * sizeof(uchar4), s));
+    t.no_iterations = 0;
+    t.n_samples = 0.0;
+    return init_lanes(t);
+}
+
+/* Assembles the kernel parameters of a tracer; uploads the dependent blocks
+   when any bound item changed since the last build. */
+er_status build(TracerItem& t)
+{
+    Context& C = ctx();
+    if (t.built && t.built_version == C.version) return ER_OK;
+    const er_tracer_desc& d = t.d;
+    auto vit = C.volumes.items.find(d.volume_id);
+    if (vit == C.volumes.items.end()) return fail(ER_ERR_INVALID_ID, "tracer references volume ID:%d which does not exist", d.volume_id);
+    VolumeItem& v = *vit->second;
+    if (d.object_count > 0) return fail(ER_ERR_UNSUPPORTED, "surface objects (ObjectIDs.Count = %d) are not implemented by the transport kernels", d.object_count);
+    if (d.settings.free_flight != ER_FREE_FLIGHT_MARCH) return fail(ER_ERR_UNSUPPORTED, "free_flight %d is not available in this build", d.settings.free_flight);
+    if (d.settings.mis != ER_MIS_LIGHT_ONLY) return fail(ER_ERR_UNSUPPORTED, "mis %d is not available in this build", d.settings.mis);
+    if (d.settings.apply_shading_type && d.settings.shading_type != ER_SHADING_BRDF_ONLY)
+        return fail(ER_ERR_UNSUPPORTED, "shading_type %d is not available in this build", d.settings.shading_type);
+    erd::Params P;
+    memset(&P, 0, sizeof(P));
+    volume_geometry(v, P);
+    camera_frame(d.camera, P);
+    const er_render_settings& s = d.settings;
+    P.step_primary = s.step_factor_primary;
+    P.step_shadow = s.step_factor_shadow;
+    P.density_scale = s.density_scale;
+    P.max_shadow_distance = s.max_shadow_distance;
+    P.shadows = s.shadows;
+    P.gradient_mode = s.gradient_computation;
+    P.shading_type = s.shading_type;
+    P.apply_shading_type = s.apply_shading_type;
+    P.opacity_modulated = s.opacity_modulated;
+    P.gradient_factor = s.gradient_factor;
+    P.gradient_threshold = s.gradient_threshold;
+    P.mis = s.mis;
+    P.volume_ior = s.volume_ior > 0.0f ? s.volume_ior : 15.0f;
+    P.seed = s.seed;
+    P.gm_inv_max = (v.gm_max > 0.0f) ? 1.0f / v.gm_max : 0.0f;
+
+    /* transfer functions */
+    erd::Tfs tf;
+    for (int c = 0; c < 3; c++) {
+        to_plf(tf.diffuse[c], d.diffuse.plf[c]);
+        to_plf(tf.specular[c], d.specular.plf[c]);
+        to_plf(tf.emission[c], d.emission.plf[c]);
+    }
+    to_plf(tf.glossiness, d.glossiness);
+    to_plf(tf.opacity, d.opacity);
+    cudaStream_t st = C.stream;
+    ER_CUDA(t.tfs.ensure(1));
+    ER_CUDA(cudaMemcpyAsync(t.tfs.p, &tf, sizeof(tf), cudaMemcpyHostToDevice, st));
+    /* sigma table over [0, max voxel] */
+    const int n = (int)v.vmax + 1;
+    ER_CUDA(t.sigma.ensure((size_t)n));
+    ER_CUDA(t.opacity.ensure(1));
+    ER_CUDA(cudaMemcpyAsync(t.opacity.p, &tf.opacity, sizeof(erd::Plf), cudaMemcpyHostToDevice, st));
+    ER_CUDA(er_launch_sigma_table(t.opacity.p, s.density_scale, t.sigma.p, n, st));
+    P.sigma = t.sigma.p;
+    P.sigma_n = n;
+    /* lights in LightIDs order */
+    const int lc = d.light_count;
+    std::vector<erd::Light> L((size_t)std::max(lc, 1));
+    std::vector<int> valid((size_t)std::max(lc, 1), 0);
+    int max_tex = -1;
+    for (auto& kv : C.textures.items) max_tex = std::max(max_tex, kv.first);
+    for (int i = 0; i < lc; i++) {
+        auto it = C.lights.items.find(d.light_ids[i]);
+        if (it == C.lights.items.end()) continue;
+        to_light(L[i], *it->second);
+        valid[i] = 1;
+        const int tid = it->second->texture_id;
+        auto tt = C.textures.items.find(tid);
+        if (tt != C.textures.items.end() && tt->second->type == ER_TEXTURE_BITMAP)
+            return fail(ER_ERR_UNSUPPORTED, "light %d uses bitmap texture %d; bitmap textures are not implemented by the transport kernels", d.light_ids[i], tid);
+    }
+    ER_CUDA(t.lights.ensure(L.size()));
+    ER_CUDA(t.light_valid.ensure(valid.size()));
+    ER_CUDA(cudaMemcpyAsync(t.lights.p, L.data(), L.size() * sizeof(erd::Light), cudaMemcpyHostToDevice, st));
+    ER_CUDA(cudaMemcpyAsync(t.light_valid.p, valid.data(), valid.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    P.light_count = lc;
+    P.lights = t.lights.p;
+    P.light_valid = t.light_valid.p;
+    /* textures indexed by texture ID; unbound IDs evaluate to black */
+    const int ntex = max_tex + 1;
+    std::vector<erd::Texture> T((size_t)std::max(ntex, 1));
+    for (auto& tx : T) { memset(&tx, 0, sizeof(tx)); tx.type = -1; tx.output_level = 0.0f; }
+    for (auto& kv : C.textures.items) to_texture(T[kv.first], *kv.second);
+    ER_CUDA(t.textures.ensure(T.size()));
+    ER_CUDA(cudaMemcpyAsync(t.textures.p, T.data(), T.size() * sizeof(erd::Texture), cudaMemcpyHostToDevice, st));
+    P.textures = t.textures.p;
+    P.n_textures = ntex;
+    P.tfs = t.tfs.p;
+    ER_CUDA(t.err.ensure(1));
+    P.err = t.err.p;
+    /* the host copies above read stack vectors: finish them before returning */
+    ER_CUDA(cudaStreamSynchronize(st));
+    t.P = P;
+    t.built = true;
+    t.built_version = C.version;
+    return ER_OK;
+}
+
+er_status check_device_error(TracerItem& t)
+{
+    if (!t.err.p) return ER_OK;
+    int e = 0;
+    ER_CUDA(cudaMemcpyAsync(&e, t.err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx().stream));
+    ER_CUDA(cudaStreamSynchronize(ctx().stream));
+    if (e) {
+        ER_CUDA(cudaMemsetAsync(t.err.p, 0, sizeof(int), ctx().stream));
+        return fail(ER_ERR_TIMEOUT, "a fixed-step march exceeded its step budget (step below the float resolution of the ray parameter)");
+    }
+    return ER_OK;
+}
+
+TracerItem* find_tracer(int id)
+{
+    auto it = ctx().tracers.items.find(id);
+    return (id < 0 || it == ctx().tracers.items.end()) ? nullptr : it->second.get();
+}
+
+BilateralTables bilateral_tables(const er_render_settings& s)
+{
+    BilateralTables T;
+    memset(&T, 0, sizeof(T));
+    int r = s.bilateral_radius;
+    r = r < 0 ? 0 : (r > 127 ? 127 : r);
+    T.radius = r;
+    const float sd = s.bilateral_sigma_d > 0.0f ? s.bilateral_sigma_d : 1.0f;
+    const float sr = s.bilateral_sigma_r > 0.0f ? s.bilateral_sigma_r : 1.0f;
+    for (int k = -r; k <= r; k++) T.spatial[r + k] = er_expf(-((float)(k * k)) / (2.0f * sd * sd));
+    for (int d = 0; d < 256; d++) T.range[d] = er_expf(-((float)(d * d)) / (2.0f * sr * sr));
+    return T;
+}
+
+er_status finish_display(TracerItem& t)
+{
+    if (t.d.settings.bilateral) {
+        const BilateralTables T = bilateral_tables(t.d.settings);
+        ER_CUDA(er_launch_bilateral(t.display.p, t.display_tmp.p, t.display_filtered.p, t.W, t.H, T, ctx().stream));
+    }
+    return ER_OK;
+}
+
+}  // namespace
+
+/* ====================================================================== */
+/* C ABI                                                                    */
+/* ====================================================================== */
+
+#define ER_LOCK std::lock_guard<std::recursive_mutex> lock_(ctx().m)
+
+extern "C" {
+
+ER_API int er_abi_version(void) { return ER_ABI_VERSION; }
+
+ER_API const char* er_last_error_message(void) { return g_last_error.c_str(); }
+
+ER_API er_status er_set_device(int device)
+{
+    ER_LOCK;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return fail(ER_ERR_NO_DEVICE, "no CUDA device");
+    if (device < 0 || device >= n) return fail(ER_ERR_INVALID_ARGUMENT, "device %d out of range (%d devices)", device, n);
+    ER_CUDA(cudaSetDevice(device));
+    ctx().device = device;
+    return ER_OK;
+}
+
+ER_API er_status er_set_stream(void* stream)
+{
+    ER_LOCK;
+    ctx().stream = (cudaStream_t)stream;
+    return ER_OK;
+}
+
+ER_API er_status er_synchronize(void)
+{
+    ER_LOCK;
+    ER_CUDA(cudaStreamSynchronize(ctx().stream));
+    for (auto& kv : ctx().tracers.items) {
+        er_status s = check_device_error(*kv.second);
+        if (s != ER_OK) return s;
+    }
+    return ER_OK;
+}
+
+ER_API er_status er_reset(void)
+{
+    ER_LOCK;
+    Context& C = ctx();
+    cudaStreamSynchronize(C.stream);
+    C.tracers.items.clear();
+    C.volumes.items.clear();
+    C.lights.items.clear();
+    C.textures.items.clear();
+    C.bitmaps.items.clear();
+    C.objects.items.clear();
+    C.clipping.items.clear();
+    C.version++;
+    return ER_OK;
+}
+
+ER_API void er_default_render_settings(er_render_settings* s)
+{
+    if (!s) return;
+    memset(s, 0, sizeof(*s));
+    s->step_factor_primary = 0.1f;
+    s->step_factor_shadow = 0.1f;
+    s->shadows = 1;
+    s->max_shadow_distance = 1.0f;
+    s->shading_type = 0;
+    s->density_scale = 100.0f;
+    s->opacity_modulated = 1;
+    s->gradient_computation = 1;
+    s->gradient_threshold = 0.5f;
+    s->gradient_factor = 0.5f;
+    s->volume_ior = 15.0f;
+    s->frame_filter = 1;
+    s->bilateral_radius = 2;
+    s->bilateral_sigma_d = 1.5f;
+    s->bilateral_sigma_r = 20.0f;
+    s->seed = 1u;
+}
+
+ER_API void er_plf_init(er_plf* p)
+{
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->node_range[0] = FLT_MAX;
+    p->node_range[1] = FLT_MIN;
+}
+
+ER_API void er_plf_add_node(er_plf* p, float position, float value)
+{
+    if (!p) return;
+    if (p->count + 1 >= ER_MAX_TF_NODES) return;
+    p->position[p->count] = position;
+    p->value[p->count] = value;
+    if (position < p->node_range[0]) p->node_range[0] = position;
+    if (position > p->node_range[1]) p->node_range[1] = position;
+    p->count++;
+}
+
+/* ---- bind lists ---- */
+
+ER_API er_status er_bind_volume(const er_volume_desc* d, int32_t* id)
+{
+    ER_LOCK;
+    if (!d || !d->voxels) return fail(ER_ERR_INVALID_ARGUMENT, "volume descriptor or voxel pointer is NULL");
+    for (int i = 0; i < 3; i++)
+        if (d->resolution[i] <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "volume resolution must be positive");
+    if (!d->normalize_size)
+        return fail(ER_ERR_INVALID_ARGUMENT, "normalize_size = 0 collapses the volume to zero size (Source/volume.h:106-117 leaves Scale = 0)");
+    Context& C = ctx();
+    bool is_new = false;
+    er_status st = reserve_id(C.volumes, id, &is_new);
+    if (st != ER_OK) return st;
+    std::unique_ptr<VolumeItem> v(new VolumeItem());
+    for (int i = 0; i < 3; i++) { v->res[i] = d->resolution[i]; v->spacing[i] = d->spacing[i]; }
+    v->normalize = d->normalize_size;
+    const size_t n = (size_t)d->resolution[0] * d->resolution[1] * d->resolution[2];
+    uint16_t vmax = 0;
+    for (size_t i = 0; i < n; i++) vmax = d->voxels[i] > vmax ? d->voxels[i] : vmax;
+    v->vmax = vmax;
+    ER_CUDA(v->vox.ensure(n));
+    ER_CUDA(cudaMemcpy(v->vox.p, d->voxels, n * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    C.volumes.items[*id] = std::move(v);
+    C.version++;
+    return ER_OK;
+}
+
+ER_API er_status er_unbind_volume(int32_t id) { ER_LOCK; return unbind(ctx().volumes, id); }
+
+ER_API er_status er_bind_light(const er_light_desc* d, int32_t* id)
+{
+    ER_LOCK;
+    if (!d) return fail(ER_ERR_INVALID_ARGUMENT, "light descriptor is NULL");
+    Context& C = ctx();
+    bool is_new = false;
+    er_status st = reserve_id(C.lights, id, &is_new);
+    if (st != ER_OK) return st;
+    C.lights.items[*id].reset(new er_light_desc(*d));
+    C.version++;
+    return ER_OK;
+}
+
+ER_API er_status er_unbind_light(int32_t id) { ER_LOCK; return unbind(ctx().lights, id); }
+
+ER_API er_status er_bind_texture(const er_texture_desc* d, int32_t* id)
+{
+    ER_LOCK;
+    if (!d) return fail(ER_ERR_INVALID_ARGUMENT, "texture descriptor is NULL");
+    Context& C = ctx();
+    bool is_new = false;
+    er_status st = reserve_id(C.textures, id, &is_new);
+    if (st != ER_OK) return st;
+    C.textures.items[*id].reset(new er_texture_desc(*d));
+    C.version++;
+    return ER_OK;
+}
+
+ER_API er_status er_unbind_texture(int32_t id) { ER_LOCK; return unbind(ctx().textures, id); }
+
+ER_API er_status er_bind_bitmap(const er_bitmap_desc* d, int32_t* id)
+{
+    ER_LOCK;
+    if (!d || !d->pixels || d->resolution[0] <= 0 || d->resolution[1] <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "invalid bitmap descriptor");
+    Context& C = ctx();
+    bool is_new = false;
+    er_status st = reserve_id(C.bitmaps, id, &is_new);
+    if (st != ER_OK) return st;
+    std::unique_ptr<BitmapItem> b(new BitmapItem());
+    b->res[0] = d->resolution[0];
+    b->res[1] = d->resolution[1];
+    const size_t n = (size_t)b->res[0] * b->res[1];
+    ER_CUDA(b->pixels.ensure(n));
+    ER_CUDA(cudaMemcpy(b->pixels.p, d->pixels, n * 4, cudaMemcpyHostToDevice));
+    C.bitmaps.items[*id] = std::move(b);
+    C.version++;
+    return ER_OK;
+}
+
+ER_API er_status er_unbind_bitmap(int32_t id) { ER_LOCK; return unbind(ctx().bitmaps, id); }
+
+ER_API er_status er_bind_object(const er_object_desc* d, int32_t* id)
+{
+    ER_LOCK;
+    if (!d) return fail(ER_ERR_INVALID_ARGUMENT, "object descriptor is NULL");
+    Context& C = ctx();
+    bool is_new = false;
+    er_status st = reserve_id(C.objects, id, &is_new);
+    if (st != ER_OK) return st;
+    C.objects.items[*id].reset(new er_object_desc(*d));
+    C.version++;
+    return ER_OK;
+}
+
+ER_API er_status er_unbind_object(int32_t id) { ER_LOCK; return unbind(ctx().objects, id); }
+
+ER_API er_status er_bind_clipping_object(const er_clipping_object_desc* d, int32_t* id)
+{
+    ER_LOCK;
+    if (!d) return fail(ER_ERR_INVALID_ARGUMENT, "clipping object descriptor is NULL");
+    Context& C = ctx();
+    bool is_new = false;
+    er_status st = reserve_id(C.clipping, id, &is_new);
+    if (st != ER_OK) return st;
+    C.clipping.items[*id].reset(new er_clipping_object_desc(*d));
+    C.version++;
+    return ER_OK;
+}
+
+ER_API er_status er_unbind_clipping_object(int32_t id) { ER_LOCK; return unbind(ctx().clipping, id); }
+
+ER_API er_status er_bind_tracer(const er_tracer_desc* d, int32_t* id)
+{
+    ER_LOCK;
+    if (!d) return fail(ER_ERR_INVALID_ARGUMENT, "tracer descriptor is NULL");
+    er_status st = check_settings(*d);
+    if (st != ER_OK) return st;
+    Context& C = ctx();
+    bool is_new = false;
+    st = reserve_id(C.tracers, id, &is_new);
+    if (st != ER_OK) return st;
+    if (is_new) C.tracers.items[*id].reset(new TracerItem());
+    TracerItem& t = *C.tracers.items[*id];
+    const bool resize = is_new || t.W != d->camera.film_size[0] || t.H != d->camera.film_size[1];
+    const bool reseed = is_new || t.d.settings.seed != d->settings.seed;
+    t.d = *d;
+    t.built = false;
+    C.version++;
+    if (resize) {
+        /* Tracer::operator= resizes the frame buffer (Source/tracer.h:45-52,
+           Source/framebuffer.h:45-68): every buffer is reallocated and cleared */
+        t.W = d->camera.film_size[0];
+        t.H = d->camera.film_size[1];
+        const size_t n = (size_t)t.W * t.H;
+        ER_CUDA(t.frame.ensure(n));
+        ER_CUDA(t.running.ensure(n));
+        ER_CUDA(t.sum.ensure(n));
+        ER_CUDA(t.display.ensure(n));
+        ER_CUDA(t.display_tmp.ensure(n));
+        ER_CUDA(t.display_filtered.ensure(n));
+        ER_CUDA(t.lanes.ensure(2 * n));
+        ER_CUDA(t.err.ensure(1));
+        ER_CUDA(cudaMemsetAsync(t.err.p, 0, sizeof(int), C.stream));
+        return reset_tracer_buffers(t);
+    }
+    if (reseed) return init_lanes(t);
+    return ER_OK;
+}
+
+ER_API er_status er_unbind_tracer(int32_t id) { ER_LOCK; return unbind(ctx().tracers, id); }
+
+/* ---- rendering ---- */
+
+ER_API er_status er_render_estimate(int32_t tracer_id)
+{
+    ER_LOCK;
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    er_status st = build(*t);
+    if (st != ER_OK) return st;
+    cudaStream_t s = ctx().stream;
+    ER_CUDA(er_launch_trace_frame(t->P, t->lanes.p, t->frame.p, s));
+    const int filt = t->d.settings.frame_filter >= 0 ? 1 : 0;
+    ER_CUDA(er_launch_post_frame(t->frame.p, t->running.p, t->display.p, t->W, t->H, t->no_iterations, t->d.camera.exposure, filt, s));
+    st = finish_display(*t);
+    if (st != ER_OK) return st;
+    t->no_iterations++;
+    return ER_OK;
+}
+
+ER_API er_status er_render_spp(int32_t tracer_id, int32_t spp)
+{
+    ER_LOCK;
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    if (spp <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "spp must be positive");
+    er_status st = build(*t);
+    if (st != ER_OK) return st;
+    cudaStream_t s = ctx().stream;
+    const uint32_t first = (uint32_t)t->n_samples;
+    ER_CUDA(er_launch_trace_sum(t->P, spp, 0u, first, t->sum.p, t->n_samples > 0.0 ? 1 : 0, s));
+    t->n_samples += spp;
+    const int filt = t->d.settings.frame_filter >= 0 ? 1 : 0;
+    ER_CUDA(er_launch_post_mean(t->sum.p, (float)t->n_samples, t->running.p, t->display.p, t->W, t->H, t->d.camera.exposure, filt, s));
+    st = finish_display(*t);
+    if (st != ER_OK) return st;
+    t->no_iterations += spp;
+    return ER_OK;
+}
+
+ER_API er_status er_reset_accumulation(int32_t tracer_id)
+{
+    ER_LOCK;
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    return reset_tracer_buffers(*t);
+}
+
+ER_API er_status er_get_estimate(int32_t tracer_id, uint8_t* rgba)
+{
+    ER_LOCK;
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    if (!rgba) return fail(ER_ERR_INVALID_ARGUMENT, "output pointer is NULL");
+    const uchar4* src = t->d.settings.bilateral ? t->display_filtered.p : t->display.p;
+    ER_CUDA(cudaMemcpyAsync(rgba, src, (size_t)t->W * t->H * 4, cudaMemcpyDeviceToHost, ctx().stream));
+    ER_CUDA(cudaStreamSynchronize(ctx().stream));
+    return check_device_error(*t);
+}
+
+ER_API er_status er_get_frame_estimate(int32_t tracer_id, float* xyza)
+{
+    ER_LOCK;
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    if (!xyza) return fail(ER_ERR_INVALID_ARGUMENT, "output pointer is NULL");
+    ER_CUDA(cudaMemcpyAsync(xyza, t->frame.p, (size_t)t->W * t->H * sizeof(float4), cudaMemcpyDeviceToHost, ctx().stream));
+    ER_CUDA(cudaStreamSynchronize(ctx().stream));
+    return check_device_error(*t);
+}
+
+ER_API er_status er_get_running_estimate(int32_t tracer_id, float* xyza)
+{
+    ER_LOCK;
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    if (!xyza) return fail(ER_ERR_INVALID_ARGUMENT, "output pointer is NULL");
+    ER_CUDA(cudaMemcpyAsync(xyza, t->running.p, (size_t)t->W * t->H * sizeof(float4), cudaMemcpyDeviceToHost, ctx().stream));
+    ER_CUDA(cudaStreamSynchronize(ctx().stream));
+    return check_device_error(*t);
+}
+
+ER_API er_status er_get_seeds(int32_t tracer_id, uint32_t* lanes)
+{
+    ER_LOCK;
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    if (!lanes) return fail(ER_ERR_INVALID_ARGUMENT, "output pointer is NULL");
+    ER_CUDA(cudaMemcpyAsync(lanes, t->lanes.p, (size_t)t->W * t->H * 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx().stream));
+    ER_CUDA(cudaStreamSynchronize(ctx().stream));
+    return ER_OK;
+}
+
+ER_API er_status er_set_seeds(int32_t tracer_id, const uint32_t* lanes)
+{
+    ER_LOCK;
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    if (!lanes) return fail(ER_ERR_INVALID_ARGUMENT, "input pointer is NULL");
+    ER_CUDA(cudaMemcpyAsync(t->lanes.p, lanes, (size_t)t->W * t->H * 2 * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx().stream));
+    ER_CUDA(cudaStreamSynchronize(ctx().stream));
+    return ER_OK;
+}
+
+ER_API er_status er_get_film_size(int32_t tracer_id, int32_t* w, int32_t* h)
+{
+    ER_LOCK;
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    if (w) *w = t->W;
+    if (h) *h = t->H;
+    return ER_OK;
+}
+
+ER_API er_status er_get_no_iterations(int32_t tracer_id, int32_t* no_iterations)
+{
+    ER_LOCK;
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    if (!no_iterations) return fail(ER_ERR_INVALID_ARGUMENT, "output pointer is NULL");
+    *no_iterations = t->no_iterations;
+    return ER_OK;
+}
+
+ER_API er_status er_get_auto_focus_distance(int32_t tracer_id, int32_t film_u, int32_t film_v, float* distance)
+{
+    ER_LOCK;
+    (void)film_u;
+    (void)film_v;
+    (void)distance;
+    if (!find_tracer(tracer_id)) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    return fail(ER_ERR_UNSUPPORTED, "auto focus is not available in this build");
+}
+
+/* ---- device-pointer entry points ---- */
+
+ER_API er_status er_trace_sum_device(int32_t tracer_id, int32_t spp, uint32_t view, uint32_t first_sample, float* d_sum,
+                                     int32_t accumulate, void* stream)
+{
+    ER_LOCK;
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    if (!d_sum || spp <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "invalid sum buffer or spp");
+    er_status st = build(*t);
+    if (st != ER_OK) return st;
+    ER_CUDA(er_launch_trace_sum(t->P, spp, view, first_sample, (float4*)d_sum, accumulate, (cudaStream_t)stream));
+    return ER_OK;
+}
+
+ER_API er_status er_trace_frame_device(int32_t tracer_id, uint32_t* d_lanes, float* d_frame, void* stream)
+{
+    ER_LOCK;
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    if (!d_lanes || !d_frame) return fail(ER_ERR_INVALID_ARGUMENT, "invalid device buffers");
+    er_status st = build(*t);
+    if (st != ER_OK) return st;
+    ER_CUDA(er_launch_trace_frame(t->P, d_lanes, (float4*)d_frame, (cudaStream_t)stream));
+    return ER_OK;
+}
+
+ER_API er_status er_post_frame_device(const float* d_frame, float* d_running, uint8_t* d_rgba, int32_t width, int32_t height,
+                                      int32_t no_iterations, float exposure, int32_t frame_filter, void* stream)
+{
+    if (!d_frame || !d_running || !d_rgba || width <= 0 || height <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "invalid post-process arguments");
+    ER_CUDA(er_launch_post_frame((const float4*)d_frame, (float4*)d_running, (uchar4*)d_rgba, width, height, no_iterations, exposure,
+                                 frame_filter >= 0 ? 1 : 0, (cudaStream_t)stream));
+    return ER_OK;
+}
+
+ER_API er_status er_tonemap_device(const float* d_xyza, float scale, uint8_t* d_rgba, int32_t width, int32_t height, float exposure,
+                                   void* stream)
+{
+    if (!d_xyza || !d_rgba || width <= 0 || height <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "invalid tone-map arguments");
+    ER_CUDA(er_launch_tonemap((const float4*)d_xyza, scale, (uchar4*)d_rgba, width * height, exposure, (cudaStream_t)stream));
+    return ER_OK;
+}
+
+ER_API er_status er_bilateral_device(const uint8_t* d_in, uint8_t* d_tmp, uint8_t* d_out, int32_t width, int32_t height, int32_t radius,
+                                     float sigma_d, float sigma_r, void* stream)
+{
+    if (!d_in || !d_tmp || !d_out || width <= 0 || height <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "invalid bilateral arguments");
+    if (radius < 0 || radius > 127) return fail(ER_ERR_INVALID_ARGUMENT, "bilateral radius %d out of range [0, 127]", radius);
+    er_render_settings s;
+    er_default_render_settings(&s);
+    s.bilateral_radius = radius;
+    s.bilateral_sigma_d = sigma_d;
+    s.bilateral_sigma_r = sigma_r;
+    const BilateralTables T = bilateral_tables(s);
+    ER_CUDA(er_launch_bilateral((const uchar4*)d_in, (uchar4*)d_tmp, (uchar4*)d_out, width, height, T, (cudaStream_t)stream));
+    return ER_OK;
+}
+
+ER_API er_status er_gradient_magnitude(int32_t volume_id, uint16_t* d_gm, float* max_gm)
+{
+    ER_LOCK;
+    auto it = ctx().volumes.items.find(volume_id);
+    if (volume_id < 0 || it == ctx().volumes.items.end()) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", volume_id);
+    VolumeItem& v = *it->second;
+    erd::Params P;
+    memset(&P, 0, sizeof(P));
+    volume_geometry(v, P);
+    ER_CUDA(v.gm_max_bits.ensure(1));
+    cudaStream_t s = ctx().stream;
+    ER_CUDA(cudaMemsetAsync(v.gm_max_bits.p, 0, sizeof(unsigned int), s));
+    ER_CUDA(er_launch_gradient_magnitude(P, d_gm, v.gm_max_bits.p, s));
+    unsigned int bits = 0;
+    ER_CUDA(cudaMemcpyAsync(&bits, v.gm_max_bits.p, sizeof(bits), cudaMemcpyDeviceToHost, s));
+    ER_CUDA(cudaStreamSynchronize(s));
+    float m;
+    memcpy(&m, &bits, sizeof(m));
+    v.gm_max = m;
+    if (max_gm) *max_gm = m;
+    ctx().version++;
+    return ER_OK;
+}
+
+ER_API er_status er_math_eval_device(int32_t fn, int32_t n, const float* d_x, const float* d_y, float* d_out, void* stream)
+{
+    if (fn < 0 || fn > 7 || n < 0 || !d_x || !d_out || ((fn == 5 || fn == 7) && !d_y))
+        return fail(ER_ERR_INVALID_ARGUMENT, "invalid math evaluation arguments");
+    if (n == 0) return ER_OK;
+    ER_CUDA(er_launch_math_eval(fn, n, d_x, d_y, d_out, (cudaStream_t)stream));
+    return ER_OK;
+}
+
+}  // extern "C"

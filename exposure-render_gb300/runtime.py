@@ -1,0 +1,114 @@
+"""Python host side over the C ABI: binds a scenes.Scene the way a reference
+application binds its Er* objects (BindTexture, BindLight, BindVolume,
+BindTracer - Source/exposurerender.h:32-38) and exposes the render calls.
+
+Every call goes through libexposurerender.so; a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_float, c_int32
+
+import numpy as np
+
+from . import capi as C
+
+
+class Renderer:
+    """One bound scene (texture/light/volume/tracer IDs) in the library context."""
+
+    def __init__(self, scene, lib=None):
+        self.lib = lib or C.load_library()
+        self.scene = scene
+        self.texture_ids = []
+        self.light_ids = []
+        for t in scene.textures:
+            i = c_int32(-1)
+            C.check(self.lib.er_bind_texture(byref(t), byref(i)))
+            self.texture_ids.append(i.value)
+        for L in scene.lights:
+            Lc = C.er_light_desc()
+            ctypes.memmove(byref(Lc), byref(L), ctypes.sizeof(L))
+            if Lc.texture_id >= 0:
+                Lc.texture_id = self.texture_ids[Lc.texture_id]
+            i = c_int32(-1)
+            C.check(self.lib.er_bind_light(byref(Lc), byref(i)))
+            self.light_ids.append(i.value)
+        vd = scene.volume_desc()
+        vid = c_int32(-1)
+        C.check(self.lib.er_bind_volume(byref(vd), byref(vid)))
+        self.volume_id = vid.value
+        t = C.er_tracer_desc()
+        ctypes.memmove(byref(t), byref(scene.tracer), ctypes.sizeof(t))
+        t.volume_id = self.volume_id
+        for k in range(t.light_count):
+            src = scene.tracer.light_ids[k]
+            t.light_ids[k] = self.light_ids[src] if 0 <= src < len(self.light_ids) else -1
+        self.tracer_desc = t
+        tid = c_int32(-1)
+        C.check(self.lib.er_bind_tracer(byref(t), byref(tid)))
+        self.tracer_id = tid.value
+
+    @property
+    def width(self) -> int:
+        return self.scene.width
+
+    @property
+    def height(self) -> int:
+        return self.scene.height
+
+    def rebind_tracer(self) -> None:
+        tid = c_int32(self.tracer_id)
+        C.check(self.lib.er_bind_tracer(byref(self.tracer_desc), byref(tid)))
+
+    def render_estimate(self) -> None:
+        C.check(self.lib.er_render_estimate(self.tracer_id))
+
+    def render_spp(self, spp: int) -> None:
+        C.check(self.lib.er_render_spp(self.tracer_id, spp))
+
+    def get_estimate(self) -> np.ndarray:
+        out = np.empty((self.height, self.width, 4), dtype=np.uint8)
+        C.check(self.lib.er_get_estimate(self.tracer_id, out.ctypes.data))
+        return out
+
+    def get_running_estimate(self) -> np.ndarray:
+        out = np.empty((self.height, self.width, 4), dtype=np.float32)
+        C.check(self.lib.er_get_running_estimate(self.tracer_id, out.ctypes.data))
+        return out
+
+    def get_frame_estimate(self) -> np.ndarray:
+        out = np.empty((self.height, self.width, 4), dtype=np.float32)
+        C.check(self.lib.er_get_frame_estimate(self.tracer_id, out.ctypes.data))
+        return out
+
+    def get_seeds(self) -> np.ndarray:
+        out = np.empty(2 * self.width * self.height, dtype=np.uint32)
+        C.check(self.lib.er_get_seeds(self.tracer_id, out.ctypes.data))
+        return out
+
+    def no_iterations(self) -> int:
+        n = c_int32(0)
+        C.check(self.lib.er_get_no_iterations(self.tracer_id, byref(n)))
+        return n.value
+
+    def trace_sum_device(self, d_sum_ptr: int, spp: int, view: int = 0, first: int = 0, accumulate: int = 0, stream=None) -> None:
+        C.check(self.lib.er_trace_sum_device(self.tracer_id, spp, view, first, d_sum_ptr, accumulate, stream))
+
+    def trace_frame_device(self, d_lanes_ptr: int, d_frame_ptr: int, stream=None) -> None:
+        C.check(self.lib.er_trace_frame_device(self.tracer_id, d_lanes_ptr, d_frame_ptr, stream))
+
+    def gradient_magnitude(self, d_gm_ptr=None) -> float:
+        m = c_float(0.0)
+        C.check(self.lib.er_gradient_magnitude(self.volume_id, d_gm_ptr, byref(m)))
+        return m.value
+
+    def close(self) -> None:
+        lib = self.lib
+        lib.er_unbind_tracer(self.tracer_id)
+        lib.er_unbind_volume(self.volume_id)
+        for i in self.light_ids:
+            lib.er_unbind_light(i)
+        for i in self.texture_ids:
+            lib.er_unbind_texture(i)
+        self.light_ids, self.texture_ids = [], []

@@ -1,0 +1,310 @@
+"""Seeded synthetic scenes with the shapes, sizes and value ranges of the
+workloads the renderer is measured on.
+
+The reference ships no datasets (its GUI example used a CT scan that is not
+distributed with it); every volume here is generated from a fixed seed, so a
+scene is fully described by its name and parameters.
+
+    c1  128^3 uint16 sum of 12 anisotropic Gaussian blobs (amplitude U[500,4000])
+        plus uniform noise U[0,50]; 4-node opacity/albedo transfer function;
+        one square area light; pinhole camera; 256^2; 64 spp.
+    c2  512^3 uint16 nested spherical shells (~1000/1400/2500 with Gaussian
+        noise sigma 30) in a soft-tissue ellipsoid; 16-node transfer function,
+        hybrid phase/BRDF (roughness 0.3); two area lights plus an environment
+        sphere light; 1024^2; 256 spp; bilateral filter and tone map.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi as C
+
+
+@dataclass
+class Scene:
+    name: str
+    volume: np.ndarray                      # uint16, shape (Z, Y, X), x fastest
+    spacing: tuple = (1.0, 1.0, 1.0)
+    normalize_size: int = 1
+    tracer: C.er_tracer_desc = None
+    lights: list = field(default_factory=list)      # er_light_desc, light i has ID i
+    textures: list = field(default_factory=list)    # er_texture_desc, texture i has ID i
+    spp: int = 1
+
+    @property
+    def width(self) -> int:
+        return int(self.tracer.camera.film_size[0])
+
+    @property
+    def height(self) -> int:
+        return int(self.tracer.camera.film_size[1])
+
+    def volume_desc(self) -> C.er_volume_desc:
+        v = np.ascontiguousarray(self.volume, dtype=np.uint16)
+        self.volume = v
+        d = C.er_volume_desc()
+        d.resolution[0] = v.shape[2]
+        d.resolution[1] = v.shape[1]
+        d.resolution[2] = v.shape[0]
+        for i in range(3):
+            d.spacing[i] = self.spacing[i]
+        d.normalize_size = self.normalize_size
+        d.voxels = v.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16))
+        return d
+
+    def light_array(self):
+        arr = (C.er_light_desc * max(1, len(self.lights)))()
+        for i, l in enumerate(self.lights):
+            arr[i] = l
+        return arr
+
+    def texture_array(self):
+        arr = (C.er_texture_desc * max(1, len(self.textures)))()
+        for i, t in enumerate(self.textures):
+            arr[i] = t
+        return arr
+
+
+# ---------------------------------------------------------------------------
+# geometry helpers
+# ---------------------------------------------------------------------------
+
+def look_at_tm(pos, target, up):
+    """Shape transform whose local +z axis points from pos towards target.
+
+    Returns (TM, InvTM) as float32-rounded 4x4 lists (rows), the layout of
+    Matrix44::NN (Source/matrix.h:55) used by TransformPoint
+    (Source/geometry.h:43-52)."""
+    p = np.asarray(pos, dtype=np.float64)
+    n = np.asarray(target, dtype=np.float64) - p
+    n /= np.linalg.norm(n)
+    u = np.cross(np.asarray(up, dtype=np.float64), n)
+    if np.linalg.norm(u) < 1e-9:
+        u = np.cross(np.array([1.0, 0.0, 0.0]), n)
+    u /= np.linalg.norm(u)
+    v = np.cross(n, u)
+    tm = np.eye(4)
+    tm[:3, 0], tm[:3, 1], tm[:3, 2], tm[:3, 3] = u, v, n, p
+    inv = np.linalg.inv(tm)
+    return tm.astype(np.float32).tolist(), inv.astype(np.float32).tolist()
+
+
+def make_shape(shape_type, tm_inv, size=(1.0, 1.0, 1.0), inner=0.0, outer=1.0, one_sided=0) -> C.er_shape:
+    s = C.er_shape()
+    tm, inv = tm_inv
+    C.set_matrix(s.tm, tm)
+    C.set_matrix(s.inv_tm, inv)
+    s.one_sided = one_sided
+    s.type = shape_type
+    for i in range(3):
+        s.size[i] = size[i]
+    s.inner_radius = inner
+    s.outer_radius = outer
+    s.area = 0.0
+    return s
+
+
+def uniform_texture(color=(1.0, 1.0, 1.0), level=1.0) -> C.er_texture_desc:
+    t = C.new_texture_desc()
+    t.procedural.type = C.PROCEDURAL_UNIFORM
+    for i in range(3):
+        t.procedural.uniform_color[i] = color[i]
+    t.output_level = level
+    return t
+
+
+def gradient_texture(nodes_rgb, level=1.0, repeat=(1.0, 1.0)) -> C.er_texture_desc:
+    t = C.new_texture_desc()
+    t.procedural.type = C.PROCEDURAL_GRADIENT
+    t.procedural.gradient = C.make_color_tf(nodes_rgb)
+    t.output_level = level
+    t.repeat[0], t.repeat[1] = repeat
+    return t
+
+
+def make_camera(film, pos, target, up=(0.0, 0.0, 1.0), fov=35.0, exposure=1.0) -> C.er_camera_desc:
+    c = C.er_camera_desc()
+    c.film_size[0], c.film_size[1] = film
+    for i in range(3):
+        c.pos[i] = pos[i]
+        c.target[i] = target[i]
+        c.up[i] = up[i]
+    c.focal_distance = -1.0
+    c.aperture_size = 0.0
+    c.clip_near = 0.0
+    c.clip_far = 1000.0
+    c.exposure = exposure
+    c.gamma = 2.2
+    c.fov = fov
+    return c
+
+
+def orbit_camera(rng, film, radius=2.0, fov=35.0, exposure=1.0) -> C.er_camera_desc:
+    """Random orbit camera looking at the volume centre."""
+    theta = rng.uniform(0.0, 2.0 * np.pi)
+    z = rng.uniform(-0.5, 0.5)
+    r = np.sqrt(1.0 - z * z)
+    pos = (radius * r * np.cos(theta), radius * r * np.sin(theta), radius * z)
+    return make_camera(film, pos, (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), fov, exposure)
+
+
+# ---------------------------------------------------------------------------
+# volumes
+# ---------------------------------------------------------------------------
+
+def blob_volume(shape_zyx, n_blobs=12, seed=1, amp=(500.0, 4000.0), sigma=(0.04, 0.14), noise=50.0) -> np.ndarray:
+    """Sum of `n_blobs` axis-aligned anisotropic Gaussians plus uniform noise,
+    truncated to uint16 (x fastest)."""
+    Z, Y, X = shape_zyx
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0.2, 0.8, size=(n_blobs, 3)) * np.array([X, Y, Z])
+    sig = rng.uniform(sigma[0], sigma[1], size=(n_blobs, 3)) * np.array([X, Y, Z])
+    amps = rng.uniform(amp[0], amp[1], size=n_blobs)
+    xs = np.arange(X, dtype=np.float32)
+    ys = np.arange(Y, dtype=np.float32)
+    vol = np.zeros((Z, Y, X), dtype=np.float32)
+    for k in range(n_blobs):
+        gx = np.exp(-0.5 * ((xs - centres[k, 0]) / sig[k, 0]) ** 2).astype(np.float32)
+        gy = np.exp(-0.5 * ((ys - centres[k, 1]) / sig[k, 1]) ** 2).astype(np.float32)
+        gxy = (gy[:, None] * gx[None, :]) * np.float32(amps[k])
+        for z in range(Z):
+            gz = np.float32(np.exp(-0.5 * ((z - centres[k, 2]) / sig[k, 2]) ** 2))
+            if gz > 1e-7:
+                vol[z] += gxy * gz
+    for z in range(Z):
+        vol[z] += rng.uniform(0.0, noise, size=(Y, X)).astype(np.float32)
+    return np.clip(np.floor(vol), 0, 65535).astype(np.uint16)
+
+
+def shell_volume(n=512, seed=2, noise_sigma=30.0) -> np.ndarray:
+    """Nested spherical shells in a soft-tissue ellipsoid (CT-like), uint16."""
+    rng = np.random.default_rng(seed)
+    out = np.empty((n, n, n), dtype=np.uint16)
+    c = (n - 1) / 2.0
+    xs = (np.arange(n, dtype=np.float32) - c) / n
+    X, Y = np.meshgrid(xs, xs, indexing="xy")
+    for zi in range(n):
+        z = np.float32((zi - c) / n)
+        ell = (X / 0.46) ** 2 + (Y / 0.40) ** 2 + (z / 0.36) ** 2 <= 1.0
+        r = np.sqrt(X * X + Y * Y + z * z)
+        v = np.where(ell, 1000.0, 0.0).astype(np.float32)
+        v = np.where((r >= 0.26) & (r < 0.30), 1400.0, v)
+        v = np.where((r >= 0.15) & (r < 0.19), 2500.0, v)
+        v = np.where(r < 0.07, 1400.0, v)
+        v = v + np.where(ell, rng.normal(0.0, noise_sigma, size=v.shape), 0.0).astype(np.float32)
+        out[zi] = np.clip(np.floor(v), 0, 65535).astype(np.uint16)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# configurations
+# ---------------------------------------------------------------------------
+
+def c1_tracer(film=(256, 256), phase=False) -> C.er_tracer_desc:
+    t = C.new_tracer_desc()
+    # 4-node opacity; the last node sits between integers so no reachable
+    # intensity equals it (PLF::Evaluate returns 0 exactly at the last node,
+    # Source/plf.h:79-90)
+    t.opacity = C.make_plf([(0.0, 0.0), (400.0, 0.0), (1500.0, 0.6), (4000.5, 1.0)])
+    t.diffuse = C.make_color_tf([(0.0, (0.8, 0.8, 0.8)), (400.0, (0.8, 0.75, 0.7)),
+                                 (1500.0, (0.85, 0.7, 0.6)), (4000.5, (0.9, 0.85, 0.8))])
+    t.specular = C.make_color_tf([(0.0, (0.2, 0.2, 0.2)), (4000.5, (0.2, 0.2, 0.2))])
+    t.glossiness = C.make_plf([(0.0, 0.6), (4000.5, 0.6)])
+    t.emission = C.make_color_tf([(0.0, (0.0, 0.0, 0.0)), (4000.5, (0.0, 0.0, 0.0))])
+    t.camera = make_camera(film, (0.0, -2.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 35.0, 1.0)
+    t.settings.seed = 1
+    if phase:
+        t.settings.apply_shading_type = 1
+        t.settings.shading_type = C.SHADING_PHASE_ONLY
+    t.volume_id = 0
+    t.light_count = 1
+    t.light_ids[0] = 0
+    return t
+
+
+def c1_lights():
+    # 0.5 x 0.5 plane light at z = +1 facing down, multiplier 20, uniform texture 0
+    L = C.er_light_desc()
+    L.visible = 1
+    L.shape = make_shape(C.SHAPE_PLANE, look_at_tm((0.0, 0.0, 1.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0)),
+                         size=(0.5, 0.5, 0.0))
+    L.texture_id = 0
+    L.multiplier = 20.0
+    L.unit = C.UNIT_POWER
+    return [L], [uniform_texture()]
+
+
+def scene_c1(res=128, film=(256, 256), spp=64, phase=False) -> Scene:
+    vol = blob_volume((res, res, res), seed=1)
+    lights, textures = c1_lights()
+    return Scene("c1", vol, tracer=c1_tracer(film, phase), lights=lights, textures=textures, spp=spp)
+
+
+def scene_tiny(res=32, film=(48, 40), spp=4, seed=3) -> Scene:
+    """Small C1-shaped scene for fast CPU/GPU parity tests."""
+    vol = blob_volume((res, res, res), n_blobs=6, seed=seed)
+    lights, textures = c1_lights()
+    t = c1_tracer(film)
+    return Scene("tiny", vol, tracer=t, lights=lights, textures=textures, spp=spp)
+
+
+def c2_tracer(film=(1024, 1024)) -> C.er_tracer_desc:
+    t = C.new_tracer_desc()
+    t.opacity = C.make_plf([
+        (0.0, 0.0), (600.0, 0.0), (850.0, 0.0), (950.0, 0.02), (1050.0, 0.04), (1150.0, 0.02),
+        (1250.0, 0.05), (1350.0, 0.2), (1450.0, 0.35), (1600.0, 0.3), (1900.0, 0.3), (2200.0, 0.6),
+        (2400.0, 0.9), (2600.0, 1.0), (3000.0, 1.0), (65535.5, 1.0)])
+    t.diffuse = C.make_color_tf([
+        (0.0, (0.6, 0.4, 0.3)), (1000.0, (0.75, 0.45, 0.35)), (1400.0, (0.8, 0.6, 0.45)),
+        (2500.0, (0.92, 0.9, 0.85)), (65535.5, (0.92, 0.9, 0.85))])
+    t.specular = C.make_color_tf([(0.0, (0.1, 0.1, 0.1)), (2500.0, (0.4, 0.4, 0.4)), (65535.5, (0.4, 0.4, 0.4))])
+    t.glossiness = C.make_plf([(0.0, 0.7), (65535.5, 0.7)])          # roughness 0.3
+    t.emission = C.make_color_tf([(0.0, (0.0, 0.0, 0.0)), (65535.5, (0.0, 0.0, 0.0))])
+    t.camera = make_camera(film, (0.3, -1.9, 0.5), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 35.0, 1.0)
+    t.settings.seed = 2
+    t.settings.apply_shading_type = 1
+    t.settings.shading_type = C.SHADING_HYBRID
+    t.settings.mis = C.MIS_FULL
+    t.settings.bilateral = 1
+    t.volume_id = 0
+    t.light_count = 3
+    for i in range(3):
+        t.light_ids[i] = i
+    return t
+
+
+def c2_lights():
+    key = C.er_light_desc()
+    key.visible = 1
+    key.shape = make_shape(C.SHAPE_PLANE, look_at_tm((0.8, -0.8, 1.0), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0)), size=(0.6, 0.6, 0.0))
+    key.texture_id = 0
+    key.multiplier = 25.0
+    key.unit = C.UNIT_POWER
+    fill = C.er_light_desc()
+    fill.visible = 1
+    fill.shape = make_shape(C.SHAPE_PLANE, look_at_tm((-1.0, -0.6, -0.2), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0)), size=(0.8, 0.8, 0.0))
+    fill.texture_id = 1
+    fill.multiplier = 8.0
+    fill.unit = C.UNIT_POWER
+    env = C.er_light_desc()
+    env.visible = 1
+    tm = np.eye(4).tolist()
+    env.shape = make_shape(C.SHAPE_SPHERE, (tm, tm), outer=5.0)
+    env.texture_id = 2
+    env.multiplier = 0.6
+    env.unit = C.UNIT_POWER
+    textures = [
+        uniform_texture((1.0, 0.97, 0.9)),
+        uniform_texture((0.7, 0.8, 1.0)),
+        gradient_texture([(0.0, (0.25, 0.22, 0.2)), (0.5, (0.5, 0.55, 0.6)), (1.0, (0.9, 0.95, 1.0))]),
+    ]
+    return [key, fill, env], textures
+
+
+def scene_c2(res=512, film=(1024, 1024), spp=256) -> Scene:
+    vol = shell_volume(res, seed=2)
+    lights, textures = c2_lights()
+    return Scene("c2", vol, tracer=c2_tracer(film), lights=lights, textures=textures, spp=spp)

@@ -1,0 +1,372 @@
+/*
+ * er_capi.h - C ABI of the GB300 Exposure Render transport library
+ * (libexposurerender.so).
+ *
+ * Plain C: POD descriptors, integer status codes, no C++ types and no
+ * exceptions across the boundary.  Every entry point names the reference
+ * interface it replaces (paths are relative to the reference project).
+ *
+ * Semantics follow the reference's global-singleton API
+ * (Source/exposurerender.h:32-42, Source/core.cu:50-155):
+ *   - one library-wide context per process (per CUDA device 0 .. n-1 chosen by
+ *     er_set_device); bind lists hold at most ER_MAX_ITEMS_PER_LIST items each,
+ *     like List<D,H,32> (Source/list.cuh:27,63);
+ *   - Bind assigns ID = counter++ on first bind and writes it back through the
+ *     `id` pointer (the reference writes the caller's `mutable int ID`,
+ *     Source/erbindable.h:65, Source/list.cuh:69-76); binding an existing ID
+ *     updates the item in place; IDs are never reused;
+ *   - lights referenced by a tracer are addressed by light ID (the reference's
+ *     packed-array index equals the ID while nothing is unbound,
+ *     Source/list.cuh:115-126, Source/lights.h:96);
+ *   - errors: the reference throws ExposureRender::Exception
+ *     (Source/exception.h:27-55) or refuses silently (Source/list.cuh:63-67);
+ *     here every call returns an er_status and er_last_error_message() holds
+ *     the text of the last failure on the calling thread.
+ */
+#ifndef ER_CAPI_H
+#define ER_CAPI_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define ER_API __declspec(dllexport)
+#else
+#define ER_API __attribute__((visibility("default")))
+#endif
+
+#define ER_ABI_VERSION 1
+
+/* Source/defines.h:76 (MAX_NO_TF_NODES); AddNode keeps Count < 128 (Source/plf.h:53) */
+#define ER_MAX_TF_NODES 128
+/* Source/list.cuh:27,63: List<D,H,MaxSize=32> accepts Map.size()+1 < 32 */
+#define ER_MAX_ITEMS_PER_LIST 31
+/* Source/vector.h:554-579: Indices holds 256 ints */
+#define ER_MAX_INDICES 256
+
+typedef enum er_status {
+    ER_OK = 0,
+    ER_ERR_INVALID_ID = 1,        /* Source/list.cuh:154-161 throws Warning */
+    ER_ERR_INVALID_ARGUMENT = 2,
+    ER_ERR_LIST_FULL = 3,         /* Source/list.cuh:63-67 refuses silently */
+    ER_ERR_CUDA = 4,              /* Source/wrapper.cuh:38-46 throws Error */
+    ER_ERR_OUT_OF_MEMORY = 5,
+    ER_ERR_UNSUPPORTED = 6,       /* a scene feature the selected kernel does not implement */
+    ER_ERR_NO_DEVICE = 7,
+    ER_ERR_TIMEOUT = 8            /* a device-side bounded wait gave up */
+} er_status;
+
+/* Source/enums.h:52-61 */
+enum { ER_SHAPE_PLANE = 0, ER_SHAPE_DISK = 1, ER_SHAPE_RING = 2, ER_SHAPE_BOX = 3, ER_SHAPE_SPHERE = 4,
+       ER_SHAPE_CYLINDER = 5, ER_SHAPE_CONE = 6 };
+/* Source/enums.h:39-50 */
+enum { ER_PROCEDURAL_UNIFORM = 0, ER_PROCEDURAL_CHECKER = 1, ER_PROCEDURAL_GRADIENT = 2 };
+enum { ER_TEXTURE_PROCEDURAL = 0, ER_TEXTURE_BITMAP = 1 };
+/* Source/enums.h:63-71 */
+enum { ER_SHADING_BRDF_ONLY = 0, ER_SHADING_PHASE_ONLY = 1, ER_SHADING_HYBRID = 2,
+       ER_SHADING_MODULATION = 3, ER_SHADING_THRESHOLD = 4, ER_SHADING_GRADIENT_MAGNITUDE = 5 };
+/* Source/enums.h:73-78 */
+enum { ER_GRADIENT_FORWARD = 0, ER_GRADIENT_CENTRAL = 1, ER_GRADIENT_FILTERED = 2 };
+/* Source/enums.h:88-93 */
+enum { ER_UNIT_POWER = 0, ER_UNIT_LUX = 1, ER_UNIT_INTENSITY = 2 };
+
+/* Free-flight estimator (extension; 0 keeps the reference's fixed-step
+   marcher of Source/raymarching.h:30-113). */
+enum { ER_FREE_FLIGHT_MARCH = 0, ER_FREE_FLIGHT_DELTA = 1 };
+/* Direct-light estimator (extension; 0 keeps the live light-sampling half of
+   Source/transport.h:58-84, 1 adds the BSDF-sampling half :86-112). */
+enum { ER_MIS_LIGHT_ONLY = 0, ER_MIS_FULL = 1 };
+
+/* PiecewiseLinearFunction<128> (Source/plf.h:26-92, Source/pf.h:35-71).
+   node_range starts at {FLT_MAX, FLT_MIN} and is widened by every AddNode. */
+typedef struct er_plf {
+    int32_t count;
+    float node_range[2];
+    float position[ER_MAX_TF_NODES];
+    float value[ER_MAX_TF_NODES];
+} er_plf;
+
+/* ColorTransferFunction1D (Source/transferfunction.h:118-154) */
+typedef struct er_color_tf {
+    er_plf plf[3];
+} er_color_tf;
+
+/* Shape (Source/shape.h:57-113); area is recomputed by the library the way
+   Shape::Update does (Source/shape.h:92-103), the field is ignored on input. */
+typedef struct er_shape {
+    float tm[4][4];
+    float inv_tm[4][4];
+    int32_t one_sided;
+    int32_t type;
+    float size[3];
+    float area;
+    float inner_radius;
+    float outer_radius;
+} er_shape;
+
+/* ErLight (Source/erlight.h:27-66) */
+typedef struct er_light_desc {
+    int32_t visible;
+    er_shape shape;
+    int32_t texture_id;
+    float multiplier;
+    int32_t unit;
+} er_light_desc;
+
+/* Procedural (Source/procedural.h:27-60) */
+typedef struct er_procedural {
+    int32_t type;
+    float uniform_color[3];
+    float checker_color1[3];
+    float checker_color2[3];
+    er_color_tf gradient;
+} er_procedural;
+
+/* ErTexture (Source/ertexture.h:27-82) */
+typedef struct er_texture_desc {
+    int32_t type;
+    float output_level;
+    int32_t bitmap_id;
+    er_procedural procedural;
+    float offset[2];
+    float repeat[2];
+    int32_t flip[2];
+} er_texture_desc;
+
+/* ErVolume (Source/ervolume.h:28-74): voxels are x-fastest
+   (z*Rx*Ry + y*Rx + x, Source/buffer3d.h:212-213) and are deep-copied at bind
+   time like BindVoxels does (Source/buffer3d.h:166-198). */
+typedef struct er_volume_desc {
+    int32_t resolution[3];
+    float spacing[3];
+    int32_t normalize_size;
+    const uint16_t* voxels;       /* host pointer, resolution[0]*[1]*[2] values */
+} er_volume_desc;
+
+/* ErBitmap (Source/erbitmap.h:28-61): RGBA8, row-major */
+typedef struct er_bitmap_desc {
+    int32_t resolution[2];
+    const uint8_t* pixels;        /* host pointer, 4*resolution[0]*resolution[1] bytes */
+} er_bitmap_desc;
+
+/* ErObject (Source/erobject.h:27-67) */
+typedef struct er_object_desc {
+    er_shape shape;
+    int32_t diffuse_texture_id;
+    int32_t specular_texture_id;
+    int32_t glossiness_texture_id;
+    float ior;
+} er_object_desc;
+
+/* ErClippingObject (Source/erclippingobject.h:27-58) */
+typedef struct er_clipping_object_desc {
+    er_shape shape;
+    int32_t invert;
+} er_clipping_object_desc;
+
+/* Camera inputs (Source/camera.h:98-108); the derived frame (N, U, V,
+   screen window) is computed by the library as Camera::Update does
+   (Source/camera.h:61-96). */
+typedef struct er_camera_desc {
+    int32_t film_size[2];
+    float pos[3];
+    float target[3];
+    float up[3];
+    float focal_distance;
+    float aperture_size;
+    float clip_near;
+    float clip_far;
+    float exposure;
+    float gamma;
+    float fov;
+} er_camera_desc;
+
+/* RenderSettings (Source/rendersettings.h:27-131) plus extension fields.
+   er_default_render_settings() fills the reference defaults. */
+typedef struct er_render_settings {
+    /* TraversalSettings (Source/rendersettings.h:30-64) */
+    float step_factor_primary;
+    float step_factor_shadow;
+    int32_t shadows;
+    float max_shadow_distance;
+    /* ShadingSettings (Source/rendersettings.h:66-106) */
+    int32_t shading_type;
+    float density_scale;
+    int32_t opacity_modulated;
+    int32_t gradient_computation;
+    float gradient_threshold;
+    float gradient_factor;
+    /* extensions: zero-initialised values keep the reference's behaviour */
+    int32_t apply_shading_type;   /* 0: every volume event uses the BRDF, as the live reference does
+                                     (Source/transport.h:138 ignores Shading.Type); 1: shading_type
+                                     selects BRDF / phase / hybrid per Source/scatterevent.h:155-212 */
+    int32_t free_flight;          /* ER_FREE_FLIGHT_* */
+    int32_t mis;                  /* ER_MIS_* */
+    float volume_ior;             /* 15 in the reference (Source/transport.h:138); 0 means 15 */
+    int32_t frame_filter;         /* 1: 3x3 Gaussian on each frame (Source/filterframeestimate.cuh:66-74); -1: off */
+    int32_t bilateral;            /* 1: separable bilateral on the display image (Source/filterrunningestimate.cuh) */
+    int32_t bilateral_radius;     /* KernelRadius of BilateralFilter (Source/filter.h:34-40) */
+    float bilateral_sigma_d;      /* spatial sigma in pixels for KernelD[] */
+    float bilateral_sigma_r;      /* range sigma in 0..255 luminance units for GaussSimilarity[] */
+    uint32_t seed;                /* counter-based seed of the per-pixel RNG lanes */
+    int32_t reserved[6];
+} er_render_settings;
+
+/* ErTracer (Source/ertracer.h:33-117).  light_ids/object_ids/clipping_ids are
+   item IDs returned by the bind calls. */
+typedef struct er_tracer_desc {
+    er_plf opacity;
+    er_color_tf diffuse;
+    er_color_tf specular;
+    er_plf glossiness;
+    er_color_tf emission;
+    er_camera_desc camera;
+    er_render_settings settings;
+    int32_t volume_id;
+    int32_t light_count;
+    int32_t light_ids[ER_MAX_INDICES];
+    int32_t object_count;
+    int32_t object_ids[ER_MAX_INDICES];
+    int32_t clipping_object_count;
+    int32_t clipping_object_ids[ER_MAX_INDICES];
+} er_tracer_desc;
+
+/* ---------------------------------------------------------------------- */
+/* library                                                                 */
+/* ---------------------------------------------------------------------- */
+
+ER_API int er_abi_version(void);
+/* Text of the last error on this thread (never NULL). */
+ER_API const char* er_last_error_message(void);
+/* Selects the CUDA device used by subsequent calls of this thread's context
+   (the reference always used the current device). */
+ER_API er_status er_set_device(int device);
+/* Stream for all asynchronous work (cudaStream_t passed as void*; NULL is the
+   legacy default stream used by the reference, Source/macros.cuh:41-65). */
+ER_API er_status er_set_stream(void* stream);
+ER_API er_status er_synchronize(void);
+/* Releases every bound item and device buffer. */
+ER_API er_status er_reset(void);
+ER_API void er_default_render_settings(er_render_settings* settings);
+/* Appends a node the way PiecewiseLinearFunction::AddNode does
+   (Source/plf.h:51-66), including the silent cap at 127 nodes. */
+ER_API void er_plf_init(er_plf* plf);
+ER_API void er_plf_add_node(er_plf* plf, float position, float value);
+
+/* ---------------------------------------------------------------------- */
+/* bind lists: Source/exposurerender.h:32-38, Source/core.cu:50-124        */
+/* ---------------------------------------------------------------------- */
+
+/* BindTracer(const ErTracer&, true) - Source/exposurerender.h:32 */
+ER_API er_status er_bind_tracer(const er_tracer_desc* desc, int32_t* id);
+/* BindTracer(const ErTracer&, false) */
+ER_API er_status er_unbind_tracer(int32_t id);
+/* BindVolume - Source/exposurerender.h:33 */
+ER_API er_status er_bind_volume(const er_volume_desc* desc, int32_t* id);
+ER_API er_status er_unbind_volume(int32_t id);
+/* BindLight - Source/exposurerender.h:34 */
+ER_API er_status er_bind_light(const er_light_desc* desc, int32_t* id);
+ER_API er_status er_unbind_light(int32_t id);
+/* BindObject - Source/exposurerender.h:35 */
+ER_API er_status er_bind_object(const er_object_desc* desc, int32_t* id);
+ER_API er_status er_unbind_object(int32_t id);
+/* BindClippingObject - Source/exposurerender.h:36 */
+ER_API er_status er_bind_clipping_object(const er_clipping_object_desc* desc, int32_t* id);
+ER_API er_status er_unbind_clipping_object(int32_t id);
+/* BindTexture - Source/exposurerender.h:37 */
+ER_API er_status er_bind_texture(const er_texture_desc* desc, int32_t* id);
+ER_API er_status er_unbind_texture(int32_t id);
+/* BindBitmap - Source/exposurerender.h:38 */
+ER_API er_status er_bind_bitmap(const er_bitmap_desc* desc, int32_t* id);
+ER_API er_status er_unbind_bitmap(int32_t id);
+
+/* ---------------------------------------------------------------------- */
+/* rendering                                                               */
+/* ---------------------------------------------------------------------- */
+
+/* RenderEstimate(int TracerID) - Source/exposurerender.h:39, Source/core.cu:126-136.
+   One frame: one sample per pixel, 3x3 Gaussian frame filter, running
+   cumulative moving average with divisor max(NoIterations,1), tone map,
+   NoIterations++.  Asynchronous on the library stream. */
+ER_API er_status er_render_estimate(int32_t tracer_id);
+/* GetEstimate(int TracerID, unsigned char*) - Source/exposurerender.h:40,
+   Source/core.cu:138-143.  Blocking copy of W*H RGBA8 into a host buffer of
+   at least 4*W*H bytes (the bilateral-filtered image when the tracer's
+   settings enable the bilateral filter). */
+ER_API er_status er_get_estimate(int32_t tracer_id, uint8_t* rgba);
+/* GetAutoFocusDistance - Source/exposurerender.h:41 (a stub at
+   Source/core.cu:145-148; the kernel design is Source/autofocus.cuh:26-63). */
+ER_API er_status er_get_auto_focus_distance(int32_t tracer_id, int32_t film_u, int32_t film_v, float* distance);
+/* GetNoIterations - Source/exposurerender.h:42 (a stub at Source/core.cu:150-153) */
+ER_API er_status er_get_no_iterations(int32_t tracer_id, int32_t* no_iterations);
+
+/* Extension: `spp` samples per pixel in one launch, accumulated as a plain
+   sample mean into the running estimate (no per-frame filter), followed by
+   the frame filter on the mean, the tone map and the optional bilateral
+   filter.  NoIterations grows by spp.  Asynchronous. */
+ER_API er_status er_render_spp(int32_t tracer_id, int32_t spp);
+/* Restarts progressive accumulation: running estimate, NoIterations and the
+   per-pixel RNG lanes (FrameBuffer::Reset, Source/framebuffer.h:70-74). */
+ER_API er_status er_reset_accumulation(int32_t tracer_id);
+/* Blocking copies of the float XYZA buffers (W*H*4 floats each). */
+ER_API er_status er_get_frame_estimate(int32_t tracer_id, float* xyza);
+ER_API er_status er_get_running_estimate(int32_t tracer_id, float* xyza);
+/* Per-pixel RNG lanes (2*W*H uint32: all lane-0 values then all lane-1 values). */
+ER_API er_status er_get_seeds(int32_t tracer_id, uint32_t* lanes);
+ER_API er_status er_set_seeds(int32_t tracer_id, const uint32_t* lanes);
+/* Film size of a bound tracer. */
+ER_API er_status er_get_film_size(int32_t tracer_id, int32_t* width, int32_t* height);
+
+/* ---------------------------------------------------------------------- */
+/* device-pointer entry points (caller owns all buffers; cudaStream_t as   */
+/* void*; no allocation, no synchronisation)                               */
+/* ---------------------------------------------------------------------- */
+
+/* Renders `spp` counter-seeded samples per pixel of a bound tracer into a
+   caller-owned float4 sum buffer (XYZ sum, alpha sum) of W*H*4 floats.
+   Sample s of pixel p uses lanes er_seed_lanes(seed, view, p, first_sample+s)
+   (include/er_math.h).  `accumulate` = 0 overwrites, 1 adds. */
+ER_API er_status er_trace_sum_device(int32_t tracer_id, int32_t spp, uint32_t view, uint32_t first_sample,
+                                     float* d_sum_xyza, int32_t accumulate, void* stream);
+
+/* One reference frame with explicit per-pixel lanes: d_lanes holds 2*W*H
+   uint32 (lane 0 block then lane 1 block) and is advanced in place exactly as
+   KrnlSingleScattering advances RandomSeeds1/2 (Source/singlescattering.cuh:27-32);
+   d_frame_xyza receives W*H float4. */
+ER_API er_status er_trace_frame_device(int32_t tracer_id, uint32_t* d_lanes, float* d_frame_xyza, void* stream);
+
+/* Post-process stages on caller buffers (W*H pixels):
+   3x3 Gaussian of a float4 image (Source/filterframeestimate.cuh:33-64) fused
+   with the running average R += (F-R)/max(n,1) (Source/estimate.cuh:27-38)
+   and the tone map (Source/tonemap.cuh:30-59). */
+ER_API er_status er_post_frame_device(const float* d_frame_xyza, float* d_running_xyza, uint8_t* d_rgba,
+                                      int32_t width, int32_t height, int32_t no_iterations, float exposure,
+                                      int32_t frame_filter, void* stream);
+/* Tone map only (Source/tonemap.cuh:30-59): float4 XYZA scaled by `scale` -> RGBA8. */
+ER_API er_status er_tonemap_device(const float* d_xyza, float scale, uint8_t* d_rgba, int32_t width, int32_t height,
+                                   float exposure, void* stream);
+/* Separable bilateral filter on RGBA8 (design of Source/filterrunningestimate.cuh:35-200):
+   horizontal pass into d_tmp, vertical pass into d_out. */
+ER_API er_status er_bilateral_device(const uint8_t* d_in, uint8_t* d_tmp, uint8_t* d_out, int32_t width, int32_t height,
+                                     int32_t radius, float sigma_d, float sigma_r, void* stream);
+
+/* Gradient-magnitude pre-pass of a bound volume (Source/gradientmagnitude.cuh:28-71
+   with the per-voxel magnitude of Source/volumes.h:93-114 at voxel centres):
+   optional u16 magnitude volume (saturating) and the maximum magnitude. */
+ER_API er_status er_gradient_magnitude(int32_t volume_id, uint16_t* d_gm_or_null, float* max_gradient_magnitude);
+
+/* Diagnostics: evaluates one include/er_math.h function on the GPU for n
+   arguments (fn 0 log, 1 exp, 2 sin, 3 cos, 4 tan, 5 pow(x,y), 6 acos,
+   7 atan2(x,y)); used to check that device and host produce the same bits.
+   No reference counterpart. */
+ER_API er_status er_math_eval_device(int32_t fn, int32_t n, const float* d_x, const float* d_y, float* d_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ER_CAPI_H */

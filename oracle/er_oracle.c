@@ -1,0 +1,1477 @@
+/*
+ * er_oracle.c - CPU oracle: a plain-C restatement of Exposure Render's
+ * single-scattering transport path and post-processing.
+ *
+ * TEST INFRASTRUCTURE ONLY (see er_oracle.h).  The product never calls this.
+ *
+ * Every function cites the reference file:line it restates (paths relative
+ * to the reference project).  Floating-point expressions keep the
+ * reference's evaluation order (C++ operators are left-associative and the
+ * Vec/Color operators of Source/vector.h and Source/color.h work
+ * component-wise), and the file must be compiled with -ffp-contract=off so
+ * that no multiply-add is fused.  Elementary functions come from
+ * include/er_math.h; the reference build in oracle/_ref routes its
+ * logf/expf/powf/sinf/cosf/tanf/acosf/atan2f calls to the same functions.
+ *
+ * std::min/std::max (the reference's `using namespace std`) are
+ * (b < a) ? b : a and (a < b) ? b : a; ExposureRender::Min/Max/Clamp
+ * (Source/vector.h:27-43) are A < B ? A : B, A > B ? A : B and
+ * Max(lo, Min(v, hi)); fminf/fmaxf are the IEEE functions.
+ */
+#include "er_oracle.h"
+#include "er_math.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ */
+/* small vector algebra (Source/vector.h:397-552)                       */
+/* ------------------------------------------------------------------ */
+
+typedef struct { float x, y, z; } v3;
+typedef struct { float x, y; } v2;
+typedef struct { float c[3]; } col3;   /* ColorXYZf */
+
+static inline v3 V3(float x, float y, float z) { v3 r; r.x = x; r.y = y; r.z = z; return r; }
+static inline v3 vadd(v3 a, v3 b) { return V3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 vsub(v3 a, v3 b) { return V3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline v3 vmul(v3 a, v3 b) { return V3(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline v3 vdivv(v3 a, v3 b) { return V3(a.x / b.x, a.y / b.y, a.z / b.z); }
+static inline v3 vscale(v3 a, float s) { return V3(a.x * s, a.y * s, a.z * s); }
+static inline v3 vneg(v3 a) { return V3(-a.x, -a.y, -a.z); }
+static inline float vdot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }               /* :477-480 */
+static inline float vlen2(v3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }                     /* :459-462 */
+static inline float vlen(v3 a) { return sqrtf(vlen2(a)); }                                        /* :464-467 */
+static inline v3 vnorm(v3 a) { const float L = vlen(a); return V3(a.x / L, a.y / L, a.z / L); }   /* :469-475 */
+static inline v3 vcross(v3 a, v3 b)                                                               /* :482-485 */
+{
+    return V3((a.y * b.z) - (a.z * b.y), (a.z * b.x) - (a.x * b.z), (a.x * b.y) - (a.y * b.x));
+}
+static inline float vabsdot(v3 a, v3 b) { return fabsf(vdot(a, b)); }                           /* :547 */
+static inline float vget(v3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+
+static inline float smin(float a, float b) { return (b < a) ? b : a; }   /* std::min */
+static inline float smax(float a, float b) { return (a < b) ? b : a; }   /* std::max */
+static inline float emin(float a, float b) { return a < b ? a : b; }     /* ExposureRender::Min */
+static inline float emax(float a, float b) { return a > b ? a : b; }     /* ExposureRender::Max */
+static inline float eclamp(float v, float lo, float hi) { return emax(lo, emin(v, hi)); }
+static inline int iclamp(int v, int lo, int hi) { int m = v < hi ? v : hi; return lo > m ? lo : m; }
+
+static inline col3 C3(float a, float b, float c) { col3 r; r.c[0] = a; r.c[1] = b; r.c[2] = c; return r; }
+static inline col3 cadd(col3 a, col3 b) { return C3(a.c[0] + b.c[0], a.c[1] + b.c[1], a.c[2] + b.c[2]); }
+static inline col3 csub(col3 a, col3 b) { return C3(a.c[0] - b.c[0], a.c[1] - b.c[1], a.c[2] - b.c[2]); }
+static inline col3 cmul(col3 a, col3 b) { return C3(a.c[0] * b.c[0], a.c[1] * b.c[1], a.c[2] * b.c[2]); }
+static inline col3 cdiv(col3 a, col3 b) { return C3(a.c[0] / b.c[0], a.c[1] / b.c[1], a.c[2] / b.c[2]); }
+static inline col3 cscale(col3 a, float s) { return C3(a.c[0] * s, a.c[1] * s, a.c[2] * s); }
+static inline col3 cdivs(col3 a, float s) { return C3(a.c[0] / s, a.c[1] / s, a.c[2] / s); }
+static inline int cblack(col3 a) { return a.c[0] == 0.0f && a.c[1] == 0.0f && a.c[2] == 0.0f; }  /* Source/color.h:27-35 */
+
+#define PI_F 3.141592654f                      /* Source/defines.h:58 */
+#define INV_PI_F 0.31830988618379067154f       /* :62 */
+#define INV_TWO_PI_F 0.15915494309189533577f   /* :63 */
+#define RAY_EPS 0.0001f                        /* :71 */
+/* INV_FOUR_PI_F expands to 1.0f / 4.0f * PI_F (:64-65), i.e. pi/4 */
+#define INV_FOUR_PI_EXPANDED (1.0f / 4.0f * PI_F)
+
+/* ------------------------------------------------------------------ */
+/* scene                                                                */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    er_light_desc d;
+    float area;
+} or_light;
+
+struct or_scene {
+    /* Volume (Source/volume.h:100-149) */
+    const uint16_t* vox;
+    int res[3];
+    v3 minp;
+    v3 inv_size;
+    v3 size;
+    v3 spacing;
+    float min_step;
+    v3 gdx, gdy, gdz;
+    /* Camera (Source/camera.h:61-116) */
+    int film[2];
+    v3 pos, N, U, V;
+    float screen[2][2];
+    float inv_screen[2];
+    float clip_near, clip_far, aperture, focal_distance, exposure;
+    /* tracer */
+    er_render_settings st;
+    er_plf opacity, glossiness;
+    er_color_tf diffuse, specular, emission;
+    int light_count;
+    int light_idx[ER_MAX_INDICES];
+    int n_lights;
+    or_light* lights;
+    int n_textures;
+    er_texture_desc* textures;
+    /* statistics */
+    uint64_t lookups;
+    uint64_t samples;
+};
+
+static double g_lookups_per_sample = 0.0;
+
+/* Shape::Update (Source/shape.h:92-103) with the area helpers :27-55 */
+static float shape_area(const er_shape* s)
+{
+    switch (s->type) {
+    case ER_SHAPE_PLANE: return s->size[0] * s->size[1];
+    case ER_SHAPE_DISK: return PI_F * (s->outer_radius * s->outer_radius);
+    case ER_SHAPE_RING: return PI_F * (s->outer_radius * s->outer_radius) - PI_F * (s->inner_radius * s->inner_radius);
+    case ER_SHAPE_BOX: return (2.0f * s->size[0] * s->size[1]) + (2.0f * s->size[0] * s->size[2]) + (2.0f * s->size[1] * s->size[2]);
+    case ER_SHAPE_SPHERE: return 4.0f * PI_F * (s->outer_radius * s->outer_radius);
+    case ER_SHAPE_CYLINDER: return (2.0f * PI_F * (s->outer_radius * s->outer_radius)) + (2.0f * PI_F * s->outer_radius * s->size[2]);
+    default: return s->area;   /* Update() leaves Area untouched for other types */
+    }
+}
+
+or_scene* ER_OR(scene_create)(const er_tracer_desc* t, const er_volume_desc* vol,
+                              const er_light_desc* lights, int32_t n_lights,
+                              const er_texture_desc* textures, int32_t n_textures)
+{
+    or_scene* s = (or_scene*)calloc(1, sizeof(or_scene));
+    if (!s) return NULL;
+    /* Volume::operator=(const ErVolume&) - Source/volume.h:100-129 */
+    s->vox = vol->voxels;
+    for (int i = 0; i < 3; i++) s->res[i] = vol->resolution[i];
+    float scale = 0.0f;
+    if (vol->normalize_size) {
+        const v3 phys = V3((float)s->res[0] * vol->spacing[0], (float)s->res[1] * vol->spacing[1], (float)s->res[2] * vol->spacing[2]);
+        scale = 1.0f / smax(phys.x, smax(phys.y, phys.z));
+    }
+    s->spacing = V3(vol->spacing[0] * scale, vol->spacing[1] * scale, vol->spacing[2] * scale);
+    s->size = V3((float)s->res[0] * s->spacing.x, (float)s->res[1] * s->spacing.y, (float)s->res[2] * s->spacing.z);
+    s->inv_size = V3(1.0f / s->size.x, 1.0f / s->size.y, 1.0f / s->size.z);
+    s->minp = vscale(s->size, -0.5f);
+    s->min_step = smin(s->spacing.x, smin(s->spacing.y, s->spacing.z));
+    s->gdx = V3(s->min_step, 0.0f, 0.0f);
+    s->gdy = V3(0.0f, s->min_step, 0.0f);
+    s->gdz = V3(0.0f, 0.0f, s->min_step);
+
+    /* Camera::Update - Source/camera.h:61-96 */
+    const er_camera_desc* c = &t->camera;
+    s->film[0] = c->film_size[0];
+    s->film[1] = c->film_size[1];
+    s->pos = V3(c->pos[0], c->pos[1], c->pos[2]);
+    const v3 target = V3(c->target[0], c->target[1], c->target[2]);
+    const v3 up = V3(c->up[0], c->up[1], c->up[2]);
+    s->N = vnorm(vsub(target, s->pos));
+    s->U = vnorm(vcross(s->N, up));
+    s->V = vnorm(vcross(s->N, s->U));
+    s->focal_distance = c->focal_distance;
+    if (s->focal_distance == -1.0f) s->focal_distance = vlen(vsub(target, s->pos));
+    const float sc = er_tanf((0.5f * c->fov / 57.29577951308232f));
+    const float aspect = (float)c->film_size[1] / (float)c->film_size[0];
+    if (aspect > 1.0f) {
+        s->screen[0][0] = -sc; s->screen[0][1] = sc;
+        s->screen[1][0] = -sc * aspect; s->screen[1][1] = sc * aspect;
+    } else {
+        s->screen[0][0] = -sc / aspect; s->screen[0][1] = sc / aspect;
+        s->screen[1][0] = -sc; s->screen[1][1] = sc;
+    }
+    s->inv_screen[0] = (s->screen[0][1] - s->screen[0][0]) / (float)c->film_size[0];
+    s->inv_screen[1] = (s->screen[1][1] - s->screen[1][0]) / (float)c->film_size[1];
+    s->clip_near = c->clip_near;
+    s->clip_far = c->clip_far;
+    s->aperture = c->aperture_size;
+    s->exposure = c->exposure;
+
+    s->st = t->settings;
+    s->opacity = t->opacity;
+    s->glossiness = t->glossiness;
+    s->diffuse = t->diffuse;
+    s->specular = t->specular;
+    s->emission = t->emission;
+    s->light_count = t->light_count;
+    for (int i = 0; i < ER_MAX_INDICES; i++) s->light_idx[i] = t->light_ids[i];
+
+    s->n_lights = n_lights;
+    s->lights = (or_light*)calloc(n_lights > 0 ? (size_t)n_lights : 1u, sizeof(or_light));
+    for (int i = 0; i < n_lights; i++) {
+        s->lights[i].d = lights[i];
+        s->lights[i].area = shape_area(&lights[i].shape);   /* Light::operator= - Source/light.h:39-45 */
+    }
+    s->n_textures = n_textures;
+    s->textures = (er_texture_desc*)calloc(n_textures > 0 ? (size_t)n_textures : 1u, sizeof(er_texture_desc));
+    if (n_textures > 0) memcpy(s->textures, textures, sizeof(er_texture_desc) * (size_t)n_textures);
+    return s;
+}
+
+void ER_OR(scene_destroy)(or_scene* s)
+{
+    if (!s) return;
+    free(s->lights);
+    free(s->textures);
+    free(s);
+}
+
+/* ------------------------------------------------------------------ */
+/* RNG - Source/rng.h:26-66                                             */
+/* ------------------------------------------------------------------ */
+
+typedef struct { uint32_t s0, s1; } rng_t;
+
+static inline float rng_get1(rng_t* r)   /* :35-51 */
+{
+    r->s0 = 36969u * (r->s0 & 65535u) + (r->s0 >> 16);
+    r->s1 = 18000u * (r->s1 & 65535u) + (r->s1 >> 16);
+    const uint32_t ires = (r->s0 << 16) + r->s1;
+    const float f = er_u2f((ires & 0x007fffffu) | 0x40000000u);
+    return (f - 2.0f) / 2.0f;
+}
+
+/* Get2/Get3 (:53-61) construct Vec2f(Get1(), Get1()); the host compiler
+   evaluates constructor arguments right to left, so the last component
+   receives the first draw (checked by tests/test_oracle_ref.py). */
+static inline v2 rng_get2(rng_t* r)
+{
+    v2 v;
+    v.y = rng_get1(r);
+    v.x = rng_get1(r);
+    return v;
+}
+static inline v3 rng_get3(rng_t* r)
+{
+    v3 v;
+    v.z = rng_get1(r);
+    v.y = rng_get1(r);
+    v.x = rng_get1(r);
+    return v;
+}
+
+/* MetroSample::LargeStep - Source/sample.h:258-262 with :142-146, :101-104,
+   :180-185, :221-225 */
+typedef struct {
+    float brdf_component;
+    v2 brdf_dir;
+    v3 light_uvw;
+    float light_num;
+    v2 film_uv;
+    v2 lens_uv;
+} metro_sample;
+
+static inline void metro_large_step(metro_sample* m, rng_t* r)
+{
+    m->brdf_component = rng_get1(r);
+    m->brdf_dir = rng_get2(r);
+    m->light_uvw = rng_get3(r);
+    m->light_num = rng_get1(r);
+    m->film_uv = rng_get2(r);
+    m->lens_uv = rng_get2(r);
+}
+
+/* ------------------------------------------------------------------ */
+/* transfer functions - Source/plf.h:68-91                              */
+/* ------------------------------------------------------------------ */
+
+static inline float plf_eval(const er_plf* p, float x)
+{
+    if (p->count <= 0) return 0.0f;
+    if (x < p->node_range[0]) return p->value[0];
+    if (x > p->node_range[1]) return p->value[p->count - 1];
+    for (int i = 1; i < p->count; i++) {
+        const float P1 = p->position[i - 1];
+        const float P2 = p->position[i];
+        const float DeltaP = P2 - P1;
+        const float LerpT = (x - P1) / DeltaP;
+        if (x >= P1 && x < P2) return p->value[i - 1] + LerpT * (p->value[i] - p->value[i - 1]);
+    }
+    return 0.0f;
+}
+
+/* ColorTransferFunction1D::Evaluate - Source/transferfunction.h:148-151 */
+static inline col3 ctf_eval(const er_color_tf* t, float x)
+{
+    return C3(plf_eval(&t->plf[0], x), plf_eval(&t->plf[1], x), plf_eval(&t->plf[2], x));
+}
+
+/* ------------------------------------------------------------------ */
+/* volume access                                                        */
+/* ------------------------------------------------------------------ */
+
+/* Buffer3D<T>::operator()(const int&,const int&,const int&) - Source/buffer3d.h:210-214 */
+static inline float voxel(const or_scene* s, int x, int y, int z)
+{
+    const int cx = iclamp(x, 0, s->res[0] - 1);
+    const int cy = iclamp(y, 0, s->res[1] - 1);
+    const int cz = iclamp(z, 0, s->res[2] - 1);
+    return (float)s->vox[(size_t)cz * (size_t)s->res[0] * (size_t)s->res[1] + (size_t)cy * (size_t)s->res[0] + (size_t)cx];
+}
+
+/* Lerp(t, v1, v2) - Source/geometry.h:87-90; the result is stored in an
+   unsigned short (T of Buffer3D<unsigned short>), i.e. truncated. */
+static inline float lerp_u16(float t, float a, float b)
+{
+    const float r = (1.0f - t) * a + t * b;
+    return (float)(unsigned short)r;
+}
+
+/* GetIntensity (Source/volumes.h:26-29) -> Volume::operator() (Source/volume.h:131-138)
+   -> Buffer3D<unsigned short>::operator()(Vec3f) (Source/buffer3d.h:222-242) */
+static inline float get_intensity(or_scene* s, v3 P)
+{
+    s->lookups++;
+    const v3 off = vsub(P, s->minp);
+    const v3 L = V3(off.x * s->inv_size.x * (float)s->res[0], off.y * s->inv_size.y * (float)s->res[1],
+                    off.z * s->inv_size.z * (float)s->res[2]);
+    const int vx = (int)floorf(L.x);
+    const int vy = (int)floorf(L.y);
+    const int vz = (int)floorf(L.z);
+    const float dx = L.x - (float)vx;
+    const float dy = L.y - (float)vy;
+    const float dz = L.z - (float)vz;
+    const float d00 = lerp_u16(dx, voxel(s, vx, vy, vz), voxel(s, vx + 1, vy, vz));
+    const float d10 = lerp_u16(dx, voxel(s, vx, vy + 1, vz), voxel(s, vx + 1, vy + 1, vz));
+    const float d01 = lerp_u16(dx, voxel(s, vx, vy, vz + 1), voxel(s, vx + 1, vy, vz + 1));
+    const float d11 = lerp_u16(dx, voxel(s, vx, vy + 1, vz + 1), voxel(s, vx + 1, vy + 1, vz + 1));
+    const float d0 = lerp_u16(dy, d00, d10);
+    const float d1 = lerp_u16(dy, d01, d11);
+    return lerp_u16(dz, d0, d1);
+}
+
+/* GradientCD / GradientFD / GradientFiltered / Gradient - Source/volumes.h:31-86 */
+static v3 gradient_cd(or_scene* s, v3 P)
+{
+    const float i00 = get_intensity(s, vadd(P, s->gdx)), i01 = get_intensity(s, vsub(P, s->gdx));
+    const float i10 = get_intensity(s, vadd(P, s->gdy)), i11 = get_intensity(s, vsub(P, s->gdy));
+    const float i20 = get_intensity(s, vadd(P, s->gdz)), i21 = get_intensity(s, vsub(P, s->gdz));
+    return V3(i01 - i00, i11 - i10, i21 - i20);
+}
+
+static v3 gradient_fd(or_scene* s, v3 P)
+{
+    const float i0 = get_intensity(s, P);
+    const float i1 = get_intensity(s, vadd(P, s->gdx));
+    const float i2 = get_intensity(s, vadd(P, s->gdy));
+    const float i3 = get_intensity(s, vadd(P, s->gdz));
+    return V3(i0 - i1, i0 - i2, i0 - i3);
+}
+
+/* Lerp(const Vec3f& A, const Vec3f& B, const float& c) = A + c*(B - A) - Source/vector.h:552 */
+static inline v3 vlerp(v3 a, v3 b, float c) { return vadd(a, vscale(vsub(b, a), c)); }
+
+static v3 gradient_filtered(or_scene* s, v3 P)
+{
+    const v3 o = V3(s->gdx.x, s->gdy.y, s->gdz.z);
+    const v3 G0 = gradient_cd(s, P);
+    const v3 G1 = gradient_cd(s, vadd(P, V3(-o.x, -o.y, -o.z)));
+    const v3 G2 = gradient_cd(s, vadd(P, V3(o.x, o.y, o.z)));
+    const v3 G3 = gradient_cd(s, vadd(P, V3(-o.x, o.y, -o.z)));
+    const v3 G4 = gradient_cd(s, vadd(P, V3(o.x, -o.y, o.z)));
+    const v3 G5 = gradient_cd(s, vadd(P, V3(-o.x, -o.y, o.z)));
+    const v3 G6 = gradient_cd(s, vadd(P, V3(o.x, o.y, -o.z)));
+    const v3 G7 = gradient_cd(s, vadd(P, V3(-o.x, o.y, o.z)));
+    const v3 G8 = gradient_cd(s, vadd(P, V3(o.x, -o.y, -o.z)));
+    const v3 L0 = vlerp(vlerp(G1, G2, 0.5f), vlerp(G3, G4, 0.5f), 0.5f);
+    const v3 L1 = vlerp(vlerp(G5, G6, 0.5f), vlerp(G7, G8, 0.5f), 0.5f);
+    return vlerp(G0, vlerp(L0, L1, 0.5f), 0.75f);
+}
+
+static v3 gradient(or_scene* s, v3 P)
+{
+    switch (s->st.gradient_computation) {
+    case ER_GRADIENT_FORWARD: return gradient_fd(s, P);
+    case ER_GRADIENT_CENTRAL: return gradient_cd(s, P);
+    case ER_GRADIENT_FILTERED: return gradient_filtered(s, P);
+    default: return gradient_fd(s, P);
+    }
+}
+
+/* NormalizedGradient - Source/volumes.h:88-91 */
+static v3 normalized_gradient(or_scene* s, v3 P) { return vnorm(gradient(s, P)); }
+
+/* GradientMagnitude - Source/volumes.h:93-114 */
+static float gradient_magnitude(or_scene* s, v3 P)
+{
+    v3 pts[3][2];
+    pts[0][0] = vadd(P, s->gdx); pts[0][1] = vsub(P, s->gdx);
+    pts[1][0] = vadd(P, s->gdy); pts[1][1] = vsub(P, s->gdy);
+    pts[2][0] = vadd(P, s->gdz); pts[2][1] = vsub(P, s->gdz);
+    float sum = 0.0f;
+    for (int i = 0; i < 3; i++) {
+        float D = get_intensity(s, pts[i][1]) - get_intensity(s, pts[i][0]);
+        D *= 0.5f / vget(s->spacing, i);
+        sum += D * D;
+    }
+    return sqrtf(sum);
+}
+
+/* ------------------------------------------------------------------ */
+/* geometry                                                             */
+/* ------------------------------------------------------------------ */
+
+typedef struct { v3 O, D; float MinT, MaxT; } ray_t;   /* Source/ray.h:26-56 */
+
+/* Ray::operator()(T) = O + Normalize(D)*T - Source/ray.h:47-50 */
+static inline v3 ray_at(const ray_t* r, float t) { return vadd(r->O, vscale(vnorm(r->D), t)); }
+
+typedef struct {                                         /* Source/intersection.h:30-78 */
+    int valid, front;
+    float near_t, far_t;
+    v3 P, N;
+    v2 UV;
+} isect_t;
+
+static inline void isect_invalid(isect_t* i)             /* :47-56 */
+{
+    i->valid = 0; i->front = 1; i->near_t = 0.0f; i->far_t = FLT_MAX;
+    i->P = V3(0, 0, 0); i->N = V3(0, 0, 0); i->UV.x = 0.0f; i->UV.y = 0.0f;
+}
+
+/* TransformPoint / TransformVector / TransformRay - Source/geometry.h:30-68 */
+static inline v3 xform_point(const float m[4][4], v3 p)
+{
+    return V3(m[0][0] * p.x + m[0][1] * p.y + m[0][2] * p.z + m[0][3],
+              m[1][0] * p.x + m[1][1] * p.y + m[1][2] * p.z + m[1][3],
+              m[2][0] * p.x + m[2][1] * p.y + m[2][2] * p.z + m[2][3]);
+}
+static inline v3 xform_vector(const float m[4][4], v3 v)
+{
+    return V3(m[0][0] * v.x + m[0][1] * v.y + m[0][2] * v.z,
+              m[1][0] * v.x + m[1][1] * v.y + m[1][2] * v.z,
+              m[2][0] * v.x + m[2][1] * v.y + m[2][2] * v.z);
+}
+static inline ray_t xform_ray(const float m[4][4], const ray_t* r)
+{
+    ray_t t;
+    const v3 P = xform_point(m, r->O);
+    const v3 MinP = xform_point(m, ray_at(r, r->MinT));
+    const v3 MaxP = xform_point(m, ray_at(r, r->MaxT));
+    t.O = P;
+    t.D = vnorm(vsub(MaxP, t.O));
+    t.MinT = vlen(vsub(MinP, t.O));
+    t.MaxT = vlen(vsub(MaxP, t.O));
+    return t;
+}
+
+/* SphericalTheta / SphericalPhi / SphericalToUV - Source/geometry.h:70-85 */
+static inline float spherical_theta(v3 w) { return er_acosf(eclamp(w.y, -1.0f, 1.0f)); }
+static inline float spherical_phi(v3 w)
+{
+    const float p = er_atan2f(w.z, w.x);
+    return (p < 0.0f) ? p + 2.0f * PI_F : p;
+}
+
+/* IntersectBox(R, MinAABB, MaxAABB, Int) - Source/box.h:51-83 */
+static void intersect_box(const ray_t* R, v3 mn, v3 mx, isect_t* I)
+{
+    const v3 InvR = V3(1.0f / R->D.x, 1.0f / R->D.y, 1.0f / R->D.z);
+    const v3 B = vmul(InvR, vsub(mn, R->O));
+    const v3 T = vmul(InvR, vsub(mx, R->O));
+    const v3 MinT = V3(smin(T.x, B.x), smin(T.y, B.y), smin(T.z, B.z));
+    const v3 MaxT = V3(smax(T.x, B.x), smax(T.y, B.y), smax(T.z, B.z));
+    const float LargestMinT = fmaxf(fmaxf(MinT.x, MinT.y), fmaxf(MinT.x, MinT.z));
+    const float LargestMaxT = fminf(fminf(MaxT.x, MaxT.y), fminf(MaxT.x, MaxT.z));
+    if (LargestMaxT < LargestMinT) return;
+    I->near_t = LargestMinT > 0.0f ? LargestMinT : 0.0f;
+    I->far_t = LargestMaxT;
+    if (I->near_t < R->MinT || I->near_t > R->MaxT) return;
+    I->valid = 1;
+    I->P = ray_at(R, I->near_t);
+    I->N = V3(0, 0, 0);
+    I->UV.x = 0.0f; I->UV.y = 0.0f;
+    float n[3] = { 0.0f, 0.0f, 0.0f };
+    for (int i = 0; i < 3; i++) {
+        if (vget(I->P, i) <= vget(mn, i) + 0.0001f) n[i] = -1.0f;
+        if (vget(I->P, i) >= vget(mx, i) - 0.0001f) n[i] = 1.0f;
+    }
+    I->N = V3(n[0], n[1], n[2]);
+}
+
+/* IntersectPlane(R, OneSided, Int) - Source/plane.h:41-62 */
+static void intersect_plane_inf(const ray_t* R, int one_sided, isect_t* I)
+{
+    if (fabsf(R->O.z - R->D.z) < RAY_EPS) return;
+    I->near_t = (0.0f - R->O.z) / R->D.z;
+    if (I->near_t < R->MinT || I->near_t > R->MaxT) return;
+    I->P = ray_at(R, I->near_t);
+    I->UV.x = I->P.x; I->UV.y = I->P.y;
+    I->N = V3(0.0f, 0.0f, 1.0f);
+    if (one_sided && R->D.z >= 0.0f) {
+        I->front = 0;
+        I->N = V3(0.0f, 0.0f, -1.0f);
+    }
+    I->valid = 1;
+}
+
+/* IntersectPlane(R, OneSided, Size, Int) - Source/plane.h:76-88 */
+static void intersect_plane(const ray_t* R, int one_sided, float sx, float sy, isect_t* I)
+{
+    intersect_plane_inf(R, one_sided, I);
+    if (I->valid && (I->UV.x < -0.5f * sx || I->UV.x > 0.5f * sx || I->UV.y < -0.5f * sy || I->UV.y > 0.5f * sy))
+        I->valid = 0;
+    I->UV.x /= sx;
+    I->UV.y /= sy;
+    I->UV.x = I->UV.x + 0.5f;
+    I->UV.y = I->UV.y + 0.5f;
+    I->UV.x = 1.0f - I->UV.x;
+}
+
+static inline float v2len(v2 a) { return sqrtf(a.x * a.x + a.y * a.y); }   /* Source/vector.h:418-426 */
+
+/* IntersectDisk - Source/disk.h:37-49 */
+static void intersect_disk(const ray_t* R, int one_sided, float radius, isect_t* I)
+{
+    intersect_plane_inf(R, one_sided, I);
+    if (I->valid && v2len(I->UV) > radius) I->valid = 0;
+    const float diameter = 2.0f * radius;
+    I->UV.x /= diameter; I->UV.y /= diameter;
+    I->UV.x = I->UV.x + 0.5f; I->UV.y = I->UV.y + 0.5f;
+    I->UV.x = 1.0f - I->UV.x;
+}
+
+/* IntersectRing - Source/ring.h:45-57 */
+static void intersect_ring(const ray_t* R, int one_sided, float inner, float outer, isect_t* I)
+{
+    intersect_plane_inf(R, one_sided, I);
+    if (I->valid && (v2len(I->UV) < inner || v2len(I->UV) > outer)) I->valid = 0;
+    const float diameter = 2.0f * outer;
+    I->UV.x /= diameter; I->UV.y /= diameter;
+    I->UV.x = I->UV.x + 0.5f; I->UV.y = I->UV.y + 0.5f;
+    I->UV.x = 1.0f - I->UV.x;
+}
+
+/* IntersectSphere - Source/sphere.h:84-140 */
+static void intersect_sphere(const ray_t* R, float radius, isect_t* I)
+{
+    const float a = vdot(R->D, R->D);
+    const float b = 2 * vdot(R->D, R->O);
+    const float c = vdot(R->O, R->O) - (radius * radius);
+    const float disc = b * b - 4 * a * c;
+    if (disc < 0) return;
+    const float distSqrt = sqrtf(disc);
+    float q;
+    if (b < 0) q = (-b - distSqrt) / 2.0f;
+    else q = (-b + distSqrt) / 2.0f;
+    float t0 = q / a;
+    float t1 = c / q;
+    if (t0 > t1) { const float tmp = t0; t0 = t1; t1 = tmp; }
+    if (t0 >= R->MinT && t0 < R->MaxT) I->near_t = t0;
+    else {
+        if (t1 >= R->MinT && t1 < R->MaxT) I->near_t = t1;
+        else return;
+    }
+    if (I->near_t < R->MinT || I->near_t > R->MaxT) return;
+    I->valid = 1;
+    I->P = ray_at(R, I->near_t);
+    I->N = vnorm(I->P);
+    const v3 Vn = vnorm(I->P);   /* SphericalToUV - Source/geometry.h:81-85 */
+    I->UV.x = INV_TWO_PI_F * spherical_phi(Vn);
+    I->UV.y = 1.0f - (INV_PI_F * spherical_theta(Vn));
+}
+
+/* IntersectShape / IntersectsShape - Source/shapes.h:44-72 (box lights use the
+   3-component size, Source/box.h:85-88) */
+static void intersect_shape(const er_shape* sh, const ray_t* R, isect_t* I)
+{
+    switch (sh->type) {
+    case ER_SHAPE_PLANE: intersect_plane(R, sh->one_sided, sh->size[0], sh->size[1], I); break;
+    case ER_SHAPE_DISK: intersect_disk(R, sh->one_sided, sh->outer_radius, I); break;
+    case ER_SHAPE_RING: intersect_ring(R, sh->one_sided, sh->inner_radius, sh->outer_radius, I); break;
+    case ER_SHAPE_BOX: {
+        const v3 size = V3(sh->size[0], sh->size[1], sh->size[2]);
+        intersect_box(R, vscale(size, -0.5f), vscale(size, 0.5f), I);
+        break;
+    }
+    case ER_SHAPE_SPHERE: intersect_sphere(R, sh->outer_radius, I); break;
+    default: break;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* sampling - Source/montecarlo.h, shape samplers                       */
+/* ------------------------------------------------------------------ */
+
+/* ConcentricSampleDisk - Source/montecarlo.h:86-137 */
+static v2 concentric_sample_disk(v2 U)
+{
+    float r, theta;
+    const float sx = 2 * U.x - 1;
+    const float sy = 2 * U.y - 1;
+    v2 out;
+    if (sx == 0.0 && sy == 0.0) { out.x = 0.0f; out.y = 0.0f; return out; }
+    if (sx >= -sy) {
+        if (sx > sy) {
+            r = sx;
+            if (sy > 0.0) theta = sy / r;
+            else theta = 8.0f + sy / r;
+        } else {
+            r = sy;
+            theta = 2.0f - sx / r;
+        }
+    } else {
+        if (sx <= sy) {
+            r = -sx;
+            theta = 4.0f - sy / r;
+        } else {
+            r = -sy;
+            theta = 6.0f + sx / r;
+        }
+    }
+    theta *= PI_F / 4.f;
+    float sn, cs;
+    er_sincosf(theta, &sn, &cs);
+    out.x = r * cs;
+    out.y = r * sn;
+    return out;
+}
+
+typedef struct { v3 P, N; v2 UV; } surf_sample;   /* Source/sample.h:57-79 */
+
+/* SampleLightSurface - Source/lights.h:28-42 with the shape samplers
+   Source/plane.h:95-107, Source/disk.h:59-74, Source/ring.h:59-75,
+   Source/box.h:122-191, Source/sphere.h:152-170 */
+static void sample_light_surface(const or_light* L, v3 UVW, surf_sample* SS)
+{
+    const er_shape* sh = &L->d.shape;
+    SS->P = V3(0, 0, 0); SS->N = V3(0.0f, 0.0f, 1.0f); SS->UV.x = 0.0f; SS->UV.y = 0.0f;
+    switch (sh->type) {
+    case ER_SHAPE_PLANE:
+        SS->P = V3(-0.5f + UVW.x, -0.5f + UVW.y, 0.0f);
+        SS->N = V3(0.0f, 0.0f, 1.0f);
+        SS->UV.x = UVW.x; SS->UV.y = UVW.y;
+        SS->P = vmul(SS->P, V3(sh->size[0], sh->size[1], 0.0f));
+        break;
+    case ER_SHAPE_DISK: {
+        const float r = sqrtf(UVW.x);
+        const float theta = 2.0f * PI_F * UVW.y;
+        float sn, cs; er_sincosf(theta, &sn, &cs);
+        SS->P = V3(r * cs, r * sn, 0.0f);
+        SS->N = V3(0.0f, 0.0f, 1.0f);
+        SS->UV.x = UVW.x; SS->UV.y = UVW.y;
+        SS->P = vscale(SS->P, sh->outer_radius);
+        break;
+    }
+    case ER_SHAPE_RING: {
+        const float inner = sh->inner_radius / sh->outer_radius;
+        const float r = inner + (1.0f - inner) * sqrtf(UVW.x);
+        const float theta = 2.0f * PI_F * UVW.y;
+        float sn, cs; er_sincosf(theta, &sn, &cs);
+        SS->P = V3(r * cs, r * sn, 0.0f);
+        SS->N = V3(0.0f, 0.0f, 1.0f);
+        SS->P = vscale(SS->P, sh->outer_radius);
+        SS->UV.x = SS->P.x; SS->UV.y = SS->P.y;
+        break;
+    }
+    case ER_SHAPE_BOX: {
+        const int side = (int)floorf(UVW.x * 6.0f);
+        v3 p = V3(0, 0, 0);
+        v3 n = SS->N;
+        switch (side) {
+        case 0: p = V3(0.5f, -0.5f + UVW.z, -0.5f + UVW.y); n = V3(1.0f, 0.0f, 0.0f); break;
+        case 1: p = V3(-0.5f, -0.5f + UVW.z, -0.5f + UVW.y); n = V3(-1.0f, 0.0f, 0.0f); break;
+        case 2: p = V3(-0.5f + UVW.y, 0.5f, -0.5f + UVW.z); n = V3(0.0f, 1.0f, 0.0f); break;
+        case 3: p = V3(-0.5f + UVW.y, -0.5f, -0.5f + UVW.z); n = V3(0.0f, -1.0f, 0.0f); break;
+        case 4: p = V3(-0.5f + UVW.y, -0.5f + UVW.z, 0.5f); n = V3(0.0f, 0.0f, 1.0f); break;
+        case 5: p = V3(-0.5f + UVW.y, -0.5f + UVW.z, -0.5f); n = V3(0.0f, 0.0f, -1.0f); break;
+        default: break;
+        }
+        SS->P = p; SS->N = n;
+        SS->UV.x = UVW.y; SS->UV.y = UVW.z;
+        SS->P = vmul(SS->P, V3(sh->size[0], sh->size[1], sh->size[2]));
+        break;
+    }
+    case ER_SHAPE_SPHERE: {
+        const float z = 1.0f - 2.0f * UVW.x;
+        const float r = sqrtf(smax(0.0f, 1.0f - z * z));
+        const float phi = 2.0f * PI_F * UVW.y;
+        float sn, cs; er_sincosf(phi, &sn, &cs);
+        SS->P = V3(r * cs, r * sn, z);
+        SS->N = SS->P;
+        SS->UV.x = spherical_theta(SS->P);
+        SS->UV.y = spherical_phi(SS->P);
+        SS->P = vscale(SS->P, sh->outer_radius);
+        break;
+    }
+    default: break;
+    }
+    SS->P = xform_point(sh->tm, SS->P);
+    SS->N = xform_vector(sh->tm, SS->N);
+}
+
+/* ------------------------------------------------------------------ */
+/* textures - Source/textures.h:26-111                                  */
+/* ------------------------------------------------------------------ */
+
+static col3 evaluate_texture(const or_scene* s, int id, v2 UV)
+{
+    if (id < 0) return C3(0, 0, 0);
+    if (id >= s->n_textures) return C3(0, 0, 0);
+    const er_texture_desc* T = &s->textures[id];
+    col3 L = C3(0, 0, 0);
+    v2 tuv = UV;
+    tuv.x *= T->repeat[0];
+    tuv.y *= T->repeat[1];
+    tuv.x += T->offset[0];
+    tuv.y += 1.0f - T->offset[1];
+    tuv.x = tuv.x - floorf(tuv.x);
+    tuv.y = tuv.y - floorf(tuv.y);
+    tuv.x = eclamp(tuv.x, 0.0f, 1.0f);
+    tuv.y = eclamp(tuv.y, 0.0f, 1.0f);
+    if (T->flip[0]) tuv.x = 1.0f - tuv.x;
+    if (T->flip[1]) tuv.y = 1.0f - tuv.y;
+    if (T->type == ER_TEXTURE_PROCEDURAL) {
+        const er_procedural* P = &T->procedural;
+        switch (P->type) {
+        case ER_PROCEDURAL_UNIFORM: L = C3(P->uniform_color[0], P->uniform_color[1], P->uniform_color[2]); break;
+        case ER_PROCEDURAL_CHECKER: {
+            const int u = (int)(tuv.x * 2.0f), v = (int)(tuv.y * 2.0f);
+            const float* c1 = P->checker_color1;
+            const float* c2 = P->checker_color2;
+            const float* c = (u % 2 == 0) ? ((v % 2 == 0) ? c1 : c2) : ((v % 2 == 0) ? c2 : c1);
+            L = C3(c[0], c[1], c[2]);
+            break;
+        }
+        case ER_PROCEDURAL_GRADIENT: L = ctf_eval(&P->gradient, tuv.y); break;
+        default: L = C3(0, 0, 0); break;
+        }
+    }
+    /* bitmap textures (Source/textures.h:101-107) are not on the configured path */
+    return cscale(L, T->output_level);
+}
+
+/* ------------------------------------------------------------------ */
+/* shading - Source/shader.h                                            */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    int type;          /* 0 = BRDF, 1 = isotropic phase (Source/enums.h:95-99) */
+    v3 Nn, Nu, Nv;
+    col3 Kd, Ks;
+    float ior;
+    float exponent;
+} shader_t;
+
+/* Shader(Type, N, Wo, Kd, Ks, Ior, Exponent) - Source/shader.h:422-427 with BRDF :323-330 */
+static void shader_init(shader_t* sh, int type, v3 N, v3 Wo, col3 Kd, col3 Ks, float ior, float exponent)
+{
+    sh->type = type;
+    sh->Nn = vnorm(N);
+    sh->Nu = vnorm(vcross(N, Wo));
+    sh->Nv = vnorm(vcross(N, sh->Nu));
+    sh->Kd = Kd;
+    sh->Ks = Ks;
+    sh->ior = ior;
+    sh->exponent = exponent;
+}
+
+/* BRDF::WorldToLocal - Source/shader.h:332-335 */
+static inline v3 world_to_local(const shader_t* sh, v3 W) { return V3(vdot(W, sh->Nu), vdot(W, sh->Nv), vdot(W, sh->Nn)); }
+/* BRDF::LocalToWorld - :337-342 */
+static inline v3 local_to_world(const shader_t* sh, v3 W)
+{
+    return V3(sh->Nu.x * W.x + sh->Nv.x * W.y + sh->Nn.x * W.z,
+              sh->Nu.y * W.x + sh->Nv.y * W.y + sh->Nn.y * W.z,
+              sh->Nu.z * W.x + sh->Nv.z * W.y + sh->Nn.z * W.z);
+}
+
+/* Fresnel::Evaluate - Source/shader.h:92-117, FrDiel :72-77 (all three
+   components of the colour are equal, so one scalar is carried) */
+static float fresnel_eval(float ei_, float et_, float cosi)
+{
+    cosi = eclamp(cosi, -1.0f, 1.0f);
+    const int entering = cosi > 0.0f;
+    float ei = ei_, et = et_;
+    if (!entering) { const float t = ei; ei = et; et = t; }
+    const float sint = ei / et * sqrtf(smax(0.f, 1.f - cosi * cosi));
+    if (sint >= 1.0f) return 1.0f;
+    const float cost = sqrtf(smax(0.f, 1.0f - sint * sint));
+    const float ci = fabsf(cosi);
+    const float Rparl = ((et * ci) - (ei * cost)) / ((et * ci) + (ei * cost));
+    const float Rperp = ((ei * ci) - (et * cost)) / ((ei * ci) + (et * cost));
+    return (Rparl * Rparl + Rperp * Rperp) / 2.f;
+}
+
+/* Blinn::D - :182-186 */
+static inline float blinn_d(float exponent, v3 Wh)
+{
+    const float c = fabsf(Wh.z);
+    return (exponent + 2) * INV_TWO_PI_F * er_powf(c, exponent);
+}
+
+/* Blinn::Pdf - :166-180 */
+static inline float blinn_pdf(float exponent, v3 Wo, v3 Wi)
+{
+    const v3 Wh = vnorm(vadd(Wo, Wi));
+    const float CosTheta = fabsf(Wh.z);
+    float pdf = ((exponent + 1.0f) * er_powf(CosTheta, exponent)) / (2.0f * PI_F * 4.0f * vdot(Wo, Wh));
+    if (vdot(Wo, Wh) <= 0.0f) pdf = 0.0f;
+    return pdf;
+}
+
+/* Microfacet::F - :212-231 with G :251-259 */
+static col3 microfacet_f(const shader_t* sh, v3 Wo, v3 Wi)
+{
+    const float cosThetaO = fabsf(Wo.z);
+    const float cosThetaI = fabsf(Wi.z);
+    if (cosThetaI == 0.f || cosThetaO == 0.f) return C3(0, 0, 0);
+    v3 Wh = vadd(Wi, Wo);
+    if (Wh.x == 0. && Wh.y == 0. && Wh.z == 0.) return C3(0, 0, 0);
+    Wh = vnorm(Wh);
+    const float cosThetaH = vdot(Wi, Wh);
+    const float F = fresnel_eval(1.0f, sh->ior, cosThetaH);
+    const float NdotWh = fabsf(Wh.z), NdotWo = fabsf(Wo.z), NdotWi = fabsf(Wi.z);
+    const float WOdotWh = vabsdot(Wo, Wh);
+    const float G = smin(1.0f, smin((2.0f * NdotWh * NdotWo / WOdotWh), (2.0f * NdotWh * NdotWi / WOdotWh)));
+    const float D = blinn_d(sh->exponent, Wh);
+    const float den = 4.0f * cosThetaI * cosThetaO;
+    col3 r = cscale(sh->Ks, D);
+    r = cscale(r, G);
+    r = cscale(r, F);
+    return cdivs(r, den);
+}
+
+static inline int same_hemisphere(v3 a, v3 b) { return (a.z * b.z) > 0.0f; }   /* Source/montecarlo.h:57-60 */
+
+/* Shader::F - :429-441 (BRDF::F :344-355, IsotropicPhase::F :288-291) */
+static col3 shader_f(const shader_t* sh, v3 Wo, v3 Wi)
+{
+    if (sh->type == 0) {
+        const v3 Wol = world_to_local(sh, Wo);
+        const v3 Wil = world_to_local(sh, Wi);
+        col3 R = C3(0, 0, 0);
+        R = cadd(R, cscale(sh->Kd, INV_PI_F));
+        R = cadd(R, microfacet_f(sh, Wol, Wil));
+        return R;
+    }
+    return cscale(sh->Kd, INV_PI_F);
+}
+
+/* Shader::Pdf - :457-469 (BRDF::Pdf :384-395, Lambertian::Pdf :58-61,
+   Microfacet::Pdf :243-249, IsotropicPhase::Pdf :301-304) */
+static float shader_pdf(const shader_t* sh, v3 Wo, v3 Wi)
+{
+    if (sh->type == 0) {
+        const v3 Wol = world_to_local(sh, Wo);
+        const v3 Wil = world_to_local(sh, Wi);
+        float pdf = 0.0f;
+        pdf += same_hemisphere(Wol, Wil) ? fabsf(Wil.z) * INV_PI_F : 0.0f;
+        pdf += same_hemisphere(Wol, Wil) ? blinn_pdf(sh->exponent, Wol, Wil) : 0.0f;
+        return pdf;
+    }
+    return INV_FOUR_PI_EXPANDED;
+}
+
+/* GlossinessExponent - Source/utilities.h:28-31 */
+static inline float glossiness_exponent(float g) { return 1000000.0f * er_powf(g, 7.0f); }
+
+/* PowerHeuristic(1, f, 1, g) - Source/montecarlo.h:223-227 */
+static inline float power_heuristic(float fPdf, float gPdf)
+{
+    const float f = 1 * fPdf, g = 1 * gPdf;
+    return (f * f) / (f * f + g * g);
+}
+
+/* ------------------------------------------------------------------ */
+/* scatter events and transport                                         */
+/* ------------------------------------------------------------------ */
+
+typedef struct {                          /* Source/scatterevent.h:31-151 */
+    int type;                             /* 0 volume, 1 light, 2 object */
+    int valid;
+    float T;
+    v3 P, N, Wo;
+    col3 Le;
+    v2 UV;
+    int light_id;
+} scatter_event;
+
+static inline void se_invalid(scatter_event* se, int type)
+{
+    se->type = type; se->valid = 0; se->T = 0.0f;
+    se->P = V3(0, 0, 0); se->N = V3(0, 0, 0); se->Wo = V3(0, 0, 0);
+    se->Le = C3(0, 0, 0); se->UV.x = 0.0f; se->UV.y = 0.0f; se->light_id = -1;
+}
+
+/* SampleVolume - Source/raymarching.h:30-71 */
+static void sample_volume(or_scene* s, ray_t R, rng_t* rng, scatter_event* SE)
+{
+    isect_t Int; isect_invalid(&Int);
+    intersect_box(&R, s->minp, vscale(s->size, 0.5f), &Int);
+    if (!Int.valid) return;
+    float MinT = smax(Int.near_t, R.MinT);
+    const float MaxT = smin(Int.far_t, R.MaxT);
+    const float S = -er_logf(rng_get1(rng)) / s->st.density_scale;
+    float Sum = 0.0f;
+    v3 Ps = V3(0, 0, 0);
+    const float StepSize = s->st.step_factor_primary * s->min_step;
+    MinT += rng_get1(rng) * StepSize;
+    while (Sum < S) {
+        Ps = vadd(R.O, vscale(R.D, MinT));
+        if (MinT >= MaxT) return;
+        const float I = get_intensity(s, Ps);
+        const float SigmaT = s->st.density_scale * plf_eval(&s->opacity, I);
+        Sum += SigmaT * StepSize;
+        MinT += StepSize;
+    }
+    SE->valid = 1;
+    SE->T = MinT;
+    SE->P = Ps;
+    SE->N = normalized_gradient(s, Ps);
+    SE->Wo = vneg(R.D);
+    SE->Le = C3(0, 0, 0);
+    SE->UV.x = 0.0f; SE->UV.y = 0.0f;
+}
+
+/* ScatterEventInVolume - Source/raymarching.h:73-113 */
+static int scatter_event_in_volume(or_scene* s, ray_t R, rng_t* rng)
+{
+    isect_t Int; isect_invalid(&Int);
+    intersect_box(&R, s->minp, vscale(s->size, 0.5f), &Int);
+    if (!Int.valid) return 0;
+    float MinT = smax(Int.near_t, R.MinT);
+    const float MaxT = smin(Int.far_t, R.MaxT);
+    const float S = -er_logf(rng_get1(rng)) / s->st.density_scale;
+    float Sum = 0.0f;
+    const float StepSize = s->st.step_factor_shadow * s->min_step;
+    MinT += rng_get1(rng) * StepSize;
+    while (Sum < S) {
+        const v3 Ps = vadd(R.O, vscale(R.D, MinT));
+        if (MinT > MaxT) return 0;
+        const float I = get_intensity(s, Ps);
+        const float SigmaT = s->st.density_scale * plf_eval(&s->opacity, I);
+        Sum += SigmaT * StepSize;
+        MinT += StepSize;
+    }
+    return 1;
+}
+
+/* IntersectLight - Source/lights.h:59-88 */
+static void intersect_light(const or_scene* s, const or_light* L, const ray_t* R, scatter_event* SE)
+{
+    const ray_t Rt = xform_ray(L->d.shape.inv_tm, R);
+    isect_t Int; isect_invalid(&Int);
+    intersect_shape(&L->d.shape, &Rt, &Int);
+    if (Int.valid) {
+        SE->valid = 1;
+        SE->P = xform_point(L->d.shape.tm, Int.P);
+        SE->N = xform_vector(L->d.shape.tm, Int.N);
+        SE->T = vlen(vsub(SE->P, R->O));
+        SE->Wo = vneg(R->D);
+        SE->UV = Int.UV;
+        SE->Le = Int.front ? cscale(evaluate_texture(s, L->d.texture_id, SE->UV), L->d.multiplier) : C3(0, 0, 0);
+        if (L->d.unit == 1) SE->Le = cdivs(SE->Le, L->area);
+    }
+}
+
+static inline const or_light* tracer_light(const or_scene* s, int i)
+{
+    const int id = s->light_idx[i];
+    if (id < 0 || id >= s->n_lights) return NULL;
+    return &s->lights[id];
+}
+
+/* IntersectLights - Source/lights.h:90-113 */
+static void intersect_lights(const or_scene* s, const ray_t* R, scatter_event* RS, int respect_visibility)
+{
+    float T = FLT_MAX;
+    for (int i = 0; i < s->light_count; i++) {
+        const or_light* L = tracer_light(s, i);
+        if (!L) continue;
+        scatter_event local; se_invalid(&local, 1);
+        local.light_id = i;
+        if (respect_visibility && !L->d.visible) continue;
+        intersect_light(s, L, R, &local);
+        if (local.valid && local.T < T) { *RS = local; T = local.T; }
+    }
+}
+
+/* IntersectsLight - Source/lights.h:115-131 */
+static int intersects_light(const or_scene* s, const ray_t* R)
+{
+    for (int i = 0; i < s->light_count; i++) {
+        const or_light* L = tracer_light(s, i);
+        if (!L) continue;
+        const ray_t Rt = xform_ray(L->d.shape.inv_tm, R);
+        isect_t Int; isect_invalid(&Int);
+        intersect_shape(&L->d.shape, &Rt, &Int);
+        if (Int.valid) return 1;
+    }
+    return 0;
+}
+
+/* Intersect / Visible - Source/transport.h:30-56 (no surface objects) */
+static int visible(or_scene* s, v3 P1, v3 P2, rng_t* rng)
+{
+    if (!s->st.shadows) return 1;
+    const v3 W = vnorm(vsub(P2, P1));
+    ray_t R;
+    R.O = vadd(P1, vscale(W, RAY_EPS));
+    R.D = W;
+    R.MinT = 0.0f;
+    R.MaxT = smin(vlen(vsub(P2, P1)) - 2.0f * RAY_EPS, s->st.max_shadow_distance);
+    if (intersects_light(s, &R)) return 0;
+    if (scatter_event_in_volume(s, R, rng)) return 0;
+    return 1;
+}
+
+/* SampleLight - Source/lights.h:44-57 */
+static void sample_light(const or_scene* s, const or_light* L, v3 uvw, surf_sample* SS, const scatter_event* SE,
+                         v3* Wi, col3* Le)
+{
+    sample_light_surface(L, uvw, SS);
+    *Wi = vnorm(vsub(SS->P, SE->P));
+    *Le = cscale(evaluate_texture(s, L->d.texture_id, SS->UV), L->d.multiplier);
+    if (L->d.shape.one_sided && vdot(vsub(SE->P, SS->P), SS->N) < 0.0f) *Le = C3(0, 0, 0);
+    if (L->d.unit == 1) *Le = cdivs(*Le, L->area);
+}
+
+/* EstimateDirectLight - Source/transport.h:58-84 (light-sampling half; the
+   function returns at :84) */
+static col3 estimate_direct_light(or_scene* s, const or_light* L, const metro_sample* ms, scatter_event* SE,
+                                  rng_t* rng, const shader_t* sh)
+{
+    v3 Wi;
+    col3 Li, Ld = C3(0, 0, 0);
+    surf_sample SS;
+    sample_light(s, L, ms->light_uvw, &SS, SE, &Wi, &Li);
+    const col3 F = shader_f(sh, SE->Wo, Wi);
+    const float BsdfPdf = shader_pdf(sh, SE->Wo, Wi);
+    if (!cblack(Li) && !cblack(F) && BsdfPdf > 0.0f && visible(s, SE->P, SS.P, rng)) {
+        const float LightPdf = vlen2(vsub(SE->P, SS.P)) / (vabsdot(SS.N, vneg(Wi)) * L->area);
+        const float Weight = power_heuristic(LightPdf, BsdfPdf);
+        if (sh->type == 0) Ld = cadd(Ld, cscale(cmul(F, Li), vabsdot(Wi, SE->N) * Weight / LightPdf));
+        else Ld = cadd(Ld, cdivs(cmul(F, Li), LightPdf));
+    }
+    return Ld;
+}
+
+/* UniformSampleOneLight - Source/transport.h:115-156 (volume events) */
+static col3 uniform_sample_one_light(or_scene* s, scatter_event* SE, rng_t* rng, const metro_sample* ms)
+{
+    col3 Ld = C3(0, 0, 0);
+    const float I = get_intensity(s, SE->P);
+    Ld = cadd(Ld, ctf_eval(&s->emission, I));
+    if (s->light_count <= 0) return Ld;
+    const int idx = (int)floorf(ms->light_num * (float)s->light_count);
+    const int light_id = s->light_idx[idx];
+    if (light_id < 0) return Ld;
+    if (light_id >= s->n_lights) return Ld;
+    const or_light* L = &s->lights[light_id];
+    shader_t sh;
+    const float vol_ior = s->st.volume_ior > 0.0f ? s->st.volume_ior : 15.0f;
+    shader_init(&sh, 0, SE->N, SE->Wo, ctf_eval(&s->diffuse, I), ctf_eval(&s->specular, I), vol_ior,
+                glossiness_exponent(plf_eval(&s->glossiness, I)));
+    Ld = cadd(Ld, estimate_direct_light(s, L, ms, SE, rng, &sh));
+    return cscale(Ld, (float)s->light_count);
+}
+
+/* SampleCamera - Source/singlescattering.h:29-50 */
+static ray_t sample_camera(const or_scene* s, int u, int v, v2 film_uv, v2 lens_uv)
+{
+    ray_t R;
+    const float sp0 = s->screen[0][0] + (s->inv_screen[0] * ((float)u + film_uv.x * 1.0f / (float)s->film[0]));
+    const float sp1 = s->screen[1][0] + (s->inv_screen[1] * ((float)v + film_uv.y * 1.0f / (float)s->film[1]));
+    R.O = s->pos;
+    R.D = vnorm(vsub(vadd(s->N, vscale(s->U, sp0)), vscale(s->V, sp1)));
+    R.MinT = s->clip_near;
+    R.MaxT = s->clip_far;
+    if (s->aperture != 0.0f) {
+        const v2 d = concentric_sample_disk(lens_uv);
+        const v2 lens = { d.x * s->aperture, d.y * s->aperture };
+        const v3 LI = vadd(vscale(s->U, lens.x), vscale(s->V, lens.y));
+        R.O = vadd(R.O, LI);
+        R.D = vnorm(vsub(vscale(R.D, s->focal_distance), LI));
+    }
+    return R;
+}
+
+/* SampleRay - Source/singlescattering.h:52-74 (no surface objects) */
+static void sample_ray(or_scene* s, ray_t R, rng_t* rng, scatter_event* nearest)
+{
+    scatter_event se[2];
+    se_invalid(&se[0], 0);
+    se_invalid(&se[1], 1);
+    sample_volume(s, R, rng, &se[0]);
+    intersect_lights(s, &R, &se[1], 1);
+    float T = FLT_MAX;
+    se_invalid(nearest, 0);
+    for (int i = 0; i < 2; i++) {
+        if (se[i].valid && se[i].T < T) { *nearest = se[i]; T = se[i].T; }
+    }
+}
+
+/* SingleScattering - Source/singlescattering.h:76-102 */
+static void single_scattering(or_scene* s, int x, int y, rng_t* rng, float out[4])
+{
+    col3 Lv = C3(0, 0, 0);
+    metro_sample ms;
+    metro_large_step(&ms, rng);
+    const ray_t R = sample_camera(s, x, y, ms.film_uv, ms.lens_uv);
+    scatter_event SE;
+    sample_ray(s, R, rng, &SE);
+    if (SE.valid && SE.type == 0) Lv = cadd(Lv, uniform_sample_one_light(s, &SE, rng, &ms));
+    if (SE.valid && SE.type == 1) Lv = cadd(Lv, SE.Le);
+    out[0] = Lv.c[0];
+    out[1] = Lv.c[1];
+    out[2] = Lv.c[2];
+    out[3] = SE.valid ? 1.0f : 0.0f;
+}
+
+/* ------------------------------------------------------------------ */
+/* threaded drivers                                                     */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    or_scene* scene;
+    or_scene local;
+    int mode;               /* 0 frame, 1 sum */
+    uint32_t* lanes;
+    float* out;
+    int spp;
+    uint32_t view, first;
+    int x0, y0, w, h;
+    int row0, row1;
+} job_t;
+
+static void* job_run(void* arg)
+{
+    job_t* j = (job_t*)arg;
+    or_scene* s = &j->local;
+    const int W = s->film[0], H = s->film[1];
+    for (int r = j->row0; r < j->row1; r++) {
+        if (j->mode == 0) {
+            for (int x = 0; x < W; x++) {
+                const size_t p = (size_t)r * (size_t)W + (size_t)x;
+                rng_t rng;
+                rng.s0 = j->lanes[p];
+                rng.s1 = j->lanes[(size_t)W * (size_t)H + p];
+                single_scattering(s, x, r, &rng, &j->out[4 * p]);
+                j->lanes[p] = rng.s0;
+                j->lanes[(size_t)W * (size_t)H + p] = rng.s1;
+                s->samples++;
+            }
+        } else {
+            const int y = j->y0 + r;
+            for (int xi = 0; xi < j->w; xi++) {
+                const int x = j->x0 + xi;
+                const uint32_t pix = (uint32_t)y * (uint32_t)W + (uint32_t)x;
+                float acc[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
+                for (int k = 0; k < j->spp; k++) {
+                    rng_t rng;
+                    er_seed_lanes(s->st.seed, j->view, pix, j->first + (uint32_t)k, &rng.s0, &rng.s1);
+                    float o[4];
+                    single_scattering(s, x, y, &rng, o);
+                    acc[0] += o[0]; acc[1] += o[1]; acc[2] += o[2]; acc[3] += o[3];
+                    s->samples++;
+                }
+                float* d = &j->out[4 * ((size_t)r * (size_t)j->w + (size_t)xi)];
+                d[0] = acc[0]; d[1] = acc[1]; d[2] = acc[2]; d[3] = acc[3];
+            }
+        }
+    }
+    return NULL;
+}
+
+static void run_jobs(or_scene* s, job_t* proto, int rows, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > rows) nthreads = rows > 0 ? rows : 1;
+    job_t* jobs = (job_t*)calloc((size_t)nthreads, sizeof(job_t));
+    pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+    for (int t = 0; t < nthreads; t++) {
+        jobs[t] = *proto;
+        jobs[t].local = *s;
+        jobs[t].local.lookups = 0;
+        jobs[t].local.samples = 0;
+        jobs[t].row0 = (int)((long long)rows * t / nthreads);
+        jobs[t].row1 = (int)((long long)rows * (t + 1) / nthreads);
+    }
+    for (int t = 1; t < nthreads; t++) pthread_create(&th[t], NULL, job_run, &jobs[t]);
+    job_run(&jobs[0]);
+    for (int t = 1; t < nthreads; t++) pthread_join(th[t], NULL);
+    uint64_t lk = 0, sm = 0;
+    for (int t = 0; t < nthreads; t++) { lk += jobs[t].local.lookups; sm += jobs[t].local.samples; }
+    g_lookups_per_sample = sm ? (double)lk / (double)sm : 0.0;
+    free(jobs);
+    free(th);
+}
+
+void ER_OR(render_frame)(or_scene* s, uint32_t* lanes, float* frame, int32_t nthreads)
+{
+    job_t proto;
+    memset(&proto, 0, sizeof(proto));
+    proto.scene = s; proto.mode = 0; proto.lanes = lanes; proto.out = frame;
+    run_jobs(s, &proto, s->film[1], nthreads);
+}
+
+void ER_OR(render_sum)(or_scene* s, int32_t spp, uint32_t view, uint32_t first_sample,
+                       int32_t x0, int32_t y0, int32_t w, int32_t h, float* sum, int32_t nthreads)
+{
+    job_t proto;
+    memset(&proto, 0, sizeof(proto));
+    proto.scene = s; proto.mode = 1; proto.out = sum; proto.spp = spp; proto.view = view; proto.first = first_sample;
+    proto.x0 = x0; proto.y0 = y0; proto.w = w; proto.h = h;
+    run_jobs(s, &proto, h, nthreads);
+}
+
+double ER_OR(lookups_per_sample)(void) { return g_lookups_per_sample; }
+
+/* ------------------------------------------------------------------ */
+/* post-processing                                                      */
+/* ------------------------------------------------------------------ */
+
+/* Gauss2D - Source/filterframeestimate.cuh:28-31 */
+static inline float gauss2d(float sigma, int X, int Y)
+{
+    return er_expf(-((float)(X * X + Y * Y) / (2 * sigma * sigma)));
+}
+
+/* ToneMap - Source/tonemap.cuh:30-47, alpha :58; FromXYZAf Source/color.h:155-164 */
+static inline void tonemap_px(const float* R, float exposure, uint8_t* o)
+{
+    float rgb[3];
+    rgb[0] = 3.240479f * R[0] - 1.537150f * R[1] - 0.498535f * R[2];
+    rgb[1] = -0.969256f * R[0] + 1.875991f * R[1] + 0.041556f * R[2];
+    rgb[2] = 0.055648f * R[0] - 0.204043f * R[1] + 1.057311f * R[2];
+    for (int i = 0; i < 3; i++) {
+        rgb[i] = 1.0f - er_expf(-(rgb[i] / exposure));
+        rgb[i] = smax(0.0f, smin(rgb[i], 1.0f));          /* ColorRGBf::Clamp, Source/vector.h:345-350 */
+        o[i] = (uint8_t)(255.0f * rgb[i]);
+    }
+    o[3] = (uint8_t)(R[3] * 255.0f);
+}
+
+void ER_OR(post_frame)(float* frame, float* running, uint8_t* rgba, int32_t W, int32_t H,
+                       int32_t no_iterations, float exposure)
+{
+    float* tmp = (float*)malloc(sizeof(float) * 4 * (size_t)W * (size_t)H);
+    /* KrnlFilterFrameEstimate(1, 1.0f) - Source/filterframeestimate.cuh:33-64 */
+    for (int IDy = 0; IDy < H; IDy++) {
+        for (int IDx = 0; IDx < W; IDx++) {
+            const int KernelRadius = 1;
+            const float Sigma = 1.0f;
+            const int x0 = (IDx - KernelRadius) > 0 ? (IDx - KernelRadius) : 0;
+            const int x1 = (IDx + KernelRadius) < (W - 1) ? (IDx + KernelRadius) : (W - 1);
+            const int y0 = (IDy - KernelRadius) > 0 ? (IDy - KernelRadius) : 0;
+            const int y1 = (IDy + KernelRadius) < (H - 1) ? (IDy + KernelRadius) : (H - 1);
+            float sum[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
+            float total = 0.0f;
+            for (int y = y0; y <= y1; y++) {
+                for (int x = x0; x <= x1; x++) {
+                    const float w = gauss2d(Sigma, x - IDx, y - IDy);
+                    const float* f = &frame[4 * ((size_t)y * W + x)];
+                    for (int k = 0; k < 4; k++) sum[k] += f[k] * w;
+                    total += w;
+                }
+            }
+            sum[3] = frame[4 * ((size_t)IDy * W + IDx) + 3];
+            float* d = &tmp[4 * ((size_t)IDy * W + IDx)];
+            for (int k = 0; k < 4; k++) d[k] = (total > 0.0f) ? sum[k] / total : 0.0f;
+        }
+    }
+    memcpy(frame, tmp, sizeof(float) * 4 * (size_t)W * (size_t)H);
+    free(tmp);
+    /* KrnlComputeEstimate - Source/estimate.cuh:27-32, CumulativeMovingAverage Source/utilities.h:59-62 */
+    const float div = smax((float)no_iterations, 1.0f);
+    for (size_t p = 0; p < (size_t)W * (size_t)H; p++) {
+        for (int k = 0; k < 4; k++) {
+            const float A = running[4 * p + k];
+            running[4 * p + k] = A + (frame[4 * p + k] - A) / div;
+        }
+    }
+    /* KrnlToneMap - Source/tonemap.cuh:49-59 */
+    for (size_t p = 0; p < (size_t)W * (size_t)H; p++) tonemap_px(&running[4 * p], exposure, &rgba[4 * p]);
+}
+
+/* ------------------------------------------------------------------ */
+/* known-answer helpers                                                 */
+/* ------------------------------------------------------------------ */
+
+void ER_OR(rng_draws)(uint32_t lane0, uint32_t lane1, int32_t n, float* out)
+{
+    rng_t r; r.s0 = lane0; r.s1 = lane1;
+    for (int i = 0; i < n; i++) out[i] = rng_get1(&r);
+}
+
+void ER_OR(rng_get2_get3)(uint32_t lane0, uint32_t lane1, float* out5)
+{
+    rng_t r; r.s0 = lane0; r.s1 = lane1;
+    const v2 a = rng_get2(&r);
+    const v3 b = rng_get3(&r);
+    out5[0] = a.x; out5[1] = a.y; out5[2] = b.x; out5[3] = b.y; out5[4] = b.z;
+}
+
+void ER_OR(plf_evaluate)(const er_plf* plf, int32_t n, const float* x, float* y)
+{
+    for (int i = 0; i < n; i++) y[i] = plf_eval(plf, x[i]);
+}
+
+void ER_OR(get_intensity)(or_scene* s, int32_t n, const float* p, float* out)
+{
+    for (int i = 0; i < n; i++) out[i] = get_intensity(s, V3(p[3 * i], p[3 * i + 1], p[3 * i + 2]));
+}
+
+void ER_OR(normalized_gradient)(or_scene* s, int32_t n, const float* p, float* out)
+{
+    for (int i = 0; i < n; i++) {
+        const v3 g = normalized_gradient(s, V3(p[3 * i], p[3 * i + 1], p[3 * i + 2]));
+        out[3 * i] = g.x; out[3 * i + 1] = g.y; out[3 * i + 2] = g.z;
+    }
+}
+
+void ER_OR(gradient_magnitude)(or_scene* s, int32_t n, const float* p, float* out)
+{
+    for (int i = 0; i < n; i++) out[i] = gradient_magnitude(s, V3(p[3 * i], p[3 * i + 1], p[3 * i + 2]));
+}
+
+void ER_OR(intersect_volume_box)(or_scene* s, int32_t n, const float* r8, float* out3)
+{
+    for (int i = 0; i < n; i++) {
+        ray_t R;
+        R.O = V3(r8[8 * i], r8[8 * i + 1], r8[8 * i + 2]);
+        R.D = V3(r8[8 * i + 3], r8[8 * i + 4], r8[8 * i + 5]);
+        R.MinT = r8[8 * i + 6]; R.MaxT = r8[8 * i + 7];
+        isect_t I; isect_invalid(&I);
+        intersect_box(&R, s->minp, vscale(s->size, 0.5f), &I);
+        out3[3 * i] = (float)I.valid; out3[3 * i + 1] = I.near_t; out3[3 * i + 2] = I.far_t;
+    }
+}
+
+void ER_OR(concentric_sample_disk)(int32_t n, const float* u2, float* out2)
+{
+    for (int i = 0; i < n; i++) {
+        v2 u; u.x = u2[2 * i]; u.y = u2[2 * i + 1];
+        const v2 d = concentric_sample_disk(u);
+        out2[2 * i] = d.x; out2[2 * i + 1] = d.y;
+    }
+}
+
+void ER_OR(tonemap)(int32_t n, const float* xyza, float exposure, uint8_t* rgba)
+{
+    for (int i = 0; i < n; i++) tonemap_px(&xyza[4 * i], exposure, &rgba[4 * i]);
+}
+
+void ER_OR(camera_ray)(or_scene* s, int32_t x, int32_t y, const float* uv4, float* out6)
+{
+    v2 f, l; f.x = uv4[0]; f.y = uv4[1]; l.x = uv4[2]; l.y = uv4[3];
+    const ray_t R = sample_camera(s, x, y, f, l);
+    out6[0] = R.O.x; out6[1] = R.O.y; out6[2] = R.O.z; out6[3] = R.D.x; out6[4] = R.D.y; out6[5] = R.D.z;
+}
+
+void ER_OR(camera_frame)(or_scene* s, float* o)
+{
+    o[0] = s->N.x; o[1] = s->N.y; o[2] = s->N.z;
+    o[3] = s->U.x; o[4] = s->U.y; o[5] = s->U.z;
+    o[6] = s->V.x; o[7] = s->V.y; o[8] = s->V.z;
+    o[9] = s->screen[0][0]; o[10] = s->screen[0][1]; o[11] = s->screen[1][0]; o[12] = s->screen[1][1];
+    o[13] = s->inv_screen[0]; o[14] = s->inv_screen[1];
+}
+
+void ER_OR(volume_frame)(or_scene* s, float* o)
+{
+    o[0] = s->minp.x; o[1] = s->minp.y; o[2] = s->minp.z;
+    o[3] = s->inv_size.x; o[4] = s->inv_size.y; o[5] = s->inv_size.z;
+    o[6] = s->min_step;
+    o[7] = s->spacing.x; o[8] = s->spacing.y; o[9] = s->spacing.z;
+    o[10] = s->size.x; o[11] = s->size.y; o[12] = s->size.z;
+}
+
+/* ------------------------------------------------------------------ */
+/* bilateral filter - design of Source/filterrunningestimate.cuh:35-200 */
+/* ------------------------------------------------------------------ */
+
+/* LUMINANCE weights (Source/color.h:37-51) applied to 0..255 channels;
+   LuminanceFromRGB is called but not defined by the reference. */
+static inline float lum255(const uint8_t* c)
+{
+    float L = 0.0f;
+    L += 0.212671f * (float)c[0];
+    L += 0.715160f * (float)c[1];
+    L += 0.072169f * (float)c[2];
+    return L;
+}
+
+static void bilateral_pass(const uint8_t* in, uint8_t* out, int W, int H, int r, const float* spatial, const float* range,
+                           int horizontal)
+{
+    for (int y = 0; y < H; y++) {
+        for (int x = 0; x < W; x++) {
+            const int i = horizontal ? x : y;
+            const int lim = horizontal ? W : H;
+            const int r0 = (i - r) > 0 ? (i - r) : 0;
+            const int r1 = (i + r) < (lim - 1) ? (i + r) : (lim - 1);
+            const uint8_t* ctr = &in[4 * ((size_t)y * W + x)];
+            const float lc = lum255(ctr);
+            float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, tot = 0.0f;
+            for (int k = r0; k < r1; k++) {   /* window end exclusive (:88, :157) */
+                const uint8_t* c = horizontal ? &in[4 * ((size_t)y * W + k)] : &in[4 * ((size_t)k * W + x)];
+                int d = (int)fabsf(lum255(c) - lc);
+                d = d > 255 ? 255 : d;
+                const float w = spatial[r + k - i] * range[d];
+                tot += w;
+                s0 += (float)c[0] * w; s1 += (float)c[1] * w; s2 += (float)c[2] * w;
+            }
+            uint8_t* o = &out[4 * ((size_t)y * W + x)];
+            if (tot > 0.0f) {
+                o[0] = (uint8_t)eclamp(s0 / tot, 0.0f, 255.0f);
+                o[1] = (uint8_t)eclamp(s1 / tot, 0.0f, 255.0f);
+                o[2] = (uint8_t)eclamp(s2 / tot, 0.0f, 255.0f);
+            } else {
+                o[0] = 0; o[1] = 0; o[2] = 0;
+            }
+            o[3] = 255;
+        }
+    }
+}
+
+/* KernelD[r + k] = exp(-k^2 / (2 sd^2)), GaussSimilarity[d] = exp(-d^2 / (2 sr^2)):
+   the tables of BilateralFilter (Source/filter.h:34-40), which the reference
+   declares but never fills */
+void ER_OR(bilateral)(const uint8_t* in, uint8_t* tmp, uint8_t* out, int32_t W, int32_t H, int32_t radius, float sigma_d,
+                      float sigma_r)
+{
+    float spatial[256], range[256];
+    const int r = radius < 0 ? 0 : (radius > 127 ? 127 : radius);
+    const float sd = sigma_d > 0.0f ? sigma_d : 1.0f;
+    const float sr = sigma_r > 0.0f ? sigma_r : 1.0f;
+    for (int k = -r; k <= r; k++) spatial[r + k] = er_expf(-((float)(k * k)) / (2.0f * sd * sd));
+    for (int d = 0; d < 256; d++) range[d] = er_expf(-((float)(d * d)) / (2.0f * sr * sr));
+    bilateral_pass(in, tmp, W, H, r, spatial, range, 1);
+    bilateral_pass(tmp, out, W, H, r, spatial, range, 0);
+}
+
+/* gradient magnitude at every voxel centre (Source/gradientmagnitude.cuh:38
+   with the current Volume fields) and its maximum */
+float ER_OR(gradient_magnitude_volume)(or_scene* s, uint16_t* gm)
+{
+    float mx = 0.0f;
+    for (int Z = 0; Z < s->res[2]; Z++)
+        for (int Y = 0; Y < s->res[1]; Y++)
+            for (int X = 0; X < s->res[0]; X++) {
+                const float sx = 2.0f * (s->size.x * 0.5f), sy = 2.0f * (s->size.y * 0.5f), sz = 2.0f * (s->size.z * 0.5f);
+                const v3 p = V3(s->minp.x + sx * (((float)X + 0.5f) * (1.0f / (float)s->res[0])),
+                                s->minp.y + sy * (((float)Y + 0.5f) * (1.0f / (float)s->res[1])),
+                                s->minp.z + sz * (((float)Z + 0.5f) * (1.0f / (float)s->res[2])));
+                const float g = gradient_magnitude(s, p);
+                if (gm) gm[(size_t)Z * s->res[0] * s->res[1] + (size_t)Y * s->res[0] + X] = (uint16_t)(g < 65535.0f ? g : 65535.0f);
+                mx = g > mx ? g : mx;
+            }
+    return mx;
+}
+
+/* er_math functions on the host: fn 0 log, 1 exp, 2 sin, 3 cos, 4 tan,
+   5 pow(x, y), 6 acos, 7 atan2(x, y) */
+void ER_OR(math_eval)(int32_t fn, int32_t n, const float* x, const float* y, float* out)
+{
+    for (int i = 0; i < n; i++) {
+        switch (fn) {
+        case 0: out[i] = er_logf(x[i]); break;
+        case 1: out[i] = er_expf(x[i]); break;
+        case 2: out[i] = er_sinf(x[i]); break;
+        case 3: out[i] = er_cosf(x[i]); break;
+        case 4: out[i] = er_tanf(x[i]); break;
+        case 5: out[i] = er_powf(x[i], y[i]); break;
+        case 6: out[i] = er_acosf(x[i]); break;
+        case 7: out[i] = er_atan2f(x[i], y[i]); break;
+        default: out[i] = 0.0f; break;
+        }
+    }
+}

@@ -1,0 +1,76 @@
+"""The C ABI library loads without a GPU and exports every entry point that
+include/er_capi.h declares; the ctypes mirrors have the C layout."""
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import pytest
+
+import oracle_lib as OL
+
+C = OL.C
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(C.LIB_PATH):
+        import __graft_entry__
+        __graft_entry__.build()
+    return ctypes.CDLL(C.LIB_PATH)
+
+
+def test_exports_every_declared_symbol(lib):
+    names = C.exported_symbols()
+    assert len(names) > 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_loader_declares_every_symbol():
+    lib = C.load_library()
+    for n in C.exported_symbols():
+        assert getattr(lib, n).argtypes is not None or n in ("er_abi_version", "er_last_error_message", "er_synchronize", "er_reset"), n
+
+
+def test_host_only_calls(lib):
+    L = C.load_library()
+    assert L.er_abi_version() == 1
+    s = C.er_render_settings()
+    L.er_default_render_settings(ctypes.byref(s))
+    ref = C.default_render_settings()
+    for f, _ in C.er_render_settings._fields_:
+        if f in ("reserved",):
+            continue
+        assert getattr(s, f) == getattr(ref, f), f
+    p = C.er_plf()
+    L.er_plf_init(ctypes.byref(p))
+    for i in range(130):
+        L.er_plf_add_node(ctypes.byref(p), float(i), float(i) * 0.5)
+    q = C.plf_init(C.er_plf())
+    for i in range(130):
+        C.plf_add_node(q, float(i), float(i) * 0.5)
+    assert p.count == 127 == q.count                      # Source/plf.h:53 cap
+    assert bytes(p) == bytes(q)
+
+
+def test_struct_layout_matches_c():
+    structs = ["er_plf", "er_color_tf", "er_shape", "er_light_desc", "er_procedural", "er_texture_desc", "er_volume_desc",
+               "er_bitmap_desc", "er_object_desc", "er_clipping_object_desc", "er_camera_desc", "er_render_settings",
+               "er_tracer_desc"]
+    src = '#include <stdio.h>\n#include <stddef.h>\n#include "er_capi.h"\nint main(void){\n'
+    for s in structs:
+        src += f'printf("{s} %zu\\n", sizeof({s}));\n'
+    src += 'printf("settings.seed %zu\\n", offsetof(er_render_settings, seed));\n'
+    src += 'printf("tracer.volume_id %zu\\n", offsetof(er_tracer_desc, volume_id));\nreturn 0;}\n'
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "s.c")
+        open(c, "w").write(src)
+        exe = os.path.join(d, "s")
+        subprocess.run(["gcc", "-I" + os.path.join(OL.ROOT, "include"), c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = dict(line.split() for line in out if line)
+    for s in structs:
+        assert int(got[s]) == ctypes.sizeof(getattr(C, s)), s
+    assert int(got["settings.seed"]) == C.er_render_settings.seed.offset
+    assert int(got["tracer.volume_id"]) == C.er_tracer_desc.volume_id.offset

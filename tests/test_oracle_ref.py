@@ -1,0 +1,128 @@
+"""The C restatement against the reference's own code built on this host
+(oracle/_ref/liberref.so), on fresh inputs.  Skipped where the reference
+sources were not available at build time."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle_lib as OL
+
+C = OL.C
+S = OL.PKG.scenes
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+@pytest.fixture(scope="module")
+def scenes(oracle, ref):
+    sc = S.scene_tiny(res=24, film=(36, 28), seed=11)
+    sc.tracer.camera.aperture_size = 0.05          # thin-lens path (Source/singlescattering.h:41-49)
+    yield sc, OL.SceneHandle(oracle, sc), OL.SceneHandle(ref, sc)
+
+
+def test_frames_bit_exact(scenes):
+    sc, a, b = scenes
+    la = OL.initial_lanes(9, sc.width, sc.height)
+    lb = la.copy()
+    for _ in range(2):
+        assert np.array_equal(bits(a.render_frame(la, 4)), bits(b.render_frame(lb, 4)))
+        assert np.array_equal(la, lb)
+
+
+@pytest.mark.parametrize("gradient_mode", [0, 1, 2])
+@pytest.mark.parametrize("shape", ["plane", "disk", "ring", "box", "sphere"])
+def test_light_shapes_and_gradients(oracle, ref, shape, gradient_mode):
+    sc = S.scene_tiny(res=20, film=(24, 20), seed=5)
+    L = sc.lights[0]
+    st = {"plane": C.SHAPE_PLANE, "disk": C.SHAPE_DISK, "ring": C.SHAPE_RING, "box": C.SHAPE_BOX, "sphere": C.SHAPE_SPHERE}[shape]
+    L.shape.type = st
+    L.shape.inner_radius, L.shape.outer_radius = 0.1, 0.3
+    L.shape.size[0], L.shape.size[1], L.shape.size[2] = 0.4, 0.3, 0.2
+    L.shape.one_sided = 1 if shape in ("plane", "disk") else 0
+    L.unit = C.UNIT_LUX if shape in ("disk", "box") else C.UNIT_POWER
+    sc.tracer.settings.gradient_computation = gradient_mode
+    a, b = OL.SceneHandle(oracle, sc), OL.SceneHandle(ref, sc)
+    assert np.array_equal(bits(a.render_sum(3, nthreads=4)), bits(b.render_sum(3, nthreads=4)))
+
+
+def test_environment_sphere_and_gradient_texture(oracle, ref):
+    sc = S.scene_tiny(res=20, film=(24, 20), seed=6)
+    tm = np.eye(4).tolist()
+    env = C.er_light_desc()
+    env.visible = 1
+    env.shape = S.make_shape(C.SHAPE_SPHERE, (tm, tm), outer=4.0)
+    env.texture_id = 1
+    env.multiplier = 0.7
+    sc.lights.append(env)
+    sc.textures.append(S.gradient_texture([(0.0, (0.2, 0.2, 0.3)), (0.5, (0.5, 0.5, 0.6)), (1.0, (1.0, 1.0, 1.0))]))
+    sc.tracer.light_count = 2
+    sc.tracer.light_ids[1] = 1
+    a, b = OL.SceneHandle(oracle, sc), OL.SceneHandle(ref, sc)
+    assert np.array_equal(bits(a.render_sum(4, nthreads=4)), bits(b.render_sum(4, nthreads=4)))
+
+
+def test_kats_against_reference(oracle, ref, scenes):
+    sc, a, b = scenes
+    rng = np.random.default_rng(3)
+    pts = rng.uniform(-0.6, 0.6, size=(500, 3)).astype(np.float32)
+    for name, width in (("get_intensity", 1), ("normalized_gradient", 3), ("gradient_magnitude", 1)):
+        oa = np.zeros((500, width), np.float32)
+        ob = np.zeros((500, width), np.float32)
+        getattr(oracle, name)(a.h, 500, OL.ptr(pts), OL.ptr(oa))
+        getattr(ref, name)(b.h, 500, OL.ptr(pts), OL.ptr(ob))
+        assert np.array_equal(bits(oa), bits(ob)), name
+    rays = np.concatenate([rng.uniform(-2, 2, (500, 3)), rng.normal(size=(500, 3)), np.zeros((500, 1)), np.full((500, 1), 10.0)], 1).astype(np.float32)
+    ia = np.zeros((500, 3), np.float32)
+    ib = np.zeros((500, 3), np.float32)
+    oracle.intersect_volume_box(a.h, 500, OL.ptr(rays), OL.ptr(ia))
+    ref.intersect_volume_box(b.h, 500, OL.ptr(rays), OL.ptr(ib))
+    assert np.array_equal(bits(ia), bits(ib))
+    u = rng.uniform(0, 1, (500, 2)).astype(np.float32)
+    u[0] = 0.5
+    da = np.zeros((500, 2), np.float32)
+    db = np.zeros((500, 2), np.float32)
+    oracle.concentric_sample_disk(500, OL.ptr(u), OL.ptr(da))
+    ref.concentric_sample_disk(500, OL.ptr(u), OL.ptr(db))
+    assert np.array_equal(bits(da), bits(db))
+    for x, y in ((0, 0), (17, 5), (35, 27)):
+        uv = rng.uniform(0, 1, 4).astype(np.float32)
+        ra = np.zeros(6, np.float32)
+        rb = np.zeros(6, np.float32)
+        oracle.camera_ray(a.h, x, y, OL.ptr(uv), OL.ptr(ra))
+        ref.camera_ray(b.h, x, y, OL.ptr(uv), OL.ptr(rb))
+        assert np.array_equal(bits(ra), bits(rb))
+
+
+def test_post_pipeline(oracle, ref):
+    rng = np.random.default_rng(4)
+    W, H = 19, 13
+    ra = np.zeros((H, W, 4), np.float32)
+    rb = ra.copy()
+    for n in range(4):
+        f = rng.uniform(0, 2, (H, W, 4)).astype(np.float32)
+        f[..., 3] = (rng.uniform(0, 1, (H, W)) > 0.4).astype(np.float32)
+        fa, fb = f.copy(), f.copy()
+        ga = np.zeros((H, W, 4), np.uint8)
+        gb = ga.copy()
+        oracle.post_frame(OL.ptr(fa), OL.ptr(ra), OL.ptr(ga), W, H, n, 1.3)
+        ref.post_frame(OL.ptr(fb), OL.ptr(rb), OL.ptr(gb), W, H, n, 1.3)
+        assert np.array_equal(bits(fa), bits(fb))
+        assert np.array_equal(bits(ra), bits(rb))
+        assert np.array_equal(ga, gb)
+
+
+def test_plf_random_unsorted(oracle, ref):
+    rng = np.random.default_rng(8)
+    for trial in range(20):
+        n = int(rng.integers(0, 130))
+        plf = C.make_plf([(float(p), float(v)) for p, v in zip(rng.uniform(-100, 5000, n), rng.uniform(0, 1, n))])
+        xs = np.concatenate([rng.uniform(-200, 5200, 200), np.array([plf.position[i] for i in range(plf.count)])]).astype(np.float32)
+        ya = np.zeros_like(xs)
+        yb = np.zeros_like(xs)
+        oracle.plf_evaluate(ctypes.byref(plf), len(xs), OL.ptr(xs), OL.ptr(ya))
+        ref.plf_evaluate(ctypes.byref(plf), len(xs), OL.ptr(xs), OL.ptr(yb))
+        assert np.array_equal(bits(ya), bits(yb))
+        assert plf.count <= 127
