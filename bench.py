@@ -56,14 +56,14 @@ def make_scene(wl):
     return S.scene_c1(res=128, film=WORKLOADS[wl]["film"], spp=WORKLOADS[wl]["spp"])
 
 
-def reference_shading(scene):
-    """Settings the current kernels implement for every workload: the live
-    reference shading (BRDF volume shader, light-sampling estimator)."""
+def describe_shading(scene):
     s = scene.tracer.settings
-    s.apply_shading_type = 0
-    s.mis = 0
-    s.free_flight = 0
-    return "brdf-light-sampling (reference live path)"
+    shading = {0: "brdf", 1: "phase", 2: "hybrid", 3: "modulation", 4: "threshold"}.get(s.shading_type, "?")
+    if not s.apply_shading_type:
+        shading = "brdf (reference live path)"
+    return {"shading": shading, "mis": "full" if s.mis else "light-sampling",
+            "free_flight": "delta+ratio tracking, %d^3 majorant bricks" % (s.majorant_brick or 8) if s.free_flight else "fixed-step march",
+            "bilateral": bool(s.bilateral)}
 
 
 class ClockSampler:
@@ -181,7 +181,8 @@ def run_reference(args, wl, rank, world):
     if rank != 0:
         return
     scene = make_scene(wl)
-    shading = reference_shading(scene)
+    scene.tracer.settings.free_flight = 0
+    shading = describe_shading(scene)
     W = WORKLOADS[wl]
     for _ in range(args.warmup):
         cpu_reference_rate(scene, seconds_target=2.0, steps=1)
@@ -190,7 +191,7 @@ def run_reference(args, wl, rank, world):
         "impl": "reference", "metric": "Msamples/s", "value": rate / 1e6, "unit": "Msamples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": W["name"], "film": list(W["film"]), "spp": W["spp"], "shading": shading},
+        "config": {"workload": W["name"], "film": list(W["film"]), "spp": W["spp"], **shading},
         "cpu_baseline": {"value": rate / 1e6, "unit": "Msamples/s", "cores": cores, "kind": kind, "sample": sample},
         "e2e": {"value": rate / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -207,7 +208,8 @@ def run_ours(args, wl, rank, world, local_rank):
     C.check(lib.er_set_device(local_rank))
     W = WORKLOADS[wl]
     scene = make_scene(wl)
-    shading = reference_shading(scene)
+    scene.tracer.settings.free_flight = 1                # the fast path: delta tracking
+    shading = describe_shading(scene)
     scene.tracer.settings.seed = 1 + rank                # one replica view per rank
     r = runtime.Renderer(scene, lib)
     spp = W["spp"]
@@ -244,6 +246,28 @@ def run_ours(args, wl, rank, world, local_rank):
     samples_per_step = width * height * spp
     value = world * samples_per_step * args.steps / (ms / 1e3) / 1e6
 
+    # the plain single-view path on the same workload and shading: the
+    # reference's fixed-step march (one warm-up, one timed step)
+    def timed_plain(settings_patch):
+        saved = {k: getattr(r.tracer_desc.settings, k) for k in settings_patch}
+        for k, v in settings_patch.items():
+            setattr(r.tracer_desc.settings, k, v)
+        r.rebind_tracer()
+        step(0)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step(1)
+        b.record(stream)
+        torch.cuda.synchronize()
+        for k, v in saved.items():
+            setattr(r.tracer_desc.settings, k, v)
+        r.rebind_tracer()
+        return samples_per_step / (a.elapsed_time(b) / 1e3) / 1e6
+
+    plain = timed_plain({"free_flight": 0})
+    ref_order = timed_plain({"free_flight": 0, "mis": 0, "apply_shading_type": 0, "bilateral": 0})
+
     # end to end through the C ABI with host buffers
     vd = scene.volume_desc()
     vol_bytes = scene.volume.nbytes
@@ -279,6 +303,8 @@ def run_ours(args, wl, rank, world, local_rank):
         return
     peaks, peak_kind = measured_peaks()
     nthreads = os.cpu_count() or 1
+    # algorithmic bytes are defined by the reference estimator (fixed-step march)
+    scene.tracer.settings.free_flight = 0
     L = lookups_per_sample(scene, nthreads)
     bytes_per_sample = BYTES_PER_LOOKUP * L + BYTES_PER_SAMPLE_FIXED
     achieved = bytes_per_sample * samples_per_step * args.steps / (ms / 1e3) / 1e9
@@ -296,8 +322,8 @@ def run_ours(args, wl, rank, world, local_rank):
         "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": W["name"], "film": list(W["film"]), "spp": W["spp"], "shading": shading,
-                   "free_flight": "fixed-step march (reference)", "kernel": "k_trace_sum (reference-order, bit-exact)",
+        "config": {"workload": W["name"], "film": list(W["film"]), "spp": W["spp"], **shading,
+                   "kernel": "k_trace_sum",
                    "l2": "inputs larger than L2 (volume %d MiB)" % (vol_bytes >> 20) if vol_bytes > (129 << 20) else
                    "volume fits in L2 (%d MiB); transport re-reads it from L2" % (vol_bytes >> 20),
                    "parallelism": "replicas" if world > 1 else "single"},
@@ -308,6 +334,10 @@ def run_ours(args, wl, rank, world, local_rank):
                 "d2h_bytes_per_step": int(out.nbytes)},
         "clocks": clk.summary(),
         "gpu_launches": args.steps,
+        "plain": {"value": plain, "unit": "Msamples/s", "speedup": value / plain,
+                  "what": "same workload and shading, fixed-step march (reference free flight)"},
+        "reference_order": {"value": ref_order, "unit": "Msamples/s",
+                            "what": "reference live path (march, BRDF, light sampling), bit-exact with the reference"},
     }
     print(json.dumps(line), flush=True)
     r.close()

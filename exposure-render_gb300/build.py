@@ -30,6 +30,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
 UNITS = {
     "er_render.cu": ["--fmad=false", "-Xptxas", "-v"],
     "er_post.cu": ["--fmad=false"],
+    "er_volume.cu": ["--fmad=false"],
     "er_runtime.cu": [],
 }
 

@@ -166,7 +166,8 @@ class er_render_settings(Structure):
         ("bilateral_sigma_d", c_float),
         ("bilateral_sigma_r", c_float),
         ("seed", c_uint32),
-        ("reserved", c_int32 * 6),
+        ("majorant_brick", c_int32),
+        ("reserved", c_int32 * 5),
     ]
 
 
@@ -268,6 +269,7 @@ def default_render_settings() -> er_render_settings:
     s.bilateral_sigma_d = 1.5
     s.bilateral_sigma_r = 20.0
     s.seed = 1
+    s.majorant_brick = 8
     return s
 
 

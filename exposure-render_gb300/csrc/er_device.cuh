@@ -88,6 +88,11 @@ struct Params {
     float min_step;
     const float* sigma;      /* DensityScale * Opacity(I), I in [0, sigma_n) */
     int sigma_n;
+    /* delta tracking: majorant per brick of `brick`^3 voxels */
+    int free_flight;
+    int brick;
+    int nb[3];
+    const float* majorant;
     float gm_inv_max;        /* 1 / max gradient magnitude (hybrid switch) */
     /* camera (Source/camera.h:98-116) */
     int film[2];
@@ -109,6 +114,7 @@ struct Params {
     int light_count;
     const Light* lights;     /* light_count entries, in LightIDs order; NULL entries are skipped */
     const int* light_valid;  /* 1 where LightIDs[i] named a bound light */
+    const int* light_ids;    /* the tracer's LightIDs (slot -> light ID) */
     const Texture* textures;
     int n_textures;
     const Tfs* tfs;

@@ -32,5 +32,7 @@ cudaError_t er_launch_bilateral(const uchar4* in, uchar4* tmp, uchar4* out, int 
                                 cudaStream_t s);
 cudaError_t er_launch_gradient_magnitude(const erd::Params& P, uint16_t* gm, unsigned int* max_bits, cudaStream_t s);
 cudaError_t er_launch_math_eval(int fn, int n, const float* x, const float* y, float* out, cudaStream_t s);
+cudaError_t er_launch_majorant(const uint16_t* vox, const int res[3], int B, const int nb[3], const float* sigma, int n,
+                               float* rmq, int levels, uint32_t* minmax, float density_scale, float* majorant, cudaStream_t s);
 
 #endif

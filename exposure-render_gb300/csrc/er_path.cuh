@@ -616,8 +616,9 @@ ER_D void intersect_light(const Params& P, const Light& L, const Ray& R, Event& 
     }
 }
 
-/* IntersectLights - Source/lights.h:90-113 */
-ER_D void intersect_lights(const Params& P, const Ray& R, Event& RS, bool respect_visibility)
+/* IntersectLights - Source/lights.h:90-113; `slot` receives the LightIDs
+   index of the nearest hit (ScatterEvent::LightID) */
+ER_D void intersect_lights_slot(const Params& P, const Ray& R, Event& RS, bool respect_visibility, int& slot)
 {
     float T = FLT_MAX;
     for (int i = 0; i < P.light_count; i++) {
@@ -628,8 +629,14 @@ ER_D void intersect_lights(const Params& P, const Ray& R, Event& RS, bool respec
         local.type = 1; local.valid = false; local.T = 0.0f;
         local.P = V3(0, 0, 0); local.N = V3(0, 0, 0); local.Wo = V3(0, 0, 0); local.Le = C3(0, 0, 0);
         intersect_light(P, L, R, local);
-        if (local.valid && local.T < T) { RS = local; T = local.T; }
+        if (local.valid && local.T < T) { RS = local; T = local.T; slot = i; }
     }
+}
+
+ER_D void intersect_lights(const Params& P, const Ray& R, Event& RS, bool respect_visibility)
+{
+    int slot = -1;
+    intersect_lights_slot(P, R, RS, respect_visibility, slot);
 }
 
 /* IntersectsLight - Source/lights.h:115-131 */
@@ -646,20 +653,198 @@ ER_D bool intersects_light(const Params& P, const Ray& R)
     return false;
 }
 
-/* Visible / Intersect - Source/transport.h:30-56 */
-ER_D bool visible(const Params& P, v3 P1, v3 P2, Rng& rng)
+/* ---- extension estimators (delta tracking, shader selection, full MIS) ---- */
+
+/* 3D DDA over the majorant bricks in local voxel units */
+struct Dda {
+    float t, tmax;
+    int b[3], step[3];
+    float tnext[3], tdelta[3];
+    bool done;
+};
+
+ER_D void dda_init(const Params& P, const Ray& R, float t0, float t1, Dda& d)
 {
-    if (!P.shadows) return true;
+    const float B = (float)P.brick;
+    d.t = t0;
+    d.tmax = t1;
+    d.done = false;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const float sc = P.inv_size[i] * (float)P.res[i];
+        const float lo = (vget(R.O, i) - P.minp[i]) * sc;
+        const float ld = vget(R.D, i) * sc;
+        const float L = lo + t0 * ld;
+        int b = (int)floorf(L / B);
+        b = b < 0 ? 0 : (b >= P.nb[i] ? P.nb[i] - 1 : b);
+        d.b[i] = b;
+        if (ld > 0.0f) { d.step[i] = 1; d.tnext[i] = ((float)(b + 1) * B - lo) / ld; d.tdelta[i] = B / ld; }
+        else if (ld < 0.0f) { d.step[i] = -1; d.tnext[i] = ((float)b * B - lo) / ld; d.tdelta[i] = -B / ld; }
+        else { d.step[i] = 0; d.tnext[i] = FLT_MAX; d.tdelta[i] = FLT_MAX; }
+    }
+}
+
+ER_D float dda_exit(const Dda& d)
+{
+    float e = d.tnext[0];
+    if (d.tnext[1] < e) e = d.tnext[1];
+    if (d.tnext[2] < e) e = d.tnext[2];
+    if (d.tmax < e) e = d.tmax;
+    return e < d.t ? d.t : e;
+}
+
+ER_D void dda_advance(const Params& P, Dda& d, float e)
+{
+    if (e >= d.tmax) { d.done = true; d.t = e; return; }
+    int a = 0;
+    if (d.tnext[1] < d.tnext[a]) a = 1;
+    if (d.tnext[2] < d.tnext[a]) a = 2;
+    d.b[a] += d.step[a];
+    if (d.b[a] < 0 || d.b[a] >= P.nb[a]) d.done = true;
+    d.tnext[a] += d.tdelta[a];
+    d.t = e;
+}
+
+ER_D float dda_majorant(const Params& P, const Dda& d)
+{
+    return __ldg(P.majorant + ((size_t)d.b[2] * (size_t)P.nb[1] + (size_t)d.b[1]) * (size_t)P.nb[0] + (size_t)d.b[0]);
+}
+
+#define ER_DELTA_MAX_COLLISIONS 1048576
+
+/* Delta tracking of the primary ray: sigma_t = DensityScale^2 * Opacity(I),
+   the extinction the reference's march integrates (Source/raymarching.h:45,64-66) */
+ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE)
+{
+    Isect Int; Int.invalid();
+    intersect_box(R, vload(P.minp), vload(P.half_size), Int, false);
+    if (!Int.valid) return;
+    const float t0 = smax(Int.near_t, R.MinT);
+    const float t1 = smin(Int.far_t, R.MaxT);
+    if (!(t0 < t1)) return;
+    Dda d;
+    dda_init(P, R, t0, t1, d);
+    float tau = -er_logf(rng.get1());
+    int guard = 0;
+    while (!d.done) {
+        const float e = dda_exit(d);
+        const float mu = dda_majorant(P, d);
+        float t = d.t;
+        if (mu > 0.0f) {
+            for (;;) {
+                const float dt = tau / mu;
+                if (!(t + dt < e)) {
+                    tau = tau - mu * (e - t);
+                    if (tau < 0.0f) tau = 0.0f;
+                    break;
+                }
+                t = t + dt;
+                const v3 Pt = vadd(R.O, vscale(R.D, t));
+                const float sig = P.density_scale * sigma_at(P, get_intensity(P, Pt));
+                if (rng.get1() * mu < sig) {
+                    SE.valid = true;
+                    SE.T = t;
+                    SE.P = Pt;
+                    SE.N = normalized_gradient(P, Pt);
+                    SE.Wo = vneg(R.D);
+                    SE.Le = C3(0, 0, 0);
+                    return;
+                }
+                if (++guard > ER_DELTA_MAX_COLLISIONS) { atomicOr(P.err, 2); return; }
+                tau = -er_logf(rng.get1());
+            }
+        }
+        dda_advance(P, d, e);
+    }
+}
+
+/* Ratio tracking of a shadow segment with Russian roulette below 0.1 */
+ER_D float transmittance_ratio(const Params& P, const Ray& R, Rng& rng)
+{
+    Isect Int; Int.invalid();
+    intersect_box(R, vload(P.minp), vload(P.half_size), Int, false);
+    if (!Int.valid) return 1.0f;
+    const float t0 = smax(Int.near_t, R.MinT);
+    const float t1 = smin(Int.far_t, R.MaxT);
+    if (!(t0 < t1)) return 1.0f;
+    Dda d;
+    dda_init(P, R, t0, t1, d);
+    float Tr = 1.0f;
+    float tau = -er_logf(rng.get1());
+    int guard = 0;
+    while (!d.done) {
+        const float e = dda_exit(d);
+        const float mu = dda_majorant(P, d);
+        float t = d.t;
+        if (mu > 0.0f) {
+            for (;;) {
+                const float dt = tau / mu;
+                if (!(t + dt < e)) {
+                    tau = tau - mu * (e - t);
+                    if (tau < 0.0f) tau = 0.0f;
+                    break;
+                }
+                t = t + dt;
+                const v3 Pt = vadd(R.O, vscale(R.D, t));
+                const float sig = P.density_scale * sigma_at(P, get_intensity(P, Pt));
+                Tr = Tr * (1.0f - sig / mu);
+                if (Tr <= 0.0f) return 0.0f;
+                if (Tr < 0.1f) {
+                    if (rng.get1() >= 0.5f) return 0.0f;
+                    Tr = Tr * 2.0f;
+                }
+                if (++guard > ER_DELTA_MAX_COLLISIONS) { atomicOr(P.err, 2); return Tr; }
+                tau = -er_logf(rng.get1());
+            }
+        }
+        dda_advance(P, d, e);
+    }
+    return Tr;
+}
+
+/* Visible / Intersect - Source/transport.h:30-56: 1/0 for the reference
+   march, the ratio-tracked transmittance with delta tracking */
+ER_D float visibility(const Params& P, v3 P1, v3 P2, Rng& rng)
+{
+    if (!P.shadows) return 1.0f;
     const v3 W = vnorm(vsub(P2, P1));
     Ray R;
     R.O = vadd(P1, vscale(W, ER_RAY_EPS));
     R.D = W;
     R.MinT = 0.0f;
     R.MaxT = smin(vlen(vsub(P2, P1)) - 2.0f * ER_RAY_EPS, P.max_shadow_distance);
-    if (intersects_light(P, R)) return false;
-    if (scatter_event_in_volume(P, R, rng)) return false;
-    return true;
+    if (intersects_light(P, R)) return 0.0f;
+    if (P.free_flight == 1) return transmittance_ratio(P, R, rng);
+    return scatter_event_in_volume(P, R, rng) ? 0.0f : 1.0f;
 }
+
+/* shader selection of the design Source/scatterevent.h:155-212 (0 BRDF, 1 phase) */
+ER_D int select_shader_type(const Params& P, const Event& SE, float I, Rng& rng)
+{
+    switch (P.shading_type) {
+    case 0: return 0;
+    case 1: return 1;
+    case 2: {
+        const float NGM = gradient_magnitude(P, SE.P) * P.gm_inv_max;
+        const float Exponent = 25.0f * er_powf(P.gradient_factor, 3.0f) * NGM;
+        const float PdfBrdf = P.opacity_modulated ? plf_eval(P.tfs->opacity, I) * (1.0f - er_expf(-Exponent))
+                                                  : 1.0f - er_expf(-Exponent);
+        return rng.get1() <= PdfBrdf ? 0 : 1;
+    }
+    case 3: {
+        const float NGM = gradient_magnitude(P, SE.P) * P.gm_inv_max;
+        const float PdfBrdf = 1.0f - er_powf(1.0f - NGM, 2.0f);
+        return rng.get1() < PdfBrdf ? 0 : 1;
+    }
+    case 4: {
+        const float NGM = gradient_magnitude(P, SE.P) * P.gm_inv_max;
+        return NGM > P.gradient_threshold ? 0 : 1;
+    }
+    default: return 1;
+    }
+}
+
+#define ER_INV_FOUR_PI_TRUE 0.0795774715f
 
 /* SampleLight - Source/lights.h:44-57 */
 ER_D void sample_light(const Params& P, const Light& L, v3 uvw, Surf& SS, const Event& SE, v3& Wi, c3& Le)
@@ -689,20 +874,114 @@ struct Metro {               /* MetroSample::LargeStep - Source/sample.h:258-262
     }
 };
 
-/* EstimateDirectLight - Source/transport.h:58-84 */
-ER_D c3 estimate_direct_light(const Params& P, const Light& L, const Metro& ms, const Event& SE, Rng& rng, const Shader& sh)
+/* mixture pdf of the full-MIS BSDF sampler (Lambertian and Blinn lobes with
+   probability 1/2 each, Source/shader.h:364-371; uniform sphere for the phase
+   function, :293-299) */
+ER_D float mis_bsdf_pdf(const Shader& sh, v3 Wo, v3 Wi)
+{
+    if (sh.type == 0) {
+        const v3 Wol = world_to_local(sh, Wo), Wil = world_to_local(sh, Wi);
+        const float pl = same_hemisphere(Wol, Wil) ? fabsf(Wil.z) * ER_INV_PI_F : 0.0f;
+        const float pm = same_hemisphere(Wol, Wil) ? blinn_pdf(sh.exponent, Wol, Wil) : 0.0f;
+        return 0.5f * (pl + pm);
+    }
+    return ER_INV_FOUR_PI_TRUE;
+}
+
+/* Lambertian::SampleF / Blinn::SampleF / IsotropicPhase::SampleF
+   (Source/shader.h:46-56, :142-164, :293-299) */
+ER_D v3 sample_bsdf_dir(const Shader& sh, v3 Wo, const Metro& ms)
+{
+    if (sh.type == 0) {
+        const v3 Wol = world_to_local(sh, Wo);
+        v3 Wil;
+        if (ms.brdf_component <= 0.5f) {
+            const v2 d = concentric_sample_disk(ms.brdf_dir);
+            Wil = V3(d.x, d.y, sqrtf(smax(0.f, 1.f - d.x * d.x - d.y * d.y)));
+            if (Wol.z < 0.0f) Wil.z *= -1.0f;
+        } else {
+            const float e = sh.exponent;
+            const float costheta = er_powf(ms.brdf_dir.x, 1.f / (e + 1));
+            const float sintheta = sqrtf(smax(0.f, 1.f - costheta * costheta));
+            const float phi = ms.brdf_dir.y * 2.f * ER_PI_F;
+            float sn, cs;
+            er_sincosf(phi, &sn, &cs);
+            v3 wh = V3(sintheta * cs, sintheta * sn, costheta);
+            if (!same_hemisphere(Wol, wh)) wh = vneg(wh);
+            Wil = vadd(vneg(Wol), vscale(wh, 2.f * vdot(Wol, wh)));
+        }
+        return local_to_world(sh, Wil);
+    }
+    const float z = 1.f - 2.f * ms.brdf_dir.x;
+    const float r = sqrtf(smax(0.f, 1.f - z * z));
+    const float phi = 2.f * ER_PI_F * ms.brdf_dir.y;
+    float sn, cs;
+    er_sincosf(phi, &sn, &cs);
+    return V3(r * cs, r * sn, z);
+}
+
+/* EstimateDirectLight - Source/transport.h:58-113: the live light-sampling
+   half (mis 0, march), or both halves with power-heuristic weights (mis 1),
+   with the ratio-tracked transmittance under delta tracking */
+ER_D c3 estimate_direct_light(const Params& P, const Light& L, int slot, const Metro& ms, const Event& SE, Rng& rng,
+                              const Shader& sh)
 {
     v3 Wi;
     c3 Li, Ld = C3(0, 0, 0);
     Surf SS;
     sample_light(P, L, ms.light_uvw, SS, SE, Wi, Li);
     const c3 F = shader_f(sh, SE.Wo, Wi);
-    const float BsdfPdf = shader_pdf(sh, SE.Wo, Wi);
-    if (!cblack(Li) && !cblack(F) && BsdfPdf > 0.0f && visible(P, SE.P, SS.P, rng)) {
-        const float LightPdf = vlen2(vsub(SE.P, SS.P)) / (vabsdot(SS.N, vneg(Wi)) * L.area);
-        const float Weight = power_heuristic(LightPdf, BsdfPdf);
-        if (sh.type == 0) Ld = cadd(Ld, cscale(cmul(F, Li), vabsdot(Wi, SE.N) * Weight / LightPdf));
-        else Ld = cadd(Ld, cdivs(cmul(F, Li), LightPdf));
+    const bool full = P.mis == 1;
+    const bool delta = P.free_flight == 1;
+    const float BsdfPdf = full ? mis_bsdf_pdf(sh, SE.Wo, Wi) : shader_pdf(sh, SE.Wo, Wi);
+    if (!full && !delta) {
+        if (!cblack(Li) && !cblack(F) && BsdfPdf > 0.0f && visibility(P, SE.P, SS.P, rng) > 0.0f) {
+            const float LightPdf = vlen2(vsub(SE.P, SS.P)) / (vabsdot(SS.N, vneg(Wi)) * L.area);
+            const float Weight = power_heuristic(LightPdf, BsdfPdf);
+            if (sh.type == 0) Ld = cadd(Ld, cscale(cmul(F, Li), vabsdot(Wi, SE.N) * Weight / LightPdf));
+            else Ld = cadd(Ld, cdivs(cmul(F, Li), LightPdf));
+        }
+        return Ld;
+    }
+    if (!cblack(Li) && !cblack(F) && BsdfPdf > 0.0f) {
+        const float Tr = visibility(P, SE.P, SS.P, rng);
+        if (Tr > 0.0f) {
+            const float LightPdf = vlen2(vsub(SE.P, SS.P)) / (vabsdot(SS.N, vneg(Wi)) * L.area);
+            c3 c;
+            if (full) {
+                const float w = power_heuristic(LightPdf, BsdfPdf);
+                c = cscale(cmul(F, Li), sh.type == 0 ? vabsdot(Wi, SE.N) * w / LightPdf : w / LightPdf);
+            } else if (sh.type == 0) {
+                c = cscale(cmul(F, Li), vabsdot(Wi, SE.N) * power_heuristic(LightPdf, BsdfPdf) / LightPdf);
+            } else {
+                c = cdivs(cmul(F, Li), LightPdf);
+            }
+            Ld = cadd(Ld, cscale(c, Tr));
+        }
+    }
+    if (!full) return Ld;
+    const v3 Wb = sample_bsdf_dir(sh, SE.Wo, ms);
+    const c3 Fb = shader_f(sh, SE.Wo, Wb);
+    const float pb = mis_bsdf_pdf(sh, SE.Wo, Wb);
+    if (cblack(Fb) || !(pb > 0.0f)) return Ld;
+    Ray R2;
+    R2.O = SE.P;
+    R2.D = Wb;
+    R2.MinT = 0.0f;
+    R2.MaxT = 1000000.0f;
+    Event SE2;
+    SE2.type = 1; SE2.valid = false; SE2.T = 0.0f; SE2.Le = C3(0, 0, 0);
+    SE2.P = V3(0, 0, 0); SE2.N = V3(0, 0, 0); SE2.Wo = V3(0, 0, 0);
+    int hit = -1;
+    intersect_lights_slot(P, R2, SE2, false, hit);
+    if (!SE2.valid || P.light_ids[hit] != P.light_ids[slot]) return Ld;
+    if (cblack(SE2.Le)) return Ld;
+    const float Tr = visibility(P, SE.P, SE2.P, rng);
+    if (Tr > 0.0f) {
+        const float LightPdf = vlen2(vsub(SE.P, SE2.P)) / (vabsdot(SE2.N, vneg(Wb)) * L.area);
+        const float w = power_heuristic(pb, LightPdf);
+        const c3 c = cscale(cmul(Fb, SE2.Le), sh.type == 0 ? vabsdot(Wb, SE.N) * w / pb : w / pb);
+        Ld = cadd(Ld, cscale(c, Tr));
     }
     return Ld;
 }
@@ -718,9 +997,10 @@ ER_D c3 uniform_sample_one_light(const Params& P, const Event& SE, Rng& rng, con
     if (idx < 0 || idx >= P.light_count || !P.light_valid[idx]) return Ld;
     const Light& L = P.lights[idx];
     Shader sh;
-    shader_init(sh, 0, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
+    const int type = P.apply_shading_type ? select_shader_type(P, SE, I, rng) : 0;
+    shader_init(sh, type, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
                 1000000.0f * er_powf(plf_eval(P.tfs->glossiness, I), 7.0f));
-    Ld = cadd(Ld, estimate_direct_light(P, L, ms, SE, rng, sh));
+    Ld = cadd(Ld, estimate_direct_light(P, L, idx, ms, SE, rng, sh));
     return cscale(Ld, (float)P.light_count);
 }
 
@@ -755,7 +1035,8 @@ ER_D float4 single_scattering(const Params& P, int x, int y, Rng& rng)
     se0.type = 0; se0.valid = false; se0.T = 0.0f; se0.Le = C3(0, 0, 0);
     se0.P = V3(0, 0, 0); se0.N = V3(0, 0, 0); se0.Wo = V3(0, 0, 0);
     se1 = se0; se1.type = 1;
-    sample_volume(P, R, rng, se0);
+    if (P.free_flight == 1) sample_volume_delta(P, R, rng, se0);
+    else sample_volume(P, R, rng, se0);
     intersect_lights(P, R, se1, true);
     SE = se0; SE.valid = false; SE.type = 0;
     float T = FLT_MAX;

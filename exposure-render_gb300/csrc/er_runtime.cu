@@ -141,6 +141,9 @@ struct TracerItem {
     DevBuf<int> light_valid;
     DevBuf<erd::Texture> textures;
     DevBuf<float> sigma;
+    DevBuf<int> light_ids;
+    DevBuf<float> majorant, rmq;
+    DevBuf<uint32_t> minmax;
     DevBuf<int> err;
     erd::Params P;
     uint64_t built_version = 0;
@@ -339,10 +342,21 @@ er_status build(TracerItem& t)
     if (vit == C.volumes.items.end()) return fail(ER_ERR_INVALID_ID, "tracer references volume ID:%d which does not exist", d.volume_id);
     VolumeItem& v = *vit->second;
     if (d.object_count > 0) return fail(ER_ERR_UNSUPPORTED, "surface objects (ObjectIDs.Count = %d) are not implemented by the transport kernels", d.object_count);
-    if (d.settings.free_flight != ER_FREE_FLIGHT_MARCH) return fail(ER_ERR_UNSUPPORTED, "free_flight %d is not available in this build", d.settings.free_flight);
-    if (d.settings.mis != ER_MIS_LIGHT_ONLY) return fail(ER_ERR_UNSUPPORTED, "mis %d is not available in this build", d.settings.mis);
-    if (d.settings.apply_shading_type && d.settings.shading_type != ER_SHADING_BRDF_ONLY)
-        return fail(ER_ERR_UNSUPPORTED, "shading_type %d is not available in this build", d.settings.shading_type);
+    if (d.settings.free_flight != ER_FREE_FLIGHT_MARCH && d.settings.free_flight != ER_FREE_FLIGHT_DELTA)
+        return fail(ER_ERR_INVALID_ARGUMENT, "free_flight %d is not an ER_FREE_FLIGHT_* value", d.settings.free_flight);
+    if (d.settings.mis != ER_MIS_LIGHT_ONLY && d.settings.mis != ER_MIS_FULL)
+        return fail(ER_ERR_INVALID_ARGUMENT, "mis %d is not an ER_MIS_* value", d.settings.mis);
+    const int brick = d.settings.majorant_brick > 0 ? d.settings.majorant_brick : 8;
+    if (brick > 64) return fail(ER_ERR_INVALID_ARGUMENT, "majorant_brick %d out of range [1, 64]", brick);
+    const bool needs_gm = d.settings.apply_shading_type && d.settings.shading_type >= ER_SHADING_HYBRID &&
+                          d.settings.shading_type <= ER_SHADING_THRESHOLD;
+    if (needs_gm && v.gm_max < 0.0f) {
+        /* GradientMagnitudeRange of the shader switch: maximum voxel-centre
+           gradient magnitude (Source/gradientmagnitude.cuh:46-71) */
+        float m = 0.0f;
+        er_status gs = er_gradient_magnitude(vit->first, nullptr, &m);
+        if (gs != ER_OK) return gs;
+    }
     erd::Params P;
     memset(&P, 0, sizeof(P));
     volume_geometry(v, P);
@@ -384,6 +398,22 @@ er_status build(TracerItem& t)
     ER_CUDA(er_launch_sigma_table(t.opacity.p, s.density_scale, t.sigma.p, n, st));
     P.sigma = t.sigma.p;
     P.sigma_n = n;
+    P.free_flight = s.free_flight;
+    if (s.free_flight == ER_FREE_FLIGHT_DELTA) {
+        int nb[3];
+        for (int i = 0; i < 3; i++) nb[i] = (v.res[i] + brick - 1) / brick;
+        const size_t total = (size_t)nb[0] * nb[1] * nb[2];
+        int levels = 1;
+        while ((1 << levels) <= n) levels++;
+        ER_CUDA(t.majorant.ensure(total));
+        ER_CUDA(t.minmax.ensure(total));
+        ER_CUDA(t.rmq.ensure((size_t)levels * n));
+        ER_CUDA(er_launch_majorant(v.vox.p, v.res, brick, nb, t.sigma.p, n, t.rmq.p, levels, t.minmax.p, s.density_scale,
+                                   t.majorant.p, st));
+        P.brick = brick;
+        for (int i = 0; i < 3; i++) P.nb[i] = nb[i];
+        P.majorant = t.majorant.p;
+    }
     /* lights in LightIDs order */
     const int lc = d.light_count;
     std::vector<erd::Light> L((size_t)std::max(lc, 1));
@@ -400,13 +430,18 @@ er_status build(TracerItem& t)
         if (tt != C.textures.items.end() && tt->second->type == ER_TEXTURE_BITMAP)
             return fail(ER_ERR_UNSUPPORTED, "light %d uses bitmap texture %d; bitmap textures are not implemented by the transport kernels", d.light_ids[i], tid);
     }
+    std::vector<int> lids((size_t)std::max(lc, 1), -1);
+    for (int i = 0; i < lc; i++) lids[i] = d.light_ids[i];
     ER_CUDA(t.lights.ensure(L.size()));
     ER_CUDA(t.light_valid.ensure(valid.size()));
+    ER_CUDA(t.light_ids.ensure(lids.size()));
     ER_CUDA(cudaMemcpyAsync(t.lights.p, L.data(), L.size() * sizeof(erd::Light), cudaMemcpyHostToDevice, st));
     ER_CUDA(cudaMemcpyAsync(t.light_valid.p, valid.data(), valid.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    ER_CUDA(cudaMemcpyAsync(t.light_ids.p, lids.data(), lids.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     P.light_count = lc;
     P.lights = t.lights.p;
     P.light_valid = t.light_valid.p;
+    P.light_ids = t.light_ids.p;
     /* textures indexed by texture ID; unbound IDs evaluate to black */
     const int ntex = max_tex + 1;
     std::vector<erd::Texture> T((size_t)std::max(ntex, 1));
@@ -524,6 +559,9 @@ ER_API er_status er_reset(void)
     C.bitmaps.items.clear();
     C.objects.items.clear();
     C.clipping.items.clear();
+    /* a reset library starts numbering from 0 again, like a fresh process */
+    C.tracers.counter = C.volumes.counter = C.lights.counter = C.textures.counter = 0;
+    C.bitmaps.counter = C.objects.counter = C.clipping.counter = 0;
     C.version++;
     return ER_OK;
 }
@@ -548,6 +586,7 @@ ER_API void er_default_render_settings(er_render_settings* s)
     s->bilateral_sigma_d = 1.5f;
     s->bilateral_sigma_r = 20.0f;
     s->seed = 1u;
+    s->majorant_brick = 8;
 }
 
 ER_API void er_plf_init(er_plf* p)

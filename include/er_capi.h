@@ -213,7 +213,8 @@ typedef struct er_render_settings {
     float bilateral_sigma_d;      /* spatial sigma in pixels for KernelD[] */
     float bilateral_sigma_r;      /* range sigma in 0..255 luminance units for GaussSimilarity[] */
     uint32_t seed;                /* counter-based seed of the per-pixel RNG lanes */
-    int32_t reserved[6];
+    int32_t majorant_brick;       /* delta tracking: edge of the cubic voxel bricks of the majorant grid (0 means 8) */
+    int32_t reserved[5];
 } er_render_settings;
 
 /* ErTracer (Source/ertracer.h:33-117).  light_ids/object_ids/clipping_ids are

@@ -114,9 +114,19 @@ struct or_scene {
     /* statistics */
     uint64_t lookups;
     uint64_t samples;
+    /* extension estimators (see er_capi.h): sigma table over integer
+       intensities, majorant grid of the delta tracker, 1 / max |grad I| */
+    uint16_t vmax;
+    float* sigma;            /* DensityScale * Opacity(I), I in [0, vmax] */
+    int brick;
+    int nb[3];
+    float* majorant;         /* per brick: DensityScale * max sigma over the brick footprint */
+    float gm_inv_max;
+    int gm_ready;
 };
 
 static double g_lookups_per_sample = 0.0;
+static void prepare_extensions(or_scene* s);
 
 /* Shape::Update (Source/shape.h:92-103) with the area helpers :27-55 */
 static float shape_area(const er_shape* s)
@@ -201,6 +211,7 @@ or_scene* ER_OR(scene_create)(const er_tracer_desc* t, const er_volume_desc* vol
     s->n_textures = n_textures;
     s->textures = (er_texture_desc*)calloc(n_textures > 0 ? (size_t)n_textures : 1u, sizeof(er_texture_desc));
     if (n_textures > 0) memcpy(s->textures, textures, sizeof(er_texture_desc) * (size_t)n_textures);
+    prepare_extensions(s);
     return s;
 }
 
@@ -209,6 +220,8 @@ void ER_OR(scene_destroy)(or_scene* s)
     if (!s) return;
     free(s->lights);
     free(s->textures);
+    free(s->sigma);
+    free(s->majorant);
     free(s);
 }
 
@@ -997,19 +1010,264 @@ static int intersects_light(const or_scene* s, const ray_t* R)
     return 0;
 }
 
-/* Intersect / Visible - Source/transport.h:30-56 (no surface objects) */
-static int visible(or_scene* s, v3 P1, v3 P2, rng_t* rng)
+/* ------------------------------------------------------------------ */
+/* extension estimators (settings fields apply_shading_type, mis,        */
+/* free_flight of er_capi.h).  The reference has no live code for these; */
+/* the designs are Source/scatterevent.h:155-212 (shader selection),     */
+/* Source/transport.h:86-112 (BSDF-sampling half) and                    */
+/* Source/raymarching.h:115-273 (macrocell delta tracking).              */
+/* ------------------------------------------------------------------ */
+
+static inline float sigma_lookup(const or_scene* s, float I)
 {
-    if (!s->st.shadows) return 1;
+    int i = (int)I;
+    i = i < 0 ? 0 : (i > (int)s->vmax ? (int)s->vmax : i);
+    return s->sigma[i];
+}
+
+/* 3D DDA over the majorant bricks, in local voxel units (the mapping of
+   Volume::operator(), Source/volume.h:131-138) */
+typedef struct {
+    float t, tmax;
+    int b[3], step[3];
+    float tnext[3], tdelta[3];
+    int done;
+} dda_t;
+
+static void dda_init(const or_scene* s, const ray_t* R, float t0, float t1, dda_t* d)
+{
+    const float B = (float)s->brick;
+    d->t = t0;
+    d->tmax = t1;
+    d->done = 0;
+    for (int i = 0; i < 3; i++) {
+        const float sc = vget(s->inv_size, i) * (float)s->res[i];
+        const float lo = (vget(R->O, i) - vget(s->minp, i)) * sc;
+        const float ld = vget(R->D, i) * sc;
+        const float L = lo + t0 * ld;
+        int b = (int)floorf(L / B);
+        b = b < 0 ? 0 : (b >= s->nb[i] ? s->nb[i] - 1 : b);
+        d->b[i] = b;
+        if (ld > 0.0f) { d->step[i] = 1; d->tnext[i] = ((float)(b + 1) * B - lo) / ld; d->tdelta[i] = B / ld; }
+        else if (ld < 0.0f) { d->step[i] = -1; d->tnext[i] = ((float)b * B - lo) / ld; d->tdelta[i] = -B / ld; }
+        else { d->step[i] = 0; d->tnext[i] = FLT_MAX; d->tdelta[i] = FLT_MAX; }
+    }
+}
+
+static inline float dda_exit(const dda_t* d)
+{
+    float e = d->tnext[0];
+    if (d->tnext[1] < e) e = d->tnext[1];
+    if (d->tnext[2] < e) e = d->tnext[2];
+    if (d->tmax < e) e = d->tmax;
+    return e < d->t ? d->t : e;
+}
+
+static inline void dda_advance(const or_scene* s, dda_t* d, float e)
+{
+    if (e >= d->tmax) { d->done = 1; d->t = e; return; }
+    int a = 0;
+    if (d->tnext[1] < d->tnext[a]) a = 1;
+    if (d->tnext[2] < d->tnext[a]) a = 2;
+    d->b[a] += d->step[a];
+    if (d->b[a] < 0 || d->b[a] >= s->nb[a]) d->done = 1;
+    d->tnext[a] += d->tdelta[a];
+    d->t = e;
+}
+
+static inline float dda_majorant(const or_scene* s, const dda_t* d)
+{
+    return s->majorant[((size_t)d->b[2] * (size_t)s->nb[1] + (size_t)d->b[1]) * (size_t)s->nb[0] + (size_t)d->b[0]];
+}
+
+#define ER_DELTA_MAX_COLLISIONS 1048576
+
+/* Delta tracking of the primary ray.  sigma_t(x) = DensityScale *
+   DensityScale * Opacity(I(x)) is the extinction the reference's march
+   integrates: Sum += DS*Op*Step against S = -ln(U)/DS
+   (Source/raymarching.h:45,64-66).  The event is the accepted collision
+   itself (the march reports one step past it, :66-70). */
+static void sample_volume_delta(or_scene* s, ray_t R, rng_t* rng, scatter_event* SE)
+{
+    isect_t Int; isect_invalid(&Int);
+    intersect_box(&R, s->minp, vscale(s->size, 0.5f), &Int);
+    if (!Int.valid) return;
+    const float t0 = smax(Int.near_t, R.MinT);
+    const float t1 = smin(Int.far_t, R.MaxT);
+    if (!(t0 < t1)) return;
+    dda_t d;
+    dda_init(s, &R, t0, t1, &d);
+    float tau = -er_logf(rng_get1(rng));
+    int guard = 0;
+    while (!d.done) {
+        const float e = dda_exit(&d);
+        const float mu = dda_majorant(s, &d);
+        float t = d.t;
+        if (mu > 0.0f) {
+            for (;;) {
+                const float dt = tau / mu;
+                if (!(t + dt < e)) {
+                    tau = tau - mu * (e - t);
+                    if (tau < 0.0f) tau = 0.0f;
+                    break;
+                }
+                t = t + dt;
+                const v3 P = vadd(R.O, vscale(R.D, t));
+                const float sig = s->st.density_scale * sigma_lookup(s, get_intensity(s, P));
+                if (rng_get1(rng) * mu < sig) {
+                    SE->valid = 1;
+                    SE->T = t;
+                    SE->P = P;
+                    SE->N = normalized_gradient(s, P);
+                    SE->Wo = vneg(R.D);
+                    SE->Le = C3(0, 0, 0);
+                    SE->UV.x = 0.0f; SE->UV.y = 0.0f;
+                    return;
+                }
+                if (++guard > ER_DELTA_MAX_COLLISIONS) return;
+                tau = -er_logf(rng_get1(rng));
+            }
+        }
+        dda_advance(s, &d, e);
+    }
+}
+
+/* Ratio tracking of a shadow segment with Russian roulette below 0.1 */
+static float transmittance_ratio(or_scene* s, ray_t R, rng_t* rng)
+{
+    isect_t Int; isect_invalid(&Int);
+    intersect_box(&R, s->minp, vscale(s->size, 0.5f), &Int);
+    if (!Int.valid) return 1.0f;
+    const float t0 = smax(Int.near_t, R.MinT);
+    const float t1 = smin(Int.far_t, R.MaxT);
+    if (!(t0 < t1)) return 1.0f;
+    dda_t d;
+    dda_init(s, &R, t0, t1, &d);
+    float Tr = 1.0f;
+    float tau = -er_logf(rng_get1(rng));
+    int guard = 0;
+    while (!d.done) {
+        const float e = dda_exit(&d);
+        const float mu = dda_majorant(s, &d);
+        float t = d.t;
+        if (mu > 0.0f) {
+            for (;;) {
+                const float dt = tau / mu;
+                if (!(t + dt < e)) {
+                    tau = tau - mu * (e - t);
+                    if (tau < 0.0f) tau = 0.0f;
+                    break;
+                }
+                t = t + dt;
+                const v3 P = vadd(R.O, vscale(R.D, t));
+                const float sig = s->st.density_scale * sigma_lookup(s, get_intensity(s, P));
+                Tr = Tr * (1.0f - sig / mu);
+                if (Tr <= 0.0f) return 0.0f;
+                if (Tr < 0.1f) {
+                    if (rng_get1(rng) >= 0.5f) return 0.0f;
+                    Tr = Tr * 2.0f;
+                }
+                if (++guard > ER_DELTA_MAX_COLLISIONS) return Tr;
+                tau = -er_logf(rng_get1(rng));
+            }
+        }
+        dda_advance(s, &d, e);
+    }
+    return Tr;
+}
+
+/* Intersect / Visible - Source/transport.h:30-56 (no surface objects):
+   1/0 for the reference march, the ratio-tracked transmittance otherwise */
+static float visibility(or_scene* s, v3 P1, v3 P2, rng_t* rng)
+{
+    if (!s->st.shadows) return 1.0f;
     const v3 W = vnorm(vsub(P2, P1));
     ray_t R;
     R.O = vadd(P1, vscale(W, RAY_EPS));
     R.D = W;
     R.MinT = 0.0f;
     R.MaxT = smin(vlen(vsub(P2, P1)) - 2.0f * RAY_EPS, s->st.max_shadow_distance);
-    if (intersects_light(s, &R)) return 0;
-    if (scatter_event_in_volume(s, R, rng)) return 0;
-    return 1;
+    if (intersects_light(s, &R)) return 0.0f;
+    if (s->st.free_flight == ER_FREE_FLIGHT_DELTA) return transmittance_ratio(s, R, rng);
+    return scatter_event_in_volume(s, R, rng) ? 0.0f : 1.0f;
+}
+
+/* shader selection of the commented design Source/scatterevent.h:155-212:
+   0 = BRDF, 1 = isotropic phase; GradientMagnitudeRange.Inv is 1 / the
+   maximum voxel-centre gradient magnitude of the pre-pass */
+static int select_shader_type(or_scene* s, const scatter_event* SE, float I, rng_t* rng)
+{
+    switch (s->st.shading_type) {
+    case ER_SHADING_BRDF_ONLY: return 0;
+    case ER_SHADING_PHASE_ONLY: return 1;
+    case ER_SHADING_HYBRID: {
+        const float NGM = gradient_magnitude(s, SE->P) * s->gm_inv_max;
+        const float Exponent = 25.0f * er_powf(s->st.gradient_factor, 3.0f) * NGM;
+        const float PdfBrdf = s->st.opacity_modulated ? plf_eval(&s->opacity, I) * (1.0f - er_expf(-Exponent))
+                                                      : 1.0f - er_expf(-Exponent);
+        return rng_get1(rng) <= PdfBrdf ? 0 : 1;
+    }
+    case ER_SHADING_MODULATION: {
+        const float NGM = gradient_magnitude(s, SE->P) * s->gm_inv_max;
+        const float PdfBrdf = 1.0f - er_powf(1.0f - NGM, 2.0f);
+        return rng_get1(rng) < PdfBrdf ? 0 : 1;
+    }
+    case ER_SHADING_THRESHOLD: {
+        const float NGM = gradient_magnitude(s, SE->P) * s->gm_inv_max;
+        return NGM > s->st.gradient_threshold ? 0 : 1;
+    }
+    default: return 1;
+    }
+}
+
+#define INV_FOUR_PI_TRUE 0.0795774715f
+
+/* pdf of the BSDF sampler of the full-MIS estimator: the equal-weight
+   mixture of Lambertian and Blinn lobes for the BRDF (BRDF::SampleF picks
+   each with probability 1/2, Source/shader.h:364-371), 1/(4 pi) for the
+   uniform sphere sampler of IsotropicPhase::SampleF (:293-299) */
+static float mis_bsdf_pdf(const shader_t* sh, v3 Wo, v3 Wi)
+{
+    if (sh->type == 0) {
+        const v3 Wol = world_to_local(sh, Wo), Wil = world_to_local(sh, Wi);
+        const float pl = same_hemisphere(Wol, Wil) ? fabsf(Wil.z) * INV_PI_F : 0.0f;
+        const float pm = same_hemisphere(Wol, Wil) ? blinn_pdf(sh->exponent, Wol, Wil) : 0.0f;
+        return 0.5f * (pl + pm);
+    }
+    return INV_FOUR_PI_TRUE;
+}
+
+/* Lambertian::SampleF (Source/shader.h:46-56), Blinn::SampleF (:142-164)
+   with the component choice of BRDF::SampleF (:364-371); the sphere sampler
+   of IsotropicPhase::SampleF (:293-299, Source/montecarlo.h:191-199) */
+static v3 sample_bsdf_dir(const shader_t* sh, v3 Wo, const metro_sample* ms)
+{
+    if (sh->type == 0) {
+        const v3 Wol = world_to_local(sh, Wo);
+        v3 Wil;
+        if (ms->brdf_component <= 0.5f) {
+            const v2 d = concentric_sample_disk(ms->brdf_dir);
+            Wil = V3(d.x, d.y, sqrtf(smax(0.f, 1.f - d.x * d.x - d.y * d.y)));
+            if (Wol.z < 0.0f) Wil.z *= -1.0f;
+        } else {
+            const float e = sh->exponent;
+            const float costheta = er_powf(ms->brdf_dir.x, 1.f / (e + 1));
+            const float sintheta = sqrtf(smax(0.f, 1.f - costheta * costheta));
+            const float phi = ms->brdf_dir.y * 2.f * PI_F;
+            float sn, cs;
+            er_sincosf(phi, &sn, &cs);
+            v3 wh = V3(sintheta * cs, sintheta * sn, costheta);
+            if (!same_hemisphere(Wol, wh)) wh = vneg(wh);
+            Wil = vadd(vneg(Wol), vscale(wh, 2.f * vdot(Wol, wh)));
+        }
+        return local_to_world(sh, Wil);
+    }
+    const float z = 1.f - 2.f * ms->brdf_dir.x;
+    const float r = sqrtf(smax(0.f, 1.f - z * z));
+    const float phi = 2.f * PI_F * ms->brdf_dir.y;
+    float sn, cs;
+    er_sincosf(phi, &sn, &cs);
+    return V3(r * cs, r * sn, z);
 }
 
 /* SampleLight - Source/lights.h:44-57 */
@@ -1023,9 +1281,14 @@ static void sample_light(const or_scene* s, const or_light* L, v3 uvw, surf_samp
     if (L->d.unit == 1) *Le = cdivs(*Le, L->area);
 }
 
-/* EstimateDirectLight - Source/transport.h:58-84 (light-sampling half; the
-   function returns at :84) */
-static col3 estimate_direct_light(or_scene* s, const or_light* L, const metro_sample* ms, scatter_event* SE,
+/* EstimateDirectLight - Source/transport.h:58-113.  With mis = 0 and the
+   fixed-step march this is the live code (the function returns at :84).
+   With mis = 1 the BSDF-sampling half of :86-112 runs as well, both halves
+   weighted by the power heuristic over (light pdf, mixture BSDF pdf), and
+   the light pdf of the BSDF half uses the light's surface normal at the hit
+   (the design divides by |N . -Wi| with the scatter point's normal, :102).
+   With delta tracking the shadow term is the ratio-tracked transmittance. */
+static col3 estimate_direct_light(or_scene* s, const or_light* L, int slot, const metro_sample* ms, scatter_event* SE,
                                   rng_t* rng, const shader_t* sh)
 {
     v3 Wi;
@@ -1033,12 +1296,55 @@ static col3 estimate_direct_light(or_scene* s, const or_light* L, const metro_sa
     surf_sample SS;
     sample_light(s, L, ms->light_uvw, &SS, SE, &Wi, &Li);
     const col3 F = shader_f(sh, SE->Wo, Wi);
-    const float BsdfPdf = shader_pdf(sh, SE->Wo, Wi);
-    if (!cblack(Li) && !cblack(F) && BsdfPdf > 0.0f && visible(s, SE->P, SS.P, rng)) {
-        const float LightPdf = vlen2(vsub(SE->P, SS.P)) / (vabsdot(SS.N, vneg(Wi)) * L->area);
-        const float Weight = power_heuristic(LightPdf, BsdfPdf);
-        if (sh->type == 0) Ld = cadd(Ld, cscale(cmul(F, Li), vabsdot(Wi, SE->N) * Weight / LightPdf));
-        else Ld = cadd(Ld, cdivs(cmul(F, Li), LightPdf));
+    const int full = s->st.mis == ER_MIS_FULL;
+    const int delta = s->st.free_flight == ER_FREE_FLIGHT_DELTA;
+    const float BsdfPdf = full ? mis_bsdf_pdf(sh, SE->Wo, Wi) : shader_pdf(sh, SE->Wo, Wi);
+    if (!full && !delta) {
+        if (!cblack(Li) && !cblack(F) && BsdfPdf > 0.0f && visibility(s, SE->P, SS.P, rng) > 0.0f) {
+            const float LightPdf = vlen2(vsub(SE->P, SS.P)) / (vabsdot(SS.N, vneg(Wi)) * L->area);
+            const float Weight = power_heuristic(LightPdf, BsdfPdf);
+            if (sh->type == 0) Ld = cadd(Ld, cscale(cmul(F, Li), vabsdot(Wi, SE->N) * Weight / LightPdf));
+            else Ld = cadd(Ld, cdivs(cmul(F, Li), LightPdf));
+        }
+        return Ld;
+    }
+    if (!cblack(Li) && !cblack(F) && BsdfPdf > 0.0f) {
+        const float Tr = visibility(s, SE->P, SS.P, rng);
+        if (Tr > 0.0f) {
+            const float LightPdf = vlen2(vsub(SE->P, SS.P)) / (vabsdot(SS.N, vneg(Wi)) * L->area);
+            col3 c;
+            if (full) {
+                const float w = power_heuristic(LightPdf, BsdfPdf);
+                c = cscale(cmul(F, Li), sh->type == 0 ? vabsdot(Wi, SE->N) * w / LightPdf : w / LightPdf);
+            } else if (sh->type == 0) {
+                c = cscale(cmul(F, Li), vabsdot(Wi, SE->N) * power_heuristic(LightPdf, BsdfPdf) / LightPdf);
+            } else {
+                c = cdivs(cmul(F, Li), LightPdf);
+            }
+            Ld = cadd(Ld, cscale(c, Tr));
+        }
+    }
+    if (!full) return Ld;
+    const v3 Wb = sample_bsdf_dir(sh, SE->Wo, ms);
+    const col3 Fb = shader_f(sh, SE->Wo, Wb);
+    const float pb = mis_bsdf_pdf(sh, SE->Wo, Wb);
+    if (cblack(Fb) || !(pb > 0.0f)) return Ld;
+    ray_t R2;
+    R2.O = SE->P;
+    R2.D = Wb;
+    R2.MinT = 0.0f;
+    R2.MaxT = 1000000.0f;                 /* Ray(SE.P, Wi) defaults, Source/ray.h:29 */
+    scatter_event SE2;
+    se_invalid(&SE2, 1);
+    intersect_lights(s, &R2, &SE2, 0);
+    if (!SE2.valid || s->light_idx[SE2.light_id] != s->light_idx[slot]) return Ld;
+    if (cblack(SE2.Le)) return Ld;
+    const float Tr = visibility(s, SE->P, SE2.P, rng);
+    if (Tr > 0.0f) {
+        const float LightPdf = vlen2(vsub(SE->P, SE2.P)) / (vabsdot(SE2.N, vneg(Wb)) * L->area);
+        const float w = power_heuristic(pb, LightPdf);
+        const col3 c = cscale(cmul(Fb, SE2.Le), sh->type == 0 ? vabsdot(Wb, SE->N) * w / pb : w / pb);
+        Ld = cadd(Ld, cscale(c, Tr));
     }
     return Ld;
 }
@@ -1057,10 +1363,103 @@ static col3 uniform_sample_one_light(or_scene* s, scatter_event* SE, rng_t* rng,
     const or_light* L = &s->lights[light_id];
     shader_t sh;
     const float vol_ior = s->st.volume_ior > 0.0f ? s->st.volume_ior : 15.0f;
-    shader_init(&sh, 0, SE->N, SE->Wo, ctf_eval(&s->diffuse, I), ctf_eval(&s->specular, I), vol_ior,
+    const int type = s->st.apply_shading_type ? select_shader_type(s, SE, I, rng) : 0;
+    shader_init(&sh, type, SE->N, SE->Wo, ctf_eval(&s->diffuse, I), ctf_eval(&s->specular, I), vol_ior,
                 glossiness_exponent(plf_eval(&s->glossiness, I)));
-    Ld = cadd(Ld, estimate_direct_light(s, L, ms, SE, rng, &sh));
+    Ld = cadd(Ld, estimate_direct_light(s, L, idx, ms, SE, rng, &sh));
     return cscale(Ld, (float)s->light_count);
+}
+
+/* ---- per-scene tables of the extension estimators ---- */
+
+typedef struct { or_scene* s; int z0, z1; float mx; } gm_job;
+
+static void* gm_run(void* arg)
+{
+    gm_job* j = (gm_job*)arg;
+    or_scene local = *j->s;
+    float mx = 0.0f;
+    for (int Z = j->z0; Z < j->z1; Z++)
+        for (int Y = 0; Y < local.res[1]; Y++)
+            for (int X = 0; X < local.res[0]; X++) {
+                const float sx = 2.0f * (local.size.x * 0.5f), sy = 2.0f * (local.size.y * 0.5f), sz = 2.0f * (local.size.z * 0.5f);
+                const v3 p = V3(local.minp.x + sx * (((float)X + 0.5f) * (1.0f / (float)local.res[0])),
+                                local.minp.y + sy * (((float)Y + 0.5f) * (1.0f / (float)local.res[1])),
+                                local.minp.z + sz * (((float)Z + 0.5f) * (1.0f / (float)local.res[2])));
+                const float g = gradient_magnitude(&local, p);
+                mx = g > mx ? g : mx;
+            }
+    j->mx = mx;
+    return NULL;
+}
+
+static float gradient_magnitude_max_threaded(or_scene* s, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > s->res[2]) nthreads = s->res[2];
+    gm_job* jobs = (gm_job*)calloc((size_t)nthreads, sizeof(gm_job));
+    pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+    for (int t = 0; t < nthreads; t++) {
+        jobs[t].s = s;
+        jobs[t].z0 = (int)((long long)s->res[2] * t / nthreads);
+        jobs[t].z1 = (int)((long long)s->res[2] * (t + 1) / nthreads);
+    }
+    for (int t = 1; t < nthreads; t++) pthread_create(&th[t], NULL, gm_run, &jobs[t]);
+    gm_run(&jobs[0]);
+    for (int t = 1; t < nthreads; t++) pthread_join(th[t], NULL);
+    float mx = 0.0f;
+    for (int t = 0; t < nthreads; t++) mx = jobs[t].mx > mx ? jobs[t].mx : mx;
+    free(jobs);
+    free(th);
+    return mx;
+}
+
+static void prepare_extensions(or_scene* s)
+{
+    const size_t n = (size_t)s->res[0] * (size_t)s->res[1] * (size_t)s->res[2];
+    uint16_t vmax = 0;
+    for (size_t i = 0; i < n; i++) vmax = s->vox[i] > vmax ? s->vox[i] : vmax;
+    s->vmax = vmax;
+    s->sigma = (float*)malloc(sizeof(float) * ((size_t)vmax + 1));
+    for (int i = 0; i <= (int)vmax; i++) s->sigma[i] = s->st.density_scale * plf_eval(&s->opacity, (float)i);
+    if (s->st.free_flight == ER_FREE_FLIGHT_DELTA) {
+        const int B = s->st.majorant_brick > 0 ? s->st.majorant_brick : 8;
+        s->brick = B;
+        for (int i = 0; i < 3; i++) s->nb[i] = (s->res[i] + B - 1) / B;
+        const size_t nbt = (size_t)s->nb[0] * s->nb[1] * s->nb[2];
+        s->majorant = (float*)malloc(sizeof(float) * nbt);
+        for (int bz = 0; bz < s->nb[2]; bz++)
+            for (int by = 0; by < s->nb[1]; by++)
+                for (int bx = 0; bx < s->nb[0]; bx++) {
+                    /* voxel footprint of the brick plus a one-voxel apron on both sides */
+                    int lo[3], hi[3];
+                    const int b[3] = { bx, by, bz };
+                    for (int i = 0; i < 3; i++) {
+                        lo[i] = b[i] * B - 1;
+                        hi[i] = (b[i] + 1) * B + 1;
+                        lo[i] = lo[i] < 0 ? 0 : lo[i];
+                        hi[i] = hi[i] > s->res[i] - 1 ? s->res[i] - 1 : hi[i];
+                    }
+                    uint16_t vlo = 65535, vhi = 0;
+                    for (int z = lo[2]; z <= hi[2]; z++)
+                        for (int y = lo[1]; y <= hi[1]; y++)
+                            for (int x = lo[0]; x <= hi[0]; x++) {
+                                const uint16_t v = s->vox[(size_t)z * s->res[0] * s->res[1] + (size_t)y * s->res[0] + x];
+                                vlo = v < vlo ? v : vlo;
+                                vhi = v > vhi ? v : vhi;
+                            }
+                    float m = 0.0f;
+                    for (int i = vlo; i <= (int)vhi; i++) m = s->sigma[i] > m ? s->sigma[i] : m;
+                    s->majorant[((size_t)bz * s->nb[1] + by) * s->nb[0] + bx] = s->st.density_scale * m;
+                }
+    }
+    s->gm_inv_max = 0.0f;
+    s->gm_ready = 0;
+    if (s->st.apply_shading_type && s->st.shading_type >= ER_SHADING_HYBRID && s->st.shading_type <= ER_SHADING_THRESHOLD) {
+        const float mx = gradient_magnitude_max_threaded(s, 8);
+        s->gm_inv_max = mx > 0.0f ? 1.0f / mx : 0.0f;
+        s->gm_ready = 1;
+    }
 }
 
 /* SampleCamera - Source/singlescattering.h:29-50 */
@@ -1089,7 +1488,8 @@ static void sample_ray(or_scene* s, ray_t R, rng_t* rng, scatter_event* nearest)
     scatter_event se[2];
     se_invalid(&se[0], 0);
     se_invalid(&se[1], 1);
-    sample_volume(s, R, rng, &se[0]);
+    if (s->st.free_flight == ER_FREE_FLIGHT_DELTA) sample_volume_delta(s, R, rng, &se[0]);
+    else sample_volume(s, R, rng, &se[0]);
     intersect_lights(s, &R, &se[1], 1);
     float T = FLT_MAX;
     se_invalid(nearest, 0);

@@ -1,0 +1,102 @@
+"""Oracle checks of the estimators the reference designs but does not run:
+delta/ratio tracking over the majorant grid, the hybrid phase/BRDF switch and
+the BSDF-sampling MIS half (no live reference code exists, so these are
+checked against analytic answers and against each other)."""
+import numpy as np
+import pytest
+
+import oracle_lib as OL
+
+C = OL.C
+S = OL.PKG.scenes
+
+
+def homogeneous_scene(free_flight, op=1e-4, res=16, film=(8, 8)):
+    vol = np.full((res, res, res), 1000, np.uint16)
+    t = S.c1_tracer(film)
+    t.opacity = C.make_plf([(0.0, op), (65535.5, op)])
+    t.camera = S.make_camera(film, (0.0, -2.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 2.0, 1.0)
+    t.light_count = 0
+    t.settings.free_flight = free_flight
+    return S.Scene("homog", vol, tracer=t, lights=[], textures=[])
+
+
+@pytest.mark.parametrize("free_flight", [0, 1])
+def test_homogeneous_slab_event_probability(oracle, free_flight):
+    """sigma_t = DensityScale^2 * opacity = 1 per unit length over a chord of
+    length 1: a camera ray scatters with probability 1 - exp(-1)."""
+    sc = homogeneous_scene(free_flight)
+    h = OL.SceneHandle(oracle, sc)
+    s = h.render_sum(512, nthreads=4)
+    alpha = s[..., 3].sum() / (512 * 64)
+    se = np.sqrt(0.632 * 0.368 / (512 * 64))
+    assert abs(alpha - (1.0 - np.exp(-1.0))) < 5 * se + 0.01 * (free_flight == 0)
+
+
+def batch_means(h, spp, batches, first=0):
+    out = []
+    for b in range(batches):
+        out.append(h.render_sum(spp, first=first + b * spp, nthreads=8) / spp)
+    return np.stack(out)
+
+
+def test_phase_mis_matches_light_sampling(oracle):
+    """For the isotropic phase function the light-only estimator is unweighted
+    (Source/transport.h:81), so it and the two-half MIS estimator estimate the
+    same integral: their means must agree within the sampling error."""
+    means = []
+    for mis in (0, 1):
+        sc = S.scene_tiny(res=20, film=(10, 8), seed=6)
+        tm = np.eye(4).tolist()
+        env = C.er_light_desc()
+        env.visible = 1
+        env.shape = S.make_shape(C.SHAPE_SPHERE, (tm, tm), outer=3.0)
+        env.texture_id = 0
+        env.multiplier = 0.5
+        sc.lights.append(env)
+        sc.tracer.light_count = 2
+        sc.tracer.light_ids[1] = 1
+        sc.tracer.settings.apply_shading_type = 1
+        sc.tracer.settings.shading_type = C.SHADING_PHASE_ONLY
+        sc.tracer.settings.free_flight = 1
+        sc.tracer.settings.mis = mis
+        h = OL.SceneHandle(oracle, sc)
+        means.append(batch_means(h, 256, 16))
+        h.close()
+    m0, m1 = means[0].mean(0), means[1].mean(0)
+    se = np.sqrt(means[0].var(0, ddof=1) / 16 + means[1].var(0, ddof=1) / 16) + 1e-6
+    z = np.abs(m0 - m1)[..., :3] / se[..., :3]
+    assert np.median(z) < 1.5 and z.max() < 6.0
+    assert abs(m0[..., :3].mean() - m1[..., :3].mean()) < 0.02 * m0[..., :3].mean() + 1e-4
+
+
+@pytest.mark.parametrize("mode", [
+    dict(free_flight=1),
+    dict(free_flight=1, mis=1),
+    dict(free_flight=0, mis=1, apply_shading_type=1, shading_type=2),
+    dict(free_flight=1, mis=1, apply_shading_type=1, shading_type=3),
+    dict(free_flight=1, apply_shading_type=1, shading_type=4),
+])
+def test_extension_modes_render(oracle, mode):
+    sc = S.scene_tiny(res=20, film=(12, 10), seed=7)
+    for k, v in mode.items():
+        setattr(sc.tracer.settings, k, v)
+    h = OL.SceneHandle(oracle, sc)
+    a = h.render_sum(8, nthreads=4)
+    b = h.render_sum(8, nthreads=4)
+    assert np.array_equal(a, b)
+    assert np.isfinite(a).all() and a[..., 3].sum() > 0
+
+
+def test_delta_and_march_agree_on_alpha(oracle):
+    """The two free-flight estimators differ only by the march's step
+    quantisation: their mean alpha over the C1-shaped tiny scene agrees."""
+    vals = []
+    for ff in (0, 1):
+        sc = S.scene_tiny(res=24, film=(16, 12), seed=8)
+        sc.tracer.settings.free_flight = ff
+        sc.tracer.light_count = 0
+        h = OL.SceneHandle(oracle, sc)
+        vals.append(h.render_sum(128, nthreads=8)[..., 3] / 128)
+        h.close()
+    assert abs(vals[0].mean() - vals[1].mean()) < 0.02

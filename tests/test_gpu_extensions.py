@@ -1,0 +1,97 @@
+"""GPU extension estimators (delta/ratio tracking, hybrid shader switch,
+full MIS) against the oracle's restatement: bit-exact per path."""
+import importlib
+
+import numpy as np
+import pytest
+
+import oracle_lib as OL
+
+pytestmark = pytest.mark.gpu
+
+C = OL.C
+S = OL.PKG.scenes
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+@pytest.fixture(scope="module")
+def env():
+    import torch
+    assert torch.cuda.is_available()
+    lib = C.load_library()
+    C.check(lib.er_set_device(0))
+    rt = importlib.import_module("exposure-render_gb300.runtime")
+    yield torch, lib, rt
+    lib.er_reset()
+
+
+def two_light_scene(seed, film=(24, 20)):
+    sc = S.scene_tiny(res=20, film=film, seed=seed)
+    tm = np.eye(4).tolist()
+    envl = C.er_light_desc()
+    envl.visible = 1
+    envl.shape = S.make_shape(C.SHAPE_SPHERE, (tm, tm), outer=3.0)
+    envl.texture_id = 1
+    envl.multiplier = 0.5
+    sc.lights.append(envl)
+    sc.textures.append(S.gradient_texture([(0.0, (0.2, 0.2, 0.3)), (1.0, (1.0, 1.0, 1.0))]))
+    sc.tracer.light_count = 2
+    sc.tracer.light_ids[1] = 1
+    return sc
+
+
+MODES = [
+    dict(free_flight=1),
+    dict(free_flight=1, majorant_brick=4),
+    dict(free_flight=1, majorant_brick=16),
+    dict(free_flight=0, mis=1),
+    dict(free_flight=1, mis=1),
+    dict(free_flight=0, apply_shading_type=1, shading_type=1),
+    dict(free_flight=1, mis=1, apply_shading_type=1, shading_type=1),
+    dict(free_flight=1, mis=1, apply_shading_type=1, shading_type=2),
+    dict(free_flight=0, mis=0, apply_shading_type=1, shading_type=2, opacity_modulated=0),
+    dict(free_flight=1, mis=1, apply_shading_type=1, shading_type=3),
+    dict(free_flight=1, mis=0, apply_shading_type=1, shading_type=4),
+]
+
+
+@pytest.mark.parametrize("mode", MODES, ids=[",".join(f"{k}={v}" for k, v in m.items()) for m in MODES])
+def test_extension_mode_bit_exact(env, oracle, mode):
+    torch, lib, rt = env
+    sc = two_light_scene(9)
+    for k, v in mode.items():
+        setattr(sc.tracer.settings, k, v)
+    r = rt.Renderer(sc, lib)
+    h = OL.SceneHandle(oracle, sc)
+    try:
+        d = torch.zeros((sc.height, sc.width, 4), dtype=torch.float32, device="cuda")
+        r.trace_sum_device(d.data_ptr(), 4, 3, 5, 0, None)
+        torch.cuda.synchronize()
+        cpu = h.render_sum(4, view=3, first=5, nthreads=4)
+        g = d.cpu().numpy()
+        assert np.array_equal(bits(g), bits(cpu))
+        assert cpu[..., 3].sum() > 0
+    finally:
+        r.close()
+        h.close()
+
+
+def test_delta_c1_crop_bit_exact(env, oracle):
+    torch, lib, rt = env
+    sc = S.scene_c1()
+    sc.tracer.settings.free_flight = 1
+    sc.tracer.settings.mis = 1
+    r = rt.Renderer(sc, lib)
+    h = OL.SceneHandle(oracle, sc)
+    try:
+        d = torch.zeros((sc.height, sc.width, 4), dtype=torch.float32, device="cuda")
+        r.trace_sum_device(d.data_ptr(), 8, 0, 0, 0, None)
+        torch.cuda.synchronize()
+        cpu = h.render_sum(8, rect=(100, 96, 48, 40), nthreads=8)
+        assert np.array_equal(bits(d.cpu().numpy()[96:136, 100:148]), bits(cpu))
+    finally:
+        r.close()
+        h.close()
