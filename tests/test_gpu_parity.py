@@ -291,6 +291,7 @@ def test_bind_list_semantics_and_errors(torch, lib):
     i = ctypes.c_int32(-1)
     C.check(lib.er_bind_texture(ctypes.byref(t), ctypes.byref(i)))
     assert i.value == 31                                                        # IDs are not reused
+    C.check(lib.er_unbind_texture(31))                                          # back to 30 items
     i2 = ctypes.c_int32(7)
     C.check(lib.er_bind_texture(ctypes.byref(t), ctypes.byref(i2)))
     assert i2.value == 7                                                        # update in place
