@@ -975,6 +975,32 @@ ER_API er_status er_gradient_magnitude(int32_t volume_id, uint16_t* d_gm, float*
     return ER_OK;
 }
 
+ER_API er_status er_build_majorant_device(const uint16_t* d_voxels, const int32_t resolution[3], int32_t brick, const float* d_sigma,
+                                          int32_t sigma_count, float density_scale, float* d_majorant, void* stream)
+{
+    ER_LOCK;
+    if (!d_voxels || !resolution || !d_sigma || !d_majorant) return fail(ER_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (brick < 1 || brick > 64) return fail(ER_ERR_INVALID_ARGUMENT, "brick %d out of range [1, 64]", brick);
+    if (sigma_count < 1 || sigma_count > 65536) return fail(ER_ERR_INVALID_ARGUMENT, "sigma_count %d out of range [1, 65536]", sigma_count);
+    int res[3], nb[3];
+    for (int i = 0; i < 3; i++) {
+        if (resolution[i] <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "resolution must be positive");
+        res[i] = resolution[i];
+        nb[i] = (res[i] + brick - 1) / brick;
+    }
+    const size_t total = (size_t)nb[0] * nb[1] * nb[2];
+    int levels = 1;
+    while ((1 << levels) <= sigma_count) levels++;
+    /* library-owned scratch, grown on demand */
+    static DevBuf<uint32_t> minmax;
+    static DevBuf<float> rmq;
+    ER_CUDA(minmax.ensure(total));
+    ER_CUDA(rmq.ensure((size_t)levels * sigma_count));
+    ER_CUDA(er_launch_majorant(d_voxels, res, brick, nb, d_sigma, sigma_count, rmq.p, levels, minmax.p, density_scale, d_majorant,
+                               (cudaStream_t)stream));
+    return ER_OK;
+}
+
 ER_API er_status er_math_eval_device(int32_t fn, int32_t n, const float* d_x, const float* d_y, float* d_out, void* stream)
 {
     if (fn < 0 || fn > 7 || n < 0 || !d_x || !d_out || ((fn == 5 || fn == 7) && !d_y))

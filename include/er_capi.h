@@ -360,6 +360,17 @@ ER_API er_status er_bilateral_device(const uint8_t* d_in, uint8_t* d_tmp, uint8_
    optional u16 magnitude volume (saturating) and the maximum magnitude. */
 ER_API er_status er_gradient_magnitude(int32_t volume_id, uint16_t* d_gm_or_null, float* max_gradient_magnitude);
 
+/* Majorant grid of the delta tracker for caller-owned device buffers:
+   d_voxels (x-fastest uint16, resolution[0]*[1]*[2]), d_sigma (sigma_count
+   floats, sigma[I] = density_scale * Opacity(I), covering every voxel value),
+   d_majorant receives ceil(res/brick) per axis floats, x fastest:
+   density_scale * max sigma over each brick's voxels plus a one-voxel apron.
+   The design precedent is the commented macrocell tracker of
+   Source/raymarching.h:115-273 (per-cell maximum extinction).  Scratch space
+   (per-brick min/max, range-max table) is allocated by the library. */
+ER_API er_status er_build_majorant_device(const uint16_t* d_voxels, const int32_t resolution[3], int32_t brick, const float* d_sigma,
+                                          int32_t sigma_count, float density_scale, float* d_majorant, void* stream);
+
 /* Diagnostics: evaluates one include/er_math.h function on the GPU for n
    arguments (fn 0 log, 1 exp, 2 sin, 3 cos, 4 tan, 5 pow(x,y), 6 acos,
    7 atan2(x,y)); used to check that device and host produce the same bits.

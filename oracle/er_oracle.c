@@ -1875,3 +1875,36 @@ void ER_OR(math_eval)(int32_t fn, int32_t n, const float* x, const float* y, flo
         }
     }
 }
+
+/* majorant grid by brute force over each brick's footprint (the grid the
+   delta tracker of this file uses, exported for the device pre-pass tests) */
+void ER_OR(majorant_grid)(const uint16_t* vox, const int32_t* res, int32_t B, const float* sigma, int32_t n, float ds, float* out)
+{
+    int nb[3];
+    for (int i = 0; i < 3; i++) nb[i] = (res[i] + B - 1) / B;
+    for (int bz = 0; bz < nb[2]; bz++)
+        for (int by = 0; by < nb[1]; by++)
+            for (int bx = 0; bx < nb[0]; bx++) {
+                int lo[3], hi[3];
+                const int b[3] = { bx, by, bz };
+                for (int i = 0; i < 3; i++) {
+                    lo[i] = b[i] * B - 1;
+                    hi[i] = (b[i] + 1) * B + 1;
+                    lo[i] = lo[i] < 0 ? 0 : lo[i];
+                    hi[i] = hi[i] > res[i] - 1 ? res[i] - 1 : hi[i];
+                }
+                int vlo = 65535, vhi = 0;
+                for (int z = lo[2]; z <= hi[2]; z++)
+                    for (int y = lo[1]; y <= hi[1]; y++)
+                        for (int x = lo[0]; x <= hi[0]; x++) {
+                            const int v = vox[(size_t)z * res[0] * res[1] + (size_t)y * res[0] + x];
+                            vlo = v < vlo ? v : vlo;
+                            vhi = v > vhi ? v : vhi;
+                        }
+                vlo = vlo > n - 1 ? n - 1 : vlo;
+                vhi = vhi > n - 1 ? n - 1 : vhi;
+                float m = 0.0f;
+                for (int i = vlo; i <= vhi; i++) m = sigma[i] > m ? sigma[i] : m;
+                out[((size_t)bz * nb[1] + by) * nb[0] + bx] = ds * m;
+            }
+}

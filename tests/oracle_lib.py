@@ -56,6 +56,7 @@ class Oracle:
             f("bilateral", None, [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_float, c_float])
             f("gradient_magnitude_volume", c_float, [c_void_p, c_void_p])
             f("math_eval", None, [c_int32, c_int32, c_void_p, c_void_p, c_void_p])
+            f("majorant_grid", None, [c_void_p, c_void_p, c_int32, c_void_p, c_int32, c_float, c_void_p])
 
     def fn(self, name, res, args):
         h = getattr(self.lib, self.p + name)

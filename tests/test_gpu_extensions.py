@@ -95,3 +95,32 @@ def test_delta_c1_crop_bit_exact(env, oracle):
     finally:
         r.close()
         h.close()
+
+
+def sigma_table(oracle, plf, n, ds):
+    xs = np.arange(n, dtype=np.float32)
+    op = np.zeros(n, np.float32)
+    oracle.plf_evaluate(OL.ctypes.byref(plf), n, OL.ptr(xs), OL.ptr(op))
+    return (np.float32(ds) * op).astype(np.float32)
+
+
+@pytest.mark.parametrize("shape,brick", [((20, 24, 28), 8), ((33, 17, 40), 4), ((16, 16, 16), 16), ((9, 10, 11), 1), ((40, 40, 40), 64)])
+def test_majorant_grid_device_bit_exact(env, oracle, shape, brick):
+    torch, lib, rt = env
+    vol = S.blob_volume(shape, n_blobs=5, seed=brick)
+    plf = C.make_plf([(0.0, 0.0), (300.0, 0.0), (1200.0, 0.7), (3000.5, 1.0)])
+    n = int(vol.max()) + 1
+    ds = 100.0
+    sig = sigma_table(oracle, plf, n, ds)
+    res = np.array([shape[2], shape[1], shape[0]], np.int32)
+    nb = [(int(r) + brick - 1) // brick for r in res]
+    want = np.zeros(nb[0] * nb[1] * nb[2], np.float32)
+    oracle.majorant_grid(OL.ptr(vol), OL.ptr(res), brick, OL.ptr(sig), n, ds, OL.ptr(want))
+    d_vol = torch.from_numpy(vol.view(np.int16).copy()).cuda()
+    d_sig = torch.from_numpy(sig).cuda()
+    d_out = torch.full((want.size,), -1.0, dtype=torch.float32, device="cuda")
+    C.check(lib.er_build_majorant_device(d_vol.data_ptr(), res.ctypes.data_as(OL.ctypes.POINTER(OL.ctypes.c_int32)), brick,
+                                         d_sig.data_ptr(), n, ds, d_out.data_ptr(), None))
+    torch.cuda.synchronize()
+    assert np.array_equal(bits(d_out.cpu().numpy()), bits(want))
+    assert want.max() > 0
