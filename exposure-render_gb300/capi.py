@@ -377,6 +377,8 @@ def _declare(lib) -> None:
         "er_gradient_magnitude": (c_int32, [c_int32, c_void_p, POINTER(c_float)]),
         "er_math_eval_device": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p]),
         "er_build_majorant_device": (c_int32, [c_void_p, POINTER(c_int32), c_int32, c_void_p, c_int32, c_float, c_void_p, c_void_p]),
+        "er_build_majorant_device_noalloc": (c_int32, [c_void_p, POINTER(c_int32), c_int32, c_void_p, c_int32, c_float, c_void_p,
+                                                       c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -35,4 +35,7 @@ cudaError_t er_launch_math_eval(int fn, int n, const float* x, const float* y, f
 cudaError_t er_launch_majorant(const uint16_t* vox, const int res[3], int B, const int nb[3], const float* sigma, int n,
                                float* rmq, int levels, uint32_t* minmax, float density_scale, float* majorant, cudaStream_t s);
 
+/* sets the text returned by er_last_error_message() on this thread */
+void er_internal_set_error(const char* message);
+
 #endif

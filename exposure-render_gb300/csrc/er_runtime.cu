@@ -506,6 +506,9 @@ er_status finish_display(TracerItem& t)
 
 }  // namespace
 
+/* last-error text for entry points implemented in other translation units */
+void er_internal_set_error(const char* message) { g_last_error = message ? message : ""; }
+
 /* ====================================================================== */
 /* C ABI                                                                    */
 /* ====================================================================== */

@@ -18,7 +18,9 @@
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <cstdio>
 
+#include "er_capi.h"
 #include "er_kernels.h"
 
 __global__ void k_brick_minmax(const uint16_t* __restrict__ vox, int rx, int ry, int rz, int B, int nbx, int nby, int nbz,
@@ -97,4 +99,128 @@ cudaError_t er_launch_majorant(const uint16_t* vox, const int res[3], int B, con
         k_rmq_level<<<(n + 255) / 256, 256, 0, s>>>(rmq + (size_t)(k - 1) * n, rmq + (size_t)k * n, n, 1 << (k - 1));
     k_majorant<<<(total + 255) / 256, 256, 0, s>>>(minmax, rmq, n, levels, density_scale, majorant, total);
     return cudaGetLastError();
+}
+
+/* ====================================================================== */
+/* Allocation-free majorant build                                           */
+/* ====================================================================== */
+/*
+ * Some callers cannot call cudaMalloc or cudaFree at the point where they
+ * need a majorant grid: an application that rebuilds the grid inside its
+ * frame loop (every edit of the opacity transfer function changes it), where
+ * cudaMalloc/cudaFree would synchronise the whole device and stall the
+ * frame; and hosts whose device memory is owned by their own pool allocator
+ * and forbid allocations behind its back.  er_build_majorant_device_noalloc
+ * serves them: the caller passes the inputs (voxels, sigma table) and the
+ * output grid, and the two scratch buffers of the build (per-brick voxel
+ * min/max, range-maximum table over the sigma table) live in the file-scope
+ * device arrays below instead of library allocations.
+ *
+ * Limits: at most ER_NOALLOC_MAX_BRICKS bricks (2^20: a 1024x1024x512 volume
+ * with 8^3 bricks) and ER_NOALLOC_MAX_SIGMA sigma entries (the full uint16
+ * range).  Together the arrays take 8.25 MiB of device memory on every GPU
+ * that loads the library, held until the process exits.
+ *
+ * Sharing: every call uses the same arrays, which keep the previous call's
+ * contents.  Nothing in them has to start at zero: each call writes every
+ * min/max entry and every range-table entry it reads before reading it.
+ * Calls that overlap on the GPU (for example on two streams at once) race on
+ * the arrays and must be serialised by the caller.
+ *
+ * Set-up: the first call on a device, with that device current, resolves the
+ * arrays' device addresses with cudaGetSymbolAddress (the host-side names of
+ * __device__ arrays are not device addresses).  Make that first call before
+ * any stream capture.
+ */
+#include <mutex>
+
+#define ER_NOALLOC_MAX_BRICKS (1u << 20)
+#define ER_NOALLOC_MAX_SIGMA 65536
+#define ER_NOALLOC_MAX_LEVELS 17
+
+static __device__ __align__(256) uint32_t g_noalloc_minmax[ER_NOALLOC_MAX_BRICKS];
+static __device__ __align__(256) float g_noalloc_rmq[ER_NOALLOC_MAX_LEVELS * ER_NOALLOC_MAX_SIGMA];
+
+namespace {
+
+struct NoallocScratch {
+    uint32_t* minmax;
+    float* rmq;
+    bool ready;
+};
+
+#define ER_NOALLOC_MAX_DEVICES 64
+std::mutex g_noalloc_mutex;
+NoallocScratch g_noalloc[ER_NOALLOC_MAX_DEVICES];
+
+/* device addresses of the scratch arrays on the current device (set up once) */
+cudaError_t noalloc_scratch(int device, NoallocScratch* out)
+{
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    NoallocScratch& s = g_noalloc[device];
+    if (!s.ready) {
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&a, g_noalloc_minmax);
+        if (e != cudaSuccess) return e;
+        e = cudaGetSymbolAddress(&b, g_noalloc_rmq);
+        if (e != cudaSuccess) return e;
+        s.minmax = (uint32_t*)a;
+        s.rmq = (float*)b;
+        s.ready = true;
+    }
+    *out = s;
+    return cudaSuccess;
+}
+
+er_status noalloc_fail(er_status st, const char* msg)
+{
+    er_internal_set_error(msg);
+    return st;
+}
+
+}  // namespace
+
+extern "C" ER_API er_status er_build_majorant_device_noalloc(const uint16_t* d_voxels, const int32_t resolution[3], int32_t brick,
+                                                             const float* d_sigma, int32_t sigma_count, float density_scale,
+                                                             float* d_majorant, void* stream)
+{
+    char msg[256];
+    if (!d_voxels || !resolution || !d_sigma || !d_majorant) return noalloc_fail(ER_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (brick < 1 || brick > 64) {
+        snprintf(msg, sizeof(msg), "brick %d out of range [1, 64]", brick);
+        return noalloc_fail(ER_ERR_INVALID_ARGUMENT, msg);
+    }
+    if (sigma_count < 1 || sigma_count > ER_NOALLOC_MAX_SIGMA) {
+        snprintf(msg, sizeof(msg), "sigma_count %d out of range [1, %d]", sigma_count, ER_NOALLOC_MAX_SIGMA);
+        return noalloc_fail(ER_ERR_INVALID_ARGUMENT, msg);
+    }
+    int res[3], nb[3];
+    for (int i = 0; i < 3; i++) {
+        if (resolution[i] <= 0) return noalloc_fail(ER_ERR_INVALID_ARGUMENT, "resolution must be positive");
+        res[i] = resolution[i];
+        nb[i] = (res[i] + brick - 1) / brick;
+    }
+    const unsigned long long total = (unsigned long long)nb[0] * nb[1] * nb[2];
+    if (total > ER_NOALLOC_MAX_BRICKS) {
+        snprintf(msg, sizeof(msg),
+                 "%llu bricks exceed the allocation-free limit of %u (use a larger brick or er_build_majorant_device)", total,
+                 ER_NOALLOC_MAX_BRICKS);
+        return noalloc_fail(ER_ERR_INVALID_ARGUMENT, msg);
+    }
+    int levels = 1;
+    while ((1 << levels) <= sigma_count) levels++;
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e == cudaSuccess && (device < 0 || device >= ER_NOALLOC_MAX_DEVICES)) return noalloc_fail(ER_ERR_INVALID_ARGUMENT, "device index out of range");
+    NoallocScratch s;
+    if (e == cudaSuccess) e = noalloc_scratch(device, &s);
+    if (e == cudaSuccess)
+        e = er_launch_majorant(d_voxels, res, brick, nb, d_sigma, sigma_count, s.rmq, levels, s.minmax, density_scale, d_majorant,
+                               (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+        snprintf(msg, sizeof(msg), "er_build_majorant_device_noalloc: %s", cudaGetErrorString(e));
+        return noalloc_fail(ER_ERR_CUDA, msg);
+    }
+    return ER_OK;
 }

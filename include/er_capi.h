@@ -371,6 +371,19 @@ ER_API er_status er_gradient_magnitude(int32_t volume_id, uint16_t* d_gm_or_null
 ER_API er_status er_build_majorant_device(const uint16_t* d_voxels, const int32_t resolution[3], int32_t brick, const float* d_sigma,
                                           int32_t sigma_count, float density_scale, float* d_majorant, void* stream);
 
+/* Allocation-free variant of er_build_majorant_device, for callers that
+   cannot allocate device memory where they rebuild the grid (inside a frame
+   loop, where cudaMalloc/cudaFree would synchronise the device, or under a
+   host-owned pool allocator).  Same arguments and result; the scratch lives
+   in static device arrays sized for at most 2^20 bricks and 65536 sigma
+   entries (8.25 MiB per GPU, held until exit); larger inputs are rejected
+   with ER_ERR_INVALID_ARGUMENT.  The first call on a device resolves the
+   arrays' addresses (make it before any stream capture); calls that overlap
+   on the GPU share the arrays and race.  No counterpart in the reference. */
+ER_API er_status er_build_majorant_device_noalloc(const uint16_t* d_voxels, const int32_t resolution[3], int32_t brick,
+                                                  const float* d_sigma, int32_t sigma_count, float density_scale, float* d_majorant,
+                                                  void* stream);
+
 /* Diagnostics: evaluates one include/er_math.h function on the GPU for n
    arguments (fn 0 log, 1 exp, 2 sin, 3 cos, 4 tan, 5 pow(x,y), 6 acos,
    7 atan2(x,y)); used to check that device and host produce the same bits.
