@@ -350,7 +350,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--film", type=int, default=0, help="square film edge (smaller profiling cases; 0 = the workload's)")
+    ap.add_argument("--spp", type=int, default=0, help="samples per pixel (0 = the workload's)")
     args = ap.parse_args()
+    if args.film or args.spp:
+        W = dict(WORKLOADS[args.workload])
+        if args.film:
+            W["film"] = (args.film, args.film)
+        if args.spp:
+            W["spp"] = args.spp
+        W["name"] = W["name"].split("-")[0] + "-%s-%dx%d-%dspp" % (W["name"].split("-")[1], W["film"][0], W["film"][1], W["spp"])
+        WORKLOADS[args.workload] = W
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

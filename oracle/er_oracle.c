@@ -26,6 +26,7 @@
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 /* ------------------------------------------------------------------ */
 /* small vector algebra (Source/vector.h:397-552)                       */
@@ -1456,7 +1457,8 @@ static void prepare_extensions(or_scene* s)
     s->gm_inv_max = 0.0f;
     s->gm_ready = 0;
     if (s->st.apply_shading_type && s->st.shading_type >= ER_SHADING_HYBRID && s->st.shading_type <= ER_SHADING_THRESHOLD) {
-        const float mx = gradient_magnitude_max_threaded(s, 8);
+        const long ncpu = sysconf(_SC_NPROCESSORS_ONLN);
+        const float mx = gradient_magnitude_max_threaded(s, ncpu > 0 ? (int)ncpu : 8);
         s->gm_inv_max = mx > 0.0f ? 1.0f / mx : 0.0f;
         s->gm_ready = 1;
     }
