@@ -167,7 +167,10 @@ class er_render_settings(Structure):
         ("bilateral_sigma_r", c_float),
         ("seed", c_uint32),
         ("majorant_brick", c_int32),
-        ("reserved", c_int32 * 5),
+        ("engine", c_int32),
+        ("tune_primary", c_int32),
+        ("tune_shadow", c_int32),
+        ("reserved", c_int32 * 2),
     ]
 
 

@@ -38,4 +38,20 @@ cudaError_t er_launch_majorant(const uint16_t* vox, const int res[3], int B, con
 /* sets the text returned by er_last_error_message() on this thread */
 void er_internal_set_error(const char* message);
 
+/* queues of the wavefront pipeline (er_wavefront.cu); max_samples bounds one chunk */
+struct WavefrontBuffers {
+    float4* results;     /* max_samples */
+    float4* events;      /* 5 * max_samples */
+    float4* jobs;        /* 6 * max_samples */
+    float4* partial;     /* film pixels */
+    uint32_t* counters;  /* 2 */
+    size_t max_samples;
+    int tune_primary;    /* resident blocks per SM targeted by the primary stage (1..4) */
+    int tune_shadow;     /* same for the shadow stage */
+};
+
+size_t er_wavefront_chunk_spp(int npix, int spp, size_t max_samples);
+cudaError_t er_launch_wavefront(const erd::Params& P, int spp, uint32_t view, uint32_t first, float4* sum, int accumulate,
+                                const WavefrontBuffers& B, cudaStream_t s);
+
 #endif

@@ -111,7 +111,11 @@ static __device__ __noinline__ v3 gradient_filtered(const Params& P, v3 p)
     return vlerp(G0, vlerp(L0, L1, 0.5f), 0.75f);
 }
 
-ER_D v3 normalized_gradient(const Params& P, v3 p)
+/* functions called once per path or per light are kept out of line, so the
+   free-flight loops do not carry their registers and code */
+#define ER_COLD static __device__ __noinline__
+
+ER_COLD v3 normalized_gradient(const Params& P, v3 p)
 {
     v3 g;
     if (P.gradient_mode == 1) g = gradient_cd(P, p);
@@ -229,7 +233,7 @@ ER_D void intersect_plane_inf(const Ray& R, int one_sided, Isect& I)
 
 ER_D float v2len(v2 a) { return sqrtf(a.x * a.x + a.y * a.y); }
 
-ER_D void intersect_shape(const Light& L, const Ray& R, Isect& I)
+ER_COLD void intersect_shape(const Light& L, const Ray& R, Isect& I)
 {
     switch (L.type) {
     case 0: {   /* Source/plane.h:76-88 */
@@ -387,7 +391,7 @@ ER_D void sample_light_surface(const Light& L, v3 UVW, Surf& SS)
 }
 
 /* EvaluateTexture - Source/textures.h:26-111 (procedural textures) */
-ER_D c3 evaluate_texture(const Params& P, int id, v2 UV)
+ER_COLD c3 evaluate_texture(const Params& P, int id, v2 UV)
 {
     if (id < 0 || id >= P.n_textures) return C3(0, 0, 0);
     const Texture& T = P.textures[id];

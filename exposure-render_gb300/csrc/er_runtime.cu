@@ -145,6 +145,9 @@ struct TracerItem {
     DevBuf<float> majorant, rmq;
     DevBuf<uint32_t> minmax;
     DevBuf<int> err;
+    /* wavefront queues */
+    DevBuf<float4> wf_results, wf_events, wf_jobs, wf_partial;
+    DevBuf<uint32_t> wf_counters;
     erd::Params P;
     uint64_t built_version = 0;
     bool built = false;
@@ -495,6 +498,33 @@ BilateralTables bilateral_tables(const er_render_settings& s)
     return T;
 }
 
+/* multi-sample transport: the wavefront stages (default) or the one-kernel path */
+er_status trace_sum(TracerItem& t, int spp, uint32_t view, uint32_t first, float4* sum, int accumulate, cudaStream_t s)
+{
+    if (t.d.settings.engine == 1) {
+        ER_CUDA(er_launch_trace_sum(t.P, spp, view, first, sum, accumulate, s));
+        return ER_OK;
+    }
+    const size_t npix = (size_t)t.W * t.H;
+    const size_t max_samples = npix * er_wavefront_chunk_spp((int)npix, spp, (size_t)8 << 20);
+    ER_CUDA(t.wf_results.ensure(max_samples));
+    ER_CUDA(t.wf_events.ensure(5 * max_samples));
+    ER_CUDA(t.wf_jobs.ensure(6 * max_samples));
+    ER_CUDA(t.wf_partial.ensure(npix));
+    ER_CUDA(t.wf_counters.ensure(2));
+    WavefrontBuffers B;
+    B.results = t.wf_results.p;
+    B.events = t.wf_events.p;
+    B.jobs = t.wf_jobs.p;
+    B.partial = t.wf_partial.p;
+    B.counters = t.wf_counters.p;
+    B.max_samples = max_samples;
+    B.tune_primary = t.d.settings.tune_primary > 0 ? t.d.settings.tune_primary : 4;
+    B.tune_shadow = t.d.settings.tune_shadow > 0 ? t.d.settings.tune_shadow : 4;
+    ER_CUDA(er_launch_wavefront(t.P, spp, view, first, sum, accumulate, B, s));
+    return ER_OK;
+}
+
 er_status finish_display(TracerItem& t)
 {
     if (t.d.settings.bilateral) {
@@ -791,7 +821,8 @@ ER_API er_status er_render_spp(int32_t tracer_id, int32_t spp)
     if (st != ER_OK) return st;
     cudaStream_t s = ctx().stream;
     const uint32_t first = (uint32_t)t->n_samples;
-    ER_CUDA(er_launch_trace_sum(t->P, spp, 0u, first, t->sum.p, t->n_samples > 0.0 ? 1 : 0, s));
+    st = trace_sum(*t, spp, 0u, first, t->sum.p, t->n_samples > 0.0 ? 1 : 0, s);
+    if (st != ER_OK) return st;
     t->n_samples += spp;
     const int filt = t->d.settings.frame_filter >= 0 ? 1 : 0;
     ER_CUDA(er_launch_post_mean(t->sum.p, (float)t->n_samples, t->running.p, t->display.p, t->W, t->H, t->d.camera.exposure, filt, s));
@@ -906,8 +937,7 @@ ER_API er_status er_trace_sum_device(int32_t tracer_id, int32_t spp, uint32_t vi
     if (!d_sum || spp <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "invalid sum buffer or spp");
     er_status st = build(*t);
     if (st != ER_OK) return st;
-    ER_CUDA(er_launch_trace_sum(t->P, spp, view, first_sample, (float4*)d_sum, accumulate, (cudaStream_t)stream));
-    return ER_OK;
+    return trace_sum(*t, spp, view, first_sample, (float4*)d_sum, accumulate, (cudaStream_t)stream);
 }
 
 ER_API er_status er_trace_frame_device(int32_t tracer_id, uint32_t* d_lanes, float* d_frame, void* stream)

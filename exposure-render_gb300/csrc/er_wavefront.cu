@@ -1,0 +1,351 @@
+/*
+ * er_wavefront.cu - the single-scattering estimator as a pipeline of small
+ * kernels (compiled with --fmad=false).
+ *
+ * The one-kernel path (k_trace_sum) inlines camera sampling, free flight,
+ * shading, light sampling, MIS and two shadow traversals into one kernel of
+ * 255 registers whose code does not fit the instruction cache; under ncu it
+ * runs 8 warps per SM with 11 of 32 lanes active.  Here each stage is its
+ * own kernel with its own register and code footprint:
+ *
+ *   k_wf_primary : MetroSample, SampleCamera, free flight, IntersectLights
+ *                  (Source/singlescattering.h:76-101).  Misses and light
+ *                  hits finish here; volume events go to the event queue.
+ *   k_wf_shade   : UniformSampleOneLight up to the shadow rays
+ *                  (Source/transport.h:115-156, :58-113): emission, light
+ *                  pick, shader selection, light sample, BSDF sample and its
+ *                  light hit.  The unoccluded contributions and the two
+ *                  shadow segments go to the shadow queue.
+ *   k_wf_shadow  : the shadow segments (march or ratio tracking) and the
+ *                  final sum of the sample.
+ *   k_wf_reduce  : per-pixel sum over the chunk's samples in sample order.
+ *
+ * Every RNG draw happens in the order of the one-kernel path (the RNG state
+ * travels with the queue records) and every float operation is the same, so
+ * the sums are bit-identical to k_trace_sum's and to the CPU oracle's.
+ *
+ * Queue records are arrays of float4 (five per event, six per shadow job):
+ * one 16-byte load or store per field group.  Queues are appended with
+ * warp-aggregated atomics; records carry their sample index, so results do
+ * not depend on the append order.
+ */
+#include "er_kernels.h"
+#include "er_path.cuh"
+
+using namespace erd;
+
+namespace {
+
+ER_D float u2f(uint32_t u) { return __uint_as_float(u); }
+ER_D uint32_t f2u(float f) { return __float_as_uint(f); }
+
+/* warp-aggregated slot in a queue for the lanes with `want` set */
+ER_D uint32_t queue_slot(bool want, uint32_t* counter)
+{
+    const unsigned mask = __ballot_sync(0xffffffffu, want);
+    uint32_t base = 0;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    if (mask && lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader < 0 ? 0 : leader);
+    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+}  // namespace
+
+/* ---- stage 1: camera ray, free flight, visible lights ---- */
+
+/* MINB: resident 256-thread blocks per SM the register allocation targets
+   (1: up to 255 registers, 2: 128, 3: 80, 4: 64); picked at run time */
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_wf_primary(const Params P, uint32_t view, uint32_t first, int spp_chunk, int npix,
+                                                    float4* __restrict__ results, float4* __restrict__ events,
+                                                    uint32_t* __restrict__ n_events)
+{
+    const int64_t total = (int64_t)spp_chunk * npix;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < total; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        const bool live = i < total;
+        bool push = false;
+        Event SE;
+        Metro ms;
+        Rng rng;
+        rng.s0 = 0u;
+        rng.s1 = 0u;
+        if (live) {
+            const int s = (int)(i / npix);
+            const int pix = (int)(i - (int64_t)s * npix);
+            const int x = pix % P.film[0], y = pix / P.film[0];
+            er_seed_lanes(P.seed, view, (uint32_t)pix, first + (uint32_t)s, &rng.s0, &rng.s1);
+            ms.large_step(rng);
+            const Ray R = sample_camera(P, x, y, ms.film_uv, ms.lens_uv);
+            Event se0, se1;
+            se0.type = 0; se0.valid = false; se0.T = 0.0f; se0.Le = C3(0, 0, 0);
+            se0.P = V3(0, 0, 0); se0.N = V3(0, 0, 0); se0.Wo = V3(0, 0, 0);
+            se1 = se0; se1.type = 1;
+            if (P.free_flight == 1) sample_volume_delta(P, R, rng, se0);
+            else sample_volume(P, R, rng, se0);
+            intersect_lights(P, R, se1, true);
+            SE = se0; SE.valid = false; SE.type = 0;
+            float T = FLT_MAX;
+            if (se0.valid && se0.T < T) { SE = se0; T = se0.T; }
+            if (se1.valid && se1.T < T) { SE = se1; T = se1.T; }
+            if (!SE.valid) {
+                results[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            } else if (SE.type == 1) {
+                const c3 Lv = cadd(C3(0, 0, 0), SE.Le);
+                results[i] = make_float4(Lv.r, Lv.g, Lv.b, 1.0f);
+            } else {
+                push = true;
+            }
+        }
+        const uint32_t slot = queue_slot(push, n_events);
+        if (push) {
+            float4* e = events + (size_t)slot * 5;
+            e[0] = make_float4(u2f((uint32_t)i), u2f(rng.s0), u2f(rng.s1), ms.light_num);
+            e[1] = make_float4(SE.P.x, SE.P.y, SE.P.z, ms.brdf_component);
+            e[2] = make_float4(SE.N.x, SE.N.y, SE.N.z, ms.brdf_dir.x);
+            e[3] = make_float4(SE.Wo.x, SE.Wo.y, SE.Wo.z, ms.brdf_dir.y);
+            e[4] = make_float4(ms.light_uvw.x, ms.light_uvw.y, ms.light_uvw.z, 0.0f);
+        }
+    }
+}
+
+/* ---- stage 2: shading up to the shadow segments ---- */
+
+/* flags of a shadow job */
+#define WF_RAY1 1u
+#define WF_RAY2 2u
+
+__global__ void __launch_bounds__(128) k_wf_shade(const Params P, const float4* __restrict__ events,
+                                                  const uint32_t* __restrict__ n_events, float4* __restrict__ results,
+                                                  float4* __restrict__ jobs, uint32_t* __restrict__ n_jobs)
+{
+    const uint32_t n = *n_events;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t e_i = base + threadIdx.x;
+        const bool live = e_i < n;
+        bool push = false;
+        uint32_t sample = 0, flags = 0;
+        Rng rng;
+        rng.s0 = 0u;
+        rng.s1 = 0u;
+        Event SE;
+        c3 Le = C3(0, 0, 0), c1 = C3(0, 0, 0), c2 = C3(0, 0, 0);
+        v3 S1 = V3(0, 0, 0), S2 = V3(0, 0, 0);
+        float count = 0.0f;
+        if (live) {
+            const float4* e = events + (size_t)e_i * 5;
+            const float4 e0 = e[0], e1 = e[1], e2 = e[2], e3 = e[3], e4 = e[4];
+            sample = f2u(e0.x);
+            rng.s0 = f2u(e0.y);
+            rng.s1 = f2u(e0.z);
+            Metro ms;
+            ms.light_num = e0.w;
+            ms.brdf_component = e1.w;
+            ms.brdf_dir.x = e2.w;
+            ms.brdf_dir.y = e3.w;
+            ms.light_uvw = V3(e4.x, e4.y, e4.z);
+            SE.type = 0; SE.valid = true; SE.T = 0.0f; SE.Le = C3(0, 0, 0);
+            SE.P = V3(e1.x, e1.y, e1.z);
+            SE.N = V3(e2.x, e2.y, e2.z);
+            SE.Wo = V3(e3.x, e3.y, e3.z);
+            /* UniformSampleOneLight - Source/transport.h:115-156 */
+            const float I = get_intensity(P, SE.P);
+            Le = cadd(C3(0, 0, 0), ctf_eval(P.tfs->emission, I));
+            bool early = P.light_count <= 0;
+            int idx = 0;
+            if (!early) {
+                idx = (int)floorf(ms.light_num * (float)P.light_count);
+                early = idx < 0 || idx >= P.light_count || !P.light_valid[idx];
+            }
+            if (early) {
+                const c3 Lv = cadd(C3(0, 0, 0), Le);
+                results[sample] = make_float4(Lv.r, Lv.g, Lv.b, 1.0f);
+            } else {
+                const Light& L = P.lights[idx];
+                Shader sh;
+                const int type = P.apply_shading_type ? select_shader_type(P, SE, I, rng) : 0;
+                shader_init(sh, type, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
+                            1000000.0f * er_powf(plf_eval(P.tfs->glossiness, I), 7.0f));
+                count = (float)P.light_count;
+                /* EstimateDirectLight - Source/transport.h:58-113, without the visibility terms */
+                v3 Wi;
+                c3 Li;
+                Surf SS;
+                sample_light(P, L, ms.light_uvw, SS, SE, Wi, Li);
+                const c3 F = shader_f(sh, SE.Wo, Wi);
+                const bool full = P.mis == 1;
+                const float BsdfPdf = full ? mis_bsdf_pdf(sh, SE.Wo, Wi) : shader_pdf(sh, SE.Wo, Wi);
+                if (!cblack(Li) && !cblack(F) && BsdfPdf > 0.0f) {
+                    const float LightPdf = vlen2(vsub(SE.P, SS.P)) / (vabsdot(SS.N, vneg(Wi)) * L.area);
+                    if (full) {
+                        const float w = power_heuristic(LightPdf, BsdfPdf);
+                        c1 = cscale(cmul(F, Li), sh.type == 0 ? vabsdot(Wi, SE.N) * w / LightPdf : w / LightPdf);
+                    } else if (sh.type == 0) {
+                        c1 = cscale(cmul(F, Li), vabsdot(Wi, SE.N) * power_heuristic(LightPdf, BsdfPdf) / LightPdf);
+                    } else {
+                        c1 = cdivs(cmul(F, Li), LightPdf);
+                    }
+                    S1 = SS.P;
+                    flags |= WF_RAY1;
+                }
+                if (full) {
+                    const v3 Wb = sample_bsdf_dir(sh, SE.Wo, ms);
+                    const c3 Fb = shader_f(sh, SE.Wo, Wb);
+                    const float pb = mis_bsdf_pdf(sh, SE.Wo, Wb);
+                    if (!cblack(Fb) && pb > 0.0f) {
+                        Ray R2;
+                        R2.O = SE.P;
+                        R2.D = Wb;
+                        R2.MinT = 0.0f;
+                        R2.MaxT = 1000000.0f;
+                        Event SE2;
+                        SE2.type = 1; SE2.valid = false; SE2.T = 0.0f; SE2.Le = C3(0, 0, 0);
+                        SE2.P = V3(0, 0, 0); SE2.N = V3(0, 0, 0); SE2.Wo = V3(0, 0, 0);
+                        int hit = -1;
+                        intersect_lights_slot(P, R2, SE2, false, hit);
+                        if (SE2.valid && P.light_ids[hit] == P.light_ids[idx] && !cblack(SE2.Le)) {
+                            const float LightPdf = vlen2(vsub(SE.P, SE2.P)) / (vabsdot(SE2.N, vneg(Wb)) * L.area);
+                            const float w = power_heuristic(pb, LightPdf);
+                            c2 = cscale(cmul(Fb, SE2.Le), sh.type == 0 ? vabsdot(Wb, SE.N) * w / pb : w / pb);
+                            S2 = SE2.P;
+                            flags |= WF_RAY2;
+                        }
+                    }
+                }
+                if (flags == 0) {
+                    const c3 Lv = cadd(C3(0, 0, 0), cscale(cadd(Le, C3(0, 0, 0)), count));
+                    results[sample] = make_float4(Lv.r, Lv.g, Lv.b, 1.0f);
+                } else {
+                    push = true;
+                }
+            }
+        }
+        const uint32_t slot = queue_slot(push, n_jobs);
+        if (push) {
+            float4* j = jobs + (size_t)slot * 6;
+            j[0] = make_float4(u2f(sample), u2f(rng.s0), u2f(rng.s1), u2f(flags));
+            j[1] = make_float4(SE.P.x, SE.P.y, SE.P.z, count);
+            j[2] = make_float4(S1.x, S1.y, S1.z, Le.r);
+            j[3] = make_float4(c1.r, c1.g, c1.b, Le.g);
+            j[4] = make_float4(S2.x, S2.y, S2.z, Le.b);
+            j[5] = make_float4(c2.r, c2.g, c2.b, 0.0f);
+        }
+    }
+}
+
+/* ---- stage 3: shadow segments and the sample's sum ---- */
+
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_wf_shadow(const Params P, const float4* __restrict__ jobs, const uint32_t* __restrict__ n_jobs,
+                                                   float4* __restrict__ results)
+{
+    const uint32_t n = *n_jobs;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const bool ref_mode = P.mis != 1 && P.free_flight != 1;
+    for (uint32_t j_i = blockIdx.x * blockDim.x + threadIdx.x; j_i < n; j_i += stride) {
+        const float4* j = jobs + (size_t)j_i * 6;
+        const float4 j0 = j[0], j1 = j[1], j2 = j[2], j3 = j[3], j4 = j[4], j5 = j[5];
+        const uint32_t sample = f2u(j0.x);
+        Rng rng;
+        rng.s0 = f2u(j0.y);
+        rng.s1 = f2u(j0.z);
+        const uint32_t flags = f2u(j0.w);
+        const v3 Pp = V3(j1.x, j1.y, j1.z);
+        const float count = j1.w;
+        const c3 Le = C3(j2.w, j3.w, j4.w);
+        c3 dl = C3(0, 0, 0);
+        if (flags & WF_RAY1) {
+            const float Tr = visibility(P, Pp, V3(j2.x, j2.y, j2.z), rng);
+            if (Tr > 0.0f) {
+                const c3 c1 = C3(j3.x, j3.y, j3.z);
+                dl = ref_mode ? cadd(dl, c1) : cadd(dl, cscale(c1, Tr));
+            }
+        }
+        if (flags & WF_RAY2) {
+            const float Tr = visibility(P, Pp, V3(j4.x, j4.y, j4.z), rng);
+            if (Tr > 0.0f) dl = cadd(dl, cscale(C3(j5.x, j5.y, j5.z), Tr));
+        }
+        const c3 Lv = cadd(C3(0, 0, 0), cscale(cadd(Le, dl), count));
+        results[sample] = make_float4(Lv.r, Lv.g, Lv.b, 1.0f);
+    }
+}
+
+/* ---- stage 4: per-pixel sum in sample order ---- */
+
+__global__ void k_wf_reduce(const float4* __restrict__ results, int spp_chunk, int npix, float4* __restrict__ partial, int first_chunk,
+                            int last_chunk, float4* __restrict__ sum, int accumulate)
+{
+    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= npix) return;
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+    if (!first_chunk) {
+        const float4 p = partial[pix];
+        a0 = p.x; a1 = p.y; a2 = p.z; a3 = p.w;
+    }
+    for (int s = 0; s < spp_chunk; s++) {
+        const float4 o = results[(size_t)s * npix + pix];
+        a0 += o.x; a1 += o.y; a2 += o.z; a3 += o.w;
+    }
+    if (!last_chunk) {
+        partial[pix] = make_float4(a0, a1, a2, a3);
+        return;
+    }
+    float4 r = make_float4(a0, a1, a2, a3);
+    if (accumulate) {
+        const float4 q = sum[pix];
+        r = make_float4(q.x + a0, q.y + a1, q.z + a2, q.w + a3);
+    }
+    sum[pix] = r;
+}
+
+/* ---- launcher ---- */
+
+size_t er_wavefront_chunk_spp(int npix, int spp, size_t max_samples)
+{
+    size_t s = max_samples / (size_t)(npix > 0 ? npix : 1);
+    if (s < 1) s = 1;
+    if (s > (size_t)spp) s = (size_t)spp;
+    return s;
+}
+
+cudaError_t er_launch_wavefront(const Params& P, int spp, uint32_t view, uint32_t first, float4* sum, int accumulate,
+                                const WavefrontBuffers& B, cudaStream_t s)
+{
+    const int npix = P.film[0] * P.film[1];
+    const int chunk = (int)er_wavefront_chunk_spp(npix, spp, B.max_samples);
+    int sm = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+    if (sm <= 0) sm = 132;
+    for (int done = 0; done < spp; done += chunk) {
+        const int c = (spp - done) < chunk ? (spp - done) : chunk;
+        cudaError_t e = cudaMemsetAsync(B.counters, 0, 2 * sizeof(uint32_t), s);
+        if (e != cudaSuccess) return e;
+        const int64_t total = (int64_t)c * npix;
+        const int g1 = (int)((total + 255) / 256 < (int64_t)sm * 64 ? (total + 255) / 256 : (int64_t)sm * 64);
+        const uint32_t f = first + (uint32_t)done;
+        switch (B.tune_primary) {
+        case 2: k_wf_primary<2><<<g1, 256, 0, s>>>(P, view, f, c, npix, B.results, B.events, B.counters); break;
+        case 3: k_wf_primary<3><<<g1, 256, 0, s>>>(P, view, f, c, npix, B.results, B.events, B.counters); break;
+        case 6: k_wf_primary<6><<<g1, 256, 0, s>>>(P, view, f, c, npix, B.results, B.events, B.counters); break;
+        case 8: k_wf_primary<8><<<g1, 256, 0, s>>>(P, view, f, c, npix, B.results, B.events, B.counters); break;
+        default: k_wf_primary<4><<<g1, 256, 0, s>>>(P, view, f, c, npix, B.results, B.events, B.counters); break;
+        }
+        k_wf_shade<<<sm * 16, 128, 0, s>>>(P, B.events, B.counters, B.results, B.jobs, B.counters + 1);
+        switch (B.tune_shadow) {
+        case 2: k_wf_shadow<2><<<sm * 8, 256, 0, s>>>(P, B.jobs, B.counters + 1, B.results); break;
+        case 3: k_wf_shadow<3><<<sm * 8, 256, 0, s>>>(P, B.jobs, B.counters + 1, B.results); break;
+        case 6: k_wf_shadow<6><<<sm * 8, 256, 0, s>>>(P, B.jobs, B.counters + 1, B.results); break;
+        case 8: k_wf_shadow<8><<<sm * 8, 256, 0, s>>>(P, B.jobs, B.counters + 1, B.results); break;
+        default: k_wf_shadow<4><<<sm * 8, 256, 0, s>>>(P, B.jobs, B.counters + 1, B.results); break;
+        }
+        k_wf_reduce<<<(npix + 255) / 256, 256, 0, s>>>(B.results, c, npix, B.partial, done == 0, done + c >= spp, sum, accumulate);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}

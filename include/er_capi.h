@@ -214,7 +214,11 @@ typedef struct er_render_settings {
     float bilateral_sigma_r;      /* range sigma in 0..255 luminance units for GaussSimilarity[] */
     uint32_t seed;                /* counter-based seed of the per-pixel RNG lanes */
     int32_t majorant_brick;       /* delta tracking: edge of the cubic voxel bricks of the majorant grid (0 means 8) */
-    int32_t reserved[5];
+    int32_t engine;               /* multi-sample launches: 0 auto (wavefront), 1 one-kernel path, 2 wavefront stages */
+    int32_t tune_primary;         /* wavefront: resident 256-thread blocks per SM the free-flight stage is compiled for:
+                                     2, 3, 4, 6 or 8 (0 or other values: 4) */
+    int32_t tune_shadow;          /* wavefront: same for the shadow stage (0 or other values: 4) */
+    int32_t reserved[2];
 } er_render_settings;
 
 /* ErTracer (Source/ertracer.h:33-117).  light_ids/object_ids/clipping_ids are
