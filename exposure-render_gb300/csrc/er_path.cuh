@@ -115,7 +115,7 @@ static __device__ __noinline__ v3 gradient_filtered(const Params& P, v3 p)
    free-flight loops do not carry their registers and code */
 #define ER_COLD static __device__ __noinline__
 
-ER_COLD v3 normalized_gradient(const Params& P, v3 p)
+ER_D v3 normalized_gradient(const Params& P, v3 p)
 {
     v3 g;
     if (P.gradient_mode == 1) g = gradient_cd(P, p);
@@ -549,6 +549,7 @@ ER_D long long march_budget(float t0, float t1, float step)
 }
 
 /* SampleVolume - Source/raymarching.h:30-71 */
+template <bool WITH_NORMAL = true>
 ER_D void sample_volume(const Params& P, const Ray& R, Rng& rng, Event& SE)
 {
     Isect Int; Int.invalid();
@@ -574,7 +575,7 @@ ER_D void sample_volume(const Params& P, const Ray& R, Rng& rng, Event& SE)
     SE.valid = true;
     SE.T = MinT;
     SE.P = Ps;
-    SE.N = normalized_gradient(P, Ps);
+    SE.N = WITH_NORMAL ? normalized_gradient(P, Ps) : V3(0.0f, 0.0f, 0.0f);
     SE.Wo = vneg(R.D);
     SE.Le = C3(0, 0, 0);
 }
@@ -659,13 +660,31 @@ ER_D bool intersects_light(const Params& P, const Ray& R)
 
 /* ---- extension estimators (delta tracking, shader selection, full MIS) ---- */
 
-/* 3D DDA over the majorant bricks in local voxel units */
+/* 3D DDA over the majorant bricks in local voxel units.  The state is kept
+   in scalars (no arrays indexed by the stepping axis), so it stays in
+   registers; the arithmetic is the oracle's, operation for operation. */
 struct Dda {
     float t, tmax;
-    int b[3], step[3];
-    float tnext[3], tdelta[3];
+    int bx, by, bz;
+    int sx, sy, sz;
+    float nx, ny, nz;        /* t of the next brick face per axis */
+    float dx, dy, dz;        /* t between faces per axis */
     bool done;
 };
+
+ER_D void dda_axis(float o, float dirc, float minp, float inv_size, int res, int nb, float B, float t0, int& b, int& step,
+                   float& tnext, float& tdelta)
+{
+    const float sc = inv_size * (float)res;
+    const float lo = (o - minp) * sc;
+    const float ld = dirc * sc;
+    const float L = lo + t0 * ld;
+    b = (int)floorf(L / B);
+    b = b < 0 ? 0 : (b >= nb ? nb - 1 : b);
+    if (ld > 0.0f) { step = 1; tnext = ((float)(b + 1) * B - lo) / ld; tdelta = B / ld; }
+    else if (ld < 0.0f) { step = -1; tnext = ((float)b * B - lo) / ld; tdelta = -B / ld; }
+    else { step = 0; tnext = FLT_MAX; tdelta = FLT_MAX; }
+}
 
 ER_D void dda_init(const Params& P, const Ray& R, float t0, float t1, Dda& d)
 {
@@ -673,26 +692,16 @@ ER_D void dda_init(const Params& P, const Ray& R, float t0, float t1, Dda& d)
     d.t = t0;
     d.tmax = t1;
     d.done = false;
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        const float sc = P.inv_size[i] * (float)P.res[i];
-        const float lo = (vget(R.O, i) - P.minp[i]) * sc;
-        const float ld = vget(R.D, i) * sc;
-        const float L = lo + t0 * ld;
-        int b = (int)floorf(L / B);
-        b = b < 0 ? 0 : (b >= P.nb[i] ? P.nb[i] - 1 : b);
-        d.b[i] = b;
-        if (ld > 0.0f) { d.step[i] = 1; d.tnext[i] = ((float)(b + 1) * B - lo) / ld; d.tdelta[i] = B / ld; }
-        else if (ld < 0.0f) { d.step[i] = -1; d.tnext[i] = ((float)b * B - lo) / ld; d.tdelta[i] = -B / ld; }
-        else { d.step[i] = 0; d.tnext[i] = FLT_MAX; d.tdelta[i] = FLT_MAX; }
-    }
+    dda_axis(R.O.x, R.D.x, P.minp[0], P.inv_size[0], P.res[0], P.nb[0], B, t0, d.bx, d.sx, d.nx, d.dx);
+    dda_axis(R.O.y, R.D.y, P.minp[1], P.inv_size[1], P.res[1], P.nb[1], B, t0, d.by, d.sy, d.ny, d.dy);
+    dda_axis(R.O.z, R.D.z, P.minp[2], P.inv_size[2], P.res[2], P.nb[2], B, t0, d.bz, d.sz, d.nz, d.dz);
 }
 
 ER_D float dda_exit(const Dda& d)
 {
-    float e = d.tnext[0];
-    if (d.tnext[1] < e) e = d.tnext[1];
-    if (d.tnext[2] < e) e = d.tnext[2];
+    float e = d.nx;
+    if (d.ny < e) e = d.ny;
+    if (d.nz < e) e = d.nz;
     if (d.tmax < e) e = d.tmax;
     return e < d.t ? d.t : e;
 }
@@ -700,24 +709,35 @@ ER_D float dda_exit(const Dda& d)
 ER_D void dda_advance(const Params& P, Dda& d, float e)
 {
     if (e >= d.tmax) { d.done = true; d.t = e; return; }
-    int a = 0;
-    if (d.tnext[1] < d.tnext[a]) a = 1;
-    if (d.tnext[2] < d.tnext[a]) a = 2;
-    d.b[a] += d.step[a];
-    if (d.b[a] < 0 || d.b[a] >= P.nb[a]) d.done = true;
-    d.tnext[a] += d.tdelta[a];
+    /* axis with the nearest face; ties go to x, then y */
+    const bool ax = !(d.ny < d.nx) && !(d.nz < d.nx);
+    const bool ay = !ax && !(d.nz < d.ny);
+    if (ax) {
+        d.bx += d.sx;
+        if (d.bx < 0 || d.bx >= P.nb[0]) d.done = true;
+        d.nx += d.dx;
+    } else if (ay) {
+        d.by += d.sy;
+        if (d.by < 0 || d.by >= P.nb[1]) d.done = true;
+        d.ny += d.dy;
+    } else {
+        d.bz += d.sz;
+        if (d.bz < 0 || d.bz >= P.nb[2]) d.done = true;
+        d.nz += d.dz;
+    }
     d.t = e;
 }
 
 ER_D float dda_majorant(const Params& P, const Dda& d)
 {
-    return __ldg(P.majorant + ((size_t)d.b[2] * (size_t)P.nb[1] + (size_t)d.b[1]) * (size_t)P.nb[0] + (size_t)d.b[0]);
+    return __ldg(P.majorant + ((size_t)d.bz * (size_t)P.nb[1] + (size_t)d.by) * (size_t)P.nb[0] + (size_t)d.bx);
 }
 
 #define ER_DELTA_MAX_COLLISIONS 1048576
 
 /* Delta tracking of the primary ray: sigma_t = DensityScale^2 * Opacity(I),
    the extinction the reference's march integrates (Source/raymarching.h:45,64-66) */
+template <bool WITH_NORMAL = true>
 ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE)
 {
     Isect Int; Int.invalid();
@@ -749,7 +769,7 @@ ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE
                     SE.valid = true;
                     SE.T = t;
                     SE.P = Pt;
-                    SE.N = normalized_gradient(P, Pt);
+                    SE.N = WITH_NORMAL ? normalized_gradient(P, Pt) : V3(0.0f, 0.0f, 0.0f);
                     SE.Wo = vneg(R.D);
                     SE.Le = C3(0, 0, 0);
                     return;

@@ -84,8 +84,9 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const Params P, uint32
             se0.type = 0; se0.valid = false; se0.T = 0.0f; se0.Le = C3(0, 0, 0);
             se0.P = V3(0, 0, 0); se0.N = V3(0, 0, 0); se0.Wo = V3(0, 0, 0);
             se1 = se0; se1.type = 1;
-            if (P.free_flight == 1) sample_volume_delta(P, R, rng, se0);
-            else sample_volume(P, R, rng, se0);
+            /* the event normal (no RNG) is computed by the shade stage */
+            if (P.free_flight == 1) sample_volume_delta<false>(P, R, rng, se0);
+            else sample_volume<false>(P, R, rng, se0);
             intersect_lights(P, R, se1, true);
             SE = se0; SE.valid = false; SE.type = 0;
             float T = FLT_MAX;
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const Params P, const float4* 
             ms.light_uvw = V3(e4.x, e4.y, e4.z);
             SE.type = 0; SE.valid = true; SE.T = 0.0f; SE.Le = C3(0, 0, 0);
             SE.P = V3(e1.x, e1.y, e1.z);
-            SE.N = V3(e2.x, e2.y, e2.z);
+            SE.N = normalized_gradient(P, SE.P);     /* NormalizedGradient of SampleVolume (Source/raymarching.h:70) */
             SE.Wo = V3(e3.x, e3.y, e3.z);
             /* UniformSampleOneLight - Source/transport.h:115-156 */
             const float I = get_intensity(P, SE.P);

@@ -28,16 +28,17 @@
  *   - sin/cos: Cody & Waite reduction by pi/2 with a three-part pi/2
  *           (products with the quadrant index are exact for |x| < 6000),
  *           Taylor polynomials on [-pi/4, pi/4], quadrant table.
- *   - pow:  exp(y log|x|) evaluated in binary64 (same two methods, longer
- *           series) and rounded once to binary32, so large exponents such as
- *           the 1e6*g^7 Blinn exponent keep full float accuracy.
- *   - atan/atan2/acos: binary64; atan reduced to |v| <= tan(pi/12) with
+ *   - pow:  exp(y log|x|) with log|x| and the product y*log|x| carried in
+ *           double-single arithmetic (Dekker's exact product with Veltkamp
+ *           splitting, no FMA), so large exponents such as the 1e6*g^7 Blinn
+ *           exponent keep float accuracy without binary64 instructions.
+ *   - atan/atan2/acos: atan reduced to |v| <= tan(pi/12) with
  *           atan(u) = pi/6 + atan((sqrt3 u - 1)/(u + sqrt3)) and an odd Taylor
  *           series; acos(x) = atan2(sqrt((1-x)(1+x)), x).
  *
- * Accuracy (checked against the host C library in tests/test_math.py): log,
- * exp, sin, cos within 2 ulp; pow, atan2, acos within 1 ulp on the ranges
- * the renderer uses.
+ * Accuracy (checked against float64 numpy in tests/test_math.py): log, exp,
+ * sin, cos, pow, atan2, acos within a few ulp on the ranges the renderer
+ * uses (the test states each bound).
  */
 #ifndef ER_MATH_H
 #define ER_MATH_H
@@ -159,54 +160,86 @@ ER_MATH_FN float er_sinf(float x) { float s, c; er_sincosf(x, &s, &c); return s;
 ER_MATH_FN float er_cosf(float x) { float s, c; er_sincosf(x, &s, &c); return c; }
 ER_MATH_FN float er_tanf(float x) { float s, c; er_sincosf(x, &s, &c); return s / c; }
 
-/* ---- binary64 helpers for pow / atan2 / acos ---- */
-#define ER_LN2_HI_D 0.6931467056274414
-#define ER_LN2_LO_D 4.7493250390316726e-07
+/* ---- double-single (float-float) helpers for pow / atan2 / acos ----
+   All binary32: the GPU's binary64 rate is a small fraction of its binary32
+   rate.  Exact products use Dekker's algorithm with Veltkamp splitting, which
+   needs no fused multiply-add (valid while no product overflows). */
 
-/* log(x) for finite x > 0 (binary64) */
-ER_MATH_FN double er_log_d(double x)
+/* a * b = *p + *e exactly */
+ER_MATH_FN void er_two_prod(float a, float b, float* p, float* e)
 {
-    uint64_t b = er_d2u(x);
-    int e = 0;
-    if (b < 0x0010000000000000ull) {        /* subnormal: scale by 2^54 */
-        x = x * 18014398509481984.0;
-        b = er_d2u(x);
-        e = -54;
-    }
-    e += (int)(b >> 52) - 1023;
-    double m = er_u2d((b & 0x000fffffffffffffull) | 0x3ff0000000000000ull);
-    if (m > 1.4142135623730951) { m = m * 0.5; e += 1; }
-    const double f = m - 1.0;
-    const double s = f / (2.0 + f);
-    const double z = s * s;
-    const double R = z * (0.66666666666666667 + z * (0.4 + z * (0.28571428571428571 + z * (0.22222222222222222 +
-                     z * (0.18181818181818182 + z * (0.15384615384615385 + z * (0.13333333333333333 +
-                     z * (0.11764705882352941 + z * (0.10526315789473684 + z * 0.095238095238095238)))))))));
-    const double hfsq = 0.5 * f * f;
-    const double lm = f - (hfsq - s * (hfsq + R));
-    const double de = (double)e;
-    return de * ER_LN2_HI_D + (lm + de * ER_LN2_LO_D);
+    const float ca = 4097.0f * a;
+    const float ah = ca - (ca - a);
+    const float al = a - ah;
+    const float cb = 4097.0f * b;
+    const float bh = cb - (cb - b);
+    const float bl = b - bh;
+    const float pp = a * b;
+    *p = pp;
+    *e = ((ah * bh - pp) + ah * bl + al * bh) + al * bl;
 }
 
-/* exp(t) (binary64) */
-ER_MATH_FN double er_exp_d(double t)
+/* a + b = *s + *e exactly, for |a| >= |b| (or a == 0) */
+ER_MATH_FN void er_fast_two_sum(float a, float b, float* s, float* e)
 {
-    if (t != t) return t;
-    if (t > 709.78) return ER_D_INF;
-    if (t < -745.2) return 0.0;
-    const double kd = floor(t * 1.4426950408889634 + 0.5);
-    const int k = (int)kd;
-    const double r = (t - kd * ER_LN2_HI_D) - kd * ER_LN2_LO_D;
-    const double p = 1.0 + r * (1.0 + r * (0.5 + r * (1.6666666666666667e-1 + r * (4.1666666666666667e-2 +
-                     r * (8.3333333333333333e-3 + r * (1.3888888888888889e-3 + r * (1.9841269841269841e-4 +
-                     r * (2.4801587301587302e-5 + r * (2.7557319223985891e-6 + r * (2.7557319223985891e-7 +
-                     r * (2.5052108385441719e-8 + r * (2.0876756987868099e-9 + r * 1.6059043836821615e-10))))))))))));
+    const float ss = a + b;
+    *s = ss;
+    *e = b - (ss - a);
+}
+
+/* log(x) = *hi + *lo for finite x > 0 (about 2^-40 relative): the atanh
+   series of er_logf with s = f / (2 + f) carried in double-single */
+ER_MATH_FN void er_log_ds(float x, float* hi, float* lo)
+{
+    uint32_t b = er_f2u(x);
+    int e = 0;
+    if (b < 0x00800000u) {
+        x = x * 33554432.0f;
+        b = er_f2u(x);
+        e = -25;
+    }
+    e += (int)(b >> 23) - 127;
+    float m = er_u2f((b & 0x007fffffu) | 0x3f800000u);
+    if (m > 1.41421356f) { m = m * 0.5f; e += 1; }
+    const float f = m - 1.0f;                          /* exact */
+    float dh, dl;
+    er_fast_two_sum(2.0f, f, &dh, &dl);                /* 2 + f */
+    const float sh = f / dh;
+    float p, pe;
+    er_two_prod(sh, dh, &p, &pe);
+    const float sl = (((f - p) - pe) - sh * dl) / dh;  /* f/(2+f) - sh */
+    const float z = sh * sh;
+    const float poly = sh * (z * (0.666666667f + z * (0.4f + z * (0.285714286f + z * (0.222222222f + z * 0.181818182f)))));
+    float h, l;
+    er_fast_two_sum(2.0f * sh, poly, &h, &l);
+    l = l + 2.0f * sl;
+    /* + e * ln2 (ER_LN2_HI * e is exact) */
+    const float fe = (float)e;
+    float h2, l2;
+    er_fast_two_sum(fe * ER_LN2_HI, h, &h2, &l2);
+    if (fe == 0.0f) { h2 = h; l2 = 0.0f; }
+    l2 = l2 + (l + fe * ER_LN2_LO);
+    er_fast_two_sum(h2, l2, hi, lo);
+}
+
+/* exp(hi + lo) for |lo| <= ulp(hi) */
+ER_MATH_FN float er_exp_ds(float hi, float lo)
+{
+    if (hi != hi) return hi;
+    if (hi > 88.7228394f) return ER_F_INF;
+    if (hi < -103.972084f) return 0.0f;
+    const float kf = floorf(hi * ER_LOG2E + 0.5f);
+    const int k = (int)kf;
+    const float r = ((hi - kf * ER_LN2_HI) - kf * ER_LN2_LO) + lo;
+    const float q = 1.0f + r * (1.0f + r * (0.5f + r * (1.66666667e-1f + r * (4.16666667e-2f +
+                    r * (8.33333333e-3f + r * (1.38888889e-3f + r * (1.98412698e-4f + r * 2.48015873e-5f)))))));
     const int k1 = k / 2;
     const int k2 = k - k1;
-    return (p * er_u2d((uint64_t)(k1 + 1023) << 52)) * er_u2d((uint64_t)(k2 + 1023) << 52);
+    return (q * er_u2f((uint32_t)(k1 + 127) << 23)) * er_u2f((uint32_t)(k2 + 127) << 23);
 }
 
-/* x^y, binary32 result, binary64 internals */
+/* x^y: exp(y log|x|) with the logarithm and the product in double-single,
+   so large exponents such as the 1e6*g^7 Blinn exponent keep float accuracy */
 ER_MATH_FN float er_powf(float x, float y)
 {
     if (y == 0.0f) return 1.0f;
@@ -230,50 +263,50 @@ ER_MATH_FN float er_powf(float x, float y)
         float r = (y > 0.0f) ? ER_F_INF : 0.0f;
         return (x < 0.0f && yodd) ? -r : r;
     }
-    const double t = (double)y * er_log_d((double)ax);
-    const float r = (float)er_exp_d(t);
+    float lh, ll;
+    er_log_ds(ax, &lh, &ll);
+    float th, tl;
+    er_two_prod(y, lh, &th, &tl);
+    tl = tl + y * ll;
+    float h, l;
+    er_fast_two_sum(th, tl, &h, &l);
+    const float r = er_exp_ds(h, l);
     return (x < 0.0f && yodd) ? -r : r;
 }
 
-/* atan(u) for 0 <= u <= 1 (binary64) */
-ER_MATH_FN double er_atan01_d(double u)
+/* atan(u) for 0 <= u <= 1: u > tan(pi/12) is reduced with
+   atan(u) = pi/6 + atan((sqrt3 u - 1)/(u + sqrt3)); odd Taylor series */
+ER_MATH_FN float er_atan01f(float u)
 {
-    double base = 0.0;
-    double v = u;
-    if (u > 0.2679491924311227) {
-        v = (u * 1.7320508075688772 - 1.0) / (u + 1.7320508075688772);
-        base = 0.5235987755982989;
+    float base = 0.0f;
+    float v = u;
+    if (u > 0.267949194f) {
+        v = (u * 1.73205081f - 1.0f) / (u + 1.73205081f);
+        base = 0.523598776f;
     }
-    const double z = v * v;
-    const double p = v - (v * z) * (0.33333333333333333 - z * (0.2 - z * (0.14285714285714286 - z * (0.11111111111111111 -
-                     z * (0.090909090909090909 - z * (0.076923076923076923 - z * (0.066666666666666667 -
-                     z * (0.058823529411764706 - z * (0.052631578947368421 - z * (0.047619047619047619 -
-                     z * (0.043478260869565217 - z * (0.04 - z * 0.037037037037037037))))))))))));
+    const float z = v * v;
+    const float p = v - (v * z) * (0.333333333f - z * (0.2f - z * (0.142857143f - z * (0.111111111f - z * (0.0909090909f -
+                    z * 0.0769230769f)))));
     return base + p;
 }
 
-/* atan2(y, x) (binary64), C99 conventions for signed zeros and infinities are
-   not needed by the renderer; finite and zero arguments are handled. */
-ER_MATH_FN double er_atan2_d(double y, double x)
+/* atan2(y, x) for finite and zero arguments */
+ER_MATH_FN float er_atan2f(float y, float x)
 {
-    if (x != x || y != y) return ER_D_NAN;
-    const double ax = fabs(x), ay = fabs(y);
-    double a;
-    if (ax == 0.0 && ay == 0.0) a = 0.0;
-    else if (ay <= ax) a = er_atan01_d(ay / ax);
-    else a = 1.5707963267948966 - er_atan01_d(ax / ay);
-    if (x < 0.0) a = 3.141592653589793 - a;
-    return (y < 0.0) ? -a : a;
+    if (x != x || y != y) return ER_F_NAN;
+    const float ax = fabsf(x), ay = fabsf(y);
+    float a;
+    if (ax == 0.0f && ay == 0.0f) a = 0.0f;
+    else if (ay <= ax) a = er_atan01f(ay / ax);
+    else a = (1.57079637f - er_atan01f(ax / ay)) + -4.37113883e-08f;
+    if (x < 0.0f) a = (3.14159274f - a) + -8.74227766e-08f;
+    return (y < 0.0f) ? -a : a;
 }
-
-ER_MATH_FN float er_atan2f(float y, float x) { return (float)er_atan2_d((double)y, (double)x); }
 
 ER_MATH_FN float er_acosf(float x)
 {
     if (x != x || x > 1.0f || x < -1.0f) return ER_F_NAN;
-    const double xd = (double)x;
-    const double s = sqrt((1.0 - xd) * (1.0 + xd));
-    return (float)er_atan2_d(s, xd);
+    return er_atan2f(sqrtf((1.0f - x) * (1.0f + x)), x);
 }
 
 /* Counter-based seeding: 32-bit integer finaliser "lowbias32" from
