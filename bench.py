@@ -343,17 +343,140 @@ def run_ours(args, wl, rank, world, local_rank):
     r.close()
 
 
+def run_batched(args, rank, world, local_rank):
+    """c3: 64 orbit views over three blob volumes, one CUDA-graph launch per
+    step (er_batch_launch), against the same views rendered one batch per view
+    and against the reference estimator one view and one frame at a time."""
+    import torch
+    torch.cuda.set_device(local_rank)
+    runtime = importlib.import_module("exposure-render_gb300.runtime")
+    S = importlib.import_module("exposure-render_gb300.scenes")
+    C = importlib.import_module("exposure-render_gb300.capi")
+    lib = C.load_library()
+    C.check(lib.er_set_device(local_rank))
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    C.check(lib.er_set_stream(sp))
+    scenes = S.c3_scenes()
+    for sc in scenes:
+        sc.tracer.settings.seed = 1 + rank
+    rs = [runtime.Renderer(sc, lib) for sc in scenes]
+    views = S.c3_views(n_views=args.views)
+    sums = [torch.zeros((cam.film_size[1], cam.film_size[0], 4), dtype=torch.float32, device="cuda") for _, cam, _ in views]
+    table = [(rs[k].tracer_id, spp, d.data_ptr(), cam) for (k, cam, spp), d in zip(views, sums)]
+    samples_per_step = sum(cam.film_size[0] * cam.film_size[1] * spp for _, cam, spp in views)
+    max_spp = max(spp for _, _, spp in views)
+    batch = runtime.Batch(table, flags=C.ER_BATCH_GRAPH)
+    info = batch.info()
+
+    def timed(fn, steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b)
+
+    def step():
+        batch.advance(max_spp, sp)       # fresh samples every step
+        batch.launch(sp)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        ms = timed(step, args.steps)
+    value = world * samples_per_step * args.steps / (ms / 1e3) / 1e6
+
+    # the same views, one single-view batch (graph) per view, back to back
+    singles = [runtime.Batch([t], flags=C.ER_BATCH_GRAPH) for t in table]
+    for b in singles:
+        b.launch(sp)
+    ms_seq = timed(lambda: [b.launch(sp) for b in singles], 1)
+    for b in singles:
+        b.close()
+    seq_value = samples_per_step / (ms_seq / 1e3) / 1e6
+
+    # plain: the reference estimator (fixed-step march, light sampling, BRDF),
+    # one frame of 1 spp per call (RenderEstimate), one view at a time
+    plain_samples, plain_ms = 0, 0.0
+    for (k, cam, spp) in views[: args.plain_views]:
+        r = rs[k]
+        saved = C.er_tracer_desc.from_buffer_copy(r.tracer_desc)
+        r.tracer_desc.camera = cam
+        r.tracer_desc.settings.free_flight = 0
+        r.rebind_tracer()
+        C.check(lib.er_reset_accumulation(r.tracer_id))
+        r.render_estimate()
+        torch.cuda.synchronize()
+        plain_ms += timed(r.render_estimate, 2)
+        plain_samples += 2 * cam.film_size[0] * cam.film_size[1]
+        ctypes.memmove(ctypes.byref(r.tracer_desc), ctypes.byref(saved), ctypes.sizeof(saved))
+        r.rebind_tracer()
+    plain_value = plain_samples / (plain_ms / 1e3) / 1e6
+
+    # end to end with host buffers: volumes bound from host memory, one batch
+    # launch, every view's sums read back into pinned host memory
+    host_sums = [torch.empty(d.shape, dtype=torch.float32, pin_memory=True) for d in sums]
+    vds = [sc.volume_desc() for sc in scenes]
+
+    def e2e_step():
+        for r, vd in zip(rs, vds):
+            vid = ctypes.c_int32(r.volume_id)
+            C.check(lib.er_bind_volume(ctypes.byref(vd), ctypes.byref(vid)))
+        step()
+        for h, d in zip(host_sums, sums):
+            h.copy_(d, non_blocking=True)
+        torch.cuda.synchronize()
+
+    e2e_step()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * samples_per_step * e2e_steps / e2e_s / 1e6
+    if rank != 0:
+        return
+    vol_bytes = sum(sc.volume.nbytes for sc in scenes)
+    line = {
+        "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "c3-batched-%d-views-3-blob-volumes" % len(views), "views": len(views),
+                   "samples_per_step": samples_per_step, "films": sorted({c.film_size[0] for _, c, _ in views}),
+                   "spp_range": [min(s for _, _, s in views), max_spp], **describe_shading(scenes[0]),
+                   "windows": info["windows"], "segments": info["segments"], "queue_bytes": info["queue_bytes"],
+                   "l2": "volumes %d MiB in total; every step renders fresh samples" % (vol_bytes >> 20),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(vol_bytes),
+                "d2h_bytes_per_step": int(sum(h.numel() * 4 for h in host_sums))},
+        "clocks": clk.summary(),
+        "gpu_launches": args.steps * (4 * info["windows"]),
+        "one_batch_per_view": {"value": seq_value, "unit": "Msamples/s", "speedup": value / seq_value},
+        "plain": {"value": plain_value, "unit": "Msamples/s", "speedup": value / plain_value, "views": args.plain_views,
+                  "what": "reference estimator (march, light sampling, BRDF), 1 spp per RenderEstimate, one view at a time"},
+    }
+    print(json.dumps(line), flush=True)
+    batch.close()
+    for r in rs:
+        r.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3"])
+    ap.add_argument("--views", type=int, default=64, help="c3: number of views")
+    ap.add_argument("--plain-views", type=int, default=16, help="c3: views timed on the plain one-view path")
     ap.add_argument("--film", type=int, default=0, help="square film edge (smaller profiling cases; 0 = the workload's)")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel (0 = the workload's)")
     args = ap.parse_args()
-    if args.film or args.spp:
+    if (args.film or args.spp) and args.workload in WORKLOADS:
         W = dict(WORKLOADS[args.workload])
         if args.film:
             W["film"] = (args.film, args.film)
@@ -366,6 +489,9 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, args.workload, rank, world)
+        return
+    if args.workload == "c3":
+        run_batched(args, rank, world, local_rank)
         return
     if world > 1:
         import torch

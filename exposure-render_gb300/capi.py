@@ -18,6 +18,8 @@ ER_MAX_ITEMS_PER_LIST = 31
 ER_MAX_INDICES = 256
 
 ER_OK = 0
+(ER_ERR_INVALID_ID, ER_ERR_INVALID_ARGUMENT, ER_ERR_LIST_FULL, ER_ERR_CUDA, ER_ERR_OUT_OF_MEMORY, ER_ERR_UNSUPPORTED,
+ ER_ERR_NO_DEVICE, ER_ERR_TIMEOUT) = range(1, 9)
 STATUS_NAMES = {
     0: "ER_OK",
     1: "ER_ERR_INVALID_ID",
@@ -191,6 +193,22 @@ class er_tracer_desc(Structure):
         ("clipping_object_count", c_int32),
         ("clipping_object_ids", c_int32 * ER_MAX_INDICES),
     ]
+
+
+class er_batch_view(Structure):
+    _fields_ = [
+        ("tracer_id", c_int32),
+        ("spp", c_int32),
+        ("view", c_uint32),
+        ("first_sample", c_uint32),
+        ("d_sum_xyza", c_void_p),
+        ("accumulate", c_int32),
+        ("display", c_int32),
+        ("camera", POINTER(er_camera_desc)),
+    ]
+
+
+ER_BATCH_GRAPH = 1
 
 
 # ---------------------------------------------------------------------------
@@ -373,6 +391,12 @@ def _declare(lib) -> None:
         "er_set_seeds": (c_int32, [c_int32, c_void_p]),
         "er_get_film_size": (c_int32, [c_int32, i32p, i32p]),
         "er_trace_sum_device": (c_int32, [c_int32, c_int32, c_uint32, c_uint32, c_void_p, c_int32, c_void_p]),
+        "er_batch_create": (c_int32, [POINTER(er_batch_view), c_int32, c_int32, c_int32, i32p]),
+        "er_batch_launch": (c_int32, [c_int32, c_void_p]),
+        "er_batch_advance": (c_int32, [c_int32, c_uint32, c_void_p]),
+        "er_batch_set_tuning": (c_int32, [c_int32, c_int32, c_int32]),
+        "er_batch_info": (c_int32, [c_int32, i32p, i32p, POINTER(ctypes.c_int64)]),
+        "er_batch_destroy": (c_int32, [c_int32]),
         "er_trace_frame_device": (c_int32, [c_int32, c_void_p, c_void_p, c_void_p]),
         "er_post_frame_device": (c_int32, [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_float, c_int32, c_void_p]),
         "er_tonemap_device": (c_int32, [c_void_p, c_float, c_void_p, c_int32, c_int32, c_float, c_void_p]),

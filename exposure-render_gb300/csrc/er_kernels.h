@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "er_device.cuh"
 
 /* spatial (KernelD) and range (GaussSimilarity) weights of the bilateral
@@ -38,20 +40,62 @@ cudaError_t er_launch_majorant(const uint16_t* vox, const int res[3], int B, con
 /* sets the text returned by er_last_error_message() on this thread */
 void er_internal_set_error(const char* message);
 
-/* queues of the wavefront pipeline (er_wavefront.cu); max_samples bounds one chunk */
+/* one view of a wavefront batch (er_wavefront.cu): the tracer's parameters,
+   its RNG stream and its output sums */
+struct WfView {
+    erd::Params P;
+    uint32_t view_id;    /* view index of the counter-based RNG stream */
+    uint32_t first;      /* sample index of the view's first sample */
+    int spp;             /* samples per pixel rendered by one batch launch */
+    int accumulate;      /* add to sum instead of overwriting it */
+    float4* sum;         /* film pixels: X, Y, Z and alpha sums */
+    /* display pass of a batch (er_post.cu k_post_batch) */
+    int display;         /* 1: mean -> frame filter -> tone map */
+    int filter;          /* 3x3 Gaussian of the mean */
+    float exposure;
+    float4* running;     /* film pixels: the filtered mean */
+    uchar4* rgba;        /* film pixels: the tone-mapped display */
+};
+
+cudaError_t er_launch_post_batch(const WfView* d_views, int n_views, int max_w, int max_h, cudaStream_t s);
+
+/* sample rows [s0, s1) of one view, at item `offset` of its window */
+struct WfSegment {
+    int view;
+    int s0, s1;
+    uint32_t offset;
+};
+
+/* windows of a batch: each is one pass of the four stages */
+struct WavefrontPlan {
+    std::vector<WfSegment> segs;          /* all windows' segments, window by window */
+    std::vector<int> window_first;        /* first segment of each window */
+    std::vector<uint32_t> window_items;   /* items of each window */
+    std::vector<int> view_npix;           /* film pixels of each view */
+    size_t max_items = 0;                 /* largest window */
+    int max_npix = 0;                     /* largest film */
+};
+
+/* queues of the wavefront pipeline, sized by a plan */
 struct WavefrontBuffers {
-    float4* results;     /* max_samples */
-    float4* events;      /* 5 * max_samples */
-    float4* jobs;        /* 6 * max_samples */
-    float4* partial;     /* film pixels */
+    float4* results;     /* max_items */
+    float4* events;      /* 5 * max_items */
+    float4* jobs;        /* 6 * max_items */
+    float4* partial;     /* 2 * max_npix: sums of a view cut by a window boundary */
     uint32_t* counters;  /* 2 */
-    size_t max_samples;
-    int tune_primary;    /* resident blocks per SM targeted by the primary stage (1..4) */
+    int tune_primary;    /* resident blocks per SM targeted by the primary stage (2, 3, 4, 6, 8) */
     int tune_shadow;     /* same for the shadow stage */
 };
 
-size_t er_wavefront_chunk_spp(int npix, int spp, size_t max_samples);
-cudaError_t er_launch_wavefront(const erd::Params& P, int spp, uint32_t view, uint32_t first, float4* sum, int accumulate,
-                                const WavefrontBuffers& B, cudaStream_t s);
+/* cuts the items of views (npix[v] * spp[v] each) into windows of whole
+   sample rows of at most window_cap items (one row at least) */
+void er_wavefront_plan(const int* npix, const int* spp, int n_views, size_t window_cap, WavefrontPlan& plan);
+
+/* one view with its parameters passed by value (no device tables) */
+cudaError_t er_launch_wavefront_one(const WfView& view, const WavefrontPlan& plan, const WavefrontBuffers& B, cudaStream_t s);
+
+/* many views: d_views / d_segs are the plan's tables in device memory */
+cudaError_t er_launch_wavefront_batch(const WfView* d_views, const WfSegment* d_segs, const WavefrontPlan& plan,
+                                      const WavefrontBuffers& B, cudaStream_t s);
 
 #endif

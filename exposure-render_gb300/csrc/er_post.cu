@@ -100,6 +100,23 @@ __global__ void k_post_mean(const float4* __restrict__ sum, float n, float4* __r
     rgba[c] = tonemap_px(R, exposure);
 }
 
+/* k_post_mean for every view of a batch (blockIdx.z = view); an accumulating
+   view's sum holds samples [0, first + spp) of its stream */
+__global__ void k_post_batch(const WfView* __restrict__ views)
+{
+    const WfView& V = views[blockIdx.z];
+    if (!V.display) return;
+    const int W = V.P.film[0], H = V.P.film[1];
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const float n = V.accumulate ? (float)(V.first + (uint32_t)V.spp) : (float)V.spp;
+    const size_t c = (size_t)y * W + x;
+    const float4 R = filtered_pixel<true>(V.sum, n, x, y, W, H, V.filter);
+    V.running[c] = R;
+    V.rgba[c] = tonemap_px(R, V.exposure);
+}
+
 __global__ void k_tonemap(const float4* __restrict__ xyza, float scale, uchar4* __restrict__ rgba, int n, float exposure)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -225,6 +242,13 @@ cudaError_t er_launch_post_mean(const float4* sum, float n, float4* running, uch
 {
     const dim3 b(16, 8), g((W + 15) / 16, (H + 7) / 8);
     k_post_mean<<<g, b, 0, s>>>(sum, n, running, rgba, W, H, exposure, filter);
+    return cudaGetLastError();
+}
+
+cudaError_t er_launch_post_batch(const WfView* d_views, int n_views, int max_w, int max_h, cudaStream_t s)
+{
+    const dim3 b(16, 8), g((max_w + 15) / 16, (max_h + 7) / 8, n_views);
+    k_post_batch<<<g, b, 0, s>>>(d_views);
     return cudaGetLastError();
 }
 

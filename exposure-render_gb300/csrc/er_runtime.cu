@@ -87,6 +87,32 @@ struct DevBuf {
     }
 };
 
+/* items of one wavefront window: 8M samples, 1.5 GB of queues */
+constexpr size_t kWindowCap = (size_t)8 << 20;
+
+/* queues of the wavefront stages, grown to the largest plan seen */
+struct WfQueues {
+    DevBuf<float4> results, events, jobs, partial;
+    DevBuf<uint32_t> counters;
+    cudaError_t ensure(const WavefrontPlan& plan, WavefrontBuffers& B)
+    {
+        cudaError_t e;
+        if ((e = results.ensure(plan.max_items)) != cudaSuccess) return e;
+        if ((e = events.ensure(5 * plan.max_items)) != cudaSuccess) return e;
+        if ((e = jobs.ensure(6 * plan.max_items)) != cudaSuccess) return e;
+        if ((e = partial.ensure(2 * (size_t)plan.max_npix)) != cudaSuccess) return e;
+        if ((e = counters.ensure(2)) != cudaSuccess) return e;
+        B.results = results.p;
+        B.events = events.p;
+        B.jobs = jobs.p;
+        B.partial = partial.p;
+        B.counters = counters.p;
+        B.tune_primary = 4;
+        B.tune_shadow = 4;
+        return cudaSuccess;
+    }
+};
+
 float smin_h(float a, float b) { return (b < a) ? b : a; }
 float smax_h(float a, float b) { return (a < b) ? b : a; }
 
@@ -145,12 +171,44 @@ struct TracerItem {
     DevBuf<float> majorant, rmq;
     DevBuf<uint32_t> minmax;
     DevBuf<int> err;
-    /* wavefront queues */
-    DevBuf<float4> wf_results, wf_events, wf_jobs, wf_partial;
-    DevBuf<uint32_t> wf_counters;
+    WfQueues wf;
     erd::Params P;
     uint64_t built_version = 0;
     bool built = false;
+};
+
+/* a planned multi-view batch (er_batch_create) */
+struct BatchItem {
+    std::vector<er_batch_view> views;
+    std::vector<er_camera_desc> cameras;
+    int flags = 0;
+    size_t window_cap = kWindowCap;
+    int tune_primary = 4, tune_shadow = 4;
+    uint64_t planned_version = 0;  /* context version the plan was made at */
+    bool planned = false;
+    WavefrontPlan plan;
+    std::vector<WfView> host_views;
+    DevBuf<WfView> d_views;
+    DevBuf<WfSegment> d_segs;
+    WfQueues wf;
+    WavefrontBuffers B;
+    int max_w = 0, max_h = 0;
+    bool any_display = false;
+    cudaStream_t capture_stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    void drop_graph()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+    ~BatchItem()
+    {
+        drop_graph();
+        if (capture_stream) cudaStreamDestroy(capture_stream);
+    }
 };
 
 template <class T>
@@ -171,6 +229,7 @@ struct Context {
     Registry<BitmapItem> bitmaps;
     Registry<er_object_desc> objects;
     Registry<er_clipping_object_desc> clipping;
+    Registry<BatchItem> batches;   /* not a reference list: no 31-item capacity */
 };
 
 Context& ctx()
@@ -505,23 +564,22 @@ er_status trace_sum(TracerItem& t, int spp, uint32_t view, uint32_t first, float
         ER_CUDA(er_launch_trace_sum(t.P, spp, view, first, sum, accumulate, s));
         return ER_OK;
     }
-    const size_t npix = (size_t)t.W * t.H;
-    const size_t max_samples = npix * er_wavefront_chunk_spp((int)npix, spp, (size_t)8 << 20);
-    ER_CUDA(t.wf_results.ensure(max_samples));
-    ER_CUDA(t.wf_events.ensure(5 * max_samples));
-    ER_CUDA(t.wf_jobs.ensure(6 * max_samples));
-    ER_CUDA(t.wf_partial.ensure(npix));
-    ER_CUDA(t.wf_counters.ensure(2));
+    const int npix = t.W * t.H;
+    WavefrontPlan plan;
+    er_wavefront_plan(&npix, &spp, 1, kWindowCap, plan);
     WavefrontBuffers B;
-    B.results = t.wf_results.p;
-    B.events = t.wf_events.p;
-    B.jobs = t.wf_jobs.p;
-    B.partial = t.wf_partial.p;
-    B.counters = t.wf_counters.p;
-    B.max_samples = max_samples;
+    ER_CUDA(t.wf.ensure(plan, B));
     B.tune_primary = t.d.settings.tune_primary > 0 ? t.d.settings.tune_primary : 4;
     B.tune_shadow = t.d.settings.tune_shadow > 0 ? t.d.settings.tune_shadow : 4;
-    ER_CUDA(er_launch_wavefront(t.P, spp, view, first, sum, accumulate, B, s));
+    WfView V;
+    memset(&V, 0, sizeof(V));
+    V.P = t.P;
+    V.view_id = view;
+    V.first = first;
+    V.spp = spp;
+    V.accumulate = accumulate;
+    V.sum = sum;
+    ER_CUDA(er_launch_wavefront_one(V, plan, B, s));
     return ER_OK;
 }
 
@@ -532,6 +590,113 @@ er_status finish_display(TracerItem& t)
         ER_CUDA(er_launch_bilateral(t.display.p, t.display_tmp.p, t.display_filtered.p, t.W, t.H, T, ctx().stream));
     }
     return ER_OK;
+}
+
+er_status batch_enqueue(BatchItem& b, cudaStream_t s);
+
+/* builds the batch's tracers, uploads its view and segment tables, sizes its
+   queues and, for ER_BATCH_GRAPH, captures one launch as a CUDA graph */
+er_status batch_plan(BatchItem& b)
+{
+    Context& C = ctx();
+    const int n = (int)b.views.size();
+    b.drop_graph();
+    b.planned = false;
+    b.host_views.assign((size_t)n, WfView());
+    std::vector<int> npix((size_t)n), spp((size_t)n);
+    b.max_w = b.max_h = 0;
+    b.any_display = false;
+    for (int v = 0; v < n; v++) {
+        const er_batch_view& bv = b.views[(size_t)v];
+        TracerItem* t = find_tracer(bv.tracer_id);
+        if (!t) return fail(ER_ERR_INVALID_ID, "batch view %d: resource item with ID:%d does not exist", v, bv.tracer_id);
+        er_status st = build(*t);
+        if (st != ER_OK) return st;
+        WfView& V = b.host_views[(size_t)v];
+        memset(&V, 0, sizeof(V));
+        V.P = t->P;
+        int W = t->W, H = t->H;
+        if (bv.camera) {
+            const er_camera_desc& c = *bv.camera;
+            if (c.film_size[0] <= 0 || c.film_size[1] <= 0 || c.film_size[0] > 32768 || c.film_size[1] > 32768)
+                return fail(ER_ERR_INVALID_ARGUMENT, "batch view %d: film size %d x %d out of range", v, c.film_size[0], c.film_size[1]);
+            if (!bv.d_sum_xyza || bv.display)
+                return fail(ER_ERR_INVALID_ARGUMENT, "batch view %d: a camera override needs its own sum buffer and no display", v);
+            camera_frame(c, V.P);
+            W = c.film_size[0];
+            H = c.film_size[1];
+        }
+        V.view_id = bv.view;
+        V.first = bv.first_sample;
+        V.spp = bv.spp;
+        V.accumulate = bv.accumulate;
+        V.sum = bv.d_sum_xyza ? (float4*)bv.d_sum_xyza : t->sum.p;
+        V.display = bv.display ? 1 : 0;
+        V.filter = t->d.settings.frame_filter >= 0 ? 1 : 0;
+        V.exposure = t->d.camera.exposure;
+        V.running = t->running.p;
+        V.rgba = t->display.p;
+        npix[(size_t)v] = W * H;
+        spp[(size_t)v] = bv.spp;
+        b.max_w = std::max(b.max_w, W);
+        b.max_h = std::max(b.max_h, H);
+        b.any_display = b.any_display || V.display;
+    }
+    for (int v = 0; v < n; v++)
+        for (int u = 0; u < v; u++)
+            if (b.host_views[(size_t)v].sum == b.host_views[(size_t)u].sum)
+                return fail(ER_ERR_INVALID_ARGUMENT, "batch views %d and %d share a sum buffer", u, v);
+    er_wavefront_plan(npix.data(), spp.data(), n, b.window_cap, b.plan);
+    ER_CUDA(b.wf.ensure(b.plan, b.B));
+    ER_CUDA(b.d_views.ensure((size_t)n));
+    ER_CUDA(b.d_segs.ensure(b.plan.segs.size()));
+    cudaStream_t st = C.stream;
+    ER_CUDA(cudaMemcpyAsync(b.d_views.p, b.host_views.data(), (size_t)n * sizeof(WfView), cudaMemcpyHostToDevice, st));
+    ER_CUDA(cudaMemcpyAsync(b.d_segs.p, b.plan.segs.data(), b.plan.segs.size() * sizeof(WfSegment), cudaMemcpyHostToDevice, st));
+    ER_CUDA(cudaStreamSynchronize(st));
+    b.B.tune_primary = b.tune_primary;
+    b.B.tune_shadow = b.tune_shadow;
+    if (b.flags & ER_BATCH_GRAPH) {
+        if (!b.capture_stream) ER_CUDA(cudaStreamCreateWithFlags(&b.capture_stream, cudaStreamNonBlocking));
+        ER_CUDA(cudaStreamBeginCapture(b.capture_stream, cudaStreamCaptureModeThreadLocal));
+        er_status rs = batch_enqueue(b, b.capture_stream);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(b.capture_stream, &g);
+        if (rs != ER_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rs;
+        }
+        ER_CUDA(ce);
+        b.graph = g;
+        ER_CUDA(cudaGraphInstantiate(&b.exec, b.graph, 0));
+    }
+    b.planned = true;
+    b.planned_version = C.version;
+    return ER_OK;
+}
+
+/* the launch sequence of a batch: wavefront windows, display pass, bilateral */
+er_status batch_enqueue(BatchItem& b, cudaStream_t s)
+{
+    ER_CUDA(er_launch_wavefront_batch(b.d_views.p, b.d_segs.p, b.plan, b.B, s));
+    if (b.any_display) {
+        ER_CUDA(er_launch_post_batch(b.d_views.p, (int)b.views.size(), b.max_w, b.max_h, s));
+        for (const er_batch_view& bv : b.views) {
+            if (!bv.display) continue;
+            TracerItem* t = find_tracer(bv.tracer_id);
+            if (t && t->d.settings.bilateral) {
+                const BilateralTables T = bilateral_tables(t->d.settings);
+                ER_CUDA(er_launch_bilateral(t->display.p, t->display_tmp.p, t->display_filtered.p, t->W, t->H, T, s));
+            }
+        }
+    }
+    return ER_OK;
+}
+
+BatchItem* find_batch(int id)
+{
+    auto it = ctx().batches.items.find(id);
+    return (id < 0 || it == ctx().batches.items.end()) ? nullptr : it->second.get();
 }
 
 }  // namespace
@@ -585,6 +750,9 @@ ER_API er_status er_reset(void)
     ER_LOCK;
     Context& C = ctx();
     cudaStreamSynchronize(C.stream);
+    cudaDeviceSynchronize();
+    C.batches.items.clear();
+    C.batches.counter = 0;
     C.tracers.items.clear();
     C.volumes.items.clear();
     C.lights.items.clear();
@@ -938,6 +1106,98 @@ ER_API er_status er_trace_sum_device(int32_t tracer_id, int32_t spp, uint32_t vi
     er_status st = build(*t);
     if (st != ER_OK) return st;
     return trace_sum(*t, spp, view, first_sample, (float4*)d_sum, accumulate, (cudaStream_t)stream);
+}
+
+ER_API er_status er_batch_create(const er_batch_view* views, int32_t n_views, int32_t flags, int32_t window_items,
+                                 int32_t* batch_id)
+{
+    ER_LOCK;
+    if (!views || n_views <= 0 || n_views > 65535 || !batch_id) return fail(ER_ERR_INVALID_ARGUMENT, "invalid batch views");
+    if (window_items < 0) return fail(ER_ERR_INVALID_ARGUMENT, "window_items must be >= 0");
+    for (int v = 0; v < n_views; v++)
+        if (views[v].spp <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "batch view %d: spp must be positive", v);
+    std::unique_ptr<BatchItem> b(new BatchItem());
+    b->views.assign(views, views + n_views);
+    /* the batch keeps its own copies of the camera overrides */
+    b->cameras.resize((size_t)n_views);
+    for (int v = 0; v < n_views; v++) {
+        if (!views[v].camera) continue;
+        b->cameras[(size_t)v] = *views[v].camera;
+        b->views[(size_t)v].camera = &b->cameras[(size_t)v];
+    }
+    b->flags = flags;
+    b->window_cap = window_items > 0 ? (size_t)window_items : kWindowCap;
+    const er_status st = batch_plan(*b);
+    if (st != ER_OK) return st;
+    const int id = ctx().batches.counter++;
+    ctx().batches.items[id] = std::move(b);
+    *batch_id = id;
+    return ER_OK;
+}
+
+ER_API er_status er_batch_launch(int32_t batch_id, void* stream)
+{
+    ER_LOCK;
+    BatchItem* b = find_batch(batch_id);
+    if (!b) return fail(ER_ERR_INVALID_ID, "batch with ID:%d does not exist", batch_id);
+    if (!b->planned || b->planned_version != ctx().version) {
+        const er_status st = batch_plan(*b);
+        if (st != ER_OK) return st;
+    }
+    if (b->exec) {
+        ER_CUDA(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+        return ER_OK;
+    }
+    return batch_enqueue(*b, (cudaStream_t)stream);
+}
+
+ER_API er_status er_batch_advance(int32_t batch_id, uint32_t samples, void* stream)
+{
+    ER_LOCK;
+    BatchItem* b = find_batch(batch_id);
+    if (!b) return fail(ER_ERR_INVALID_ID, "batch with ID:%d does not exist", batch_id);
+    for (size_t v = 0; v < b->views.size(); v++) {
+        b->views[v].first_sample += samples;
+        b->host_views[v].first += samples;
+    }
+    /* a pageable source is staged before the call returns */
+    ER_CUDA(cudaMemcpyAsync(b->d_views.p, b->host_views.data(), b->host_views.size() * sizeof(WfView), cudaMemcpyHostToDevice,
+                            (cudaStream_t)stream));
+    return ER_OK;
+}
+
+ER_API er_status er_batch_set_tuning(int32_t batch_id, int32_t tune_primary, int32_t tune_shadow)
+{
+    ER_LOCK;
+    BatchItem* b = find_batch(batch_id);
+    if (!b) return fail(ER_ERR_INVALID_ID, "batch with ID:%d does not exist", batch_id);
+    auto valid = [](int v) { return v == 0 || v == 2 || v == 3 || v == 4 || v == 6 || v == 8; };
+    if (!valid(tune_primary) || !valid(tune_shadow)) return fail(ER_ERR_INVALID_ARGUMENT, "tuning values must be 0, 2, 3, 4, 6 or 8");
+    if (tune_primary) b->tune_primary = tune_primary;
+    if (tune_shadow) b->tune_shadow = tune_shadow;
+    b->planned = false;   /* re-captured at the next launch */
+    return ER_OK;
+}
+
+ER_API er_status er_batch_info(int32_t batch_id, int32_t* n_windows, int32_t* n_segments, int64_t* queue_bytes)
+{
+    ER_LOCK;
+    BatchItem* b = find_batch(batch_id);
+    if (!b) return fail(ER_ERR_INVALID_ID, "batch with ID:%d does not exist", batch_id);
+    if (n_windows) *n_windows = (int32_t)b->plan.window_first.size();
+    if (n_segments) *n_segments = (int32_t)b->plan.segs.size();
+    if (queue_bytes) *queue_bytes = (int64_t)((12 * b->plan.max_items + 2 * (size_t)b->plan.max_npix) * sizeof(float4));
+    return ER_OK;
+}
+
+ER_API er_status er_batch_destroy(int32_t batch_id)
+{
+    ER_LOCK;
+    auto it = ctx().batches.items.find(batch_id);
+    if (batch_id < 0 || it == ctx().batches.items.end()) return fail(ER_ERR_INVALID_ID, "batch with ID:%d does not exist", batch_id);
+    ER_CUDA(cudaDeviceSynchronize());
+    ctx().batches.items.erase(it);
+    return ER_OK;
 }
 
 ER_API er_status er_trace_frame_device(int32_t tracer_id, uint32_t* d_lanes, float* d_frame, void* stream)

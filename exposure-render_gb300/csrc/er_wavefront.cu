@@ -1,6 +1,6 @@
 /*
  * er_wavefront.cu - the single-scattering estimator as a pipeline of small
- * kernels (compiled with --fmad=false).
+ * kernels over a batch of views (compiled with --fmad=false).
  *
  * The one-kernel path (k_trace_sum) inlines camera sampling, free flight,
  * shading, light sampling, MIS and two shadow traversals into one kernel of
@@ -12,23 +12,29 @@
  *                  (Source/singlescattering.h:76-101).  Misses and light
  *                  hits finish here; volume events go to the event queue.
  *   k_wf_shade   : UniformSampleOneLight up to the shadow rays
- *                  (Source/transport.h:115-156, :58-113): emission, light
- *                  pick, shader selection, light sample, BSDF sample and its
- *                  light hit.  The unoccluded contributions and the two
- *                  shadow segments go to the shadow queue.
+ *                  (Source/transport.h:115-156, :58-113): event normal,
+ *                  emission, light pick, shader selection, light sample,
+ *                  BSDF sample and its light hit.  Unoccluded contributions
+ *                  and the two shadow segments go to the shadow queue.
  *   k_wf_shadow  : the shadow segments (march or ratio tracking) and the
  *                  final sum of the sample.
- *   k_wf_reduce  : per-pixel sum over the chunk's samples in sample order.
+ *   k_wf_reduce  : per-pixel sum over the window's samples in sample order.
+ *
+ * Batching: every view of a batch (its own tracer: camera, film, transfer
+ * functions, lights, volume) has a record in a view table in HBM.  The
+ * samples of all views form one index space (view by view, sample-major
+ * inside a view: item = s * npix + pixel), cut on the host into windows of
+ * whole sample rows; each window is one pass of the four stages over items
+ * of many views, so uneven views load-balance inside each launch.  The
+ * reduction keeps each pixel's samples in order, so a view's sum is the same
+ * whether it is rendered alone or in a batch.
  *
  * Every RNG draw happens in the order of the one-kernel path (the RNG state
  * travels with the queue records) and every float operation is the same, so
  * the sums are bit-identical to k_trace_sum's and to the CPU oracle's.
- *
- * Queue records are arrays of float4 (five per event, six per shadow job):
- * one 16-byte load or store per field group.  Queues are appended with
- * warp-aggregated atomics; records carry their sample index, so results do
- * not depend on the append order.
  */
+#include <cstring>
+
 #include "er_kernels.h"
 #include "er_path.cuh"
 
@@ -51,33 +57,60 @@ ER_D uint32_t queue_slot(bool want, uint32_t* counter)
     return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
 }
 
+/* the view record: a kernel parameter for a one-view launch, else the table */
+template <bool ONE>
+ER_D const WfView& view_of(const WfView* __restrict__ views, const WfView& one, uint32_t v)
+{
+    if (ONE) return one;
+    return views[v];
+}
+
+/* segment of a window holding window-local item i (segments are sorted by offset) */
+ER_D int find_segment(const WfSegment* __restrict__ segs, int nseg, uint32_t i)
+{
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (segs[mid].offset <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 }  // namespace
 
 /* ---- stage 1: camera ray, free flight, visible lights ---- */
 
 /* MINB: resident 256-thread blocks per SM the register allocation targets
-   (1: up to 255 registers, 2: 128, 3: 80, 4: 64); picked at run time */
-template <int MINB>
-__global__ void __launch_bounds__(256, MINB) k_wf_primary(const Params P, uint32_t view, uint32_t first, int spp_chunk, int npix,
-                                                    float4* __restrict__ results, float4* __restrict__ events,
-                                                    uint32_t* __restrict__ n_events)
+   (2: 128 registers, 3: ~80, 4: 64, 6: 40, 8: 32); picked at run time */
+template <int MINB, bool ONE>
+__global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restrict__ views, const WfSegment* __restrict__ segs, int nseg,
+                                                           const WfView one, const WfSegment one_seg, uint32_t items,
+                                                           float4* __restrict__ results, float4* __restrict__ events,
+                                                           uint32_t* __restrict__ n_events)
 {
-    const int64_t total = (int64_t)spp_chunk * npix;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < total; base += stride) {
-        const int64_t i = base + threadIdx.x;
-        const bool live = i < total;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < items; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool live = i < items;
         bool push = false;
         Event SE;
         Metro ms;
         Rng rng;
         rng.s0 = 0u;
         rng.s1 = 0u;
+        int v = 0;
         if (live) {
-            const int s = (int)(i / npix);
-            const int pix = (int)(i - (int64_t)s * npix);
+            const WfSegment sg = ONE ? one_seg : segs[find_segment(segs, nseg, i)];
+            v = sg.view;
+            const WfView& V = view_of<ONE>(views, one, v);
+            const Params& P = V.P;
+            const uint32_t local = i - sg.offset;
+            const uint32_t npix = (uint32_t)(P.film[0] * P.film[1]);
+            const int s = sg.s0 + (int)(local / npix);
+            const int pix = (int)(local % npix);
             const int x = pix % P.film[0], y = pix / P.film[0];
-            er_seed_lanes(P.seed, view, (uint32_t)pix, first + (uint32_t)s, &rng.s0, &rng.s1);
+            er_seed_lanes(P.seed, V.view_id, (uint32_t)pix, V.first + (uint32_t)s, &rng.s0, &rng.s1);
             ms.large_step(rng);
             const Ray R = sample_camera(P, x, y, ms.film_uv, ms.lens_uv);
             Event se0, se1;
@@ -104,11 +137,11 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const Params P, uint32
         const uint32_t slot = queue_slot(push, n_events);
         if (push) {
             float4* e = events + (size_t)slot * 5;
-            e[0] = make_float4(u2f((uint32_t)i), u2f(rng.s0), u2f(rng.s1), ms.light_num);
+            e[0] = make_float4(u2f(i), u2f(rng.s0), u2f(rng.s1), ms.light_num);
             e[1] = make_float4(SE.P.x, SE.P.y, SE.P.z, ms.brdf_component);
-            e[2] = make_float4(SE.N.x, SE.N.y, SE.N.z, ms.brdf_dir.x);
+            e[2] = make_float4(0.0f, 0.0f, 0.0f, ms.brdf_dir.x);
             e[3] = make_float4(SE.Wo.x, SE.Wo.y, SE.Wo.z, ms.brdf_dir.y);
-            e[4] = make_float4(ms.light_uvw.x, ms.light_uvw.y, ms.light_uvw.z, 0.0f);
+            e[4] = make_float4(ms.light_uvw.x, ms.light_uvw.y, ms.light_uvw.z, u2f((uint32_t)v));
         }
     }
 }
@@ -119,7 +152,8 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const Params P, uint32
 #define WF_RAY1 1u
 #define WF_RAY2 2u
 
-__global__ void __launch_bounds__(128) k_wf_shade(const Params P, const float4* __restrict__ events,
+template <bool ONE>
+__global__ void __launch_bounds__(128) k_wf_shade(const WfView* __restrict__ views, const WfView one, const float4* __restrict__ events,
                                                   const uint32_t* __restrict__ n_events, float4* __restrict__ results,
                                                   float4* __restrict__ jobs, uint32_t* __restrict__ n_jobs)
 {
@@ -129,7 +163,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const Params P, const float4* 
         const uint32_t e_i = base + threadIdx.x;
         const bool live = e_i < n;
         bool push = false;
-        uint32_t sample = 0, flags = 0;
+        uint32_t sample = 0, flags = 0, v = 0;
         Rng rng;
         rng.s0 = 0u;
         rng.s1 = 0u;
@@ -143,6 +177,8 @@ __global__ void __launch_bounds__(128) k_wf_shade(const Params P, const float4* 
             sample = f2u(e0.x);
             rng.s0 = f2u(e0.y);
             rng.s1 = f2u(e0.z);
+            v = f2u(e4.w);
+            const Params& P = view_of<ONE>(views, one, v).P;
             Metro ms;
             ms.light_num = e0.w;
             ms.brdf_component = e1.w;
@@ -233,23 +269,24 @@ __global__ void __launch_bounds__(128) k_wf_shade(const Params P, const float4* 
             j[2] = make_float4(S1.x, S1.y, S1.z, Le.r);
             j[3] = make_float4(c1.r, c1.g, c1.b, Le.g);
             j[4] = make_float4(S2.x, S2.y, S2.z, Le.b);
-            j[5] = make_float4(c2.r, c2.g, c2.b, 0.0f);
+            j[5] = make_float4(c2.r, c2.g, c2.b, u2f(v));
         }
     }
 }
 
 /* ---- stage 3: shadow segments and the sample's sum ---- */
 
-template <int MINB>
-__global__ void __launch_bounds__(256, MINB) k_wf_shadow(const Params P, const float4* __restrict__ jobs, const uint32_t* __restrict__ n_jobs,
-                                                   float4* __restrict__ results)
+template <int MINB, bool ONE>
+__global__ void __launch_bounds__(256, MINB) k_wf_shadow(const WfView* __restrict__ views, const WfView one, const float4* __restrict__ jobs,
+                                                          const uint32_t* __restrict__ n_jobs, float4* __restrict__ results)
 {
     const uint32_t n = *n_jobs;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const bool ref_mode = P.mis != 1 && P.free_flight != 1;
     for (uint32_t j_i = blockIdx.x * blockDim.x + threadIdx.x; j_i < n; j_i += stride) {
         const float4* j = jobs + (size_t)j_i * 6;
         const float4 j0 = j[0], j1 = j[1], j2 = j[2], j3 = j[3], j4 = j[4], j5 = j[5];
+        const Params& P = view_of<ONE>(views, one, f2u(j5.w)).P;
+        const bool ref_mode = P.mis != 1 && P.free_flight != 1;
         const uint32_t sample = f2u(j0.x);
         Rng rng;
         rng.s0 = f2u(j0.y);
@@ -275,78 +312,149 @@ __global__ void __launch_bounds__(256, MINB) k_wf_shadow(const Params P, const f
     }
 }
 
-/* ---- stage 4: per-pixel sum in sample order ---- */
+/* ---- stage 4: per-pixel sum in sample order (blockIdx.y = segment) ---- */
 
-__global__ void k_wf_reduce(const float4* __restrict__ results, int spp_chunk, int npix, float4* __restrict__ partial, int first_chunk,
-                            int last_chunk, float4* __restrict__ sum, int accumulate)
+/* partial_in holds the sums of the previous window's last view when this
+   window's first segment continues it; partial_out receives the sums of this
+   window's last view when the next window continues it */
+template <bool ONE>
+__global__ void k_wf_reduce(const WfView* __restrict__ views, const WfSegment* __restrict__ segs, const WfView one,
+                            const WfSegment one_seg, const float4* __restrict__ results, const float4* __restrict__ partial_in,
+                            float4* __restrict__ partial_out)
 {
+    const WfSegment sg = ONE ? one_seg : segs[blockIdx.y];
+    const WfView& V = view_of<ONE>(views, one, sg.view);
+    const int npix = V.P.film[0] * V.P.film[1];
     const int pix = blockIdx.x * blockDim.x + threadIdx.x;
     if (pix >= npix) return;
     float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
-    if (!first_chunk) {
-        const float4 p = partial[pix];
+    if (sg.s0 > 0) {
+        const float4 p = partial_in[pix];
         a0 = p.x; a1 = p.y; a2 = p.z; a3 = p.w;
     }
-    for (int s = 0; s < spp_chunk; s++) {
-        const float4 o = results[(size_t)s * npix + pix];
+    for (int s = sg.s0; s < sg.s1; s++) {
+        const float4 o = results[(size_t)sg.offset + (size_t)(s - sg.s0) * npix + pix];
         a0 += o.x; a1 += o.y; a2 += o.z; a3 += o.w;
     }
-    if (!last_chunk) {
-        partial[pix] = make_float4(a0, a1, a2, a3);
+    if (sg.s1 < V.spp) {
+        partial_out[pix] = make_float4(a0, a1, a2, a3);
         return;
     }
     float4 r = make_float4(a0, a1, a2, a3);
-    if (accumulate) {
-        const float4 q = sum[pix];
+    if (V.accumulate) {
+        const float4 q = V.sum[pix];
         r = make_float4(q.x + a0, q.y + a1, q.z + a2, q.w + a3);
     }
-    sum[pix] = r;
+    V.sum[pix] = r;
 }
 
-/* ---- launcher ---- */
+/* ---- host side ---- */
 
-size_t er_wavefront_chunk_spp(int npix, int spp, size_t max_samples)
+void er_wavefront_plan(const int* npix, const int* spp, int n_views, size_t window_cap, WavefrontPlan& plan)
 {
-    size_t s = max_samples / (size_t)(npix > 0 ? npix : 1);
-    if (s < 1) s = 1;
-    if (s > (size_t)spp) s = (size_t)spp;
-    return s;
+    plan.segs.clear();
+    plan.window_first.clear();
+    plan.window_items.clear();
+    plan.view_npix.assign(npix, npix + n_views);
+    plan.max_items = 0;
+    plan.max_npix = 0;
+    size_t used = 0;
+    for (int v = 0; v < n_views; v++) {
+        if (npix[v] > plan.max_npix) plan.max_npix = npix[v];
+        int s = 0;
+        while (s < spp[v]) {
+            if (plan.window_first.empty() || used + (size_t)npix[v] > window_cap) {
+                plan.window_first.push_back((int)plan.segs.size());
+                plan.window_items.push_back(0);
+                used = 0;
+            }
+            size_t rows = (window_cap - used) / (size_t)npix[v];
+            if (rows < 1) rows = 1;
+            if (rows > (size_t)(spp[v] - s)) rows = (size_t)(spp[v] - s);
+            WfSegment g;
+            g.view = v;
+            g.s0 = s;
+            g.s1 = s + (int)rows;
+            g.offset = (uint32_t)used;
+            plan.segs.push_back(g);
+            used += rows * (size_t)npix[v];
+            plan.window_items.back() = (uint32_t)used;
+            if (used > plan.max_items) plan.max_items = used;
+            s += (int)rows;
+        }
+    }
 }
 
-cudaError_t er_launch_wavefront(const Params& P, int spp, uint32_t view, uint32_t first, float4* sum, int accumulate,
-                                const WavefrontBuffers& B, cudaStream_t s)
+namespace {
+
+int sm_count()
 {
-    const int npix = P.film[0] * P.film[1];
-    const int chunk = (int)er_wavefront_chunk_spp(npix, spp, B.max_samples);
     int sm = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
-    if (sm <= 0) sm = 132;
-    for (int done = 0; done < spp; done += chunk) {
-        const int c = (spp - done) < chunk ? (spp - done) : chunk;
+    return sm > 0 ? sm : 132;
+}
+
+template <bool ONE>
+cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const WfView& one, const WavefrontPlan& plan,
+                           const WavefrontBuffers& B, cudaStream_t s)
+{
+    const int sm = sm_count();
+    const int nw = (int)plan.window_first.size();
+    for (int w = 0; w < nw; w++) {
+        const int s0 = plan.window_first[w];
+        const int s1 = (w + 1 < nw) ? plan.window_first[w + 1] : (int)plan.segs.size();
+        const int nseg = s1 - s0;
+        const uint32_t items = plan.window_items[w];
+        const WfSegment* dseg = ONE ? nullptr : d_segs + s0;
+        const WfSegment one_seg = plan.segs[s0];
+        float4* p_in = B.partial + (size_t)((w + 1) & 1) * plan.max_npix;
+        float4* p_out = B.partial + (size_t)(w & 1) * plan.max_npix;
         cudaError_t e = cudaMemsetAsync(B.counters, 0, 2 * sizeof(uint32_t), s);
         if (e != cudaSuccess) return e;
-        const int64_t total = (int64_t)c * npix;
-        const int g1 = (int)((total + 255) / 256 < (int64_t)sm * 64 ? (total + 255) / 256 : (int64_t)sm * 64);
-        const uint32_t f = first + (uint32_t)done;
+        const uint32_t g1 = (items + 255) / 256 < (uint32_t)sm * 64 ? (items + 255) / 256 : (uint32_t)sm * 64;
+#define ER_PRIMARY(M) k_wf_primary<M, ONE><<<g1, 256, 0, s>>>(d_views, dseg, nseg, one, one_seg, items, B.results, B.events, B.counters)
         switch (B.tune_primary) {
-        case 2: k_wf_primary<2><<<g1, 256, 0, s>>>(P, view, f, c, npix, B.results, B.events, B.counters); break;
-        case 3: k_wf_primary<3><<<g1, 256, 0, s>>>(P, view, f, c, npix, B.results, B.events, B.counters); break;
-        case 6: k_wf_primary<6><<<g1, 256, 0, s>>>(P, view, f, c, npix, B.results, B.events, B.counters); break;
-        case 8: k_wf_primary<8><<<g1, 256, 0, s>>>(P, view, f, c, npix, B.results, B.events, B.counters); break;
-        default: k_wf_primary<4><<<g1, 256, 0, s>>>(P, view, f, c, npix, B.results, B.events, B.counters); break;
+        case 2: ER_PRIMARY(2); break;
+        case 3: ER_PRIMARY(3); break;
+        case 6: ER_PRIMARY(6); break;
+        case 8: ER_PRIMARY(8); break;
+        default: ER_PRIMARY(4); break;
         }
-        k_wf_shade<<<sm * 16, 128, 0, s>>>(P, B.events, B.counters, B.results, B.jobs, B.counters + 1);
+#undef ER_PRIMARY
+        k_wf_shade<ONE><<<sm * 16, 128, 0, s>>>(d_views, one, B.events, B.counters, B.results, B.jobs, B.counters + 1);
+#define ER_SHADOW(M) k_wf_shadow<M, ONE><<<sm * 8, 256, 0, s>>>(d_views, one, B.jobs, B.counters + 1, B.results)
         switch (B.tune_shadow) {
-        case 2: k_wf_shadow<2><<<sm * 8, 256, 0, s>>>(P, B.jobs, B.counters + 1, B.results); break;
-        case 3: k_wf_shadow<3><<<sm * 8, 256, 0, s>>>(P, B.jobs, B.counters + 1, B.results); break;
-        case 6: k_wf_shadow<6><<<sm * 8, 256, 0, s>>>(P, B.jobs, B.counters + 1, B.results); break;
-        case 8: k_wf_shadow<8><<<sm * 8, 256, 0, s>>>(P, B.jobs, B.counters + 1, B.results); break;
-        default: k_wf_shadow<4><<<sm * 8, 256, 0, s>>>(P, B.jobs, B.counters + 1, B.results); break;
+        case 2: ER_SHADOW(2); break;
+        case 3: ER_SHADOW(3); break;
+        case 6: ER_SHADOW(6); break;
+        case 8: ER_SHADOW(8); break;
+        default: ER_SHADOW(4); break;
         }
-        k_wf_reduce<<<(npix + 255) / 256, 256, 0, s>>>(B.results, c, npix, B.partial, done == 0, done + c >= spp, sum, accumulate);
+#undef ER_SHADOW
+        int max_npix = 0;
+        for (int g = s0; g < s1; g++) {
+            const int np = plan.view_npix[plan.segs[g].view];
+            if (np > max_npix) max_npix = np;
+        }
+        k_wf_reduce<ONE><<<dim3((max_npix + 255) / 256, ONE ? 1 : nseg), 256, 0, s>>>(d_views, dseg, one, one_seg, B.results, p_in, p_out);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t er_launch_wavefront_one(const WfView& view, const WavefrontPlan& plan, const WavefrontBuffers& B, cudaStream_t s)
+{
+    return launch_windows<true>(nullptr, nullptr, view, plan, B, s);
+}
+
+cudaError_t er_launch_wavefront_batch(const WfView* d_views, const WfSegment* d_segs, const WavefrontPlan& plan,
+                                      const WavefrontBuffers& B, cudaStream_t s)
+{
+    WfView unused;
+    memset(&unused, 0, sizeof(unused));
+    return launch_windows<false>(d_views, d_segs, unused, plan, B, s);
 }

@@ -112,3 +112,59 @@ class Renderer:
         for i in self.texture_ids:
             lib.er_unbind_texture(i)
         self.light_ids, self.texture_ids = [], []
+
+
+class Batch:
+    """Many views rendered by one submission (er_batch_create / er_batch_launch).
+
+    `views` holds (tracer_id, spp, d_sum_ptr, camera or None) tuples or
+    er_batch_view records; `first`, `view` and `accumulate` default to 0 and
+    view index i.  The plan is made at construction; binding anything
+    re-plans it at the next launch."""
+
+    def __init__(self, views, flags=C.ER_BATCH_GRAPH, window_items=0, lib=None, accumulate=0, display=0):
+        self.lib = lib or C.load_library()
+        n = len(views)
+        arr = (C.er_batch_view * n)()
+        self._cams = []
+        for i, v in enumerate(views):
+            if isinstance(v, C.er_batch_view):
+                arr[i] = v
+                continue
+            tid, spp, d_sum, cam = v
+            b = arr[i]
+            b.tracer_id = tid
+            b.spp = spp
+            b.view = i
+            b.first_sample = 0
+            b.d_sum_xyza = d_sum
+            b.accumulate = accumulate
+            b.display = display
+            if cam is not None:
+                c = C.er_camera_desc()
+                ctypes.memmove(byref(c), byref(cam), ctypes.sizeof(c))
+                self._cams.append(c)
+                b.camera = ctypes.pointer(c)
+        self.views = arr
+        bid = c_int32(-1)
+        C.check(self.lib.er_batch_create(arr, n, flags, window_items, byref(bid)))
+        self.batch_id = bid.value
+
+    def launch(self, stream=None) -> None:
+        C.check(self.lib.er_batch_launch(self.batch_id, stream))
+
+    def advance(self, samples: int, stream=None) -> None:
+        C.check(self.lib.er_batch_advance(self.batch_id, samples, stream))
+
+    def set_tuning(self, primary: int = 0, shadow: int = 0) -> None:
+        C.check(self.lib.er_batch_set_tuning(self.batch_id, primary, shadow))
+
+    def info(self) -> dict:
+        w, s, q = c_int32(0), c_int32(0), ctypes.c_int64(0)
+        C.check(self.lib.er_batch_info(self.batch_id, byref(w), byref(s), byref(q)))
+        return {"windows": w.value, "segments": s.value, "queue_bytes": q.value}
+
+    def close(self) -> None:
+        if self.batch_id >= 0:
+            self.lib.er_batch_destroy(self.batch_id)
+            self.batch_id = -1

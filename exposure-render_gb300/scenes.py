@@ -12,6 +12,9 @@ scene is fully described by its name and parameters.
         noise sigma 30) in a soft-tissue ellipsoid; 16-node transfer function,
         hybrid phase/BRDF (roughness 0.3); two area lights plus an environment
         sphere light; 1024^2; 256 spp; bilateral filter and tone map.
+    c3  batched forward: 64 random orbit views over three blob volumes of
+        96^3, 256^3 and 384x384x256 (x, y, z); films drawn from
+        {128, 256, 384, 512}^2; 32-128 spp per view; delta tracking.
 """
 from __future__ import annotations
 
@@ -308,3 +311,37 @@ def scene_c2(res=512, film=(1024, 1024), spp=256) -> Scene:
     vol = shell_volume(res, seed=2)
     lights, textures = c2_lights()
     return Scene("c2", vol, tracer=c2_tracer(film), lights=lights, textures=textures, spp=spp)
+
+
+# ---------------------------------------------------------------------------
+# batched forward (c3)
+# ---------------------------------------------------------------------------
+
+C3_FILMS = (128, 256, 384, 512)
+C3_VOLUMES = ((96, 96, 96), (256, 256, 256), (256, 384, 384))   # (z, y, x)
+
+
+def c3_scenes(volumes=C3_VOLUMES, seed=30) -> list:
+    """One C1-style scene (4-node transfer function, one area light) per blob
+    volume, delta-tracked free flight; each scene's tracer is the template of
+    the views that look at its volume."""
+    out = []
+    for k, shp in enumerate(volumes):
+        vol = blob_volume(shp, seed=seed + k)
+        lights, textures = c1_lights()
+        t = c1_tracer((C3_FILMS[0], C3_FILMS[0]))
+        t.settings.free_flight = C.FREE_FLIGHT_DELTA
+        out.append(Scene(f"c3v{k}", vol, tracer=t, lights=lights, textures=textures, spp=32))
+    return out
+
+
+def c3_views(n_views=64, n_volumes=3, seed=7, films=C3_FILMS, spp=(32, 128)) -> list:
+    """(volume index, orbit camera, spp) of each view, from a fixed seed."""
+    rng = np.random.default_rng(seed)
+    views = []
+    for _ in range(n_views):
+        k = int(rng.integers(0, n_volumes))
+        f = int(films[int(rng.integers(0, len(films)))])
+        cam = orbit_camera(rng, (f, f), radius=float(rng.uniform(1.8, 2.6)))
+        views.append((k, cam, int(rng.integers(spp[0], spp[1] + 1))))
+    return views

@@ -338,6 +338,51 @@ ER_API er_status er_get_film_size(int32_t tracer_id, int32_t* width, int32_t* he
 ER_API er_status er_trace_sum_device(int32_t tracer_id, int32_t spp, uint32_t view, uint32_t first_sample,
                                      float* d_sum_xyza, int32_t accumulate, void* stream);
 
+/* ---------------------------------------------------------------------- */
+/* batched multi-view transport (no reference counterpart: the reference   */
+/* renders one tracer per call, Source/core.cu:126-136 RenderEstimate)     */
+/* ---------------------------------------------------------------------- */
+
+/* One view of a batch: a bound tracer (its camera, film, volume, transfer
+   functions and lights) and the samples to render into its sum buffer. */
+typedef struct er_batch_view {
+    int32_t tracer_id;
+    int32_t spp;             /* samples per pixel per launch, > 0 */
+    uint32_t view;           /* view index of the counter-based RNG stream */
+    uint32_t first_sample;   /* stream index of the first sample (er_batch_advance moves it) */
+    float* d_sum_xyza;       /* device, W*H*4 floats; NULL: the tracer's own sum buffer */
+    int32_t accumulate;      /* 0 overwrites the sums, 1 adds to them */
+    int32_t display;         /* 1: tone-map the mean into the tracer's display (er_get_estimate) */
+    const er_camera_desc* camera;  /* NULL: the tracer's camera; else this camera and film
+                                      (then d_sum_xyza is required and display must be 0) */
+} er_batch_view;
+
+#define ER_BATCH_GRAPH 1     /* er_batch_launch replays one captured CUDA graph */
+
+/* Plans a batch: the samples of all views form one index space cut into
+   windows of at most window_items samples (0: 8M), each window one pass of
+   the wavefront stages over many views.  Every view's sums are bit-identical
+   to er_trace_sum_device with the same tracer, spp, view, first_sample and
+   accumulate.  With display set, the view's mean sum / n (n = first_sample +
+   spp for an accumulating view, spp otherwise) goes through the frame
+   filter, tone map and bilateral filter of the tracer's settings into the
+   tracer's running estimate and display.  Binding or unbinding any resource
+   re-plans the batch at its next launch.  Views share no output buffers. */
+ER_API er_status er_batch_create(const er_batch_view* views, int32_t n_views, int32_t flags, int32_t window_items,
+                                 int32_t* batch_id);
+/* Enqueues one render of every view on `stream` (asynchronous). */
+ER_API er_status er_batch_launch(int32_t batch_id, void* stream);
+/* Enqueues on `stream` an update that adds `samples` to every view's
+   first_sample, for progressive accumulation (first launch at 0, then
+   advance by spp before each further launch). */
+ER_API er_status er_batch_advance(int32_t batch_id, uint32_t samples, void* stream);
+/* Resource-occupancy variants of the primary and shadow stages (2, 3, 4, 6
+   or 8 resident blocks of 256 threads per SM; 0 keeps the current value). */
+ER_API er_status er_batch_set_tuning(int32_t batch_id, int32_t tune_primary, int32_t tune_shadow);
+/* Windows, segments and queue bytes of the plan. */
+ER_API er_status er_batch_info(int32_t batch_id, int32_t* n_windows, int32_t* n_segments, int64_t* queue_bytes);
+ER_API er_status er_batch_destroy(int32_t batch_id);
+
 /* One reference frame with explicit per-pixel lanes: d_lanes holds 2*W*H
    uint32 (lane 0 block then lane 1 block) and is advanced in place exactly as
    KrnlSingleScattering advances RandomSeeds1/2 (Source/singlescattering.cuh:27-32);

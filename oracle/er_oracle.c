@@ -18,7 +18,7 @@
  * (Source/vector.h:27-43) are A < B ? A : B, A > B ? A : B and
  * Max(lo, Min(v, hi)); fminf/fmaxf are the IEEE functions.
  */
-#include "er_oracle.h"
+#include "er_capi.h"
 #include "er_math.h"
 
 #include <float.h>
@@ -27,6 +27,33 @@
 #include <stdlib.h>
 #include <string.h>
 #include <unistd.h>
+
+/* a float field of an er_capi.h descriptor (stays float in the FP64 build) */
+typedef float desc_f32;
+
+#ifdef ER_ORACLE_FP64
+/* FP64 oracle build: every float of the restatement (and of er_oracle.h,
+   included below) is a double, and the elementary functions are the C
+   library's double functions.  The descriptors of er_capi.h keep their
+   float fields (included above); the RNG keeps its 23-bit uniforms. */
+#define float double
+#define sqrtf sqrt
+#define fabsf fabs
+#define floorf floor
+#define fminf fmin
+#define fmaxf fmax
+#define er_logf log
+#define er_expf exp
+#define er_powf pow
+#define er_sinf sin
+#define er_cosf cos
+#define er_tanf tan
+#define er_acosf acos
+#define er_atan2f atan2
+#define er_sincosf(x, s, c) (*(s) = sin(x), *(c) = cos(x))
+#endif
+
+#include "er_oracle.h"
 
 /* ------------------------------------------------------------------ */
 /* small vector algebra (Source/vector.h:397-552)                       */
@@ -440,19 +467,19 @@ static inline void isect_invalid(isect_t* i)             /* :47-56 */
 }
 
 /* TransformPoint / TransformVector / TransformRay - Source/geometry.h:30-68 */
-static inline v3 xform_point(const float m[4][4], v3 p)
+static inline v3 xform_point(const desc_f32 m[4][4], v3 p)
 {
     return V3(m[0][0] * p.x + m[0][1] * p.y + m[0][2] * p.z + m[0][3],
               m[1][0] * p.x + m[1][1] * p.y + m[1][2] * p.z + m[1][3],
               m[2][0] * p.x + m[2][1] * p.y + m[2][2] * p.z + m[2][3]);
 }
-static inline v3 xform_vector(const float m[4][4], v3 v)
+static inline v3 xform_vector(const desc_f32 m[4][4], v3 v)
 {
     return V3(m[0][0] * v.x + m[0][1] * v.y + m[0][2] * v.z,
               m[1][0] * v.x + m[1][1] * v.y + m[1][2] * v.z,
               m[2][0] * v.x + m[2][1] * v.y + m[2][2] * v.z);
 }
-static inline ray_t xform_ray(const float m[4][4], const ray_t* r)
+static inline ray_t xform_ray(const desc_f32 m[4][4], const ray_t* r)
 {
     ray_t t;
     const v3 P = xform_point(m, r->O);
@@ -737,9 +764,9 @@ static col3 evaluate_texture(const or_scene* s, int id, v2 UV)
         case ER_PROCEDURAL_UNIFORM: L = C3(P->uniform_color[0], P->uniform_color[1], P->uniform_color[2]); break;
         case ER_PROCEDURAL_CHECKER: {
             const int u = (int)(tuv.x * 2.0f), v = (int)(tuv.y * 2.0f);
-            const float* c1 = P->checker_color1;
-            const float* c2 = P->checker_color2;
-            const float* c = (u % 2 == 0) ? ((v % 2 == 0) ? c1 : c2) : ((v % 2 == 0) ? c2 : c1);
+            const desc_f32* c1 = P->checker_color1;
+            const desc_f32* c2 = P->checker_color2;
+            const desc_f32* c = (u % 2 == 0) ? ((v % 2 == 0) ? c1 : c2) : ((v % 2 == 0) ? c2 : c1);
             L = C3(c[0], c[1], c[2]);
             break;
         }
@@ -1527,6 +1554,7 @@ typedef struct {
     int mode;               /* 0 frame, 1 sum */
     uint32_t* lanes;
     float* out;
+    float* out2;            /* sums of squares (render_moments) or NULL */
     int spp;
     uint32_t view, first;
     int x0, y0, w, h;
@@ -1556,16 +1584,25 @@ static void* job_run(void* arg)
                 const int x = j->x0 + xi;
                 const uint32_t pix = (uint32_t)y * (uint32_t)W + (uint32_t)x;
                 float acc[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
+                float acc2[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
                 for (int k = 0; k < j->spp; k++) {
                     rng_t rng;
                     er_seed_lanes(s->st.seed, j->view, pix, j->first + (uint32_t)k, &rng.s0, &rng.s1);
                     float o[4];
                     single_scattering(s, x, y, &rng, o);
                     acc[0] += o[0]; acc[1] += o[1]; acc[2] += o[2]; acc[3] += o[3];
+                    if (j->out2) {
+                        acc2[0] += o[0] * o[0]; acc2[1] += o[1] * o[1]; acc2[2] += o[2] * o[2]; acc2[3] += o[3] * o[3];
+                    }
                     s->samples++;
                 }
-                float* d = &j->out[4 * ((size_t)r * (size_t)j->w + (size_t)xi)];
+                const size_t q = 4 * ((size_t)r * (size_t)j->w + (size_t)xi);
+                float* d = &j->out[q];
                 d[0] = acc[0]; d[1] = acc[1]; d[2] = acc[2]; d[3] = acc[3];
+                if (j->out2) {
+                    float* d2 = &j->out2[q];
+                    d2[0] = acc2[0]; d2[1] = acc2[1]; d2[2] = acc2[2]; d2[3] = acc2[3];
+                }
             }
         }
     }
@@ -1610,6 +1647,17 @@ void ER_OR(render_sum)(or_scene* s, int32_t spp, uint32_t view, uint32_t first_s
     job_t proto;
     memset(&proto, 0, sizeof(proto));
     proto.scene = s; proto.mode = 1; proto.out = sum; proto.spp = spp; proto.view = view; proto.first = first_sample;
+    proto.x0 = x0; proto.y0 = y0; proto.w = w; proto.h = h;
+    run_jobs(s, &proto, h, nthreads);
+}
+
+void ER_OR(render_moments)(or_scene* s, int32_t spp, uint32_t view, uint32_t first_sample,
+                           int32_t x0, int32_t y0, int32_t w, int32_t h, float* sum, float* sum2, int32_t nthreads)
+{
+    job_t proto;
+    memset(&proto, 0, sizeof(proto));
+    proto.scene = s; proto.mode = 1; proto.out = sum; proto.out2 = sum2; proto.spp = spp; proto.view = view;
+    proto.first = first_sample;
     proto.x0 = x0; proto.y0 = y0; proto.w = w; proto.h = h;
     run_jobs(s, &proto, h, nthreads);
 }

@@ -14,6 +14,12 @@
  * The same entry points are exported by both libraries with the prefixes
  * or_ (this restatement, oracle/_build/liberoracle.so) and ref_ (the
  * reference, oracle/_ref/liberref.so), so a test can run both on one input.
+ *
+ * FP64 oracle: er_oracle.c compiled with -DER_ORACLE_FP64 (prefix fp64_,
+ * oracle/_build/liberfp64.so) evaluates the same estimators in binary64
+ * with the C library's double functions; every `float` of this header is a
+ * `double` there.  It is the converged reference of the image-RMSE
+ * measurements, not a bit-exact checker.
  */
 #ifndef ER_ORACLE_H
 #define ER_ORACLE_H
@@ -51,6 +57,10 @@ void ER_OR(render_frame)(or_scene* scene, uint32_t* lanes, float* frame, int32_t
    [x0, x0+w) x [y0, y0+h); sum receives w*h float4. */
 void ER_OR(render_sum)(or_scene* scene, int32_t spp, uint32_t view, uint32_t first_sample,
                        int32_t x0, int32_t y0, int32_t w, int32_t h, float* sum, int32_t nthreads);
+/* render_sum plus the per-pixel sums of squares of the four components
+   (sum2 receives w*h float4) */
+void ER_OR(render_moments)(or_scene* scene, int32_t spp, uint32_t view, uint32_t first_sample,
+                           int32_t x0, int32_t y0, int32_t w, int32_t h, float* sum, float* sum2, int32_t nthreads);
 
 /* The reference pipeline of RenderEstimate after the transport kernel
    (Source/core.cu:130-135): 3x3 Gaussian frame filter, running estimate

@@ -1,6 +1,7 @@
 """ctypes loader of the CPU oracle (test infrastructure).
 
 `or_` = oracle/_build/liberoracle.so, the C restatement of the reference path;
+`fp64_` = oracle/_build/liberfp64.so, the same restatement in binary64;
 `ref_` = oracle/_ref/liberref.so, the reference's own code built for this host
 (present only where the reference sources were available at build time).
 """
@@ -22,6 +23,7 @@ PKG = importlib.import_module("exposure-render_gb300")
 C = PKG.capi
 
 ORACLE_SO = os.path.join(ROOT, "oracle", "_build", "liberoracle.so")
+FP64_SO = os.path.join(ROOT, "oracle", "_build", "liberfp64.so")
 REF_SO = os.path.join(ROOT, "oracle", "_ref", "liberref.so")
 
 
@@ -38,6 +40,11 @@ class Oracle:
         f("scene_destroy", None, [c_void_p])
         f("render_frame", None, [c_void_p, c_void_p, c_void_p, c_int32])
         f("render_sum", None, [c_void_p, c_int32, c_uint32, c_uint32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_int32])
+        if prefix != "ref_":
+            f("render_moments", None, [c_void_p, c_int32, c_uint32, c_uint32, c_int32, c_int32, c_int32, c_int32, c_void_p,
+                                       c_void_p, c_int32])
+        # the FP64 build takes double buffers wherever the float build takes float
+        self.real = np.float64 if prefix == "fp64_" else np.float32
         f("post_frame", None, [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_float])
         f("lookups_per_sample", c_double, [])
         f("rng_draws", None, [c_uint32, c_uint32, c_int32, c_void_p])
@@ -98,9 +105,18 @@ class SceneHandle:
     def render_sum(self, spp: int, view: int = 0, first: int = 0, rect=None, nthreads: int = 8) -> np.ndarray:
         W, H = self.scene.width, self.scene.height
         x0, y0, w, h = rect if rect is not None else (0, 0, W, H)
-        out = np.zeros((h, w, 4), dtype=np.float32)
+        out = np.zeros((h, w, 4), dtype=self.orc.real)
         self.orc.render_sum(self.h, spp, view, first, x0, y0, w, h, ptr(out), nthreads)
         return out
+
+    def render_moments(self, spp: int, view: int = 0, first: int = 0, rect=None, nthreads: int = 8):
+        """(sum, sum of squares) per pixel and component"""
+        W, H = self.scene.width, self.scene.height
+        x0, y0, w, h = rect if rect is not None else (0, 0, W, H)
+        out = np.zeros((h, w, 4), dtype=self.orc.real)
+        out2 = np.zeros((h, w, 4), dtype=self.orc.real)
+        self.orc.render_moments(self.h, spp, view, first, x0, y0, w, h, ptr(out), ptr(out2), nthreads)
+        return out, out2
 
 
 def initial_lanes(seed: int, width: int, height: int) -> np.ndarray:
@@ -143,6 +159,13 @@ def load_oracle() -> Oracle:
     if not os.path.exists(ORACLE_SO):
         build_oracle()
     return Oracle(ORACLE_SO, "or_")
+
+
+def load_fp64() -> Oracle:
+    """The FP64 oracle (oracle/_build/liberfp64.so): converged reference images."""
+    if not os.path.exists(FP64_SO):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "fp64"], check=True)
+    return Oracle(FP64_SO, "fp64_")
 
 
 def load_ref() -> Oracle | None:

@@ -57,12 +57,13 @@ def test_host_only_calls(lib):
 def test_struct_layout_matches_c():
     structs = ["er_plf", "er_color_tf", "er_shape", "er_light_desc", "er_procedural", "er_texture_desc", "er_volume_desc",
                "er_bitmap_desc", "er_object_desc", "er_clipping_object_desc", "er_camera_desc", "er_render_settings",
-               "er_tracer_desc"]
+               "er_tracer_desc", "er_batch_view"]
     src = '#include <stdio.h>\n#include <stddef.h>\n#include "er_capi.h"\nint main(void){\n'
     for s in structs:
         src += f'printf("{s} %zu\\n", sizeof({s}));\n'
     src += 'printf("settings.seed %zu\\n", offsetof(er_render_settings, seed));\n'
-    src += 'printf("tracer.volume_id %zu\\n", offsetof(er_tracer_desc, volume_id));\nreturn 0;}\n'
+    src += 'printf("tracer.volume_id %zu\\n", offsetof(er_tracer_desc, volume_id));\n'
+    src += 'printf("batch.d_sum %zu\\n", offsetof(er_batch_view, d_sum_xyza));\nreturn 0;}\n'
     with tempfile.TemporaryDirectory() as d:
         c = os.path.join(d, "s.c")
         open(c, "w").write(src)
@@ -74,3 +75,4 @@ def test_struct_layout_matches_c():
         assert int(got[s]) == ctypes.sizeof(getattr(C, s)), s
     assert int(got["settings.seed"]) == C.er_render_settings.seed.offset
     assert int(got["tracer.volume_id"]) == C.er_tracer_desc.volume_id.offset
+    assert int(got["batch.d_sum"]) == C.er_batch_view.d_sum_xyza.offset
