@@ -42,11 +42,8 @@ WORKLOADS = {
     "c2": dict(name="c2-ct-shells-512^3-1024^2-256spp", res=512, film=(1024, 1024), spp=256),
     "c1": dict(name="c1-blobs-128^3-256^2-64spp", res=128, film=(256, 256), spp=64),
 }
-# algorithmic bytes per sample: 16 bytes per reference volume lookup (8 corners
-# x uint16) plus one float4 accumulate read+write, with the mean lookups per
-# sample of the reference estimator measured by the oracle on the workload
+# algorithmic bytes: 16 per volume lookup (8 corners x uint16)
 BYTES_PER_LOOKUP = 16.0
-BYTES_PER_SAMPLE_FIXED = 32.0
 
 
 def make_scene(wl):
@@ -133,20 +130,6 @@ def profile_traffic(wl):
     return None
 
 
-def lookups_per_sample(scene, nthreads, crop=24):
-    """Mean reference-estimator volume lookups per sample on a centre crop (oracle)."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle_lib as OL
-    orc = OL.load_oracle()
-    h = OL.SceneHandle(orc, scene)
-    W, H = scene.width, scene.height
-    x0, y0 = W // 2 - crop // 2, H // 2 - crop // 2
-    h.render_sum(1, rect=(x0, y0, crop, crop), nthreads=nthreads)
-    L = orc.lookups_per_sample()
-    h.close()
-    return L
-
-
 def cpu_reference_rate(scene, seconds_target=12.0, nthreads=None, steps=1):
     """Samples/s of the reference transport on the host cores (all threads)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -175,6 +158,153 @@ def cpu_reference_rate(scene, seconds_target=12.0, nthreads=None, steps=1):
         rates.append(side * side / (time.perf_counter() - t0))
     h.close()
     return float(np.median(rates)), kind, nthreads, f"{side}x{side} centre crop x 1 spp per step"
+
+
+def read_profile(lib, C):
+    """(ms, launches) per wavefront stage since the previous read"""
+    ms = np.zeros(4, dtype=np.float64)
+    n = np.zeros(4, dtype=np.int64)
+    C.check(lib.er_profile_read(ms.ctypes.data, n.ctypes.data))
+    return ms, n
+
+
+def oracle_work(scene, settings, nthreads):
+    """Per-sample work counters of the estimator (oracle, same settings) over
+    the whole field of view at a 128^2 film."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as OL
+    C = importlib.import_module("exposure-render_gb300.capi")
+    t = C.er_tracer_desc.from_buffer_copy(scene.tracer)
+    ctypes.memmove(ctypes.byref(t.settings), ctypes.byref(settings), ctypes.sizeof(settings))
+    t.camera.film_size[0] = t.camera.film_size[1] = 128
+    saved = scene.tracer
+    scene.tracer = t
+    orc = OL.load_oracle()
+    h = OL.SceneHandle(orc, scene)
+    h.render_sum(2, nthreads=nthreads)
+    h.close()
+    scene.tracer = saved
+    return OL.render_stats(orc)
+
+
+# bytes of the queue records (er_wavefront.cu): event 5 float4, shadow job 6 float4, result 1 float4
+EVENT_BYTES, JOB_BYTES, RESULT_BYTES = 80.0, 96.0, 16.0
+
+
+def stage_bytes(w):
+    """Algorithmic bytes per sample of each wavefront stage: 16 per volume
+    lookup (8 uint16 corners), 4 per majorant-grid read, the queue records
+    written and read.  The event normal is computed by the shade stage."""
+    ev = w["events"]
+    ff = w["free_flight_lookups"] - w["normal_lookups"]
+    shade_lk = w["lookups"] - ff - w["shadow_lookups"]
+    return {
+        "primary": BYTES_PER_LOOKUP * ff + 4.0 * (w["majorant_reads"] - w["shadow_majorant_reads"])
+        + RESULT_BYTES * (1.0 - ev) + EVENT_BYTES * ev,
+        "shade": EVENT_BYTES * ev + BYTES_PER_LOOKUP * shade_lk + JOB_BYTES * ev,
+        "shadow": JOB_BYTES * ev + BYTES_PER_LOOKUP * w["shadow_lookups"] + 4.0 * w["shadow_majorant_reads"] + RESULT_BYTES * ev,
+        "reduce": RESULT_BYTES,
+    }
+
+
+def stage_roofline(work, stage_ms, stage_launches, samples, peaks, peak_kind, wl):
+    names = ("primary", "shade", "shadow", "reduce")
+    bps = stage_bytes(work)
+    total = float(sum(stage_ms)) or 1.0
+    stages = {}
+    for i, n in enumerate(names):
+        t = float(stage_ms[i])
+        stages[n] = {"ms": t, "share": t / total, "launches": int(stage_launches[i]),
+                     "bytes_per_sample": bps[n], "achieved_gbs": (bps[n] * samples / (t / 1e3) / 1e9) if t > 0 else None}
+    top = max(names, key=lambda n: stages[n]["ms"])
+    i = names.index(top)
+    launches = max(int(stage_launches[i]), 1)
+    achieved = stages[top]["achieved_gbs"] or 0.0
+    traffic = profile_traffic(wl)
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+        "peak_source": peak_kind, "kernel": "k_wf_" + top, "avg_launch_ms": stages[top]["ms"] / launches,
+        "algorithmic_bytes_per_launch": bps[top] * samples / launches,
+        "traffic": (traffic.get(top) if traffic else None),
+    }
+    return roofline, stages
+
+
+def convergence(lib, runtime, torch, names, patches, max_spp=4096, target=1e-2):
+    """RMSE against the FP64 references (tests/golden/fp64_<name>.npz) of the
+    views `names` of scenes.rmse_views(), for each estimator configuration in
+    `patches` (settings overrides), at 1, 2, 4, ... samples per pixel, and the
+    samples per pixel at which each reaches `target`."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import convergence as CV
+    S = importlib.import_module("exposure-render_gb300.scenes")
+    out = {}
+    for name, sc in S.rmse_views(names=names):
+        ref = CV.load_reference(name)
+        r = runtime.Renderer(sc, lib)
+        W, H = sc.width, sc.height
+        res = {}
+        for label, patch in patches.items():
+            for k, v in patch.items():
+                setattr(r.tracer_desc.settings, k, v)
+            r.rebind_tracer()
+            acc = torch.zeros((H, W, 4), dtype=torch.float64, device="cuda")
+            d = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+            n, spps, errs = 0, [], []
+            while n < max_spp:
+                chunk = max(n, 1)
+                r.trace_sum_device(d.data_ptr(), chunk, 0, n, 0, None)
+                acc += d.double()
+                n += chunk
+                err = CV.rmse((acc / n).cpu().numpy(), ref)
+                spps.append(n)
+                errs.append(err)
+                if err < 0.5 * target:
+                    break
+            res[label] = {"spp": spps, "rmse": errs, "spp_to_target": CV.spp_to_rmse(spps, errs, target)}
+        res["reference_noise"] = float(np.sqrt(ref["noise2"]))
+        res["reference_spp"] = int(ref["spp"])
+        out[name] = res
+        r.close()
+    return out
+
+
+def rmse_summary(conv, name, fast_value, plain_value, npix, target=1e-2):
+    """time to reach image RMSE `target` on the workload's film, from the
+    samples per pixel the 128^2 reference view needed and the measured rates"""
+    if not conv or name not in conv:
+        return None
+    c = conv[name]
+    f, p = c["fast"]["spp_to_target"], c["plain"]["spp_to_target"]
+    out = {"target": target, "reference": f"FP64 oracle, {c['reference_spp']} spp, noise {c['reference_noise']:.1e}",
+           "fast": {"spp": f, "seconds": f * npix / (fast_value * 1e6) if f else None},
+           "plain": {"spp": p, "seconds": p * npix / (plain_value * 1e6) if p else None,
+                     "rmse_at_max_spp": c["plain"]["rmse"][-1]},
+           "curves": c}
+    if f and p:
+        out["speedup_equal_rmse"] = out["plain"]["seconds"] / out["fast"]["seconds"]
+    return out
+
+
+def batched_rmse_summary(conv, value, plain_value, target=1e-2):
+    """speed-up of the batched path over the plain path at equal RMSE: the
+    throughput ratio times the geometric mean over the three volumes' views of
+    the ratio of samples per pixel each estimator needs to reach `target`"""
+    if not conv:
+        return None
+    ratios, per = [], {}
+    for name, c in conv.items():
+        f, p = c["fast"]["spp_to_target"], c["plain"]["spp_to_target"]
+        per[name] = {"fast_spp": f, "plain_spp": p, "plain_rmse_at_max_spp": c["plain"]["rmse"][-1],
+                     "reference_noise": c["reference_noise"]}
+        if f and p:
+            ratios.append(p / f)
+    out = {"target": target, "views": per, "throughput_ratio": value / plain_value}
+    if ratios and len(ratios) == len(conv):
+        g = float(np.exp(np.mean(np.log(ratios))))
+        out["spp_ratio_geomean"] = g
+        out["speedup_equal_rmse"] = value / plain_value * g
+    return out
 
 
 def run_reference(args, wl, rank, world):
@@ -216,6 +346,7 @@ def run_ours(args, wl, rank, world, local_rank):
     width, height = scene.width, scene.height
     stream = torch.cuda.current_stream()
     C.check(lib.er_set_stream(ctypes.c_void_p(stream.cuda_stream)))
+    tuned = r.autotune(2) if not args.no_tune else None     # majorant brick and stage occupancy
     d_sum = torch.zeros((height, width, 4), dtype=torch.float32, device="cuda")
 
     def step(k):
@@ -231,6 +362,8 @@ def run_ours(args, wl, rank, world, local_rank):
         dist.barrier()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stage_ms, stage_launches = read_profile(lib, C)          # clears earlier marks
+    C.check(lib.er_profile_enable(1))
     with ClockSampler(local_rank) as clk:
         ev0.record(stream)
         for k in range(args.steps):
@@ -238,6 +371,8 @@ def run_ours(args, wl, rank, world, local_rank):
         ev1.record(stream)
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
+    C.check(lib.er_profile_enable(0))
+    stage_ms, stage_launches = read_profile(lib, C)
     if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -265,7 +400,7 @@ def run_ours(args, wl, rank, world, local_rank):
         r.rebind_tracer()
         return samples_per_step / (a.elapsed_time(b) / 1e3) / 1e6
 
-    plain = timed_plain({"free_flight": 0})
+    plain = timed_plain({"free_flight": 0, "mis": 0})
     ref_order = timed_plain({"free_flight": 0, "mis": 0, "apply_shading_type": 0, "bilateral": 0})
 
     # end to end through the C ABI with host buffers
@@ -301,20 +436,16 @@ def run_ours(args, wl, rank, world, local_rank):
 
     if rank != 0:
         return
+    conv = None
+    if world == 1 and not args.no_rmse:
+        conv = convergence(lib, runtime, torch, ["c2"], {
+            "fast": {"free_flight": 1, "majorant_brick": r.tracer_desc.settings.majorant_brick},
+            "plain": {"free_flight": 0, "mis": 0}})
     peaks, peak_kind = measured_peaks()
     nthreads = os.cpu_count() or 1
-    # algorithmic bytes are defined by the reference estimator (fixed-step march)
-    scene.tracer.settings.free_flight = 0
-    L = lookups_per_sample(scene, nthreads)
-    bytes_per_sample = BYTES_PER_LOOKUP * L + BYTES_PER_SAMPLE_FIXED
-    achieved = bytes_per_sample * samples_per_step * args.steps / (ms / 1e3) / 1e9
-    traffic = profile_traffic(wl)
-    roofline = {
-        "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-        "peak_source": peak_kind, "kernel": "k_trace_sum",
-        "algorithmic_bytes_per_sample": bytes_per_sample, "reference_lookups_per_sample": L,
-        "traffic": (traffic["dram_bytes_per_launch"] if traffic else None),
-    }
+    # work per sample of the measured configuration (oracle, whole field of view at 128^2)
+    work = oracle_work(scene, r.tracer_desc.settings, nthreads)
+    roofline, stages = stage_roofline(work, stage_ms, stage_launches, samples_per_step * args.steps, peaks, peak_kind, wl)
     cpu_rate, kind, cores, sample = (None, None, None, None)
     if world == 1:
         cpu_rate, kind, cores, sample = cpu_reference_rate(scene, seconds_target=12.0, steps=1)
@@ -323,7 +454,8 @@ def run_ours(args, wl, rank, world, local_rank):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": W["name"], "film": list(W["film"]), "spp": W["spp"], **shading,
-                   "kernel": "k_trace_sum",
+                   "kernels": "k_wf_primary / k_wf_shade / k_wf_shadow / k_wf_reduce (wavefront stages)",
+                   "autotune": tuned,
                    "l2": "inputs larger than L2 (volume %d MiB)" % (vol_bytes >> 20) if vol_bytes > (129 << 20) else
                    "volume fits in L2 (%d MiB); transport re-reads it from L2" % (vol_bytes >> 20),
                    "parallelism": "replicas" if world > 1 else "single"},
@@ -333,9 +465,12 @@ def run_ours(args, wl, rank, world, local_rank):
         "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(vol_bytes + tr_bytes),
                 "d2h_bytes_per_step": int(out.nbytes)},
         "clocks": clk.summary(),
-        "gpu_launches": args.steps,
+        "gpu_launches": int(sum(stage_launches)),
+        "stages": stages,
+        "work_per_sample": work,
         "plain": {"value": plain, "unit": "Msamples/s", "speedup": value / plain,
-                  "what": "same workload and shading, fixed-step march (reference free flight)"},
+                  "what": "same workload and shading model, the reference's estimator: fixed-step march, light sampling only"},
+        "time_to_rmse": rmse_summary(conv, "c2", value, plain, width * height),
         "reference_order": {"value": ref_order, "unit": "Msamples/s",
                             "what": "reference live path (march, BRDF, light sampling), bit-exact with the reference"},
     }
@@ -362,6 +497,14 @@ def run_batched(args, rank, world, local_rank):
         sc.tracer.settings.seed = 1 + rank
     rs = [runtime.Renderer(sc, lib) for sc in scenes]
     views = S.c3_views(n_views=args.views)
+    # autotune each volume's tracer on one of its views (probe: 2 spp)
+    tuned = []
+    for k, r in enumerate(rs):
+        cams = [cam for (kk, cam, _) in views if kk == k]
+        if cams and not args.no_tune:
+            r.tracer_desc.camera = cams[0]
+            r.rebind_tracer()
+            tuned.append(r.autotune(2))
     sums = [torch.zeros((cam.film_size[1], cam.film_size[0], 4), dtype=torch.float32, device="cuda") for _, cam, _ in views]
     table = [(rs[k].tracer_id, spp, d.data_ptr(), cam) for (k, cam, spp), d in zip(views, sums)]
     samples_per_step = sum(cam.film_size[0] * cam.film_size[1] * spp for _, cam, spp in views)
@@ -389,6 +532,17 @@ def run_batched(args, rank, world, local_rank):
         ms = timed(step, args.steps)
     value = world * samples_per_step * args.steps / (ms / 1e3) / 1e6
 
+    # stage shares: the same batch launched without the graph, profiled
+    prof = runtime.Batch(table, flags=0)
+    prof.launch(sp)
+    torch.cuda.synchronize()
+    read_profile(lib, C)
+    C.check(lib.er_profile_enable(1))
+    prof_ms = timed(lambda: prof.launch(sp), 1)
+    C.check(lib.er_profile_enable(0))
+    stage_ms, stage_launches = read_profile(lib, C)
+    prof.close()
+
     # the same views, one single-view batch (graph) per view, back to back
     singles = [runtime.Batch([t], flags=C.ER_BATCH_GRAPH) for t in table]
     for b in singles:
@@ -415,6 +569,12 @@ def run_batched(args, rank, world, local_rank):
         ctypes.memmove(ctypes.byref(r.tracer_desc), ctypes.byref(saved), ctypes.sizeof(saved))
         r.rebind_tracer()
     plain_value = plain_samples / (plain_ms / 1e3) / 1e6
+
+    # equal-RMSE comparison on the first view of each volume (128^2, FP64 references)
+    conv = None
+    if world == 1 and not args.no_rmse:
+        conv = convergence(lib, runtime, torch, ["c3v0", "c3v1", "c3v2"],
+                           {"fast": {"free_flight": 1}, "plain": {"free_flight": 0, "mis": 0}})
 
     # end to end with host buffers: volumes bound from host memory, one batch
     # launch, every view's sums read back into pinned host memory
@@ -448,15 +608,20 @@ def run_batched(args, rank, world, local_rank):
                    "samples_per_step": samples_per_step, "films": sorted({c.film_size[0] for _, c, _ in views}),
                    "spp_range": [min(s for _, _, s in views), max_spp], **describe_shading(scenes[0]),
                    "windows": info["windows"], "segments": info["segments"], "queue_bytes": info["queue_bytes"],
+                   "autotune": tuned,
                    "l2": "volumes %d MiB in total; every step renders fresh samples" % (vol_bytes >> 20),
                    "parallelism": "replicas" if world > 1 else "single"},
         "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(vol_bytes),
                 "d2h_bytes_per_step": int(sum(h.numel() * 4 for h in host_sums))},
         "clocks": clk.summary(),
         "gpu_launches": args.steps * (4 * info["windows"]),
+        "stages": {n: {"ms": float(stage_ms[i]), "share": float(stage_ms[i] / max(stage_ms.sum(), 1e-9)),
+                       "launches": int(stage_launches[i])} for i, n in enumerate(("primary", "shade", "shadow", "reduce"))},
+        "profiled_pass_ms": prof_ms,
         "one_batch_per_view": {"value": seq_value, "unit": "Msamples/s", "speedup": value / seq_value},
         "plain": {"value": plain_value, "unit": "Msamples/s", "speedup": value / plain_value, "views": args.plain_views,
                   "what": "reference estimator (march, light sampling, BRDF), 1 spp per RenderEstimate, one view at a time"},
+        "equal_rmse": batched_rmse_summary(conv, value, plain_value),
     }
     print(json.dumps(line), flush=True)
     batch.close()
@@ -475,6 +640,8 @@ def main():
     ap.add_argument("--plain-views", type=int, default=16, help="c3: views timed on the plain one-view path")
     ap.add_argument("--film", type=int, default=0, help="square film edge (smaller profiling cases; 0 = the workload's)")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel (0 = the workload's)")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default settings)")
+    ap.add_argument("--no-rmse", action="store_true", help="skip the time-to-RMSE measurement")
     args = ap.parse_args()
     if (args.film or args.spp) and args.workload in WORKLOADS:
         W = dict(WORKLOADS[args.workload])

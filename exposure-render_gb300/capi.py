@@ -195,6 +195,17 @@ class er_tracer_desc(Structure):
     ]
 
 
+class er_tune_result(Structure):
+    _fields_ = [
+        ("majorant_brick", c_int32),
+        ("tune_primary", c_int32),
+        ("tune_shadow", c_int32),
+        ("from_cache", c_int32),
+        ("msamples_per_s", c_float),
+        ("candidates", c_int32),
+    ]
+
+
 class er_batch_view(Structure):
     _fields_ = [
         ("tracer_id", c_int32),
@@ -397,6 +408,10 @@ def _declare(lib) -> None:
         "er_batch_set_tuning": (c_int32, [c_int32, c_int32, c_int32]),
         "er_batch_info": (c_int32, [c_int32, i32p, i32p, POINTER(ctypes.c_int64)]),
         "er_batch_destroy": (c_int32, [c_int32]),
+        "er_autotune_tracer": (c_int32, [c_int32, c_int32, POINTER(er_tune_result)]),
+        "er_get_render_settings": (c_int32, [c_int32, POINTER(er_render_settings)]),
+        "er_profile_enable": (c_int32, [c_int32]),
+        "er_profile_read": (c_int32, [c_void_p, c_void_p]),
         "er_trace_frame_device": (c_int32, [c_int32, c_void_p, c_void_p, c_void_p]),
         "er_post_frame_device": (c_int32, [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_float, c_int32, c_void_p]),
         "er_tonemap_device": (c_int32, [c_void_p, c_float, c_void_p, c_int32, c_int32, c_float, c_void_p]),

@@ -91,6 +91,13 @@ struct WavefrontBuffers {
    sample rows of at most window_cap items (one row at least) */
 void er_wavefront_plan(const int* npix, const int* spp, int n_views, size_t window_cap, WavefrontPlan& plan);
 
+/* stage timing of the wavefront launches: 0 primary, 1 shade, 2 shadow,
+   3 reduce; read returns the accumulated milliseconds and launch counts since
+   the previous read (and clears them) */
+#define WF_STAGES 4
+void er_wavefront_profile_enable(bool on);
+cudaError_t er_wavefront_profile_read(double* ms, int64_t* launches);
+
 /* one view with its parameters passed by value (no device tables) */
 cudaError_t er_launch_wavefront_one(const WfView& view, const WavefrontPlan& plan, const WavefrontBuffers& B, cudaStream_t s);
 

@@ -32,6 +32,8 @@
 #include <string>
 #include <vector>
 
+#include <sys/stat.h>
+
 #include "er_capi.h"
 #include "er_kernels.h"
 #include "er_math.h"
@@ -86,6 +88,18 @@ struct DevBuf {
         return e;
     }
 };
+
+/* FNV-1a, 64 bit */
+constexpr uint64_t kFnvBasis = 14695981039346656037ull;
+uint64_t fnv1a(uint64_t h, const void* data, size_t n)
+{
+    const unsigned char* p = (const unsigned char*)data;
+    for (size_t i = 0; i < n; i++) {
+        h ^= p[i];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
 
 /* items of one wavefront window: 8M samples, 1.5 GB of queues */
 constexpr size_t kWindowCap = (size_t)8 << 20;
@@ -143,6 +157,7 @@ struct VolumeItem {
     float spacing[3];
     int normalize;
     uint16_t vmax = 0;
+    uint64_t signature = 0;        /* sampled content hash (tuning cache key) */
     DevBuf<uint16_t> vox;
     DevBuf<unsigned int> gm_max_bits;
     float gm_max = -1.0f;          /* lazily computed maximum gradient magnitude */
@@ -172,6 +187,7 @@ struct TracerItem {
     DevBuf<uint32_t> minmax;
     DevBuf<int> err;
     WfQueues wf;
+    DevBuf<float4> tune_sum;       /* probe renders of the autotuner */
     erd::Params P;
     uint64_t built_version = 0;
     bool built = false;
@@ -184,6 +200,7 @@ struct BatchItem {
     int flags = 0;
     size_t window_cap = kWindowCap;
     int tune_primary = 4, tune_shadow = 4;
+    bool tune_explicit = false;    /* set by er_batch_set_tuning; else the first view's tracer settings */
     uint64_t planned_version = 0;  /* context version the plan was made at */
     bool planned = false;
     WavefrontPlan plan;
@@ -654,6 +671,11 @@ er_status batch_plan(BatchItem& b)
     ER_CUDA(cudaMemcpyAsync(b.d_views.p, b.host_views.data(), (size_t)n * sizeof(WfView), cudaMemcpyHostToDevice, st));
     ER_CUDA(cudaMemcpyAsync(b.d_segs.p, b.plan.segs.data(), b.plan.segs.size() * sizeof(WfSegment), cudaMemcpyHostToDevice, st));
     ER_CUDA(cudaStreamSynchronize(st));
+    if (!b.tune_explicit) {
+        const er_render_settings& s0 = find_tracer(b.views[0].tracer_id)->d.settings;
+        b.tune_primary = s0.tune_primary > 0 ? s0.tune_primary : 4;
+        b.tune_shadow = s0.tune_shadow > 0 ? s0.tune_shadow : 4;
+    }
     b.B.tune_primary = b.tune_primary;
     b.B.tune_shadow = b.tune_shadow;
     if (b.flags & ER_BATCH_GRAPH) {
@@ -697,6 +719,110 @@ BatchItem* find_batch(int id)
 {
     auto it = ctx().batches.items.find(id);
     return (id < 0 || it == ctx().batches.items.end()) ? nullptr : it->second.get();
+}
+
+/* ---- autotuner ---- */
+
+std::string tune_cache_path()
+{
+    const char* e = getenv("ER_TUNE_CACHE");
+    if (e && *e) return std::string(e);
+    const char* home = getenv("HOME");
+    if (!home || !*home) return std::string();
+    return std::string(home) + "/.cache/exposurerender_gb300/autotune.txt";
+}
+
+/* device, volume content and every setting that changes the work of a sample */
+uint64_t tune_key(const TracerItem& t, const VolumeItem& v, int probe_spp)
+{
+    cudaDeviceProp prop;
+    memset(&prop, 0, sizeof(prop));
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaGetDeviceProperties(&prop, dev);
+    uint64_t h = fnv1a(kFnvBasis, prop.name, strnlen(prop.name, sizeof(prop.name)));
+    h = fnv1a(h, &prop.multiProcessorCount, sizeof(int));
+    h = fnv1a(h, &v.signature, sizeof(v.signature));
+    h = fnv1a(h, v.spacing, sizeof(v.spacing));
+    er_render_settings s = t.d.settings;
+    s.majorant_brick = 0;
+    s.tune_primary = s.tune_shadow = 0;
+    s.seed = 0;
+    s.bilateral = 0;
+    s.bilateral_radius = 0;
+    s.bilateral_sigma_d = s.bilateral_sigma_r = 0.0f;
+    s.frame_filter = 0;
+    h = fnv1a(h, &s, sizeof(s));
+    h = fnv1a(h, &t.d.opacity, sizeof(t.d.opacity));
+    h = fnv1a(h, &t.d.glossiness, sizeof(t.d.glossiness));
+    h = fnv1a(h, t.d.camera.film_size, sizeof(t.d.camera.film_size));
+    h = fnv1a(h, &t.d.light_count, sizeof(t.d.light_count));
+    h = fnv1a(h, &probe_spp, sizeof(probe_spp));
+    return h;
+}
+
+bool tune_cache_lookup(uint64_t key, er_tune_result& r)
+{
+    const std::string path = tune_cache_path();
+    if (path.empty() || path == "off") return false;
+    FILE* f = fopen(path.c_str(), "r");
+    if (!f) return false;
+    bool found = false;
+    char line[256];
+    while (fgets(line, sizeof(line), f)) {
+        unsigned long long k = 0;
+        int b = 0, p = 0, sh = 0;
+        float m = 0.0f;
+        if (sscanf(line, "%llx %d %d %d %f", &k, &b, &p, &sh, &m) == 5 && (uint64_t)k == key) {
+            r.majorant_brick = b;
+            r.tune_primary = p;
+            r.tune_shadow = sh;
+            r.msamples_per_s = m;
+            found = true;          /* the last entry for a key wins */
+        }
+    }
+    fclose(f);
+    return found;
+}
+
+void tune_cache_store(uint64_t key, const er_tune_result& r)
+{
+    const std::string path = tune_cache_path();
+    if (path.empty() || path == "off") return;
+    /* create the parent directories */
+    for (size_t i = 1; i < path.size(); i++)
+        if (path[i] == '/') mkdir(path.substr(0, i).c_str(), 0755);
+    FILE* f = fopen(path.c_str(), "a");
+    if (!f) return;
+    fprintf(f, "%016llx %d %d %d %.3f\n", (unsigned long long)key, r.majorant_brick, r.tune_primary, r.tune_shadow, r.msamples_per_s);
+    fclose(f);
+}
+
+/* Msamples/s of one probe render with the tracer's current settings */
+er_status time_probe(TracerItem& t, int spp, float* msps)
+{
+    t.built = false;
+    er_status st = build(t);
+    if (st != ER_OK) return st;
+    const size_t npix = (size_t)t.W * t.H;
+    ER_CUDA(t.tune_sum.ensure(npix));
+    cudaStream_t s = ctx().stream;
+    st = trace_sum(t, spp, 0x7fffffffu, 0u, t.tune_sum.p, 0, s);
+    if (st != ER_OK) return st;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ER_CUDA(cudaEventCreate(&a));
+    ER_CUDA(cudaEventCreate(&b));
+    ER_CUDA(cudaEventRecord(a, s));
+    st = trace_sum(t, spp, 0x7fffffffu, (uint32_t)spp, t.tune_sum.p, 0, s);
+    ER_CUDA(cudaEventRecord(b, s));
+    ER_CUDA(cudaEventSynchronize(b));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (st != ER_OK) return st;
+    *msps = ms > 0.0f ? (float)((double)npix * spp / (ms * 1e3)) : 0.0f;
+    return check_device_error(t);
 }
 
 }  // namespace
@@ -830,6 +956,10 @@ ER_API er_status er_bind_volume(const er_volume_desc* d, int32_t* id)
     uint16_t vmax = 0;
     for (size_t i = 0; i < n; i++) vmax = d->voxels[i] > vmax ? d->voxels[i] : vmax;
     v->vmax = vmax;
+    /* content signature of the tuning cache: every 61st voxel */
+    uint64_t sig = fnv1a(kFnvBasis, d->resolution, sizeof(d->resolution));
+    for (size_t i = 0; i < n; i += 61) sig = fnv1a(sig, &d->voxels[i], sizeof(uint16_t));
+    v->signature = sig;
     ER_CUDA(v->vox.ensure(n));
     ER_CUDA(cudaMemcpy(v->vox.p, d->voxels, n * sizeof(uint16_t), cudaMemcpyHostToDevice));
     C.volumes.items[*id] = std::move(v);
@@ -1175,6 +1305,7 @@ ER_API er_status er_batch_set_tuning(int32_t batch_id, int32_t tune_primary, int
     if (!valid(tune_primary) || !valid(tune_shadow)) return fail(ER_ERR_INVALID_ARGUMENT, "tuning values must be 0, 2, 3, 4, 6 or 8");
     if (tune_primary) b->tune_primary = tune_primary;
     if (tune_shadow) b->tune_shadow = tune_shadow;
+    b->tune_explicit = true;
     b->planned = false;   /* re-captured at the next launch */
     return ER_OK;
 }
@@ -1197,6 +1328,93 @@ ER_API er_status er_batch_destroy(int32_t batch_id)
     if (batch_id < 0 || it == ctx().batches.items.end()) return fail(ER_ERR_INVALID_ID, "batch with ID:%d does not exist", batch_id);
     ER_CUDA(cudaDeviceSynchronize());
     ctx().batches.items.erase(it);
+    return ER_OK;
+}
+
+ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tune_result* result)
+{
+    ER_LOCK;
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    if (probe_spp <= 0 || probe_spp > 4096) return fail(ER_ERR_INVALID_ARGUMENT, "probe_spp %d out of range [1, 4096]", probe_spp);
+    er_status st = build(*t);
+    if (st != ER_OK) return st;
+    Context& C = ctx();
+    const VolumeItem& v = *C.volumes.items.find(t->d.volume_id)->second;
+    const uint64_t key = tune_key(*t, v, probe_spp);
+    er_tune_result r;
+    memset(&r, 0, sizeof(r));
+    er_render_settings& s = t->d.settings;
+    const er_render_settings saved = s;
+    if (tune_cache_lookup(key, r)) {
+        r.from_cache = 1;
+    } else {
+        const bool delta = s.free_flight == ER_FREE_FLIGHT_DELTA;
+        const bool wavefront = s.engine != 1;
+        s.tune_primary = s.tune_primary > 0 ? s.tune_primary : 4;
+        s.tune_shadow = s.tune_shadow > 0 ? s.tune_shadow : 4;
+        r.majorant_brick = s.majorant_brick > 0 ? s.majorant_brick : 8;
+        r.tune_primary = s.tune_primary;
+        r.tune_shadow = s.tune_shadow;
+        r.msamples_per_s = -1.0f;
+        /* majorant brick first (the dominant term for delta tracking), then
+           the occupancy variants at the best brick */
+        const int bricks[] = {2, 4, 8, 16};
+        for (int b : bricks) {
+            if (!delta && b != r.majorant_brick) continue;
+            s.majorant_brick = b;
+            float m = 0.0f;
+            st = time_probe(*t, probe_spp, &m);
+            if (st != ER_OK) { s = saved; t->built = false; return st; }
+            r.candidates++;
+            if (m > r.msamples_per_s) { r.msamples_per_s = m; r.majorant_brick = b; }
+        }
+        s.majorant_brick = r.majorant_brick;
+        if (wavefront) {
+            const int variants[][2] = {{4, 4}, {3, 3}, {3, 4}, {4, 3}, {6, 4}, {4, 6}, {2, 3}, {8, 8}};
+            for (const auto& vv : variants) {
+                s.tune_primary = vv[0];
+                s.tune_shadow = vv[1];
+                float m = 0.0f;
+                st = time_probe(*t, probe_spp, &m);
+                if (st != ER_OK) { s = saved; t->built = false; return st; }
+                r.candidates++;
+                if (m > r.msamples_per_s) { r.msamples_per_s = m; r.tune_primary = vv[0]; r.tune_shadow = vv[1]; }
+            }
+        }
+        tune_cache_store(key, r);
+    }
+    s.majorant_brick = r.majorant_brick;
+    s.tune_primary = r.tune_primary;
+    s.tune_shadow = r.tune_shadow;
+    t->built = false;
+    C.version++;            /* batches over this tracer re-plan */
+    st = build(*t);
+    if (st != ER_OK) return st;
+    if (result) *result = r;
+    return ER_OK;
+}
+
+ER_API er_status er_profile_enable(int32_t enable)
+{
+    er_wavefront_profile_enable(enable != 0);
+    return ER_OK;
+}
+
+ER_API er_status er_profile_read(double* ms, int64_t* launches)
+{
+    if (!ms || !launches) return fail(ER_ERR_INVALID_ARGUMENT, "output pointers are NULL");
+    ER_CUDA(er_wavefront_profile_read(ms, launches));
+    return ER_OK;
+}
+
+ER_API er_status er_get_render_settings(int32_t tracer_id, er_render_settings* settings)
+{
+    ER_LOCK;
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    if (!settings) return fail(ER_ERR_INVALID_ARGUMENT, "settings pointer is NULL");
+    *settings = t->d.settings;
     return ER_OK;
 }
 

@@ -34,6 +34,7 @@
  * the sums are bit-identical to k_trace_sum's and to the CPU oracle's.
  */
 #include <cstring>
+#include <mutex>
 
 #include "er_kernels.h"
 #include "er_path.cuh"
@@ -387,6 +388,59 @@ void er_wavefront_plan(const int* npix, const int* spp, int n_views, size_t wind
 
 namespace {
 
+/* stage timing (er_profile_*): CUDA events around every stage launch on the
+   launching stream, read back and accumulated by er_wavefront_profile_read */
+struct StageProfiler {
+    std::mutex m;
+    bool enabled = false;
+    struct Mark { cudaEvent_t a, b; int stage; };
+    std::vector<Mark> pending;
+    std::vector<cudaEvent_t> pool;
+    double ms[WF_STAGES] = {0.0, 0.0, 0.0, 0.0};
+    int64_t launches[WF_STAGES] = {0, 0, 0, 0};
+    cudaEvent_t get()
+    {
+        if (!pool.empty()) {
+            cudaEvent_t e = pool.back();
+            pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+};
+
+StageProfiler& profiler()
+{
+    static StageProfiler* p = new StageProfiler();
+    return *p;
+}
+
+/* records the start of a stage; returns the event or nullptr when off */
+cudaEvent_t stage_begin(cudaStream_t s)
+{
+    StageProfiler& P = profiler();
+    std::lock_guard<std::mutex> lock(P.m);
+    if (!P.enabled) return nullptr;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cs);
+    if (cs != cudaStreamCaptureStatusNone) return nullptr;   /* not inside graphs */
+    cudaEvent_t a = P.get();
+    cudaEventRecord(a, s);
+    return a;
+}
+
+void stage_end(cudaEvent_t a, int stage, cudaStream_t s)
+{
+    if (!a) return;
+    StageProfiler& P = profiler();
+    std::lock_guard<std::mutex> lock(P.m);
+    cudaEvent_t b = P.get();
+    cudaEventRecord(b, s);
+    P.pending.push_back({a, b, stage});
+}
+
 int sm_count()
 {
     int sm = 0, dev = 0;
@@ -413,6 +467,7 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         cudaError_t e = cudaMemsetAsync(B.counters, 0, 2 * sizeof(uint32_t), s);
         if (e != cudaSuccess) return e;
         const uint32_t g1 = (items + 255) / 256 < (uint32_t)sm * 64 ? (items + 255) / 256 : (uint32_t)sm * 64;
+        cudaEvent_t t0 = stage_begin(s);
 #define ER_PRIMARY(M) k_wf_primary<M, ONE><<<g1, 256, 0, s>>>(d_views, dseg, nseg, one, one_seg, items, B.results, B.events, B.counters)
         switch (B.tune_primary) {
         case 2: ER_PRIMARY(2); break;
@@ -422,7 +477,11 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         default: ER_PRIMARY(4); break;
         }
 #undef ER_PRIMARY
+        stage_end(t0, 0, s);
+        t0 = stage_begin(s);
         k_wf_shade<ONE><<<sm * 16, 128, 0, s>>>(d_views, one, B.events, B.counters, B.results, B.jobs, B.counters + 1);
+        stage_end(t0, 1, s);
+        t0 = stage_begin(s);
 #define ER_SHADOW(M) k_wf_shadow<M, ONE><<<sm * 8, 256, 0, s>>>(d_views, one, B.jobs, B.counters + 1, B.results)
         switch (B.tune_shadow) {
         case 2: ER_SHADOW(2); break;
@@ -432,12 +491,15 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         default: ER_SHADOW(4); break;
         }
 #undef ER_SHADOW
+        stage_end(t0, 2, s);
         int max_npix = 0;
         for (int g = s0; g < s1; g++) {
             const int np = plan.view_npix[plan.segs[g].view];
             if (np > max_npix) max_npix = np;
         }
+        t0 = stage_begin(s);
         k_wf_reduce<ONE><<<dim3((max_npix + 255) / 256, ONE ? 1 : nseg), 256, 0, s>>>(d_views, dseg, one, one_seg, B.results, p_in, p_out);
+        stage_end(t0, 3, s);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
@@ -457,4 +519,36 @@ cudaError_t er_launch_wavefront_batch(const WfView* d_views, const WfSegment* d_
     WfView unused;
     memset(&unused, 0, sizeof(unused));
     return launch_windows<false>(d_views, d_segs, unused, plan, B, s);
+}
+
+void er_wavefront_profile_enable(bool on)
+{
+    StageProfiler& P = profiler();
+    std::lock_guard<std::mutex> lock(P.m);
+    P.enabled = on;
+}
+
+cudaError_t er_wavefront_profile_read(double* ms, int64_t* launches)
+{
+    StageProfiler& P = profiler();
+    std::lock_guard<std::mutex> lock(P.m);
+    cudaError_t err = cudaSuccess;
+    for (const auto& k : P.pending) {
+        cudaError_t e = cudaEventSynchronize(k.b);
+        float t = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, k.a, k.b);
+        if (e != cudaSuccess) err = e;
+        P.ms[k.stage] += t;
+        P.launches[k.stage]++;
+        P.pool.push_back(k.a);
+        P.pool.push_back(k.b);
+    }
+    P.pending.clear();
+    for (int i = 0; i < WF_STAGES; i++) {
+        ms[i] = P.ms[i];
+        launches[i] = P.launches[i];
+        P.ms[i] = 0.0;
+        P.launches[i] = 0;
+    }
+    return err;
 }

@@ -98,6 +98,16 @@ class Renderer:
     def trace_frame_device(self, d_lanes_ptr: int, d_frame_ptr: int, stream=None) -> None:
         C.check(self.lib.er_trace_frame_device(self.tracer_id, d_lanes_ptr, d_frame_ptr, stream))
 
+    def autotune(self, probe_spp: int = 2) -> dict:
+        """er_autotune_tracer; the chosen settings are copied into tracer_desc so
+        that a later rebind_tracer keeps them"""
+        r = C.er_tune_result()
+        C.check(self.lib.er_autotune_tracer(self.tracer_id, probe_spp, byref(r)))
+        s = self.tracer_desc.settings
+        s.majorant_brick, s.tune_primary, s.tune_shadow = r.majorant_brick, r.tune_primary, r.tune_shadow
+        return {"majorant_brick": r.majorant_brick, "tune_primary": r.tune_primary, "tune_shadow": r.tune_shadow,
+                "from_cache": bool(r.from_cache), "msamples_per_s": r.msamples_per_s, "candidates": r.candidates}
+
     def gradient_magnitude(self, d_gm_ptr=None) -> float:
         m = c_float(0.0)
         C.check(self.lib.er_gradient_magnitude(self.volume_id, d_gm_ptr, byref(m)))

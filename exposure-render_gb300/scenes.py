@@ -345,3 +345,89 @@ def c3_views(n_views=64, n_volumes=3, seed=7, films=C3_FILMS, spp=(32, 128)) -> 
         cam = orbit_camera(rng, (f, f), radius=float(rng.uniform(1.8, 2.6)))
         views.append((k, cam, int(rng.integers(spp[0], spp[1] + 1))))
     return views
+
+
+# ---------------------------------------------------------------------------
+# views with converged FP64 references (image RMSE measurements)
+# ---------------------------------------------------------------------------
+
+def rmse_views(film=128, names=None) -> list:
+    """(name, Scene) of the views whose converged images the FP64 oracle
+    provides: the c1 scene, the first view of each c3 volume, and c2 - all
+    at a film of `film`^2 with each workload's camera and settings.  `names`
+    restricts the list (and the volumes generated)."""
+    want = set(names) if names else {"c1", "c3v0", "c3v1", "c3v2", "c2"}
+    out = []
+    if "c1" in want:
+        out.append(("c1", scene_c1(res=128, film=(film, film))))
+    c3 = [k for k in range(3) if f"c3v{k}" in want]
+    if c3:
+        views = c3_views()
+        for k in c3:
+            sc = c3_scenes(volumes=(C3_VOLUMES[k],), seed=30 + k)[0]
+            sc.name = f"c3v{k}"
+            cam = C.er_camera_desc.from_buffer_copy([c for (kk, c, _) in views if kk == k][0])
+            cam.film_size[0] = cam.film_size[1] = film
+            sc.tracer.camera = cam
+            out.append((f"c3v{k}", sc))
+    if "c2" in want:
+        out.append(("c2", scene_c2(res=512, film=(film, film))))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# differentiable medium (c4)
+# ---------------------------------------------------------------------------
+
+def blob_density(shape_zyx, n_blobs=10, seed=40) -> np.ndarray:
+    """float32 density in [0, 1]: a clipped sum of anisotropic Gaussians"""
+    Z, Y, X = shape_zyx
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0.25, 0.75, size=(n_blobs, 3)) * np.array([X, Y, Z])
+    sig = rng.uniform(0.06, 0.16, size=(n_blobs, 3)) * np.array([X, Y, Z])
+    amps = rng.uniform(0.3, 0.9, size=n_blobs)
+    z, y, x = np.meshgrid(np.arange(Z), np.arange(Y), np.arange(X), indexing="ij")
+    rho = np.zeros((Z, Y, X), dtype=np.float64)
+    for k in range(n_blobs):
+        rho += amps[k] * np.exp(-0.5 * (((x - centres[k, 0]) / sig[k, 0]) ** 2 + ((y - centres[k, 1]) / sig[k, 1]) ** 2
+                                        + ((z - centres[k, 2]) / sig[k, 2]) ** 2))
+    return np.clip(rho, 0.0, 1.0).astype(np.float32)
+
+
+def ramp_opacity(n=64, lo=0.15, hi=0.7) -> np.ndarray:
+    """opacity B-spline values: 0 below `lo`, rising linearly to 1 at `hi`
+    (control i sits at density (i - 2) / (n - 5))"""
+    u = (np.arange(n) - 2.0) / (n - 5.0)
+    return np.clip((u - lo) / (hi - lo), 0.0, 1.0).astype(np.float32)
+
+
+def spline_majorant(rho, tf, scale, brick=8, margin=1.25, floor=1e-3) -> np.ndarray:
+    """per-brick upper bound of sigma = scale * alpha(rho): the largest
+    B-spline control value over the spline segments that the brick's density
+    range (with a 1-voxel apron) covers (convex-hull property), times
+    `margin`, plus `floor` * scale.  Shape (nbz, nby, nbx), float32."""
+    n = len(tf)
+    Z, Y, X = rho.shape
+    nb = [(d + brick - 1) // brick for d in (Z, Y, X)]
+    out = np.zeros(nb, dtype=np.float32)
+    for bz in range(nb[0]):
+        for by in range(nb[1]):
+            for bx in range(nb[2]):
+                sl = rho[max(bz * brick - 1, 0):min((bz + 1) * brick + 1, Z),
+                         max(by * brick - 1, 0):min((by + 1) * brick + 1, Y),
+                         max(bx * brick - 1, 0):min((bx + 1) * brick + 1, X)]
+                u0 = np.clip(2.0 + float(sl.min()) * (n - 5), 1.0, n - 2.0)
+                u1 = np.clip(2.0 + float(sl.max()) * (n - 5), 1.0, n - 2.0)
+                i0 = min(int(np.floor(u0)), n - 3)
+                i1 = min(int(np.floor(u1)), n - 3)
+                vmax = float(np.max(tf[i0 - 1:i1 + 3]))
+                out[bz, by, bx] = scale * (vmax * margin + floor)
+    return out
+
+
+def medium_scene(res=(128, 128, 128), film=(256, 256), seed=40) -> Scene:
+    """the c1 camera and light around a zero intensity volume of the medium's
+    resolution (the tracer's volume gives the medium its placement)"""
+    lights, textures = c1_lights()
+    t = c1_tracer(film)
+    return Scene("medium", np.zeros(res, dtype=np.uint16), tracer=t, lights=lights, textures=textures, spp=32)

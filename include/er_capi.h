@@ -377,11 +377,48 @@ ER_API er_status er_batch_launch(int32_t batch_id, void* stream);
    advance by spp before each further launch). */
 ER_API er_status er_batch_advance(int32_t batch_id, uint32_t samples, void* stream);
 /* Resource-occupancy variants of the primary and shadow stages (2, 3, 4, 6
-   or 8 resident blocks of 256 threads per SM; 0 keeps the current value). */
+   or 8 resident blocks of 256 threads per SM; 0 keeps the current value).
+   Without this call a batch uses the settings of its first view's tracer. */
 ER_API er_status er_batch_set_tuning(int32_t batch_id, int32_t tune_primary, int32_t tune_shadow);
 /* Windows, segments and queue bytes of the plan. */
 ER_API er_status er_batch_info(int32_t batch_id, int32_t* n_windows, int32_t* n_segments, int64_t* queue_bytes);
 ER_API er_status er_batch_destroy(int32_t batch_id);
+
+/* ---------------------------------------------------------------------- */
+/* autotuner (no reference counterpart)                                    */
+/* ---------------------------------------------------------------------- */
+
+typedef struct er_tune_result {
+    int32_t majorant_brick;   /* edge of the delta tracker's majorant bricks */
+    int32_t tune_primary;     /* occupancy variant of the primary stage */
+    int32_t tune_shadow;      /* occupancy variant of the shadow stage */
+    int32_t from_cache;       /* 1: read from the tuning cache, nothing measured */
+    float msamples_per_s;     /* probe throughput of the chosen configuration */
+    int32_t candidates;       /* configurations timed */
+} er_tune_result;
+
+/* Times probe renders of a bound tracer (probe_spp samples per pixel of its
+   film, one warm-up each) over majorant bricks {2, 4, 8, 16} (delta
+   tracking only) and then the occupancy variants of the wavefront stages,
+   and writes the fastest configuration into the bound tracer's settings (the
+   caller's descriptor is not changed; re-binding it restores its values).
+   Results are cached per device, volume and shading configuration in the
+   file named by the environment variable ER_TUNE_CACHE (default
+   $HOME/.cache/exposurerender_gb300/autotune.txt; "off" disables the
+   cache).  Brick and occupancy change which random numbers a sample draws,
+   not the estimator: the tuned tracer stays bit-exact with the CPU oracle
+   given the same settings.  Synchronous. */
+ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tune_result* result);
+/* Stage timing of the wavefront transport (no reference counterpart): while
+   enabled, every launch outside a CUDA-graph capture records CUDA events
+   around its stages on the launching stream.  er_profile_read waits for them
+   and returns, per stage (0 primary: camera ray, free flight, visible lights;
+   1 shade; 2 shadow segments; 3 per-pixel reduction), the milliseconds and
+   launch counts accumulated since the previous read. */
+ER_API er_status er_profile_enable(int32_t enable);
+ER_API er_status er_profile_read(double* ms4, int64_t* launches4);
+/* The settings the bound tracer renders with (after er_autotune_tracer). */
+ER_API er_status er_get_render_settings(int32_t tracer_id, er_render_settings* settings);
 
 /* One reference frame with explicit per-pixel lanes: d_lanes holds 2*W*H
    uint32 (lane 0 block then lane 1 block) and is advanced in place exactly as

@@ -141,6 +141,7 @@ struct or_scene {
     er_texture_desc* textures;
     /* statistics */
     uint64_t lookups;
+    uint64_t stat[OR_NSTATS];   /* work counters of the last render (render_stats) */
     uint64_t samples;
     /* extension estimators (see er_capi.h): sigma table over integer
        intensities, majorant grid of the delta tracker, 1 / max |grad I| */
@@ -151,9 +152,19 @@ struct or_scene {
     float* majorant;         /* per brick: DensityScale * max sigma over the brick footprint */
     float gm_inv_max;
     int gm_ready;
+    /* differentiable medium (dm_attach): float density grid, cubic B-spline
+       opacity over density, albedo, NEE probability; the majorant grid above
+       is the caller's fixed grid */
+    const float* rho;
+    const float* tf_val;
+    int tf_n;
+    float dm_scale;
+    col3 dm_albedo;
+    float dm_q;
 };
 
 static double g_lookups_per_sample = 0.0;
+static double g_stats[OR_NSTATS];
 static void prepare_extensions(or_scene* s);
 
 /* Shape::Update (Source/shape.h:92-103) with the area helpers :27-55 */
@@ -426,7 +437,13 @@ static v3 gradient(or_scene* s, v3 P)
 }
 
 /* NormalizedGradient - Source/volumes.h:88-91 */
-static v3 normalized_gradient(or_scene* s, v3 P) { return vnorm(gradient(s, P)); }
+static v3 normalized_gradient(or_scene* s, v3 P)
+{
+    const uint64_t lk = s->lookups;
+    const v3 g = vnorm(gradient(s, P));
+    s->stat[OR_STAT_NORMAL_LOOKUPS] += s->lookups - lk;
+    return g;
+}
 
 /* GradientMagnitude - Source/volumes.h:93-114 */
 static float gradient_magnitude(or_scene* s, v3 P)
@@ -1103,8 +1120,9 @@ static inline void dda_advance(const or_scene* s, dda_t* d, float e)
     d->t = e;
 }
 
-static inline float dda_majorant(const or_scene* s, const dda_t* d)
+static inline float dda_majorant(or_scene* s, const dda_t* d)
 {
+    s->stat[OR_STAT_MAJORANT]++;
     return s->majorant[((size_t)d->b[2] * (size_t)s->nb[1] + (size_t)d->b[1]) * (size_t)s->nb[0] + (size_t)d->b[0]];
 }
 
@@ -1206,7 +1224,17 @@ static float transmittance_ratio(or_scene* s, ray_t R, rng_t* rng)
 
 /* Intersect / Visible - Source/transport.h:30-56 (no surface objects):
    1/0 for the reference march, the ratio-tracked transmittance otherwise */
+static float visibility_segment(or_scene* s, v3 P1, v3 P2, rng_t* rng);
 static float visibility(or_scene* s, v3 P1, v3 P2, rng_t* rng)
+{
+    const uint64_t lk = s->lookups, mj = s->stat[OR_STAT_MAJORANT];
+    s->stat[OR_STAT_SHADOW_RAYS]++;
+    const float v = visibility_segment(s, P1, P2, rng);
+    s->stat[OR_STAT_SHADOW_LOOKUPS] += s->lookups - lk;
+    s->stat[OR_STAT_SHADOW_MAJORANT] += s->stat[OR_STAT_MAJORANT] - mj;
+    return v;
+}
+static float visibility_segment(or_scene* s, v3 P1, v3 P2, rng_t* rng)
 {
     if (!s->st.shadows) return 1.0f;
     const v3 W = vnorm(vsub(P2, P1));
@@ -1535,7 +1563,10 @@ static void single_scattering(or_scene* s, int x, int y, rng_t* rng, float out[4
     metro_large_step(&ms, rng);
     const ray_t R = sample_camera(s, x, y, ms.film_uv, ms.lens_uv);
     scatter_event SE;
+    const uint64_t lk = s->lookups;
     sample_ray(s, R, rng, &SE);
+    s->stat[OR_STAT_FREE_FLIGHT_LOOKUPS] += s->lookups - lk;
+    if (SE.valid && SE.type == 0) s->stat[OR_STAT_EVENTS]++;
     if (SE.valid && SE.type == 0) Lv = cadd(Lv, uniform_sample_one_light(s, &SE, rng, &ms));
     if (SE.valid && SE.type == 1) Lv = cadd(Lv, SE.Le);
     out[0] = Lv.c[0];
@@ -1620,6 +1651,7 @@ static void run_jobs(or_scene* s, job_t* proto, int rows, int nthreads)
         jobs[t].local = *s;
         jobs[t].local.lookups = 0;
         jobs[t].local.samples = 0;
+        memset(jobs[t].local.stat, 0, sizeof(jobs[t].local.stat));
         jobs[t].row0 = (int)((long long)rows * t / nthreads);
         jobs[t].row1 = (int)((long long)rows * (t + 1) / nthreads);
     }
@@ -1627,8 +1659,14 @@ static void run_jobs(or_scene* s, job_t* proto, int rows, int nthreads)
     job_run(&jobs[0]);
     for (int t = 1; t < nthreads; t++) pthread_join(th[t], NULL);
     uint64_t lk = 0, sm = 0;
-    for (int t = 0; t < nthreads; t++) { lk += jobs[t].local.lookups; sm += jobs[t].local.samples; }
+    uint64_t st[OR_NSTATS] = {0};
+    for (int t = 0; t < nthreads; t++) {
+        lk += jobs[t].local.lookups;
+        sm += jobs[t].local.samples;
+        for (int k = 0; k < OR_NSTATS; k++) st[k] += jobs[t].local.stat[k];
+    }
     g_lookups_per_sample = sm ? (double)lk / (double)sm : 0.0;
+    for (int k = 0; k < OR_NSTATS; k++) g_stats[k] = sm ? (double)st[k] / (double)sm : 0.0;
     free(jobs);
     free(th);
 }
@@ -1663,6 +1701,11 @@ void ER_OR(render_moments)(or_scene* s, int32_t spp, uint32_t view, uint32_t fir
 }
 
 double ER_OR(lookups_per_sample)(void) { return g_lookups_per_sample; }
+
+void ER_OR(render_stats)(double* out)
+{
+    for (int k = 0; k < OR_NSTATS; k++) out[k] = g_stats[k];
+}
 
 /* ------------------------------------------------------------------ */
 /* post-processing                                                      */
@@ -1957,4 +2000,366 @@ void ER_OR(majorant_grid)(const uint16_t* vox, const int32_t* res, int32_t B, co
                 for (int i = vlo; i <= vhi; i++) m = sigma[i] > m ? sigma[i] : m;
                 out[((size_t)bz * nb[1] + by) * nb[0] + bx] = ds * m;
             }
+}
+
+/* ------------------------------------------------------------------ */
+/* differentiable medium (extension, no reference counterpart)           */
+/*                                                                      */
+/* sigma(x) = scale * alpha(rho(x)): rho is the trilinear interpolation  */
+/* of a float density grid with the addressing of the intensity volume  */
+/* (Source/buffer3d.h:222-242, without the unsigned-short truncation);  */
+/* alpha is a uniform cubic B-spline of the n opacity values over       */
+/* u = 2 + rho * (n - 5), so that alpha is C2 in rho on                  */
+/* [-1/(n-5), 1 + 1/(n-5)] and linear in the values.                     */
+/*                                                                      */
+/* Estimator (per sample): the camera ray's tentative collisions are    */
+/* drawn from the fixed majorant grid (DDA as the delta tracker); at    */
+/* each, with probability q (a random number independent of the        */
+/* medium), next-event estimation to one uniformly picked light with a  */
+/* ratio-tracked shadow segment; the contribution is weighted by the    */
+/* collision weight sigma/mu and the ratio-tracked throughput          */
+/* T = prod (1 - sigma_j/mu_j) of the earlier collisions.  Nothing the  */
+/* RNG draws depends on the medium, so for fixed seeds the estimate is  */
+/* a smooth function of the density and opacity values; the adjoint     */
+/* replays the same draws (path replay).                                */
+/* ------------------------------------------------------------------ */
+
+#define DM_INV_4PI 0.0795774715459476678f
+
+void ER_OR(dm_attach)(or_scene* s, const float* rho, const float* tf_val, int32_t tf_n, float scale, const float* albedo,
+                      float q, const float* majorant, int32_t brick)
+{
+    s->rho = rho;
+    s->tf_val = tf_val;
+    s->tf_n = tf_n;
+    s->dm_scale = scale;
+    s->dm_albedo = C3(albedo[0], albedo[1], albedo[2]);
+    s->dm_q = q;
+    s->brick = brick;
+    for (int i = 0; i < 3; i++) s->nb[i] = (s->res[i] + brick - 1) / brick;
+    const size_t nbt = (size_t)s->nb[0] * (size_t)s->nb[1] * (size_t)s->nb[2];
+    free(s->majorant);
+    s->majorant = (float*)malloc(sizeof(float) * nbt);
+    for (size_t i = 0; i < nbt; i++) s->majorant[i] = majorant[i];
+}
+
+/* corners and weights of the trilinear density lookup */
+typedef struct { size_t idx[8]; float w[8]; float rho; } dm_lookup;
+
+static inline size_t dm_index(const or_scene* s, int x, int y, int z)
+{
+    const int cx = iclamp(x, 0, s->res[0] - 1);
+    const int cy = iclamp(y, 0, s->res[1] - 1);
+    const int cz = iclamp(z, 0, s->res[2] - 1);
+    return (size_t)cz * (size_t)s->res[0] * (size_t)s->res[1] + (size_t)cy * (size_t)s->res[0] + (size_t)cx;
+}
+
+static void dm_density(or_scene* s, v3 P, dm_lookup* k)
+{
+    s->lookups++;
+    const v3 off = vsub(P, s->minp);
+    const v3 L = V3(off.x * s->inv_size.x * (float)s->res[0], off.y * s->inv_size.y * (float)s->res[1],
+                    off.z * s->inv_size.z * (float)s->res[2]);
+    const int vx = (int)floorf(L.x), vy = (int)floorf(L.y), vz = (int)floorf(L.z);
+    const float dx = L.x - (float)vx, dy = L.y - (float)vy, dz = L.z - (float)vz;
+    const float ex = 1.0f - dx, ey = 1.0f - dy, ez = 1.0f - dz;
+    float r = 0.0f;
+    for (int c = 0; c < 8; c++) {
+        const int ox = c & 1, oy = (c >> 1) & 1, oz = (c >> 2) & 1;
+        k->idx[c] = dm_index(s, vx + ox, vy + oy, vz + oz);
+        k->w[c] = (ox ? dx : ex) * (oy ? dy : ey) * (oz ? dz : ez);
+        r = r + k->w[c] * s->rho[k->idx[c]];
+    }
+    k->rho = r;
+}
+
+/* opacity spline: value, d alpha / d rho, first control index and weights */
+typedef struct { float alpha, dalpha; int i0; float b[4]; } dm_tf;
+
+static void dm_opacity(const or_scene* s, float rho, dm_tf* o)
+{
+    const int n = s->tf_n;
+    const float du = (float)(n - 5);
+    float u = 2.0f + rho * du;
+    int slope = 1;
+    if (u < 1.0f) { u = 1.0f; slope = 0; }
+    if (u > (float)(n - 2)) { u = (float)(n - 2); slope = 0; }
+    int i = (int)floorf(u);
+    if (i > n - 3) i = n - 3;
+    const float f = u - (float)i;
+    const float g = 1.0f - f;
+    const float f2 = f * f, f3 = f2 * f;
+    o->b[0] = g * g * g / 6.0f;
+    o->b[1] = (3.0f * f3 - 6.0f * f2 + 4.0f) / 6.0f;
+    o->b[2] = (-3.0f * f3 + 3.0f * f2 + 3.0f * f + 1.0f) / 6.0f;
+    o->b[3] = f3 / 6.0f;
+    const float d0 = -0.5f * g * g, d1 = 1.5f * f2 - 2.0f * f, d2 = -1.5f * f2 + f + 0.5f, d3 = 0.5f * f2;
+    o->i0 = i - 1;
+    const float* v = &s->tf_val[i - 1];
+    o->alpha = o->b[0] * v[0] + o->b[1] * v[1] + o->b[2] * v[2] + o->b[3] * v[3];
+    o->dalpha = slope ? du * (d0 * v[0] + d1 * v[1] + d2 * v[2] + d3 * v[3]) : 0.0f;
+}
+
+/* adjoint of sigma at a lookup: a = dLoss/dsigma, scattered into the
+   density and opacity gradients */
+static void dm_scatter(const or_scene* s, const dm_lookup* k, const dm_tf* o, float a, float* g_rho, float* g_tf)
+{
+    const float as = a * s->dm_scale;
+    if (g_tf)
+        for (int j = 0; j < 4; j++) g_tf[o->i0 + j] += as * o->b[j];
+    if (g_rho && o->dalpha != 0.0f) {
+        const float ar = as * o->dalpha;
+        for (int c = 0; c < 8; c++) g_rho[k->idx[c]] += ar * k->w[c];
+    }
+}
+
+/* the ray's box segment, as the delta tracker clips it */
+static int dm_segment(or_scene* s, const ray_t* R, float* t0, float* t1)
+{
+    isect_t Int; isect_invalid(&Int);
+    intersect_box(R, s->minp, vscale(s->size, 0.5f), &Int);
+    if (!Int.valid) return 0;
+    *t0 = smax(Int.near_t, R->MinT);
+    *t1 = smin(Int.far_t, R->MaxT);
+    return *t0 < *t1;
+}
+
+/* ratio-tracked transmittance of a shadow segment; with a_scale != 0 the
+   adjoint pass scatters -a_scale / (mu - sigma) at every collision */
+static float dm_shadow(or_scene* s, v3 P1, v3 P2, rng_t* rng, float a_scale, float* g_rho, float* g_tf)
+{
+    if (!s->st.shadows) return 1.0f;
+    const v3 W = vnorm(vsub(P2, P1));
+    ray_t R;
+    R.O = vadd(P1, vscale(W, RAY_EPS));
+    R.D = W;
+    R.MinT = 0.0f;
+    R.MaxT = smin(vlen(vsub(P2, P1)) - 2.0f * RAY_EPS, s->st.max_shadow_distance);
+    float t0, t1;
+    if (!dm_segment(s, &R, &t0, &t1)) return 1.0f;
+    dda_t d;
+    dda_init(s, &R, t0, t1, &d);
+    float Tr = 1.0f;
+    float tau = -er_logf(rng_get1(rng));
+    while (!d.done) {
+        const float e = dda_exit(&d);
+        const float mu = dda_majorant(s, &d);
+        float t = d.t;
+        if (mu > 0.0f) {
+            for (;;) {
+                const float dt = tau / mu;
+                if (!(t + dt < e)) {
+                    tau = tau - mu * (e - t);
+                    if (tau < 0.0f) tau = 0.0f;
+                    break;
+                }
+                t = t + dt;
+                const v3 P = vadd(R.O, vscale(R.D, t));
+                dm_lookup k;
+                dm_density(s, P, &k);
+                dm_tf o;
+                dm_opacity(s, k.rho, &o);
+                const float sig = s->dm_scale * o.alpha;
+                if (a_scale != 0.0f) dm_scatter(s, &k, &o, -a_scale / (mu - sig), g_rho, g_tf);
+                Tr = Tr * (1.0f - sig / mu);
+                tau = -er_logf(rng_get1(rng));
+            }
+        }
+        dda_advance(s, &d, e);
+    }
+    return Tr;
+}
+
+/* next-event estimate at P (without the collision weight): one uniformly
+   picked light, isotropic phase, albedo, ratio-tracked shadow; the light
+   sample is written to *S for the adjoint's shadow replay */
+static col3 dm_nee(or_scene* s, v3 P, rng_t* rng, v3* S, float* unshadowed_scale)
+{
+    *unshadowed_scale = 0.0f;
+    const float pick = rng_get1(rng);
+    const v3 uvw = rng_get3(rng);
+    if (s->light_count <= 0) return C3(0, 0, 0);
+    int idx = (int)floorf(pick * (float)s->light_count);
+    if (idx >= s->light_count) idx = s->light_count - 1;
+    const int light_id = s->light_idx[idx];
+    if (light_id < 0 || light_id >= s->n_lights) return C3(0, 0, 0);
+    const or_light* L = &s->lights[light_id];
+    scatter_event SE;
+    se_invalid(&SE, 0);
+    SE.P = P;
+    v3 Wi;
+    col3 Li;
+    surf_sample SS;
+    sample_light(s, L, uvw, &SS, &SE, &Wi, &Li);
+    *S = SS.P;
+    if (cblack(Li)) return C3(0, 0, 0);
+    const float LightPdf = vlen2(vsub(P, SS.P)) / (vabsdot(SS.N, vneg(Wi)) * L->area);
+    if (!(LightPdf > 0.0f)) return C3(0, 0, 0);
+    const col3 c = cscale(cmul(s->dm_albedo, Li), DM_INV_4PI * (float)s->light_count / (LightPdf * s->dm_q));
+    *unshadowed_scale = 1.0f;
+    return c;
+}
+
+/* one sample; with g != NULL the adjoint pass (Ltot = the sample's forward
+   value, g = dLoss/dL) */
+static col3 dm_sample(or_scene* s, int x, int y, rng_t* rng, const col3* g, col3 Ltot, float* g_rho, float* g_tf)
+{
+    col3 L = C3(0, 0, 0);
+    const v2 film_uv = rng_get2(rng);
+    const v2 lens_uv = rng_get2(rng);
+    const ray_t R = sample_camera(s, x, y, film_uv, lens_uv);
+    float t0, t1;
+    if (!dm_segment(s, &R, &t0, &t1)) return L;
+    dda_t d;
+    dda_init(s, &R, t0, t1, &d);
+    float T = 1.0f;
+    float tau = -er_logf(rng_get1(rng));
+    while (!d.done) {
+        const float e = dda_exit(&d);
+        const float mu = dda_majorant(s, &d);
+        float t = d.t;
+        if (mu > 0.0f) {
+            for (;;) {
+                const float dt = tau / mu;
+                if (!(t + dt < e)) {
+                    tau = tau - mu * (e - t);
+                    if (tau < 0.0f) tau = 0.0f;
+                    break;
+                }
+                t = t + dt;
+                const v3 P = vadd(R.O, vscale(R.D, t));
+                dm_lookup k;
+                dm_density(s, P, &k);
+                dm_tf o;
+                dm_opacity(s, k.rho, &o);
+                const float sig = s->dm_scale * o.alpha;
+                const float w = sig / mu;
+                col3 A = C3(0, 0, 0);
+                if (rng_get1(rng) < s->dm_q) {
+                    v3 S;
+                    float has;
+                    const col3 A0 = dm_nee(s, P, rng, &S, &has);
+                    if (has != 0.0f) {
+                        if (g) {
+                            /* the shadow factor first (forward draws), then the
+                               adjoint replay of the same segment */
+                            rng_t keep = *rng;
+                            const float Tr = dm_shadow(s, P, S, rng, 0.0f, NULL, NULL);
+                            A = cscale(A0, Tr);
+                            const col3 c = cscale(A, T * w);
+                            const float gc = g->c[0] * c.c[0] + g->c[1] * c.c[1] + g->c[2] * c.c[2];
+                            if (gc != 0.0f) dm_shadow(s, P, S, &keep, gc, g_rho, g_tf);
+                        } else {
+                            A = cscale(A0, dm_shadow(s, P, S, rng, 0.0f, NULL, NULL));
+                        }
+                    }
+                }
+                const col3 c = cscale(A, T * w);
+                L = cadd(L, c);
+                if (g) {
+                    /* dL/dsigma = T A / mu - (Ltot - L_<=k) / (mu - sigma) */
+                    const col3 rest = csub(Ltot, L);
+                    const col3 dLds = csub(cscale(A, T / mu), cdivs(rest, mu - sig));
+                    const float a = g->c[0] * dLds.c[0] + g->c[1] * dLds.c[1] + g->c[2] * dLds.c[2];
+                    if (a != 0.0f) dm_scatter(s, &k, &o, a, g_rho, g_tf);
+                }
+                T = T * (1.0f - w);
+                tau = -er_logf(rng_get1(rng));
+            }
+        }
+        dda_advance(s, &d, e);
+    }
+    return L;
+}
+
+typedef struct {
+    or_scene local;
+    int spp;
+    uint32_t view, first;
+    int row0, row1;
+    float* sum;            /* W*H*3 */
+    float* samples;        /* W*H*spp*3 or NULL (sample-major: (s*H*W + p)*3) */
+    const float* dimg;     /* adjoint: dLoss/dImage-sum per pixel, W*H*3 */
+    const float* fwd;      /* adjoint: the forward samples */
+    float* g_rho;          /* per-thread gradient buffers */
+    float* g_tf;
+} dm_job_t;
+
+static void* dm_job_run(void* arg)
+{
+    dm_job_t* j = (dm_job_t*)arg;
+    or_scene* s = &j->local;
+    const int W = s->film[0], H = s->film[1];
+    for (int y = j->row0; y < j->row1; y++)
+        for (int x = 0; x < W; x++) {
+            const uint32_t pix = (uint32_t)y * (uint32_t)W + (uint32_t)x;
+            float acc[3] = { 0.0f, 0.0f, 0.0f };
+            for (int k = 0; k < j->spp; k++) {
+                rng_t rng;
+                er_seed_lanes(s->st.seed, j->view, pix, j->first + (uint32_t)k, &rng.s0, &rng.s1);
+                const size_t q = ((size_t)k * (size_t)W * (size_t)H + pix) * 3;
+                if (j->dimg) {
+                    const col3 g = C3(j->dimg[3 * pix], j->dimg[3 * pix + 1], j->dimg[3 * pix + 2]);
+                    const col3 Lt = C3(j->fwd[q], j->fwd[q + 1], j->fwd[q + 2]);
+                    dm_sample(s, x, y, &rng, &g, Lt, j->g_rho, j->g_tf);
+                } else {
+                    const col3 L = dm_sample(s, x, y, &rng, NULL, C3(0, 0, 0), NULL, NULL);
+                    acc[0] += L.c[0]; acc[1] += L.c[1]; acc[2] += L.c[2];
+                    if (j->samples) { j->samples[q] = L.c[0]; j->samples[q + 1] = L.c[1]; j->samples[q + 2] = L.c[2]; }
+                }
+                s->samples++;
+            }
+            if (!j->dimg) { j->sum[3 * pix] = acc[0]; j->sum[3 * pix + 1] = acc[1]; j->sum[3 * pix + 2] = acc[2]; }
+        }
+    return NULL;
+}
+
+static void dm_run(or_scene* s, dm_job_t* proto, int nthreads, float* g_rho, float* g_tf)
+{
+    const int H = s->film[1];
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > H) nthreads = H;
+    const size_t nvox = (size_t)s->res[0] * (size_t)s->res[1] * (size_t)s->res[2];
+    dm_job_t* jobs = (dm_job_t*)calloc((size_t)nthreads, sizeof(dm_job_t));
+    pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+    for (int t = 0; t < nthreads; t++) {
+        jobs[t] = *proto;
+        jobs[t].local = *s;
+        jobs[t].row0 = (int)((long long)H * t / nthreads);
+        jobs[t].row1 = (int)((long long)H * (t + 1) / nthreads);
+        if (proto->dimg) {
+            jobs[t].g_rho = g_rho ? (float*)calloc(nvox, sizeof(float)) : NULL;
+            jobs[t].g_tf = g_tf ? (float*)calloc((size_t)s->tf_n, sizeof(float)) : NULL;
+        }
+    }
+    for (int t = 1; t < nthreads; t++) pthread_create(&th[t], NULL, dm_job_run, &jobs[t]);
+    dm_job_run(&jobs[0]);
+    for (int t = 1; t < nthreads; t++) pthread_join(th[t], NULL);
+    /* per-thread gradients summed in thread order */
+    for (int t = 0; t < nthreads; t++) {
+        if (jobs[t].g_rho) { for (size_t i = 0; i < nvox; i++) g_rho[i] += jobs[t].g_rho[i]; free(jobs[t].g_rho); }
+        if (jobs[t].g_tf) { for (int i = 0; i < s->tf_n; i++) g_tf[i] += jobs[t].g_tf[i]; free(jobs[t].g_tf); }
+    }
+    free(jobs);
+    free(th);
+}
+
+/* forward: per-pixel sums (W*H*3) and, if samples != NULL, every sample */
+void ER_OR(dm_render)(or_scene* s, int32_t spp, uint32_t view, uint32_t first, float* sum, float* samples, int32_t nthreads)
+{
+    dm_job_t proto;
+    memset(&proto, 0, sizeof(proto));
+    proto.spp = spp; proto.view = view; proto.first = first; proto.sum = sum; proto.samples = samples;
+    dm_run(s, &proto, nthreads, NULL, NULL);
+}
+
+/* adjoint: dimg = dLoss/d(pixel sum) (W*H*3), fwd = the forward samples;
+   gradients are added to g_rho (density grid) and g_tf (opacity values) */
+void ER_OR(dm_adjoint)(or_scene* s, int32_t spp, uint32_t view, uint32_t first, const float* dimg, const float* fwd,
+                       float* g_rho, float* g_tf, int32_t nthreads)
+{
+    dm_job_t proto;
+    memset(&proto, 0, sizeof(proto));
+    proto.spp = spp; proto.view = view; proto.first = first; proto.dimg = dimg; proto.fwd = fwd;
+    dm_run(s, &proto, nthreads, g_rho, g_tf);
 }

@@ -62,6 +62,30 @@ void ER_OR(render_sum)(or_scene* scene, int32_t spp, uint32_t view, uint32_t fir
 void ER_OR(render_moments)(or_scene* scene, int32_t spp, uint32_t view, uint32_t first_sample,
                            int32_t x0, int32_t y0, int32_t w, int32_t h, float* sum, float* sum2, int32_t nthreads);
 
+/* Work counters per sample of the last render_frame / render_sum /
+   render_moments, in the order of the OR_STAT_* indices: volume lookups
+   (GetIntensity calls) in the primary free flight (with the event normal),
+   majorant-grid reads (all rays), shadow-segment lookups, shadow-segment
+   majorant reads, volume scatter events, shadow segments, lookups of the
+   event normals (all normals). */
+enum { OR_STAT_FREE_FLIGHT_LOOKUPS = 0, OR_STAT_MAJORANT = 1, OR_STAT_SHADOW_LOOKUPS = 2, OR_STAT_SHADOW_MAJORANT = 3,
+       OR_STAT_EVENTS = 4, OR_STAT_SHADOW_RAYS = 5, OR_STAT_NORMAL_LOOKUPS = 6, OR_NSTATS = 7 };
+void ER_OR(render_stats)(double* out);
+
+/* Differentiable medium (extension): a float density grid (the scene
+   volume's resolution and placement), n cubic B-spline opacity values over
+   density, sigma = scale * opacity, albedo, NEE probability q and a fixed
+   majorant grid of brick^3 voxels (copied).  dm_render writes per-pixel
+   sums (W*H*3) and optionally every sample ((s*H*W + pixel)*3);
+   dm_adjoint adds dLoss/d(density) and dLoss/d(opacity values) given
+   dLoss/d(pixel sum) and the forward samples.  In the FP64 build every
+   float buffer is double. */
+void ER_OR(dm_attach)(or_scene* scene, const float* rho, const float* tf_val, int32_t tf_n, float scale, const float* albedo,
+                      float q, const float* majorant, int32_t brick);
+void ER_OR(dm_render)(or_scene* scene, int32_t spp, uint32_t view, uint32_t first, float* sum, float* samples, int32_t nthreads);
+void ER_OR(dm_adjoint)(or_scene* scene, int32_t spp, uint32_t view, uint32_t first, const float* dimg, const float* fwd,
+                       float* g_rho, float* g_tf, int32_t nthreads);
+
 /* The reference pipeline of RenderEstimate after the transport kernel
    (Source/core.cu:130-135): 3x3 Gaussian frame filter, running estimate
    update with divisor max(no_iterations,1), tone map.  frame is filtered in

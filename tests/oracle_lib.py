@@ -41,8 +41,14 @@ class Oracle:
         f("render_frame", None, [c_void_p, c_void_p, c_void_p, c_int32])
         f("render_sum", None, [c_void_p, c_int32, c_uint32, c_uint32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_int32])
         if prefix != "ref_":
+            f("render_stats", None, [c_void_p])
             f("render_moments", None, [c_void_p, c_int32, c_uint32, c_uint32, c_int32, c_int32, c_int32, c_int32, c_void_p,
                                        c_void_p, c_int32])
+        if prefix != "ref_":
+            f("dm_attach", None, [c_void_p, c_void_p, c_void_p, c_int32, self._real_c(prefix), c_void_p,
+                                  self._real_c(prefix), c_void_p, c_int32])
+            f("dm_render", None, [c_void_p, c_int32, c_uint32, c_uint32, c_void_p, c_void_p, c_int32])
+            f("dm_adjoint", None, [c_void_p, c_int32, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p, c_int32])
         # the FP64 build takes double buffers wherever the float build takes float
         self.real = np.float64 if prefix == "fp64_" else np.float32
         f("post_frame", None, [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_float])
@@ -65,11 +71,29 @@ class Oracle:
             f("math_eval", None, [c_int32, c_int32, c_void_p, c_void_p, c_void_p])
             f("majorant_grid", None, [c_void_p, c_void_p, c_int32, c_void_p, c_int32, c_float, c_void_p])
 
+    @staticmethod
+    def _real_c(prefix):
+        return c_double if prefix == "fp64_" else c_float
+
     def fn(self, name, res, args):
         h = getattr(self.lib, self.p + name)
         h.restype = res
         h.argtypes = args
         setattr(self, name, h)
+
+
+STAT_NAMES = ("free_flight_lookups", "majorant_reads", "shadow_lookups", "shadow_majorant_reads", "events", "shadow_rays",
+              "normal_lookups")
+
+
+def render_stats(orc: Oracle) -> dict:
+    """Work counters per sample of the oracle's last render, plus the total
+    lookups per sample."""
+    out = np.zeros(len(STAT_NAMES), dtype=np.float64)
+    orc.render_stats(out.ctypes.data_as(c_void_p))
+    d = dict(zip(STAT_NAMES, out.tolist()))
+    d["lookups"] = float(orc.lookups_per_sample())
+    return d
 
 
 def ptr(a: np.ndarray):
@@ -117,6 +141,37 @@ class SceneHandle:
         out2 = np.zeros((h, w, 4), dtype=self.orc.real)
         self.orc.render_moments(self.h, spp, view, first, x0, y0, w, h, ptr(out), ptr(out2), nthreads)
         return out, out2
+
+
+class MediumHandle(SceneHandle):
+    """An oracle scene with a differentiable medium attached: `rho` (Z, Y, X)
+    float density, `tf` opacity B-spline values, fixed `majorant` grid."""
+
+    def __init__(self, orc: Oracle, scene, rho, tf, scale, albedo, q, majorant, brick):
+        super().__init__(orc, scene)
+        r = orc.real
+        self.rho = np.ascontiguousarray(rho, dtype=r)
+        self.tf = np.ascontiguousarray(tf, dtype=r)
+        self.albedo = np.ascontiguousarray(albedo, dtype=r)
+        self.maj = np.ascontiguousarray(majorant, dtype=r)
+        orc.dm_attach(self.h, ptr(self.rho), ptr(self.tf), len(self.tf), scale, ptr(self.albedo), q, ptr(self.maj), brick)
+
+    def render(self, spp, view=0, first=0, keep_samples=False, nthreads=8):
+        W, H = self.scene.width, self.scene.height
+        r = self.orc.real
+        out = np.zeros((H, W, 3), dtype=r)
+        smp = np.zeros((spp, H, W, 3), dtype=r) if keep_samples else None
+        self.orc.dm_render(self.h, spp, view, first, ptr(out), ptr(smp) if keep_samples else None, nthreads)
+        return (out, smp) if keep_samples else out
+
+    def adjoint(self, spp, dimg, samples, view=0, first=0, nthreads=8):
+        r = self.orc.real
+        g_rho = np.zeros(self.rho.shape, dtype=r)
+        g_tf = np.zeros(self.tf.shape, dtype=r)
+        d = np.ascontiguousarray(dimg, dtype=r)
+        f = np.ascontiguousarray(samples, dtype=r)
+        self.orc.dm_adjoint(self.h, spp, view, first, ptr(d), ptr(f), ptr(g_rho), ptr(g_tf), nthreads)
+        return g_rho, g_tf
 
 
 def initial_lanes(seed: int, width: int, height: int) -> np.ndarray:

@@ -272,3 +272,31 @@ def test_batch_argument_errors(torch, lib, pair):
     assert lib.er_batch_set_tuning(bid.value, 5, 0) == C.ER_ERR_INVALID_ARGUMENT
     C.check(lib.er_batch_destroy(bid.value))
     assert lib.er_batch_destroy(bid.value) == C.ER_ERR_INVALID_ID
+
+
+def test_stage_profiler(torch, lib, pair):
+    """er_profile_*: per-stage launch counts of a one-view render (one window)
+    and of a batch launched without its graph; graph replays record nothing"""
+    ra, rb = pair
+    ms = np.zeros(4, dtype=np.float64)
+    n = np.zeros(4, dtype=np.int64)
+    C.check(lib.er_profile_read(ms.ctypes.data, n.ctypes.data))          # clear
+    C.check(lib.er_profile_enable(1))
+    d = torch.zeros((ra.height, ra.width, 4), dtype=torch.float32, device="cuda")
+    C.check(lib.er_trace_sum_device(ra.tracer_id, 3, 0, 0, d.data_ptr(), 0, None))
+    C.check(lib.er_profile_read(ms.ctypes.data, n.ctypes.data))
+    assert list(n) == [1, 1, 1, 1] and (ms > 0).all()
+    table = view_table(ra, rb)
+    for flags in (0, C.ER_BATCH_GRAPH):
+        bid, outs = make_batch(torch, lib, table, flags, 3000)
+        nw = ctypes.c_int32(0)
+        C.check(lib.er_batch_info(bid, ctypes.byref(nw), None, None))
+        C.check(lib.er_profile_read(ms.ctypes.data, n.ctypes.data))      # the plan's capture records nothing either
+        C.check(lib.er_batch_launch(bid, None))
+        C.check(lib.er_profile_read(ms.ctypes.data, n.ctypes.data))
+        assert list(n) == ([nw.value] * 4 if flags == 0 else [0, 0, 0, 0])
+        C.check(lib.er_batch_destroy(bid))
+    C.check(lib.er_profile_enable(0))
+    C.check(lib.er_trace_sum_device(ra.tracer_id, 1, 0, 0, d.data_ptr(), 0, None))
+    C.check(lib.er_profile_read(ms.ctypes.data, n.ctypes.data))
+    assert list(n) == [0, 0, 0, 0]

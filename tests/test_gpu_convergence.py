@@ -1,0 +1,59 @@
+"""The GPU estimators converge to the FP64 oracle's converged images
+(tests/golden/fp64_*.npz): image RMSE falls like spp^-1/2 for the unbiased
+delta-tracking path and reaches 1e-2."""
+import importlib
+
+import numpy as np
+import pytest
+
+import convergence as CV
+import oracle_lib as OL
+
+pytestmark = pytest.mark.gpu
+
+C = OL.C
+S = OL.PKG.scenes
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as T
+    assert T.cuda.is_available(), "GPU tests need CUDA"
+    return T
+
+
+@pytest.fixture(scope="module")
+def lib(torch):
+    L = C.load_library()
+    C.check(L.er_set_device(0))
+    yield L
+    L.er_reset()
+
+
+@pytest.fixture(scope="module")
+def runtime():
+    return importlib.import_module("exposure-render_gb300.runtime")
+
+
+def render_mean(torch, r, spp, first=0):
+    d = torch.zeros((r.height, r.width, 4), dtype=torch.float32, device="cuda")
+    r.trace_sum_device(d.data_ptr(), spp, 0, first, 0, None)
+    torch.cuda.synchronize()
+    return d.double().cpu().numpy() / spp
+
+
+@pytest.mark.parametrize("name", ["c1", "c3v2"])
+@pytest.mark.parametrize("mis", [0, 1])
+def test_delta_tracking_converges_to_fp64(torch, lib, runtime, name, mis):
+    sc = dict(S.rmse_views(names=[name]))[name]
+    sc.tracer.settings.free_flight = C.FREE_FLIGHT_DELTA
+    sc.tracer.settings.mis = mis
+    ref = CV.load_reference(name)
+    r = runtime.Renderer(sc, lib)
+    try:
+        e64 = CV.rmse(render_mean(torch, r, 64), ref)
+        e1k = CV.rmse(render_mean(torch, r, 1024, first=64), ref)
+        assert e1k < 0.35 * e64          # 1/sqrt(16) = 0.25 for an unbiased estimator
+        assert e1k < 1e-2
+    finally:
+        r.close()
