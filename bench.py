@@ -307,11 +307,24 @@ def batched_rmse_summary(conv, value, plain_value, target=1e-2):
     return out
 
 
+def reference_path(scene):
+    """the scene with the reference's live estimator: fixed-step march, BRDF
+    at every volume event, light sampling only (bit-exact with the reference)"""
+    C = importlib.import_module("exposure-render_gb300.capi")
+    t = C.er_tracer_desc.from_buffer_copy(scene.tracer)
+    t.settings.free_flight = 0
+    t.settings.mis = 0
+    t.settings.apply_shading_type = 0
+    import copy
+    out = copy.copy(scene)
+    out.tracer = t
+    return out
+
+
 def run_reference(args, wl, rank, world):
     if rank != 0:
         return
-    scene = make_scene(wl)
-    scene.tracer.settings.free_flight = 0
+    scene = reference_path(make_scene(wl))
     shading = describe_shading(scene)
     W = WORKLOADS[wl]
     for _ in range(args.warmup):
@@ -338,7 +351,8 @@ def run_ours(args, wl, rank, world, local_rank):
     C.check(lib.er_set_device(local_rank))
     W = WORKLOADS[wl]
     scene = make_scene(wl)
-    scene.tracer.settings.free_flight = 1                # the fast path: delta tracking
+    scene.tracer.settings.free_flight = 1                # the fast path: delta tracking, full MIS
+    scene.tracer.settings.mis = 1
     shading = describe_shading(scene)
     scene.tracer.settings.seed = 1 + rank                # one replica view per rank
     r = runtime.Renderer(scene, lib)
@@ -400,7 +414,7 @@ def run_ours(args, wl, rank, world, local_rank):
         r.rebind_tracer()
         return samples_per_step / (a.elapsed_time(b) / 1e3) / 1e6
 
-    plain = timed_plain({"free_flight": 0, "mis": 0})
+    plain = timed_plain({"free_flight": 0})
     ref_order = timed_plain({"free_flight": 0, "mis": 0, "apply_shading_type": 0, "bilateral": 0})
 
     # end to end through the C ABI with host buffers
@@ -440,7 +454,7 @@ def run_ours(args, wl, rank, world, local_rank):
     if world == 1 and not args.no_rmse:
         conv = convergence(lib, runtime, torch, ["c2"], {
             "fast": {"free_flight": 1, "majorant_brick": r.tracer_desc.settings.majorant_brick},
-            "plain": {"free_flight": 0, "mis": 0}})
+            "plain": {"free_flight": 0}})
     peaks, peak_kind = measured_peaks()
     nthreads = os.cpu_count() or 1
     # work per sample of the measured configuration (oracle, whole field of view at 128^2)
@@ -448,7 +462,7 @@ def run_ours(args, wl, rank, world, local_rank):
     roofline, stages = stage_roofline(work, stage_ms, stage_launches, samples_per_step * args.steps, peaks, peak_kind, wl)
     cpu_rate, kind, cores, sample = (None, None, None, None)
     if world == 1:
-        cpu_rate, kind, cores, sample = cpu_reference_rate(scene, seconds_target=12.0, steps=1)
+        cpu_rate, kind, cores, sample = cpu_reference_rate(reference_path(scene), seconds_target=12.0, steps=1)
     line = {
         "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -469,7 +483,7 @@ def run_ours(args, wl, rank, world, local_rank):
         "stages": stages,
         "work_per_sample": work,
         "plain": {"value": plain, "unit": "Msamples/s", "speedup": value / plain,
-                  "what": "same workload and shading model, the reference's estimator: fixed-step march, light sampling only"},
+                  "what": "same workload and estimator, the reference's fixed-step march for free flight and shadows"},
         "time_to_rmse": rmse_summary(conv, "c2", value, plain, width * height),
         "reference_order": {"value": ref_order, "unit": "Msamples/s",
                             "what": "reference live path (march, BRDF, light sampling), bit-exact with the reference"},
@@ -574,7 +588,7 @@ def run_batched(args, rank, world, local_rank):
     conv = None
     if world == 1 and not args.no_rmse:
         conv = convergence(lib, runtime, torch, ["c3v0", "c3v1", "c3v2"],
-                           {"fast": {"free_flight": 1}, "plain": {"free_flight": 0, "mis": 0}})
+                           {"fast": {"free_flight": 1}, "plain": {"free_flight": 0}})
 
     # end to end with host buffers: volumes bound from host memory, one batch
     # launch, every view's sums read back into pinned host memory
@@ -629,13 +643,95 @@ def run_batched(args, rank, world, local_rank):
         r.close()
 
 
+def run_medium(args, rank, world, local_rank):
+    """c4: differentiable medium, 128^3 float density + 64 opacity values,
+    256^2 x 32 spp; forward (every sample kept) and path-replay adjoint of an
+    L2 image loss against a target rendered at 1024 spp from parameters
+    perturbed by N(0, 0.05)"""
+    import torch
+    torch.cuda.set_device(local_rank)
+    runtime = importlib.import_module("exposure-render_gb300.runtime")
+    medium = importlib.import_module("exposure-render_gb300.medium")
+    S = importlib.import_module("exposure-render_gb300.scenes")
+    C = importlib.import_module("exposure-render_gb300.capi")
+    lib = C.load_library()
+    C.check(lib.er_set_device(local_rank))
+    stream = torch.cuda.current_stream()
+    C.check(lib.er_set_stream(ctypes.c_void_p(stream.cuda_stream)))
+    res, film, spp = (128, 128, 128), (256, 256), 32
+    sc = S.medium_scene(res=res, film=film)
+    sc.tracer.settings.seed = 1 + rank
+    r = runtime.Renderer(sc, lib)
+    rho = torch.from_numpy(S.blob_density(res, n_blobs=10, seed=40)).cuda()
+    tf = torch.from_numpy(S.ramp_opacity(64)).cuda()
+    m = medium.Medium(r, rho, tf, 40.0, albedo=(0.8, 0.7, 0.6), nee_probability=0.5, brick=8)
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    rho_t = (rho + 0.05 * torch.randn(rho.shape, device="cuda", generator=gen)).contiguous()
+    tf_t = (tf + 0.05 * torch.randn(tf.shape, device="cuda", generator=gen)).contiguous()
+    maj0 = m.majorant.clone()
+    m.rebuild_majorant(rho_t, tf_t)
+    m.majorant = torch.maximum(maj0, m.majorant).contiguous()
+    _, ts = m.render_samples(rho_t, tf_t, 1024, view=1)
+    target = ts / 1024
+
+    def timed(fn, steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / steps
+
+    state = {}
+
+    def fwd():
+        state["smp"], state["s"] = m.render_samples(rho, tf, spp)
+
+    def bwd():
+        d = 2.0 * (state["s"] / spp - target) / spp / target.numel()
+        state["g"] = m.adjoint(rho, tf, spp, d, state["smp"])
+
+    def bwd_recompute():
+        d = 2.0 * (state["s"] / spp - target) / spp / target.numel()
+        m.adjoint(rho, tf, spp, d, None)
+
+    for _ in range(args.warmup):
+        fwd()
+        bwd()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        f_ms = timed(fwd, args.steps)
+        b_ms = timed(bwd, args.steps)
+    br_ms = timed(bwd_recompute, 1)
+    C.check(lib.er_synchronize())
+    samples = film[0] * film[1] * spp
+    loss = float(((state["s"] / spp - target) ** 2).mean())
+    if rank != 0:
+        return
+    line = {
+        "metric": "Msamples/s", "value": world * samples / (f_ms / 1e3) / 1e6, "unit": "Msamples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": f_ms + b_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "c4-differentiable-128^3-density-64-opacity-256^2-32spp", "scale": 40.0, "nee_probability": 0.5,
+                   "majorant_brick": 8, "loss": "mean squared error vs 1024-spp target of perturbed parameters",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "forward_ms": f_ms, "adjoint_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
+        "adjoint_recompute_ms": br_ms, "adjoint_recompute_over_forward": br_ms / f_ms,
+        "loss": loss, "grad_norm": {"density": float(state["g"][0].norm()), "opacity": float(state["g"][1].norm())},
+        "clocks": clk.summary(), "gpu_launches": args.steps * 3,
+    }
+    print(json.dumps(line), flush=True)
+    r.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3", "c4"])
     ap.add_argument("--views", type=int, default=64, help="c3: number of views")
     ap.add_argument("--plain-views", type=int, default=16, help="c3: views timed on the plain one-view path")
     ap.add_argument("--film", type=int, default=0, help="square film edge (smaller profiling cases; 0 = the workload's)")
@@ -659,6 +755,9 @@ def main():
         return
     if args.workload == "c3":
         run_batched(args, rank, world, local_rank)
+        return
+    if args.workload == "c4":
+        run_medium(args, rank, world, local_rank)
         return
     if world > 1:
         import torch

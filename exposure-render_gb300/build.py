@@ -32,6 +32,7 @@ UNITS = {
     "er_post.cu": ["--fmad=false"],
     "er_volume.cu": ["--fmad=false"],
     "er_wavefront.cu": ["--fmad=false", "-Xptxas", "-v"],
+    "er_medium.cu": ["--fmad=false", "-Xptxas", "-v"],
     "er_runtime.cu": [],
     "er_cxx_api.cpp": [],
 }

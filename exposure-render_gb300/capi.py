@@ -172,7 +172,8 @@ class er_render_settings(Structure):
         ("engine", c_int32),
         ("tune_primary", c_int32),
         ("tune_shadow", c_int32),
-        ("reserved", c_int32 * 2),
+        ("tune_shade", c_int32),
+        ("reserved", c_int32 * 1),
     ]
 
 
@@ -195,6 +196,19 @@ class er_tracer_desc(Structure):
     ]
 
 
+class er_medium_desc(Structure):
+    _fields_ = [
+        ("d_density", c_void_p),
+        ("d_opacity", c_void_p),
+        ("n_opacity", c_int32),
+        ("scale", c_float),
+        ("albedo", c_float * 3),
+        ("nee_probability", c_float),
+        ("d_majorant", c_void_p),
+        ("brick", c_int32),
+    ]
+
+
 class er_tune_result(Structure):
     _fields_ = [
         ("majorant_brick", c_int32),
@@ -203,6 +217,7 @@ class er_tune_result(Structure):
         ("from_cache", c_int32),
         ("msamples_per_s", c_float),
         ("candidates", c_int32),
+        ("tune_shade", c_int32),
     ]
 
 
@@ -411,6 +426,12 @@ def _declare(lib) -> None:
         "er_autotune_tracer": (c_int32, [c_int32, c_int32, POINTER(er_tune_result)]),
         "er_get_render_settings": (c_int32, [c_int32, POINTER(er_render_settings)]),
         "er_profile_enable": (c_int32, [c_int32]),
+        "er_medium_majorant": (c_int32, [c_int32, POINTER(er_medium_desc), c_float, c_float, c_void_p, c_void_p]),
+        "er_medium_render": (c_int32, [c_int32, POINTER(er_medium_desc), c_int32, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]),
+        "er_medium_render_f64": (c_int32, [c_int32, POINTER(er_medium_desc), c_int32, c_uint32, c_uint32, c_void_p, c_void_p,
+                                           c_void_p]),
+        "er_medium_adjoint": (c_int32, [c_int32, POINTER(er_medium_desc), c_int32, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p,
+                                        c_void_p, c_void_p]),
         "er_profile_read": (c_int32, [c_void_p, c_void_p]),
         "er_trace_frame_device": (c_int32, [c_int32, c_void_p, c_void_p, c_void_p]),
         "er_post_frame_device": (c_int32, [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_float, c_int32, c_void_p]),

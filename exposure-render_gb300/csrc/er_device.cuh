@@ -154,6 +154,7 @@ ER_D int iclamp(int v, int lo, int hi) { const int m = v < hi ? v : hi; return l
 
 ER_D c3 C3(float r, float g, float b) { c3 c; c.r = r; c.g = g; c.b = b; return c; }
 ER_D c3 cadd(c3 a, c3 b) { return C3(a.r + b.r, a.g + b.g, a.b + b.b); }
+ER_D c3 csub(c3 a, c3 b) { return C3(a.r - b.r, a.g - b.g, a.b - b.b); }
 ER_D c3 cmul(c3 a, c3 b) { return C3(a.r * b.r, a.g * b.g, a.b * b.b); }
 ER_D c3 cscale(c3 a, float s) { return C3(a.r * s, a.g * s, a.b * s); }
 ER_D c3 cdivs(c3 a, float s) { return C3(a.r / s, a.g / s, a.b / s); }

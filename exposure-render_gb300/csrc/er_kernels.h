@@ -37,6 +37,24 @@ cudaError_t er_launch_math_eval(int fn, int n, const float* x, const float* y, f
 cudaError_t er_launch_majorant(const uint16_t* vox, const int res[3], int B, const int nb[3], const float* sigma, int n,
                                float* rmq, int levels, uint32_t* minmax, float density_scale, float* majorant, cudaStream_t s);
 
+/* the differentiable medium (er_medium.cu) */
+struct DmParams {
+    const float* rho;    /* density grid, the tracer volume's resolution, x fastest */
+    const float* tf;     /* tf_n opacity B-spline values */
+    int tf_n;
+    float scale;         /* sigma = scale * opacity */
+    float albedo[3];
+    float q;             /* next-event probability per collision */
+};
+cudaError_t er_launch_dm_forward(const erd::Params& P, const DmParams& M, int spp, uint32_t view, uint32_t first, float* samples,
+                                 float* sum, cudaStream_t s);
+cudaError_t er_launch_dm_forward64(const erd::Params& P, const DmParams& M, int spp, uint32_t view, uint32_t first, double* samples,
+                                   double* sum, cudaStream_t s);
+cudaError_t er_launch_dm_adjoint(const erd::Params& P, const DmParams& M, int spp, uint32_t view, uint32_t first, const float* dimg,
+                                 const float* fwd, float* g_rho, float* g_tf, cudaStream_t s);
+cudaError_t er_launch_dm_majorant(const float* rho, const int res[3], int B, const float* tf, int n, float scale, float margin,
+                                  float floor_, float* out, cudaStream_t s);
+
 /* sets the text returned by er_last_error_message() on this thread */
 void er_internal_set_error(const char* message);
 
@@ -85,6 +103,7 @@ struct WavefrontBuffers {
     uint32_t* counters;  /* 2 */
     int tune_primary;    /* resident blocks per SM targeted by the primary stage (2, 3, 4, 6, 8) */
     int tune_shadow;     /* same for the shadow stage */
+    int tune_shade;      /* resident 128-thread blocks per SM of the shade stage (2, 3, 4, 6) */
 };
 
 /* cuts the items of views (npix[v] * spp[v] each) into windows of whole

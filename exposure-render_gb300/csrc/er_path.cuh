@@ -124,6 +124,38 @@ ER_D v3 normalized_gradient(const Params& P, v3 p)
     return vnorm(g);
 }
 
+/* GradientCD and GradientMagnitude read the same six intensities
+   (p -/+ the gradient delta of each axis): read once, both follow */
+struct Grad6 {
+    float m[3], p[3];    /* I(p - d_i), I(p + d_i) */
+};
+
+ER_D void gradient_samples(const Params& P, v3 p, Grad6& g)
+{
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const v3 d = gdelta(P, i);
+        g.m[i] = get_intensity(P, vsub(p, d));
+        g.p[i] = get_intensity(P, vadd(p, d));
+    }
+}
+
+/* gradient_cd from the six samples */
+ER_D v3 gradient_cd6(const Grad6& g) { return V3(g.m[0] - g.p[0], g.m[1] - g.p[1], g.m[2] - g.p[2]); }
+
+/* gradient_magnitude from the six samples */
+ER_D float gradient_magnitude6(const Params& P, const Grad6& g)
+{
+    float sum = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float D = g.m[i] - g.p[i];
+        D *= 0.5f / P.spacing[i];
+        sum += D * D;
+    }
+    return sqrtf(sum);
+}
+
 ER_D float gradient_magnitude(const Params& P, v3 p)
 {
     float sum = 0.0f;
@@ -843,25 +875,26 @@ ER_D float visibility(const Params& P, v3 P1, v3 P2, Rng& rng)
 }
 
 /* shader selection of the design Source/scatterevent.h:155-212 (0 BRDF, 1 phase) */
-ER_D int select_shader_type(const Params& P, const Event& SE, float I, Rng& rng)
+/* gm: the gradient magnitude at SE.P when the caller has it, else < 0 */
+ER_D int select_shader_type(const Params& P, const Event& SE, float I, Rng& rng, float gm = -1.0f)
 {
     switch (P.shading_type) {
     case 0: return 0;
     case 1: return 1;
     case 2: {
-        const float NGM = gradient_magnitude(P, SE.P) * P.gm_inv_max;
+        const float NGM = (gm >= 0.0f ? gm : gradient_magnitude(P, SE.P)) * P.gm_inv_max;
         const float Exponent = 25.0f * er_powf(P.gradient_factor, 3.0f) * NGM;
         const float PdfBrdf = P.opacity_modulated ? plf_eval(P.tfs->opacity, I) * (1.0f - er_expf(-Exponent))
                                                   : 1.0f - er_expf(-Exponent);
         return rng.get1() <= PdfBrdf ? 0 : 1;
     }
     case 3: {
-        const float NGM = gradient_magnitude(P, SE.P) * P.gm_inv_max;
+        const float NGM = (gm >= 0.0f ? gm : gradient_magnitude(P, SE.P)) * P.gm_inv_max;
         const float PdfBrdf = 1.0f - er_powf(1.0f - NGM, 2.0f);
         return rng.get1() < PdfBrdf ? 0 : 1;
     }
     case 4: {
-        const float NGM = gradient_magnitude(P, SE.P) * P.gm_inv_max;
+        const float NGM = (gm >= 0.0f ? gm : gradient_magnitude(P, SE.P)) * P.gm_inv_max;
         return NGM > P.gradient_threshold ? 0 : 1;
     }
     default: return 1;

@@ -123,6 +123,7 @@ struct WfQueues {
         B.counters = counters.p;
         B.tune_primary = 4;
         B.tune_shadow = 4;
+        B.tune_shade = 2;
         return cudaSuccess;
     }
 };
@@ -199,7 +200,7 @@ struct BatchItem {
     std::vector<er_camera_desc> cameras;
     int flags = 0;
     size_t window_cap = kWindowCap;
-    int tune_primary = 4, tune_shadow = 4;
+    int tune_primary = 4, tune_shadow = 4, tune_shade = 2;
     bool tune_explicit = false;    /* set by er_batch_set_tuning; else the first view's tracer settings */
     uint64_t planned_version = 0;  /* context version the plan was made at */
     bool planned = false;
@@ -588,6 +589,7 @@ er_status trace_sum(TracerItem& t, int spp, uint32_t view, uint32_t first, float
     ER_CUDA(t.wf.ensure(plan, B));
     B.tune_primary = t.d.settings.tune_primary > 0 ? t.d.settings.tune_primary : 4;
     B.tune_shadow = t.d.settings.tune_shadow > 0 ? t.d.settings.tune_shadow : 4;
+    B.tune_shade = t.d.settings.tune_shade > 0 ? t.d.settings.tune_shade : 2;
     WfView V;
     memset(&V, 0, sizeof(V));
     V.P = t.P;
@@ -675,9 +677,11 @@ er_status batch_plan(BatchItem& b)
         const er_render_settings& s0 = find_tracer(b.views[0].tracer_id)->d.settings;
         b.tune_primary = s0.tune_primary > 0 ? s0.tune_primary : 4;
         b.tune_shadow = s0.tune_shadow > 0 ? s0.tune_shadow : 4;
+        b.tune_shade = s0.tune_shade > 0 ? s0.tune_shade : 2;
     }
     b.B.tune_primary = b.tune_primary;
     b.B.tune_shadow = b.tune_shadow;
+    b.B.tune_shade = b.tune_shade;
     if (b.flags & ER_BATCH_GRAPH) {
         if (!b.capture_stream) ER_CUDA(cudaStreamCreateWithFlags(&b.capture_stream, cudaStreamNonBlocking));
         ER_CUDA(cudaStreamBeginCapture(b.capture_stream, cudaStreamCaptureModeThreadLocal));
@@ -746,7 +750,7 @@ uint64_t tune_key(const TracerItem& t, const VolumeItem& v, int probe_spp)
     h = fnv1a(h, v.spacing, sizeof(v.spacing));
     er_render_settings s = t.d.settings;
     s.majorant_brick = 0;
-    s.tune_primary = s.tune_shadow = 0;
+    s.tune_primary = s.tune_shadow = s.tune_shade = 0;
     s.seed = 0;
     s.bilateral = 0;
     s.bilateral_radius = 0;
@@ -771,12 +775,13 @@ bool tune_cache_lookup(uint64_t key, er_tune_result& r)
     char line[256];
     while (fgets(line, sizeof(line), f)) {
         unsigned long long k = 0;
-        int b = 0, p = 0, sh = 0;
+        int b = 0, p = 0, sh = 0, sd = 0;
         float m = 0.0f;
-        if (sscanf(line, "%llx %d %d %d %f", &k, &b, &p, &sh, &m) == 5 && (uint64_t)k == key) {
+        if (sscanf(line, "%llx %d %d %d %d %f", &k, &b, &p, &sh, &sd, &m) == 6 && (uint64_t)k == key) {
             r.majorant_brick = b;
             r.tune_primary = p;
             r.tune_shadow = sh;
+            r.tune_shade = sd;
             r.msamples_per_s = m;
             found = true;          /* the last entry for a key wins */
         }
@@ -794,7 +799,8 @@ void tune_cache_store(uint64_t key, const er_tune_result& r)
         if (path[i] == '/') mkdir(path.substr(0, i).c_str(), 0755);
     FILE* f = fopen(path.c_str(), "a");
     if (!f) return;
-    fprintf(f, "%016llx %d %d %d %.3f\n", (unsigned long long)key, r.majorant_brick, r.tune_primary, r.tune_shadow, r.msamples_per_s);
+    fprintf(f, "%016llx %d %d %d %d %.3f\n", (unsigned long long)key, r.majorant_brick, r.tune_primary, r.tune_shadow, r.tune_shade,
+            r.msamples_per_s);
     fclose(f);
 }
 
@@ -1353,6 +1359,8 @@ ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tun
         const bool wavefront = s.engine != 1;
         s.tune_primary = s.tune_primary > 0 ? s.tune_primary : 4;
         s.tune_shadow = s.tune_shadow > 0 ? s.tune_shadow : 4;
+        s.tune_shade = s.tune_shade > 0 ? s.tune_shade : 2;
+        r.tune_shade = s.tune_shade;
         r.majorant_brick = s.majorant_brick > 0 ? s.majorant_brick : 8;
         r.tune_primary = s.tune_primary;
         r.tune_shadow = s.tune_shadow;
@@ -1381,17 +1389,119 @@ ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tun
                 r.candidates++;
                 if (m > r.msamples_per_s) { r.msamples_per_s = m; r.tune_primary = vv[0]; r.tune_shadow = vv[1]; }
             }
+            s.tune_primary = r.tune_primary;
+            s.tune_shadow = r.tune_shadow;
+            const int shades[] = {2, 3, 4, 6};
+            for (int sd : shades) {
+                s.tune_shade = sd;
+                float m = 0.0f;
+                st = time_probe(*t, probe_spp, &m);
+                if (st != ER_OK) { s = saved; t->built = false; return st; }
+                r.candidates++;
+                if (m > r.msamples_per_s) { r.msamples_per_s = m; r.tune_shade = sd; }
+            }
         }
         tune_cache_store(key, r);
     }
     s.majorant_brick = r.majorant_brick;
     s.tune_primary = r.tune_primary;
     s.tune_shadow = r.tune_shadow;
+    s.tune_shade = r.tune_shade;
     t->built = false;
     C.version++;            /* batches over this tracer re-plan */
     st = build(*t);
     if (st != ER_OK) return st;
     if (result) *result = r;
+    return ER_OK;
+}
+
+/* the tracer's parameters with the medium's majorant grid, and the medium */
+static er_status medium_params(int32_t tracer_id, const er_medium_desc* m, erd::Params& P, DmParams& M, TracerItem** tp)
+{
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    if (!m || !m->d_density || !m->d_opacity) return fail(ER_ERR_INVALID_ARGUMENT, "medium descriptor or its buffers are NULL");
+    if (m->n_opacity < 6 || m->n_opacity > ER_MAX_TF_NODES)
+        return fail(ER_ERR_INVALID_ARGUMENT, "n_opacity %d out of range [6, %d]", m->n_opacity, ER_MAX_TF_NODES);
+    if (m->brick < 1 || m->brick > 64) return fail(ER_ERR_INVALID_ARGUMENT, "brick %d out of range [1, 64]", m->brick);
+    if (!(m->nee_probability > 0.0f && m->nee_probability <= 1.0f))
+        return fail(ER_ERR_INVALID_ARGUMENT, "nee_probability must lie in (0, 1]");
+    if (!(m->scale > 0.0f) || !std::isfinite(m->scale)) return fail(ER_ERR_INVALID_ARGUMENT, "scale must be finite and positive");
+    er_status st = build(*t);
+    if (st != ER_OK) return st;
+    P = t->P;
+    P.brick = m->brick;
+    for (int i = 0; i < 3; i++) P.nb[i] = (P.res[i] + m->brick - 1) / m->brick;
+    P.majorant = m->d_majorant;
+    M.rho = m->d_density;
+    M.tf = m->d_opacity;
+    M.tf_n = m->n_opacity;
+    M.scale = m->scale;
+    for (int i = 0; i < 3; i++) M.albedo[i] = m->albedo[i];
+    M.q = m->nee_probability;
+    *tp = t;
+    return ER_OK;
+}
+
+ER_API er_status er_medium_majorant(int32_t tracer_id, const er_medium_desc* medium, float margin, float floor_, float* d_majorant,
+                                    void* stream)
+{
+    ER_LOCK;
+    erd::Params P;
+    DmParams M;
+    TracerItem* t = nullptr;
+    er_medium_desc m = medium ? *medium : er_medium_desc();
+    m.d_majorant = d_majorant;
+    er_status st = medium_params(tracer_id, medium ? &m : nullptr, P, M, &t);
+    if (st != ER_OK) return st;
+    if (!d_majorant) return fail(ER_ERR_INVALID_ARGUMENT, "d_majorant is NULL");
+    if (!(margin >= 1.0f) || !(floor_ >= 0.0f)) return fail(ER_ERR_INVALID_ARGUMENT, "margin must be >= 1 and floor >= 0");
+    ER_CUDA(er_launch_dm_majorant(M.rho, P.res, P.brick, M.tf, M.tf_n, M.scale, margin, floor_, d_majorant, (cudaStream_t)stream));
+    return ER_OK;
+}
+
+ER_API er_status er_medium_render(int32_t tracer_id, const er_medium_desc* medium, int32_t spp, uint32_t view,
+                                  uint32_t first_sample, float* d_samples, float* d_sum_rgb, void* stream)
+{
+    ER_LOCK;
+    erd::Params P;
+    DmParams M;
+    TracerItem* t = nullptr;
+    er_status st = medium_params(tracer_id, medium, P, M, &t);
+    if (st != ER_OK) return st;
+    if (!medium->d_majorant || !d_samples || spp <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "invalid majorant, samples buffer or spp");
+    ER_CUDA(er_launch_dm_forward(P, M, spp, view, first_sample, d_samples, d_sum_rgb, (cudaStream_t)stream));
+    return ER_OK;
+}
+
+ER_API er_status er_medium_render_f64(int32_t tracer_id, const er_medium_desc* medium, int32_t spp, uint32_t view,
+                                      uint32_t first_sample, double* d_samples64, double* d_sum64, void* stream)
+{
+    ER_LOCK;
+    erd::Params P;
+    DmParams M;
+    TracerItem* t = nullptr;
+    er_status st = medium_params(tracer_id, medium, P, M, &t);
+    if (st != ER_OK) return st;
+    if (!medium->d_majorant || !d_samples64 || !d_sum64 || spp <= 0)
+        return fail(ER_ERR_INVALID_ARGUMENT, "invalid majorant, output buffers or spp");
+    ER_CUDA(er_launch_dm_forward64(P, M, spp, view, first_sample, d_samples64, d_sum64, (cudaStream_t)stream));
+    return ER_OK;
+}
+
+ER_API er_status er_medium_adjoint(int32_t tracer_id, const er_medium_desc* medium, int32_t spp, uint32_t view,
+                                   uint32_t first_sample, const float* d_dloss_dsum, const float* d_samples,
+                                   float* d_grad_density, float* d_grad_opacity, void* stream)
+{
+    ER_LOCK;
+    erd::Params P;
+    DmParams M;
+    TracerItem* t = nullptr;
+    er_status st = medium_params(tracer_id, medium, P, M, &t);
+    if (st != ER_OK) return st;
+    if (!medium->d_majorant || !d_dloss_dsum || spp <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "invalid majorant, dLoss buffer or spp");
+    ER_CUDA(er_launch_dm_adjoint(P, M, spp, view, first_sample, d_dloss_dsum, d_samples, d_grad_density, d_grad_opacity,
+                                 (cudaStream_t)stream));
     return ER_OK;
 }
 

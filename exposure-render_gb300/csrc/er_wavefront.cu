@@ -153,8 +153,9 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
 #define WF_RAY1 1u
 #define WF_RAY2 2u
 
-template <bool ONE>
-__global__ void __launch_bounds__(128) k_wf_shade(const WfView* __restrict__ views, const WfView one, const float4* __restrict__ events,
+/* MINB: resident 128-thread blocks per SM (2: 255 registers, 3: 168, 4: 128, 6: 80) */
+template <bool ONE, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict__ views, const WfView one, const float4* __restrict__ events,
                                                   const uint32_t* __restrict__ n_events, float4* __restrict__ results,
                                                   float4* __restrict__ jobs, uint32_t* __restrict__ n_jobs)
 {
@@ -188,7 +189,18 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfView* __restrict__ vie
             ms.light_uvw = V3(e4.x, e4.y, e4.z);
             SE.type = 0; SE.valid = true; SE.T = 0.0f; SE.Le = C3(0, 0, 0);
             SE.P = V3(e1.x, e1.y, e1.z);
-            SE.N = normalized_gradient(P, SE.P);     /* NormalizedGradient of SampleVolume (Source/raymarching.h:70) */
+            /* NormalizedGradient of SampleVolume (Source/raymarching.h:70); with
+               central differences its six intensities also give the gradient
+               magnitude of the shader switch */
+            float gm = -1.0f;
+            if (P.gradient_mode == 1) {
+                Grad6 g6;
+                gradient_samples(P, SE.P, g6);
+                SE.N = vnorm(gradient_cd6(g6));
+                if (P.apply_shading_type && P.shading_type >= 2 && P.shading_type <= 4) gm = gradient_magnitude6(P, g6);
+            } else {
+                SE.N = normalized_gradient(P, SE.P);
+            }
             SE.Wo = V3(e3.x, e3.y, e3.z);
             /* UniformSampleOneLight - Source/transport.h:115-156 */
             const float I = get_intensity(P, SE.P);
@@ -205,7 +217,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfView* __restrict__ vie
             } else {
                 const Light& L = P.lights[idx];
                 Shader sh;
-                const int type = P.apply_shading_type ? select_shader_type(P, SE, I, rng) : 0;
+                const int type = P.apply_shading_type ? select_shader_type(P, SE, I, rng, gm) : 0;
                 shader_init(sh, type, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
                             1000000.0f * er_powf(plf_eval(P.tfs->glossiness, I), 7.0f));
                 count = (float)P.light_count;
@@ -479,7 +491,14 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
 #undef ER_PRIMARY
         stage_end(t0, 0, s);
         t0 = stage_begin(s);
-        k_wf_shade<ONE><<<sm * 16, 128, 0, s>>>(d_views, one, B.events, B.counters, B.results, B.jobs, B.counters + 1);
+#define ER_SHADE(M) k_wf_shade<ONE, M><<<sm * 16, 128, 0, s>>>(d_views, one, B.events, B.counters, B.results, B.jobs, B.counters + 1)
+        switch (B.tune_shade) {
+        case 3: ER_SHADE(3); break;
+        case 4: ER_SHADE(4); break;
+        case 6: ER_SHADE(6); break;
+        default: ER_SHADE(2); break;
+        }
+#undef ER_SHADE
         stage_end(t0, 1, s);
         t0 = stage_begin(s);
 #define ER_SHADOW(M) k_wf_shadow<M, ONE><<<sm * 8, 256, 0, s>>>(d_views, one, B.jobs, B.counters + 1, B.results)

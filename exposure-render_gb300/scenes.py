@@ -14,7 +14,7 @@ scene is fully described by its name and parameters.
         sphere light; 1024^2; 256 spp; bilateral filter and tone map.
     c3  batched forward: 64 random orbit views over three blob volumes of
         96^3, 256^3 and 384x384x256 (x, y, z); films drawn from
-        {128, 256, 384, 512}^2; 32-128 spp per view; delta tracking.
+        {128, 256, 384, 512}^2; 32-128 spp per view; delta tracking, full MIS.
 """
 from __future__ import annotations
 
@@ -323,14 +323,16 @@ C3_VOLUMES = ((96, 96, 96), (256, 256, 256), (256, 384, 384))   # (z, y, x)
 
 def c3_scenes(volumes=C3_VOLUMES, seed=30) -> list:
     """One C1-style scene (4-node transfer function, one area light) per blob
-    volume, delta-tracked free flight; each scene's tracer is the template of
-    the views that look at its volume."""
+    volume, delta-tracked free flight and full MIS (the unbiased estimator);
+    each scene's tracer is the template of the views that look at its
+    volume."""
     out = []
     for k, shp in enumerate(volumes):
         vol = blob_volume(shp, seed=seed + k)
         lights, textures = c1_lights()
         t = c1_tracer((C3_FILMS[0], C3_FILMS[0]))
         t.settings.free_flight = C.FREE_FLIGHT_DELTA
+        t.settings.mis = C.MIS_FULL
         out.append(Scene(f"c3v{k}", vol, tracer=t, lights=lights, textures=textures, spp=32))
     return out
 

@@ -218,7 +218,9 @@ typedef struct er_render_settings {
     int32_t tune_primary;         /* wavefront: resident 256-thread blocks per SM the free-flight stage is compiled for:
                                      2, 3, 4, 6 or 8 (0 or other values: 4) */
     int32_t tune_shadow;          /* wavefront: same for the shadow stage (0 or other values: 4) */
-    int32_t reserved[2];
+    int32_t tune_shade;           /* wavefront: resident 128-thread blocks per SM of the shade stage
+                                     (2, 3, 4 or 6; 0 or other values: 2) */
+    int32_t reserved[1];
 } er_render_settings;
 
 /* ErTracer (Source/ertracer.h:33-117).  light_ids/object_ids/clipping_ids are
@@ -385,6 +387,58 @@ ER_API er_status er_batch_info(int32_t batch_id, int32_t* n_windows, int32_t* n_
 ER_API er_status er_batch_destroy(int32_t batch_id);
 
 /* ---------------------------------------------------------------------- */
+/* differentiable medium (no reference counterpart)                        */
+/* ---------------------------------------------------------------------- */
+
+/* A float density grid in place of the tracer volume's intensities (same
+   resolution and placement; the tracer supplies camera, lights and
+   settings).  sigma(x) = scale * opacity(rho(x)), rho the trilinear
+   interpolation of the grid, opacity a uniform cubic B-spline of the
+   n_opacity values over u = 2 + rho * (n_opacity - 5) (control i at density
+   (i - 2) / (n_opacity - 5)); isotropic phase function with `albedo`.
+   The estimator (per sample: tentative collisions from the fixed majorant
+   grid, next-event estimation with probability nee_probability and a
+   ratio-tracked shadow segment, ratio-tracked throughput) draws random
+   numbers independently of the medium, so for fixed seeds its samples are
+   smooth functions of density and opacity values.  The majorant must bound
+   sigma (er_medium_majorant with a margin); a violation sets the tracer's
+   error word (ER_ERR_TIMEOUT at the next synchronising call). */
+typedef struct er_medium_desc {
+    const float* d_density;       /* device, the tracer volume's resolution, x fastest */
+    const float* d_opacity;       /* device, n_opacity B-spline values */
+    int32_t n_opacity;            /* 6 .. ER_MAX_TF_NODES */
+    float scale;                  /* sigma = scale * opacity */
+    float albedo[3];
+    float nee_probability;        /* (0, 1] */
+    const float* d_majorant;      /* device, one float per brick of brick^3 voxels (x fastest) */
+    int32_t brick;                /* 1 .. 64 */
+} er_medium_desc;
+
+/* Per-brick majorant of a medium into d_majorant: scale * (max opacity
+   control value over the spline segments of the brick's density range with
+   a 1-voxel apron * margin + floor). */
+ER_API er_status er_medium_majorant(int32_t tracer_id, const er_medium_desc* medium, float margin, float floor_, float* d_majorant,
+                                    void* stream);
+/* Renders spp samples per pixel: d_samples receives every sample
+   ((s * H * W + pixel) * 3 floats, RGB of the phase-function albedo times
+   light), d_sum_rgb (optional) the per-pixel sums in sample order. */
+ER_API er_status er_medium_render(int32_t tracer_id, const er_medium_desc* medium, int32_t spp, uint32_t view,
+                                  uint32_t first_sample, float* d_samples, float* d_sum_rgb, void* stream);
+/* The same samples with every medium-dependent quantity (density, opacity,
+   collision weights, transmittances, sums) in binary64; the geometry, which
+   does not depend on the medium, stays float.  For finite-difference checks
+   of the adjoint: d_samples64 (spp*W*H*3 doubles) and d_sum64 (W*H*3). */
+ER_API er_status er_medium_render_f64(int32_t tracer_id, const er_medium_desc* medium, int32_t spp, uint32_t view,
+                                      uint32_t first_sample, double* d_samples64, double* d_sum64, void* stream);
+/* Path-replay adjoint: given dLoss/d(pixel sum) (W*H*3) and the forward
+   samples (NULL: each thread recomputes its sample first), adds
+   dLoss/d(density) (grid) and dLoss/d(opacity values) to the gradient
+   buffers (either may be NULL). */
+ER_API er_status er_medium_adjoint(int32_t tracer_id, const er_medium_desc* medium, int32_t spp, uint32_t view,
+                                   uint32_t first_sample, const float* d_dloss_dsum, const float* d_samples,
+                                   float* d_grad_density, float* d_grad_opacity, void* stream);
+
+/* ---------------------------------------------------------------------- */
 /* autotuner (no reference counterpart)                                    */
 /* ---------------------------------------------------------------------- */
 
@@ -395,13 +449,15 @@ typedef struct er_tune_result {
     int32_t from_cache;       /* 1: read from the tuning cache, nothing measured */
     float msamples_per_s;     /* probe throughput of the chosen configuration */
     int32_t candidates;       /* configurations timed */
+    int32_t tune_shade;       /* occupancy variant of the shade stage */
 } er_tune_result;
 
 /* Times probe renders of a bound tracer (probe_spp samples per pixel of its
    film, one warm-up each) over majorant bricks {2, 4, 8, 16} (delta
    tracking only) and then the occupancy variants of the wavefront stages,
    and writes the fastest configuration into the bound tracer's settings (the
-   caller's descriptor is not changed; re-binding it restores its values).
+   caller's descriptor is not changed; re-binding it restores its values),
+   and last the shade stage's variants.
    Results are cached per device, volume and shading configuration in the
    file named by the environment variable ER_TUNE_CACHE (default
    $HOME/.cache/exposurerender_gb300/autotune.txt; "off" disables the

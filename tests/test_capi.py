@@ -57,7 +57,7 @@ def test_host_only_calls(lib):
 def test_struct_layout_matches_c():
     structs = ["er_plf", "er_color_tf", "er_shape", "er_light_desc", "er_procedural", "er_texture_desc", "er_volume_desc",
                "er_bitmap_desc", "er_object_desc", "er_clipping_object_desc", "er_camera_desc", "er_render_settings",
-               "er_tracer_desc", "er_batch_view", "er_tune_result"]
+               "er_tracer_desc", "er_batch_view", "er_tune_result", "er_medium_desc"]
     src = '#include <stdio.h>\n#include <stddef.h>\n#include "er_capi.h"\nint main(void){\n'
     for s in structs:
         src += f'printf("{s} %zu\\n", sizeof({s}));\n'

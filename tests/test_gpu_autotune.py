@@ -53,11 +53,12 @@ def test_autotune_delta_sweep_and_cache(torch, lib, runtime, oracle, cache):
         first = r.autotune(2)
         assert first["majorant_brick"] in (2, 4, 8, 16)
         assert first["tune_primary"] in (2, 3, 4, 6, 8) and first["tune_shadow"] in (2, 3, 4, 6, 8)
-        assert first["candidates"] == 4 + 8 and not first["from_cache"] and first["msamples_per_s"] > 0
+        assert first["tune_shade"] in (2, 3, 4, 6)
+        assert first["candidates"] == 4 + 8 + 4 and not first["from_cache"] and first["msamples_per_s"] > 0
         assert cache.exists() and len(cache.read_text().splitlines()) == 1
         again = r.autotune(2)
         assert again["from_cache"] and again["candidates"] == 0
-        for k in ("majorant_brick", "tune_primary", "tune_shadow"):
+        for k in ("majorant_brick", "tune_primary", "tune_shadow", "tune_shade"):
             assert again[k] == first[k]
         s = C.er_render_settings()
         C.check(lib.er_get_render_settings(r.tracer_id, s))
@@ -80,7 +81,7 @@ def test_autotune_march_skips_bricks(torch, lib, runtime, cache):
     r = runtime.Renderer(sc, lib)
     try:
         res = r.autotune(1)
-        assert res["candidates"] == 1 + 8          # the brick does not matter to the march
+        assert res["candidates"] == 1 + 8 + 4      # the brick does not matter to the march
         assert res["majorant_brick"] == 8
     finally:
         r.close()
