@@ -211,23 +211,38 @@ ER_D c3 dm_nee(const Params& P, const DmParams& M, v3 Pt, Rng& rng, v3& S, bool&
     return cscale(cmul(C3(M.albedo[0], M.albedo[1], M.albedo[2]), Li), DM_INV_4PI * (float)P.light_count / (LightPdf * M.q));
 }
 
-/* the sample's value; Real = double returns it in L64 (L is then unused) */
-template <bool ADJ, typename Real = float>
-ER_D c3 dm_sample(const Params& P, const DmParams& M, int x, int y, Rng& rng, c3 g, c3 Ltot, float* g_rho, float* s_tf,
-                  double* L64 = nullptr)
+/* random stream of the k-th next-event shadow segment of a sample: its own
+   lanes, so the camera ray's draws do not depend on the segments' */
+ER_D void dm_shadow_stream(uint32_t seed, uint32_t view, uint32_t pix, uint32_t sample, uint32_t k, Rng& r)
 {
-    c3 L = C3(0, 0, 0);
-    double Ld[3] = {0.0, 0.0, 0.0};
-    double Td = 1.0;
+    er_seed_lanes(seed ^ er_hash32(0x51ED2705u + k), view ^ 0x6A09E667u, pix, sample, &r.s0, &r.s1);
+}
+
+/* one tentative collision of the camera ray, as the walker hands it over */
+struct DmHit {
+    v3 Pt;
+    float mu;
+    bool nee, has;       /* next-event estimate drawn here; it found a light sample */
+    uint32_t k_nee;      /* index of the estimate along the ray (its shadow stream) */
+    c3 A0;               /* unshadowed next-event estimate */
+    v3 S;                /* light sample point */
+};
+
+/* the camera ray's tentative collisions in order; visit(hit, lookup,
+   opacity, sigma, w, T) sees each with the throughput T before it */
+template <typename Real, typename Visit>
+ER_D void dm_walk(const Params& P, const DmParams& M, int x, int y, Rng& rng, Visit& visit)
+{
     const v2 film_uv = rng.get2();
     const v2 lens_uv = rng.get2();
     const Ray R = sample_camera(P, x, y, film_uv, lens_uv);
     float t0, t1;
-    if (!dm_segment(P, R, t0, t1)) return L;
+    if (!dm_segment(P, R, t0, t1)) return;
     Dda d;
     dda_init(P, R, t0, t1, d);
-    float T = 1.0f;
+    Real T = 1.0f;
     float tau = -er_logf(rng.get1());
+    uint32_t nee = 0;
     int guard = 0;
     while (!d.done) {
         const float e = dda_exit(d);
@@ -242,94 +257,251 @@ ER_D c3 dm_sample(const Params& P, const DmParams& M, int x, int y, Rng& rng, c3
                     break;
                 }
                 t = t + dt;
-                const v3 Pt = vadd(R.O, vscale(R.D, t));
+                DmHit h;
+                h.Pt = vadd(R.O, vscale(R.D, t));
+                h.mu = mu;
                 DmLookup<Real> k;
-                dm_density(P, M, Pt, k);
+                dm_density(P, M, h.Pt, k);
                 DmTf<Real> o;
                 dm_opacity(M, k.rho, o);
-                if constexpr (sizeof(Real) == 8) {
-                    /* binary64 evaluation of the same sample: the draws are those of the float path */
-                    const double sig = (double)M.scale * o.alpha;
-                    const double w = sig / (double)mu;
-                    if (rng.get1() < M.q) {
-                        v3 S;
-                        bool has;
-                        const c3 A0 = dm_nee(P, M, Pt, rng, S, has);
-                        if (has) {
-                            const double Tr = dm_shadow<false, double>(P, M, Pt, S, rng, 0.0f, nullptr, nullptr);
-                            Ld[0] += (double)A0.r * Tr * Td * w;
-                            Ld[1] += (double)A0.g * Tr * Td * w;
-                            Ld[2] += (double)A0.b * Tr * Td * w;
-                        }
-                    }
-                    Td = Td * (1.0 - w);
-                    if (++guard > ER_DELTA_MAX_COLLISIONS) { atomicOr(P.err, 2); break; }
-                    tau = -er_logf(rng.get1());
-                    continue;
-                } else {
-                const float sig = M.scale * o.alpha;
-                if (!(sig < mu)) atomicOr(P.err, 4);     /* the majorant no longer bounds sigma */
-                const float w = sig / mu;
-                c3 A = C3(0, 0, 0);
-                if (rng.get1() < M.q) {
-                    v3 S;
-                    bool has;
-                    const c3 A0 = dm_nee(P, M, Pt, rng, S, has);
-                    if (has) {
-                        if constexpr (ADJ) {
-                            const Rng keep = rng;
-                            const float Tr = dm_shadow<false>(P, M, Pt, S, rng, 0.0f, nullptr, nullptr);
-                            A = cscale(A0, Tr);
-                            const c3 c = cscale(A, T * w);
-                            const float gc = g.r * c.r + g.g * c.g + g.b * c.b;
-                            if (gc != 0.0f) {
-                                Rng r2 = keep;
-                                dm_shadow<true>(P, M, Pt, S, r2, gc, g_rho, s_tf);
-                            }
-                        } else {
-                            A = cscale(A0, dm_shadow<false>(P, M, Pt, S, rng, 0.0f, nullptr, nullptr));
-                        }
-                    }
+                const Real sig = (Real)M.scale * o.alpha;
+                if (!(sig < (Real)mu)) atomicOr(P.err, 4);   /* the majorant no longer bounds sigma */
+                const Real w = sig / (Real)mu;
+                h.has = false;
+                h.nee = rng.get1() < M.q;
+                if (h.nee) {
+                    h.A0 = dm_nee(P, M, h.Pt, rng, h.S, h.has);
+                    h.k_nee = nee++;
                 }
-                const c3 c = cscale(A, T * w);
-                L = cadd(L, c);
-                if constexpr (ADJ) {
-                    const c3 rest = csub(Ltot, L);
-                    const c3 dLds = csub(cscale(A, T / mu), cdivs(rest, mu - sig));
-                    const float a = g.r * dLds.r + g.g * dLds.g + g.b * dLds.b;
-                    if (a != 0.0f) dm_scatter(M, k, o, a, g_rho, s_tf);
-                }
-                T = T * (1.0f - w);
-                if (++guard > ER_DELTA_MAX_COLLISIONS) { atomicOr(P.err, 2); return L; }
+                visit(h, k, o, sig, w, T);
+                T = T * ((Real)1.0f - w);
+                if (++guard > ER_DELTA_MAX_COLLISIONS) { atomicOr(P.err, 2); return; }
                 tau = -er_logf(rng.get1());
-                }
             }
         }
         dda_advance(P, d, e);
     }
-    if (L64) { L64[0] = Ld[0]; L64[1] = Ld[1]; L64[2] = Ld[2]; }
-    return L;
 }
 
-__global__ void __launch_bounds__(256) k_dm_forward(const Params P, const DmParams M, int spp, uint32_t view, uint32_t first,
-                                                    uint32_t npix, float* __restrict__ samples)
+/* ---- the wavefront estimator ------------------------------------------
+   A window of items (item = s * npix + pixel, s counted from the window's
+   first sample row):
+     k_dm_count   : walk, count the item's shadow jobs, reserve their slots
+     k_dm_jobs    : walk again, write the jobs in order (point, light
+                    sample, unshadowed estimate, T * w, stream index)
+     k_dm_shadow  : one thread per job: the ratio-tracked transmittance
+     k_dm_gather  : per item, L = sum over its jobs in order of (A0 Tr) (T w)
+   adjoint (after the four above):
+     k_dm_adj_primary : walk again with each job's transmittance: the
+                        collision terms, and g . c per job
+     k_dm_adj_shadow  : one thread per job: the shadow-segment terms
+   Every float operation and its order are the oracle's. */
+
+struct DmJobs {
+    float4* P;         /* Pt, T * w */
+    float4* S;         /* light sample, g . c (adjoint) */
+    float4* A;         /* A0, transmittance */
+    uint2* id;         /* item in the window, k_nee */
+    uint32_t* off;     /* per item: first job */
+    uint32_t* cnt;     /* per item: jobs */
+    uint32_t* total;   /* jobs of the window */
+    uint32_t cap;      /* job slots */
+};
+
+struct DmWindow {
+    uint32_t npix;
+    uint32_t s0;       /* first sample row of the window */
+    uint32_t items;
+    uint32_t view, first;
+};
+
+ER_D void dm_item(const Params& P, const DmWindow& W, uint32_t i, uint32_t& pix, uint32_t& sample, int& x, int& y)
 {
-    const uint64_t items = (uint64_t)spp * npix;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < items; i += stride) {
-        const uint32_t s = (uint32_t)(i / npix);
-        const uint32_t pix = (uint32_t)(i - (uint64_t)s * npix);
-        Rng rng;
-        er_seed_lanes(P.seed, view, pix, first + s, &rng.s0, &rng.s1);
-        const int x = (int)(pix % (uint32_t)P.film[0]), y = (int)(pix / (uint32_t)P.film[0]);
-        const c3 L = dm_sample<false>(P, M, x, y, rng, C3(0, 0, 0), C3(0, 0, 0), nullptr, nullptr);
-        samples[3 * i] = L.r;
-        samples[3 * i + 1] = L.g;
-        samples[3 * i + 2] = L.b;
+    const uint32_t s = W.s0 + i / W.npix;
+    pix = i % W.npix;
+    sample = W.first + s;
+    x = (int)(pix % (uint32_t)P.film[0]);
+    y = (int)(pix / (uint32_t)P.film[0]);
+}
+
+__global__ void __launch_bounds__(256) k_dm_count(const Params P, const DmParams M, const DmWindow W, DmJobs J)
+{
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < W.items; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        uint32_t n = 0;
+        if (i < W.items) {
+            uint32_t pix, sample;
+            int x, y;
+            dm_item(P, W, i, pix, sample, x, y);
+            Rng rng;
+            er_seed_lanes(P.seed, W.view, pix, sample, &rng.s0, &rng.s1);
+            auto count = [&](const DmHit& h, const DmLookup<float>&, const DmTf<float>&, float, float, float) { n += h.has ? 1u : 0u; };
+            dm_walk<float>(P, M, x, y, rng, count);
+        }
+        /* warp-aggregated reservation of the item's job slots */
+        const int lane = threadIdx.x & 31;
+        uint32_t incl = n;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        uint32_t base_slot = 0;
+        if (lane == 31) base_slot = atomicAdd(J.total, incl);
+        base_slot = __shfl_sync(0xffffffffu, base_slot, 31);
+        if (i < W.items) {
+            J.off[i] = base_slot + incl - n;
+            J.cnt[i] = n;
+        }
     }
 }
 
-/* the binary64 evaluation: per-sample values in double (finite differences) */
+__global__ void __launch_bounds__(256) k_dm_jobs(const Params P, const DmParams M, const DmWindow W, DmJobs J)
+{
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < W.items; i += stride) {
+        uint32_t pix, sample;
+        int x, y;
+        dm_item(P, W, i, pix, sample, x, y);
+        Rng rng;
+        er_seed_lanes(P.seed, W.view, pix, sample, &rng.s0, &rng.s1);
+        uint32_t j = J.off[i];
+        const uint32_t end = j + J.cnt[i];
+        auto write = [&](const DmHit& h, const DmLookup<float>&, const DmTf<float>&, float, float w, float T) {
+            if (!h.has || j >= end || j >= J.cap) return;
+            J.P[j] = make_float4(h.Pt.x, h.Pt.y, h.Pt.z, T * w);
+            J.S[j] = make_float4(h.S.x, h.S.y, h.S.z, 0.0f);
+            J.A[j] = make_float4(h.A0.r, h.A0.g, h.A0.b, 0.0f);
+            J.id[j] = make_uint2(i, h.k_nee);
+            j++;
+        };
+        dm_walk<float>(P, M, x, y, rng, write);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_dm_shadow(const Params P, const DmParams M, const DmWindow W, DmJobs J)
+{
+    const uint32_t n = min(*J.total, J.cap);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+        const uint2 id = J.id[j];
+        uint32_t pix, sample;
+        int x, y;
+        dm_item(P, W, id.x, pix, sample, x, y);
+        Rng sh;
+        dm_shadow_stream(P.seed, W.view, pix, sample, id.y, sh);
+        const float4 p = J.P[j], s = J.S[j];
+        const float Tr = dm_shadow<false>(P, M, V3(p.x, p.y, p.z), V3(s.x, s.y, s.z), sh, 0.0f, nullptr, nullptr);
+        J.A[j].w = Tr;
+    }
+}
+
+/* L of every item of the window in sample order; out = the item's slot of the
+   whole launch's samples (window item i is launch item base + i) */
+__global__ void k_dm_gather(const DmWindow W, const DmJobs J, uint64_t base, float* __restrict__ samples)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W.items) return;
+    c3 L = C3(0, 0, 0);
+    const uint32_t j0 = J.off[i], j1 = j0 + J.cnt[i];
+    for (uint32_t j = j0; j < j1 && j < J.cap; j++) {
+        const float4 a = J.A[j];
+        const float Tw = J.P[j].w;
+        const c3 A = cscale(C3(a.x, a.y, a.z), a.w);
+        L = cadd(L, cscale(A, Tw));
+    }
+    const uint64_t q = 3 * (base + i);
+    samples[q] = L.r;
+    samples[q + 1] = L.g;
+    samples[q + 2] = L.b;
+}
+
+/* one opacity-gradient row per warp: no block barrier, so a warp that
+   finishes its items does not wait for the block's slowest */
+#define DM_WARPS (256 / 32)
+
+ER_D float* dm_tf_row(float (*rows)[ER_MAX_TF_NODES])
+{
+    float* r = rows[threadIdx.x >> 5];
+    for (int j = threadIdx.x & 31; j < ER_MAX_TF_NODES; j += 32) r[j] = 0.0f;
+    __syncwarp();
+    return r;
+}
+
+ER_D void dm_tf_flush(const DmParams& M, const float* row, float* g_tf)
+{
+    __syncwarp();
+    for (int j = threadIdx.x & 31; j < M.tf_n; j += 32)
+        if (row[j] != 0.0f) atomicAdd(g_tf + j, row[j]);
+}
+
+__global__ void __launch_bounds__(256) k_dm_adj_primary(const Params P, const DmParams M, const DmWindow W, DmJobs J, uint64_t base,
+                                                        const float* __restrict__ dimg, const float* __restrict__ fwd,
+                                                        float* __restrict__ g_rho, float* __restrict__ g_tf)
+{
+    __shared__ float rows[DM_WARPS][ER_MAX_TF_NODES];
+    float* row = dm_tf_row(rows);
+    float* s_tf = g_tf ? row : nullptr;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < W.items; i += stride) {
+        uint32_t pix, sample;
+        int x, y;
+        dm_item(P, W, i, pix, sample, x, y);
+        const c3 g = C3(dimg[3 * pix], dimg[3 * pix + 1], dimg[3 * pix + 2]);
+        if (g.r == 0.0f && g.g == 0.0f && g.b == 0.0f) continue;
+        const uint64_t q = 3 * (base + i);
+        const c3 Lt = C3(fwd[q], fwd[q + 1], fwd[q + 2]);
+        Rng rng;
+        er_seed_lanes(P.seed, W.view, pix, sample, &rng.s0, &rng.s1);
+        uint32_t j = J.off[i];
+        const uint32_t end = j + J.cnt[i];
+        c3 L = C3(0, 0, 0);
+        auto adj = [&](const DmHit& h, const DmLookup<float>& k, const DmTf<float>& o, float sig, float w, float T) {
+            c3 A = C3(0, 0, 0);
+            if (h.has && j < end && j < J.cap) {
+                const float4 a = J.A[j];
+                A = cscale(C3(a.x, a.y, a.z), a.w);
+                const c3 c = cscale(A, T * w);
+                L = cadd(L, c);
+                J.S[j].w = g.r * c.r + g.g * c.g + g.b * c.b;
+                j++;
+            }
+            /* dL/dsigma = T A / mu - (Ltot - L_<=k) / (mu - sigma) */
+            const c3 rest = csub(Lt, L);
+            const c3 dLds = csub(cscale(A, T / h.mu), cdivs(rest, h.mu - sig));
+            const float a = g.r * dLds.r + g.g * dLds.g + g.b * dLds.b;
+            if (a != 0.0f) dm_scatter(M, k, o, a, g_rho, s_tf);
+        };
+        dm_walk<float>(P, M, x, y, rng, adj);
+    }
+    if (g_tf) dm_tf_flush(M, row, g_tf);
+}
+
+__global__ void __launch_bounds__(256) k_dm_adj_shadow(const Params P, const DmParams M, const DmWindow W, DmJobs J,
+                                                       float* __restrict__ g_rho, float* __restrict__ g_tf)
+{
+    __shared__ float rows[DM_WARPS][ER_MAX_TF_NODES];
+    float* row = dm_tf_row(rows);
+    float* s_tf = g_tf ? row : nullptr;
+    const uint32_t n = min(*J.total, J.cap);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+        const float gc = J.S[j].w;
+        if (gc == 0.0f) continue;
+        const uint2 id = J.id[j];
+        uint32_t pix, sample;
+        int x, y;
+        dm_item(P, W, id.x, pix, sample, x, y);
+        Rng sh;
+        dm_shadow_stream(P.seed, W.view, pix, sample, id.y, sh);
+        const float4 p = J.P[j], s = J.S[j];
+        dm_shadow<true>(P, M, V3(p.x, p.y, p.z), V3(s.x, s.y, s.z), sh, gc, g_rho, s_tf);
+    }
+    if (g_tf) dm_tf_flush(M, row, g_tf);
+}
+
+/* the binary64 evaluation: one thread per sample, every medium-dependent
+   quantity in double */
 __global__ void __launch_bounds__(256) k_dm_forward64(const Params P, const DmParams M, int spp, uint32_t view, uint32_t first,
                                                       uint32_t npix, double* __restrict__ samples)
 {
@@ -341,11 +513,20 @@ __global__ void __launch_bounds__(256) k_dm_forward64(const Params P, const DmPa
         Rng rng;
         er_seed_lanes(P.seed, view, pix, first + s, &rng.s0, &rng.s1);
         const int x = (int)(pix % (uint32_t)P.film[0]), y = (int)(pix / (uint32_t)P.film[0]);
-        double L[3];
-        dm_sample<false, double>(P, M, x, y, rng, C3(0, 0, 0), C3(0, 0, 0), nullptr, nullptr, L);
-        samples[3 * i] = L[0];
-        samples[3 * i + 1] = L[1];
-        samples[3 * i + 2] = L[2];
+        double L0 = 0.0, L1 = 0.0, L2 = 0.0;
+        auto acc = [&](const DmHit& h, const DmLookup<double>&, const DmTf<double>&, double, double w, double T) {
+            if (!h.has) return;
+            Rng sh;
+            dm_shadow_stream(P.seed, view, pix, first + s, h.k_nee, sh);
+            const double Tr = dm_shadow<false, double>(P, M, h.Pt, h.S, sh, 0.0f, nullptr, nullptr);
+            L0 += (double)h.A0.r * Tr * T * w;
+            L1 += (double)h.A0.g * Tr * T * w;
+            L2 += (double)h.A0.b * Tr * T * w;
+        };
+        dm_walk<double>(P, M, x, y, rng, acc);
+        samples[3 * i] = L0;
+        samples[3 * i + 1] = L1;
+        samples[3 * i + 2] = L2;
     }
 }
 
@@ -380,40 +561,6 @@ __global__ void k_dm_reduce(const float* __restrict__ samples, int spp, uint32_t
     sum[3 * pix] = a0;
     sum[3 * pix + 1] = a1;
     sum[3 * pix + 2] = a2;
-}
-
-__global__ void __launch_bounds__(256) k_dm_adjoint(const Params P, const DmParams M, int spp, uint32_t view, uint32_t first,
-                                                    uint32_t npix, const float* __restrict__ dimg,
-                                                    const float* __restrict__ fwd, float* __restrict__ g_rho,
-                                                    float* __restrict__ g_tf)
-{
-    __shared__ float s_tf[ER_MAX_TF_NODES];
-    for (int j = threadIdx.x; j < ER_MAX_TF_NODES; j += blockDim.x) s_tf[j] = 0.0f;
-    __syncthreads();
-    float* stf = g_tf ? s_tf : nullptr;
-    const uint64_t items = (uint64_t)spp * npix;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < items; i += stride) {
-        const uint32_t s = (uint32_t)(i / npix);
-        const uint32_t pix = (uint32_t)(i - (uint64_t)s * npix);
-        const c3 g = C3(dimg[3 * pix], dimg[3 * pix + 1], dimg[3 * pix + 2]);
-        if (g.r == 0.0f && g.g == 0.0f && g.b == 0.0f) continue;
-        const int x = (int)(pix % (uint32_t)P.film[0]), y = (int)(pix / (uint32_t)P.film[0]);
-        Rng rng;
-        c3 Lt;
-        if (fwd) {
-            Lt = C3(fwd[3 * i], fwd[3 * i + 1], fwd[3 * i + 2]);
-        } else {
-            er_seed_lanes(P.seed, view, pix, first + s, &rng.s0, &rng.s1);
-            Lt = dm_sample<false>(P, M, x, y, rng, C3(0, 0, 0), C3(0, 0, 0), nullptr, nullptr);
-        }
-        er_seed_lanes(P.seed, view, pix, first + s, &rng.s0, &rng.s1);
-        dm_sample<true>(P, M, x, y, rng, g, Lt, g_rho, stf);
-    }
-    __syncthreads();
-    if (g_tf)
-        for (int j = threadIdx.x; j < M.tf_n; j += blockDim.x)
-            if (s_tf[j] != 0.0f) atomicAdd(g_tf + j, s_tf[j]);
 }
 
 /* per-brick bound: the largest spline control value over the segments the
@@ -462,15 +609,118 @@ int sm_count()
     return sm > 0 ? sm : 132;
 }
 
+unsigned grid_for(uint64_t items, int per_sm)
+{
+    const uint64_t want = (items + 255) / 256, cap = (uint64_t)sm_count() * per_sm;
+    return (unsigned)(want < cap ? want : cap);
+}
+
 }  // namespace
+
+/* job storage of the wavefront medium estimator, grown on demand */
+struct DmWorkspace {
+    float4 *P = nullptr, *S = nullptr, *A = nullptr;
+    uint2* id = nullptr;
+    uint32_t *off = nullptr, *cnt = nullptr, *total = nullptr, *host_total = nullptr;
+    size_t cap = 0, item_cap = 0;
+    ~DmWorkspace()
+    {
+        cudaFree(P); cudaFree(S); cudaFree(A); cudaFree(id); cudaFree(off); cudaFree(cnt); cudaFree(total);
+        if (host_total) cudaFreeHost(host_total);
+    }
+    cudaError_t ensure_items(size_t n)
+    {
+        if (!total) {
+            cudaError_t e = cudaMalloc(&total, sizeof(uint32_t));
+            if (e == cudaSuccess) e = cudaMallocHost(&host_total, sizeof(uint32_t));
+            if (e != cudaSuccess) return e;
+        }
+        if (n <= item_cap) return cudaSuccess;
+        cudaFree(off); cudaFree(cnt);
+        off = cnt = nullptr;
+        cudaError_t e = cudaMalloc(&off, n * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc(&cnt, n * sizeof(uint32_t));
+        item_cap = e == cudaSuccess ? n : 0;
+        return e;
+    }
+    cudaError_t ensure_jobs(size_t n)
+    {
+        if (n <= cap) return cudaSuccess;
+        n = n + n / 4;
+        cudaFree(P); cudaFree(S); cudaFree(A); cudaFree(id);
+        P = S = A = nullptr;
+        id = nullptr;
+        cudaError_t e = cudaMalloc(&P, n * sizeof(float4));
+        if (e == cudaSuccess) e = cudaMalloc(&S, n * sizeof(float4));
+        if (e == cudaSuccess) e = cudaMalloc(&A, n * sizeof(float4));
+        if (e == cudaSuccess) e = cudaMalloc(&id, n * sizeof(uint2));
+        cap = e == cudaSuccess ? n : 0;
+        return e;
+    }
+};
+
+/* one workspace per device (callers hold the library lock) */
+static DmWorkspace& dm_workspace()
+{
+    static DmWorkspace* w[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    dev = dev < 0 ? 0 : (dev > 63 ? 63 : dev);
+    if (!w[dev]) w[dev] = new DmWorkspace();
+    return *w[dev];
+}
+
+/* the four forward stages (and the two adjoint stages when dimg != NULL)
+   over windows of whole sample rows; synchronises once per window to size
+   the job storage */
+static cudaError_t dm_windows(const Params& P, const DmParams& M, int spp, uint32_t view, uint32_t first, float* samples,
+                              const float* dimg, float* g_rho, float* g_tf, cudaStream_t s)
+{
+    DmWorkspace& ws = dm_workspace();
+    const uint32_t npix = (uint32_t)P.film[0] * (uint32_t)P.film[1];
+    uint32_t rows = (uint32_t)((1u << 21) / (npix ? npix : 1));
+    if (rows < 1) rows = 1;
+    cudaError_t e = ws.ensure_items((size_t)rows * npix);
+    if (e != cudaSuccess) return e;
+    for (uint32_t s0 = 0; s0 < (uint32_t)spp; s0 += rows) {
+        DmWindow W;
+        W.npix = npix;
+        W.s0 = s0;
+        W.items = ((uint32_t)spp - s0 < rows ? (uint32_t)spp - s0 : rows) * npix;
+        W.view = view;
+        W.first = first;
+        DmJobs J;
+        J.P = ws.P; J.S = ws.S; J.A = ws.A; J.id = ws.id; J.off = ws.off; J.cnt = ws.cnt; J.total = ws.total;
+        J.cap = (uint32_t)ws.cap;
+        if ((e = cudaMemsetAsync(ws.total, 0, sizeof(uint32_t), s)) != cudaSuccess) return e;
+        k_dm_count<<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
+        if ((e = cudaMemcpyAsync(ws.host_total, ws.total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+        const uint32_t njobs = *ws.host_total;
+        if ((e = ws.ensure_jobs(njobs)) != cudaSuccess) return e;
+        J.P = ws.P; J.S = ws.S; J.A = ws.A; J.id = ws.id; J.cap = (uint32_t)ws.cap;
+        const uint64_t base = (uint64_t)s0 * npix;
+        k_dm_jobs<<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
+        if (njobs) k_dm_shadow<<<grid_for(njobs, 16), 256, 0, s>>>(P, M, W, J);
+        if (!dimg || samples) {
+            /* forward values: written by the forward, read by the adjoint */
+            if (!dimg) k_dm_gather<<<(W.items + 255) / 256, 256, 0, s>>>(W, J, base, samples);
+        }
+        if (dimg) {
+            k_dm_adj_primary<<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J, base, dimg, samples, g_rho, g_tf);
+            if (njobs) k_dm_adj_shadow<<<grid_for(njobs, 16), 256, 0, s>>>(P, M, W, J, g_rho, g_tf);
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
 
 cudaError_t er_launch_dm_forward(const Params& P, const DmParams& M, int spp, uint32_t view, uint32_t first, float* samples,
                                  float* sum, cudaStream_t s)
 {
+    cudaError_t e = dm_windows(P, M, spp, view, first, samples, nullptr, nullptr, nullptr, s);
+    if (e != cudaSuccess) return e;
     const uint32_t npix = (uint32_t)P.film[0] * (uint32_t)P.film[1];
-    const uint64_t items = (uint64_t)spp * npix;
-    const uint64_t want = (items + 255) / 256, cap = (uint64_t)sm_count() * 32;
-    k_dm_forward<<<(unsigned)(want < cap ? want : cap), 256, 0, s>>>(P, M, spp, view, first, npix, samples);
     if (sum) k_dm_reduce<<<(npix + 255) / 256, 256, 0, s>>>(samples, spp, npix, sum);
     return cudaGetLastError();
 }
@@ -479,21 +729,29 @@ cudaError_t er_launch_dm_forward64(const Params& P, const DmParams& M, int spp, 
                                    double* sum, cudaStream_t s)
 {
     const uint32_t npix = (uint32_t)P.film[0] * (uint32_t)P.film[1];
-    const uint64_t items = (uint64_t)spp * npix;
-    const uint64_t want = (items + 255) / 256, cap = (uint64_t)sm_count() * 32;
-    k_dm_forward64<<<(unsigned)(want < cap ? want : cap), 256, 0, s>>>(P, M, spp, view, first, npix, samples);
+    k_dm_forward64<<<grid_for((uint64_t)spp * npix, 32), 256, 0, s>>>(P, M, spp, view, first, npix, samples);
     k_dm_reduce64<<<(npix + 255) / 256, 256, 0, s>>>(samples, spp, npix, sum);
     return cudaGetLastError();
 }
 
+/* fwd: the forward samples (spp * npix * 3); without them a scratch buffer
+   receives the recomputed values window by window */
 cudaError_t er_launch_dm_adjoint(const Params& P, const DmParams& M, int spp, uint32_t view, uint32_t first, const float* dimg,
                                  const float* fwd, float* g_rho, float* g_tf, cudaStream_t s)
 {
+    float* samples = const_cast<float*>(fwd);
+    float* scratch = nullptr;
     const uint32_t npix = (uint32_t)P.film[0] * (uint32_t)P.film[1];
-    const uint64_t items = (uint64_t)spp * npix;
-    const uint64_t want = (items + 255) / 256, cap = (uint64_t)sm_count() * 8;
-    k_dm_adjoint<<<(unsigned)(want < cap ? want : cap), 256, 0, s>>>(P, M, spp, view, first, npix, dimg, fwd, g_rho, g_tf);
-    return cudaGetLastError();
+    if (!fwd) {
+        cudaError_t e = cudaMallocAsync(&scratch, (size_t)spp * npix * 3 * sizeof(float), s);
+        if (e != cudaSuccess) return e;
+        e = dm_windows(P, M, spp, view, first, scratch, nullptr, nullptr, nullptr, s);
+        if (e != cudaSuccess) { cudaFreeAsync(scratch, s); return e; }
+        samples = scratch;
+    }
+    cudaError_t e = dm_windows(P, M, spp, view, first, samples, dimg, g_rho, g_tf, s);
+    if (scratch) cudaFreeAsync(scratch, s);
+    return e;
 }
 
 cudaError_t er_launch_dm_majorant(const float* rho, const int res[3], int B, const float* tf, int n, float scale, float margin,

@@ -2016,7 +2016,8 @@ void ER_OR(majorant_grid)(const uint16_t* vox, const int32_t* res, int32_t B, co
 /* drawn from the fixed majorant grid (DDA as the delta tracker); at    */
 /* each, with probability q (a random number independent of the        */
 /* medium), next-event estimation to one uniformly picked light with a  */
-/* ratio-tracked shadow segment; the contribution is weighted by the    */
+/* ratio-tracked shadow segment (its own random stream, by the index of  */
+/* the next-event estimate along the ray); the contribution is weighted by the */
 /* collision weight sigma/mu and the ratio-tracked throughput          */
 /* T = prod (1 - sigma_j/mu_j) of the earlier collisions.  Nothing the  */
 /* RNG draws depends on the medium, so for fixed seeds the estimate is  */
@@ -2124,6 +2125,14 @@ static int dm_segment(or_scene* s, const ray_t* R, float* t0, float* t1)
     return *t0 < *t1;
 }
 
+/* random stream of the k-th next-event shadow segment of a sample: its own
+   lanes, so that the camera ray's draws do not depend on how many the
+   shadow segments take */
+static void dm_shadow_stream(uint32_t seed, uint32_t view, uint32_t pix, uint32_t sample, uint32_t k, rng_t* r)
+{
+    er_seed_lanes(seed ^ er_hash32(0x51ED2705u + k), view ^ 0x6A09E667u, pix, sample, &r->s0, &r->s1);
+}
+
 /* ratio-tracked transmittance of a shadow segment; with a_scale != 0 the
    adjoint pass scatters -a_scale / (mu - sigma) at every collision */
 static float dm_shadow(or_scene* s, v3 P1, v3 P2, rng_t* rng, float a_scale, float* g_rho, float* g_tf)
@@ -2200,10 +2209,12 @@ static col3 dm_nee(or_scene* s, v3 P, rng_t* rng, v3* S, float* unshadowed_scale
     return c;
 }
 
-/* one sample; with g != NULL the adjoint pass (Ltot = the sample's forward
-   value, g = dLoss/dL) */
-static col3 dm_sample(or_scene* s, int x, int y, rng_t* rng, const col3* g, col3 Ltot, float* g_rho, float* g_tf)
+/* one sample (pixel pix, stream index sample); with g != NULL the adjoint
+   pass (Ltot = the sample's forward value, g = dLoss/dL) */
+static col3 dm_sample(or_scene* s, int x, int y, uint32_t view, uint32_t pix, uint32_t sample, rng_t* rng, const col3* g, col3 Ltot,
+                      float* g_rho, float* g_tf)
 {
+    uint32_t nee = 0;
     col3 L = C3(0, 0, 0);
     const v2 film_uv = rng_get2(rng);
     const v2 lens_uv = rng_get2(rng);
@@ -2239,18 +2250,20 @@ static col3 dm_sample(or_scene* s, int x, int y, rng_t* rng, const col3* g, col3
                     v3 S;
                     float has;
                     const col3 A0 = dm_nee(s, P, rng, &S, &has);
+                    const uint32_t k_nee = nee++;
                     if (has != 0.0f) {
+                        rng_t sh;
+                        dm_shadow_stream(s->st.seed, view, pix, sample, k_nee, &sh);
+                        const float Tr = dm_shadow(s, P, S, &sh, 0.0f, NULL, NULL);
+                        A = cscale(A0, Tr);
                         if (g) {
-                            /* the shadow factor first (forward draws), then the
-                               adjoint replay of the same segment */
-                            rng_t keep = *rng;
-                            const float Tr = dm_shadow(s, P, S, rng, 0.0f, NULL, NULL);
-                            A = cscale(A0, Tr);
+                            /* the adjoint replay of the same segment */
                             const col3 c = cscale(A, T * w);
                             const float gc = g->c[0] * c.c[0] + g->c[1] * c.c[1] + g->c[2] * c.c[2];
-                            if (gc != 0.0f) dm_shadow(s, P, S, &keep, gc, g_rho, g_tf);
-                        } else {
-                            A = cscale(A0, dm_shadow(s, P, S, rng, 0.0f, NULL, NULL));
+                            if (gc != 0.0f) {
+                                dm_shadow_stream(s->st.seed, view, pix, sample, k_nee, &sh);
+                                dm_shadow(s, P, S, &sh, gc, g_rho, g_tf);
+                            }
                         }
                     }
                 }
@@ -2301,9 +2314,9 @@ static void* dm_job_run(void* arg)
                 if (j->dimg) {
                     const col3 g = C3(j->dimg[3 * pix], j->dimg[3 * pix + 1], j->dimg[3 * pix + 2]);
                     const col3 Lt = C3(j->fwd[q], j->fwd[q + 1], j->fwd[q + 2]);
-                    dm_sample(s, x, y, &rng, &g, Lt, j->g_rho, j->g_tf);
+                    dm_sample(s, x, y, j->view, pix, j->first + (uint32_t)k, &rng, &g, Lt, j->g_rho, j->g_tf);
                 } else {
-                    const col3 L = dm_sample(s, x, y, &rng, NULL, C3(0, 0, 0), NULL, NULL);
+                    const col3 L = dm_sample(s, x, y, j->view, pix, j->first + (uint32_t)k, &rng, NULL, C3(0, 0, 0), NULL, NULL);
                     acc[0] += L.c[0]; acc[1] += L.c[1]; acc[2] += L.c[2];
                     if (j->samples) { j->samples[q] = L.c[0]; j->samples[q + 1] = L.c[1]; j->samples[q + 2] = L.c[2]; }
                 }
