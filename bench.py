@@ -719,7 +719,10 @@ def run_medium(args, rank, world, local_rank):
         "forward_ms": f_ms, "adjoint_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
         "adjoint_recompute_ms": br_ms, "adjoint_recompute_over_forward": br_ms / f_ms,
         "loss": loss, "grad_norm": {"density": float(state["g"][0].norm()), "opacity": float(state["g"][1].norm())},
-        "clocks": clk.summary(), "gpu_launches": args.steps * 3,
+        "clocks": clk.summary(),
+        # per window of 2^21 items: forward count, jobs, shadow, gather (+ one reduce per step);
+        # adjoint count, jobs, shadow, primary replay, shadow replay
+        "gpu_launches": args.steps * (9 * (-(-spp // max(1, (1 << 21) // (film[0] * film[1])))) + 1),
     }
     print(json.dumps(line), flush=True)
     r.close()
