@@ -694,18 +694,28 @@ ER_D bool intersects_light(const Params& P, const Ray& R)
 
 /* 3D DDA over the majorant bricks in local voxel units.  The state is kept
    in scalars (no arrays indexed by the stepping axis), so it stays in
-   registers; the arithmetic is the oracle's, operation for operation. */
+   registers; the arithmetic is the oracle's, operation for operation.  The
+   face times are computed from the brick index (no accumulation along the
+   ray), so the empty-space skip lands on the same faces as brick stepping. */
 struct Dda {
     float t, tmax;
     int bx, by, bz;
     int sx, sy, sz;
     float nx, ny, nz;        /* t of the next brick face per axis */
-    float dx, dy, dz;        /* t between faces per axis */
+    float lx, ly, lz;        /* ray origin in local voxel units */
+    float dx, dy, dz;        /* ray direction in local voxel units */
     bool done;
 };
 
+ER_D float dda_face(int step, int b, float B, float lo, float ld)
+{
+    if (step > 0) return ((float)(b + 1) * B - lo) / ld;
+    if (step < 0) return ((float)b * B - lo) / ld;
+    return FLT_MAX;
+}
+
 ER_D void dda_axis(float o, float dirc, float minp, float inv_size, int res, int nb, float B, float t0, int& b, int& step,
-                   float& tnext, float& tdelta)
+                   float& tnext, float& lo_out, float& ld_out)
 {
     const float sc = inv_size * (float)res;
     const float lo = (o - minp) * sc;
@@ -713,9 +723,10 @@ ER_D void dda_axis(float o, float dirc, float minp, float inv_size, int res, int
     const float L = lo + t0 * ld;
     b = (int)floorf(L / B);
     b = b < 0 ? 0 : (b >= nb ? nb - 1 : b);
-    if (ld > 0.0f) { step = 1; tnext = ((float)(b + 1) * B - lo) / ld; tdelta = B / ld; }
-    else if (ld < 0.0f) { step = -1; tnext = ((float)b * B - lo) / ld; tdelta = -B / ld; }
-    else { step = 0; tnext = FLT_MAX; tdelta = FLT_MAX; }
+    step = ld > 0.0f ? 1 : (ld < 0.0f ? -1 : 0);
+    tnext = dda_face(step, b, B, lo, ld);
+    lo_out = lo;
+    ld_out = ld;
 }
 
 ER_D void dda_init(const Params& P, const Ray& R, float t0, float t1, Dda& d)
@@ -724,9 +735,9 @@ ER_D void dda_init(const Params& P, const Ray& R, float t0, float t1, Dda& d)
     d.t = t0;
     d.tmax = t1;
     d.done = false;
-    dda_axis(R.O.x, R.D.x, P.minp[0], P.inv_size[0], P.res[0], P.nb[0], B, t0, d.bx, d.sx, d.nx, d.dx);
-    dda_axis(R.O.y, R.D.y, P.minp[1], P.inv_size[1], P.res[1], P.nb[1], B, t0, d.by, d.sy, d.ny, d.dy);
-    dda_axis(R.O.z, R.D.z, P.minp[2], P.inv_size[2], P.res[2], P.nb[2], B, t0, d.bz, d.sz, d.nz, d.dz);
+    dda_axis(R.O.x, R.D.x, P.minp[0], P.inv_size[0], P.res[0], P.nb[0], B, t0, d.bx, d.sx, d.nx, d.lx, d.dx);
+    dda_axis(R.O.y, R.D.y, P.minp[1], P.inv_size[1], P.res[1], P.nb[1], B, t0, d.by, d.sy, d.ny, d.ly, d.dy);
+    dda_axis(R.O.z, R.D.z, P.minp[2], P.inv_size[2], P.res[2], P.nb[2], B, t0, d.bz, d.sz, d.nz, d.lz, d.dz);
 }
 
 ER_D float dda_exit(const Dda& d)
@@ -741,23 +752,78 @@ ER_D float dda_exit(const Dda& d)
 ER_D void dda_advance(const Params& P, Dda& d, float e)
 {
     if (e >= d.tmax) { d.done = true; d.t = e; return; }
+    const float B = (float)P.brick;
     /* axis with the nearest face; ties go to x, then y */
     const bool ax = !(d.ny < d.nx) && !(d.nz < d.nx);
     const bool ay = !ax && !(d.nz < d.ny);
     if (ax) {
         d.bx += d.sx;
         if (d.bx < 0 || d.bx >= P.nb[0]) d.done = true;
-        d.nx += d.dx;
+        d.nx = dda_face(d.sx, d.bx, B, d.lx, d.dx);
     } else if (ay) {
         d.by += d.sy;
         if (d.by < 0 || d.by >= P.nb[1]) d.done = true;
-        d.ny += d.dy;
+        d.ny = dda_face(d.sy, d.by, B, d.ly, d.dy);
     } else {
         d.bz += d.sz;
         if (d.bz < 0 || d.bz >= P.nb[2]) d.done = true;
-        d.nz += d.dz;
+        d.nz = dda_face(d.sz, d.bz, B, d.lz, d.dz);
     }
     d.t = e;
+}
+
+/* brick index of axis j at ray parameter e, clamped into coarse cell c */
+ER_D int dda_cell_brick(float lo, float ld, float e, float B, int c, int K, int nb)
+{
+    int b = (int)floorf((lo + e * ld) / B);
+    const int l = c * K, h = (c * K + K - 1) < (nb - 1) ? (c * K + K - 1) : (nb - 1);
+    return b < l ? l : (b > h ? h : b);
+}
+
+/* Empty-space skip (the oracle's dda_skip): when the coarse cell of ck^3
+   bricks around the current brick has a zero majorant, jump to where the
+   ray leaves it.  No random numbers are drawn in empty bricks.  Returns
+   true when it moved or ended the walk. */
+ER_D bool dda_skip(const Params& P, Dda& d)
+{
+    if (!P.coarse) return false;
+    const int K = P.ck;
+    const int cx = d.bx / K, cy = d.by / K, cz = d.bz / K;
+    if (__ldg(P.coarse + ((size_t)cz * (size_t)P.ncb[1] + (size_t)cy) * (size_t)P.ncb[0] + (size_t)cx) > 0.0f) return false;
+    const float B = (float)P.brick;
+    const float ex = d.sx > 0 ? ((float)((cx + 1) * K) * B - d.lx) / d.dx : (d.sx < 0 ? ((float)(cx * K) * B - d.lx) / d.dx : FLT_MAX);
+    const float ey = d.sy > 0 ? ((float)((cy + 1) * K) * B - d.ly) / d.dy : (d.sy < 0 ? ((float)(cy * K) * B - d.ly) / d.dy : FLT_MAX);
+    const float ez = d.sz > 0 ? ((float)((cz + 1) * K) * B - d.lz) / d.dz : (d.sz < 0 ? ((float)(cz * K) * B - d.lz) / d.dz : FLT_MAX);
+    /* axis that leaves first; ties go to x, then y */
+    const bool ax = !(ey < ex) && !(ez < ex);
+    const bool ay = !ax && !(ez < ey);
+    float e = ax ? ex : (ay ? ey : ez);
+    if (e < d.t) e = d.t;
+    if (e >= d.tmax) { d.done = true; d.t = e; return true; }
+    if (ax) {
+        const int na = (cx + d.sx) * K + (d.sx > 0 ? 0 : K - 1);
+        if (na < 0 || na >= P.nb[0]) { d.done = true; d.t = e; return true; }
+        d.by = dda_cell_brick(d.ly, d.dy, e, B, cy, K, P.nb[1]);
+        d.bz = dda_cell_brick(d.lz, d.dz, e, B, cz, K, P.nb[2]);
+        d.bx = na;
+    } else if (ay) {
+        const int na = (cy + d.sy) * K + (d.sy > 0 ? 0 : K - 1);
+        if (na < 0 || na >= P.nb[1]) { d.done = true; d.t = e; return true; }
+        d.bx = dda_cell_brick(d.lx, d.dx, e, B, cx, K, P.nb[0]);
+        d.bz = dda_cell_brick(d.lz, d.dz, e, B, cz, K, P.nb[2]);
+        d.by = na;
+    } else {
+        const int na = (cz + d.sz) * K + (d.sz > 0 ? 0 : K - 1);
+        if (na < 0 || na >= P.nb[2]) { d.done = true; d.t = e; return true; }
+        d.bx = dda_cell_brick(d.lx, d.dx, e, B, cx, K, P.nb[0]);
+        d.by = dda_cell_brick(d.ly, d.dy, e, B, cy, K, P.nb[1]);
+        d.bz = na;
+    }
+    d.nx = dda_face(d.sx, d.bx, B, d.lx, d.dx);
+    d.ny = dda_face(d.sy, d.by, B, d.ly, d.dy);
+    d.nz = dda_face(d.sz, d.bz, B, d.lz, d.dz);
+    d.t = e;
+    return true;
 }
 
 ER_D float dda_majorant(const Params& P, const Dda& d)
@@ -783,6 +849,7 @@ ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE
     float tau = -er_logf(rng.get1());
     int guard = 0;
     while (!d.done) {
+        if (dda_skip(P, d)) continue;
         const float e = dda_exit(d);
         const float mu = dda_majorant(P, d);
         float t = d.t;
@@ -829,6 +896,7 @@ ER_D float transmittance_ratio(const Params& P, const Ray& R, Rng& rng)
     float tau = -er_logf(rng.get1());
     int guard = 0;
     while (!d.done) {
+        if (dda_skip(P, d)) continue;
         const float e = dda_exit(d);
         const float mu = dda_majorant(P, d);
         float t = d.t;

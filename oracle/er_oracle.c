@@ -150,6 +150,9 @@ struct or_scene {
     int brick;
     int nb[3];
     float* majorant;         /* per brick: DensityScale * max sigma over the brick footprint */
+    float* coarse;           /* per coarse cell of ck^3 bricks: the largest majorant (empty-space skip) */
+    int ck;
+    int ncb[3];
     float gm_inv_max;
     int gm_ready;
     /* differentiable medium (dm_attach): float density grid, cubic B-spline
@@ -261,6 +264,7 @@ void ER_OR(scene_destroy)(or_scene* s)
     free(s->textures);
     free(s->sigma);
     free(s->majorant);
+    free(s->coarse);
     free(s);
 }
 
@@ -1075,9 +1079,20 @@ static inline float sigma_lookup(const or_scene* s, float I)
 typedef struct {
     float t, tmax;
     int b[3], step[3];
-    float tnext[3], tdelta[3];
+    float lo[3], ld[3];      /* ray origin and direction in local voxel units */
+    float tnext[3];
     int done;
 } dda_t;
+
+/* t at which the ray leaves brick b of axis i in its stepping direction,
+   computed from the brick index (no accumulation along the ray, so the
+   empty-space skip below lands on the same faces as brick stepping) */
+static inline float dda_face(const dda_t* d, int i, int b, float B)
+{
+    if (d->step[i] > 0) return ((float)(b + 1) * B - d->lo[i]) / d->ld[i];
+    if (d->step[i] < 0) return ((float)b * B - d->lo[i]) / d->ld[i];
+    return FLT_MAX;
+}
 
 static void dda_init(const or_scene* s, const ray_t* R, float t0, float t1, dda_t* d)
 {
@@ -1093,9 +1108,10 @@ static void dda_init(const or_scene* s, const ray_t* R, float t0, float t1, dda_
         int b = (int)floorf(L / B);
         b = b < 0 ? 0 : (b >= s->nb[i] ? s->nb[i] - 1 : b);
         d->b[i] = b;
-        if (ld > 0.0f) { d->step[i] = 1; d->tnext[i] = ((float)(b + 1) * B - lo) / ld; d->tdelta[i] = B / ld; }
-        else if (ld < 0.0f) { d->step[i] = -1; d->tnext[i] = ((float)b * B - lo) / ld; d->tdelta[i] = -B / ld; }
-        else { d->step[i] = 0; d->tnext[i] = FLT_MAX; d->tdelta[i] = FLT_MAX; }
+        d->lo[i] = lo;
+        d->ld[i] = ld;
+        d->step[i] = ld > 0.0f ? 1 : (ld < 0.0f ? -1 : 0);
+        d->tnext[i] = dda_face(d, i, b, B);
     }
 }
 
@@ -1116,8 +1132,48 @@ static inline void dda_advance(const or_scene* s, dda_t* d, float e)
     if (d->tnext[2] < d->tnext[a]) a = 2;
     d->b[a] += d->step[a];
     if (d->b[a] < 0 || d->b[a] >= s->nb[a]) d->done = 1;
-    d->tnext[a] += d->tdelta[a];
+    d->tnext[a] = dda_face(d, a, d->b[a], (float)s->brick);
     d->t = e;
+}
+
+/* Empty-space skip: when the coarse cell (ck^3 bricks) around the current
+   brick has a zero majorant, jump to where the ray leaves it: the axis
+   that leaves first enters the next coarse cell, the other axes take the
+   brick at the exit point, clamped into the cell.  No random numbers are
+   drawn in empty bricks, so skipping changes nothing but the brick walk.
+   Returns 1 when it moved (or ended the walk). */
+static int dda_skip(or_scene* s, dda_t* d)
+{
+    if (!s->coarse) return 0;
+    const int K = s->ck;
+    const int c[3] = { d->b[0] / K, d->b[1] / K, d->b[2] / K };
+    if (s->coarse[((size_t)c[2] * (size_t)s->ncb[1] + (size_t)c[1]) * (size_t)s->ncb[0] + (size_t)c[0]] > 0.0f) return 0;
+    const float B = (float)s->brick;
+    float ce[3];
+    for (int i = 0; i < 3; i++) {
+        if (d->step[i] > 0) ce[i] = ((float)((c[i] + 1) * K) * B - d->lo[i]) / d->ld[i];
+        else if (d->step[i] < 0) ce[i] = ((float)(c[i] * K) * B - d->lo[i]) / d->ld[i];
+        else ce[i] = FLT_MAX;
+    }
+    int a = 0;
+    if (ce[1] < ce[a]) a = 1;
+    if (ce[2] < ce[a]) a = 2;
+    float e = ce[a];
+    if (e < d->t) e = d->t;
+    if (e >= d->tmax) { d->done = 1; d->t = e; return 1; }
+    const int na = (c[a] + d->step[a]) * K + (d->step[a] > 0 ? 0 : K - 1);
+    if (na < 0 || na >= s->nb[a]) { d->done = 1; d->t = e; return 1; }
+    for (int j = 0; j < 3; j++) {
+        if (j == a) continue;
+        int bj = (int)floorf((d->lo[j] + e * d->ld[j]) / B);
+        const int lo = c[j] * K, hi = (c[j] * K + K - 1) < (s->nb[j] - 1) ? (c[j] * K + K - 1) : (s->nb[j] - 1);
+        bj = bj < lo ? lo : (bj > hi ? hi : bj);
+        d->b[j] = bj;
+    }
+    d->b[a] = na;
+    for (int i = 0; i < 3; i++) d->tnext[i] = dda_face(d, i, d->b[i], B);
+    d->t = e;
+    return 1;
 }
 
 static inline float dda_majorant(or_scene* s, const dda_t* d)
@@ -1146,6 +1202,7 @@ static void sample_volume_delta(or_scene* s, ray_t R, rng_t* rng, scatter_event*
     float tau = -er_logf(rng_get1(rng));
     int guard = 0;
     while (!d.done) {
+        if (dda_skip(s, &d)) continue;
         const float e = dda_exit(&d);
         const float mu = dda_majorant(s, &d);
         float t = d.t;
@@ -1193,6 +1250,7 @@ static float transmittance_ratio(or_scene* s, ray_t R, rng_t* rng)
     float tau = -er_logf(rng_get1(rng));
     int guard = 0;
     while (!d.done) {
+        if (dda_skip(s, &d)) continue;
         const float e = dda_exit(&d);
         const float mu = dda_majorant(s, &d);
         float t = d.t;
@@ -1470,6 +1528,25 @@ static float gradient_magnitude_max_threaded(or_scene* s, int nthreads)
     return mx;
 }
 
+/* coarse cells of ck^3 bricks (16 voxels a side) holding the largest
+   majorant of their bricks: the empty-space skip's grid */
+static int coarse_bricks(int brick) { return brick >= 16 ? 1 : 16 / brick; }
+
+static void build_coarse(or_scene* s)
+{
+    s->ck = coarse_bricks(s->brick);
+    for (int i = 0; i < 3; i++) s->ncb[i] = (s->nb[i] + s->ck - 1) / s->ck;
+    free(s->coarse);
+    s->coarse = (float*)calloc((size_t)s->ncb[0] * s->ncb[1] * s->ncb[2], sizeof(float));
+    for (int bz = 0; bz < s->nb[2]; bz++)
+        for (int by = 0; by < s->nb[1]; by++)
+            for (int bx = 0; bx < s->nb[0]; bx++) {
+                const float m = s->majorant[((size_t)bz * s->nb[1] + by) * s->nb[0] + bx];
+                float* c = &s->coarse[((size_t)(bz / s->ck) * s->ncb[1] + (by / s->ck)) * s->ncb[0] + (bx / s->ck)];
+                *c = m > *c ? m : *c;
+            }
+}
+
 static void prepare_extensions(or_scene* s)
 {
     const size_t n = (size_t)s->res[0] * (size_t)s->res[1] * (size_t)s->res[2];
@@ -1508,6 +1585,7 @@ static void prepare_extensions(or_scene* s)
                     for (int i = vlo; i <= (int)vhi; i++) m = s->sigma[i] > m ? s->sigma[i] : m;
                     s->majorant[((size_t)bz * s->nb[1] + by) * s->nb[0] + bx] = s->st.density_scale * m;
                 }
+        build_coarse(s);
     }
     s->gm_inv_max = 0.0f;
     s->gm_ready = 0;
@@ -2042,6 +2120,8 @@ void ER_OR(dm_attach)(or_scene* s, const float* rho, const float* tf_val, int32_
     free(s->majorant);
     s->majorant = (float*)malloc(sizeof(float) * nbt);
     for (size_t i = 0; i < nbt; i++) s->majorant[i] = majorant[i];
+    free(s->coarse);             /* the medium's walk has no empty-space skip */
+    s->coarse = NULL;
 }
 
 /* corners and weights of the trilinear density lookup */
@@ -2151,6 +2231,7 @@ static float dm_shadow(or_scene* s, v3 P1, v3 P2, rng_t* rng, float a_scale, flo
     float Tr = 1.0f;
     float tau = -er_logf(rng_get1(rng));
     while (!d.done) {
+        if (dda_skip(s, &d)) continue;
         const float e = dda_exit(&d);
         const float mu = dda_majorant(s, &d);
         float t = d.t;
@@ -2226,6 +2307,7 @@ static col3 dm_sample(or_scene* s, int x, int y, uint32_t view, uint32_t pix, ui
     float T = 1.0f;
     float tau = -er_logf(rng_get1(rng));
     while (!d.done) {
+        if (dda_skip(s, &d)) continue;
         const float e = dda_exit(&d);
         const float mu = dda_majorant(s, &d);
         float t = d.t;
