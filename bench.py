@@ -37,6 +37,7 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+R = importlib.import_module("exposure-render_gb300.replicas")
 
 WORKLOADS = {
     "c2": dict(name="c2-ct-shells-512^3-1024^2-256spp", res=512, film=(1024, 1024), spp=256),
@@ -354,7 +355,7 @@ def run_ours(args, wl, rank, world, local_rank):
     scene.tracer.settings.free_flight = 1                # the fast path: delta tracking, full MIS
     scene.tracer.settings.mis = 1
     shading = describe_shading(scene)
-    scene.tracer.settings.seed = 1 + rank                # one replica view per rank
+    scene.tracer.settings.seed = R.view_seed(1, rank)    # one replica view per rank
     r = runtime.Renderer(scene, lib)
     spp = W["spp"]
     width, height = scene.width, scene.height
@@ -387,13 +388,10 @@ def run_ours(args, wl, rank, world, local_rank):
     ms = ev0.elapsed_time(ev1)
     C.check(lib.er_profile_enable(0))
     stage_ms, stage_launches = read_profile(lib, C)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
+    ms = R.max_over_ranks(ms, dist)
+    R.barrier(dist)
     samples_per_step = width * height * spp
-    value = world * samples_per_step * args.steps / (ms / 1e3) / 1e6
+    value = R.whole_job_rate(samples_per_step * args.steps, ms / 1e3, world) / 1e6
 
     # the plain single-view path on the same workload and shading: the
     # reference's fixed-step march (one warm-up, one timed step)
@@ -441,12 +439,8 @@ def run_ours(args, wl, rank, world, local_rank):
     for _ in range(e2e_steps):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * samples_per_step * e2e_steps / e2e_s / 1e6
+    e2e_s = R.max_over_ranks(time.perf_counter() - t0, dist)
+    e2e_value = R.whole_job_rate(samples_per_step * e2e_steps, e2e_s, world) / 1e6
 
     if rank != 0:
         return
@@ -508,7 +502,10 @@ def run_batched(args, rank, world, local_rank):
     C.check(lib.er_set_stream(sp))
     scenes = S.c3_scenes()
     for sc in scenes:
-        sc.tracer.settings.seed = 1 + rank
+        sc.tracer.settings.seed = R.view_seed(1, rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
     rs = [runtime.Renderer(sc, lib) for sc in scenes]
     views = S.c3_views(n_views=args.views)
     # autotune each volume's tracer on one of its views (probe: 2 spp)
@@ -542,9 +539,11 @@ def run_batched(args, rank, world, local_rank):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
+    R.barrier(dist)
     with ClockSampler(local_rank) as clk:
         ms = timed(step, args.steps)
-    value = world * samples_per_step * args.steps / (ms / 1e3) / 1e6
+    ms = R.max_over_ranks(ms, dist)
+    value = R.whole_job_rate(samples_per_step * args.steps, ms / 1e3, world) / 1e6
 
     # stage shares: the same batch launched without the graph, profiled
     prof = runtime.Batch(table, flags=0)
@@ -609,8 +608,8 @@ def run_batched(args, rank, world, local_rank):
     e2e_steps = max(1, min(args.steps, 3))
     for _ in range(e2e_steps):
         e2e_step()
-    e2e_s = time.perf_counter() - t0
-    e2e_value = world * samples_per_step * e2e_steps / e2e_s / 1e6
+    e2e_s = R.max_over_ranks(time.perf_counter() - t0, dist)
+    e2e_value = R.whole_job_rate(samples_per_step * e2e_steps, e2e_s, world) / 1e6
     if rank != 0:
         return
     vol_bytes = sum(sc.volume.nbytes for sc in scenes)
@@ -660,7 +659,10 @@ def run_medium(args, rank, world, local_rank):
     C.check(lib.er_set_stream(ctypes.c_void_p(stream.cuda_stream)))
     res, film, spp = (128, 128, 128), (256, 256), 32
     sc = S.medium_scene(res=res, film=film)
-    sc.tracer.settings.seed = 1 + rank
+    sc.tracer.settings.seed = R.view_seed(1, rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
     r = runtime.Renderer(sc, lib)
     rho = torch.from_numpy(S.blob_density(res, n_blobs=10, seed=40)).cuda()
     tf = torch.from_numpy(S.ramp_opacity(64)).cuda()
@@ -700,9 +702,11 @@ def run_medium(args, rank, world, local_rank):
         fwd()
         bwd()
     torch.cuda.synchronize()
+    R.barrier(dist)
     with ClockSampler(local_rank) as clk:
         f_ms = timed(fwd, args.steps)
         b_ms = timed(bwd, args.steps)
+    f_ms, b_ms = R.max_over_ranks(f_ms, dist), R.max_over_ranks(b_ms, dist)
     br_ms = timed(bwd_recompute, 1)
     C.check(lib.er_synchronize())
     samples = film[0] * film[1] * spp
@@ -710,7 +714,7 @@ def run_medium(args, rank, world, local_rank):
     if rank != 0:
         return
     line = {
-        "metric": "Msamples/s", "value": world * samples / (f_ms / 1e3) / 1e6, "unit": "Msamples/s", "n_gpus": world,
+        "metric": "Msamples/s", "value": R.whole_job_rate(samples, f_ms / 1e3, world) / 1e6, "unit": "Msamples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": f_ms + b_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "c4-differentiable-128^3-density-64-opacity-256^2-32spp", "scale": 40.0, "nee_probability": 0.5,
@@ -750,9 +754,7 @@ def main():
             W["spp"] = args.spp
         W["name"] = W["name"].split("-")[0] + "-%s-%dx%d-%dspp" % (W["name"].split("-")[1], W["film"][0], W["film"][1], W["spp"])
         WORKLOADS[args.workload] = W
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    rank, world, local_rank = R.rank_info()
     if args.impl == "reference":
         run_reference(args, args.workload, rank, world)
         return
