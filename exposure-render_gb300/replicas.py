@@ -40,3 +40,19 @@ def whole_job_rate(samples_per_rank: float, seconds_max: float, world: int) -> f
     """all ranks' samples over the slowest rank's time (weak scaling: the
     per-rank work is fixed as the world grows)"""
     return world * samples_per_rank / seconds_max
+
+
+def split_samples(spp: int, rank: int, world: int) -> tuple[int, int]:
+    """(first sample, count) of a rank's share of one view's spp samples per
+    pixel: contiguous ranges of the view's sample stream"""
+    base, extra = divmod(spp, world)
+    first = rank * base + min(rank, extra)
+    return first, base + (1 if rank < extra else 0)
+
+
+def sum_over_ranks(t, dist):
+    """in-place all-reduce sum of a tensor (per-pixel sums of a view whose
+    samples were split across ranks, or gradients of the adjoint)"""
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return t
