@@ -169,7 +169,7 @@ def read_profile(lib, C):
     return ms, n
 
 
-def oracle_work(scene, settings, nthreads):
+def oracle_work(scene, settings, nthreads, spp=2):
     """Per-sample work counters of the estimator (oracle, same settings) over
     the whole field of view at a 128^2 film."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -182,7 +182,7 @@ def oracle_work(scene, settings, nthreads):
     scene.tracer = t
     orc = OL.load_oracle()
     h = OL.SceneHandle(orc, scene)
-    h.render_sum(2, nthreads=nthreads)
+    h.render_sum(spp, nthreads=nthreads)
     h.close()
     scene.tracer = saved
     return OL.render_stats(orc)
@@ -208,7 +208,13 @@ def stage_bytes(w):
     }
 
 
-def stage_roofline(work, stage_ms, stage_launches, samples, peaks, peak_kind, wl):
+def stage_roofline(work, ref_work, stage_ms, stage_launches, samples, peaks, peak_kind, wl):
+    """roofline of the transport: the reference estimator's algorithmic bytes
+    per sample (16 per lookup of the fixed-step march + 32 for the float4
+    accumulate) over the wavefront window's time (its four stage launches);
+    a fraction above 1 means fewer lookups than the reference needs.  The
+    stages' own bytes (this estimator's lookups and queue records) are
+    reported per stage."""
     names = ("primary", "shade", "shadow", "reduce")
     bps = stage_bytes(work)
     total = float(sum(stage_ms)) or 1.0
@@ -218,15 +224,19 @@ def stage_roofline(work, stage_ms, stage_launches, samples, peaks, peak_kind, wl
         stages[n] = {"ms": t, "share": t / total, "launches": int(stage_launches[i]),
                      "bytes_per_sample": bps[n], "achieved_gbs": (bps[n] * samples / (t / 1e3) / 1e9) if t > 0 else None}
     top = max(names, key=lambda n: stages[n]["ms"])
-    i = names.index(top)
-    launches = max(int(stage_launches[i]), 1)
-    achieved = stages[top]["achieved_gbs"] or 0.0
+    windows = max(int(stage_launches[0]), 1)
+    b_ref = BYTES_PER_LOOKUP * ref_work["lookups"] + 32.0
+    achieved = b_ref * samples / (total / 1e3) / 1e9
     traffic = profile_traffic(wl)
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-        "peak_source": peak_kind, "kernel": "k_wf_" + top, "avg_launch_ms": stages[top]["ms"] / launches,
-        "algorithmic_bytes_per_launch": bps[top] * samples / launches,
-        "traffic": (traffic.get(top) if traffic else None),
+        "peak_source": peak_kind, "kernel": "wavefront window (k_wf_primary + k_wf_shade + k_wf_shadow + k_wf_reduce)",
+        "avg_launch_ms": total / windows, "algorithmic_bytes_per_launch": b_ref * samples / windows,
+        "basis": "reference estimator: %.1f lookups/sample (fixed-step march, oracle) x 16 B + 32 B" % ref_work["lookups"],
+        "traffic": (traffic.get("window") if traffic else None),
+        "dominant_stage": {"kernel": "k_wf_" + top, "bytes_per_sample": bps[top], "achieved_gbs": stages[top]["achieved_gbs"],
+                           "frac": (stages[top]["achieved_gbs"] or 0.0) / peaks["hbm_gbs"],
+                           "traffic": (traffic.get(top) if traffic else None)},
     }
     return roofline, stages
 
@@ -453,7 +463,8 @@ def run_ours(args, wl, rank, world, local_rank):
     nthreads = os.cpu_count() or 1
     # work per sample of the measured configuration (oracle, whole field of view at 128^2)
     work = oracle_work(scene, r.tracer_desc.settings, nthreads)
-    roofline, stages = stage_roofline(work, stage_ms, stage_launches, samples_per_step * args.steps, peaks, peak_kind, wl)
+    ref_work = oracle_work(reference_path(scene), reference_path(scene).tracer.settings, nthreads, spp=1)
+    roofline, stages = stage_roofline(work, ref_work, stage_ms, stage_launches, samples_per_step * args.steps, peaks, peak_kind, wl)
     cpu_rate, kind, cores, sample = (None, None, None, None)
     if world == 1:
         cpu_rate, kind, cores, sample = cpu_reference_rate(reference_path(scene), seconds_target=12.0, steps=1)
@@ -476,6 +487,7 @@ def run_ours(args, wl, rank, world, local_rank):
         "gpu_launches": int(sum(stage_launches)),
         "stages": stages,
         "work_per_sample": work,
+        "reference_work_per_sample": ref_work,
         "plain": {"value": plain, "unit": "Msamples/s", "speedup": value / plain,
                   "what": "same workload and estimator, the reference's fixed-step march for free flight and shadows"},
         "time_to_rmse": rmse_summary(conv, "c2", value, plain, width * height),

@@ -694,19 +694,25 @@ ER_D bool intersects_light(const Params& P, const Ray& R)
 
 /* 3D DDA over the majorant bricks in local voxel units.  The state is kept
    in scalars (no arrays indexed by the stepping axis), so it stays in
-   registers; the arithmetic is the oracle's, operation for operation.  The
-   face times are computed from the brick index (no accumulation along the
-   ray), so the empty-space skip lands on the same faces as brick stepping. */
+   registers; the arithmetic is the oracle's, operation for operation. */
 struct Dda {
     float t, tmax;
     int bx, by, bz;
     int sx, sy, sz;
     float nx, ny, nz;        /* t of the next brick face per axis */
-    float lx, ly, lz;        /* ray origin in local voxel units */
-    float dx, dy, dz;        /* ray direction in local voxel units */
+    float dx, dy, dz;        /* t between faces per axis */
     bool done;
 };
 
+/* the ray's origin and direction of one axis in local voxel units */
+ER_D void dda_local(float o, float dirc, float minp, float inv_size, int res, float& lo, float& ld)
+{
+    const float sc = inv_size * (float)res;
+    lo = (o - minp) * sc;
+    ld = dirc * sc;
+}
+
+/* t at which the ray leaves brick b of one axis in its stepping direction */
 ER_D float dda_face(int step, int b, float B, float lo, float ld)
 {
     if (step > 0) return ((float)(b + 1) * B - lo) / ld;
@@ -715,18 +721,16 @@ ER_D float dda_face(int step, int b, float B, float lo, float ld)
 }
 
 ER_D void dda_axis(float o, float dirc, float minp, float inv_size, int res, int nb, float B, float t0, int& b, int& step,
-                   float& tnext, float& lo_out, float& ld_out)
+                   float& tnext, float& tdelta)
 {
-    const float sc = inv_size * (float)res;
-    const float lo = (o - minp) * sc;
-    const float ld = dirc * sc;
+    float lo, ld;
+    dda_local(o, dirc, minp, inv_size, res, lo, ld);
     const float L = lo + t0 * ld;
     b = (int)floorf(L / B);
     b = b < 0 ? 0 : (b >= nb ? nb - 1 : b);
-    step = ld > 0.0f ? 1 : (ld < 0.0f ? -1 : 0);
-    tnext = dda_face(step, b, B, lo, ld);
-    lo_out = lo;
-    ld_out = ld;
+    if (ld > 0.0f) { step = 1; tnext = ((float)(b + 1) * B - lo) / ld; tdelta = B / ld; }
+    else if (ld < 0.0f) { step = -1; tnext = ((float)b * B - lo) / ld; tdelta = -B / ld; }
+    else { step = 0; tnext = FLT_MAX; tdelta = FLT_MAX; }
 }
 
 ER_D void dda_init(const Params& P, const Ray& R, float t0, float t1, Dda& d)
@@ -735,9 +739,9 @@ ER_D void dda_init(const Params& P, const Ray& R, float t0, float t1, Dda& d)
     d.t = t0;
     d.tmax = t1;
     d.done = false;
-    dda_axis(R.O.x, R.D.x, P.minp[0], P.inv_size[0], P.res[0], P.nb[0], B, t0, d.bx, d.sx, d.nx, d.lx, d.dx);
-    dda_axis(R.O.y, R.D.y, P.minp[1], P.inv_size[1], P.res[1], P.nb[1], B, t0, d.by, d.sy, d.ny, d.ly, d.dy);
-    dda_axis(R.O.z, R.D.z, P.minp[2], P.inv_size[2], P.res[2], P.nb[2], B, t0, d.bz, d.sz, d.nz, d.lz, d.dz);
+    dda_axis(R.O.x, R.D.x, P.minp[0], P.inv_size[0], P.res[0], P.nb[0], B, t0, d.bx, d.sx, d.nx, d.dx);
+    dda_axis(R.O.y, R.D.y, P.minp[1], P.inv_size[1], P.res[1], P.nb[1], B, t0, d.by, d.sy, d.ny, d.dy);
+    dda_axis(R.O.z, R.D.z, P.minp[2], P.inv_size[2], P.res[2], P.nb[2], B, t0, d.bz, d.sz, d.nz, d.dz);
 }
 
 ER_D float dda_exit(const Dda& d)
@@ -752,27 +756,26 @@ ER_D float dda_exit(const Dda& d)
 ER_D void dda_advance(const Params& P, Dda& d, float e)
 {
     if (e >= d.tmax) { d.done = true; d.t = e; return; }
-    const float B = (float)P.brick;
     /* axis with the nearest face; ties go to x, then y */
     const bool ax = !(d.ny < d.nx) && !(d.nz < d.nx);
     const bool ay = !ax && !(d.nz < d.ny);
     if (ax) {
         d.bx += d.sx;
         if (d.bx < 0 || d.bx >= P.nb[0]) d.done = true;
-        d.nx = dda_face(d.sx, d.bx, B, d.lx, d.dx);
+        d.nx += d.dx;
     } else if (ay) {
         d.by += d.sy;
         if (d.by < 0 || d.by >= P.nb[1]) d.done = true;
-        d.ny = dda_face(d.sy, d.by, B, d.ly, d.dy);
+        d.ny += d.dy;
     } else {
         d.bz += d.sz;
         if (d.bz < 0 || d.bz >= P.nb[2]) d.done = true;
-        d.nz = dda_face(d.sz, d.bz, B, d.lz, d.dz);
+        d.nz += d.dz;
     }
     d.t = e;
 }
 
-/* brick index of axis j at ray parameter e, clamped into coarse cell c */
+/* brick index of one axis at ray parameter e, clamped into coarse cell c */
 ER_D int dda_cell_brick(float lo, float ld, float e, float B, int c, int K, int nb)
 {
     int b = (int)floorf((lo + e * ld) / B);
@@ -780,20 +783,25 @@ ER_D int dda_cell_brick(float lo, float ld, float e, float B, int c, int K, int 
     return b < l ? l : (b > h ? h : b);
 }
 
-/* Empty-space skip (the oracle's dda_skip): when the coarse cell of ck^3
-   bricks around the current brick has a zero majorant, jump to where the
-   ray leaves it.  No random numbers are drawn in empty bricks.  Returns
-   true when it moved or ended the walk. */
-ER_D bool dda_skip(const Params& P, Dda& d)
+/* Empty-space skip (the oracle's dda_skip), tried when the current brick's
+   majorant is zero: when the coarse cell of ck^3 bricks around it is empty
+   too, jump to where the ray leaves the cell; the next faces are computed
+   from the brick indices.  No random numbers are drawn in empty bricks.
+   Returns true when it moved or ended the walk. */
+static __device__ __noinline__ bool dda_skip(const Params& P, const Ray& R, Dda& d)
 {
     if (!P.coarse) return false;
     const int K = P.ck;
     const int cx = d.bx / K, cy = d.by / K, cz = d.bz / K;
     if (__ldg(P.coarse + ((size_t)cz * (size_t)P.ncb[1] + (size_t)cy) * (size_t)P.ncb[0] + (size_t)cx) > 0.0f) return false;
     const float B = (float)P.brick;
-    const float ex = d.sx > 0 ? ((float)((cx + 1) * K) * B - d.lx) / d.dx : (d.sx < 0 ? ((float)(cx * K) * B - d.lx) / d.dx : FLT_MAX);
-    const float ey = d.sy > 0 ? ((float)((cy + 1) * K) * B - d.ly) / d.dy : (d.sy < 0 ? ((float)(cy * K) * B - d.ly) / d.dy : FLT_MAX);
-    const float ez = d.sz > 0 ? ((float)((cz + 1) * K) * B - d.lz) / d.dz : (d.sz < 0 ? ((float)(cz * K) * B - d.lz) / d.dz : FLT_MAX);
+    float lx, dx_, ly, dy_, lz, dz_;
+    dda_local(R.O.x, R.D.x, P.minp[0], P.inv_size[0], P.res[0], lx, dx_);
+    dda_local(R.O.y, R.D.y, P.minp[1], P.inv_size[1], P.res[1], ly, dy_);
+    dda_local(R.O.z, R.D.z, P.minp[2], P.inv_size[2], P.res[2], lz, dz_);
+    const float ex = dda_face(d.sx, d.sx > 0 ? cx * K + K - 1 : cx * K, B, lx, dx_);
+    const float ey = dda_face(d.sy, d.sy > 0 ? cy * K + K - 1 : cy * K, B, ly, dy_);
+    const float ez = dda_face(d.sz, d.sz > 0 ? cz * K + K - 1 : cz * K, B, lz, dz_);
     /* axis that leaves first; ties go to x, then y */
     const bool ax = !(ey < ex) && !(ez < ex);
     const bool ay = !ax && !(ez < ey);
@@ -803,25 +811,25 @@ ER_D bool dda_skip(const Params& P, Dda& d)
     if (ax) {
         const int na = (cx + d.sx) * K + (d.sx > 0 ? 0 : K - 1);
         if (na < 0 || na >= P.nb[0]) { d.done = true; d.t = e; return true; }
-        d.by = dda_cell_brick(d.ly, d.dy, e, B, cy, K, P.nb[1]);
-        d.bz = dda_cell_brick(d.lz, d.dz, e, B, cz, K, P.nb[2]);
+        d.by = dda_cell_brick(ly, dy_, e, B, cy, K, P.nb[1]);
+        d.bz = dda_cell_brick(lz, dz_, e, B, cz, K, P.nb[2]);
         d.bx = na;
     } else if (ay) {
         const int na = (cy + d.sy) * K + (d.sy > 0 ? 0 : K - 1);
         if (na < 0 || na >= P.nb[1]) { d.done = true; d.t = e; return true; }
-        d.bx = dda_cell_brick(d.lx, d.dx, e, B, cx, K, P.nb[0]);
-        d.bz = dda_cell_brick(d.lz, d.dz, e, B, cz, K, P.nb[2]);
+        d.bx = dda_cell_brick(lx, dx_, e, B, cx, K, P.nb[0]);
+        d.bz = dda_cell_brick(lz, dz_, e, B, cz, K, P.nb[2]);
         d.by = na;
     } else {
         const int na = (cz + d.sz) * K + (d.sz > 0 ? 0 : K - 1);
         if (na < 0 || na >= P.nb[2]) { d.done = true; d.t = e; return true; }
-        d.bx = dda_cell_brick(d.lx, d.dx, e, B, cx, K, P.nb[0]);
-        d.by = dda_cell_brick(d.ly, d.dy, e, B, cy, K, P.nb[1]);
+        d.bx = dda_cell_brick(lx, dx_, e, B, cx, K, P.nb[0]);
+        d.by = dda_cell_brick(ly, dy_, e, B, cy, K, P.nb[1]);
         d.bz = na;
     }
-    d.nx = dda_face(d.sx, d.bx, B, d.lx, d.dx);
-    d.ny = dda_face(d.sy, d.by, B, d.ly, d.dy);
-    d.nz = dda_face(d.sz, d.bz, B, d.lz, d.dz);
+    d.nx = dda_face(d.sx, d.bx, B, lx, dx_);
+    d.ny = dda_face(d.sy, d.by, B, ly, dy_);
+    d.nz = dda_face(d.sz, d.bz, B, lz, dz_);
     d.t = e;
     return true;
 }
@@ -849,9 +857,9 @@ ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE
     float tau = -er_logf(rng.get1());
     int guard = 0;
     while (!d.done) {
-        if (dda_skip(P, d)) continue;
-        const float e = dda_exit(d);
         const float mu = dda_majorant(P, d);
+        if (mu == 0.0f && dda_skip(P, R, d)) continue;
+        const float e = dda_exit(d);
         float t = d.t;
         if (mu > 0.0f) {
             for (;;) {
@@ -896,9 +904,9 @@ ER_D float transmittance_ratio(const Params& P, const Ray& R, Rng& rng)
     float tau = -er_logf(rng.get1());
     int guard = 0;
     while (!d.done) {
-        if (dda_skip(P, d)) continue;
-        const float e = dda_exit(d);
         const float mu = dda_majorant(P, d);
+        if (mu == 0.0f && dda_skip(P, R, d)) continue;
+        const float e = dda_exit(d);
         float t = d.t;
         if (mu > 0.0f) {
             for (;;) {

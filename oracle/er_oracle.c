@@ -1079,18 +1079,23 @@ static inline float sigma_lookup(const or_scene* s, float I)
 typedef struct {
     float t, tmax;
     int b[3], step[3];
-    float lo[3], ld[3];      /* ray origin and direction in local voxel units */
-    float tnext[3];
+    float tnext[3], tdelta[3];
     int done;
 } dda_t;
 
-/* t at which the ray leaves brick b of axis i in its stepping direction,
-   computed from the brick index (no accumulation along the ray, so the
-   empty-space skip below lands on the same faces as brick stepping) */
-static inline float dda_face(const dda_t* d, int i, int b, float B)
+/* the ray's origin and direction of axis i in local voxel units */
+static inline void dda_local(const or_scene* s, const ray_t* R, int i, float* lo, float* ld)
 {
-    if (d->step[i] > 0) return ((float)(b + 1) * B - d->lo[i]) / d->ld[i];
-    if (d->step[i] < 0) return ((float)b * B - d->lo[i]) / d->ld[i];
+    const float sc = vget(s->inv_size, i) * (float)s->res[i];
+    *lo = (vget(R->O, i) - vget(s->minp, i)) * sc;
+    *ld = vget(R->D, i) * sc;
+}
+
+/* t at which the ray leaves brick b of axis i in its stepping direction */
+static inline float dda_face(int step, int b, float B, float lo, float ld)
+{
+    if (step > 0) return ((float)(b + 1) * B - lo) / ld;
+    if (step < 0) return ((float)b * B - lo) / ld;
     return FLT_MAX;
 }
 
@@ -1101,17 +1106,15 @@ static void dda_init(const or_scene* s, const ray_t* R, float t0, float t1, dda_
     d->tmax = t1;
     d->done = 0;
     for (int i = 0; i < 3; i++) {
-        const float sc = vget(s->inv_size, i) * (float)s->res[i];
-        const float lo = (vget(R->O, i) - vget(s->minp, i)) * sc;
-        const float ld = vget(R->D, i) * sc;
+        float lo, ld;
+        dda_local(s, R, i, &lo, &ld);
         const float L = lo + t0 * ld;
         int b = (int)floorf(L / B);
         b = b < 0 ? 0 : (b >= s->nb[i] ? s->nb[i] - 1 : b);
         d->b[i] = b;
-        d->lo[i] = lo;
-        d->ld[i] = ld;
-        d->step[i] = ld > 0.0f ? 1 : (ld < 0.0f ? -1 : 0);
-        d->tnext[i] = dda_face(d, i, b, B);
+        if (ld > 0.0f) { d->step[i] = 1; d->tnext[i] = ((float)(b + 1) * B - lo) / ld; d->tdelta[i] = B / ld; }
+        else if (ld < 0.0f) { d->step[i] = -1; d->tnext[i] = ((float)b * B - lo) / ld; d->tdelta[i] = -B / ld; }
+        else { d->step[i] = 0; d->tnext[i] = FLT_MAX; d->tdelta[i] = FLT_MAX; }
     }
 }
 
@@ -1132,28 +1135,28 @@ static inline void dda_advance(const or_scene* s, dda_t* d, float e)
     if (d->tnext[2] < d->tnext[a]) a = 2;
     d->b[a] += d->step[a];
     if (d->b[a] < 0 || d->b[a] >= s->nb[a]) d->done = 1;
-    d->tnext[a] = dda_face(d, a, d->b[a], (float)s->brick);
+    d->tnext[a] += d->tdelta[a];
     d->t = e;
 }
 
-/* Empty-space skip: when the coarse cell (ck^3 bricks) around the current
-   brick has a zero majorant, jump to where the ray leaves it: the axis
-   that leaves first enters the next coarse cell, the other axes take the
-   brick at the exit point, clamped into the cell.  No random numbers are
-   drawn in empty bricks, so skipping changes nothing but the brick walk.
-   Returns 1 when it moved (or ended the walk). */
-static int dda_skip(or_scene* s, dda_t* d)
+/* Empty-space skip, tried when the current brick's majorant is zero: when
+   the coarse cell (ck^3 bricks) around it is empty too, jump to where the
+   ray leaves the cell: the axis that leaves first enters the next coarse
+   cell, the other axes take the brick at the exit point, clamped into the
+   cell, and the next faces are computed from the brick indices.  No random
+   numbers are drawn in empty bricks, so skipping changes nothing but the
+   brick walk.  Returns 1 when it moved (or ended the walk). */
+static int dda_skip(or_scene* s, const ray_t* R, dda_t* d)
 {
     if (!s->coarse) return 0;
     const int K = s->ck;
     const int c[3] = { d->b[0] / K, d->b[1] / K, d->b[2] / K };
     if (s->coarse[((size_t)c[2] * (size_t)s->ncb[1] + (size_t)c[1]) * (size_t)s->ncb[0] + (size_t)c[0]] > 0.0f) return 0;
     const float B = (float)s->brick;
-    float ce[3];
+    float lo[3], ld[3], ce[3];
     for (int i = 0; i < 3; i++) {
-        if (d->step[i] > 0) ce[i] = ((float)((c[i] + 1) * K) * B - d->lo[i]) / d->ld[i];
-        else if (d->step[i] < 0) ce[i] = ((float)(c[i] * K) * B - d->lo[i]) / d->ld[i];
-        else ce[i] = FLT_MAX;
+        dda_local(s, R, i, &lo[i], &ld[i]);
+        ce[i] = dda_face(d->step[i], d->step[i] > 0 ? c[i] * K + K - 1 : c[i] * K, B, lo[i], ld[i]);
     }
     int a = 0;
     if (ce[1] < ce[a]) a = 1;
@@ -1165,13 +1168,13 @@ static int dda_skip(or_scene* s, dda_t* d)
     if (na < 0 || na >= s->nb[a]) { d->done = 1; d->t = e; return 1; }
     for (int j = 0; j < 3; j++) {
         if (j == a) continue;
-        int bj = (int)floorf((d->lo[j] + e * d->ld[j]) / B);
+        int bj = (int)floorf((lo[j] + e * ld[j]) / B);
         const int lo = c[j] * K, hi = (c[j] * K + K - 1) < (s->nb[j] - 1) ? (c[j] * K + K - 1) : (s->nb[j] - 1);
         bj = bj < lo ? lo : (bj > hi ? hi : bj);
         d->b[j] = bj;
     }
     d->b[a] = na;
-    for (int i = 0; i < 3; i++) d->tnext[i] = dda_face(d, i, d->b[i], B);
+    for (int i = 0; i < 3; i++) d->tnext[i] = dda_face(d->step[i], d->b[i], B, lo[i], ld[i]);
     d->t = e;
     return 1;
 }
@@ -1202,9 +1205,9 @@ static void sample_volume_delta(or_scene* s, ray_t R, rng_t* rng, scatter_event*
     float tau = -er_logf(rng_get1(rng));
     int guard = 0;
     while (!d.done) {
-        if (dda_skip(s, &d)) continue;
-        const float e = dda_exit(&d);
         const float mu = dda_majorant(s, &d);
+        if (mu == 0.0f && dda_skip(s, &R, &d)) continue;
+        const float e = dda_exit(&d);
         float t = d.t;
         if (mu > 0.0f) {
             for (;;) {
@@ -1250,9 +1253,9 @@ static float transmittance_ratio(or_scene* s, ray_t R, rng_t* rng)
     float tau = -er_logf(rng_get1(rng));
     int guard = 0;
     while (!d.done) {
-        if (dda_skip(s, &d)) continue;
-        const float e = dda_exit(&d);
         const float mu = dda_majorant(s, &d);
+        if (mu == 0.0f && dda_skip(s, &R, &d)) continue;
+        const float e = dda_exit(&d);
         float t = d.t;
         if (mu > 0.0f) {
             for (;;) {
@@ -2231,9 +2234,9 @@ static float dm_shadow(or_scene* s, v3 P1, v3 P2, rng_t* rng, float a_scale, flo
     float Tr = 1.0f;
     float tau = -er_logf(rng_get1(rng));
     while (!d.done) {
-        if (dda_skip(s, &d)) continue;
-        const float e = dda_exit(&d);
         const float mu = dda_majorant(s, &d);
+        if (mu == 0.0f && dda_skip(s, &R, &d)) continue;
+        const float e = dda_exit(&d);
         float t = d.t;
         if (mu > 0.0f) {
             for (;;) {
@@ -2307,9 +2310,9 @@ static col3 dm_sample(or_scene* s, int x, int y, uint32_t view, uint32_t pix, ui
     float T = 1.0f;
     float tau = -er_logf(rng_get1(rng));
     while (!d.done) {
-        if (dda_skip(s, &d)) continue;
-        const float e = dda_exit(&d);
         const float mu = dda_majorant(s, &d);
+        if (mu == 0.0f && dda_skip(s, &R, &d)) continue;
+        const float e = dda_exit(&d);
         float t = d.t;
         if (mu > 0.0f) {
             for (;;) {
