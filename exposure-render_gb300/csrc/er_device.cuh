@@ -93,9 +93,6 @@ struct Params {
     int brick;
     int nb[3];
     const float* majorant;
-    const float* coarse;     /* largest majorant per coarse cell of ck^3 bricks (empty-space skip), or NULL */
-    int ck;
-    int ncb[3];
     float gm_inv_max;        /* 1 / max gradient magnitude (hybrid switch) */
     /* camera (Source/camera.h:98-116) */
     int film[2];

@@ -55,9 +55,6 @@ cudaError_t er_launch_dm_adjoint(const erd::Params& P, const DmParams& M, int sp
 cudaError_t er_launch_dm_majorant(const float* rho, const int res[3], int B, const float* tf, int n, float scale, float margin,
                                   float floor_, float* out, cudaStream_t s);
 
-/* coarse cells of K^3 bricks with the largest majorant of their bricks */
-cudaError_t er_launch_coarse(const float* majorant, const int nb[3], int K, const int ncb[3], float* coarse, cudaStream_t s);
-
 /* sets the text returned by er_last_error_message() on this thread */
 void er_internal_set_error(const char* message);
 

@@ -156,9 +156,8 @@ ER_D Real dm_shadow(const Params& P, const DmParams& M, v3 P1, v3 P2, Rng& rng, 
     float tau = -er_logf(rng.get1());
     int guard = 0;
     while (!d.done) {
-        const float mu = dda_majorant(P, d);
-        if (mu == 0.0f && dda_skip(P, R, d)) continue;
         const float e = dda_exit(d);
+        const float mu = dda_majorant(P, d);
         float t = d.t;
         if (mu > 0.0f) {
             for (;;) {
@@ -246,9 +245,8 @@ ER_D void dm_walk(const Params& P, const DmParams& M, int x, int y, Rng& rng, Vi
     uint32_t nee = 0;
     int guard = 0;
     while (!d.done) {
-        const float mu = dda_majorant(P, d);
-        if (mu == 0.0f && dda_skip(P, R, d)) continue;
         const float e = dda_exit(d);
+        const float mu = dda_majorant(P, d);
         float t = d.t;
         if (mu > 0.0f) {
             for (;;) {

@@ -704,27 +704,12 @@ struct Dda {
     bool done;
 };
 
-/* the ray's origin and direction of one axis in local voxel units */
-ER_D void dda_local(float o, float dirc, float minp, float inv_size, int res, float& lo, float& ld)
-{
-    const float sc = inv_size * (float)res;
-    lo = (o - minp) * sc;
-    ld = dirc * sc;
-}
-
-/* t at which the ray leaves brick b of one axis in its stepping direction */
-ER_D float dda_face(int step, int b, float B, float lo, float ld)
-{
-    if (step > 0) return ((float)(b + 1) * B - lo) / ld;
-    if (step < 0) return ((float)b * B - lo) / ld;
-    return FLT_MAX;
-}
-
 ER_D void dda_axis(float o, float dirc, float minp, float inv_size, int res, int nb, float B, float t0, int& b, int& step,
                    float& tnext, float& tdelta)
 {
-    float lo, ld;
-    dda_local(o, dirc, minp, inv_size, res, lo, ld);
+    const float sc = inv_size * (float)res;
+    const float lo = (o - minp) * sc;
+    const float ld = dirc * sc;
     const float L = lo + t0 * ld;
     b = (int)floorf(L / B);
     b = b < 0 ? 0 : (b >= nb ? nb - 1 : b);
@@ -775,65 +760,6 @@ ER_D void dda_advance(const Params& P, Dda& d, float e)
     d.t = e;
 }
 
-/* brick index of one axis at ray parameter e, clamped into coarse cell c */
-ER_D int dda_cell_brick(float lo, float ld, float e, float B, int c, int K, int nb)
-{
-    int b = (int)floorf((lo + e * ld) / B);
-    const int l = c * K, h = (c * K + K - 1) < (nb - 1) ? (c * K + K - 1) : (nb - 1);
-    return b < l ? l : (b > h ? h : b);
-}
-
-/* Empty-space skip (the oracle's dda_skip), tried when the current brick's
-   majorant is zero: when the coarse cell of ck^3 bricks around it is empty
-   too, jump to where the ray leaves the cell; the next faces are computed
-   from the brick indices.  No random numbers are drawn in empty bricks.
-   Returns true when it moved or ended the walk. */
-static __device__ __noinline__ bool dda_skip(const Params& P, const Ray& R, Dda& d)
-{
-    if (!P.coarse) return false;
-    const int K = P.ck;
-    const int cx = d.bx / K, cy = d.by / K, cz = d.bz / K;
-    if (__ldg(P.coarse + ((size_t)cz * (size_t)P.ncb[1] + (size_t)cy) * (size_t)P.ncb[0] + (size_t)cx) > 0.0f) return false;
-    const float B = (float)P.brick;
-    float lx, dx_, ly, dy_, lz, dz_;
-    dda_local(R.O.x, R.D.x, P.minp[0], P.inv_size[0], P.res[0], lx, dx_);
-    dda_local(R.O.y, R.D.y, P.minp[1], P.inv_size[1], P.res[1], ly, dy_);
-    dda_local(R.O.z, R.D.z, P.minp[2], P.inv_size[2], P.res[2], lz, dz_);
-    const float ex = dda_face(d.sx, d.sx > 0 ? cx * K + K - 1 : cx * K, B, lx, dx_);
-    const float ey = dda_face(d.sy, d.sy > 0 ? cy * K + K - 1 : cy * K, B, ly, dy_);
-    const float ez = dda_face(d.sz, d.sz > 0 ? cz * K + K - 1 : cz * K, B, lz, dz_);
-    /* axis that leaves first; ties go to x, then y */
-    const bool ax = !(ey < ex) && !(ez < ex);
-    const bool ay = !ax && !(ez < ey);
-    float e = ax ? ex : (ay ? ey : ez);
-    if (e < d.t) e = d.t;
-    if (e >= d.tmax) { d.done = true; d.t = e; return true; }
-    if (ax) {
-        const int na = (cx + d.sx) * K + (d.sx > 0 ? 0 : K - 1);
-        if (na < 0 || na >= P.nb[0]) { d.done = true; d.t = e; return true; }
-        d.by = dda_cell_brick(ly, dy_, e, B, cy, K, P.nb[1]);
-        d.bz = dda_cell_brick(lz, dz_, e, B, cz, K, P.nb[2]);
-        d.bx = na;
-    } else if (ay) {
-        const int na = (cy + d.sy) * K + (d.sy > 0 ? 0 : K - 1);
-        if (na < 0 || na >= P.nb[1]) { d.done = true; d.t = e; return true; }
-        d.bx = dda_cell_brick(lx, dx_, e, B, cx, K, P.nb[0]);
-        d.bz = dda_cell_brick(lz, dz_, e, B, cz, K, P.nb[2]);
-        d.by = na;
-    } else {
-        const int na = (cz + d.sz) * K + (d.sz > 0 ? 0 : K - 1);
-        if (na < 0 || na >= P.nb[2]) { d.done = true; d.t = e; return true; }
-        d.bx = dda_cell_brick(lx, dx_, e, B, cx, K, P.nb[0]);
-        d.by = dda_cell_brick(ly, dy_, e, B, cy, K, P.nb[1]);
-        d.bz = na;
-    }
-    d.nx = dda_face(d.sx, d.bx, B, lx, dx_);
-    d.ny = dda_face(d.sy, d.by, B, ly, dy_);
-    d.nz = dda_face(d.sz, d.bz, B, lz, dz_);
-    d.t = e;
-    return true;
-}
-
 ER_D float dda_majorant(const Params& P, const Dda& d)
 {
     return __ldg(P.majorant + ((size_t)d.bz * (size_t)P.nb[1] + (size_t)d.by) * (size_t)P.nb[0] + (size_t)d.bx);
@@ -857,9 +783,8 @@ ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE
     float tau = -er_logf(rng.get1());
     int guard = 0;
     while (!d.done) {
-        const float mu = dda_majorant(P, d);
-        if (mu == 0.0f && dda_skip(P, R, d)) continue;
         const float e = dda_exit(d);
+        const float mu = dda_majorant(P, d);
         float t = d.t;
         if (mu > 0.0f) {
             for (;;) {
@@ -904,9 +829,8 @@ ER_D float transmittance_ratio(const Params& P, const Ray& R, Rng& rng)
     float tau = -er_logf(rng.get1());
     int guard = 0;
     while (!d.done) {
-        const float mu = dda_majorant(P, d);
-        if (mu == 0.0f && dda_skip(P, R, d)) continue;
         const float e = dda_exit(d);
+        const float mu = dda_majorant(P, d);
         float t = d.t;
         if (mu > 0.0f) {
             for (;;) {

@@ -184,7 +184,7 @@ struct TracerItem {
     DevBuf<erd::Texture> textures;
     DevBuf<float> sigma;
     DevBuf<int> light_ids;
-    DevBuf<float> majorant, rmq, coarse;
+    DevBuf<float> majorant, rmq;
     DevBuf<uint32_t> minmax;
     DevBuf<int> err;
     WfQueues wf;
@@ -493,15 +493,6 @@ er_status build(TracerItem& t)
         P.brick = brick;
         for (int i = 0; i < 3; i++) P.nb[i] = nb[i];
         P.majorant = t.majorant.p;
-        /* coarse cells of 16 voxels a side for the empty-space skip */
-        const int K = brick >= 16 ? 1 : 16 / brick;
-        int ncb[3];
-        for (int i = 0; i < 3; i++) ncb[i] = (nb[i] + K - 1) / K;
-        ER_CUDA(t.coarse.ensure((size_t)ncb[0] * ncb[1] * ncb[2]));
-        ER_CUDA(er_launch_coarse(t.majorant.p, nb, K, ncb, t.coarse.p, st));
-        P.coarse = t.coarse.p;
-        P.ck = K;
-        for (int i = 0; i < 3; i++) P.ncb[i] = ncb[i];
     }
     /* lights in LightIDs order */
     const int lc = d.light_count;
@@ -1442,7 +1433,6 @@ static er_status medium_params(int32_t tracer_id, const er_medium_desc* m, erd::
     P.brick = m->brick;
     for (int i = 0; i < 3; i++) P.nb[i] = (P.res[i] + m->brick - 1) / m->brick;
     P.majorant = m->d_majorant;
-    P.coarse = nullptr;          /* the medium's walk has no empty-space skip */
     M.rho = m->d_density;
     M.tf = m->d_opacity;
     M.tf_n = m->n_opacity;

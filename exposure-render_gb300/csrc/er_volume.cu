@@ -101,31 +101,6 @@ cudaError_t er_launch_majorant(const uint16_t* vox, const int res[3], int B, con
     return cudaGetLastError();
 }
 
-/* coarse cells of ck^3 bricks holding the largest majorant of their bricks
-   (the empty-space skip's grid); one thread per coarse cell */
-__global__ void k_coarse(const float* __restrict__ majorant, int nbx, int nby, int nbz, int K, int ncx, int ncy, int ncz,
-                         float* __restrict__ coarse)
-{
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncx * ncy * ncz) return;
-    const int cx = c % ncx, cy = (c / ncx) % ncy, cz = c / (ncx * ncy);
-    float m = 0.0f;
-    for (int bz = cz * K; bz < min(cz * K + K, nbz); bz++)
-        for (int by = cy * K; by < min(cy * K + K, nby); by++)
-            for (int bx = cx * K; bx < min(cx * K + K, nbx); bx++) {
-                const float v = majorant[((size_t)bz * nby + by) * nbx + bx];
-                m = v > m ? v : m;
-            }
-    coarse[c] = m;
-}
-
-cudaError_t er_launch_coarse(const float* majorant, const int nb[3], int K, const int ncb[3], float* coarse, cudaStream_t s)
-{
-    const int total = ncb[0] * ncb[1] * ncb[2];
-    k_coarse<<<(total + 255) / 256, 256, 0, s>>>(majorant, nb[0], nb[1], nb[2], K, ncb[0], ncb[1], ncb[2], coarse);
-    return cudaGetLastError();
-}
-
 /* ====================================================================== */
 /* Allocation-free majorant build                                           */
 /* ====================================================================== */

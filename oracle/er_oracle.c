@@ -150,9 +150,6 @@ struct or_scene {
     int brick;
     int nb[3];
     float* majorant;         /* per brick: DensityScale * max sigma over the brick footprint */
-    float* coarse;           /* per coarse cell of ck^3 bricks: the largest majorant (empty-space skip) */
-    int ck;
-    int ncb[3];
     float gm_inv_max;
     int gm_ready;
     /* differentiable medium (dm_attach): float density grid, cubic B-spline
@@ -264,7 +261,6 @@ void ER_OR(scene_destroy)(or_scene* s)
     free(s->textures);
     free(s->sigma);
     free(s->majorant);
-    free(s->coarse);
     free(s);
 }
 
@@ -1083,22 +1079,6 @@ typedef struct {
     int done;
 } dda_t;
 
-/* the ray's origin and direction of axis i in local voxel units */
-static inline void dda_local(const or_scene* s, const ray_t* R, int i, float* lo, float* ld)
-{
-    const float sc = vget(s->inv_size, i) * (float)s->res[i];
-    *lo = (vget(R->O, i) - vget(s->minp, i)) * sc;
-    *ld = vget(R->D, i) * sc;
-}
-
-/* t at which the ray leaves brick b of axis i in its stepping direction */
-static inline float dda_face(int step, int b, float B, float lo, float ld)
-{
-    if (step > 0) return ((float)(b + 1) * B - lo) / ld;
-    if (step < 0) return ((float)b * B - lo) / ld;
-    return FLT_MAX;
-}
-
 static void dda_init(const or_scene* s, const ray_t* R, float t0, float t1, dda_t* d)
 {
     const float B = (float)s->brick;
@@ -1106,8 +1086,9 @@ static void dda_init(const or_scene* s, const ray_t* R, float t0, float t1, dda_
     d->tmax = t1;
     d->done = 0;
     for (int i = 0; i < 3; i++) {
-        float lo, ld;
-        dda_local(s, R, i, &lo, &ld);
+        const float sc = vget(s->inv_size, i) * (float)s->res[i];
+        const float lo = (vget(R->O, i) - vget(s->minp, i)) * sc;
+        const float ld = vget(R->D, i) * sc;
         const float L = lo + t0 * ld;
         int b = (int)floorf(L / B);
         b = b < 0 ? 0 : (b >= s->nb[i] ? s->nb[i] - 1 : b);
@@ -1139,46 +1120,6 @@ static inline void dda_advance(const or_scene* s, dda_t* d, float e)
     d->t = e;
 }
 
-/* Empty-space skip, tried when the current brick's majorant is zero: when
-   the coarse cell (ck^3 bricks) around it is empty too, jump to where the
-   ray leaves the cell: the axis that leaves first enters the next coarse
-   cell, the other axes take the brick at the exit point, clamped into the
-   cell, and the next faces are computed from the brick indices.  No random
-   numbers are drawn in empty bricks, so skipping changes nothing but the
-   brick walk.  Returns 1 when it moved (or ended the walk). */
-static int dda_skip(or_scene* s, const ray_t* R, dda_t* d)
-{
-    if (!s->coarse) return 0;
-    const int K = s->ck;
-    const int c[3] = { d->b[0] / K, d->b[1] / K, d->b[2] / K };
-    if (s->coarse[((size_t)c[2] * (size_t)s->ncb[1] + (size_t)c[1]) * (size_t)s->ncb[0] + (size_t)c[0]] > 0.0f) return 0;
-    const float B = (float)s->brick;
-    float lo[3], ld[3], ce[3];
-    for (int i = 0; i < 3; i++) {
-        dda_local(s, R, i, &lo[i], &ld[i]);
-        ce[i] = dda_face(d->step[i], d->step[i] > 0 ? c[i] * K + K - 1 : c[i] * K, B, lo[i], ld[i]);
-    }
-    int a = 0;
-    if (ce[1] < ce[a]) a = 1;
-    if (ce[2] < ce[a]) a = 2;
-    float e = ce[a];
-    if (e < d->t) e = d->t;
-    if (e >= d->tmax) { d->done = 1; d->t = e; return 1; }
-    const int na = (c[a] + d->step[a]) * K + (d->step[a] > 0 ? 0 : K - 1);
-    if (na < 0 || na >= s->nb[a]) { d->done = 1; d->t = e; return 1; }
-    for (int j = 0; j < 3; j++) {
-        if (j == a) continue;
-        int bj = (int)floorf((lo[j] + e * ld[j]) / B);
-        const int lo = c[j] * K, hi = (c[j] * K + K - 1) < (s->nb[j] - 1) ? (c[j] * K + K - 1) : (s->nb[j] - 1);
-        bj = bj < lo ? lo : (bj > hi ? hi : bj);
-        d->b[j] = bj;
-    }
-    d->b[a] = na;
-    for (int i = 0; i < 3; i++) d->tnext[i] = dda_face(d->step[i], d->b[i], B, lo[i], ld[i]);
-    d->t = e;
-    return 1;
-}
-
 static inline float dda_majorant(or_scene* s, const dda_t* d)
 {
     s->stat[OR_STAT_MAJORANT]++;
@@ -1205,9 +1146,8 @@ static void sample_volume_delta(or_scene* s, ray_t R, rng_t* rng, scatter_event*
     float tau = -er_logf(rng_get1(rng));
     int guard = 0;
     while (!d.done) {
-        const float mu = dda_majorant(s, &d);
-        if (mu == 0.0f && dda_skip(s, &R, &d)) continue;
         const float e = dda_exit(&d);
+        const float mu = dda_majorant(s, &d);
         float t = d.t;
         if (mu > 0.0f) {
             for (;;) {
@@ -1253,9 +1193,8 @@ static float transmittance_ratio(or_scene* s, ray_t R, rng_t* rng)
     float tau = -er_logf(rng_get1(rng));
     int guard = 0;
     while (!d.done) {
-        const float mu = dda_majorant(s, &d);
-        if (mu == 0.0f && dda_skip(s, &R, &d)) continue;
         const float e = dda_exit(&d);
+        const float mu = dda_majorant(s, &d);
         float t = d.t;
         if (mu > 0.0f) {
             for (;;) {
@@ -1531,25 +1470,6 @@ static float gradient_magnitude_max_threaded(or_scene* s, int nthreads)
     return mx;
 }
 
-/* coarse cells of ck^3 bricks (16 voxels a side) holding the largest
-   majorant of their bricks: the empty-space skip's grid */
-static int coarse_bricks(int brick) { return brick >= 16 ? 1 : 16 / brick; }
-
-static void build_coarse(or_scene* s)
-{
-    s->ck = coarse_bricks(s->brick);
-    for (int i = 0; i < 3; i++) s->ncb[i] = (s->nb[i] + s->ck - 1) / s->ck;
-    free(s->coarse);
-    s->coarse = (float*)calloc((size_t)s->ncb[0] * s->ncb[1] * s->ncb[2], sizeof(float));
-    for (int bz = 0; bz < s->nb[2]; bz++)
-        for (int by = 0; by < s->nb[1]; by++)
-            for (int bx = 0; bx < s->nb[0]; bx++) {
-                const float m = s->majorant[((size_t)bz * s->nb[1] + by) * s->nb[0] + bx];
-                float* c = &s->coarse[((size_t)(bz / s->ck) * s->ncb[1] + (by / s->ck)) * s->ncb[0] + (bx / s->ck)];
-                *c = m > *c ? m : *c;
-            }
-}
-
 static void prepare_extensions(or_scene* s)
 {
     const size_t n = (size_t)s->res[0] * (size_t)s->res[1] * (size_t)s->res[2];
@@ -1588,7 +1508,6 @@ static void prepare_extensions(or_scene* s)
                     for (int i = vlo; i <= (int)vhi; i++) m = s->sigma[i] > m ? s->sigma[i] : m;
                     s->majorant[((size_t)bz * s->nb[1] + by) * s->nb[0] + bx] = s->st.density_scale * m;
                 }
-        build_coarse(s);
     }
     s->gm_inv_max = 0.0f;
     s->gm_ready = 0;
@@ -2123,8 +2042,6 @@ void ER_OR(dm_attach)(or_scene* s, const float* rho, const float* tf_val, int32_
     free(s->majorant);
     s->majorant = (float*)malloc(sizeof(float) * nbt);
     for (size_t i = 0; i < nbt; i++) s->majorant[i] = majorant[i];
-    free(s->coarse);             /* the medium's walk has no empty-space skip */
-    s->coarse = NULL;
 }
 
 /* corners and weights of the trilinear density lookup */
@@ -2234,9 +2151,8 @@ static float dm_shadow(or_scene* s, v3 P1, v3 P2, rng_t* rng, float a_scale, flo
     float Tr = 1.0f;
     float tau = -er_logf(rng_get1(rng));
     while (!d.done) {
-        const float mu = dda_majorant(s, &d);
-        if (mu == 0.0f && dda_skip(s, &R, &d)) continue;
         const float e = dda_exit(&d);
+        const float mu = dda_majorant(s, &d);
         float t = d.t;
         if (mu > 0.0f) {
             for (;;) {
@@ -2310,9 +2226,8 @@ static col3 dm_sample(or_scene* s, int x, int y, uint32_t view, uint32_t pix, ui
     float T = 1.0f;
     float tau = -er_logf(rng_get1(rng));
     while (!d.done) {
-        const float mu = dda_majorant(s, &d);
-        if (mu == 0.0f && dda_skip(s, &R, &d)) continue;
         const float e = dda_exit(&d);
+        const float mu = dda_majorant(s, &d);
         float t = d.t;
         if (mu > 0.0f) {
             for (;;) {
