@@ -80,6 +80,7 @@ struct Texture {             /* ErTexture + Procedural (Source/ertexture.h, Sour
 struct Params {
     /* volume (Source/volume.h:140-149) */
     const uint16_t* vox;
+    const uint2* quad;       /* per voxel (x, y, z): the x/y 2x2 corner quad at z, packed uint16 pairs, or NULL */
     int res[3];
     float minp[3];
     float inv_size[3];

@@ -53,6 +53,19 @@ ER_D float get_intensity(const Params& P, v3 p)
     const float dx = Lx - (float)vx;
     const float dy = Ly - (float)vy;
     const float dz = Lz - (float)vz;
+    if (P.quad && vx >= 0 && vx < P.res[0] - 1 && vy >= 0 && vy < P.res[1] - 1) {
+        /* the same eight corners from two 8-byte quad loads (no x/y clamping
+           needed inside the volume; z clamps per corner) */
+        const size_t slice = (size_t)P.res[0] * (size_t)P.res[1];
+        const size_t xy = (size_t)vy * (size_t)P.res[0] + (size_t)vx;
+        const uint2 a = __ldg(P.quad + (size_t)iclamp(vz, 0, P.res[2] - 1) * slice + xy);
+        const uint2 b = __ldg(P.quad + (size_t)iclamp(vz + 1, 0, P.res[2] - 1) * slice + xy);
+        const float q00 = lerp_u16(dx, (float)(a.x & 0xffffu), (float)(a.x >> 16));
+        const float q10 = lerp_u16(dx, (float)(a.y & 0xffffu), (float)(a.y >> 16));
+        const float q01 = lerp_u16(dx, (float)(b.x & 0xffffu), (float)(b.x >> 16));
+        const float q11 = lerp_u16(dx, (float)(b.y & 0xffffu), (float)(b.y >> 16));
+        return lerp_u16(dz, lerp_u16(dy, q00, q10), lerp_u16(dy, q01, q11));
+    }
     const float d00 = lerp_u16(dx, voxel(P, vx, vy, vz), voxel(P, vx + 1, vy, vz));
     const float d10 = lerp_u16(dx, voxel(P, vx, vy + 1, vz), voxel(P, vx + 1, vy + 1, vz));
     const float d01 = lerp_u16(dx, voxel(P, vx, vy, vz + 1), voxel(P, vx + 1, vy, vz + 1));

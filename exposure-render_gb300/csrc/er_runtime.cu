@@ -160,6 +160,7 @@ struct VolumeItem {
     uint16_t vmax = 0;
     uint64_t signature = 0;        /* sampled content hash (tuning cache key) */
     DevBuf<uint16_t> vox;
+    DevBuf<uint2> quad;            /* corner quads (NULL when they do not fit in memory) */
     DevBuf<unsigned int> gm_max_bits;
     float gm_max = -1.0f;          /* lazily computed maximum gradient magnitude */
 };
@@ -340,6 +341,7 @@ void volume_geometry(const VolumeItem& v, erd::Params& P)
     }
     P.min_step = smin_h(sp[0], smin_h(sp[1], sp[2]));
     P.vox = v.vox.p;
+    P.quad = v.quad.p;
 }
 
 /* Camera::Update - Source/camera.h:61-96 */
@@ -968,6 +970,14 @@ ER_API er_status er_bind_volume(const er_volume_desc* d, int32_t* id)
     v->signature = sig;
     ER_CUDA(v->vox.ensure(n));
     ER_CUDA(cudaMemcpy(v->vox.p, d->voxels, n * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    /* corner quads for the transport's lookups; without room for them the
+       kernels read the plain voxels (same values, more loads) */
+    if (v->quad.ensure(n) == cudaSuccess) {
+        ER_CUDA(er_launch_quads(v->vox.p, v->res, v->quad.p, 0));
+        ER_CUDA(cudaDeviceSynchronize());
+    } else {
+        cudaGetLastError();
+    }
     C.volumes.items[*id] = std::move(v);
     C.version++;
     return ER_OK;

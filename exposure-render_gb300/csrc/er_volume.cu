@@ -101,6 +101,29 @@ cudaError_t er_launch_majorant(const uint16_t* vox, const int res[3], int B, con
     return cudaGetLastError();
 }
 
+/* corner quads: for voxel (x, y, z) the intensities at (x, y), (x+1, y),
+   (x, y+1), (x+1, y+1) of slice z, packed as two uint16 pairs, so that a
+   trilinear lookup reads two 8-byte words instead of eight 2-byte ones */
+__global__ void k_quads(const uint16_t* __restrict__ vox, int rx, int ry, int rz, uint2* __restrict__ quad)
+{
+    const size_t n = (size_t)rx * ry * rz;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int x = (int)(i % rx), y = (int)((i / rx) % ry);
+        const size_t z0 = i - (size_t)y * rx - x;
+        const int x1 = x + 1 < rx ? x + 1 : rx - 1, y1 = y + 1 < ry ? y + 1 : ry - 1;
+        const uint32_t v00 = vox[z0 + (size_t)y * rx + x], v10 = vox[z0 + (size_t)y * rx + x1];
+        const uint32_t v01 = vox[z0 + (size_t)y1 * rx + x], v11 = vox[z0 + (size_t)y1 * rx + x1];
+        quad[i] = make_uint2(v00 | (v10 << 16), v01 | (v11 << 16));
+    }
+}
+
+cudaError_t er_launch_quads(const uint16_t* vox, const int res[3], uint2* quad, cudaStream_t s)
+{
+    k_quads<<<2048, 256, 0, s>>>(vox, res[0], res[1], res[2], quad);
+    return cudaGetLastError();
+}
+
 /* ====================================================================== */
 /* Allocation-free majorant build                                           */
 /* ====================================================================== */
