@@ -1377,7 +1377,7 @@ ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tun
         r.msamples_per_s = -1.0f;
         /* majorant brick first (the dominant term for delta tracking), then
            the occupancy variants at the best brick */
-        const int bricks[] = {2, 4, 8, 16};
+        const int bricks[] = {1, 2, 4, 8, 16};
         for (int b : bricks) {
             if (!delta && b != r.majorant_brick) continue;
             s.majorant_brick = b;

@@ -453,7 +453,7 @@ typedef struct er_tune_result {
 } er_tune_result;
 
 /* Times probe renders of a bound tracer (probe_spp samples per pixel of its
-   film, one warm-up each) over majorant bricks {2, 4, 8, 16} (delta
+   film, one warm-up each) over majorant bricks {1, 2, 4, 8, 16} (delta
    tracking only) and then the occupancy variants of the wavefront stages,
    and writes the fastest configuration into the bound tracer's settings (the
    caller's descriptor is not changed; re-binding it restores its values),

@@ -51,10 +51,10 @@ def test_autotune_delta_sweep_and_cache(torch, lib, runtime, oracle, cache):
     r = runtime.Renderer(sc, lib)
     try:
         first = r.autotune(2)
-        assert first["majorant_brick"] in (2, 4, 8, 16)
+        assert first["majorant_brick"] in (1, 2, 4, 8, 16)
         assert first["tune_primary"] in (2, 3, 4, 6, 8) and first["tune_shadow"] in (2, 3, 4, 6, 8)
         assert first["tune_shade"] in (2, 3, 4, 6)
-        assert first["candidates"] == 4 + 8 + 4 and not first["from_cache"] and first["msamples_per_s"] > 0
+        assert first["candidates"] == 5 + 8 + 4 and not first["from_cache"] and first["msamples_per_s"] > 0
         assert cache.exists() and len(cache.read_text().splitlines()) == 1
         again = r.autotune(2)
         assert again["from_cache"] and again["candidates"] == 0
