@@ -229,11 +229,7 @@ EXPOSURE_RENDER_DLL void GetEstimate(int TracerID, unsigned char* pData) { raise
 
 EXPOSURE_RENDER_DLL void GetAutoFocusDistance(int TracerID, int FilmU, int FilmV, float& AutoFocusDistance)
 {
-    const er_status st = er_get_auto_focus_distance(TracerID, FilmU, FilmV, &AutoFocusDistance);
-    /* the reference's entry point is a stub that leaves the output untouched
-       (Source/core.cu:145-148); only a missing tracer is an error here */
-    if (st == ER_ERR_UNSUPPORTED) return;
-    raise(st);
+    raise(er_get_auto_focus_distance(TracerID, FilmU, FilmV, &AutoFocusDistance));
 }
 
 EXPOSURE_RENDER_DLL void GetNoIterations(int TracerID, int& NoIterations)

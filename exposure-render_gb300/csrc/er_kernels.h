@@ -23,6 +23,8 @@ struct BilateralTables {
 cudaError_t er_launch_trace_frame(const erd::Params& P, uint32_t* lanes, float4* frame, cudaStream_t s);
 cudaError_t er_launch_trace_sum(const erd::Params& P, int spp, uint32_t view, uint32_t first, float4* sum, int accumulate,
                                 cudaStream_t s);
+/* the autofocus distance of film pixel (u, v) into out (one float) */
+cudaError_t er_launch_autofocus(const erd::Params& P, int u, int v, uint32_t lane0, uint32_t lane1, float* out, cudaStream_t s);
 cudaError_t er_launch_sigma_table(const erd::Plf* opacity, float density_scale, float* table, int n, cudaStream_t s);
 
 cudaError_t er_launch_post_frame(const float4* frame, float4* running, uchar4* rgba, int W, int H, int n_iter, float exposure,

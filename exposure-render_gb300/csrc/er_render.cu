@@ -61,6 +61,49 @@ __global__ void k_sigma_table(const Plf* __restrict__ opacity, float density_sca
 
 /* ---- launchers ---- */
 
+/* KrnlComputeAutoFocusDistance (Source/autofocus.cuh:26-62, one thread):
+   100 rays through the screen point of film pixel (u, v), each moved by
+   0.01 x ConcentricSampleDisk(Get2()), traced by the fixed-step march; the
+   mean camera-to-event distance.  The event is not reset between rays (a
+   miss after a hit counts the previous hit again); without any hit the
+   result is the distance from the camera to the origin. */
+__global__ void k_autofocus(const Params P, int u, int v, uint32_t lane0, uint32_t lane1, float* out)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    Rng rng;
+    rng.s0 = lane0;
+    rng.s1 = lane1;
+    Event SE;
+    SE.type = 0; SE.valid = false; SE.T = 0.0f; SE.Le = C3(0, 0, 0);
+    SE.P = V3(0, 0, 0); SE.N = V3(0, 0, 0); SE.Wo = V3(0, 0, 0);
+    Ray Rc;
+    Rc.O = vload(P.pos); Rc.D = vload(P.N); Rc.MinT = P.clip_near; Rc.MaxT = P.clip_far;
+    float Sum = 0.0f, SumWeight = 0.0f;
+    for (int i = 0; i < 100; i++) {
+        float sp0 = P.screen00 + (P.inv_screen0 * (float)u);
+        float sp1 = P.screen10 + (P.inv_screen1 * (float)v);
+        const v2 d = concentric_sample_disk(rng.get2());
+        sp0 += 0.01f * d.x;
+        sp1 += 0.01f * d.y;
+        Rc.O = vload(P.pos);
+        Rc.D = vnorm(vsub(vadd(vload(P.N), vscale(vload(P.U), sp0)), vscale(vload(P.V), sp1)));
+        Rc.MinT = P.clip_near;
+        Rc.MaxT = P.clip_far;
+        sample_volume<false>(P, Rc, rng, SE);
+        if (SE.valid) {
+            Sum += vlen(vsub(SE.P, Rc.O));
+            SumWeight += 1.0f;
+        }
+    }
+    *out = Sum <= 0.0f ? vlen(vsub(SE.P, Rc.O)) : Sum / SumWeight;
+}
+
+cudaError_t er_launch_autofocus(const Params& P, int u, int v, uint32_t lane0, uint32_t lane1, float* out, cudaStream_t s)
+{
+    k_autofocus<<<1, 32, 0, s>>>(P, u, v, lane0, lane1, out);
+    return cudaGetLastError();
+}
+
 cudaError_t er_launch_trace_frame(const Params& P, uint32_t* lanes, float4* frame, cudaStream_t s)
 {
     const dim3 b(16, 8);

@@ -188,6 +188,7 @@ struct TracerItem {
     DevBuf<float> majorant, rmq;
     DevBuf<uint32_t> minmax;
     DevBuf<int> err;
+    DevBuf<float> autofocus;       /* er_get_auto_focus_distance's result */
     WfQueues wf;
     DevBuf<float4> tune_sum;       /* probe renders of the autotuner */
     erd::Params P;
@@ -1233,11 +1234,23 @@ ER_API er_status er_get_no_iterations(int32_t tracer_id, int32_t* no_iterations)
 ER_API er_status er_get_auto_focus_distance(int32_t tracer_id, int32_t film_u, int32_t film_v, float* distance)
 {
     ER_LOCK;
-    (void)film_u;
-    (void)film_v;
-    (void)distance;
-    if (!find_tracer(tracer_id)) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
-    return fail(ER_ERR_UNSUPPORTED, "auto focus is not available in this build");
+    TracerItem* t = find_tracer(tracer_id);
+    if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
+    if (!distance) return fail(ER_ERR_INVALID_ARGUMENT, "output pointer is NULL");
+    er_status st = build(*t);
+    if (st != ER_OK) return st;
+    if (film_u < 0 || film_v < 0 || film_u >= t->W || film_v >= t->H)
+        return fail(ER_ERR_INVALID_ARGUMENT, "film position (%d, %d) outside the %d x %d film", film_u, film_v, t->W, t->H);
+    /* the reference seeds its one-thread kernel with rand(); here the lanes
+       come from the tracer's seed and the pixel (view ER_AUTOFOCUS_VIEW) */
+    uint32_t l0 = 0, l1 = 0;
+    er_seed_lanes(t->d.settings.seed, ER_AUTOFOCUS_VIEW, (uint32_t)film_v * (uint32_t)t->W + (uint32_t)film_u, 0u, &l0, &l1);
+    ER_CUDA(t->autofocus.ensure(1));
+    cudaStream_t s = ctx().stream;
+    ER_CUDA(er_launch_autofocus(t->P, film_u, film_v, l0, l1, t->autofocus.p, s));
+    ER_CUDA(cudaMemcpyAsync(distance, t->autofocus.p, sizeof(float), cudaMemcpyDeviceToHost, s));
+    ER_CUDA(cudaStreamSynchronize(s));
+    return check_device_error(*t);
 }
 
 /* ---- device-pointer entry points ---- */

@@ -306,7 +306,13 @@ ER_API er_status er_render_estimate(int32_t tracer_id);
    settings enable the bilateral filter). */
 ER_API er_status er_get_estimate(int32_t tracer_id, uint8_t* rgba);
 /* GetAutoFocusDistance - Source/exposurerender.h:41 (a stub at
-   Source/core.cu:145-148; the kernel design is Source/autofocus.cuh:26-63). */
+   Source/core.cu:145-148) computed as Source/autofocus.cuh:26-62 designs it:
+   the mean distance from the camera to the fixed-step march's scatter event
+   over 100 rays jittered around the screen point of film pixel
+   (film_u, film_v).  Its random lanes are er_seed_lanes(seed,
+   ER_AUTOFOCUS_VIEW, film_v * W + film_u, 0) with the tracer's seed (the
+   reference draws rand()).  Synchronous. */
+#define ER_AUTOFOCUS_VIEW 0x41F0C05Eu
 ER_API er_status er_get_auto_focus_distance(int32_t tracer_id, int32_t film_u, int32_t film_v, float* distance);
 /* GetNoIterations - Source/exposurerender.h:42 (a stub at Source/core.cu:150-153) */
 ER_API er_status er_get_no_iterations(int32_t tracer_id, int32_t* no_iterations);

@@ -1575,6 +1575,44 @@ static void single_scattering(or_scene* s, int x, int y, rng_t* rng, float out[4
     out[3] = SE.valid ? 1.0f : 0.0f;
 }
 
+/* KrnlComputeAutoFocusDistance - Source/autofocus.cuh:26-62: 100 rays
+   through the screen point of film pixel (u, v) (no film jitter), each
+   moved by 0.01 x ConcentricSampleDisk(Get2()), pinhole, traced by the
+   fixed-step march; the mean distance from the camera to the scatter
+   event.  The event is not reset between rays, so after the first hit a
+   ray that misses adds the previous hit's distance again; with no hit at
+   all the result is the distance from the camera to the origin (the
+   invalid event's P). */
+float ER_OR(autofocus)(or_scene* s, int32_t u, int32_t v, uint32_t lane0, uint32_t lane1)
+{
+    rng_t rng;
+    rng.s0 = lane0;
+    rng.s1 = lane1;
+    scatter_event SE;
+    se_invalid(&SE, 0);
+    ray_t Rc;
+    Rc.O = s->pos; Rc.D = s->N; Rc.MinT = s->clip_near; Rc.MaxT = s->clip_far;
+    float Sum = 0.0f, SumWeight = 0.0f;
+    for (int i = 0; i < 100; i++) {
+        float sp0 = s->screen[0][0] + (s->inv_screen[0] * (float)u);
+        float sp1 = s->screen[1][0] + (s->inv_screen[1] * (float)v);
+        const v2 d = concentric_sample_disk(rng_get2(&rng));
+        sp0 += 0.01f * d.x;
+        sp1 += 0.01f * d.y;
+        Rc.O = s->pos;
+        Rc.D = vnorm(vsub(vadd(s->N, vscale(s->U, sp0)), vscale(s->V, sp1)));
+        Rc.MinT = s->clip_near;
+        Rc.MaxT = s->clip_far;
+        sample_volume(s, Rc, &rng, &SE);
+        if (SE.valid) {
+            Sum += vlen(vsub(SE.P, Rc.O));
+            SumWeight += 1.0f;
+        }
+    }
+    if (Sum <= 0.0f) return vlen(vsub(SE.P, Rc.O));
+    return Sum / SumWeight;
+}
+
 /* ------------------------------------------------------------------ */
 /* threaded drivers                                                     */
 /* ------------------------------------------------------------------ */

@@ -62,6 +62,10 @@ void ER_OR(render_sum)(or_scene* scene, int32_t spp, uint32_t view, uint32_t fir
 void ER_OR(render_moments)(or_scene* scene, int32_t spp, uint32_t view, uint32_t first_sample,
                            int32_t x0, int32_t y0, int32_t w, int32_t h, float* sum, float* sum2, int32_t nthreads);
 
+/* KrnlComputeAutoFocusDistance (Source/autofocus.cuh:26-62) for film
+   pixel (u, v) with RNG lanes (lane0, lane1) */
+float ER_OR(autofocus)(or_scene* scene, int32_t u, int32_t v, uint32_t lane0, uint32_t lane1);
+
 /* Work counters per sample of the last render_frame / render_sum /
    render_moments, in the order of the OR_STAT_* indices: volume lookups
    (GetIntensity calls) in the primary free flight (with the event normal),

@@ -41,6 +41,7 @@ class Oracle:
         f("render_frame", None, [c_void_p, c_void_p, c_void_p, c_int32])
         f("render_sum", None, [c_void_p, c_int32, c_uint32, c_uint32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_int32])
         if prefix != "ref_":
+            f("autofocus", c_float if prefix == "or_" else c_double, [c_void_p, c_int32, c_int32, c_uint32, c_uint32])
             f("render_stats", None, [c_void_p])
             f("render_moments", None, [c_void_p, c_int32, c_uint32, c_uint32, c_int32, c_int32, c_int32, c_int32, c_void_p,
                                        c_void_p, c_int32])

@@ -305,3 +305,17 @@ def test_bind_list_semantics_and_errors(torch, lib):
     assert lib.er_render_estimate(r.tracer_id) == 6                             # objects unsupported
     r.close()
     lib.er_reset()
+
+
+@pytest.mark.parametrize("uv", [(24, 20), (0, 0), (47, 39), (10, 30)])
+def test_autofocus_bits_equal_oracle(torch, lib, tiny, uv):
+    """er_get_auto_focus_distance against the oracle's restatement of
+    KrnlComputeAutoFocusDistance, with the same seed lanes"""
+    sc, r, h = tiny
+    u, v = uv
+    d = ctypes.c_float(0.0)
+    C.check(lib.er_get_auto_focus_distance(r.tracer_id, u, v, ctypes.byref(d)))
+    l0, l1 = OL.seed_lanes(sc.tracer.settings.seed, 0x41F0C05E, v * sc.width + u, 0)
+    ref = h.orc.autofocus(h.h, u, v, l0, l1)
+    assert np.float32(d.value).view(np.uint32) == np.float32(ref).view(np.uint32)
+    assert lib.er_get_auto_focus_distance(r.tracer_id, sc.width, 0, ctypes.byref(d)) == C.ER_ERR_INVALID_ARGUMENT
