@@ -1479,6 +1479,8 @@ ER_API er_status er_medium_majorant(int32_t tracer_id, const er_medium_desc* med
     if (st != ER_OK) return st;
     if (!d_majorant) return fail(ER_ERR_INVALID_ARGUMENT, "d_majorant is NULL");
     if (!(margin >= 1.0f) || !(floor_ >= 0.0f)) return fail(ER_ERR_INVALID_ARGUMENT, "margin must be >= 1 and floor >= 0");
+    if ((long long)P.nb[0] * P.nb[1] * P.nb[2] > (1ll << 26))
+        return fail(ER_ERR_INVALID_ARGUMENT, "%d x %d x %d bricks exceed the majorant build's 2^26", P.nb[0], P.nb[1], P.nb[2]);
     ER_CUDA(er_launch_dm_majorant(M.rho, P.res, P.brick, M.tf, M.tf_n, M.scale, margin, floor_, d_majorant, (cudaStream_t)stream));
     return ER_OK;
 }

@@ -26,11 +26,12 @@
 __global__ void k_brick_minmax(const uint16_t* __restrict__ vox, int rx, int ry, int rz, int B, int nbx, int nby, int nbz,
                                uint32_t* __restrict__ minmax)
 {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    const int total = nbx * nby * nbz;
-    if (warp >= total) return;
-    const int bx = warp % nbx, by = (warp / nbx) % nby, bz = warp / (nbx * nby);
+    const long long total = (long long)nbx * nby * nbz;
+    const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+    /* one warp per brick, grid-stride over the bricks (2^27 at 1^3 bricks of 512^3) */
+    for (long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < total; warp += nwarps) {
+    const int bx = (int)(warp % nbx), by = (int)((warp / nbx) % nby), bz = (int)(warp / ((long long)nbx * nby));
     int x0 = bx * B - 1, x1 = (bx + 1) * B + 1;
     int y0 = by * B - 1, y1 = (by + 1) * B + 1;
     int z0 = bz * B - 1, z1 = (bz + 1) * B + 1;
@@ -57,6 +58,7 @@ __global__ void k_brick_minmax(const uint16_t* __restrict__ vox, int rx, int ry,
         hi = b > hi ? b : hi;
     }
     if (lane == 0) minmax[warp] = lo | (hi << 16);
+    }
 }
 
 __global__ void k_rmq_level(const float* __restrict__ prev, float* __restrict__ next, int n, int half)
@@ -69,9 +71,9 @@ __global__ void k_rmq_level(const float* __restrict__ prev, float* __restrict__ 
 }
 
 __global__ void k_majorant(const uint32_t* __restrict__ minmax, const float* __restrict__ table, int n, int levels, float ds,
-                           float* __restrict__ majorant, int total)
+                           float* __restrict__ majorant, long long total)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= total) return;
     const uint32_t mm = minmax[i];
     int lo = (int)(mm & 0xffffu), hi = (int)(mm >> 16);
@@ -91,13 +93,15 @@ __global__ void k_majorant(const uint32_t* __restrict__ minmax, const float* __r
 cudaError_t er_launch_majorant(const uint16_t* vox, const int res[3], int B, const int nb[3], const float* sigma, int n,
                                float* rmq, int levels, uint32_t* minmax, float density_scale, float* majorant, cudaStream_t s)
 {
-    const int total = nb[0] * nb[1] * nb[2];
-    k_brick_minmax<<<(total * 32 + 255) / 256, 256, 0, s>>>(vox, res[0], res[1], res[2], B, nb[0], nb[1], nb[2], minmax);
+    const long long total = (long long)nb[0] * nb[1] * nb[2];
+    const long long want = (total * 32 + 255) / 256;
+    k_brick_minmax<<<(unsigned)(want < 65536 ? want : 65536), 256, 0, s>>>(vox, res[0], res[1], res[2], B, nb[0], nb[1], nb[2],
+                                                                           minmax);
     cudaError_t e = cudaMemcpyAsync(rmq, sigma, (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return e;
     for (int k = 1; k < levels; k++)
         k_rmq_level<<<(n + 255) / 256, 256, 0, s>>>(rmq + (size_t)(k - 1) * n, rmq + (size_t)k * n, n, 1 << (k - 1));
-    k_majorant<<<(total + 255) / 256, 256, 0, s>>>(minmax, rmq, n, levels, density_scale, majorant, total);
+    k_majorant<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(minmax, rmq, n, levels, density_scale, majorant, total);
     return cudaGetLastError();
 }
 
