@@ -1396,10 +1396,17 @@ ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tun
             s.majorant_brick = b;
             float m = 0.0f;
             st = time_probe(*t, probe_spp, &m);
-            if (st != ER_OK) { s = saved; t->built = false; return st; }
+            if (st != ER_OK) {
+                /* a brick size whose grid does not fit (memory, launch limits) is
+                   skipped; a fault that poisons the context ends the sweep */
+                if (cudaDeviceSynchronize() != cudaSuccess) { s = saved; t->built = false; return st; }
+                cudaGetLastError();
+                continue;
+            }
             r.candidates++;
             if (m > r.msamples_per_s) { r.msamples_per_s = m; r.majorant_brick = b; }
         }
+        if (r.msamples_per_s < 0.0f) { s = saved; t->built = false; return fail(ER_ERR_CUDA, "no majorant brick size could be timed"); }
         s.majorant_brick = r.majorant_brick;
         if (wavefront) {
             const int variants[][2] = {{4, 4}, {3, 3}, {3, 4}, {4, 3}, {6, 4}, {4, 6}, {2, 3}, {8, 8}};
