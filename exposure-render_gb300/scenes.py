@@ -36,6 +36,7 @@ class Scene:
     lights: list = field(default_factory=list)      # er_light_desc, light i has ID i
     textures: list = field(default_factory=list)    # er_texture_desc, texture i has ID i
     spp: int = 1
+    objects: list = field(default_factory=list)     # er_object_desc, object i has ID i
 
     @property
     def width(self) -> int:
@@ -433,3 +434,45 @@ def medium_scene(res=(128, 128, 128), film=(256, 256), seed=40) -> Scene:
     lights, textures = c1_lights()
     t = c1_tracer(film)
     return Scene("medium", np.zeros(res, dtype=np.uint16), tracer=t, lights=lights, textures=textures, spp=32)
+
+
+# ---------------------------------------------------------------------------
+# surface objects (SampleRay's third event type)
+# ---------------------------------------------------------------------------
+
+def checker_texture(c1, c2, level=1.0, repeat=(1.0, 1.0)) -> C.er_texture_desc:
+    t = C.new_texture_desc()
+    t.procedural.type = C.PROCEDURAL_CHECKER
+    for i in range(3):
+        t.procedural.checker_color1[i] = c1[i]
+        t.procedural.checker_color2[i] = c2[i]
+    t.output_level = level
+    t.repeat[0], t.repeat[1] = repeat
+    return t
+
+
+def make_object(shape, diffuse=-1, specular=-1, glossiness=-1, ior=5.0) -> C.er_object_desc:
+    o = C.er_object_desc()
+    o.shape = shape
+    o.diffuse_texture_id = diffuse
+    o.specular_texture_id = specular
+    o.glossiness_texture_id = glossiness
+    o.ior = ior
+    return o
+
+
+def scene_objects(res=32, film=(48, 40), spp=4, seed=3) -> Scene:
+    """The tiny blob scene on a textured floor plane with a sphere beside it:
+    volume, light and object events in one image, objects shadowing the
+    volume and the volume shadowing the floor."""
+    vol = blob_volume((res, res, res), n_blobs=6, seed=seed)
+    lights, textures = c1_lights()
+    textures = textures + [uniform_texture((0.7, 0.5, 0.3)), checker_texture((0.3, 0.3, 0.3), (0.05, 0.05, 0.05), repeat=(4.0, 4.0)),
+                           uniform_texture((0.6, 0.6, 0.6))]
+    floor = make_shape(C.SHAPE_PLANE, look_at_tm((0.0, 0.0, -0.6), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0)), size=(3.0, 3.0, 0.0))
+    ball = make_shape(C.SHAPE_SPHERE, look_at_tm((0.55, -0.1, 0.25), (0.55, -0.1, 1.25), (0.0, 1.0, 0.0)), outer=0.2)
+    objects = [make_object(floor, 1, 2, 3), make_object(ball, 1, 1, 3)]
+    t = c1_tracer(film)
+    t.object_count = 2
+    t.object_ids[0], t.object_ids[1] = 0, 1
+    return Scene("objects", vol, tracer=t, lights=lights, textures=textures, spp=spp, objects=objects)

@@ -139,6 +139,12 @@ struct or_scene {
     or_light* lights;
     int n_textures;
     er_texture_desc* textures;
+    /* surface objects: the tracer's ObjectIDs.Count and the bound objects in
+       device-array order (IntersectObjects indexes gpObjects[i] by the loop
+       index, Source/objects.h:52) */
+    int object_count;
+    int n_objects;
+    er_object_desc* objects;
     /* statistics */
     uint64_t lookups;
     uint64_t stat[OR_NSTATS];   /* work counters of the last render (render_stats) */
@@ -239,6 +245,7 @@ or_scene* ER_OR(scene_create)(const er_tracer_desc* t, const er_volume_desc* vol
     s->specular = t->specular;
     s->emission = t->emission;
     s->light_count = t->light_count;
+    s->object_count = t->object_count > 0 ? t->object_count : 0;
     for (int i = 0; i < ER_MAX_INDICES; i++) s->light_idx[i] = t->light_ids[i];
 
     s->n_lights = n_lights;
@@ -259,6 +266,7 @@ void ER_OR(scene_destroy)(or_scene* s)
     if (!s) return;
     free(s->lights);
     free(s->textures);
+    free(s->objects);
     free(s->sigma);
     free(s->majorant);
     free(s);
@@ -939,13 +947,14 @@ typedef struct {                          /* Source/scatterevent.h:31-151 */
     col3 Le;
     v2 UV;
     int light_id;
+    int object_id;
 } scatter_event;
 
 static inline void se_invalid(scatter_event* se, int type)
 {
     se->type = type; se->valid = 0; se->T = 0.0f;
     se->P = V3(0, 0, 0); se->N = V3(0, 0, 0); se->Wo = V3(0, 0, 0);
-    se->Le = C3(0, 0, 0); se->UV.x = 0.0f; se->UV.y = 0.0f; se->light_id = -1;
+    se->Le = C3(0, 0, 0); se->UV.x = 0.0f; se->UV.y = 0.0f; se->light_id = -1; se->object_id = -1;
 }
 
 /* SampleVolume - Source/raymarching.h:30-71 */
@@ -1053,6 +1062,55 @@ static int intersects_light(const or_scene* s, const ray_t* R)
         if (Int.valid) return 1;
     }
     return 0;
+}
+
+/* IntersectObject / IntersectObjects - Source/objects.h:26-62: the nearest
+   of the tracer's first ObjectIDs.Count bound objects (array order) */
+static void intersect_objects(const or_scene* s, const ray_t* R, scatter_event* RS)
+{
+    float T = FLT_MAX;
+    for (int i = 0; i < s->object_count && i < s->n_objects; i++) {
+        const er_shape* sh = &s->objects[i].shape;
+        scatter_event local; se_invalid(&local, 2);
+        local.object_id = i;
+        const ray_t Rt = xform_ray(sh->inv_tm, R);
+        isect_t Int; isect_invalid(&Int);
+        intersect_shape(sh, &Rt, &Int);
+        if (Int.valid) {
+            local.valid = 1;
+            local.N = xform_vector(sh->tm, Int.N);
+            local.P = xform_point(sh->tm, Int.P);
+            local.T = vlen(vsub(local.P, R->O));
+            local.Wo = vneg(R->D);
+            local.Le = C3(0, 0, 0);
+            local.UV = Int.UV;
+        }
+        if (local.valid && local.T < T) { *RS = local; T = local.T; }
+    }
+}
+
+/* IntersectsObject - Source/objects.h:64-80 */
+static int intersects_object(const or_scene* s, const ray_t* R)
+{
+    for (int i = 0; i < s->object_count && i < s->n_objects; i++) {
+        const er_shape* sh = &s->objects[i].shape;
+        const ray_t Rt = xform_ray(sh->inv_tm, R);
+        isect_t Int; isect_invalid(&Int);
+        intersect_shape(sh, &Rt, &Int);
+        if (Int.valid) return 1;
+    }
+    return 0;
+}
+
+void ER_OR(scene_set_objects)(or_scene* s, const er_object_desc* objects, int32_t n)
+{
+    free(s->objects);
+    s->objects = NULL;
+    s->n_objects = n > 0 ? n : 0;
+    if (s->n_objects) {
+        s->objects = (er_object_desc*)malloc(sizeof(er_object_desc) * (size_t)n);
+        memcpy(s->objects, objects, sizeof(er_object_desc) * (size_t)n);
+    }
 }
 
 /* ------------------------------------------------------------------ */
@@ -1244,6 +1302,7 @@ static float visibility_segment(or_scene* s, v3 P1, v3 P2, rng_t* rng)
     R.MinT = 0.0f;
     R.MaxT = smin(vlen(vsub(P2, P1)) - 2.0f * RAY_EPS, s->st.max_shadow_distance);
     if (intersects_light(s, &R)) return 0.0f;
+    if (intersects_object(s, &R)) return 0.0f;
     if (s->st.free_flight == ER_FREE_FLIGHT_DELTA) return transmittance_ratio(s, R, rng);
     return scatter_event_in_volume(s, R, rng) ? 0.0f : 1.0f;
 }
@@ -1418,10 +1477,24 @@ static col3 uniform_sample_one_light(or_scene* s, scatter_event* SE, rng_t* rng,
     if (light_id >= s->n_lights) return Ld;
     const or_light* L = &s->lights[light_id];
     shader_t sh;
-    const float vol_ior = s->st.volume_ior > 0.0f ? s->st.volume_ior : 15.0f;
-    const int type = s->st.apply_shading_type ? select_shader_type(s, SE, I, rng) : 0;
-    shader_init(&sh, type, SE->N, SE->Wo, ctf_eval(&s->diffuse, I), ctf_eval(&s->specular, I), vol_ior,
-                glossiness_exponent(plf_eval(&s->glossiness, I)));
+    if (SE->type == 2) {
+        /* Source/transport.h:141-149: the object's textures at the hit, IOR 15,
+           exponent from the glossiness texture's luminance */
+        const er_object_desc* o = &s->objects[SE->object_id];
+        const col3 Kd = evaluate_texture(s, o->diffuse_texture_id, SE->UV);
+        const col3 Ks = evaluate_texture(s, o->specular_texture_id, SE->UV);
+        const col3 G = evaluate_texture(s, o->glossiness_texture_id, SE->UV);
+        float Y = 0.0f;
+        Y += 0.212671f * G.c[0];
+        Y += 0.715160f * G.c[1];
+        Y += 0.072169f * G.c[2];
+        shader_init(&sh, 0, SE->N, SE->Wo, Kd, Ks, 15.0f, glossiness_exponent(Y));
+    } else {
+        const float vol_ior = s->st.volume_ior > 0.0f ? s->st.volume_ior : 15.0f;
+        const int type = s->st.apply_shading_type ? select_shader_type(s, SE, I, rng) : 0;
+        shader_init(&sh, type, SE->N, SE->Wo, ctf_eval(&s->diffuse, I), ctf_eval(&s->specular, I), vol_ior,
+                    glossiness_exponent(plf_eval(&s->glossiness, I)));
+    }
     Ld = cadd(Ld, estimate_direct_light(s, L, idx, ms, SE, rng, &sh));
     return cscale(Ld, (float)s->light_count);
 }
@@ -1539,18 +1612,20 @@ static ray_t sample_camera(const or_scene* s, int u, int v, v2 film_uv, v2 lens_
     return R;
 }
 
-/* SampleRay - Source/singlescattering.h:52-74 (no surface objects) */
+/* SampleRay - Source/singlescattering.h:52-74: volume, light and object events, nearest wins */
 static void sample_ray(or_scene* s, ray_t R, rng_t* rng, scatter_event* nearest)
 {
-    scatter_event se[2];
+    scatter_event se[3];
     se_invalid(&se[0], 0);
     se_invalid(&se[1], 1);
+    se_invalid(&se[2], 2);
     if (s->st.free_flight == ER_FREE_FLIGHT_DELTA) sample_volume_delta(s, R, rng, &se[0]);
     else sample_volume(s, R, rng, &se[0]);
     intersect_lights(s, &R, &se[1], 1);
+    intersect_objects(s, &R, &se[2]);
     float T = FLT_MAX;
     se_invalid(nearest, 0);
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < 3; i++) {
         if (se[i].valid && se[i].T < T) { *nearest = se[i]; T = se[i].T; }
     }
 }
@@ -1569,6 +1644,7 @@ static void single_scattering(or_scene* s, int x, int y, rng_t* rng, float out[4
     if (SE.valid && SE.type == 0) s->stat[OR_STAT_EVENTS]++;
     if (SE.valid && SE.type == 0) Lv = cadd(Lv, uniform_sample_one_light(s, &SE, rng, &ms));
     if (SE.valid && SE.type == 1) Lv = cadd(Lv, SE.Le);
+    if (SE.valid && SE.type == 2) Lv = cadd(Lv, uniform_sample_one_light(s, &SE, rng, &ms));
     out[0] = Lv.c[0];
     out[1] = Lv.c[1];
     out[2] = Lv.c[2];

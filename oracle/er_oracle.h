@@ -46,6 +46,9 @@ or_scene* ER_OR(scene_create)(const er_tracer_desc* tracer, const er_volume_desc
                               const er_light_desc* lights, int32_t n_lights,
                               const er_texture_desc* textures, int32_t n_textures);
 void ER_OR(scene_destroy)(or_scene* scene);
+/* BindObject for the scene: object i of `objects` is the i-th bound object
+   (gpObjects[i]); the tracer's object_count says how many are intersected */
+void ER_OR(scene_set_objects)(or_scene* scene, const er_object_desc* objects, int32_t n);
 
 /* KrnlSingleScattering over the whole film with stateful lanes
    (lanes[0..W*H) = RandomSeeds1, lanes[W*H..2W*H) = RandomSeeds2, advanced in

@@ -60,11 +60,14 @@ ExposureRender::Bitmap* gpBitmaps = NULL;
 
 using namespace ExposureRender;
 
+#define MAX_NO_INDICES_HARNESS 256
+
 struct or_scene {
     ErVolume* ervolume;
     Volume* volume;
     std::vector<Light> lights;
     std::vector<Texture> textures;
+    std::vector<Object> objects;
     Tracer* tracer;
     int W, H;
     uint32_t seed;
@@ -170,7 +173,8 @@ extern "C" or_scene* ref_scene_create(const er_tracer_desc* t, const er_volume_d
     et.VolumeID = 0;
     for (int i = 0; i < t->light_count; i++) et.LightIDs[i] = t->light_ids[i];
     et.LightIDs.Count = t->light_count;
-    et.ObjectIDs.Count = 0;
+    for (int i = 0; i < t->object_count && i < MAX_NO_INDICES_HARNESS; i++) et.ObjectIDs[i] = t->object_ids[i];
+    et.ObjectIDs.Count = t->object_count;
     et.ClippingObjectIDs.Count = 0;
 
     s->tracer = new Tracer();
@@ -194,7 +198,7 @@ extern "C" or_scene* ref_scene_create(const er_tracer_desc* t, const er_volume_d
     gpVolumes = s->volume;
     gpLights = s->lights.empty() ? NULL : &s->lights[0];
     gpTextures = s->textures.empty() ? NULL : &s->textures[0];
-    gpObjects = NULL;
+    gpObjects = s->objects.empty() ? NULL : &s->objects[0];
     gpClippingObjects = NULL;
     gpBitmaps = NULL;
     return s;
@@ -218,6 +222,23 @@ static void bind_scene(or_scene* s)
     gpVolumes = s->volume;
     gpLights = s->lights.empty() ? NULL : &s->lights[0];
     gpTextures = s->textures.empty() ? NULL : &s->textures[0];
+    gpObjects = s->objects.empty() ? NULL : &s->objects[0];
+}
+
+/* BindObject: object i is the i-th entry of gpObjects */
+extern "C" void ref_scene_set_objects(or_scene* s, const er_object_desc* objects, int32_t n)
+{
+    s->objects.clear();
+    for (int i = 0; i < n; i++) {
+        ErObject eo;
+        set_shape(eo.Shape, objects[i].shape);
+        eo.DiffuseTextureID = objects[i].diffuse_texture_id;
+        eo.SpecularTextureID = objects[i].specular_texture_id;
+        eo.GlossinessTextureID = objects[i].glossiness_texture_id;
+        eo.Ior = objects[i].ior;
+        s->objects.push_back(Object(eo));
+    }
+    bind_scene(s);
 }
 
 /* one KERNEL_2D "thread" for pixel (x, y) with a 16x8 block, as the launch of

@@ -38,6 +38,7 @@ class Oracle:
         f = self.fn
         f("scene_create", c_void_p, [POINTER(C.er_tracer_desc), POINTER(C.er_volume_desc), c_void_p, c_int32, c_void_p, c_int32])
         f("scene_destroy", None, [c_void_p])
+        f("scene_set_objects", None, [c_void_p, c_void_p, c_int32])
         f("render_frame", None, [c_void_p, c_void_p, c_void_p, c_int32])
         f("render_sum", None, [c_void_p, c_int32, c_uint32, c_uint32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_int32])
         if prefix != "ref_":
@@ -112,6 +113,10 @@ class SceneHandle:
         self.ta = scene.texture_array()
         self.h = orc.scene_create(ctypes.byref(scene.tracer), ctypes.byref(self.vd), ctypes.cast(self.la, c_void_p),
                                   len(scene.lights), ctypes.cast(self.ta, c_void_p), len(scene.textures))
+        objs = getattr(scene, "objects", [])
+        if objs:
+            self.oa = (C.er_object_desc * len(objs))(*objs)
+            orc.scene_set_objects(self.h, ctypes.cast(self.oa, c_void_p), len(objs))
 
     def close(self):
         if self.h:

@@ -308,10 +308,13 @@ def test_bind_list_semantics_and_errors(torch, lib):
 
 
 @pytest.mark.parametrize("uv", [(24, 20), (0, 0), (47, 39), (10, 30)])
-def test_autofocus_bits_equal_oracle(torch, lib, tiny, uv):
+def test_autofocus_bits_equal_oracle(torch, lib, runtime, oracle, uv):
     """er_get_auto_focus_distance against the oracle's restatement of
-    KrnlComputeAutoFocusDistance, with the same seed lanes"""
-    sc, r, h = tiny
+    KrnlComputeAutoFocusDistance, with the same seed lanes (a scene of its
+    own: the resource tests before it reset the library)"""
+    sc = S.scene_tiny()
+    r = runtime.Renderer(sc, lib)
+    h = OL.SceneHandle(oracle, sc)
     u, v = uv
     d = ctypes.c_float(0.0)
     C.check(lib.er_get_auto_focus_distance(r.tracer_id, u, v, ctypes.byref(d)))
@@ -319,3 +322,5 @@ def test_autofocus_bits_equal_oracle(torch, lib, tiny, uv):
     ref = h.orc.autofocus(h.h, u, v, l0, l1)
     assert np.float32(d.value).view(np.uint32) == np.float32(ref).view(np.uint32)
     assert lib.er_get_auto_focus_distance(r.tracer_id, sc.width, 0, ctypes.byref(d)) == C.ER_ERR_INVALID_ARGUMENT
+    r.close()
+    h.close()

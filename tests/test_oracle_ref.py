@@ -126,3 +126,32 @@ def test_plf_random_unsorted(oracle, ref):
         ref.plf_evaluate(ctypes.byref(plf), len(xs), OL.ptr(xs), OL.ptr(yb))
         assert np.array_equal(bits(ya), bits(yb))
         assert plf.count <= 127
+
+
+def test_surface_objects_sum_and_frames(oracle, ref):
+    """objects (SampleRay's third event type, Source/objects.h) against the
+    reference: textured floor and sphere, shadowed by and shadowing the volume"""
+    sc = S.scene_objects()
+    a, b = OL.SceneHandle(oracle, sc), OL.SceneHandle(ref, sc)
+    sa = a.render_sum(4, nthreads=4)
+    assert np.array_equal(bits(sa), bits(b.render_sum(4, nthreads=4)))
+    la = OL.initial_lanes(21, sc.width, sc.height)
+    lb = la.copy()
+    for _ in range(2):
+        assert np.array_equal(bits(a.render_frame(la, 4)), bits(b.render_frame(lb, 4)))
+    sc.tracer.object_count = 0
+    c = OL.SceneHandle(oracle, sc)
+    assert not np.array_equal(sa, c.render_sum(4, nthreads=4))       # the objects show
+
+
+@pytest.mark.parametrize("shape", ["disk", "ring", "box"])
+def test_surface_object_shapes(oracle, ref, shape):
+    sc = S.scene_objects(res=20, film=(28, 24), seed=8)
+    st = {"disk": C.SHAPE_DISK, "ring": C.SHAPE_RING, "box": C.SHAPE_BOX}[shape]
+    sh = sc.objects[1].shape
+    sh.type = st
+    sh.inner_radius, sh.outer_radius = 0.1, 0.3
+    sh.size[0], sh.size[1], sh.size[2] = 0.4, 0.3, 0.2
+    sc.objects[0].glossiness_texture_id = 2                     # luminance of a checker
+    a, b = OL.SceneHandle(oracle, sc), OL.SceneHandle(ref, sc)
+    assert np.array_equal(bits(a.render_sum(3, nthreads=4)), bits(b.render_sum(3, nthreads=4)))
