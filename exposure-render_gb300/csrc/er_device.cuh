@@ -63,6 +63,15 @@ struct Light {               /* ErLight + Shape (Source/erlight.h, Source/shape.
     int unit;
 };
 
+struct Object {              /* ErObject (Source/erobject.h:27-67) */
+    Light shape;             /* the shape fields of a light record (tm, inv_tm, type, one_sided, size, radii);
+                                the emitter fields are unused */
+    int diffuse_texture_id;
+    int specular_texture_id;
+    int glossiness_texture_id;
+    int pad;
+};
+
 struct Texture {             /* ErTexture + Procedural (Source/ertexture.h, Source/procedural.h) */
     int type;
     float output_level;
@@ -75,6 +84,11 @@ struct Texture {             /* ErTexture + Procedural (Source/ertexture.h, Sour
     float repeat[2];
     int flip[2];
     Plf gradient[3];
+};
+
+struct Bitmap {              /* Bitmap (Source/bitmap.h): RGBA8, row-major */
+    const uchar4* pixels;
+    int res[2];
 };
 
 struct Params {
@@ -116,8 +130,14 @@ struct Params {
     const Light* lights;     /* light_count entries, in LightIDs order; NULL entries are skipped */
     const int* light_valid;  /* 1 where LightIDs[i] named a bound light */
     const int* light_ids;    /* the tracer's LightIDs (slot -> light ID) */
+    /* surface objects: the first ObjectIDs.Count bound objects in bind-list
+       order, as IntersectObjects indexes gpObjects[i] (Source/objects.h:45-62) */
+    int object_count;
+    const Object* objects;
     const Texture* textures;
     int n_textures;
+    const Bitmap* bitmaps;   /* indexed by ErTexture::BitmapID */
+    int n_bitmaps;
     const Tfs* tfs;
     int* err;                /* device error word (bit 0: a march exceeded its step budget) */
 };

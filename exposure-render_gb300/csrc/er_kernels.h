@@ -109,6 +109,8 @@ struct WavefrontBuffers {
     int tune_primary;    /* resident blocks per SM targeted by the primary stage (2, 3, 4, 6, 8) */
     int tune_shadow;     /* same for the shadow stage */
     int tune_shade;      /* resident 128-thread blocks per SM of the shade stage (2, 3, 4, 6) */
+    int objects;         /* 1 when a view has surface objects: the primary and shade stages run their
+                            object-handling variants (at the default occupancy) */
 };
 
 /* cuts the items of views (npix[v] * spp[v] each) into windows of whole

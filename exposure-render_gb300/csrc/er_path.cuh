@@ -435,7 +435,46 @@ ER_D void sample_light_surface(const Light& L, v3 UVW, Surf& SS)
     SS.N = xform_vector(L.tm, SS.N);
 }
 
-/* EvaluateTexture - Source/textures.h:26-111 (procedural textures) */
+/* Buffer2D<ColorRGBAuc>::operator()(Vec2f, Normalized = true)
+   (Source/buffer2d.h:227-254) and ColorXYZf::FromRGBAuc (Source/color.h:195-209).
+   `float * ColorRGBAuc` converts the weight to the unsigned char component
+   type and multiplies per component in unsigned char arithmetic
+   (Source/color.h:282-283, Source/vector.h:183-190), colour sums wrap in
+   unsigned char: the lookup returns the floor texel where the scaled
+   coordinate is an integer and black elsewhere, as the reference does. */
+ER_D uint8_t uc_weight(float w) { return (uint8_t)w; }
+
+ER_COLD c3 bitmap_xyz(const Bitmap& B, v2 uv)
+{
+    const int w = B.res[0], h = B.res[1];
+    const float U = uv.x * (float)w, V = uv.y * (float)h;
+    int x0 = (int)floorf(U), x1 = (int)ceilf(U), y0 = (int)floorf(V), y1 = (int)ceilf(V);
+    const float du = U - (float)x0;
+    const float dv = V - (float)y0;
+    x0 = min(max(x0, 0), w - 1);
+    x1 = min(max(x1, 0), w - 1);
+    y0 = min(max(y0, 0), h - 1);
+    y1 = min(max(y1, 0), h - 1);
+    const uchar4 v00 = B.pixels[(size_t)y0 * w + x0], v10 = B.pixels[(size_t)y0 * w + x1];
+    const uchar4 v01 = B.pixels[(size_t)y1 * w + x0], v11 = B.pixels[(size_t)y1 * w + x1];
+    const uint8_t wu0 = uc_weight(1.0f - du), wu1 = uc_weight(du);
+    const uint8_t wv0 = uc_weight(1.0f - dv), wv1 = uc_weight(dv);
+    const uint8_t a00[3] = { v00.x, v00.y, v00.z }, a10[3] = { v10.x, v10.y, v10.z };
+    const uint8_t a01[3] = { v01.x, v01.y, v01.z }, a11[3] = { v11.x, v11.y, v11.z };
+    uint8_t rgb[3];
+    for (int c = 0; c < 3; c++) {
+        const uint8_t top = (uint8_t)((uint8_t)(wu0 * a00[c]) + (uint8_t)(wu1 * a10[c]));
+        const uint8_t bot = (uint8_t)((uint8_t)(wu0 * a01[c]) + (uint8_t)(wu1 * a11[c]));
+        rgb[c] = (uint8_t)((uint8_t)(wv0 * top) + (uint8_t)(wv1 * bot));
+    }
+    const float k = 1.0f / 255.0f;
+    const float r = k * (float)rgb[0], g = k * (float)rgb[1], b = k * (float)rgb[2];
+    return C3(0.412453f * r + 0.357580f * g + 0.180423f * b,
+              0.212671f * r + 0.715160f * g + 0.072169f * b,
+              0.019334f * r + 0.119193f * g + 0.950227f * b);
+}
+
+/* EvaluateTexture - Source/textures.h:26-111 (procedural and bitmap textures) */
 ER_COLD c3 evaluate_texture(const Params& P, int id, v2 UV)
 {
     if (id < 0 || id >= P.n_textures) return C3(0, 0, 0);
@@ -464,6 +503,8 @@ ER_COLD c3 evaluate_texture(const Params& P, int id, v2 UV)
         case 2: L = ctf_eval(T.gradient, t.y); break;
         default: break;
         }
+    } else if (T.type == 1 && T.bitmap_id >= 0 && T.bitmap_id < P.n_bitmaps && P.bitmaps[T.bitmap_id].pixels) {
+        L = bitmap_xyz(P.bitmaps[T.bitmap_id], t);
     }
     return cscale(L, T.output_level);
 }
@@ -576,11 +617,13 @@ ER_D float power_heuristic(float fPdf, float gPdf)
 /* ---- events ---- */
 
 struct Event {
-    int type;            /* 0 volume, 1 light */
+    int type;            /* 0 volume, 1 light, 2 object */
     bool valid;
     float T;
     v3 P, N, Wo;
     c3 Le;
+    v2 UV;               /* object events: the surface parameters of the hit */
+    int object_id;       /* object events: index into the tracer's objects */
 };
 
 /* step budget of a fixed-step march: the loop ends after at most
@@ -698,6 +741,44 @@ ER_D bool intersects_light(const Params& P, const Ray& R)
         const Ray Rt = xform_ray(L.inv_tm, R);
         Isect Int; Int.invalid();
         intersect_shape(L, Rt, Int);
+        if (Int.valid) return true;
+    }
+    return false;
+}
+
+/* IntersectObject / IntersectObjects - Source/objects.h:26-62: the nearest of
+   the tracer's objects (array order, ObjectID = index) */
+ER_D void intersect_objects(const Params& P, const Ray& R, Event& RS)
+{
+    float T = FLT_MAX;
+    for (int i = 0; i < P.object_count; i++) {
+        const Object& O = P.objects[i];
+        const Ray Rt = xform_ray(O.shape.inv_tm, R);
+        Isect Int; Int.invalid();
+        intersect_shape(O.shape, Rt, Int);
+        if (!Int.valid) continue;
+        Event local;
+        local.type = 2;
+        local.valid = true;
+        local.N = xform_vector(O.shape.tm, Int.N);
+        local.P = xform_point(O.shape.tm, Int.P);
+        local.T = vlen(vsub(local.P, R.O));
+        local.Wo = vneg(R.D);
+        local.Le = C3(0, 0, 0);
+        local.UV = Int.UV;
+        local.object_id = i;
+        if (local.T < T) { RS = local; T = local.T; }
+    }
+}
+
+/* IntersectsObject - Source/objects.h:64-80 */
+ER_D bool intersects_object(const Params& P, const Ray& R)
+{
+    for (int i = 0; i < P.object_count; i++) {
+        const Object& O = P.objects[i];
+        const Ray Rt = xform_ray(O.shape.inv_tm, R);
+        Isect Int; Int.invalid();
+        intersect_shape(O.shape, Rt, Int);
         if (Int.valid) return true;
     }
     return false;
@@ -873,6 +954,7 @@ ER_D float transmittance_ratio(const Params& P, const Ray& R, Rng& rng)
 
 /* Visible / Intersect - Source/transport.h:30-56: 1/0 for the reference
    march, the ratio-tracked transmittance with delta tracking */
+template <bool OBJ = true>
 ER_D float visibility(const Params& P, v3 P1, v3 P2, Rng& rng)
 {
     if (!P.shadows) return 1.0f;
@@ -883,6 +965,7 @@ ER_D float visibility(const Params& P, v3 P1, v3 P2, Rng& rng)
     R.MinT = 0.0f;
     R.MaxT = smin(vlen(vsub(P2, P1)) - 2.0f * ER_RAY_EPS, P.max_shadow_distance);
     if (intersects_light(P, R)) return 0.0f;
+    if (OBJ && P.object_count > 0 && intersects_object(P, R)) return 0.0f;
     if (P.free_flight == 1) return transmittance_ratio(P, R, rng);
     return scatter_event_in_volume(P, R, rng) ? 0.0f : 1.0f;
 }
@@ -1056,7 +1139,23 @@ ER_D c3 estimate_direct_light(const Params& P, const Light& L, int slot, const M
     return Ld;
 }
 
-/* UniformSampleOneLight - Source/transport.h:115-156 (volume events) */
+/* the object shader of UniformSampleOneLight (Source/transport.h:141-149):
+   BRDF with the object's diffuse and specular textures at the hit, IOR 15 and
+   the exponent of the glossiness texture's luminance (ColorXYZf::Y) */
+ER_D void object_shader(const Params& P, const Event& SE, Shader& sh)
+{
+    const Object& O = P.objects[SE.object_id];
+    const c3 Kd = evaluate_texture(P, O.diffuse_texture_id, SE.UV);
+    const c3 Ks = evaluate_texture(P, O.specular_texture_id, SE.UV);
+    const c3 G = evaluate_texture(P, O.glossiness_texture_id, SE.UV);
+    float Y = 0.0f;
+    Y += 0.212671f * G.r;
+    Y += 0.715160f * G.g;
+    Y += 0.072169f * G.b;
+    shader_init(sh, 0, SE.N, SE.Wo, Kd, Ks, 15.0f, 1000000.0f * er_powf(Y, 7.0f));
+}
+
+/* UniformSampleOneLight - Source/transport.h:115-156 (volume and object events) */
 ER_D c3 uniform_sample_one_light(const Params& P, const Event& SE, Rng& rng, const Metro& ms)
 {
     c3 Ld = C3(0, 0, 0);
@@ -1067,9 +1166,13 @@ ER_D c3 uniform_sample_one_light(const Params& P, const Event& SE, Rng& rng, con
     if (idx < 0 || idx >= P.light_count || !P.light_valid[idx]) return Ld;
     const Light& L = P.lights[idx];
     Shader sh;
-    const int type = P.apply_shading_type ? select_shader_type(P, SE, I, rng) : 0;
-    shader_init(sh, type, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
-                1000000.0f * er_powf(plf_eval(P.tfs->glossiness, I), 7.0f));
+    if (SE.type == 2) {
+        object_shader(P, SE, sh);
+    } else {
+        const int type = P.apply_shading_type ? select_shader_type(P, SE, I, rng) : 0;
+        shader_init(sh, type, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
+                    1000000.0f * er_powf(plf_eval(P.tfs->glossiness, I), 7.0f));
+    }
     Ld = cadd(Ld, estimate_direct_light(P, L, idx, ms, SE, rng, sh));
     return cscale(Ld, (float)P.light_count);
 }
@@ -1101,19 +1204,23 @@ ER_D float4 single_scattering(const Params& P, int x, int y, Rng& rng)
     Metro ms;
     ms.large_step(rng);
     const Ray R = sample_camera(P, x, y, ms.film_uv, ms.lens_uv);
-    Event se0, se1, SE;
+    Event se0, se1, se2, SE;
     se0.type = 0; se0.valid = false; se0.T = 0.0f; se0.Le = C3(0, 0, 0);
     se0.P = V3(0, 0, 0); se0.N = V3(0, 0, 0); se0.Wo = V3(0, 0, 0);
     se1 = se0; se1.type = 1;
+    se2.type = 2; se2.valid = false; se2.T = 0.0f;
     if (P.free_flight == 1) sample_volume_delta(P, R, rng, se0);
     else sample_volume(P, R, rng, se0);
     intersect_lights(P, R, se1, true);
+    if (P.object_count > 0) intersect_objects(P, R, se2);
     SE = se0; SE.valid = false; SE.type = 0;
     float T = FLT_MAX;
     if (se0.valid && se0.T < T) { SE = se0; T = se0.T; }
     if (se1.valid && se1.T < T) { SE = se1; T = se1.T; }
+    if (se2.valid && se2.T < T) { SE = se2; T = se2.T; }
     if (SE.valid && SE.type == 0) Lv = cadd(Lv, uniform_sample_one_light(P, SE, rng, ms));
     if (SE.valid && SE.type == 1) Lv = cadd(Lv, SE.Le);
+    if (SE.valid && SE.type == 2) Lv = cadd(Lv, uniform_sample_one_light(P, SE, rng, ms));
     return make_float4(Lv.r, Lv.g, Lv.b, SE.valid ? 1.0f : 0.0f);
 }
 

@@ -124,6 +124,7 @@ struct WfQueues {
         B.tune_primary = 4;
         B.tune_shadow = 4;
         B.tune_shade = 2;
+        B.objects = 0;
         return cudaSuccess;
     }
 };
@@ -181,6 +182,8 @@ struct TracerItem {
     DevBuf<erd::Tfs> tfs;
     DevBuf<erd::Plf> opacity;
     DevBuf<erd::Light> lights;
+    DevBuf<erd::Object> objects;
+    DevBuf<erd::Bitmap> bitmaps;
     DevBuf<int> light_valid;
     DevBuf<erd::Texture> textures;
     DevBuf<float> sigma;
@@ -289,16 +292,22 @@ void to_plf(erd::Plf& o, const er_plf& s)
     for (int i = 0; i < 128; i++) { o.pos[i] = s.position[i]; o.val[i] = s.value[i]; }
 }
 
-void to_light(erd::Light& o, const er_light_desc& s)
+/* Shape (Source/shape.h): transforms, type, sizes and the area */
+void to_shape(erd::Light& o, const er_shape& sh)
 {
     for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 4; j++) { o.tm[i][j] = s.shape.tm[i][j]; o.inv_tm[i][j] = s.shape.inv_tm[i][j]; }
-    o.one_sided = s.shape.one_sided;
-    o.type = s.shape.type;
-    for (int i = 0; i < 3; i++) o.size[i] = s.shape.size[i];
-    o.area = shape_area(s.shape);
-    o.inner_radius = s.shape.inner_radius;
-    o.outer_radius = s.shape.outer_radius;
+        for (int j = 0; j < 4; j++) { o.tm[i][j] = sh.tm[i][j]; o.inv_tm[i][j] = sh.inv_tm[i][j]; }
+    o.one_sided = sh.one_sided;
+    o.type = sh.type;
+    for (int i = 0; i < 3; i++) o.size[i] = sh.size[i];
+    o.area = shape_area(sh);
+    o.inner_radius = sh.inner_radius;
+    o.outer_radius = sh.outer_radius;
+}
+
+void to_light(erd::Light& o, const er_light_desc& s)
+{
+    to_shape(o, s.shape);
     o.visible = s.visible;
     o.texture_id = s.texture_id;
     o.multiplier = s.multiplier;
@@ -424,7 +433,6 @@ er_status build(TracerItem& t)
     auto vit = C.volumes.items.find(d.volume_id);
     if (vit == C.volumes.items.end()) return fail(ER_ERR_INVALID_ID, "tracer references volume ID:%d which does not exist", d.volume_id);
     VolumeItem& v = *vit->second;
-    if (d.object_count > 0) return fail(ER_ERR_UNSUPPORTED, "surface objects (ObjectIDs.Count = %d) are not implemented by the transport kernels", d.object_count);
     if (d.settings.free_flight != ER_FREE_FLIGHT_MARCH && d.settings.free_flight != ER_FREE_FLIGHT_DELTA)
         return fail(ER_ERR_INVALID_ARGUMENT, "free_flight %d is not an ER_FREE_FLIGHT_* value", d.settings.free_flight);
     if (d.settings.mis != ER_MIS_LIGHT_ONLY && d.settings.mis != ER_MIS_FULL)
@@ -508,10 +516,6 @@ er_status build(TracerItem& t)
         if (it == C.lights.items.end()) continue;
         to_light(L[i], *it->second);
         valid[i] = 1;
-        const int tid = it->second->texture_id;
-        auto tt = C.textures.items.find(tid);
-        if (tt != C.textures.items.end() && tt->second->type == ER_TEXTURE_BITMAP)
-            return fail(ER_ERR_UNSUPPORTED, "light %d uses bitmap texture %d; bitmap textures are not implemented by the transport kernels", d.light_ids[i], tid);
     }
     std::vector<int> lids((size_t)std::max(lc, 1), -1);
     for (int i = 0; i < lc; i++) lids[i] = d.light_ids[i];
@@ -525,6 +529,26 @@ er_status build(TracerItem& t)
     P.lights = t.lights.p;
     P.light_valid = t.light_valid.p;
     P.light_ids = t.light_ids.p;
+    /* surface objects: IntersectObjects reads gpObjects[i] for i below
+       ObjectIDs.Count (Source/objects.h:45-62), i.e. the first Count bound
+       objects in bind-list (ID) order */
+    std::vector<erd::Object> O;
+    for (auto& kv : C.objects.items) {
+        if ((int)O.size() >= d.object_count) break;
+        erd::Object o;
+        memset(&o, 0, sizeof(o));
+        to_shape(o.shape, kv.second->shape);
+        o.diffuse_texture_id = kv.second->diffuse_texture_id;
+        o.specular_texture_id = kv.second->specular_texture_id;
+        o.glossiness_texture_id = kv.second->glossiness_texture_id;
+        O.push_back(o);
+    }
+    P.object_count = (int)O.size();
+    if (!O.empty()) {
+        ER_CUDA(t.objects.ensure(O.size()));
+        ER_CUDA(cudaMemcpyAsync(t.objects.p, O.data(), O.size() * sizeof(erd::Object), cudaMemcpyHostToDevice, st));
+        P.objects = t.objects.p;
+    }
     /* textures indexed by texture ID; unbound IDs evaluate to black */
     const int ntex = max_tex + 1;
     std::vector<erd::Texture> T((size_t)std::max(ntex, 1));
@@ -534,6 +558,24 @@ er_status build(TracerItem& t)
     ER_CUDA(cudaMemcpyAsync(t.textures.p, T.data(), T.size() * sizeof(erd::Texture), cudaMemcpyHostToDevice, st));
     P.textures = t.textures.p;
     P.n_textures = ntex;
+    /* bitmaps indexed by bitmap ID (ErTexture::BitmapID); unbound IDs read black */
+    int max_bmp = -1;
+    for (auto& kv : C.bitmaps.items) max_bmp = std::max(max_bmp, kv.first);
+    P.n_bitmaps = max_bmp + 1;
+    P.bitmaps = nullptr;
+    if (P.n_bitmaps > 0) {
+        std::vector<erd::Bitmap> B((size_t)P.n_bitmaps);
+        for (auto& b : B) { b.pixels = nullptr; b.res[0] = b.res[1] = 0; }
+        for (auto& kv : C.bitmaps.items) {
+            erd::Bitmap& b = B[(size_t)kv.first];
+            b.pixels = kv.second->pixels.p;
+            b.res[0] = kv.second->res[0];
+            b.res[1] = kv.second->res[1];
+        }
+        ER_CUDA(t.bitmaps.ensure(B.size()));
+        ER_CUDA(cudaMemcpyAsync(t.bitmaps.p, B.data(), B.size() * sizeof(erd::Bitmap), cudaMemcpyHostToDevice, st));
+        P.bitmaps = t.bitmaps.p;
+    }
     P.tfs = t.tfs.p;
     ER_CUDA(t.err.ensure(1));
     P.err = t.err.p;
@@ -593,6 +635,7 @@ er_status trace_sum(TracerItem& t, int spp, uint32_t view, uint32_t first, float
     B.tune_primary = t.d.settings.tune_primary > 0 ? t.d.settings.tune_primary : 4;
     B.tune_shadow = t.d.settings.tune_shadow > 0 ? t.d.settings.tune_shadow : 4;
     B.tune_shade = t.d.settings.tune_shade > 0 ? t.d.settings.tune_shade : 2;
+    B.objects = t.P.object_count > 0;
     WfView V;
     memset(&V, 0, sizeof(V));
     V.P = t.P;
@@ -685,6 +728,8 @@ er_status batch_plan(BatchItem& b)
     b.B.tune_primary = b.tune_primary;
     b.B.tune_shadow = b.tune_shadow;
     b.B.tune_shade = b.tune_shade;
+    b.B.objects = 0;
+    for (const WfView& hv : b.host_views) b.B.objects |= hv.P.object_count > 0;
     if (b.flags & ER_BATCH_GRAPH) {
         if (!b.capture_stream) ER_CUDA(cudaStreamCreateWithFlags(&b.capture_stream, cudaStreamNonBlocking));
         ER_CUDA(cudaStreamBeginCapture(b.capture_stream, cudaStreamCaptureModeThreadLocal));

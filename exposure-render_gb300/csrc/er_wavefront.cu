@@ -80,11 +80,16 @@ ER_D int find_segment(const WfSegment* __restrict__ segs, int nseg, uint32_t i)
 
 }  // namespace
 
-/* ---- stage 1: camera ray, free flight, visible lights ---- */
+/* top bit of an event record's view word: a surface-object event */
+#define WF_OBJECT_EVENT 0x80000000u
+
+/* ---- stage 1: camera ray, free flight, visible lights and objects ---- */
 
 /* MINB: resident 256-thread blocks per SM the register allocation targets
    (2: 128 registers, 3: ~80, 4: 64, 6: 40, 8: 32); picked at run time */
-template <int MINB, bool ONE>
+/* OBJ: the variant that also intersects surface objects (scenes without
+   objects run the lean one) */
+template <int MINB, bool ONE, bool OBJ>
 __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restrict__ views, const WfSegment* __restrict__ segs, int nseg,
                                                            const WfView one, const WfSegment one_seg, uint32_t items,
                                                            float4* __restrict__ results, float4* __restrict__ events,
@@ -126,6 +131,12 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
             float T = FLT_MAX;
             if (se0.valid && se0.T < T) { SE = se0; T = se0.T; }
             if (se1.valid && se1.T < T) { SE = se1; T = se1.T; }
+            if (OBJ && P.object_count > 0) {
+                Event se2;
+                se2.type = 2; se2.valid = false; se2.T = 0.0f;
+                intersect_objects(P, R, se2);
+                if (se2.valid && se2.T < T) { SE = se2; T = se2.T; }
+            }
             if (!SE.valid) {
                 results[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             } else if (SE.type == 1) {
@@ -133,16 +144,23 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
                 results[i] = make_float4(Lv.r, Lv.g, Lv.b, 1.0f);
             } else {
                 push = true;
+                /* an object event parks its surface parameters in the sample's
+                   result slot, which the shade stage reads before it writes
+                   the sample's value there */
+                if (SE.type == 2) results[i] = make_float4(SE.UV.x, SE.UV.y, u2f((uint32_t)SE.object_id), 0.0f);
             }
         }
         const uint32_t slot = queue_slot(push, n_events);
         if (push) {
+            /* volume events: the normal is computed by the shade stage; object
+               events carry theirs and set the top bit of the view word */
+            const bool obj = SE.type == 2;
             float4* e = events + (size_t)slot * 5;
             e[0] = make_float4(u2f(i), u2f(rng.s0), u2f(rng.s1), ms.light_num);
             e[1] = make_float4(SE.P.x, SE.P.y, SE.P.z, ms.brdf_component);
-            e[2] = make_float4(0.0f, 0.0f, 0.0f, ms.brdf_dir.x);
+            e[2] = obj ? make_float4(SE.N.x, SE.N.y, SE.N.z, ms.brdf_dir.x) : make_float4(0.0f, 0.0f, 0.0f, ms.brdf_dir.x);
             e[3] = make_float4(SE.Wo.x, SE.Wo.y, SE.Wo.z, ms.brdf_dir.y);
-            e[4] = make_float4(ms.light_uvw.x, ms.light_uvw.y, ms.light_uvw.z, u2f((uint32_t)v));
+            e[4] = make_float4(ms.light_uvw.x, ms.light_uvw.y, ms.light_uvw.z, u2f((uint32_t)v | (obj ? WF_OBJECT_EVENT : 0u)));
         }
     }
 }
@@ -154,7 +172,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
 #define WF_RAY2 2u
 
 /* MINB: resident 128-thread blocks per SM (2: 255 registers, 3: 168, 4: 128, 6: 80) */
-template <bool ONE, int MINB>
+template <bool ONE, int MINB, bool OBJ>
 __global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict__ views, const WfView one, const float4* __restrict__ events,
                                                   const uint32_t* __restrict__ n_events, float4* __restrict__ results,
                                                   float4* __restrict__ jobs, uint32_t* __restrict__ n_jobs)
@@ -179,7 +197,9 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict
             sample = f2u(e0.x);
             rng.s0 = f2u(e0.y);
             rng.s1 = f2u(e0.z);
-            v = f2u(e4.w);
+            const uint32_t vw = f2u(e4.w);
+            v = vw & ~WF_OBJECT_EVENT;
+            const bool obj = OBJ && (vw & WF_OBJECT_EVENT) != 0u;
             const Params& P = view_of<ONE>(views, one, v).P;
             Metro ms;
             ms.light_num = e0.w;
@@ -193,7 +213,14 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict
                central differences its six intensities also give the gradient
                magnitude of the shader switch */
             float gm = -1.0f;
-            if (P.gradient_mode == 1) {
+            if (obj) {
+                const float4 o = results[sample];
+                SE.type = 2;
+                SE.UV.x = o.x;
+                SE.UV.y = o.y;
+                SE.object_id = (int)f2u(o.z);
+                SE.N = V3(e2.x, e2.y, e2.z);
+            } else if (P.gradient_mode == 1) {
                 Grad6 g6;
                 gradient_samples(P, SE.P, g6);
                 SE.N = vnorm(gradient_cd6(g6));
@@ -217,9 +244,13 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict
             } else {
                 const Light& L = P.lights[idx];
                 Shader sh;
-                const int type = P.apply_shading_type ? select_shader_type(P, SE, I, rng, gm) : 0;
-                shader_init(sh, type, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
-                            1000000.0f * er_powf(plf_eval(P.tfs->glossiness, I), 7.0f));
+                if (obj) {
+                    object_shader(P, SE, sh);
+                } else {
+                    const int type = P.apply_shading_type ? select_shader_type(P, SE, I, rng, gm) : 0;
+                    shader_init(sh, type, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
+                                1000000.0f * er_powf(plf_eval(P.tfs->glossiness, I), 7.0f));
+                }
                 count = (float)P.light_count;
                 /* EstimateDirectLight - Source/transport.h:58-113, without the visibility terms */
                 v3 Wi;
@@ -289,7 +320,7 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict
 
 /* ---- stage 3: shadow segments and the sample's sum ---- */
 
-template <int MINB, bool ONE>
+template <int MINB, bool ONE, bool OBJ>
 __global__ void __launch_bounds__(256, MINB) k_wf_shadow(const WfView* __restrict__ views, const WfView one, const float4* __restrict__ jobs,
                                                           const uint32_t* __restrict__ n_jobs, float4* __restrict__ results)
 {
@@ -310,14 +341,14 @@ __global__ void __launch_bounds__(256, MINB) k_wf_shadow(const WfView* __restric
         const c3 Le = C3(j2.w, j3.w, j4.w);
         c3 dl = C3(0, 0, 0);
         if (flags & WF_RAY1) {
-            const float Tr = visibility(P, Pp, V3(j2.x, j2.y, j2.z), rng);
+            const float Tr = visibility<OBJ>(P, Pp, V3(j2.x, j2.y, j2.z), rng);
             if (Tr > 0.0f) {
                 const c3 c1 = C3(j3.x, j3.y, j3.z);
                 dl = ref_mode ? cadd(dl, c1) : cadd(dl, cscale(c1, Tr));
             }
         }
         if (flags & WF_RAY2) {
-            const float Tr = visibility(P, Pp, V3(j4.x, j4.y, j4.z), rng);
+            const float Tr = visibility<OBJ>(P, Pp, V3(j4.x, j4.y, j4.z), rng);
             if (Tr > 0.0f) dl = cadd(dl, cscale(C3(j5.x, j5.y, j5.z), Tr));
         }
         const c3 Lv = cadd(C3(0, 0, 0), cscale(cadd(Le, dl), count));
@@ -480,34 +511,37 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         if (e != cudaSuccess) return e;
         const uint32_t g1 = (items + 255) / 256 < (uint32_t)sm * 64 ? (items + 255) / 256 : (uint32_t)sm * 64;
         cudaEvent_t t0 = stage_begin(s);
-#define ER_PRIMARY(M) k_wf_primary<M, ONE><<<g1, 256, 0, s>>>(d_views, dseg, nseg, one, one_seg, items, B.results, B.events, B.counters)
-        switch (B.tune_primary) {
-        case 2: ER_PRIMARY(2); break;
-        case 3: ER_PRIMARY(3); break;
-        case 6: ER_PRIMARY(6); break;
-        case 8: ER_PRIMARY(8); break;
-        default: ER_PRIMARY(4); break;
+#define ER_PRIMARY(M, O) k_wf_primary<M, ONE, O><<<g1, 256, 0, s>>>(d_views, dseg, nseg, one, one_seg, items, B.results, B.events, B.counters)
+        if (B.objects) ER_PRIMARY(4, true);
+        else switch (B.tune_primary) {
+        case 2: ER_PRIMARY(2, false); break;
+        case 3: ER_PRIMARY(3, false); break;
+        case 6: ER_PRIMARY(6, false); break;
+        case 8: ER_PRIMARY(8, false); break;
+        default: ER_PRIMARY(4, false); break;
         }
 #undef ER_PRIMARY
         stage_end(t0, 0, s);
         t0 = stage_begin(s);
-#define ER_SHADE(M) k_wf_shade<ONE, M><<<sm * 16, 128, 0, s>>>(d_views, one, B.events, B.counters, B.results, B.jobs, B.counters + 1)
-        switch (B.tune_shade) {
-        case 3: ER_SHADE(3); break;
-        case 4: ER_SHADE(4); break;
-        case 6: ER_SHADE(6); break;
-        default: ER_SHADE(2); break;
+#define ER_SHADE(M, O) k_wf_shade<ONE, M, O><<<sm * 16, 128, 0, s>>>(d_views, one, B.events, B.counters, B.results, B.jobs, B.counters + 1)
+        if (B.objects) ER_SHADE(2, true);
+        else switch (B.tune_shade) {
+        case 3: ER_SHADE(3, false); break;
+        case 4: ER_SHADE(4, false); break;
+        case 6: ER_SHADE(6, false); break;
+        default: ER_SHADE(2, false); break;
         }
 #undef ER_SHADE
         stage_end(t0, 1, s);
         t0 = stage_begin(s);
-#define ER_SHADOW(M) k_wf_shadow<M, ONE><<<sm * 8, 256, 0, s>>>(d_views, one, B.jobs, B.counters + 1, B.results)
-        switch (B.tune_shadow) {
-        case 2: ER_SHADOW(2); break;
-        case 3: ER_SHADOW(3); break;
-        case 6: ER_SHADOW(6); break;
-        case 8: ER_SHADOW(8); break;
-        default: ER_SHADOW(4); break;
+#define ER_SHADOW(M, O) k_wf_shadow<M, ONE, O><<<sm * 8, 256, 0, s>>>(d_views, one, B.jobs, B.counters + 1, B.results)
+        if (B.objects) ER_SHADOW(4, true);
+        else switch (B.tune_shadow) {
+        case 2: ER_SHADOW(2, false); break;
+        case 3: ER_SHADOW(3, false); break;
+        case 6: ER_SHADOW(6, false); break;
+        case 8: ER_SHADOW(8, false); break;
+        default: ER_SHADOW(4, false); break;
         }
 #undef ER_SHADOW
         stage_end(t0, 2, s);

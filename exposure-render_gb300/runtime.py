@@ -22,9 +22,24 @@ class Renderer:
         self.scene = scene
         self.texture_ids = []
         self.light_ids = []
-        for t in scene.textures:
+        # BindBitmap (Source/exposurerender.h:38): bitmap i of the scene
+        self.bitmap_ids = []
+        for px in getattr(scene, "bitmaps", []):
+            px = np.ascontiguousarray(px, dtype=np.uint8)
+            b = C.er_bitmap_desc()
+            b.resolution[0], b.resolution[1] = px.shape[1], px.shape[0]
+            b.pixels = px.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
             i = c_int32(-1)
-            C.check(self.lib.er_bind_texture(byref(t), byref(i)))
+            C.check(self.lib.er_bind_bitmap(byref(b), byref(i)))
+            self.bitmap_ids.append(i.value)
+        for t in scene.textures:
+            tc = C.er_texture_desc()
+            ctypes.memmove(byref(tc), byref(t), ctypes.sizeof(t))
+            if tc.type == C.TEXTURE_BITMAP:
+                k = tc.bitmap_id
+                tc.bitmap_id = self.bitmap_ids[k] if 0 <= k < len(self.bitmap_ids) else -1
+            i = c_int32(-1)
+            C.check(self.lib.er_bind_texture(byref(tc), byref(i)))
             self.texture_ids.append(i.value)
         for L in scene.lights:
             Lc = C.er_light_desc()
@@ -34,6 +49,18 @@ class Renderer:
             i = c_int32(-1)
             C.check(self.lib.er_bind_light(byref(Lc), byref(i)))
             self.light_ids.append(i.value)
+        # BindObject (Source/exposurerender.h:35): object i of the scene is the
+        # i-th bound object, the order IntersectObjects walks (Source/objects.h:52)
+        self.object_ids = []
+        for o in getattr(scene, "objects", []):
+            oc = C.er_object_desc()
+            ctypes.memmove(byref(oc), byref(o), ctypes.sizeof(o))
+            for f in ("diffuse_texture_id", "specular_texture_id", "glossiness_texture_id"):
+                k = getattr(oc, f)
+                setattr(oc, f, self.texture_ids[k] if 0 <= k < len(self.texture_ids) else -1)
+            i = c_int32(-1)
+            C.check(self.lib.er_bind_object(byref(oc), byref(i)))
+            self.object_ids.append(i.value)
         vd = scene.volume_desc()
         vid = c_int32(-1)
         C.check(self.lib.er_bind_volume(byref(vd), byref(vid)))
@@ -44,6 +71,9 @@ class Renderer:
         for k in range(t.light_count):
             src = scene.tracer.light_ids[k]
             t.light_ids[k] = self.light_ids[src] if 0 <= src < len(self.light_ids) else -1
+        for k in range(t.object_count):
+            src = scene.tracer.object_ids[k]
+            t.object_ids[k] = self.object_ids[src] if 0 <= src < len(self.object_ids) else -1
         self.tracer_desc = t
         tid = c_int32(-1)
         C.check(self.lib.er_bind_tracer(byref(t), byref(tid)))
@@ -119,11 +149,16 @@ class Renderer:
         lib = self.lib
         lib.er_unbind_tracer(self.tracer_id)
         lib.er_unbind_volume(self.volume_id)
+        for i in self.object_ids:
+            lib.er_unbind_object(i)
         for i in self.light_ids:
             lib.er_unbind_light(i)
         for i in self.texture_ids:
             lib.er_unbind_texture(i)
-        self.light_ids, self.texture_ids = [], []
+        for i in self.bitmap_ids:
+            lib.er_unbind_bitmap(i)
+        self.bitmap_ids = []
+        self.light_ids, self.texture_ids, self.object_ids = [], [], []
 
 
 class Batch:

@@ -37,6 +37,7 @@ class Scene:
     textures: list = field(default_factory=list)    # er_texture_desc, texture i has ID i
     spp: int = 1
     objects: list = field(default_factory=list)     # er_object_desc, object i has ID i
+    bitmaps: list = field(default_factory=list)     # uint8 (H, W, 4) RGBA arrays, bitmap i has ID i
 
     @property
     def width(self) -> int:
@@ -476,3 +477,37 @@ def scene_objects(res=32, film=(48, 40), spp=4, seed=3) -> Scene:
     t.object_count = 2
     t.object_ids[0], t.object_ids[1] = 0, 1
     return Scene("objects", vol, tracer=t, lights=lights, textures=textures, spp=spp, objects=objects)
+
+
+# ---------------------------------------------------------------------------
+# bitmap textures (ErTexture of type Bitmap over a bound ErBitmap)
+# ---------------------------------------------------------------------------
+
+def bitmap_texture(bitmap_id, level=1.0, repeat=(1.0, 1.0), offset=(0.0, 0.0), flip=(0, 0)) -> C.er_texture_desc:
+    t = C.new_texture_desc()
+    t.type = C.TEXTURE_BITMAP
+    t.bitmap_id = bitmap_id
+    t.output_level = level
+    t.repeat[0], t.repeat[1] = repeat
+    t.offset[0], t.offset[1] = offset
+    t.flip[0], t.flip[1] = flip
+    return t
+
+
+def scene_bitmaps(res=32, film=(48, 40), spp=4, seed=3) -> Scene:
+    """The objects scene with bitmap textures.  The reference's bitmap lookup
+    (Source/buffer2d.h:227-254) carries its bilinear weights in unsigned char,
+    so it returns the floor texel where the scaled coordinate is an integer
+    and black elsewhere: texture 4 (repeat 0, offsets on the texel grid of a
+    4x2 bitmap) reads texel (1, 1) everywhere and lights the scene; texture 5
+    (a repeated 16x16 bitmap) shows the black case on the sphere."""
+    sc = scene_objects(res=res, film=film, spp=spp, seed=seed)
+    rng = np.random.default_rng(seed + 100)
+    sc.bitmaps = [rng.integers(0, 256, size=(2, 4, 4), dtype=np.uint8),
+                  rng.integers(0, 256, size=(16, 16, 4), dtype=np.uint8)]
+    sc.textures = sc.textures + [bitmap_texture(0, level=1.5, repeat=(0.0, 0.0), offset=(0.25, 0.5)),
+                                 bitmap_texture(1, repeat=(3.0, 3.0), flip=(1, 0))]
+    sc.objects[0].diffuse_texture_id = 4
+    sc.objects[1].specular_texture_id = 5
+    sc.lights[0].texture_id = 4
+    return sc

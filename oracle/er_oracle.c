@@ -40,6 +40,7 @@ typedef float desc_f32;
 #define sqrtf sqrt
 #define fabsf fabs
 #define floorf floor
+#define ceilf ceil
 #define fminf fmin
 #define fmaxf fmax
 #define er_logf log
@@ -145,6 +146,11 @@ struct or_scene {
     int object_count;
     int n_objects;
     er_object_desc* objects;
+    /* bitmaps (gpBitmaps in device-array order, ErTexture::BitmapID indexes
+       it, Source/textures.h:101-107): RGBA8 row-major */
+    int n_bitmaps;
+    int* bitmap_res;            /* 2 per bitmap */
+    uint8_t** bitmap_pixels;
     /* statistics */
     uint64_t lookups;
     uint64_t stat[OR_NSTATS];   /* work counters of the last render (render_stats) */
@@ -267,6 +273,9 @@ void ER_OR(scene_destroy)(or_scene* s)
     free(s->lights);
     free(s->textures);
     free(s->objects);
+    for (int i = 0; i < s->n_bitmaps; i++) free(s->bitmap_pixels[i]);
+    free(s->bitmap_pixels);
+    free(s->bitmap_res);
     free(s->sigma);
     free(s->majorant);
     free(s);
@@ -766,6 +775,48 @@ static void sample_light_surface(const or_light* L, v3 UVW, surf_sample* SS)
 /* textures - Source/textures.h:26-111                                  */
 /* ------------------------------------------------------------------ */
 
+/* scalar * ColorRGBAuc as the reference evaluates it: the float converts to
+   the colour's unsigned char component type (truncation), then multiplies each
+   component in unsigned char arithmetic (Source/color.h:282-283,
+   Source/vector.h:183-190); sums of colours wrap in unsigned char
+   (Source/vector.h OPERATOR_PLUS) */
+static inline uint8_t uc_weight(float w) { return (uint8_t)w; }
+
+/* Buffer2D<ColorRGBAuc>::operator()(Vec2f, Normalized = true)
+   (Source/buffer2d.h:227-254) followed by ColorXYZf::FromRGBAuc
+   (Source/color.h:195-209).  The bilinear weights pass through unsigned char,
+   so a lookup is the floor texel when the scaled coordinate is an integer
+   and black otherwise; kept as the reference computes it. */
+static col3 bitmap_xyz(const uint8_t* px, int w, int h, v2 uv)
+{
+    const float U = uv.x * (float)w, V = uv.y * (float)h;
+    int c0[2] = { (int)floorf(U), (int)ceilf(U) };
+    int c1[2] = { (int)floorf(V), (int)ceilf(V) };
+    const float du = U - (float)c0[0];
+    const float dv = V - (float)c1[0];
+    for (int k = 0; k < 2; k++) {
+        c0[k] = c0[k] < 0 ? 0 : (c0[k] > w - 1 ? w - 1 : c0[k]);
+        c1[k] = c1[k] < 0 ? 0 : (c1[k] > h - 1 ? h - 1 : c1[k]);
+    }
+    const uint8_t* v00 = px + 4 * ((size_t)c1[0] * w + c0[0]);
+    const uint8_t* v10 = px + 4 * ((size_t)c1[0] * w + c0[1]);
+    const uint8_t* v01 = px + 4 * ((size_t)c1[1] * w + c0[0]);
+    const uint8_t* v11 = px + 4 * ((size_t)c1[1] * w + c0[1]);
+    const uint8_t wu0 = uc_weight(1.0f - du), wu1 = uc_weight(du);
+    const uint8_t wv0 = uc_weight(1.0f - dv), wv1 = uc_weight(dv);
+    uint8_t rgb[3];
+    for (int c = 0; c < 3; c++) {
+        const uint8_t top = (uint8_t)((uint8_t)(wu0 * v00[c]) + (uint8_t)(wu1 * v10[c]));
+        const uint8_t bot = (uint8_t)((uint8_t)(wu0 * v01[c]) + (uint8_t)(wu1 * v11[c]));
+        rgb[c] = (uint8_t)((uint8_t)(wv0 * top) + (uint8_t)(wv1 * bot));
+    }
+    const float k = 1.0f / 255.0f;
+    const float r = k * (float)rgb[0], g = k * (float)rgb[1], b = k * (float)rgb[2];
+    return C3(0.412453f * r + 0.357580f * g + 0.180423f * b,
+              0.212671f * r + 0.715160f * g + 0.072169f * b,
+              0.019334f * r + 0.119193f * g + 0.950227f * b);
+}
+
 static col3 evaluate_texture(const or_scene* s, int id, v2 UV)
 {
     if (id < 0) return C3(0, 0, 0);
@@ -799,7 +850,8 @@ static col3 evaluate_texture(const or_scene* s, int id, v2 UV)
         default: L = C3(0, 0, 0); break;
         }
     }
-    /* bitmap textures (Source/textures.h:101-107) are not on the configured path */
+    if (T->type == ER_TEXTURE_BITMAP && T->bitmap_id >= 0 && T->bitmap_id < s->n_bitmaps)
+        L = bitmap_xyz(s->bitmap_pixels[T->bitmap_id], s->bitmap_res[2 * T->bitmap_id], s->bitmap_res[2 * T->bitmap_id + 1], tuv);
     return cscale(L, T->output_level);
 }
 
@@ -1100,6 +1152,26 @@ static int intersects_object(const or_scene* s, const ray_t* R)
         if (Int.valid) return 1;
     }
     return 0;
+}
+
+void ER_OR(scene_set_bitmaps)(or_scene* s, const er_bitmap_desc* bitmaps, int32_t n)
+{
+    for (int i = 0; i < s->n_bitmaps; i++) free(s->bitmap_pixels[i]);
+    free(s->bitmap_pixels);
+    free(s->bitmap_res);
+    s->n_bitmaps = n > 0 ? n : 0;
+    s->bitmap_pixels = NULL;
+    s->bitmap_res = NULL;
+    if (!s->n_bitmaps) return;
+    s->bitmap_pixels = (uint8_t**)calloc((size_t)n, sizeof(uint8_t*));
+    s->bitmap_res = (int*)calloc(2 * (size_t)n, sizeof(int));
+    for (int i = 0; i < n; i++) {
+        const size_t bytes = 4 * (size_t)bitmaps[i].resolution[0] * (size_t)bitmaps[i].resolution[1];
+        s->bitmap_res[2 * i] = bitmaps[i].resolution[0];
+        s->bitmap_res[2 * i + 1] = bitmaps[i].resolution[1];
+        s->bitmap_pixels[i] = (uint8_t*)malloc(bytes ? bytes : 1);
+        if (bytes) memcpy(s->bitmap_pixels[i], bitmaps[i].pixels, bytes);
+    }
 }
 
 void ER_OR(scene_set_objects)(or_scene* s, const er_object_desc* objects, int32_t n)

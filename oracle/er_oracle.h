@@ -49,6 +49,8 @@ void ER_OR(scene_destroy)(or_scene* scene);
 /* BindObject for the scene: object i of `objects` is the i-th bound object
    (gpObjects[i]); the tracer's object_count says how many are intersected */
 void ER_OR(scene_set_objects)(or_scene* scene, const er_object_desc* objects, int32_t n);
+/* BindBitmap for the scene: bitmap i is gpBitmaps[i] (ErTexture::BitmapID) */
+void ER_OR(scene_set_bitmaps)(or_scene* scene, const er_bitmap_desc* bitmaps, int32_t n);
 
 /* KrnlSingleScattering over the whole film with stateful lanes
    (lanes[0..W*H) = RandomSeeds1, lanes[W*H..2W*H) = RandomSeeds2, advanced in

@@ -68,6 +68,7 @@ struct or_scene {
     std::vector<Light> lights;
     std::vector<Texture> textures;
     std::vector<Object> objects;
+    std::vector<Bitmap> bitmaps;
     Tracer* tracer;
     int W, H;
     uint32_t seed;
@@ -208,7 +209,7 @@ extern "C" void ref_scene_destroy(or_scene* s)
 {
     if (!s) return;
     if (gpTracer == s->tracer) {
-        gpTracer = NULL; gpVolumes = NULL; gpLights = NULL; gpTextures = NULL;
+        gpTracer = NULL; gpVolumes = NULL; gpLights = NULL; gpTextures = NULL; gpObjects = NULL; gpBitmaps = NULL;
     }
     delete s->tracer;
     delete s->volume;
@@ -223,6 +224,24 @@ static void bind_scene(or_scene* s)
     gpLights = s->lights.empty() ? NULL : &s->lights[0];
     gpTextures = s->textures.empty() ? NULL : &s->textures[0];
     gpObjects = s->objects.empty() ? NULL : &s->objects[0];
+    gpBitmaps = s->bitmaps.empty() ? NULL : &s->bitmaps[0];
+}
+
+/* BindBitmap: bitmap i is the i-th entry of gpBitmaps.  The Bitmap records
+   are sized first and switched to host memory before the ErBitmap is
+   assigned (device buffers are not allocated in a host build,
+   Source/buffer2d.h:118-131). */
+extern "C" void ref_scene_set_bitmaps(or_scene* s, const er_bitmap_desc* bitmaps, int32_t n)
+{
+    s->bitmaps.clear();
+    s->bitmaps.resize((size_t)(n > 0 ? n : 0));
+    for (int i = 0; i < n; i++) {
+        ErBitmap eb;
+        eb.BindPixels(Vec2i(bitmaps[i].resolution[0], bitmaps[i].resolution[1]), (ColorRGBAuc*)bitmaps[i].pixels);
+        s->bitmaps[i].Pixels.MemoryType = Enums::Host;
+        s->bitmaps[i] = eb;
+    }
+    bind_scene(s);
 }
 
 /* BindObject: object i is the i-th entry of gpObjects */

@@ -39,6 +39,7 @@ class Oracle:
         f("scene_create", c_void_p, [POINTER(C.er_tracer_desc), POINTER(C.er_volume_desc), c_void_p, c_int32, c_void_p, c_int32])
         f("scene_destroy", None, [c_void_p])
         f("scene_set_objects", None, [c_void_p, c_void_p, c_int32])
+        f("scene_set_bitmaps", None, [c_void_p, c_void_p, c_int32])
         f("render_frame", None, [c_void_p, c_void_p, c_void_p, c_int32])
         f("render_sum", None, [c_void_p, c_int32, c_uint32, c_uint32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_int32])
         if prefix != "ref_":
@@ -113,6 +114,15 @@ class SceneHandle:
         self.ta = scene.texture_array()
         self.h = orc.scene_create(ctypes.byref(scene.tracer), ctypes.byref(self.vd), ctypes.cast(self.la, c_void_p),
                                   len(scene.lights), ctypes.cast(self.ta, c_void_p), len(scene.textures))
+        bms = getattr(scene, "bitmaps", [])
+        if bms:
+            self.bitmap_pixels = [np.ascontiguousarray(b, dtype=np.uint8) for b in bms]
+            self.ba = (C.er_bitmap_desc * len(bms))()
+            for i, px in enumerate(self.bitmap_pixels):
+                self.ba[i].resolution[0] = px.shape[1]
+                self.ba[i].resolution[1] = px.shape[0]
+                self.ba[i].pixels = px.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+            orc.scene_set_bitmaps(self.h, ctypes.cast(self.ba, c_void_p), len(bms))
         objs = getattr(scene, "objects", [])
         if objs:
             self.oa = (C.er_object_desc * len(objs))(*objs)

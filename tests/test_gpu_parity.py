@@ -302,7 +302,8 @@ def test_bind_list_semantics_and_errors(torch, lib):
     sc.tracer.object_count = 1
     rt = importlib.import_module("exposure-render_gb300.runtime")
     r = rt.Renderer(sc, lib)
-    assert lib.er_render_estimate(r.tracer_id) == 6                             # objects unsupported
+    # ObjectIDs.Count above the bound objects: only bound objects are walked
+    assert lib.er_render_estimate(r.tracer_id) == 0
     r.close()
     lib.er_reset()
 

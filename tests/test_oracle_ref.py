@@ -155,3 +155,17 @@ def test_surface_object_shapes(oracle, ref, shape):
     sc.objects[0].glossiness_texture_id = 2                     # luminance of a checker
     a, b = OL.SceneHandle(oracle, sc), OL.SceneHandle(ref, sc)
     assert np.array_equal(bits(a.render_sum(3, nthreads=4)), bits(b.render_sum(3, nthreads=4)))
+
+
+def test_bitmap_textures(oracle, ref):
+    """bitmap textures on a light and on objects (Source/textures.h:101-107,
+    Source/buffer2d.h:227-254) against the reference"""
+    sc = S.scene_bitmaps()
+    a, b = OL.SceneHandle(oracle, sc), OL.SceneHandle(ref, sc)
+    sa = a.render_sum(4, nthreads=4)
+    assert np.array_equal(bits(sa), bits(b.render_sum(4, nthreads=4)))
+    assert sa[..., :3].max() > 0
+    sc.tracer.settings.free_flight = 1
+    sc.tracer.settings.mis = 1
+    c = OL.SceneHandle(oracle, sc)
+    assert c.render_sum(2, nthreads=4)[..., :3].max() > 0
