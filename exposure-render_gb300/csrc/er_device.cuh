@@ -61,6 +61,9 @@ struct Light {               /* ErLight + Shape (Source/erlight.h, Source/shape.
     int texture_id;
     float multiplier;
     int unit;
+    int tex_const;           /* 1 when the light's texture does not vary over the surface (a uniform
+                                procedural texture, or none): tex_rgb is its value */
+    float tex_rgb[3];
 };
 
 struct Object {              /* ErObject (Source/erobject.h:27-67) */

@@ -444,7 +444,7 @@ ER_D void sample_light_surface(const Light& L, v3 UVW, Surf& SS)
    coordinate is an integer and black elsewhere, as the reference does. */
 ER_D uint8_t uc_weight(float w) { return (uint8_t)w; }
 
-ER_COLD c3 bitmap_xyz(const Bitmap& B, v2 uv)
+ER_D c3 bitmap_xyz(const Bitmap& B, v2 uv)
 {
     const int w = B.res[0], h = B.res[1];
     const float U = uv.x * (float)w, V = uv.y * (float)h;
@@ -507,6 +507,14 @@ ER_COLD c3 evaluate_texture(const Params& P, int id, v2 UV)
         L = bitmap_xyz(P.bitmaps[T.bitmap_id], t);
     }
     return cscale(L, T.output_level);
+}
+
+/* EvaluateTexture(L.TextureID, UV) of a light; uniform textures were
+   evaluated on the host (the same float products) */
+ER_D c3 light_texture(const Params& P, const Light& L, v2 UV)
+{
+    if (L.tex_const) return C3(L.tex_rgb[0], L.tex_rgb[1], L.tex_rgb[2]);
+    return evaluate_texture(P, L.texture_id, UV);
 }
 
 /* ---- shading: Source/shader.h ---- */
@@ -622,8 +630,13 @@ struct Event {
     float T;
     v3 P, N, Wo;
     c3 Le;
-    v2 UV;               /* object events: the surface parameters of the hit */
-    int object_id;       /* object events: index into the tracer's objects */
+};
+
+/* the surface of an object event (ScatterEvent::UV and ::ObjectID), kept
+   apart from Event so that volume-only code carries none of it */
+struct ObjHit {
+    v2 UV;
+    int id;
 };
 
 /* step budget of a fixed-step march: the loop ends after at most
@@ -704,7 +717,7 @@ ER_D void intersect_light(const Params& P, const Light& L, const Ray& R, Event& 
         SE.N = xform_vector(L.tm, Int.N);
         SE.T = vlen(vsub(SE.P, R.O));
         SE.Wo = vneg(R.D);
-        SE.Le = Int.front ? cscale(evaluate_texture(P, L.texture_id, Int.UV), L.multiplier) : C3(0, 0, 0);
+        SE.Le = Int.front ? cscale(light_texture(P, L, Int.UV), L.multiplier) : C3(0, 0, 0);
         if (L.unit == 1) SE.Le = cdivs(SE.Le, L.area);
     }
 }
@@ -748,7 +761,7 @@ ER_D bool intersects_light(const Params& P, const Ray& R)
 
 /* IntersectObject / IntersectObjects - Source/objects.h:26-62: the nearest of
    the tracer's objects (array order, ObjectID = index) */
-ER_D void intersect_objects(const Params& P, const Ray& R, Event& RS)
+ER_D void intersect_objects(const Params& P, const Ray& R, Event& RS, ObjHit& hit)
 {
     float T = FLT_MAX;
     for (int i = 0; i < P.object_count; i++) {
@@ -765,9 +778,7 @@ ER_D void intersect_objects(const Params& P, const Ray& R, Event& RS)
         local.T = vlen(vsub(local.P, R.O));
         local.Wo = vneg(R.D);
         local.Le = C3(0, 0, 0);
-        local.UV = Int.UV;
-        local.object_id = i;
-        if (local.T < T) { RS = local; T = local.T; }
+        if (local.T < T) { RS = local; T = local.T; hit.UV = Int.UV; hit.id = i; }
     }
 }
 
@@ -1004,7 +1015,7 @@ ER_D void sample_light(const Params& P, const Light& L, v3 uvw, Surf& SS, const 
 {
     sample_light_surface(L, uvw, SS);
     Wi = vnorm(vsub(SS.P, SE.P));
-    Le = cscale(evaluate_texture(P, L.texture_id, SS.UV), L.multiplier);
+    Le = cscale(light_texture(P, L, SS.UV), L.multiplier);
     if (L.one_sided && vdot(vsub(SE.P, SS.P), SS.N) < 0.0f) Le = C3(0, 0, 0);
     if (L.unit == 1) Le = cdivs(Le, L.area);
 }
@@ -1142,12 +1153,12 @@ ER_D c3 estimate_direct_light(const Params& P, const Light& L, int slot, const M
 /* the object shader of UniformSampleOneLight (Source/transport.h:141-149):
    BRDF with the object's diffuse and specular textures at the hit, IOR 15 and
    the exponent of the glossiness texture's luminance (ColorXYZf::Y) */
-ER_D void object_shader(const Params& P, const Event& SE, Shader& sh)
+ER_D void object_shader(const Params& P, const Event& SE, const ObjHit& hit, Shader& sh)
 {
-    const Object& O = P.objects[SE.object_id];
-    const c3 Kd = evaluate_texture(P, O.diffuse_texture_id, SE.UV);
-    const c3 Ks = evaluate_texture(P, O.specular_texture_id, SE.UV);
-    const c3 G = evaluate_texture(P, O.glossiness_texture_id, SE.UV);
+    const Object& O = P.objects[hit.id];
+    const c3 Kd = evaluate_texture(P, O.diffuse_texture_id, hit.UV);
+    const c3 Ks = evaluate_texture(P, O.specular_texture_id, hit.UV);
+    const c3 G = evaluate_texture(P, O.glossiness_texture_id, hit.UV);
     float Y = 0.0f;
     Y += 0.212671f * G.r;
     Y += 0.715160f * G.g;
@@ -1156,7 +1167,7 @@ ER_D void object_shader(const Params& P, const Event& SE, Shader& sh)
 }
 
 /* UniformSampleOneLight - Source/transport.h:115-156 (volume and object events) */
-ER_D c3 uniform_sample_one_light(const Params& P, const Event& SE, Rng& rng, const Metro& ms)
+ER_D c3 uniform_sample_one_light(const Params& P, const Event& SE, Rng& rng, const Metro& ms, const ObjHit& hit)
 {
     c3 Ld = C3(0, 0, 0);
     const float I = get_intensity(P, SE.P);
@@ -1167,7 +1178,7 @@ ER_D c3 uniform_sample_one_light(const Params& P, const Event& SE, Rng& rng, con
     const Light& L = P.lights[idx];
     Shader sh;
     if (SE.type == 2) {
-        object_shader(P, SE, sh);
+        object_shader(P, SE, hit, sh);
     } else {
         const int type = P.apply_shading_type ? select_shader_type(P, SE, I, rng) : 0;
         shader_init(sh, type, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
@@ -1209,18 +1220,20 @@ ER_D float4 single_scattering(const Params& P, int x, int y, Rng& rng)
     se0.P = V3(0, 0, 0); se0.N = V3(0, 0, 0); se0.Wo = V3(0, 0, 0);
     se1 = se0; se1.type = 1;
     se2.type = 2; se2.valid = false; se2.T = 0.0f;
+    ObjHit hit;
+    hit.UV.x = 0.0f; hit.UV.y = 0.0f; hit.id = 0;
     if (P.free_flight == 1) sample_volume_delta(P, R, rng, se0);
     else sample_volume(P, R, rng, se0);
     intersect_lights(P, R, se1, true);
-    if (P.object_count > 0) intersect_objects(P, R, se2);
+    if (P.object_count > 0) intersect_objects(P, R, se2, hit);
     SE = se0; SE.valid = false; SE.type = 0;
     float T = FLT_MAX;
     if (se0.valid && se0.T < T) { SE = se0; T = se0.T; }
     if (se1.valid && se1.T < T) { SE = se1; T = se1.T; }
     if (se2.valid && se2.T < T) { SE = se2; T = se2.T; }
-    if (SE.valid && SE.type == 0) Lv = cadd(Lv, uniform_sample_one_light(P, SE, rng, ms));
+    if (SE.valid && SE.type == 0) Lv = cadd(Lv, uniform_sample_one_light(P, SE, rng, ms, hit));
     if (SE.valid && SE.type == 1) Lv = cadd(Lv, SE.Le);
-    if (SE.valid && SE.type == 2) Lv = cadd(Lv, uniform_sample_one_light(P, SE, rng, ms));
+    if (SE.valid && SE.type == 2) Lv = cadd(Lv, uniform_sample_one_light(P, SE, rng, ms, hit));
     return make_float4(Lv.r, Lv.g, Lv.b, SE.valid ? 1.0f : 0.0f);
 }
 

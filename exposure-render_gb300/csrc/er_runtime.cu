@@ -517,6 +517,26 @@ er_status build(TracerItem& t)
         to_light(L[i], *it->second);
         valid[i] = 1;
     }
+    /* lights whose texture is uniform (or unbound: black) get its value here,
+       as EvaluateTexture computes it: colour * OutputLevel in float
+       (Source/textures.h:63-111) */
+    for (int i = 0; i < lc; i++) {
+        if (!valid[i]) continue;
+        erd::Light& l = L[i];
+        l.tex_const = 0;
+        auto tt = C.textures.items.find(l.texture_id);
+        if (l.texture_id < 0 || tt == C.textures.items.end()) {
+            l.tex_const = 1;
+            l.tex_rgb[0] = l.tex_rgb[1] = l.tex_rgb[2] = 0.0f;
+        } else if (tt->second->type == ER_TEXTURE_PROCEDURAL && tt->second->procedural.type == ER_PROCEDURAL_UNIFORM) {
+            const volatile float lvl = tt->second->output_level;
+            l.tex_const = 1;
+            for (int c = 0; c < 3; c++) {
+                const volatile float u = tt->second->procedural.uniform_color[c];
+                l.tex_rgb[c] = u * lvl;
+            }
+        }
+    }
     std::vector<int> lids((size_t)std::max(lc, 1), -1);
     for (int i = 0; i < lc; i++) lids[i] = d.light_ids[i];
     ER_CUDA(t.lights.ensure(L.size()));

@@ -101,6 +101,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
         const bool live = i < items;
         bool push = false;
         Event SE;
+        ObjHit hit;
         Metro ms;
         Rng rng;
         rng.s0 = 0u;
@@ -134,7 +135,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
             if (OBJ && P.object_count > 0) {
                 Event se2;
                 se2.type = 2; se2.valid = false; se2.T = 0.0f;
-                intersect_objects(P, R, se2);
+                intersect_objects(P, R, se2, hit);
                 if (se2.valid && se2.T < T) { SE = se2; T = se2.T; }
             }
             if (!SE.valid) {
@@ -147,14 +148,14 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
                 /* an object event parks its surface parameters in the sample's
                    result slot, which the shade stage reads before it writes
                    the sample's value there */
-                if (SE.type == 2) results[i] = make_float4(SE.UV.x, SE.UV.y, u2f((uint32_t)SE.object_id), 0.0f);
+                if (OBJ && SE.type == 2) results[i] = make_float4(hit.UV.x, hit.UV.y, u2f((uint32_t)hit.id), 0.0f);
             }
         }
         const uint32_t slot = queue_slot(push, n_events);
         if (push) {
             /* volume events: the normal is computed by the shade stage; object
                events carry theirs and set the top bit of the view word */
-            const bool obj = SE.type == 2;
+            const bool obj = OBJ && SE.type == 2;
             float4* e = events + (size_t)slot * 5;
             e[0] = make_float4(u2f(i), u2f(rng.s0), u2f(rng.s1), ms.light_num);
             e[1] = make_float4(SE.P.x, SE.P.y, SE.P.z, ms.brdf_component);
@@ -198,7 +199,7 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict
             rng.s0 = f2u(e0.y);
             rng.s1 = f2u(e0.z);
             const uint32_t vw = f2u(e4.w);
-            v = vw & ~WF_OBJECT_EVENT;
+            v = OBJ ? (vw & ~WF_OBJECT_EVENT) : vw;
             const bool obj = OBJ && (vw & WF_OBJECT_EVENT) != 0u;
             const Params& P = view_of<ONE>(views, one, v).P;
             Metro ms;
@@ -213,12 +214,13 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict
                central differences its six intensities also give the gradient
                magnitude of the shader switch */
             float gm = -1.0f;
+            ObjHit hit;
             if (obj) {
                 const float4 o = results[sample];
                 SE.type = 2;
-                SE.UV.x = o.x;
-                SE.UV.y = o.y;
-                SE.object_id = (int)f2u(o.z);
+                hit.UV.x = o.x;
+                hit.UV.y = o.y;
+                hit.id = (int)f2u(o.z);
                 SE.N = V3(e2.x, e2.y, e2.z);
             } else if (P.gradient_mode == 1) {
                 Grad6 g6;
@@ -245,7 +247,7 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict
                 const Light& L = P.lights[idx];
                 Shader sh;
                 if (obj) {
-                    object_shader(P, SE, sh);
+                    object_shader(P, SE, hit, sh);
                 } else {
                     const int type = P.apply_shading_type ? select_shader_type(P, SE, I, rng, gm) : 0;
                     shader_init(sh, type, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
