@@ -1,10 +1,13 @@
 """Throughput benchmark of the GB300 transport path.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload c2|c1]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload c2|c1|c3|c4|c5]
 
 A step is one full render of the workload: every pixel of the film at the
 configured samples per pixel (c2: 1024x1024 x 256 spp over the 512^3 CT-like
-shell volume; c1: 256x256 x 64 spp over the 128^3 blob volume).  Inputs are
+shell volume; c1: 256x256 x 64 spp over the 128^3 blob volume; c3: 64 views
+over three blob volumes in one batch; c4: the differentiable medium's
+forward and adjoint; c5: 16 views of 2048^2 x 64 spp over a 1024x1024x512
+volume in one batch, plus the adjoint on a 256^3 block of it).  Inputs are
 seeded synthetic volumes (the reference ships no dataset).
 
 value : samples/s of the transport kernel with the scene resident in HBM,
@@ -455,7 +458,7 @@ def run_ours(args, wl, rank, world, local_rank):
     if rank != 0:
         return
     conv = None
-    if world == 1 and not args.no_rmse:
+    if world == 1 and not args.no_rmse and wl == "c3":
         conv = convergence(lib, runtime, torch, ["c2"], {
             "fast": {"free_flight": 1, "majorant_brick": r.tracer_desc.settings.majorant_brick},
             "plain": {"free_flight": 0}})
@@ -498,10 +501,12 @@ def run_ours(args, wl, rank, world, local_rank):
     r.close()
 
 
-def run_batched(args, rank, world, local_rank):
-    """c3: 64 orbit views over three blob volumes, one CUDA-graph launch per
-    step (er_batch_launch), against the same views rendered one batch per view
-    and against the reference estimator one view and one frame at a time."""
+def run_batched(args, rank, world, local_rank, wl="c3"):
+    """c3: 64 orbit views over three blob volumes; c5: 16 orbit views of 2048^2
+    at 64 spp over the 1024x1024x512 volume, plus the path-replay adjoint on
+    a 256^3 density sub-block of it.  One CUDA-graph launch per step
+    (er_batch_launch), against the same views rendered one batch per view and
+    against the reference estimator one view and one frame at a time."""
     import torch
     torch.cuda.set_device(local_rank)
     runtime = importlib.import_module("exposure-render_gb300.runtime")
@@ -512,14 +517,21 @@ def run_batched(args, rank, world, local_rank):
     stream = torch.cuda.current_stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
     C.check(lib.er_set_stream(sp))
-    scenes = S.c3_scenes()
+    c5_vol = None
+    if wl == "c5":
+        t_gen = time.perf_counter()
+        c5_vol = S.c5_volume()
+        gen_s = time.perf_counter() - t_gen
+        scenes = [S.scene_c5(c5_vol)]
+    else:
+        scenes = S.c3_scenes()
     for sc in scenes:
         sc.tracer.settings.seed = R.view_seed(1, rank)
     dist = None
     if world > 1:
         import torch.distributed as dist
     rs = [runtime.Renderer(sc, lib) for sc in scenes]
-    views = S.c3_views(n_views=args.views)
+    views = S.c5_views(n_views=args.views or 16) if wl == "c5" else S.c3_views(n_views=args.views or 64)
     # autotune each volume's tracer on one of its views (probe: 2 spp)
     tuned = []
     for k, r in enumerate(rs):
@@ -580,7 +592,8 @@ def run_batched(args, rank, world, local_rank):
     # plain: the reference estimator (fixed-step march, light sampling, BRDF),
     # one frame of 1 spp per call (RenderEstimate), one view at a time
     plain_samples, plain_ms = 0, 0.0
-    for (k, cam, spp) in views[: args.plain_views]:
+    n_plain = args.plain_views if args.plain_views is not None else (4 if wl == "c5" else 16)
+    for (k, cam, spp) in views[:n_plain]:
         r = rs[k]
         saved = C.er_tracer_desc.from_buffer_copy(r.tracer_desc)
         r.tracer_desc.camera = cam
@@ -597,7 +610,7 @@ def run_batched(args, rank, world, local_rank):
 
     # equal-RMSE comparison on the first view of each volume (128^2, FP64 references)
     conv = None
-    if world == 1 and not args.no_rmse:
+    if world == 1 and not args.no_rmse and wl == "c3":
         conv = convergence(lib, runtime, torch, ["c3v0", "c3v1", "c3v2"],
                            {"fast": {"free_flight": 1}, "plain": {"free_flight": 0}})
 
@@ -622,6 +635,14 @@ def run_batched(args, rank, world, local_rank):
         e2e_step()
     e2e_s = R.max_over_ranks(time.perf_counter() - t0, dist)
     e2e_value = R.whole_job_rate(samples_per_step * e2e_steps, e2e_s, world) / 1e6
+    d2h_bytes = int(sum(h.numel() * 4 for h in host_sums))
+    adjoint = None
+    if wl == "c5":
+        # the batch's queues and films are released before the adjoint's buffers are made
+        batch.close()
+        del sums, host_sums, table
+        torch.cuda.empty_cache()
+        adjoint = c5_adjoint(args, lib, runtime, torch, stream, c5_vol)
     if rank != 0:
         return
     vol_bytes = sum(sc.volume.nbytes for sc in scenes)
@@ -629,7 +650,8 @@ def run_batched(args, rank, world, local_rank):
         "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "c3-batched-%d-views-3-blob-volumes" % len(views), "views": len(views),
+        "config": {"workload": ("c5-batched-%d-views-2048^2-1024x1024x512-volume" % len(views)) if wl == "c5" else
+                   ("c3-batched-%d-views-3-blob-volumes" % len(views)), "views": len(views),
                    "samples_per_step": samples_per_step, "films": sorted({c.film_size[0] for _, c, _ in views}),
                    "spp_range": [min(s for _, _, s in views), max_spp], **describe_shading(scenes[0]),
                    "windows": info["windows"], "segments": info["segments"], "queue_bytes": info["queue_bytes"],
@@ -637,21 +659,84 @@ def run_batched(args, rank, world, local_rank):
                    "l2": "volumes %d MiB in total; every step renders fresh samples" % (vol_bytes >> 20),
                    "parallelism": "replicas" if world > 1 else "single"},
         "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(vol_bytes),
-                "d2h_bytes_per_step": int(sum(h.numel() * 4 for h in host_sums))},
+                "d2h_bytes_per_step": d2h_bytes},
         "clocks": clk.summary(),
         "gpu_launches": args.steps * (4 * info["windows"]),
         "stages": {n: {"ms": float(stage_ms[i]), "share": float(stage_ms[i] / max(stage_ms.sum(), 1e-9)),
                        "launches": int(stage_launches[i])} for i, n in enumerate(("primary", "shade", "shadow", "reduce"))},
         "profiled_pass_ms": prof_ms,
         "one_batch_per_view": {"value": seq_value, "unit": "Msamples/s", "speedup": value / seq_value},
-        "plain": {"value": plain_value, "unit": "Msamples/s", "speedup": value / plain_value, "views": args.plain_views,
+        "plain": {"value": plain_value, "unit": "Msamples/s", "speedup": value / plain_value, "views": n_plain,
                   "what": "reference estimator (march, light sampling, BRDF), 1 spp per RenderEstimate, one view at a time"},
-        "equal_rmse": batched_rmse_summary(conv, value, plain_value),
+        "equal_rmse": batched_rmse_summary(conv, value, plain_value) if wl == "c3" else
+        {"throughput_ratio": value / plain_value, "note": "no FP64 reference of the c5 volume: samples-to-RMSE ratios are measured on c2 and c3"},
     }
+    if wl == "c5":
+        line["volume_generation_s"] = gen_s
+        line["adjoint"] = adjoint
     print(json.dumps(line), flush=True)
-    batch.close()
+    if wl != "c5":
+        batch.close()
     for r in rs:
         r.close()
+
+
+def c5_adjoint(args, lib, runtime, torch, stream, vol, film=(2048, 2048), spp=8, size=256):
+    """c5's adjoint: the differentiable medium on the centred 256^3 block of
+    the c5 volume (a float density window) with a 64-value opacity spline, one
+    2048^2 view at 8 spp; forward, adjoint with the forward's samples kept,
+    and adjoint with seed-replay recomputation (nothing kept)"""
+    medium = importlib.import_module("exposure-render_gb300.medium")
+    S = importlib.import_module("exposure-render_gb300.scenes")
+    rho = torch.from_numpy(S.density_subblock(vol, size)).cuda()
+    tf = torch.from_numpy(S.ramp_opacity(64)).cuda()
+    sc = S.medium_scene(res=(size, size, size), film=film)
+    r = runtime.Renderer(sc, lib)
+    m = medium.Medium(r, rho, tf, 40.0, albedo=(0.8, 0.7, 0.6), nee_probability=0.5, brick=8)
+    target = torch.zeros((film[1], film[0], 3), device="cuda")
+
+    def timed(fn, steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / steps
+
+    state = {}
+
+    def fwd():
+        state["smp"], state["s"] = m.render_samples(rho, tf, spp)
+
+    def bwd():
+        d = 2.0 * (state["s"] / spp - target) / spp / target.numel()
+        state["g"] = m.adjoint(rho, tf, spp, d, state["smp"])
+
+    def bwd_recompute():
+        d = 2.0 * (state["s"] / spp - target) / spp / target.numel()
+        state["g2"] = m.adjoint(rho, tf, spp, d, None)
+
+    steps = max(1, min(args.steps, 2))
+    for _ in range(max(1, min(args.warmup, 2))):
+        fwd()
+        bwd()
+    torch.cuda.synchronize()
+    f_ms = timed(fwd, steps)
+    b_ms = timed(bwd, steps)
+    br_ms = timed(bwd_recompute, 1)
+    # the adjoints gather with atomics, so the two agree to float summation order
+    rel = max(float((state["g"][i] - state["g2"][i]).norm() / max(float(state["g"][i].norm()), 1e-30)) for i in range(2))
+    out = {"what": "differentiable medium on the centred %d^3 block of the c5 volume, 64 opacity values, %dx%d x %d spp"
+                   % (size, film[0], film[1], spp),
+           "samples": film[0] * film[1] * spp, "forward_ms": f_ms, "adjoint_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
+           "adjoint_recompute_ms": br_ms, "adjoint_recompute_over_forward": br_ms / f_ms,
+           "forward_msamples_per_s": film[0] * film[1] * spp / (f_ms / 1e3) / 1e6,
+           "recompute_vs_kept_rel_diff": rel,
+           "grad_norm": {"density": float(state["g"][0].norm()), "opacity": float(state["g"][1].norm())}}
+    del state
+    r.close()
+    return out
 
 
 def run_medium(args, rank, world, local_rank):
@@ -750,9 +835,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3", "c4"])
-    ap.add_argument("--views", type=int, default=64, help="c3: number of views")
-    ap.add_argument("--plain-views", type=int, default=16, help="c3: views timed on the plain one-view path")
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3", "c4", "c5"])
+    ap.add_argument("--views", type=int, default=0, help="c3/c5: number of views (0: 64 for c3, 16 for c5)")
+    ap.add_argument("--plain-views", type=int, default=None, help="c3/c5: views timed on the plain one-view path (16 / 4)")
     ap.add_argument("--film", type=int, default=0, help="square film edge (smaller profiling cases; 0 = the workload's)")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel (0 = the workload's)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default settings)")
@@ -770,8 +855,8 @@ def main():
     if args.impl == "reference":
         run_reference(args, args.workload, rank, world)
         return
-    if args.workload == "c3":
-        run_batched(args, rank, world, local_rank)
+    if args.workload in ("c3", "c5"):
+        run_batched(args, rank, world, local_rank, args.workload)
         return
     if args.workload == "c4":
         run_medium(args, rank, world, local_rank)

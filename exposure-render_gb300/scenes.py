@@ -352,6 +352,88 @@ def c3_views(n_views=64, n_volumes=3, seed=7, films=C3_FILMS, spp=(32, 128)) -> 
 
 
 # ---------------------------------------------------------------------------
+# large batched forward + adjoint (c5)
+# ---------------------------------------------------------------------------
+
+C5_SHAPE = (512, 1024, 1024)     # (z, y, x): 1024 x 1024 x 512 voxels, 1 GiB of uint16
+
+
+def c5_volume(shape_zyx=C5_SHAPE, seed=5, noise_sigma=30.0, n_blobs=24) -> np.ndarray:
+    """Shells in a soft-tissue ellipsoid (the c2 design on a 2:2:1 grid) plus
+    `n_blobs` Gaussian blobs of amplitude 500-4000 inside it, with Gaussian
+    noise inside the ellipsoid; uint16, x fastest.  Built slab by slab in
+    float32."""
+    Z, Y, X = shape_zyx
+    rng = np.random.default_rng(seed)
+    ext = np.array([X, Y, Z], dtype=np.float64)
+    centres = rng.uniform(0.3, 0.7, size=(n_blobs, 3)) * ext
+    sig = rng.uniform(0.02, 0.06, size=(n_blobs, 3)) * ext
+    amps = rng.uniform(500.0, 4000.0, size=n_blobs)
+    xs = np.arange(X, dtype=np.float32)
+    ys = np.arange(Y, dtype=np.float32)
+    gx = [np.exp(-0.5 * ((xs - centres[k, 0]) / sig[k, 0]) ** 2).astype(np.float32) for k in range(n_blobs)]
+    gy = [np.exp(-0.5 * ((ys - centres[k, 1]) / sig[k, 1]) ** 2).astype(np.float32) * np.float32(amps[k]) for k in range(n_blobs)]
+    # each blob's support (values above 1e-4 of its amplitude)
+    boxes = []
+    for k in range(n_blobs):
+        ry = np.nonzero(gy[k] > 1e-4 * amps[k])[0]
+        rx = np.nonzero(gx[k] > 1e-4)[0]
+        boxes.append(((int(ry[0]), int(ry[-1]) + 1), (int(rx[0]), int(rx[-1]) + 1)))
+    out = np.empty((Z, Y, X), dtype=np.uint16)
+    # normalised coordinates: the longest axis spans [-0.5, 0.5]
+    L = float(max(X, Y, Z))
+    nx = (xs - (X - 1) / 2.0) / np.float32(L)
+    ny = (ys - (Y - 1) / 2.0) / np.float32(L)
+    PX, PY = np.meshgrid(nx, ny, indexing="xy")
+    base = (PX / 0.46) ** 2 + (PY / 0.40) ** 2
+    rxy = PX * PX + PY * PY
+    for zi in range(Z):
+        z = np.float32((zi - (Z - 1) / 2.0) / L)
+        ell = base + (z / 0.22) ** 2 <= 1.0
+        r = np.sqrt(rxy + z * z)
+        v = np.where(ell, np.float32(1000.0), np.float32(0.0)).astype(np.float32)
+        v = np.where((r >= 0.16) & (r < 0.19), np.float32(1400.0), v)
+        v = np.where((r >= 0.08) & (r < 0.11), np.float32(2500.0), v)
+        for k in range(n_blobs):
+            gz = np.float32(np.exp(-0.5 * ((zi - centres[k, 2]) / sig[k, 2]) ** 2))
+            if gz > 1e-4:
+                (y0, y1), (x0, x1) = boxes[k]
+                v[y0:y1, x0:x1] += (gy[k][y0:y1, None] * gx[k][None, x0:x1]) * gz
+        v = v + np.where(ell, rng.standard_normal(size=v.shape, dtype=np.float32) * np.float32(noise_sigma), np.float32(0.0))
+        out[zi] = np.clip(np.floor(v), 0, 65535).astype(np.uint16)
+    return out
+
+
+def scene_c5(volume=None, film=(2048, 2048), spp=64) -> Scene:
+    """The c5 volume under the c2 tracer (16-node transfer function, hybrid
+    shader, full MIS, two area lights and an environment sphere) with delta
+    tracking; the views override its camera."""
+    vol = c5_volume() if volume is None else volume
+    lights, textures = c2_lights()
+    t = c2_tracer(film)
+    t.settings.free_flight = C.FREE_FLIGHT_DELTA
+    t.settings.bilateral = 0
+    t.settings.seed = 5
+    return Scene("c5", vol, tracer=t, lights=lights, textures=textures, spp=spp)
+
+
+def c5_views(n_views=16, film=2048, spp=64, seed=11) -> list:
+    """(volume index 0, orbit camera, spp) of the c5 views"""
+    rng = np.random.default_rng(seed)
+    return [(0, orbit_camera(rng, (film, film), radius=float(rng.uniform(1.6, 2.2))), spp) for _ in range(n_views)]
+
+
+def density_subblock(volume, size=256, lo=800.0, hi=3000.0) -> np.ndarray:
+    """The centred size^3 block of a uint16 volume as a float density in
+    [0, 1] (a linear window from lo to hi), the parameter grid of the c5
+    adjoint."""
+    Z, Y, X = volume.shape
+    z0, y0, x0 = (Z - size) // 2, (Y - size) // 2, (X - size) // 2
+    b = volume[z0:z0 + size, y0:y0 + size, x0:x0 + size].astype(np.float32)
+    return np.ascontiguousarray(np.clip((b - lo) / (hi - lo), 0.0, 1.0), dtype=np.float32)
+
+
+# ---------------------------------------------------------------------------
 # views with converged FP64 references (image RMSE measurements)
 # ---------------------------------------------------------------------------
 
