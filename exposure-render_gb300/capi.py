@@ -395,6 +395,8 @@ def _declare(lib) -> None:
         "er_unbind_tracer": (c_int32, [c_int32]),
         "er_bind_volume": (c_int32, [POINTER(er_volume_desc), i32p]),
         "er_unbind_volume": (c_int32, [c_int32]),
+        "er_update_volume_region": (c_int32, [c_int32, POINTER(c_int32), POINTER(c_int32), c_void_p]),
+        "er_update_volume_region_device": (c_int32, [c_int32, POINTER(c_int32), POINTER(c_int32), c_void_p, c_void_p]),
         "er_bind_light": (c_int32, [POINTER(er_light_desc), i32p]),
         "er_unbind_light": (c_int32, [c_int32]),
         "er_bind_object": (c_int32, [POINTER(er_object_desc), i32p]),

@@ -59,6 +59,10 @@ cudaError_t er_launch_dm_majorant(const float* rho, const int res[3], int B, con
 
 /* corner quads of a uint16 volume (8 bytes per voxel) */
 cudaError_t er_launch_quads(const uint16_t* vox, const int res[3], uint2* quad, cudaStream_t s);
+/* corner quads (quad may be NULL) and atomicMax of the voxel values over the
+   box [lo, lo + n) */
+cudaError_t er_launch_box_quads_max(const uint16_t* vox, const int res[3], const int lo[3], const int n[3], uint2* quad,
+                                    unsigned int* vmax, cudaStream_t s);
 
 /* sets the text returned by er_last_error_message() on this thread */
 void er_internal_set_error(const char* message);

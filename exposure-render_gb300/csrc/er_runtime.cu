@@ -163,6 +163,7 @@ struct VolumeItem {
     DevBuf<uint16_t> vox;
     DevBuf<uint2> quad;            /* corner quads (NULL when they do not fit in memory) */
     DevBuf<unsigned int> gm_max_bits;
+    DevBuf<unsigned int> box_max;  /* largest voxel of an uploaded box */
     float gm_max = -1.0f;          /* lazily computed maximum gradient magnitude */
 };
 
@@ -1011,6 +1012,31 @@ ER_API void er_plf_add_node(er_plf* p, float position, float value)
 
 /* ---- bind lists ---- */
 
+/* Copies the box [lo, lo + n) of voxels (x fastest, packed) from host or
+   device memory into a bound volume, refreshes the corner quads it changes
+   (one voxel below the box in x and y as well) and returns the largest voxel
+   of the refreshed box.  Synchronous. */
+er_status upload_box(VolumeItem& v, const int lo[3], const int n[3], const uint16_t* src, cudaMemcpyKind kind, cudaStream_t s,
+                     unsigned int* box_max)
+{
+    cudaMemcpy3DParms p;
+    memset(&p, 0, sizeof(p));
+    p.srcPtr = make_cudaPitchedPtr((void*)src, (size_t)n[0] * sizeof(uint16_t), (size_t)n[0], (size_t)n[1]);
+    p.dstPtr = make_cudaPitchedPtr(v.vox.p, (size_t)v.res[0] * sizeof(uint16_t), (size_t)v.res[0], (size_t)v.res[1]);
+    p.dstPos = make_cudaPos((size_t)lo[0] * sizeof(uint16_t), (size_t)lo[1], (size_t)lo[2]);
+    p.extent = make_cudaExtent((size_t)n[0] * sizeof(uint16_t), (size_t)n[1], (size_t)n[2]);
+    p.kind = kind;
+    ER_CUDA(cudaMemcpy3DAsync(&p, s));
+    int qlo[3] = { lo[0] > 0 ? lo[0] - 1 : 0, lo[1] > 0 ? lo[1] - 1 : 0, lo[2] };
+    int qn[3] = { n[0] + (lo[0] - qlo[0]), n[1] + (lo[1] - qlo[1]), n[2] };
+    ER_CUDA(v.box_max.ensure(1));
+    ER_CUDA(cudaMemsetAsync(v.box_max.p, 0, sizeof(unsigned int), s));
+    ER_CUDA(er_launch_box_quads_max(v.vox.p, v.res, qlo, qn, v.quad.p, v.box_max.p, s));
+    ER_CUDA(cudaMemcpyAsync(box_max, v.box_max.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+    ER_CUDA(cudaStreamSynchronize(s));
+    return ER_OK;
+}
+
 ER_API er_status er_bind_volume(const er_volume_desc* d, int32_t* id)
 {
     ER_LOCK;
@@ -1023,30 +1049,82 @@ ER_API er_status er_bind_volume(const er_volume_desc* d, int32_t* id)
     bool is_new = false;
     er_status st = reserve_id(C.volumes, id, &is_new);
     if (st != ER_OK) return st;
-    std::unique_ptr<VolumeItem> v(new VolumeItem());
+    /* a rebind of an ID at the same resolution refills its buffers in place
+       (after the work queued on them); otherwise a new item is made */
+    std::unique_ptr<VolumeItem> fresh;
+    VolumeItem* v = nullptr;
+    if (!is_new) {
+        VolumeItem& old = *C.volumes.items[*id];
+        if (old.res[0] == d->resolution[0] && old.res[1] == d->resolution[1] && old.res[2] == d->resolution[2]) {
+            ER_CUDA(cudaStreamSynchronize(C.stream));
+            v = &old;
+        }
+    }
+    const size_t n = (size_t)d->resolution[0] * d->resolution[1] * d->resolution[2];
+    if (!v) {
+        fresh.reset(new VolumeItem());
+        v = fresh.get();
+        ER_CUDA(v->vox.ensure(n));
+        /* corner quads for the transport's lookups; without room for them the
+           kernels read the plain voxels (same values, more loads) */
+        if (v->quad.ensure(n) != cudaSuccess) cudaGetLastError();
+    }
     for (int i = 0; i < 3; i++) { v->res[i] = d->resolution[i]; v->spacing[i] = d->spacing[i]; }
     v->normalize = d->normalize_size;
-    const size_t n = (size_t)d->resolution[0] * d->resolution[1] * d->resolution[2];
-    uint16_t vmax = 0;
-    for (size_t i = 0; i < n; i++) vmax = d->voxels[i] > vmax ? d->voxels[i] : vmax;
-    v->vmax = vmax;
+    v->gm_max = -1.0f;
     /* content signature of the tuning cache: every 61st voxel */
     uint64_t sig = fnv1a(kFnvBasis, d->resolution, sizeof(d->resolution));
     for (size_t i = 0; i < n; i += 61) sig = fnv1a(sig, &d->voxels[i], sizeof(uint16_t));
     v->signature = sig;
-    ER_CUDA(v->vox.ensure(n));
-    ER_CUDA(cudaMemcpy(v->vox.p, d->voxels, n * sizeof(uint16_t), cudaMemcpyHostToDevice));
-    /* corner quads for the transport's lookups; without room for them the
-       kernels read the plain voxels (same values, more loads) */
-    if (v->quad.ensure(n) == cudaSuccess) {
-        ER_CUDA(er_launch_quads(v->vox.p, v->res, v->quad.p, 0));
-        ER_CUDA(cudaDeviceSynchronize());
-    } else {
-        cudaGetLastError();
-    }
-    C.volumes.items[*id] = std::move(v);
+    const int lo[3] = { 0, 0, 0 };
+    unsigned int vmax = 0;
+    er_status us = upload_box(*v, lo, d->resolution, d->voxels, cudaMemcpyHostToDevice, C.stream, &vmax);
+    if (us != ER_OK) return us;
+    v->vmax = (uint16_t)vmax;
+    if (fresh) C.volumes.items[*id] = std::move(fresh);
     C.version++;
     return ER_OK;
+}
+
+/* shared by the host and device variants of the region update */
+static er_status update_volume_region(int32_t id, const int32_t* offset, const int32_t* size, const uint16_t* voxels,
+                                      cudaMemcpyKind kind, cudaStream_t s)
+{
+    Context& C = ctx();
+    auto it = C.volumes.items.find(id);
+    if (id < 0 || it == C.volumes.items.end()) return fail(ER_ERR_INVALID_ID, "volume ID:%d does not exist", id);
+    if (!offset || !size || !voxels) return fail(ER_ERR_INVALID_ARGUMENT, "offset, size or voxel pointer is NULL");
+    VolumeItem& v = *it->second;
+    for (int i = 0; i < 3; i++) {
+        if (offset[i] < 0 || size[i] <= 0 || (int64_t)offset[i] + size[i] > v.res[i])
+            return fail(ER_ERR_INVALID_ARGUMENT, "region [%d, %d) on axis %d is outside the volume's [0, %d)", offset[i],
+                        offset[i] + size[i], i, v.res[i]);
+    }
+    /* the volume may be read by queued work: the edit follows it */
+    ER_CUDA(cudaStreamSynchronize(C.stream));
+    unsigned int bmax = 0;
+    er_status us = upload_box(v, offset, size, voxels, kind, s, &bmax);
+    if (us != ER_OK) return us;
+    if (bmax > v.vmax) v.vmax = (uint16_t)bmax;
+    v.gm_max = -1.0f;
+    v.signature = fnv1a(v.signature, offset, 3 * sizeof(int32_t));
+    v.signature = fnv1a(v.signature, size, 3 * sizeof(int32_t));
+    C.version++;
+    return ER_OK;
+}
+
+ER_API er_status er_update_volume_region(int32_t volume_id, const int32_t offset[3], const int32_t size[3], const uint16_t* voxels)
+{
+    ER_LOCK;
+    return update_volume_region(volume_id, offset, size, voxels, cudaMemcpyHostToDevice, ctx().stream);
+}
+
+ER_API er_status er_update_volume_region_device(int32_t volume_id, const int32_t offset[3], const int32_t size[3],
+                                                const uint16_t* d_voxels, void* stream)
+{
+    ER_LOCK;
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx().stream;
+    return update_volume_region(volume_id, offset, size, d_voxels, cudaMemcpyDeviceToDevice, s);
 }
 
 ER_API er_status er_unbind_volume(int32_t id) { ER_LOCK; return unbind(ctx().volumes, id); }

@@ -128,6 +128,42 @@ cudaError_t er_launch_quads(const uint16_t* vox, const int res[3], uint2* quad, 
     return cudaGetLastError();
 }
 
+/* the corner quads of the voxels in the box [lo, lo + n) (a region edit
+   changes the quads of the voxels one below it in x and y as well) and the
+   largest voxel value in the box */
+__global__ void k_box_quads_max(const uint16_t* __restrict__ vox, int rx, int ry, int x0, int y0, int z0, int nx, int ny, int nz,
+                                uint2* __restrict__ quad, unsigned int* __restrict__ vmax)
+{
+    const size_t n = (size_t)nx * ny * nz;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    unsigned int m = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int x = x0 + (int)(i % nx), y = y0 + (int)((i / nx) % ny), z = z0 + (int)(i / ((size_t)nx * ny));
+        const size_t zb = (size_t)z * rx * ry;
+        const int x1 = x + 1 < rx ? x + 1 : rx - 1, y1 = y + 1 < ry ? y + 1 : ry - 1;
+        const uint32_t v00 = vox[zb + (size_t)y * rx + x], v10 = vox[zb + (size_t)y * rx + x1];
+        const uint32_t v01 = vox[zb + (size_t)y1 * rx + x], v11 = vox[zb + (size_t)y1 * rx + x1];
+        if (quad) quad[zb + (size_t)y * rx + x] = make_uint2(v00 | (v10 << 16), v01 | (v11 << 16));
+        m = v00 > m ? v00 : m;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned int t = __shfl_xor_sync(0xffffffffu, m, o);
+        m = t > m ? t : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(vmax, m);
+}
+
+cudaError_t er_launch_box_quads_max(const uint16_t* vox, const int res[3], const int lo[3], const int n[3], uint2* quad,
+                                    unsigned int* vmax, cudaStream_t s)
+{
+    const size_t total = (size_t)n[0] * n[1] * n[2];
+    if (total == 0) return cudaSuccess;
+    size_t blocks = (total + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    k_box_quads_max<<<(unsigned)blocks, 256, 0, s>>>(vox, res[0], res[1], lo[0], lo[1], lo[2], n[0], n[1], n[2], quad, vmax);
+    return cudaGetLastError();
+}
+
 /* ====================================================================== */
 /* Allocation-free majorant build                                           */
 /* ====================================================================== */

@@ -275,6 +275,20 @@ ER_API er_status er_unbind_tracer(int32_t id);
 /* BindVolume - Source/exposurerender.h:33 */
 ER_API er_status er_bind_volume(const er_volume_desc* desc, int32_t* id);
 ER_API er_status er_unbind_volume(int32_t id);
+/* Partial re-upload of a bound volume (no counterpart in the reference, which
+   re-uploads every voxel of every bound volume on each bind,
+   Source/list.cuh:115-133): the box [offset, offset + size) of the volume
+   (voxel units, x fastest) receives `voxels`, size[0]*size[1]*size[2] values
+   packed x fastest.  The corner quads of the edited voxels, the maximum
+   voxel, the gradient-magnitude range and every tracer's sigma table and
+   majorant grid over this volume are refreshed; renders afterwards equal
+   those of a fresh bind of the edited volume.  Waits for work queued on the
+   volume.  ER_ERR_INVALID_ARGUMENT when the box leaves the volume. */
+ER_API er_status er_update_volume_region(int32_t volume_id, const int32_t offset[3], const int32_t size[3], const uint16_t* voxels);
+/* The same with the box's voxels in device memory, copied on `stream`
+   (NULL: the library's stream). */
+ER_API er_status er_update_volume_region_device(int32_t volume_id, const int32_t offset[3], const int32_t size[3],
+                                                const uint16_t* d_voxels, void* stream);
 /* BindLight - Source/exposurerender.h:34 */
 ER_API er_status er_bind_light(const er_light_desc* desc, int32_t* id);
 ER_API er_status er_unbind_light(int32_t id);
