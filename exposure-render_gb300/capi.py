@@ -35,6 +35,7 @@ STATUS_NAMES = {
 SHAPE_PLANE, SHAPE_DISK, SHAPE_RING, SHAPE_BOX, SHAPE_SPHERE, SHAPE_CYLINDER, SHAPE_CONE = range(7)
 PROCEDURAL_UNIFORM, PROCEDURAL_CHECKER, PROCEDURAL_GRADIENT = range(3)
 TEXTURE_PROCEDURAL, TEXTURE_BITMAP = range(2)
+PERSISTENT_SHADOW, PERSISTENT_BOTH, PERSISTENT_NONE, PERSISTENT_PRIMARY = range(4)
 SHADING_BRDF_ONLY, SHADING_PHASE_ONLY, SHADING_HYBRID, SHADING_MODULATION, SHADING_THRESHOLD, SHADING_GRADIENT_MAGNITUDE = range(6)
 GRADIENT_FORWARD, GRADIENT_CENTRAL, GRADIENT_FILTERED = range(3)
 UNIT_POWER, UNIT_LUX, UNIT_INTENSITY = range(3)
@@ -173,7 +174,7 @@ class er_render_settings(Structure):
         ("tune_primary", c_int32),
         ("tune_shadow", c_int32),
         ("tune_shade", c_int32),
-        ("reserved", c_int32 * 1),
+        ("tune_persistent", c_int32),
     ]
 
 
@@ -218,6 +219,7 @@ class er_tune_result(Structure):
         ("msamples_per_s", c_float),
         ("candidates", c_int32),
         ("tune_shade", c_int32),
+        ("tune_persistent", c_int32),
     ]
 
 

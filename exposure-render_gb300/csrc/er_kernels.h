@@ -109,12 +109,14 @@ struct WavefrontBuffers {
     float4* events;      /* 5 * max_items */
     float4* jobs;        /* 6 * max_items */
     float4* partial;     /* 2 * max_npix: sums of a view cut by a window boundary */
-    uint32_t* counters;  /* 2 */
+    uint32_t* counters;  /* 4: events, shadow jobs, items and jobs taken by the persistent stages */
     int tune_primary;    /* resident blocks per SM targeted by the primary stage (2, 3, 4, 6, 8) */
     int tune_shadow;     /* same for the shadow stage */
     int tune_shade;      /* resident 128-thread blocks per SM of the shade stage (2, 3, 4, 6) */
     int objects;         /* 1 when a view has surface objects: the primary and shade stages run their
                             object-handling variants (at the default occupancy) */
+    int pt_primary;      /* the persistent-lane primary stage runs (every view delta-tracks) */
+    int pt_shadow;       /* the persistent-lane shadow stage runs (every view delta-tracks) */
 };
 
 /* cuts the items of views (npix[v] * spp[v] each) into windows of whole

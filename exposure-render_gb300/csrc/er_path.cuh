@@ -919,7 +919,128 @@ ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE
     }
 }
 
-/* Ratio tracking of a shadow segment with Russian roulette below 0.1 */
+/* Delta tracking of the primary ray (sample_volume_delta) as a resumable
+   state machine for the persistent primary stage: delta_begin sets the ray
+   up, each delta_step makes one tentative collision or crosses one majorant
+   brick; at the end `hit` says whether a real collision was found, at ray
+   parameter t.  Same operations in the same order as sample_volume_delta. */
+struct DeltaTracker {
+    Dda d;
+    float tau, t, e, mu;
+    int guard;
+    bool in_brick, done, hit;
+};
+
+ER_D void delta_begin(const Params& P, const Ray& R, Rng& rng, DeltaTracker& k)
+{
+    k.done = true;
+    k.hit = false;
+    Isect Int; Int.invalid();
+    intersect_box(R, vload(P.minp), vload(P.half_size), Int, false);
+    if (!Int.valid) return;
+    const float t0 = smax(Int.near_t, R.MinT);
+    const float t1 = smin(Int.far_t, R.MaxT);
+    if (!(t0 < t1)) return;
+    dda_init(P, R, t0, t1, k.d);
+    k.tau = -er_logf(rng.get1());
+    k.guard = 0;
+    k.in_brick = false;
+    k.done = false;
+}
+
+ER_D void delta_step(const Params& P, const Ray& R, Rng& rng, DeltaTracker& k)
+{
+    if (!k.in_brick) {
+        k.e = dda_exit(k.d);
+        k.mu = dda_majorant(P, k.d);
+        k.t = k.d.t;
+        k.in_brick = true;
+    }
+    if (k.mu > 0.0f) {
+        const float dt = k.tau / k.mu;
+        if (k.t + dt < k.e) {
+            k.t = k.t + dt;
+            const v3 Pt = vadd(R.O, vscale(R.D, k.t));
+            const float sig = P.density_scale * sigma_at(P, get_intensity(P, Pt));
+            if (rng.get1() * k.mu < sig) { k.hit = true; k.done = true; return; }
+            if (++k.guard > ER_DELTA_MAX_COLLISIONS) { atomicOr(P.err, 2); k.done = true; return; }
+            k.tau = -er_logf(rng.get1());
+            return;
+        }
+        k.tau = k.tau - k.mu * (k.e - k.t);
+        if (k.tau < 0.0f) k.tau = 0.0f;
+    }
+    dda_advance(P, k.d, k.e);
+    k.in_brick = false;
+    if (k.d.done) k.done = true;
+}
+
+/* Ratio tracking of a shadow segment with Russian roulette below 0.1, as a
+   resumable state machine: ratio_begin sets the segment up, each ratio_step
+   makes one collision or crosses one majorant brick.  The persistent shadow
+   stage interleaves the steps of one lane's successive segments, so a lane
+   whose segment ended takes the next one instead of idling until its warp's
+   longest segment ends.  transmittance_ratio below is the same tracking as
+   one loop: both make the same floating-point operations in the same order
+   (the parity tests compare both paths with the oracle). */
+struct RatioTracker {
+    Dda d;
+    float Tr, tau, t, e, mu;
+    int guard;
+    bool in_brick, done;
+};
+
+ER_D void ratio_begin(const Params& P, const Ray& R, Rng& rng, RatioTracker& k)
+{
+    k.Tr = 1.0f;
+    k.done = true;
+    Isect Int; Int.invalid();
+    intersect_box(R, vload(P.minp), vload(P.half_size), Int, false);
+    if (!Int.valid) return;
+    const float t0 = smax(Int.near_t, R.MinT);
+    const float t1 = smin(Int.far_t, R.MaxT);
+    if (!(t0 < t1)) return;
+    dda_init(P, R, t0, t1, k.d);
+    k.tau = -er_logf(rng.get1());
+    k.guard = 0;
+    k.in_brick = false;
+    k.done = false;
+}
+
+ER_D void ratio_step(const Params& P, const Ray& R, Rng& rng, RatioTracker& k)
+{
+    if (!k.in_brick) {
+        k.e = dda_exit(k.d);
+        k.mu = dda_majorant(P, k.d);
+        k.t = k.d.t;
+        k.in_brick = true;
+    }
+    if (k.mu > 0.0f) {
+        const float dt = k.tau / k.mu;
+        if (k.t + dt < k.e) {
+            k.t = k.t + dt;
+            const v3 Pt = vadd(R.O, vscale(R.D, k.t));
+            const float sig = P.density_scale * sigma_at(P, get_intensity(P, Pt));
+            k.Tr = k.Tr * (1.0f - sig / k.mu);
+            if (k.Tr <= 0.0f) { k.Tr = 0.0f; k.done = true; return; }
+            if (k.Tr < 0.1f) {
+                if (rng.get1() >= 0.5f) { k.Tr = 0.0f; k.done = true; return; }
+                k.Tr = k.Tr * 2.0f;
+            }
+            if (++k.guard > ER_DELTA_MAX_COLLISIONS) { atomicOr(P.err, 2); k.done = true; return; }
+            k.tau = -er_logf(rng.get1());
+            return;
+        }
+        k.tau = k.tau - k.mu * (k.e - k.t);
+        if (k.tau < 0.0f) k.tau = 0.0f;
+    }
+    dda_advance(P, k.d, k.e);
+    k.in_brick = false;
+    if (k.d.done) k.done = true;
+}
+
+/* the same tracking as one loop (the one-kernel paths and the non-persistent
+   shadow stage, where it compiles to fewer registers) */
 ER_D float transmittance_ratio(const Params& P, const Ray& R, Rng& rng)
 {
     Isect Int; Int.invalid();
@@ -965,16 +1086,23 @@ ER_D float transmittance_ratio(const Params& P, const Ray& R, Rng& rng)
 
 /* Visible / Intersect - Source/transport.h:30-56: 1/0 for the reference
    march, the ratio-tracked transmittance with delta tracking */
-template <bool OBJ = true>
-ER_D float visibility(const Params& P, v3 P1, v3 P2, Rng& rng)
+/* the shadow ray of Visible (Source/transport.h:46-56) */
+ER_D Ray shadow_ray(const Params& P, v3 P1, v3 P2)
 {
-    if (!P.shadows) return 1.0f;
     const v3 W = vnorm(vsub(P2, P1));
     Ray R;
     R.O = vadd(P1, vscale(W, ER_RAY_EPS));
     R.D = W;
     R.MinT = 0.0f;
     R.MaxT = smin(vlen(vsub(P2, P1)) - 2.0f * ER_RAY_EPS, P.max_shadow_distance);
+    return R;
+}
+
+template <bool OBJ = true>
+ER_D float visibility(const Params& P, v3 P1, v3 P2, Rng& rng)
+{
+    if (!P.shadows) return 1.0f;
+    const Ray R = shadow_ray(P, P1, P2);
     if (intersects_light(P, R)) return 0.0f;
     if (OBJ && P.object_count > 0 && intersects_object(P, R)) return 0.0f;
     if (P.free_flight == 1) return transmittance_ratio(P, R, rng);

@@ -115,7 +115,7 @@ struct WfQueues {
         if ((e = events.ensure(5 * plan.max_items)) != cudaSuccess) return e;
         if ((e = jobs.ensure(6 * plan.max_items)) != cudaSuccess) return e;
         if ((e = partial.ensure(2 * (size_t)plan.max_npix)) != cudaSuccess) return e;
-        if ((e = counters.ensure(2)) != cudaSuccess) return e;
+        if ((e = counters.ensure(4)) != cudaSuccess) return e;
         B.results = results.p;
         B.events = events.p;
         B.jobs = jobs.p;
@@ -125,6 +125,8 @@ struct WfQueues {
         B.tune_shadow = 4;
         B.tune_shade = 2;
         B.objects = 0;
+        B.pt_primary = 0;
+        B.pt_shadow = 0;
         return cudaSuccess;
     }
 };
@@ -206,7 +208,7 @@ struct BatchItem {
     std::vector<er_camera_desc> cameras;
     int flags = 0;
     size_t window_cap = kWindowCap;
-    int tune_primary = 4, tune_shadow = 4, tune_shade = 2;
+    int tune_primary = 4, tune_shadow = 4, tune_shade = 2, tune_persistent = 0;
     bool tune_explicit = false;    /* set by er_batch_set_tuning; else the first view's tracer settings */
     uint64_t planned_version = 0;  /* context version the plan was made at */
     bool planned = false;
@@ -408,6 +410,13 @@ er_status init_lanes(TracerItem& t)
     ER_CUDA(cudaMemcpyAsync(t.lanes.p, h.data(), 2 * n * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx().stream));
     ER_CUDA(cudaStreamSynchronize(ctx().stream));
     return ER_OK;
+}
+
+/* which tracking stages run persistent lanes (ER_PERSISTENT_*; delta tracking only) */
+void persistent_stages(int mode, bool all_delta, WavefrontBuffers& B)
+{
+    B.pt_primary = all_delta && (mode == ER_PERSISTENT_BOTH || mode == ER_PERSISTENT_PRIMARY);
+    B.pt_shadow = all_delta && (mode == ER_PERSISTENT_SHADOW || mode == ER_PERSISTENT_BOTH);
 }
 
 er_status reset_tracer_buffers(TracerItem& t)
@@ -657,6 +666,7 @@ er_status trace_sum(TracerItem& t, int spp, uint32_t view, uint32_t first, float
     B.tune_shadow = t.d.settings.tune_shadow > 0 ? t.d.settings.tune_shadow : 4;
     B.tune_shade = t.d.settings.tune_shade > 0 ? t.d.settings.tune_shade : 2;
     B.objects = t.P.object_count > 0;
+    persistent_stages(t.d.settings.tune_persistent, t.P.free_flight == ER_FREE_FLIGHT_DELTA, B);
     WfView V;
     memset(&V, 0, sizeof(V));
     V.P = t.P;
@@ -745,12 +755,18 @@ er_status batch_plan(BatchItem& b)
         b.tune_primary = s0.tune_primary > 0 ? s0.tune_primary : 4;
         b.tune_shadow = s0.tune_shadow > 0 ? s0.tune_shadow : 4;
         b.tune_shade = s0.tune_shade > 0 ? s0.tune_shade : 2;
+        b.tune_persistent = s0.tune_persistent;
     }
     b.B.tune_primary = b.tune_primary;
     b.B.tune_shadow = b.tune_shadow;
     b.B.tune_shade = b.tune_shade;
     b.B.objects = 0;
-    for (const WfView& hv : b.host_views) b.B.objects |= hv.P.object_count > 0;
+    bool all_delta = true;
+    for (const WfView& hv : b.host_views) {
+        b.B.objects |= hv.P.object_count > 0;
+        all_delta = all_delta && hv.P.free_flight == ER_FREE_FLIGHT_DELTA;
+    }
+    persistent_stages(b.tune_persistent, all_delta, b.B);
     if (b.flags & ER_BATCH_GRAPH) {
         if (!b.capture_stream) ER_CUDA(cudaStreamCreateWithFlags(&b.capture_stream, cudaStreamNonBlocking));
         ER_CUDA(cudaStreamBeginCapture(b.capture_stream, cudaStreamCaptureModeThreadLocal));
@@ -820,6 +836,7 @@ uint64_t tune_key(const TracerItem& t, const VolumeItem& v, int probe_spp)
     er_render_settings s = t.d.settings;
     s.majorant_brick = 0;
     s.tune_primary = s.tune_shadow = s.tune_shade = 0;
+    s.tune_persistent = 0;
     s.seed = 0;
     s.bilateral = 0;
     s.bilateral_radius = 0;
@@ -844,14 +861,16 @@ bool tune_cache_lookup(uint64_t key, er_tune_result& r)
     char line[256];
     while (fgets(line, sizeof(line), f)) {
         unsigned long long k = 0;
-        int b = 0, p = 0, sh = 0, sd = 0;
+        int b = 0, p = 0, sh = 0, sd = 0, pt = 0;
         float m = 0.0f;
-        if (sscanf(line, "%llx %d %d %d %d %f", &k, &b, &p, &sh, &sd, &m) == 6 && (uint64_t)k == key) {
+        /* lines carry the persistent-lane choice after the throughput */
+        if (sscanf(line, "%llx %d %d %d %d %f %d", &k, &b, &p, &sh, &sd, &m, &pt) == 7 && (uint64_t)k == key) {
             r.majorant_brick = b;
             r.tune_primary = p;
             r.tune_shadow = sh;
             r.tune_shade = sd;
             r.msamples_per_s = m;
+            r.tune_persistent = pt;
             found = true;          /* the last entry for a key wins */
         }
     }
@@ -868,8 +887,8 @@ void tune_cache_store(uint64_t key, const er_tune_result& r)
         if (path[i] == '/') mkdir(path.substr(0, i).c_str(), 0755);
     FILE* f = fopen(path.c_str(), "a");
     if (!f) return;
-    fprintf(f, "%016llx %d %d %d %d %.3f\n", (unsigned long long)key, r.majorant_brick, r.tune_primary, r.tune_shadow, r.tune_shade,
-            r.msamples_per_s);
+    fprintf(f, "%016llx %d %d %d %d %.3f %d\n", (unsigned long long)key, r.majorant_brick, r.tune_primary, r.tune_shadow, r.tune_shade,
+            r.msamples_per_s, r.tune_persistent);
     fclose(f);
 }
 
@@ -880,6 +899,10 @@ er_status time_probe(TracerItem& t, int spp, float* msps)
     er_status st = build(t);
     if (st != ER_OK) return st;
     const size_t npix = (size_t)t.W * t.H;
+    /* at least 2^21 samples per probe: a smaller launch does not fill the
+       persistent stages' resident wave and misranks them */
+    const size_t min_samples = (size_t)1 << 21;
+    if ((size_t)spp * npix < min_samples) spp = (int)std::min<size_t>((min_samples + npix - 1) / npix, 4096);
     ER_CUDA(t.tune_sum.ensure(npix));
     cudaStream_t s = ctx().stream;
     st = trace_sum(t, spp, 0x7fffffffu, 0u, t.tune_sum.p, 0, s);
@@ -1552,18 +1575,33 @@ ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tun
         if (r.msamples_per_s < 0.0f) { s = saved; t->built = false; return fail(ER_ERR_CUDA, "no majorant brick size could be timed"); }
         s.majorant_brick = r.majorant_brick;
         if (wavefront) {
+            /* occupancy pairs, with persistent-lane tracking stages or not (delta tracking) */
             const int variants[][2] = {{4, 4}, {3, 3}, {3, 4}, {4, 3}, {6, 4}, {4, 6}, {2, 3}, {8, 8}};
-            for (const auto& vv : variants) {
-                s.tune_primary = vv[0];
-                s.tune_shadow = vv[1];
-                float m = 0.0f;
-                st = time_probe(*t, probe_spp, &m);
-                if (st != ER_OK) { s = saved; t->built = false; return st; }
-                r.candidates++;
-                if (m > r.msamples_per_s) { r.msamples_per_s = m; r.tune_primary = vv[0]; r.tune_shadow = vv[1]; }
+            const int modes_delta[] = {ER_PERSISTENT_SHADOW, ER_PERSISTENT_BOTH, ER_PERSISTENT_NONE};
+            const int modes_march[] = {ER_PERSISTENT_SHADOW};
+            const int* modes = delta ? modes_delta : modes_march;
+            const int n_modes = delta ? 3 : 1;
+            r.tune_persistent = s.tune_persistent;
+            for (int mi = 0; mi < n_modes; mi++) {
+                s.tune_persistent = modes[mi];
+                for (const auto& vv : variants) {
+                    s.tune_primary = vv[0];
+                    s.tune_shadow = vv[1];
+                    float m = 0.0f;
+                    st = time_probe(*t, probe_spp, &m);
+                    if (st != ER_OK) { s = saved; t->built = false; return st; }
+                    r.candidates++;
+                    if (m > r.msamples_per_s) {
+                        r.msamples_per_s = m;
+                        r.tune_primary = vv[0];
+                        r.tune_shadow = vv[1];
+                        r.tune_persistent = modes[mi];
+                    }
+                }
             }
             s.tune_primary = r.tune_primary;
             s.tune_shadow = r.tune_shadow;
+            s.tune_persistent = r.tune_persistent;
             const int shades[] = {2, 3, 4, 6};
             for (int sd : shades) {
                 s.tune_shade = sd;
@@ -1580,6 +1618,7 @@ ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tun
     s.tune_primary = r.tune_primary;
     s.tune_shadow = r.tune_shadow;
     s.tune_shade = r.tune_shade;
+    s.tune_persistent = r.tune_persistent;
     t->built = false;
     C.version++;            /* batches over this tracer re-plan */
     st = build(*t);

@@ -166,6 +166,142 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
     }
 }
 
+/* queue slot among the lanes that are here together (persistent stages,
+   where lanes reach their queue pushes at different loop trips) */
+ER_D uint32_t queue_slot_active(bool want, uint32_t* counter)
+{
+    const unsigned active = __activemask();
+    const unsigned mask = __ballot_sync(active, want);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (mask && lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(active, base, leader < 0 ? (__ffs(active) - 1) : leader);
+    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+/* ---- stage 1, persistent lanes (delta tracking) ----
+
+   The work of k_wf_primary with lanes tracking one tentative collision or
+   majorant brick per inner loop trip: when a quarter of a warp's tracking
+   lanes have ended their rays, the warp finishes those samples and gives the
+   lanes the next items of the window (consecutive ones, one atomic per
+   warp), while the other lanes keep their rays.  The MetroSample values an event
+   record carries are drawn again from the sample's seed when the sample
+   finishes instead of being held through the tracking. */
+template <int MINB, bool ONE, bool OBJ>
+__global__ void __launch_bounds__(256, MINB) k_wf_primary_pt(const WfView* __restrict__ views, const WfSegment* __restrict__ segs,
+                                                              int nseg, const WfView one, const WfSegment one_seg, uint32_t items,
+                                                              float4* __restrict__ results, float4* __restrict__ events,
+                                                              uint32_t* __restrict__ n_events, uint32_t* __restrict__ fetch)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t i = 0;
+    bool tracking = false, exhausted = false;
+    int seg = 0;
+    Rng rng;
+    rng.s0 = 0u;
+    rng.s1 = 0u;
+    Ray R;
+    DeltaTracker k;
+    k.done = true;
+    k.hit = false;
+    for (;;) {
+        /* lanes without a sample take the next items of the window together
+           (one atomic per warp), so a warp's new samples are neighbours */
+        const unsigned needy = __ballot_sync(0xffffffffu, !tracking && !exhausted);
+        if (needy) {
+            const int leader = __ffs(needy) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(needy));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!tracking && !exhausted) {
+                i = base + (uint32_t)__popc(needy & ((1u << lane) - 1u));
+                exhausted = i >= items;
+            }
+        }
+        if (!tracking && !exhausted) {
+            seg = ONE ? 0 : find_segment(segs, nseg, i);
+            const WfSegment sg = ONE ? one_seg : segs[seg];
+            const WfView& V = view_of<ONE>(views, one, sg.view);
+            const Params& P = V.P;
+            const uint32_t local = i - sg.offset;
+            const uint32_t npix = (uint32_t)(P.film[0] * P.film[1]);
+            const int s = sg.s0 + (int)(local / npix);
+            const int pix = (int)(local % npix);
+            er_seed_lanes(P.seed, V.view_id, (uint32_t)pix, V.first + (uint32_t)s, &rng.s0, &rng.s1);
+            Metro ms;
+            ms.large_step(rng);
+            R = sample_camera(P, pix % P.film[0], pix / P.film[0], ms.film_uv, ms.lens_uv);
+            delta_begin(P, R, rng, k);
+            tracking = true;
+        }
+        if (!__any_sync(0xffffffffu, tracking)) break;
+        const WfSegment sg = ONE ? one_seg : segs[seg];
+        const WfView& V = view_of<ONE>(views, one, sg.view);
+        const Params& P = V.P;
+        /* track until a quarter of the lanes that were tracking have ended */
+        const int n_work = __popc(__ballot_sync(0xffffffffu, tracking && !k.done));
+        while (tracking && !k.done) {
+            delta_step(P, R, rng, k);
+            if (k.done || 4 * __popc(__activemask()) < 3 * n_work) break;
+        }
+        if (!tracking || !k.done) continue;
+        /* the sample's nearest event: volume, visible lights, objects */
+        Event SE, se1;
+        SE.type = 0; SE.valid = false; SE.T = 0.0f; SE.Le = C3(0, 0, 0);
+        SE.P = V3(0, 0, 0); SE.N = V3(0, 0, 0); SE.Wo = V3(0, 0, 0);
+        se1 = SE; se1.type = 1;
+        if (k.hit) {
+            SE.valid = true;
+            SE.T = k.t;
+            SE.P = vadd(R.O, vscale(R.D, k.t));
+            SE.N = V3(0.0f, 0.0f, 0.0f);
+            SE.Wo = vneg(R.D);
+        }
+        const Event se0 = SE;
+        intersect_lights(P, R, se1, true);
+        SE.valid = false; SE.type = 0;
+        float T = FLT_MAX;
+        if (se0.valid && se0.T < T) { SE = se0; T = se0.T; }
+        if (se1.valid && se1.T < T) { SE = se1; T = se1.T; }
+        ObjHit hit;
+        if (OBJ && P.object_count > 0) {
+            Event se2;
+            se2.type = 2; se2.valid = false; se2.T = 0.0f;
+            intersect_objects(P, R, se2, hit);
+            if (se2.valid && se2.T < T) { SE = se2; T = se2.T; }
+        }
+        bool push = false;
+        if (!SE.valid) {
+            results[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        } else if (SE.type == 1) {
+            const c3 Lv = cadd(C3(0, 0, 0), SE.Le);
+            results[i] = make_float4(Lv.r, Lv.g, Lv.b, 1.0f);
+        } else {
+            push = true;
+            if (OBJ && SE.type == 2) results[i] = make_float4(hit.UV.x, hit.UV.y, u2f((uint32_t)hit.id), 0.0f);
+        }
+        const uint32_t slot = queue_slot_active(push, n_events);
+        if (push) {
+            const uint32_t local = i - sg.offset;
+            const uint32_t npix = (uint32_t)(P.film[0] * P.film[1]);
+            Rng r0;
+            er_seed_lanes(P.seed, V.view_id, local % npix, V.first + (uint32_t)(sg.s0 + (int)(local / npix)), &r0.s0, &r0.s1);
+            Metro ms;
+            ms.large_step(r0);
+            const bool obj = OBJ && SE.type == 2;
+            float4* e = events + (size_t)slot * 5;
+            e[0] = make_float4(u2f(i), u2f(rng.s0), u2f(rng.s1), ms.light_num);
+            e[1] = make_float4(SE.P.x, SE.P.y, SE.P.z, ms.brdf_component);
+            e[2] = obj ? make_float4(SE.N.x, SE.N.y, SE.N.z, ms.brdf_dir.x) : make_float4(0.0f, 0.0f, 0.0f, ms.brdf_dir.x);
+            e[3] = make_float4(SE.Wo.x, SE.Wo.y, SE.Wo.z, ms.brdf_dir.y);
+            e[4] = make_float4(ms.light_uvw.x, ms.light_uvw.y, ms.light_uvw.z, u2f((uint32_t)sg.view | (obj ? WF_OBJECT_EVENT : 0u)));
+        }
+        tracking = false;
+    }
+}
+
 /* ---- stage 2: shading up to the shadow segments ---- */
 
 /* flags of a shadow job */
@@ -358,6 +494,111 @@ __global__ void __launch_bounds__(256, MINB) k_wf_shadow(const WfView* __restric
     }
 }
 
+/* ---- stage 3, persistent lanes (delta tracking: ratio-tracked shadows) ----
+
+   The same jobs and arithmetic as k_wf_shadow, with the work split
+   differently: lanes track one collision or majorant brick per inner loop
+   trip; when a quarter of a warp's tracking lanes have ended their segments,
+   the warp starts their next segments or takes new jobs (consecutive ones,
+   one atomic per warp) and tracks on.  In k_wf_shadow a warp runs until its
+   longest segment ends while the other lanes idle (5.5 of 32 lanes active
+   per instruction on the c2 workload). */
+template <int MINB, bool ONE, bool OBJ>
+__global__ void __launch_bounds__(256, MINB) k_wf_shadow_pt(const WfView* __restrict__ views, const WfView one,
+                                                             const float4* __restrict__ jobs, const uint32_t* __restrict__ n_jobs,
+                                                             float4* __restrict__ results, uint32_t* __restrict__ fetch)
+{
+    const uint32_t n = *n_jobs;
+    const int lane = threadIdx.x & 31;
+    uint32_t j_i = 0;
+    bool exhausted = false;
+    /* phase 0: take a job; 1, 2: tracking shadow segment 1 or 2; 3: write the sample */
+    int phase = 0;
+    uint32_t flags = 0, v = 0;
+    Rng rng;
+    rng.s0 = 0u;
+    rng.s1 = 0u;
+    c3 dl = C3(0, 0, 0);
+    Ray R;
+    RatioTracker k;
+    k.done = true;
+    k.Tr = 1.0f;
+    for (;;) {
+        /* lanes without a job take the next jobs together (one atomic per warp) */
+        const unsigned needy = __ballot_sync(0xffffffffu, phase == 0 && !exhausted);
+        if (needy) {
+            const int leader = __ffs(needy) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(needy));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (phase == 0 && !exhausted) {
+                j_i = base + (uint32_t)__popc(needy & ((1u << lane) - 1u));
+                exhausted = j_i >= n;
+            }
+        }
+        if (phase == 0 && !exhausted) {
+            const float4* j = jobs + (size_t)j_i * 6;
+            const float4 j0 = j[0];
+            rng.s0 = f2u(j0.y);
+            rng.s1 = f2u(j0.z);
+            flags = f2u(j0.w);
+            v = f2u(j[5].w);
+            dl = C3(0, 0, 0);
+            phase = (flags & WF_RAY1) ? 1 : ((flags & WF_RAY2) ? 2 : 3);
+            if (phase != 3) {
+                /* Visible (Source/transport.h:46-56) up to the tracking */
+                const Params& P = view_of<ONE>(views, one, v).P;
+                const float4 j1 = j[1], js = j[phase == 1 ? 2 : 4];
+                k.done = true;
+                k.Tr = 1.0f;
+                if (P.shadows) {
+                    R = shadow_ray(P, V3(j1.x, j1.y, j1.z), V3(js.x, js.y, js.z));
+                    if (intersects_light(P, R) || (OBJ && P.object_count > 0 && intersects_object(P, R))) k.Tr = 0.0f;
+                    else ratio_begin(P, R, rng, k);
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, phase != 0)) break;
+        const bool seg_phase = phase == 1 || phase == 2;
+        const Params& P = view_of<ONE>(views, one, v).P;
+        /* track until a quarter of the lanes that were tracking have ended */
+        const int n_work = __popc(__ballot_sync(0xffffffffu, seg_phase && !k.done));
+        while (seg_phase && !k.done) {
+            ratio_step(P, R, rng, k);
+            if (k.done || 4 * __popc(__activemask()) < 3 * n_work) break;
+        }
+        if (seg_phase && k.done) {
+            const float4* j = jobs + (size_t)j_i * 6;
+            const float Tr = k.Tr;
+            if (Tr > 0.0f) {
+                const float4 c = j[phase == 1 ? 3 : 5];
+                dl = cadd(dl, cscale(C3(c.x, c.y, c.z), Tr));
+            }
+            if (phase == 1 && (flags & WF_RAY2)) {
+                phase = 2;
+                const float4 j1 = j[1], js = j[4];
+                k.done = true;
+                k.Tr = 1.0f;
+                if (P.shadows) {
+                    R = shadow_ray(P, V3(j1.x, j1.y, j1.z), V3(js.x, js.y, js.z));
+                    if (intersects_light(P, R) || (OBJ && P.object_count > 0 && intersects_object(P, R))) k.Tr = 0.0f;
+                    else ratio_begin(P, R, rng, k);
+                }
+            } else {
+                phase = 3;
+            }
+        }
+        if (phase == 3) {
+            const float4* j = jobs + (size_t)j_i * 6;
+            const float4 j0 = j[0], j1 = j[1], j2 = j[2], j3 = j[3], j4 = j[4];
+            const c3 Le = C3(j2.w, j3.w, j4.w);
+            const c3 Lv = cadd(C3(0, 0, 0), cscale(cadd(Le, dl), j1.w));
+            results[f2u(j0.x)] = make_float4(Lv.r, Lv.g, Lv.b, 1.0f);
+            phase = 0;
+        }
+    }
+}
+
 /* ---- stage 4: per-pixel sum in sample order (blockIdx.y = segment) ---- */
 
 /* partial_in holds the sums of the previous window's last view when this
@@ -509,12 +750,23 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         const WfSegment one_seg = plan.segs[s0];
         float4* p_in = B.partial + (size_t)((w + 1) & 1) * plan.max_npix;
         float4* p_out = B.partial + (size_t)(w & 1) * plan.max_npix;
-        cudaError_t e = cudaMemsetAsync(B.counters, 0, 2 * sizeof(uint32_t), s);
+        cudaError_t e = cudaMemsetAsync(B.counters, 0, 4 * sizeof(uint32_t), s);
         if (e != cudaSuccess) return e;
         const uint32_t g1 = (items + 255) / 256 < (uint32_t)sm * 64 ? (items + 255) / 256 : (uint32_t)sm * 64;
         cudaEvent_t t0 = stage_begin(s);
 #define ER_PRIMARY(M, O) k_wf_primary<M, ONE, O><<<g1, 256, 0, s>>>(d_views, dseg, nseg, one, one_seg, items, B.results, B.events, B.counters)
-        if (B.objects) ER_PRIMARY(4, true);
+#define ER_PRIMARY_PT(M, O) k_wf_primary_pt<M, ONE, O><<<sm * M, 256, 0, s>>>(d_views, dseg, nseg, one, one_seg, items, B.results, B.events, B.counters, B.counters + 2)
+        if (B.pt_primary) {
+            /* delta tracking: persistent lanes, one resident wave */
+            if (B.objects) ER_PRIMARY_PT(4, true);
+            else switch (B.tune_primary) {
+            case 2: ER_PRIMARY_PT(2, false); break;
+            case 3: ER_PRIMARY_PT(3, false); break;
+            case 6: ER_PRIMARY_PT(6, false); break;
+            case 8: ER_PRIMARY_PT(8, false); break;
+            default: ER_PRIMARY_PT(4, false); break;
+            }
+        } else if (B.objects) ER_PRIMARY(4, true);
         else switch (B.tune_primary) {
         case 2: ER_PRIMARY(2, false); break;
         case 3: ER_PRIMARY(3, false); break;
@@ -522,6 +774,7 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         case 8: ER_PRIMARY(8, false); break;
         default: ER_PRIMARY(4, false); break;
         }
+#undef ER_PRIMARY_PT
 #undef ER_PRIMARY
         stage_end(t0, 0, s);
         t0 = stage_begin(s);
@@ -537,7 +790,18 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         stage_end(t0, 1, s);
         t0 = stage_begin(s);
 #define ER_SHADOW(M, O) k_wf_shadow<M, ONE, O><<<sm * 8, 256, 0, s>>>(d_views, one, B.jobs, B.counters + 1, B.results)
-        if (B.objects) ER_SHADOW(4, true);
+#define ER_SHADOW_PT(M, O) k_wf_shadow_pt<M, ONE, O><<<sm * M, 256, 0, s>>>(d_views, one, B.jobs, B.counters + 1, B.results, B.counters + 3)
+        if (B.pt_shadow) {
+            /* ratio-tracked shadows: persistent lanes, one resident wave */
+            if (B.objects) ER_SHADOW_PT(4, true);
+            else switch (B.tune_shadow) {
+            case 2: ER_SHADOW_PT(2, false); break;
+            case 3: ER_SHADOW_PT(3, false); break;
+            case 6: ER_SHADOW_PT(6, false); break;
+            case 8: ER_SHADOW_PT(8, false); break;
+            default: ER_SHADOW_PT(4, false); break;
+            }
+        } else if (B.objects) ER_SHADOW(4, true);
         else switch (B.tune_shadow) {
         case 2: ER_SHADOW(2, false); break;
         case 3: ER_SHADOW(3, false); break;
@@ -545,6 +809,7 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         case 8: ER_SHADOW(8, false); break;
         default: ER_SHADOW(4, false); break;
         }
+#undef ER_SHADOW_PT
 #undef ER_SHADOW
         stage_end(t0, 2, s);
         int max_npix = 0;

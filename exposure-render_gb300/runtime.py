@@ -136,8 +136,9 @@ class Renderer:
         s = self.tracer_desc.settings
         s.majorant_brick, s.tune_primary, s.tune_shadow = r.majorant_brick, r.tune_primary, r.tune_shadow
         s.tune_shade = r.tune_shade
+        s.tune_persistent = r.tune_persistent
         return {"majorant_brick": r.majorant_brick, "tune_primary": r.tune_primary, "tune_shadow": r.tune_shadow,
-                "tune_shade": r.tune_shade,
+                "tune_shade": r.tune_shade, "tune_persistent": r.tune_persistent,
                 "from_cache": bool(r.from_cache), "msamples_per_s": r.msamples_per_s, "candidates": r.candidates}
 
     def gradient_magnitude(self, d_gm_ptr=None) -> float:

@@ -220,8 +220,19 @@ typedef struct er_render_settings {
     int32_t tune_shadow;          /* wavefront: same for the shadow stage (0 or other values: 4) */
     int32_t tune_shade;           /* wavefront: resident 128-thread blocks per SM of the shade stage
                                      (2, 3, 4 or 6; 0 or other values: 2) */
-    int32_t reserved[1];
+    int32_t tune_persistent;      /* delta tracking, wavefront: which tracking stages run persistent lanes
+                                     (ER_PERSISTENT_*; 0: the shadow stage only) */
 } er_render_settings;
+
+/* tune_persistent: the persistent-lane stages keep every warp's lanes busy by
+   handing a lane whose ray ended the next ray of the window; the per-thread
+   stages keep neighbouring pixels' rays together in a warp */
+enum {
+    ER_PERSISTENT_SHADOW = 0,     /* persistent shadow stage, per-thread primary stage */
+    ER_PERSISTENT_BOTH = 1,
+    ER_PERSISTENT_NONE = 2,
+    ER_PERSISTENT_PRIMARY = 3
+};
 
 /* ErTracer (Source/ertracer.h:33-117).  light_ids/object_ids/clipping_ids are
    item IDs returned by the bind calls. */
@@ -470,14 +481,17 @@ typedef struct er_tune_result {
     float msamples_per_s;     /* probe throughput of the chosen configuration */
     int32_t candidates;       /* configurations timed */
     int32_t tune_shade;       /* occupancy variant of the shade stage */
+    int32_t tune_persistent;  /* ER_PERSISTENT_* of the chosen configuration */
 } er_tune_result;
 
 /* Times probe renders of a bound tracer (probe_spp samples per pixel of its
-   film, one warm-up each) over majorant bricks {1, 2, 4, 8, 16} (delta
-   tracking only) and then the occupancy variants of the wavefront stages,
-   and writes the fastest configuration into the bound tracer's settings (the
-   caller's descriptor is not changed; re-binding it restores its values),
-   and last the shade stage's variants.
+   film, raised to at least 2^21 samples per probe, one warm-up each) over
+   majorant bricks {1, 2, 4, 8, 16} (delta tracking only), then the occupancy
+   variants of the wavefront stages under each persistent-lane mode
+   (ER_PERSISTENT_*, delta tracking only), and last the shade stage's
+   variants, and writes the fastest configuration into the bound tracer's
+   settings (the caller's descriptor is not changed; re-binding it restores
+   its values).
    Results are cached per device, volume and shading configuration in the
    file named by the environment variable ER_TUNE_CACHE (default
    $HOME/.cache/exposurerender_gb300/autotune.txt; "off" disables the

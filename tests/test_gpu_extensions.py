@@ -124,3 +124,29 @@ def test_majorant_grid_device_bit_exact(env, oracle, shape, brick):
     torch.cuda.synchronize()
     assert np.array_equal(bits(d_out.cpu().numpy()), bits(want))
     assert want.max() > 0
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2, 3], ids=["shadow", "both", "none", "primary"])
+def test_persistent_stage_modes_bit_exact(env, oracle, mode):
+    """every persistent-lane mode of the delta-tracking stages (tune_persistent)
+    gives the oracle's sums, alone and with the hybrid shader and full MIS"""
+    torch, lib, rt = env
+    sc = two_light_scene(13)
+    sc.tracer.settings.free_flight = 1
+    sc.tracer.settings.mis = 1
+    sc.tracer.settings.apply_shading_type = 1
+    sc.tracer.settings.shading_type = 2
+    sc.tracer.settings.tune_persistent = mode
+    r = rt.Renderer(sc, lib)
+    h = OL.SceneHandle(oracle, sc)
+    try:
+        for tp, ts in ((4, 4), (2, 3), (8, 8)):
+            r.tracer_desc.settings.tune_primary, r.tracer_desc.settings.tune_shadow = tp, ts
+            r.rebind_tracer()
+            d = torch.zeros((sc.height, sc.width, 4), dtype=torch.float32, device="cuda")
+            r.trace_sum_device(d.data_ptr(), 5, 1, 2, 0, None)
+            torch.cuda.synchronize()
+            assert np.array_equal(bits(d.cpu().numpy()), bits(h.render_sum(5, view=1, first=2, nthreads=4))), (tp, ts)
+    finally:
+        r.close()
+        h.close()
