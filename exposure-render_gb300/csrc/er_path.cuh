@@ -181,6 +181,22 @@ ER_D float gradient_magnitude(const Params& P, v3 p)
     return sqrtf(sum);
 }
 
+/* Out-of-line copies of the elementary functions for code that runs once per
+   event or per light sample (shading, light and BSDF sampling, shape UVs):
+   one copy each instead of one inlined copy per call site keeps the shade
+   stage within the instruction cache.  Same functions, same results; the
+   tracking loops keep the inlined er_logf. */
+ER_COLD float pow_c(float x, float y) { return er_powf(x, y); }
+ER_COLD float exp_c(float x) { return er_expf(x); }
+ER_COLD float acos_c(float x) { return er_acosf(x); }
+ER_COLD float atan2_c(float y, float x) { return er_atan2f(y, x); }
+ER_COLD v2 sincos_c(float x)
+{
+    v2 r;
+    er_sincosf(x, &r.x, &r.y);
+    return r;
+}
+
 /* ---- geometry ---- */
 
 struct Ray { v3 O, D; float MinT, MaxT; };
@@ -224,10 +240,10 @@ ER_D Ray xform_ray(const float m[3][4], const Ray& r)
     return t;
 }
 
-ER_D float spherical_theta(v3 w) { return er_acosf(eclamp(w.y, -1.0f, 1.0f)); }
+ER_D float spherical_theta(v3 w) { return acos_c(eclamp(w.y, -1.0f, 1.0f)); }
 ER_D float spherical_phi(v3 w)
 {
-    const float p = er_atan2f(w.z, w.x);
+    const float p = atan2_c(w.z, w.x);
     return (p < 0.0f) ? p + 2.0f * ER_PI_F : p;
 }
 
@@ -362,8 +378,8 @@ ER_D v2 concentric_sample_disk(v2 U)   /* Source/montecarlo.h:86-137 */
         else { r = -sy; theta = 6.0f + sx / r; }
     }
     theta *= ER_PI_F / 4.f;
-    float sn, cs;
-    er_sincosf(theta, &sn, &cs);
+    const v2 scv = sincos_c(theta);
+    const float sn = scv.x, cs = scv.y;
     out.x = r * cs;
     out.y = r * sn;
     return out;
@@ -384,7 +400,7 @@ ER_D void sample_light_surface(const Light& L, v3 UVW, Surf& SS)
     case 1: {
         const float r = sqrtf(UVW.x);
         const float theta = 2.0f * ER_PI_F * UVW.y;
-        float sn, cs; er_sincosf(theta, &sn, &cs);
+        const v2 scv = sincos_c(theta); const float sn = scv.x, cs = scv.y;
         SS.P = V3(r * cs, r * sn, 0.0f);
         SS.UV.x = UVW.x; SS.UV.y = UVW.y;
         SS.P = vscale(SS.P, L.outer_radius);
@@ -394,7 +410,7 @@ ER_D void sample_light_surface(const Light& L, v3 UVW, Surf& SS)
         const float inner = L.inner_radius / L.outer_radius;
         const float r = inner + (1.0f - inner) * sqrtf(UVW.x);
         const float theta = 2.0f * ER_PI_F * UVW.y;
-        float sn, cs; er_sincosf(theta, &sn, &cs);
+        const v2 scv = sincos_c(theta); const float sn = scv.x, cs = scv.y;
         SS.P = V3(r * cs, r * sn, 0.0f);
         SS.P = vscale(SS.P, L.outer_radius);
         SS.UV.x = SS.P.x; SS.UV.y = SS.P.y;
@@ -421,7 +437,7 @@ ER_D void sample_light_surface(const Light& L, v3 UVW, Surf& SS)
         const float z = 1.0f - 2.0f * UVW.x;
         const float r = sqrtf(smax(0.0f, 1.0f - z * z));
         const float phi = 2.0f * ER_PI_F * UVW.y;
-        float sn, cs; er_sincosf(phi, &sn, &cs);
+        const v2 scv = sincos_c(phi); const float sn = scv.x, cs = scv.y;
         SS.P = V3(r * cs, r * sn, z);
         SS.N = SS.P;
         SS.UV.x = spherical_theta(SS.P);
@@ -558,13 +574,13 @@ ER_D float fresnel_eval(float ei_, float et_, float cosi)
     return (Rparl * Rparl + Rperp * Rperp) / 2.f;
 }
 
-ER_D float blinn_d(float e, v3 Wh) { return (e + 2) * ER_INV_TWO_PI_F * er_powf(fabsf(Wh.z), e); }
+ER_D float blinn_d(float e, v3 Wh) { return (e + 2) * ER_INV_TWO_PI_F * pow_c(fabsf(Wh.z), e); }
 
 ER_D float blinn_pdf(float e, v3 Wo, v3 Wi)
 {
     const v3 Wh = vnorm(vadd(Wo, Wi));
     const float ct = fabsf(Wh.z);
-    float pdf = ((e + 1.0f) * er_powf(ct, e)) / (2.0f * ER_PI_F * 4.0f * vdot(Wo, Wh));
+    float pdf = ((e + 1.0f) * pow_c(ct, e)) / (2.0f * ER_PI_F * 4.0f * vdot(Wo, Wh));
     if (vdot(Wo, Wh) <= 0.0f) pdf = 0.0f;
     return pdf;
 }
@@ -1118,14 +1134,14 @@ ER_D int select_shader_type(const Params& P, const Event& SE, float I, Rng& rng,
     case 1: return 1;
     case 2: {
         const float NGM = (gm >= 0.0f ? gm : gradient_magnitude(P, SE.P)) * P.gm_inv_max;
-        const float Exponent = 25.0f * er_powf(P.gradient_factor, 3.0f) * NGM;
-        const float PdfBrdf = P.opacity_modulated ? plf_eval(P.tfs->opacity, I) * (1.0f - er_expf(-Exponent))
-                                                  : 1.0f - er_expf(-Exponent);
+        const float Exponent = 25.0f * pow_c(P.gradient_factor, 3.0f) * NGM;
+        const float PdfBrdf = P.opacity_modulated ? plf_eval(P.tfs->opacity, I) * (1.0f - exp_c(-Exponent))
+                                                  : 1.0f - exp_c(-Exponent);
         return rng.get1() <= PdfBrdf ? 0 : 1;
     }
     case 3: {
         const float NGM = (gm >= 0.0f ? gm : gradient_magnitude(P, SE.P)) * P.gm_inv_max;
-        const float PdfBrdf = 1.0f - er_powf(1.0f - NGM, 2.0f);
+        const float PdfBrdf = 1.0f - pow_c(1.0f - NGM, 2.0f);
         return rng.get1() < PdfBrdf ? 0 : 1;
     }
     case 4: {
@@ -1193,11 +1209,11 @@ ER_D v3 sample_bsdf_dir(const Shader& sh, v3 Wo, const Metro& ms)
             if (Wol.z < 0.0f) Wil.z *= -1.0f;
         } else {
             const float e = sh.exponent;
-            const float costheta = er_powf(ms.brdf_dir.x, 1.f / (e + 1));
+            const float costheta = pow_c(ms.brdf_dir.x, 1.f / (e + 1));
             const float sintheta = sqrtf(smax(0.f, 1.f - costheta * costheta));
             const float phi = ms.brdf_dir.y * 2.f * ER_PI_F;
-            float sn, cs;
-            er_sincosf(phi, &sn, &cs);
+            const v2 scv = sincos_c(phi);
+            const float sn = scv.x, cs = scv.y;
             v3 wh = V3(sintheta * cs, sintheta * sn, costheta);
             if (!same_hemisphere(Wol, wh)) wh = vneg(wh);
             Wil = vadd(vneg(Wol), vscale(wh, 2.f * vdot(Wol, wh)));
@@ -1207,8 +1223,8 @@ ER_D v3 sample_bsdf_dir(const Shader& sh, v3 Wo, const Metro& ms)
     const float z = 1.f - 2.f * ms.brdf_dir.x;
     const float r = sqrtf(smax(0.f, 1.f - z * z));
     const float phi = 2.f * ER_PI_F * ms.brdf_dir.y;
-    float sn, cs;
-    er_sincosf(phi, &sn, &cs);
+    const v2 scv = sincos_c(phi);
+    const float sn = scv.x, cs = scv.y;
     return V3(r * cs, r * sn, z);
 }
 
@@ -1291,7 +1307,7 @@ ER_D void object_shader(const Params& P, const Event& SE, const ObjHit& hit, Sha
     Y += 0.212671f * G.r;
     Y += 0.715160f * G.g;
     Y += 0.072169f * G.b;
-    shader_init(sh, 0, SE.N, SE.Wo, Kd, Ks, 15.0f, 1000000.0f * er_powf(Y, 7.0f));
+    shader_init(sh, 0, SE.N, SE.Wo, Kd, Ks, 15.0f, 1000000.0f * pow_c(Y, 7.0f));
 }
 
 /* UniformSampleOneLight - Source/transport.h:115-156 (volume and object events) */
@@ -1310,7 +1326,7 @@ ER_D c3 uniform_sample_one_light(const Params& P, const Event& SE, Rng& rng, con
     } else {
         const int type = P.apply_shading_type ? select_shader_type(P, SE, I, rng) : 0;
         shader_init(sh, type, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
-                    1000000.0f * er_powf(plf_eval(P.tfs->glossiness, I), 7.0f));
+                    1000000.0f * pow_c(plf_eval(P.tfs->glossiness, I), 7.0f));
     }
     Ld = cadd(Ld, estimate_direct_light(P, L, idx, ms, SE, rng, sh));
     return cscale(Ld, (float)P.light_count);

@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict
                 } else {
                     const int type = P.apply_shading_type ? select_shader_type(P, SE, I, rng, gm) : 0;
                     shader_init(sh, type, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
-                                1000000.0f * er_powf(plf_eval(P.tfs->glossiness, I), 7.0f));
+                                1000000.0f * pow_c(plf_eval(P.tfs->glossiness, I), 7.0f));
                 }
                 count = (float)P.light_count;
                 /* EstimateDirectLight - Source/transport.h:58-113, without the visibility terms */
