@@ -545,6 +545,9 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
     samples_per_step = sum(cam.film_size[0] * cam.film_size[1] * spp for _, cam, spp in views)
     max_spp = max(spp for _, _, spp in views)
     batch = runtime.Batch(table, flags=C.ER_BATCH_GRAPH)
+    # the tracking stages' persistent-lane mode and empty-space skips, timed
+    # on whole launches of this batch
+    batch_tune = batch.autotune(sp) if not args.no_tune else None
     info = batch.info()
 
     def timed(fn, steps):
@@ -571,6 +574,8 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
 
     # stage shares: the same batch launched without the graph, profiled
     prof = runtime.Batch(table, flags=0)
+    if batch_tune:
+        prof.set_stages(batch_tune["tune_stages"])
     prof.launch(sp)
     torch.cuda.synchronize()
     read_profile(lib, C)
@@ -655,7 +660,7 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
                    "samples_per_step": samples_per_step, "films": sorted({c.film_size[0] for _, c, _ in views}),
                    "spp_range": [min(s for _, _, s in views), max_spp], **describe_shading(scenes[0]),
                    "windows": info["windows"], "segments": info["segments"], "queue_bytes": info["queue_bytes"],
-                   "autotune": tuned,
+                   "autotune": tuned, "batch_autotune": batch_tune,
                    "l2": "volumes %d MiB in total; every step renders fresh samples" % (vol_bytes >> 20),
                    "parallelism": "replicas" if world > 1 else "single"},
         "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(vol_bytes),

@@ -36,6 +36,8 @@ SHAPE_PLANE, SHAPE_DISK, SHAPE_RING, SHAPE_BOX, SHAPE_SPHERE, SHAPE_CYLINDER, SH
 PROCEDURAL_UNIFORM, PROCEDURAL_CHECKER, PROCEDURAL_GRADIENT = range(3)
 TEXTURE_PROCEDURAL, TEXTURE_BITMAP = range(2)
 PERSISTENT_SHADOW, PERSISTENT_BOTH, PERSISTENT_NONE, PERSISTENT_PRIMARY = range(4)
+TUNE_NO_SKIP_PRIMARY, TUNE_NO_SKIP_SHADOW = 4, 8
+TUNE_NO_SKIP = TUNE_NO_SKIP_PRIMARY | TUNE_NO_SKIP_SHADOW
 SHADING_BRDF_ONLY, SHADING_PHASE_ONLY, SHADING_HYBRID, SHADING_MODULATION, SHADING_THRESHOLD, SHADING_GRADIENT_MAGNITUDE = range(6)
 GRADIENT_FORWARD, GRADIENT_CENTRAL, GRADIENT_FILTERED = range(3)
 UNIT_POWER, UNIT_LUX, UNIT_INTENSITY = range(3)
@@ -174,7 +176,7 @@ class er_render_settings(Structure):
         ("tune_primary", c_int32),
         ("tune_shadow", c_int32),
         ("tune_shade", c_int32),
-        ("tune_persistent", c_int32),
+        ("tune_stages", c_int32),
     ]
 
 
@@ -219,7 +221,7 @@ class er_tune_result(Structure):
         ("msamples_per_s", c_float),
         ("candidates", c_int32),
         ("tune_shade", c_int32),
-        ("tune_persistent", c_int32),
+        ("tune_stages", c_int32),
     ]
 
 
@@ -426,6 +428,8 @@ def _declare(lib) -> None:
         "er_batch_advance": (c_int32, [c_int32, c_uint32, c_void_p]),
         "er_batch_set_tuning": (c_int32, [c_int32, c_int32, c_int32]),
         "er_batch_info": (c_int32, [c_int32, i32p, i32p, POINTER(ctypes.c_int64)]),
+        "er_batch_set_stages": (c_int32, [c_int32, c_int32]),
+        "er_batch_autotune": (c_int32, [c_int32, c_void_p, i32p, POINTER(c_float)]),
         "er_batch_destroy": (c_int32, [c_int32]),
         "er_autotune_tracer": (c_int32, [c_int32, c_int32, POINTER(er_tune_result)]),
         "er_get_render_settings": (c_int32, [c_int32, POINTER(er_render_settings)]),

@@ -38,6 +38,9 @@ cudaError_t er_launch_gradient_magnitude(const erd::Params& P, uint16_t* gm, uns
 cudaError_t er_launch_math_eval(int fn, int n, const float* x, const float* y, float* out, cudaStream_t s);
 cudaError_t er_launch_majorant(const uint16_t* vox, const int res[3], int B, const int nb[3], const float* sigma, int n,
                                float* rmq, int levels, uint32_t* minmax, float density_scale, float* majorant, cudaStream_t s);
+/* writes -(Chebyshev distance to the nearest non-empty brick, capped at 32)
+   into the empty bricks of a majorant grid; tmp holds 2 bytes per brick */
+cudaError_t er_launch_empty_skip(float* majorant, const int nb[3], uint8_t* tmp, cudaStream_t s);
 
 /* the differentiable medium (er_medium.cu) */
 struct DmParams {
@@ -117,6 +120,8 @@ struct WavefrontBuffers {
                             object-handling variants (at the default occupancy) */
     int pt_primary;      /* the persistent-lane primary stage runs (every view delta-tracks) */
     int pt_shadow;       /* the persistent-lane shadow stage runs (every view delta-tracks) */
+    int skip_primary;    /* the free-flight stage compiles the empty-space skip */
+    int skip_shadow;     /* the shadow stage compiles the empty-space skip */
 };
 
 /* cuts the items of views (npix[v] * spp[v] each) into windows of whole

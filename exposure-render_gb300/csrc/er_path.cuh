@@ -888,9 +888,27 @@ ER_D float dda_majorant(const Params& P, const Dda& d)
 
 #define ER_DELTA_MAX_COLLISIONS 1048576
 
+/* Empty-space skip.  An empty brick of the tracker's majorant grid holds
+   -k, k the Chebyshev distance in bricks to the nearest non-empty brick
+   (er_volume.cu k_skip_pass), so every brick within k-1 of it is empty.
+   dda_skip steps the DDA through that cube of empty bricks without reading
+   their majorants: each step is the exit and advance that brick-by-brick
+   tracking makes in an empty brick (which draws nothing and leaves tau
+   alone), so the DDA leaves the cube with exactly the face times and brick
+   indices of plain stepping and renders are bit-identical with or without
+   the skip; only the dependent majorant loads are saved. */
+ER_D void dda_skip(const Params& P, Dda& d, int k, float e)
+{
+    const int x0 = d.bx, y0 = d.by, z0 = d.bz, r = k - 1;
+    dda_advance(P, d, e);
+    while (!d.done && abs(d.bx - x0) <= r && abs(d.by - y0) <= r && abs(d.bz - z0) <= r) dda_advance(P, d, dda_exit(d));
+}
+
 /* Delta tracking of the primary ray: sigma_t = DensityScale^2 * Opacity(I),
    the extinction the reference's march integrates (Source/raymarching.h:45,64-66) */
-template <bool WITH_NORMAL = true>
+/* SKIP: compile the empty-space skip (a grid without skip distances reads
+   the same either way; the variant without it needs fewer registers) */
+template <bool WITH_NORMAL = true, bool SKIP = true>
 ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE)
 {
     Isect Int; Int.invalid();
@@ -930,6 +948,9 @@ ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE
                 if (++guard > ER_DELTA_MAX_COLLISIONS) { atomicOr(P.err, 2); return; }
                 tau = -er_logf(rng.get1());
             }
+        } else if (SKIP && mu <= -2.0f) {
+            dda_skip(P, d, (int)(-mu), e);
+            continue;
         }
         dda_advance(P, d, e);
     }
@@ -964,6 +985,7 @@ ER_D void delta_begin(const Params& P, const Ray& R, Rng& rng, DeltaTracker& k)
     k.done = false;
 }
 
+template <bool SKIP = true>
 ER_D void delta_step(const Params& P, const Ray& R, Rng& rng, DeltaTracker& k)
 {
     if (!k.in_brick) {
@@ -985,6 +1007,11 @@ ER_D void delta_step(const Params& P, const Ray& R, Rng& rng, DeltaTracker& k)
         }
         k.tau = k.tau - k.mu * (k.e - k.t);
         if (k.tau < 0.0f) k.tau = 0.0f;
+    } else if (SKIP && k.mu <= -2.0f) {
+        dda_skip(P, k.d, (int)(-k.mu), k.e);
+        k.in_brick = false;
+        if (k.d.done) k.done = true;
+        return;
     }
     dda_advance(P, k.d, k.e);
     k.in_brick = false;
@@ -1023,6 +1050,7 @@ ER_D void ratio_begin(const Params& P, const Ray& R, Rng& rng, RatioTracker& k)
     k.done = false;
 }
 
+template <bool SKIP = true>
 ER_D void ratio_step(const Params& P, const Ray& R, Rng& rng, RatioTracker& k)
 {
     if (!k.in_brick) {
@@ -1049,6 +1077,11 @@ ER_D void ratio_step(const Params& P, const Ray& R, Rng& rng, RatioTracker& k)
         }
         k.tau = k.tau - k.mu * (k.e - k.t);
         if (k.tau < 0.0f) k.tau = 0.0f;
+    } else if (SKIP && k.mu <= -2.0f) {
+        dda_skip(P, k.d, (int)(-k.mu), k.e);
+        k.in_brick = false;
+        if (k.d.done) k.done = true;
+        return;
     }
     dda_advance(P, k.d, k.e);
     k.in_brick = false;
@@ -1057,6 +1090,7 @@ ER_D void ratio_step(const Params& P, const Ray& R, Rng& rng, RatioTracker& k)
 
 /* the same tracking as one loop (the one-kernel paths and the non-persistent
    shadow stage, where it compiles to fewer registers) */
+template <bool SKIP = true>
 ER_D float transmittance_ratio(const Params& P, const Ray& R, Rng& rng)
 {
     Isect Int; Int.invalid();
@@ -1094,6 +1128,9 @@ ER_D float transmittance_ratio(const Params& P, const Ray& R, Rng& rng)
                 if (++guard > ER_DELTA_MAX_COLLISIONS) { atomicOr(P.err, 2); return Tr; }
                 tau = -er_logf(rng.get1());
             }
+        } else if (SKIP && mu <= -2.0f) {
+            dda_skip(P, d, (int)(-mu), e);
+            continue;
         }
         dda_advance(P, d, e);
     }
@@ -1114,14 +1151,14 @@ ER_D Ray shadow_ray(const Params& P, v3 P1, v3 P2)
     return R;
 }
 
-template <bool OBJ = true>
+template <bool OBJ = true, bool SKIP = true>
 ER_D float visibility(const Params& P, v3 P1, v3 P2, Rng& rng)
 {
     if (!P.shadows) return 1.0f;
     const Ray R = shadow_ray(P, P1, P2);
     if (intersects_light(P, R)) return 0.0f;
     if (OBJ && P.object_count > 0 && intersects_object(P, R)) return 0.0f;
-    if (P.free_flight == 1) return transmittance_ratio(P, R, rng);
+    if (P.free_flight == 1) return transmittance_ratio<SKIP>(P, R, rng);
     return scatter_event_in_volume(P, R, rng) ? 0.0f : 1.0f;
 }
 

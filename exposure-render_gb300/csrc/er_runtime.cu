@@ -127,6 +127,8 @@ struct WfQueues {
         B.objects = 0;
         B.pt_primary = 0;
         B.pt_shadow = 0;
+        B.skip_primary = 0;
+        B.skip_shadow = 0;
         return cudaSuccess;
     }
 };
@@ -191,7 +193,8 @@ struct TracerItem {
     DevBuf<erd::Texture> textures;
     DevBuf<float> sigma;
     DevBuf<int> light_ids;
-    DevBuf<float> majorant, rmq;
+    DevBuf<float> majorant, rmq;   /* majorant: per brick, or -(distance to a non-empty brick) when empty */
+    DevBuf<uint8_t> skip_tmp;
     DevBuf<uint32_t> minmax;
     DevBuf<int> err;
     DevBuf<float> autofocus;       /* er_get_auto_focus_distance's result */
@@ -208,8 +211,9 @@ struct BatchItem {
     std::vector<er_camera_desc> cameras;
     int flags = 0;
     size_t window_cap = kWindowCap;
-    int tune_primary = 4, tune_shadow = 4, tune_shade = 2, tune_persistent = 0;
+    int tune_primary = 4, tune_shadow = 4, tune_shade = 2, tune_stages = 0;
     bool tune_explicit = false;    /* set by er_batch_set_tuning; else the first view's tracer settings */
+    bool stages_explicit = false;  /* set by er_batch_set_stages / er_batch_autotune */
     uint64_t planned_version = 0;  /* context version the plan was made at */
     bool planned = false;
     WavefrontPlan plan;
@@ -415,6 +419,9 @@ er_status init_lanes(TracerItem& t)
 /* which tracking stages run persistent lanes (ER_PERSISTENT_*; delta tracking only) */
 void persistent_stages(int mode, bool all_delta, WavefrontBuffers& B)
 {
+    B.skip_primary = all_delta && !(mode & ER_TUNE_NO_SKIP_PRIMARY);
+    B.skip_shadow = all_delta && !(mode & ER_TUNE_NO_SKIP_SHADOW);
+    mode &= 3;
     B.pt_primary = all_delta && (mode == ER_PERSISTENT_BOTH || mode == ER_PERSISTENT_PRIMARY);
     B.pt_shadow = all_delta && (mode == ER_PERSISTENT_SHADOW || mode == ER_PERSISTENT_BOTH);
 }
@@ -511,6 +518,10 @@ er_status build(TracerItem& t)
         ER_CUDA(t.rmq.ensure((size_t)levels * n));
         ER_CUDA(er_launch_majorant(v.vox.p, v.res, brick, nb, t.sigma.p, n, t.rmq.p, levels, t.minmax.p, s.density_scale,
                                    t.majorant.p, st));
+        /* empty bricks carry minus their distance to the nearest non-empty
+           one (read by the skipping stages, ignored by the others) */
+        ER_CUDA(t.skip_tmp.ensure(2 * total));
+        ER_CUDA(er_launch_empty_skip(t.majorant.p, nb, t.skip_tmp.p, st));
         P.brick = brick;
         for (int i = 0; i < 3; i++) P.nb[i] = nb[i];
         P.majorant = t.majorant.p;
@@ -666,7 +677,7 @@ er_status trace_sum(TracerItem& t, int spp, uint32_t view, uint32_t first, float
     B.tune_shadow = t.d.settings.tune_shadow > 0 ? t.d.settings.tune_shadow : 4;
     B.tune_shade = t.d.settings.tune_shade > 0 ? t.d.settings.tune_shade : 2;
     B.objects = t.P.object_count > 0;
-    persistent_stages(t.d.settings.tune_persistent, t.P.free_flight == ER_FREE_FLIGHT_DELTA, B);
+    persistent_stages(t.d.settings.tune_stages, t.P.free_flight == ER_FREE_FLIGHT_DELTA, B);
     WfView V;
     memset(&V, 0, sizeof(V));
     V.P = t.P;
@@ -755,8 +766,8 @@ er_status batch_plan(BatchItem& b)
         b.tune_primary = s0.tune_primary > 0 ? s0.tune_primary : 4;
         b.tune_shadow = s0.tune_shadow > 0 ? s0.tune_shadow : 4;
         b.tune_shade = s0.tune_shade > 0 ? s0.tune_shade : 2;
-        b.tune_persistent = s0.tune_persistent;
     }
+    if (!b.stages_explicit) b.tune_stages = find_tracer(b.views[0].tracer_id)->d.settings.tune_stages;
     b.B.tune_primary = b.tune_primary;
     b.B.tune_shadow = b.tune_shadow;
     b.B.tune_shade = b.tune_shade;
@@ -766,7 +777,7 @@ er_status batch_plan(BatchItem& b)
         b.B.objects |= hv.P.object_count > 0;
         all_delta = all_delta && hv.P.free_flight == ER_FREE_FLIGHT_DELTA;
     }
-    persistent_stages(b.tune_persistent, all_delta, b.B);
+    persistent_stages(b.tune_stages, all_delta, b.B);
     if (b.flags & ER_BATCH_GRAPH) {
         if (!b.capture_stream) ER_CUDA(cudaStreamCreateWithFlags(&b.capture_stream, cudaStreamNonBlocking));
         ER_CUDA(cudaStreamBeginCapture(b.capture_stream, cudaStreamCaptureModeThreadLocal));
@@ -836,7 +847,7 @@ uint64_t tune_key(const TracerItem& t, const VolumeItem& v, int probe_spp)
     er_render_settings s = t.d.settings;
     s.majorant_brick = 0;
     s.tune_primary = s.tune_shadow = s.tune_shade = 0;
-    s.tune_persistent = 0;
+    s.tune_stages = 0;
     s.seed = 0;
     s.bilateral = 0;
     s.bilateral_radius = 0;
@@ -870,7 +881,7 @@ bool tune_cache_lookup(uint64_t key, er_tune_result& r)
             r.tune_shadow = sh;
             r.tune_shade = sd;
             r.msamples_per_s = m;
-            r.tune_persistent = pt;
+            r.tune_stages = pt;
             found = true;          /* the last entry for a key wins */
         }
     }
@@ -888,7 +899,7 @@ void tune_cache_store(uint64_t key, const er_tune_result& r)
     FILE* f = fopen(path.c_str(), "a");
     if (!f) return;
     fprintf(f, "%016llx %d %d %d %d %.3f %d\n", (unsigned long long)key, r.majorant_brick, r.tune_primary, r.tune_shadow, r.tune_shade,
-            r.msamples_per_s, r.tune_persistent);
+            r.msamples_per_s, r.tune_stages);
     fclose(f);
 }
 
@@ -1505,6 +1516,64 @@ ER_API er_status er_batch_set_tuning(int32_t batch_id, int32_t tune_primary, int
     return ER_OK;
 }
 
+ER_API er_status er_batch_set_stages(int32_t batch_id, int32_t tune_stages)
+{
+    ER_LOCK;
+    BatchItem* b = find_batch(batch_id);
+    if (!b) return fail(ER_ERR_INVALID_ID, "batch with ID:%d does not exist", batch_id);
+    if (tune_stages < 0 || tune_stages > (3 | ER_TUNE_NO_SKIP))
+        return fail(ER_ERR_INVALID_ARGUMENT, "tune_stages %d is not ER_PERSISTENT_* with ER_TUNE_NO_SKIP_* bits", tune_stages);
+    b->tune_stages = tune_stages;
+    b->stages_explicit = true;
+    b->planned = false;   /* re-captured at the next launch */
+    return ER_OK;
+}
+
+ER_API er_status er_batch_autotune(int32_t batch_id, void* stream, int32_t* tune_stages, float* msamples_per_s)
+{
+    ER_LOCK;
+    BatchItem* b = find_batch(batch_id);
+    if (!b) return fail(ER_ERR_INVALID_ID, "batch with ID:%d does not exist", batch_id);
+    double samples = 0.0;
+    for (const er_batch_view& v : b->views) {
+        const TracerItem* t = find_tracer(v.tracer_id);
+        const int W = v.camera ? v.camera->film_size[0] : (t ? t->W : 0);
+        const int H = v.camera ? v.camera->film_size[1] : (t ? t->H : 0);
+        samples += (double)W * H * v.spp;
+    }
+    /* persistent-lane modes with the skip in both, one or neither tracking stage */
+    const int candidates[] = {ER_PERSISTENT_BOTH, ER_PERSISTENT_BOTH | ER_TUNE_NO_SKIP_SHADOW, ER_PERSISTENT_BOTH | ER_TUNE_NO_SKIP,
+                              ER_PERSISTENT_SHADOW, ER_PERSISTENT_SHADOW | ER_TUNE_NO_SKIP_SHADOW, ER_PERSISTENT_SHADOW | ER_TUNE_NO_SKIP,
+                              ER_PERSISTENT_NONE | ER_TUNE_NO_SKIP_SHADOW, ER_PERSISTENT_NONE | ER_TUNE_NO_SKIP};
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t a = nullptr, e = nullptr;
+    ER_CUDA(cudaEventCreate(&a));
+    ER_CUDA(cudaEventCreate(&e));
+    int best = -1;
+    float best_rate = -1.0f;
+    for (int c : candidates) {
+        er_status rs = er_batch_set_stages(batch_id, c);
+        if (rs == ER_OK) rs = er_batch_launch(batch_id, stream);          /* plans and captures */
+        if (rs != ER_OK) { cudaEventDestroy(a); cudaEventDestroy(e); return rs; }
+        ER_CUDA(cudaEventRecord(a, st));
+        rs = er_batch_launch(batch_id, stream);
+        if (rs != ER_OK) { cudaEventDestroy(a); cudaEventDestroy(e); return rs; }
+        ER_CUDA(cudaEventRecord(e, st));
+        ER_CUDA(cudaEventSynchronize(e));
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, a, e);
+        const float rate = ms > 0.0f ? (float)(samples / (ms * 1e3)) : 0.0f;
+        if (rate > best_rate) { best_rate = rate; best = c; }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(e);
+    er_status rs = er_batch_set_stages(batch_id, best);
+    if (rs != ER_OK) return rs;
+    if (tune_stages) *tune_stages = best;
+    if (msamples_per_s) *msamples_per_s = best_rate;
+    return ER_OK;
+}
+
 ER_API er_status er_batch_info(int32_t batch_id, int32_t* n_windows, int32_t* n_segments, int64_t* queue_bytes)
 {
     ER_LOCK;
@@ -1557,33 +1626,40 @@ ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tun
         /* majorant brick first (the dominant term for delta tracking), then
            the occupancy variants at the best brick */
         const int bricks[] = {1, 2, 4, 8, 16};
+        const int base_stages = s.tune_stages & 3;
+        r.tune_stages = s.tune_stages;
         for (int b : bricks) {
             if (!delta && b != r.majorant_brick) continue;
-            s.majorant_brick = b;
-            float m = 0.0f;
-            st = time_probe(*t, probe_spp, &m);
-            if (st != ER_OK) {
-                /* a brick size whose grid does not fit (memory, launch limits) is
-                   skipped; a fault that poisons the context ends the sweep */
-                if (cudaDeviceSynchronize() != cudaSuccess) { s = saved; t->built = false; return st; }
-                cudaGetLastError();
-                continue;
+            const int skips[] = {0, ER_TUNE_NO_SKIP_SHADOW, ER_TUNE_NO_SKIP};
+            for (int si = 0; si < (delta ? 3 : 1); si++) {
+                s.majorant_brick = b;
+                s.tune_stages = base_stages | skips[si];
+                float m = 0.0f;
+                st = time_probe(*t, probe_spp, &m);
+                if (st != ER_OK) {
+                    /* a brick size whose grid does not fit (memory, launch limits) is
+                       skipped; a fault that poisons the context ends the sweep */
+                    if (cudaDeviceSynchronize() != cudaSuccess) { s = saved; t->built = false; return st; }
+                    cudaGetLastError();
+                    continue;
+                }
+                r.candidates++;
+                if (m > r.msamples_per_s) { r.msamples_per_s = m; r.majorant_brick = b; r.tune_stages = s.tune_stages; }
             }
-            r.candidates++;
-            if (m > r.msamples_per_s) { r.msamples_per_s = m; r.majorant_brick = b; }
         }
         if (r.msamples_per_s < 0.0f) { s = saved; t->built = false; return fail(ER_ERR_CUDA, "no majorant brick size could be timed"); }
         s.majorant_brick = r.majorant_brick;
+        s.tune_stages = r.tune_stages;
+        const int skip_bit = r.tune_stages & ER_TUNE_NO_SKIP;
         if (wavefront) {
             /* occupancy pairs, with persistent-lane tracking stages or not (delta tracking) */
-            const int variants[][2] = {{4, 4}, {3, 3}, {3, 4}, {4, 3}, {6, 4}, {4, 6}, {2, 3}, {8, 8}};
+            const int variants[][2] = {{4, 4}, {3, 3}, {3, 4}, {4, 3}, {2, 3}, {3, 2}, {2, 2}, {2, 4}};
             const int modes_delta[] = {ER_PERSISTENT_SHADOW, ER_PERSISTENT_BOTH, ER_PERSISTENT_NONE};
             const int modes_march[] = {ER_PERSISTENT_SHADOW};
             const int* modes = delta ? modes_delta : modes_march;
             const int n_modes = delta ? 3 : 1;
-            r.tune_persistent = s.tune_persistent;
             for (int mi = 0; mi < n_modes; mi++) {
-                s.tune_persistent = modes[mi];
+                s.tune_stages = modes[mi] | skip_bit;
                 for (const auto& vv : variants) {
                     s.tune_primary = vv[0];
                     s.tune_shadow = vv[1];
@@ -1595,13 +1671,13 @@ ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tun
                         r.msamples_per_s = m;
                         r.tune_primary = vv[0];
                         r.tune_shadow = vv[1];
-                        r.tune_persistent = modes[mi];
+                        r.tune_stages = modes[mi] | skip_bit;
                     }
                 }
             }
             s.tune_primary = r.tune_primary;
             s.tune_shadow = r.tune_shadow;
-            s.tune_persistent = r.tune_persistent;
+            s.tune_stages = r.tune_stages;
             const int shades[] = {2, 3, 4, 6};
             for (int sd : shades) {
                 s.tune_shade = sd;
@@ -1618,7 +1694,7 @@ ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tun
     s.tune_primary = r.tune_primary;
     s.tune_shadow = r.tune_shadow;
     s.tune_shade = r.tune_shade;
-    s.tune_persistent = r.tune_persistent;
+    s.tune_stages = r.tune_stages;
     t->built = false;
     C.version++;            /* batches over this tracer re-plan */
     st = build(*t);

@@ -105,6 +105,50 @@ cudaError_t er_launch_majorant(const uint16_t* vox, const int res[3], int B, con
     return cudaGetLastError();
 }
 
+/* Empty-space distances of the majorant grid.  For an empty brick (majorant
+   0) dist = min over non-empty bricks q of max_a |b_a - q_a| (Chebyshev
+   distance in bricks), capped at ER_SKIP_CAP; computed exactly by three 1D
+   passes (x: nearest non-empty along the row; y and z: min over offsets of
+   max(offset, previous pass)).  The last pass writes -dist into the empty
+   bricks of the majorant grid: a tracker in such a brick knows every brick
+   within dist-1 of it is empty too (er_path.cuh dda_skip). */
+#define ER_SKIP_CAP 32
+
+__global__ void k_skip_pass(const float* __restrict__ majorant, const uint8_t* __restrict__ in, uint8_t* __restrict__ out,
+                            float* __restrict__ majorant_out, int axis, int nbx, int nby, int nbz, long long total)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+        const int b[3] = { (int)(i % nbx), (int)((i / nbx) % nby), (int)(i / ((long long)nbx * nby)) };
+        const int n = axis == 0 ? nbx : (axis == 1 ? nby : nbz);
+        const long long step = axis == 0 ? 1 : (axis == 1 ? (long long)nbx : (long long)nbx * nby);
+        int best = ER_SKIP_CAP;
+        for (int o = -(ER_SKIP_CAP - 1); o <= ER_SKIP_CAP - 1; o++) {
+            const int c = b[axis] + o;
+            if (c < 0 || c >= n) continue;
+            const int ao = o < 0 ? -o : o;
+            if (ao >= best) continue;
+            const long long j = i + (long long)o * step;
+            const int v = axis == 0 ? (majorant[j] > 0.0f ? 0 : ER_SKIP_CAP) : (int)in[j];
+            const int d = v > ao ? v : ao;
+            best = d < best ? d : best;
+        }
+        if (axis < 2) out[i] = (uint8_t)best;
+        else if (!(majorant_out[i] > 0.0f)) majorant_out[i] = -(float)best;
+    }
+}
+
+cudaError_t er_launch_empty_skip(float* majorant, const int nb[3], uint8_t* tmp, cudaStream_t s)
+{
+    const long long total = (long long)nb[0] * nb[1] * nb[2];
+    const long long want = (total + 255) / 256;
+    const unsigned blocks = (unsigned)(want < 65536 ? want : 65536);
+    k_skip_pass<<<blocks, 256, 0, s>>>(majorant, nullptr, tmp, nullptr, 0, nb[0], nb[1], nb[2], total);
+    k_skip_pass<<<blocks, 256, 0, s>>>(majorant, tmp, tmp + total, nullptr, 1, nb[0], nb[1], nb[2], total);
+    k_skip_pass<<<blocks, 256, 0, s>>>(majorant, tmp + total, nullptr, majorant, 2, nb[0], nb[1], nb[2], total);
+    return cudaGetLastError();
+}
+
 /* corner quads: for voxel (x, y, z) the intensities at (x, y), (x+1, y),
    (x, y+1), (x+1, y+1) of slice z, packed as two uint16 pairs, so that a
    trilinear lookup reads two 8-byte words instead of eight 2-byte ones */

@@ -89,7 +89,7 @@ ER_D int find_segment(const WfSegment* __restrict__ segs, int nseg, uint32_t i)
    (2: 128 registers, 3: ~80, 4: 64, 6: 40, 8: 32); picked at run time */
 /* OBJ: the variant that also intersects surface objects (scenes without
    objects run the lean one) */
-template <int MINB, bool ONE, bool OBJ>
+template <int MINB, bool ONE, bool OBJ, bool SKIP>
 __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restrict__ views, const WfSegment* __restrict__ segs, int nseg,
                                                            const WfView one, const WfSegment one_seg, uint32_t items,
                                                            float4* __restrict__ results, float4* __restrict__ events,
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
             se0.P = V3(0, 0, 0); se0.N = V3(0, 0, 0); se0.Wo = V3(0, 0, 0);
             se1 = se0; se1.type = 1;
             /* the event normal (no RNG) is computed by the shade stage */
-            if (P.free_flight == 1) sample_volume_delta<false>(P, R, rng, se0);
+            if (P.free_flight == 1) sample_volume_delta<false, SKIP>(P, R, rng, se0);
             else sample_volume<false>(P, R, rng, se0);
             intersect_lights(P, R, se1, true);
             SE = se0; SE.valid = false; SE.type = 0;
@@ -189,7 +189,7 @@ ER_D uint32_t queue_slot_active(bool want, uint32_t* counter)
    warp), while the other lanes keep their rays.  The MetroSample values an event
    record carries are drawn again from the sample's seed when the sample
    finishes instead of being held through the tracking. */
-template <int MINB, bool ONE, bool OBJ>
+template <int MINB, bool ONE, bool OBJ, bool SKIP>
 __global__ void __launch_bounds__(256, MINB) k_wf_primary_pt(const WfView* __restrict__ views, const WfSegment* __restrict__ segs,
                                                               int nseg, const WfView one, const WfSegment one_seg, uint32_t items,
                                                               float4* __restrict__ results, float4* __restrict__ events,
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary_pt(const WfView* __res
         /* track until a quarter of the lanes that were tracking have ended */
         const int n_work = __popc(__ballot_sync(0xffffffffu, tracking && !k.done));
         while (tracking && !k.done) {
-            delta_step(P, R, rng, k);
+            delta_step<SKIP>(P, R, rng, k);
             if (k.done || 4 * __popc(__activemask()) < 3 * n_work) break;
         }
         if (!tracking || !k.done) continue;
@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict
 
 /* ---- stage 3: shadow segments and the sample's sum ---- */
 
-template <int MINB, bool ONE, bool OBJ>
+template <int MINB, bool ONE, bool OBJ, bool SKIP>
 __global__ void __launch_bounds__(256, MINB) k_wf_shadow(const WfView* __restrict__ views, const WfView one, const float4* __restrict__ jobs,
                                                           const uint32_t* __restrict__ n_jobs, float4* __restrict__ results)
 {
@@ -479,14 +479,14 @@ __global__ void __launch_bounds__(256, MINB) k_wf_shadow(const WfView* __restric
         const c3 Le = C3(j2.w, j3.w, j4.w);
         c3 dl = C3(0, 0, 0);
         if (flags & WF_RAY1) {
-            const float Tr = visibility<OBJ>(P, Pp, V3(j2.x, j2.y, j2.z), rng);
+            const float Tr = visibility<OBJ, SKIP>(P, Pp, V3(j2.x, j2.y, j2.z), rng);
             if (Tr > 0.0f) {
                 const c3 c1 = C3(j3.x, j3.y, j3.z);
                 dl = ref_mode ? cadd(dl, c1) : cadd(dl, cscale(c1, Tr));
             }
         }
         if (flags & WF_RAY2) {
-            const float Tr = visibility<OBJ>(P, Pp, V3(j4.x, j4.y, j4.z), rng);
+            const float Tr = visibility<OBJ, SKIP>(P, Pp, V3(j4.x, j4.y, j4.z), rng);
             if (Tr > 0.0f) dl = cadd(dl, cscale(C3(j5.x, j5.y, j5.z), Tr));
         }
         const c3 Lv = cadd(C3(0, 0, 0), cscale(cadd(Le, dl), count));
@@ -503,7 +503,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_shadow(const WfView* __restric
    one atomic per warp) and tracks on.  In k_wf_shadow a warp runs until its
    longest segment ends while the other lanes idle (5.5 of 32 lanes active
    per instruction on the c2 workload). */
-template <int MINB, bool ONE, bool OBJ>
+template <int MINB, bool ONE, bool OBJ, bool SKIP>
 __global__ void __launch_bounds__(256, MINB) k_wf_shadow_pt(const WfView* __restrict__ views, const WfView one,
                                                              const float4* __restrict__ jobs, const uint32_t* __restrict__ n_jobs,
                                                              float4* __restrict__ results, uint32_t* __restrict__ fetch)
@@ -564,7 +564,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_shadow_pt(const WfView* __rest
         /* track until a quarter of the lanes that were tracking have ended */
         const int n_work = __popc(__ballot_sync(0xffffffffu, seg_phase && !k.done));
         while (seg_phase && !k.done) {
-            ratio_step(P, R, rng, k);
+            ratio_step<SKIP>(P, R, rng, k);
             if (k.done || 4 * __popc(__activemask()) < 3 * n_work) break;
         }
         if (seg_phase && k.done) {
@@ -735,6 +735,10 @@ int sm_count()
     return sm > 0 ? sm : 132;
 }
 
+/* occupancy variants of the persistent and empty-space-skipping stages: 2,
+   3 or 4 resident blocks per SM (other values run 4) */
+int narrow_minb(int m) { return (m == 2 || m == 3) ? m : 4; }
+
 template <bool ONE>
 cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const WfView& one, const WavefrontPlan& plan,
                            const WavefrontBuffers& B, cudaStream_t s)
@@ -754,25 +758,39 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         if (e != cudaSuccess) return e;
         const uint32_t g1 = (items + 255) / 256 < (uint32_t)sm * 64 ? (items + 255) / 256 : (uint32_t)sm * 64;
         cudaEvent_t t0 = stage_begin(s);
-#define ER_PRIMARY(M, O) k_wf_primary<M, ONE, O><<<g1, 256, 0, s>>>(d_views, dseg, nseg, one, one_seg, items, B.results, B.events, B.counters)
-#define ER_PRIMARY_PT(M, O) k_wf_primary_pt<M, ONE, O><<<sm * M, 256, 0, s>>>(d_views, dseg, nseg, one, one_seg, items, B.results, B.events, B.counters, B.counters + 2)
+#define ER_PRIMARY(M, O, K) k_wf_primary<M, ONE, O, K><<<g1, 256, 0, s>>>(d_views, dseg, nseg, one, one_seg, items, B.results, B.events, B.counters)
+#define ER_PRIMARY_PT(M, O, K) k_wf_primary_pt<M, ONE, O, K><<<sm * M, 256, 0, s>>>(d_views, dseg, nseg, one, one_seg, items, B.results, B.events, B.counters, B.counters + 2)
         if (B.pt_primary) {
             /* delta tracking: persistent lanes, one resident wave */
-            if (B.objects) ER_PRIMARY_PT(4, true);
-            else switch (B.tune_primary) {
-            case 2: ER_PRIMARY_PT(2, false); break;
-            case 3: ER_PRIMARY_PT(3, false); break;
-            case 6: ER_PRIMARY_PT(6, false); break;
-            case 8: ER_PRIMARY_PT(8, false); break;
-            default: ER_PRIMARY_PT(4, false); break;
+            if (B.objects) ER_PRIMARY_PT(4, true, true);
+            else if (B.skip_primary) {
+                switch (narrow_minb(B.tune_primary)) {
+                case 2: ER_PRIMARY_PT(2, false, true); break;
+                case 3: ER_PRIMARY_PT(3, false, true); break;
+                default: ER_PRIMARY_PT(4, false, true); break;
+                }
+            } else {
+                switch (narrow_minb(B.tune_primary)) {
+                case 2: ER_PRIMARY_PT(2, false, false); break;
+                case 3: ER_PRIMARY_PT(3, false, false); break;
+                default: ER_PRIMARY_PT(4, false, false); break;
+                }
             }
-        } else if (B.objects) ER_PRIMARY(4, true);
-        else switch (B.tune_primary) {
-        case 2: ER_PRIMARY(2, false); break;
-        case 3: ER_PRIMARY(3, false); break;
-        case 6: ER_PRIMARY(6, false); break;
-        case 8: ER_PRIMARY(8, false); break;
-        default: ER_PRIMARY(4, false); break;
+        } else if (B.objects) ER_PRIMARY(4, true, true);
+        else if (B.skip_primary) {
+            switch (narrow_minb(B.tune_primary)) {
+            case 2: ER_PRIMARY(2, false, true); break;
+            case 3: ER_PRIMARY(3, false, true); break;
+            default: ER_PRIMARY(4, false, true); break;
+            }
+        } else {
+            switch (B.tune_primary) {
+            case 2: ER_PRIMARY(2, false, false); break;
+            case 3: ER_PRIMARY(3, false, false); break;
+            case 6: ER_PRIMARY(6, false, false); break;
+            case 8: ER_PRIMARY(8, false, false); break;
+            default: ER_PRIMARY(4, false, false); break;
+            }
         }
 #undef ER_PRIMARY_PT
 #undef ER_PRIMARY
@@ -789,25 +807,39 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
 #undef ER_SHADE
         stage_end(t0, 1, s);
         t0 = stage_begin(s);
-#define ER_SHADOW(M, O) k_wf_shadow<M, ONE, O><<<sm * 8, 256, 0, s>>>(d_views, one, B.jobs, B.counters + 1, B.results)
-#define ER_SHADOW_PT(M, O) k_wf_shadow_pt<M, ONE, O><<<sm * M, 256, 0, s>>>(d_views, one, B.jobs, B.counters + 1, B.results, B.counters + 3)
+#define ER_SHADOW(M, O, K) k_wf_shadow<M, ONE, O, K><<<sm * 8, 256, 0, s>>>(d_views, one, B.jobs, B.counters + 1, B.results)
+#define ER_SHADOW_PT(M, O, K) k_wf_shadow_pt<M, ONE, O, K><<<sm * M, 256, 0, s>>>(d_views, one, B.jobs, B.counters + 1, B.results, B.counters + 3)
         if (B.pt_shadow) {
             /* ratio-tracked shadows: persistent lanes, one resident wave */
-            if (B.objects) ER_SHADOW_PT(4, true);
-            else switch (B.tune_shadow) {
-            case 2: ER_SHADOW_PT(2, false); break;
-            case 3: ER_SHADOW_PT(3, false); break;
-            case 6: ER_SHADOW_PT(6, false); break;
-            case 8: ER_SHADOW_PT(8, false); break;
-            default: ER_SHADOW_PT(4, false); break;
+            if (B.objects) ER_SHADOW_PT(4, true, true);
+            else if (B.skip_shadow) {
+                switch (narrow_minb(B.tune_shadow)) {
+                case 2: ER_SHADOW_PT(2, false, true); break;
+                case 3: ER_SHADOW_PT(3, false, true); break;
+                default: ER_SHADOW_PT(4, false, true); break;
+                }
+            } else {
+                switch (narrow_minb(B.tune_shadow)) {
+                case 2: ER_SHADOW_PT(2, false, false); break;
+                case 3: ER_SHADOW_PT(3, false, false); break;
+                default: ER_SHADOW_PT(4, false, false); break;
+                }
             }
-        } else if (B.objects) ER_SHADOW(4, true);
-        else switch (B.tune_shadow) {
-        case 2: ER_SHADOW(2, false); break;
-        case 3: ER_SHADOW(3, false); break;
-        case 6: ER_SHADOW(6, false); break;
-        case 8: ER_SHADOW(8, false); break;
-        default: ER_SHADOW(4, false); break;
+        } else if (B.objects) ER_SHADOW(4, true, true);
+        else if (B.skip_shadow) {
+            switch (narrow_minb(B.tune_shadow)) {
+            case 2: ER_SHADOW(2, false, true); break;
+            case 3: ER_SHADOW(3, false, true); break;
+            default: ER_SHADOW(4, false, true); break;
+            }
+        } else {
+            switch (B.tune_shadow) {
+            case 2: ER_SHADOW(2, false, false); break;
+            case 3: ER_SHADOW(3, false, false); break;
+            case 6: ER_SHADOW(6, false, false); break;
+            case 8: ER_SHADOW(8, false, false); break;
+            default: ER_SHADOW(4, false, false); break;
+            }
         }
 #undef ER_SHADOW_PT
 #undef ER_SHADOW

@@ -136,9 +136,9 @@ class Renderer:
         s = self.tracer_desc.settings
         s.majorant_brick, s.tune_primary, s.tune_shadow = r.majorant_brick, r.tune_primary, r.tune_shadow
         s.tune_shade = r.tune_shade
-        s.tune_persistent = r.tune_persistent
+        s.tune_stages = r.tune_stages
         return {"majorant_brick": r.majorant_brick, "tune_primary": r.tune_primary, "tune_shadow": r.tune_shadow,
-                "tune_shade": r.tune_shade, "tune_persistent": r.tune_persistent,
+                "tune_shade": r.tune_shade, "tune_stages": r.tune_stages,
                 "from_cache": bool(r.from_cache), "msamples_per_s": r.msamples_per_s, "candidates": r.candidates}
 
     def gradient_magnitude(self, d_gm_ptr=None) -> float:
@@ -206,6 +206,16 @@ class Batch:
 
     def set_tuning(self, primary: int = 0, shadow: int = 0) -> None:
         C.check(self.lib.er_batch_set_tuning(self.batch_id, primary, shadow))
+
+    def set_stages(self, tune_stages: int) -> None:
+        C.check(self.lib.er_batch_set_stages(self.batch_id, tune_stages))
+
+    def autotune(self, stream=None) -> dict:
+        """er_batch_autotune: the fastest tune_stages for this batch, timed on
+        whole launches (the views' sums are rendered into)"""
+        st, m = c_int32(0), ctypes.c_float(0.0)
+        C.check(self.lib.er_batch_autotune(self.batch_id, stream, byref(st), byref(m)))
+        return {"tune_stages": st.value, "msamples_per_s": m.value}
 
     def info(self) -> dict:
         w, s, q = c_int32(0), c_int32(0), ctypes.c_int64(0)

@@ -220,19 +220,29 @@ typedef struct er_render_settings {
     int32_t tune_shadow;          /* wavefront: same for the shadow stage (0 or other values: 4) */
     int32_t tune_shade;           /* wavefront: resident 128-thread blocks per SM of the shade stage
                                      (2, 3, 4 or 6; 0 or other values: 2) */
-    int32_t tune_persistent;      /* delta tracking, wavefront: which tracking stages run persistent lanes
-                                     (ER_PERSISTENT_*; 0: the shadow stage only) */
+    int32_t tune_stages;          /* delta tracking: bits 0-1 which wavefront tracking stages run persistent
+                                     lanes (ER_PERSISTENT_*; 0: the shadow stage only); bits 2 and 3
+                                     (ER_TUNE_NO_SKIP_PRIMARY, ER_TUNE_NO_SKIP_SHADOW) turn empty-space
+                                     skipping off in the free-flight and shadow stages */
 } er_render_settings;
 
-/* tune_persistent: the persistent-lane stages keep every warp's lanes busy by
-   handing a lane whose ray ended the next ray of the window; the per-thread
-   stages keep neighbouring pixels' rays together in a warp */
+/* tune_stages bits 0-1: the persistent-lane stages keep every warp's lanes
+   busy by handing a lane whose ray ended the next ray of the window; the
+   per-thread stages keep neighbouring pixels' rays together in a warp */
 enum {
     ER_PERSISTENT_SHADOW = 0,     /* persistent shadow stage, per-thread primary stage */
     ER_PERSISTENT_BOTH = 1,
     ER_PERSISTENT_NONE = 2,
     ER_PERSISTENT_PRIMARY = 3
 };
+/* tune_stages bits 2, 3: no empty-space skipping in the free-flight or the
+   shadow stage.  With skipping, each empty majorant brick stores its
+   distance to the nearest non-empty brick and the trackers cross the empty
+   bricks around it without reading their majorants; images are
+   bit-identical either way. */
+#define ER_TUNE_NO_SKIP_PRIMARY 4
+#define ER_TUNE_NO_SKIP_SHADOW 8
+#define ER_TUNE_NO_SKIP (ER_TUNE_NO_SKIP_PRIMARY | ER_TUNE_NO_SKIP_SHADOW)
 
 /* ErTracer (Source/ertracer.h:33-117).  light_ids/object_ids/clipping_ids are
    item IDs returned by the bind calls. */
@@ -413,6 +423,17 @@ ER_API er_status er_batch_advance(int32_t batch_id, uint32_t samples, void* stre
    or 8 resident blocks of 256 threads per SM; 0 keeps the current value).
    Without this call a batch uses the settings of its first view's tracer. */
 ER_API er_status er_batch_set_tuning(int32_t batch_id, int32_t tune_primary, int32_t tune_shadow);
+/* The tracking stages' persistent-lane mode and empty-space skips of a batch
+   (tune_stages of er_render_settings: ER_PERSISTENT_* | ER_TUNE_NO_SKIP_*).
+   Without this call (or er_batch_autotune) a batch uses its first view's
+   tracer's value. */
+ER_API er_status er_batch_set_stages(int32_t batch_id, int32_t tune_stages);
+/* Times one launch of the whole batch under each of eight tune_stages
+   candidates (after one untimed launch that captures it) and keeps the
+   fastest: the batch, not a one-view probe, is what runs with it.  The
+   views' sums are rendered into (accumulating views accumulate), so reset
+   them afterwards.  Synchronous. */
+ER_API er_status er_batch_autotune(int32_t batch_id, void* stream, int32_t* tune_stages, float* msamples_per_s);
 /* Windows, segments and queue bytes of the plan. */
 ER_API er_status er_batch_info(int32_t batch_id, int32_t* n_windows, int32_t* n_segments, int64_t* queue_bytes);
 ER_API er_status er_batch_destroy(int32_t batch_id);
@@ -481,12 +502,14 @@ typedef struct er_tune_result {
     float msamples_per_s;     /* probe throughput of the chosen configuration */
     int32_t candidates;       /* configurations timed */
     int32_t tune_shade;       /* occupancy variant of the shade stage */
-    int32_t tune_persistent;  /* ER_PERSISTENT_* of the chosen configuration */
+    int32_t tune_stages;      /* tune_stages of the chosen configuration (ER_PERSISTENT_*, ER_TUNE_NO_SKIP_*) */
 } er_tune_result;
 
 /* Times probe renders of a bound tracer (probe_spp samples per pixel of its
    film, raised to at least 2^21 samples per probe, one warm-up each) over
-   majorant bricks {1, 2, 4, 8, 16} (delta tracking only), then the occupancy
+   majorant bricks {1, 2, 4, 8, 16} with empty-space skipping in both
+   tracking stages, the free-flight stage only or neither (delta tracking
+   only), then the occupancy
    variants of the wavefront stages under each persistent-lane mode
    (ER_PERSISTENT_*, delta tracking only), and last the shade stage's
    variants, and writes the fastest configuration into the bound tracer's

@@ -300,3 +300,27 @@ def test_stage_profiler(torch, lib, pair):
     C.check(lib.er_trace_sum_device(ra.tracer_id, 1, 0, 0, d.data_ptr(), 0, None))
     C.check(lib.er_profile_read(ms.ctypes.data, n.ctypes.data))
     assert list(n) == [0, 0, 0, 0]
+
+
+def test_batch_stages_and_autotune(torch, lib, pair):
+    """a batch's tune_stages (set or autotuned on whole launches) changes which
+    kernels run, not the sums"""
+    ra, rb = pair
+    table = [(rb, None, 3, 1, 0), (rb, S.orbit_camera(np.random.default_rng(2), (40, 24), radius=2.1), 2, 2, 0)]
+    ref = expected(torch, lib, table)
+    bid, outs = make_batch(torch, lib, table, C.ER_BATCH_GRAPH, 0)
+    for stages in (1, 1 | C.TUNE_NO_SKIP, 2, 3 | C.TUNE_NO_SKIP_SHADOW):
+        C.check(lib.er_batch_set_stages(bid, stages))
+        C.check(lib.er_batch_launch(bid, None))
+        torch.cuda.synchronize()
+        for k, d in enumerate(outs):
+            assert np.array_equal(bits(d.cpu().numpy()), bits(ref[k])), (stages, k)
+    st, m = ctypes.c_int32(-1), ctypes.c_float(0.0)
+    C.check(lib.er_batch_autotune(bid, None, ctypes.byref(st), ctypes.byref(m)))
+    assert 0 <= st.value <= 15 and m.value > 0
+    C.check(lib.er_batch_launch(bid, None))
+    torch.cuda.synchronize()
+    for k, d in enumerate(outs):
+        assert np.array_equal(bits(d.cpu().numpy()), bits(ref[k]))
+    assert lib.er_batch_set_stages(bid, 16) == C.ER_ERR_INVALID_ARGUMENT
+    C.check(lib.er_batch_destroy(bid))

@@ -126,17 +126,19 @@ def test_majorant_grid_device_bit_exact(env, oracle, shape, brick):
     assert want.max() > 0
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2, 3], ids=["shadow", "both", "none", "primary"])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 0 | 12, 1 | 12, 1 | 8, 2 | 4], ids=["shadow", "both", "none", "primary", "shadow-noskip",
+                                                                        "both-noskip", "both-skip-primary", "none-skip-shadow"])
 def test_persistent_stage_modes_bit_exact(env, oracle, mode):
-    """every persistent-lane mode of the delta-tracking stages (tune_persistent)
-    gives the oracle's sums, alone and with the hybrid shader and full MIS"""
+    """every persistent-lane mode of the delta-tracking stages, with and
+    without empty-space skipping (tune_stages), gives the oracle's sums with
+    the hybrid shader and full MIS"""
     torch, lib, rt = env
     sc = two_light_scene(13)
     sc.tracer.settings.free_flight = 1
     sc.tracer.settings.mis = 1
     sc.tracer.settings.apply_shading_type = 1
     sc.tracer.settings.shading_type = 2
-    sc.tracer.settings.tune_persistent = mode
+    sc.tracer.settings.tune_stages = mode
     r = rt.Renderer(sc, lib)
     h = OL.SceneHandle(oracle, sc)
     try:
