@@ -458,7 +458,7 @@ def run_ours(args, wl, rank, world, local_rank):
     if rank != 0:
         return
     conv = None
-    if world == 1 and not args.no_rmse and wl == "c3":
+    if world == 1 and not args.no_rmse and wl == "c2":
         conv = convergence(lib, runtime, torch, ["c2"], {
             "fast": {"free_flight": 1, "majorant_brick": r.tracer_desc.settings.majorant_brick},
             "plain": {"free_flight": 0}})
