@@ -548,6 +548,14 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
     # the tracking stages' persistent-lane mode and empty-space skips, timed
     # on whole launches of this batch
     batch_tune = batch.autotune(sp) if not args.no_tune else None
+    if batch_tune:
+        # the batch tuner writes the tracers' bricks: keep the Python-side
+        # descriptors in step, so that later rebinds keep them
+        for r in rs:
+            st = C.er_render_settings()
+            C.check(lib.er_get_render_settings(r.tracer_id, st))
+            r.tracer_desc.settings = st
+        batch_tune["bricks"] = [r.tracer_desc.settings.majorant_brick for r in rs]
     info = batch.info()
 
     def timed(fn, steps):

@@ -1541,37 +1541,75 @@ ER_API er_status er_batch_autotune(int32_t batch_id, void* stream, int32_t* tune
         const int H = v.camera ? v.camera->film_size[1] : (t ? t->H : 0);
         samples += (double)W * H * v.spp;
     }
-    /* persistent-lane modes with the skip in both, one or neither tracking stage */
-    const int candidates[] = {ER_PERSISTENT_BOTH, ER_PERSISTENT_BOTH | ER_TUNE_NO_SKIP_SHADOW, ER_PERSISTENT_BOTH | ER_TUNE_NO_SKIP,
-                              ER_PERSISTENT_SHADOW, ER_PERSISTENT_SHADOW | ER_TUNE_NO_SKIP_SHADOW, ER_PERSISTENT_SHADOW | ER_TUNE_NO_SKIP,
-                              ER_PERSISTENT_NONE | ER_TUNE_NO_SKIP_SHADOW, ER_PERSISTENT_NONE | ER_TUNE_NO_SKIP};
     cudaStream_t st = (cudaStream_t)stream;
     cudaEvent_t a = nullptr, e = nullptr;
     ER_CUDA(cudaEventCreate(&a));
     ER_CUDA(cudaEventCreate(&e));
-    int best = -1;
-    float best_rate = -1.0f;
-    for (int c : candidates) {
-        er_status rs = er_batch_set_stages(batch_id, c);
-        if (rs == ER_OK) rs = er_batch_launch(batch_id, stream);          /* plans and captures */
-        if (rs != ER_OK) { cudaEventDestroy(a); cudaEventDestroy(e); return rs; }
+    /* one timed launch of the whole batch in its current configuration
+       (planned and captured first, outside the timed region) */
+    auto time_batch = [&](float* rate) -> er_status {
+        if (!b->planned || b->planned_version != ctx().version) {
+            const er_status ps = batch_plan(*b);
+            if (ps != ER_OK) return ps;
+        }
         ER_CUDA(cudaEventRecord(a, st));
-        rs = er_batch_launch(batch_id, stream);
-        if (rs != ER_OK) { cudaEventDestroy(a); cudaEventDestroy(e); return rs; }
+        const er_status ls = er_batch_launch(batch_id, stream);
+        if (ls != ER_OK) return ls;
         ER_CUDA(cudaEventRecord(e, st));
         ER_CUDA(cudaEventSynchronize(e));
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, a, e);
-        const float rate = ms > 0.0f ? (float)(samples / (ms * 1e3)) : 0.0f;
-        if (rate > best_rate) { best_rate = rate; best = c; }
+        *rate = ms > 0.0f ? (float)(samples / (ms * 1e3)) : 0.0f;
+        return ER_OK;
+    };
+    auto done = [&](er_status rs) { cudaEventDestroy(a); cudaEventDestroy(e); return rs; };
+    float best_rate = 0.0f;
+    er_status rs = time_batch(&best_rate);
+    if (rs != ER_OK) return done(rs);
+    /* each delta-tracking tracer's majorant brick in turn, on whole launches
+       (a brick that helps one view can hurt the others of its volume) */
+    std::vector<int32_t> tids;
+    for (const er_batch_view& v : b->views) {
+        const TracerItem* t = find_tracer(v.tracer_id);
+        if (t && t->d.settings.free_flight == ER_FREE_FLIGHT_DELTA && std::find(tids.begin(), tids.end(), v.tracer_id) == tids.end())
+            tids.push_back(v.tracer_id);
     }
-    cudaEventDestroy(a);
-    cudaEventDestroy(e);
-    er_status rs = er_batch_set_stages(batch_id, best);
-    if (rs != ER_OK) return rs;
+    for (int32_t tid : tids) {
+        TracerItem* t = find_tracer(tid);
+        const int cur = t->d.settings.majorant_brick > 0 ? t->d.settings.majorant_brick : 8;
+        int best_b = cur;
+        for (int bb : {1, 2, 4, 8}) {
+            if (bb == cur) continue;
+            t->d.settings.majorant_brick = bb;
+            t->built = false;
+            ctx().version++;
+            float r = 0.0f;
+            rs = time_batch(&r);
+            if (rs != ER_OK) return done(rs);
+            if (r > best_rate) { best_rate = r; best_b = bb; }
+        }
+        t->d.settings.majorant_brick = best_b;
+        t->built = false;
+        ctx().version++;
+    }
+    /* then the tracking stages' persistent-lane mode and empty-space skips */
+    const int candidates[] = {ER_PERSISTENT_BOTH, ER_PERSISTENT_BOTH | ER_TUNE_NO_SKIP_SHADOW, ER_PERSISTENT_BOTH | ER_TUNE_NO_SKIP,
+                              ER_PERSISTENT_SHADOW, ER_PERSISTENT_SHADOW | ER_TUNE_NO_SKIP_SHADOW, ER_PERSISTENT_SHADOW | ER_TUNE_NO_SKIP,
+                              ER_PERSISTENT_NONE | ER_TUNE_NO_SKIP_SHADOW, ER_PERSISTENT_NONE | ER_TUNE_NO_SKIP};
+    int best = b->tune_stages;
+    for (int c : candidates) {
+        rs = er_batch_set_stages(batch_id, c);
+        if (rs != ER_OK) return done(rs);
+        float r = 0.0f;
+        rs = time_batch(&r);
+        if (rs != ER_OK) return done(rs);
+        if (r > best_rate) { best_rate = r; best = c; }
+    }
+    rs = er_batch_set_stages(batch_id, best);
+    if (rs != ER_OK) return done(rs);
     if (tune_stages) *tune_stages = best;
     if (msamples_per_s) *msamples_per_s = best_rate;
-    return ER_OK;
+    return done(ER_OK);
 }
 
 ER_API er_status er_batch_info(int32_t batch_id, int32_t* n_windows, int32_t* n_segments, int64_t* queue_bytes)

@@ -428,11 +428,13 @@ ER_API er_status er_batch_set_tuning(int32_t batch_id, int32_t tune_primary, int
    Without this call (or er_batch_autotune) a batch uses its first view's
    tracer's value. */
 ER_API er_status er_batch_set_stages(int32_t batch_id, int32_t tune_stages);
-/* Times one launch of the whole batch under each of eight tune_stages
-   candidates (after one untimed launch that captures it) and keeps the
-   fastest: the batch, not a one-view probe, is what runs with it.  The
-   views' sums are rendered into (accumulating views accumulate), so reset
-   them afterwards.  Synchronous. */
+/* Tunes a batch on its own launches (a one-view probe misjudges a batch):
+   times one launch of the whole batch per candidate, first each
+   delta-tracking tracer's majorant brick in {1, 2, 4, 8} in turn (written
+   into that tracer's settings, as er_autotune_tracer does), then eight
+   tune_stages candidates, keeping the fastest of each.  The views' sums are
+   rendered into (accumulating views accumulate), so reset them afterwards.
+   Synchronous. */
 ER_API er_status er_batch_autotune(int32_t batch_id, void* stream, int32_t* tune_stages, float* msamples_per_s);
 /* Windows, segments and queue bytes of the plan. */
 ER_API er_status er_batch_info(int32_t batch_id, int32_t* n_windows, int32_t* n_segments, int64_t* queue_bytes);
