@@ -388,7 +388,7 @@ ER_D v2 concentric_sample_disk(v2 U)   /* Source/montecarlo.h:86-137 */
 struct Surf { v3 P, N; v2 UV; };
 
 /* SampleLightSurface - Source/lights.h:28-42 and the shape samplers */
-ER_D void sample_light_surface(const Light& L, v3 UVW, Surf& SS)
+ER_COLD void sample_light_surface(const Light& L, v3 UVW, Surf& SS)
 {
     SS.P = V3(0, 0, 0); SS.N = V3(0.0f, 0.0f, 1.0f); SS.UV.x = 0.0f; SS.UV.y = 0.0f;
     switch (L.type) {
@@ -585,7 +585,7 @@ ER_D float blinn_pdf(float e, v3 Wo, v3 Wi)
     return pdf;
 }
 
-ER_D c3 microfacet_f(const Shader& sh, v3 Wo, v3 Wi)
+ER_COLD c3 microfacet_f(const Shader& sh, v3 Wo, v3 Wi)
 {
     const float co = fabsf(Wo.z), ci = fabsf(Wi.z);
     if (ci == 0.f || co == 0.f) return C3(0, 0, 0);
@@ -1235,7 +1235,7 @@ ER_D float mis_bsdf_pdf(const Shader& sh, v3 Wo, v3 Wi)
 
 /* Lambertian::SampleF / Blinn::SampleF / IsotropicPhase::SampleF
    (Source/shader.h:46-56, :142-164, :293-299) */
-ER_D v3 sample_bsdf_dir(const Shader& sh, v3 Wo, const Metro& ms)
+ER_COLD v3 sample_bsdf_dir(const Shader& sh, v3 Wo, const Metro& ms)
 {
     if (sh.type == 0) {
         const v3 Wol = world_to_local(sh, Wo);
