@@ -166,6 +166,13 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
     }
 }
 
+/* persistent stages: a warp stops tracking to refill when fewer than
+   ER_PT_REFILL_EIGHTHS / 8 of the lanes that were tracking still are
+   (C3 batch: 3/8 and 4/8 give 1249 and 1240 Msamples/s, 6/8 1138, 7/8 978) */
+#ifndef ER_PT_REFILL_EIGHTHS
+#define ER_PT_REFILL_EIGHTHS 3
+#endif
+
 /* queue slot among the lanes that are here together (persistent stages,
    where lanes reach their queue pushes at different loop trips) */
 ER_D uint32_t queue_slot_active(bool want, uint32_t* counter)
@@ -183,8 +190,8 @@ ER_D uint32_t queue_slot_active(bool want, uint32_t* counter)
 /* ---- stage 1, persistent lanes (delta tracking) ----
 
    The work of k_wf_primary with lanes tracking one tentative collision or
-   majorant brick per inner loop trip: when a quarter of a warp's tracking
-   lanes have ended their rays, the warp finishes those samples and gives the
+   majorant brick per inner loop trip: when most of a warp's tracking lanes
+   have ended their rays, the warp finishes those samples and gives the
    lanes the next items of the window (consecutive ones, one atomic per
    warp), while the other lanes keep their rays.  The MetroSample values an event
    record carries are drawn again from the sample's seed when the sample
@@ -240,11 +247,11 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary_pt(const WfView* __res
         const WfSegment sg = ONE ? one_seg : segs[seg];
         const WfView& V = view_of<ONE>(views, one, sg.view);
         const Params& P = V.P;
-        /* track until a quarter of the lanes that were tracking have ended */
+        /* track until most of the lanes that were tracking have ended */
         const int n_work = __popc(__ballot_sync(0xffffffffu, tracking && !k.done));
         while (tracking && !k.done) {
             delta_step<SKIP>(P, R, rng, k);
-            if (k.done || 4 * __popc(__activemask()) < 3 * n_work) break;
+            if (k.done || 8 * __popc(__activemask()) < ER_PT_REFILL_EIGHTHS * n_work) break;
         }
         if (!tracking || !k.done) continue;
         /* the sample's nearest event: volume, visible lights, objects */
@@ -498,7 +505,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_shadow(const WfView* __restric
 
    The same jobs and arithmetic as k_wf_shadow, with the work split
    differently: lanes track one collision or majorant brick per inner loop
-   trip; when a quarter of a warp's tracking lanes have ended their segments,
+   trip; when most of a warp's tracking lanes have ended their segments,
    the warp starts their next segments or takes new jobs (consecutive ones,
    one atomic per warp) and tracks on.  In k_wf_shadow a warp runs until its
    longest segment ends while the other lanes idle (5.5 of 32 lanes active
@@ -561,11 +568,11 @@ __global__ void __launch_bounds__(256, MINB) k_wf_shadow_pt(const WfView* __rest
         if (!__any_sync(0xffffffffu, phase != 0)) break;
         const bool seg_phase = phase == 1 || phase == 2;
         const Params& P = view_of<ONE>(views, one, v).P;
-        /* track until a quarter of the lanes that were tracking have ended */
+        /* track until most of the lanes that were tracking have ended */
         const int n_work = __popc(__ballot_sync(0xffffffffu, seg_phase && !k.done));
         while (seg_phase && !k.done) {
             ratio_step<SKIP>(P, R, rng, k);
-            if (k.done || 4 * __popc(__activemask()) < 3 * n_work) break;
+            if (k.done || 8 * __popc(__activemask()) < ER_PT_REFILL_EIGHTHS * n_work) break;
         }
         if (seg_phase && k.done) {
             const float4* j = jobs + (size_t)j_i * 6;
