@@ -329,6 +329,7 @@ def reference_path(scene):
     t.settings.free_flight = 0
     t.settings.mis = 0
     t.settings.apply_shading_type = 0
+    t.settings.stratify = 0
     import copy
     out = copy.copy(scene)
     out.tracer = t
@@ -365,8 +366,9 @@ def run_ours(args, wl, rank, world, local_rank):
     C.check(lib.er_set_device(local_rank))
     W = WORKLOADS[wl]
     scene = make_scene(wl)
-    scene.tracer.settings.free_flight = 1                # the fast path: delta tracking, full MIS
-    scene.tracer.settings.mis = 1
+    scene.tracer.settings.free_flight = 1                # the fast path: delta tracking, full MIS,
+    scene.tracer.settings.mis = 1                        # stratified light samples
+    scene.tracer.settings.stratify = 1
     shading = describe_shading(scene)
     scene.tracer.settings.seed = R.view_seed(1, rank)    # one replica view per rank
     r = runtime.Renderer(scene, lib)
@@ -425,8 +427,8 @@ def run_ours(args, wl, rank, world, local_rank):
         r.rebind_tracer()
         return samples_per_step / (a.elapsed_time(b) / 1e3) / 1e6
 
-    plain = timed_plain({"free_flight": 0})
-    ref_order = timed_plain({"free_flight": 0, "mis": 0, "apply_shading_type": 0, "bilateral": 0})
+    plain = timed_plain({"free_flight": 0, "stratify": 0})
+    ref_order = timed_plain({"free_flight": 0, "mis": 0, "apply_shading_type": 0, "bilateral": 0, "stratify": 0})
 
     # end to end through the C ABI with host buffers
     vd = scene.volume_desc()
@@ -460,8 +462,8 @@ def run_ours(args, wl, rank, world, local_rank):
     conv = None
     if world == 1 and not args.no_rmse and wl == "c2":
         conv = convergence(lib, runtime, torch, ["c2"], {
-            "fast": {"free_flight": 1, "majorant_brick": r.tracer_desc.settings.majorant_brick},
-            "plain": {"free_flight": 0}})
+            "fast": {"free_flight": 1, "stratify": 1, "majorant_brick": r.tracer_desc.settings.majorant_brick},
+            "plain": {"free_flight": 0, "stratify": 0}})
     peaks, peak_kind = measured_peaks()
     nthreads = os.cpu_count() or 1
     # work per sample of the measured configuration (oracle, whole field of view at 128^2)
@@ -611,6 +613,7 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
         saved = C.er_tracer_desc.from_buffer_copy(r.tracer_desc)
         r.tracer_desc.camera = cam
         r.tracer_desc.settings.free_flight = 0
+        r.tracer_desc.settings.stratify = 0
         r.rebind_tracer()
         C.check(lib.er_reset_accumulation(r.tracer_id))
         r.render_estimate()
@@ -625,7 +628,7 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
     conv = None
     if world == 1 and not args.no_rmse and wl == "c3":
         conv = convergence(lib, runtime, torch, ["c3v0", "c3v1", "c3v2"],
-                           {"fast": {"free_flight": 1}, "plain": {"free_flight": 0}})
+                           {"fast": {"free_flight": 1, "stratify": 1}, "plain": {"free_flight": 0, "stratify": 0}})
 
     # end to end with host buffers: volumes bound from host memory, one batch
     # launch, every view's sums read back into pinned host memory

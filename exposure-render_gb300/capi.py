@@ -176,6 +176,7 @@ class er_render_settings(Structure):
         ("tune_primary", c_int32),
         ("tune_shadow", c_int32),
         ("tune_shade", c_int32),
+        ("stratify", c_int32),
         ("tune_stages", c_int32),
     ]
 

@@ -126,6 +126,7 @@ EXPOSURE_RENDER_DLL void BindTracer(const ErTracer& T, const bool& Bind)
     d.settings.bilateral_sigma_r = r.Extensions.BilateralSigmaR;
     d.settings.seed = r.Extensions.Seed;
     d.settings.majorant_brick = r.Extensions.MajorantBrick;
+    d.settings.stratify = r.Extensions.Stratify ? 1 : 0;
     d.volume_id = T.VolumeID;
     d.light_count = T.LightIDs.Count;
     d.object_count = T.ObjectIDs.Count;

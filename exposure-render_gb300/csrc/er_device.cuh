@@ -128,6 +128,7 @@ struct Params {
     int mis;
     float volume_ior;
     uint32_t seed;
+    int stratify;            /* multi-sample renders: light samples from er_stratified_light */
     /* lights (tracer's LightIDs resolved to light records) */
     int light_count;
     const Light* lights;     /* light_count entries, in LightIDs order; NULL entries are skipped */

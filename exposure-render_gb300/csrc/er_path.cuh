@@ -1217,6 +1217,18 @@ struct Metro {               /* MetroSample::LargeStep - Source/sample.h:258-262
         film_uv = r.get2();
         lens_uv = r.get2();
     }
+    /* settings.stratify: the light sample of sample `index` of a pixel from
+       the per-pixel shifted lattice (after large_step, whose draws keep the
+       random stream unchanged) */
+    ER_D void stratify_light(const Params& P, uint32_t view, uint32_t pixel, uint32_t index)
+    {
+        if (!P.stratify) return;
+        float u, v, pick;
+        er_stratified_light(P.seed, view, pixel, index, &u, &v, &pick);
+        light_uvw.x = u;
+        light_uvw.y = v;
+        light_num = pick;
+    }
 };
 
 /* mixture pdf of the full-MIS BSDF sampler (Lambertian and Blinn lobes with
@@ -1389,12 +1401,15 @@ ER_D Ray sample_camera(const Params& P, int u, int v, v2 film_uv, v2 lens_uv)
     return R;
 }
 
-/* SingleScattering - Source/singlescattering.h:76-102 */
-ER_D float4 single_scattering(const Params& P, int x, int y, Rng& rng)
+/* SingleScattering - Source/singlescattering.h:76-102.  `sample` >= 0 marks
+   sample `sample` of view `view` of a multi-sample render (stratified light
+   samples when enabled); -1 a frame of the reference's pipeline. */
+ER_D float4 single_scattering(const Params& P, int x, int y, Rng& rng, uint32_t view = 0, int64_t sample = -1)
 {
     c3 Lv = C3(0, 0, 0);
     Metro ms;
     ms.large_step(rng);
+    if (sample >= 0) ms.stratify_light(P, view, (uint32_t)y * (uint32_t)P.film[0] + (uint32_t)x, (uint32_t)sample);
     const Ray R = sample_camera(P, x, y, ms.film_uv, ms.lens_uv);
     Event se0, se1, se2, SE;
     se0.type = 0; se0.valid = false; se0.T = 0.0f; se0.Le = C3(0, 0, 0);

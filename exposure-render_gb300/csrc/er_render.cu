@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(128) k_trace_sum(const Params P, int spp, uint
     for (int k = 0; k < spp; k++) {
         Rng rng;
         er_seed_lanes(P.seed, view, pix, first + (uint32_t)k, &rng.s0, &rng.s1);
-        const float4 o = single_scattering(P, x, y, rng);
+        const float4 o = single_scattering(P, x, y, rng, view, (int64_t)(first + (uint32_t)k));
         a0 += o.x; a1 += o.y; a2 += o.z; a3 += o.w;
     }
     float4 r = make_float4(a0, a1, a2, a3);

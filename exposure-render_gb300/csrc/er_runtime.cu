@@ -484,6 +484,7 @@ er_status build(TracerItem& t)
     P.mis = s.mis;
     P.volume_ior = s.volume_ior > 0.0f ? s.volume_ior : 15.0f;
     P.seed = s.seed;
+    P.stratify = s.stratify ? 1 : 0;
     P.gm_inv_max = (v.gm_max > 0.0f) ? 1.0f / v.gm_max : 0.0f;
 
     /* transfer functions */

@@ -119,6 +119,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
             const int x = pix % P.film[0], y = pix / P.film[0];
             er_seed_lanes(P.seed, V.view_id, (uint32_t)pix, V.first + (uint32_t)s, &rng.s0, &rng.s1);
             ms.large_step(rng);
+            ms.stratify_light(P, V.view_id, (uint32_t)pix, V.first + (uint32_t)s);
             const Ray R = sample_camera(P, x, y, ms.film_uv, ms.lens_uv);
             Event se0, se1;
             se0.type = 0; se0.valid = false; se0.T = 0.0f; se0.Le = C3(0, 0, 0);
@@ -294,9 +295,11 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary_pt(const WfView* __res
             const uint32_t local = i - sg.offset;
             const uint32_t npix = (uint32_t)(P.film[0] * P.film[1]);
             Rng r0;
-            er_seed_lanes(P.seed, V.view_id, local % npix, V.first + (uint32_t)(sg.s0 + (int)(local / npix)), &r0.s0, &r0.s1);
+            const uint32_t sidx = V.first + (uint32_t)(sg.s0 + (int)(local / npix));
+            er_seed_lanes(P.seed, V.view_id, local % npix, sidx, &r0.s0, &r0.s1);
             Metro ms;
             ms.large_step(r0);
+            ms.stratify_light(P, V.view_id, local % npix, sidx);
             const bool obj = OBJ && SE.type == 2;
             float4* e = events + (size_t)slot * 5;
             e[0] = make_float4(u2f(i), u2f(rng.s0), u2f(rng.s1), ms.light_num);

@@ -325,7 +325,8 @@ C3_VOLUMES = ((96, 96, 96), (256, 256, 256), (256, 384, 384))   # (z, y, x)
 
 def c3_scenes(volumes=C3_VOLUMES, seed=30) -> list:
     """One C1-style scene (4-node transfer function, one area light) per blob
-    volume, delta-tracked free flight and full MIS (the unbiased estimator);
+    volume, delta-tracked free flight, full MIS and stratified light samples
+    (the unbiased estimator);
     each scene's tracer is the template of the views that look at its
     volume."""
     out = []
@@ -335,6 +336,7 @@ def c3_scenes(volumes=C3_VOLUMES, seed=30) -> list:
         t = c1_tracer((C3_FILMS[0], C3_FILMS[0]))
         t.settings.free_flight = C.FREE_FLIGHT_DELTA
         t.settings.mis = C.MIS_FULL
+        t.settings.stratify = 1
         out.append(Scene(f"c3v{k}", vol, tracer=t, lights=lights, textures=textures, spp=32))
     return out
 
@@ -412,6 +414,7 @@ def scene_c5(volume=None, film=(2048, 2048), spp=64) -> Scene:
     lights, textures = c2_lights()
     t = c2_tracer(film)
     t.settings.free_flight = C.FREE_FLIGHT_DELTA
+    t.settings.stratify = 1
     t.settings.bilateral = 0
     t.settings.seed = 5
     return Scene("c5", vol, tracer=t, lights=lights, textures=textures, spp=spp)

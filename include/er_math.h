@@ -340,6 +340,28 @@ ER_MATH_FN void er_seed_lanes(uint32_t seed, uint32_t view, uint32_t pixel, uint
     *lane1 = b;
 }
 
+/* Stratified light samples (er_render_settings.stratify): for sample
+   `sample` of `pixel` in `view`, the point on the light (u, v) comes from the
+   R2 sequence (generators 2^32/g and 2^32/g^2, g the plastic number) and the
+   light choice from the golden-ratio sequence, each shifted per pixel by a
+   hash of (seed, view, pixel) (a Cranley-Patterson rotation of a rank-1
+   lattice).  Successive samples of a pixel cover the light evenly; each
+   sample alone is uniform, so estimates stay unbiased.  Integer arithmetic,
+   23-bit mantissas: identical on every host and device. */
+ER_MATH_FN void er_stratified_light(uint32_t seed, uint32_t view, uint32_t pixel, uint32_t sample, float* u, float* v,
+                                    float* pick)
+{
+    uint32_t h = er_hash32(seed * 0x9e3779b9u + 0x1b873593u);
+    h = er_hash32(h ^ (view * 0x85ebca6bu));
+    h = er_hash32(h + pixel);
+    const uint32_t a = er_hash32(h ^ 0x3c6ef372u) + sample * 3242174889u;
+    const uint32_t b = er_hash32(h ^ 0xa54ff53au) + sample * 2447445413u;
+    const uint32_t c = er_hash32(h ^ 0x510e527fu) + sample * 2654435769u;
+    *u = ((float)(a >> 9) + 0.5f) * (1.0f / 8388608.0f);
+    *v = ((float)(b >> 9) + 0.5f) * (1.0f / 8388608.0f);
+    *pick = ((float)(c >> 9) + 0.5f) * (1.0f / 8388608.0f);
+}
+
 #ifdef __cplusplus
 }
 #endif

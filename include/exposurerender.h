@@ -329,7 +329,8 @@ public:
     {
     public:
         ExtensionSettings() : ApplyShadingType(false), FreeFlight(0), Mis(0), VolumeIor(15.0f), FrameFilter(true), Bilateral(false),
-                              BilateralRadius(2), BilateralSigmaD(1.5f), BilateralSigmaR(20.0f), Seed(1u), MajorantBrick(8) {}
+                              BilateralRadius(2), BilateralSigmaD(1.5f), BilateralSigmaR(20.0f), Seed(1u), MajorantBrick(8),
+                              Stratify(false) {}
         bool ApplyShadingType;   /* Shading.Type selects BRDF / phase / hybrid (Source/scatterevent.h:155-212) */
         int FreeFlight;          /* 0 fixed-step march (reference), 1 delta tracking */
         int Mis;                 /* 0 light sampling (reference), 1 light + BSDF sampling */
@@ -341,6 +342,7 @@ public:
         float BilateralSigmaR;
         unsigned int Seed;
         int MajorantBrick;
+        bool Stratify;           /* multi-sample renders: light samples from a per-pixel shifted lattice */
     };
 
     TraversalSettings Traversal;

@@ -1703,11 +1703,24 @@ static void sample_ray(or_scene* s, ray_t R, rng_t* rng, scatter_event* nearest)
 }
 
 /* SingleScattering - Source/singlescattering.h:76-102 */
-static void single_scattering(or_scene* s, int x, int y, rng_t* rng, float out[4])
+/* `sample` (view, pixel, sample index) identifies a sample of a
+   multi-sample render, NULL for a frame; with settings.stratify the light
+   sample's (u, v) and light choice come from er_stratified_light (the
+   random stream still draws them first, so every later draw is unchanged) */
+typedef struct { uint32_t view, pixel, index; } sample_id;
+
+static void single_scattering(or_scene* s, int x, int y, rng_t* rng, float out[4], const sample_id* sample)
 {
     col3 Lv = C3(0, 0, 0);
     metro_sample ms;
     metro_large_step(&ms, rng);
+    if (sample && s->st.stratify) {
+        desc_f32 u, v, pick;
+        er_stratified_light(s->st.seed, sample->view, sample->pixel, sample->index, &u, &v, &pick);
+        ms.light_uvw.x = u;
+        ms.light_uvw.y = v;
+        ms.light_num = pick;
+    }
     const ray_t R = sample_camera(s, x, y, ms.film_uv, ms.lens_uv);
     scatter_event SE;
     const uint64_t lk = s->lookups;
@@ -1790,7 +1803,7 @@ static void* job_run(void* arg)
                 rng_t rng;
                 rng.s0 = j->lanes[p];
                 rng.s1 = j->lanes[(size_t)W * (size_t)H + p];
-                single_scattering(s, x, r, &rng, &j->out[4 * p]);
+                single_scattering(s, x, r, &rng, &j->out[4 * p], NULL);
                 j->lanes[p] = rng.s0;
                 j->lanes[(size_t)W * (size_t)H + p] = rng.s1;
                 s->samples++;
@@ -1806,7 +1819,8 @@ static void* job_run(void* arg)
                     rng_t rng;
                     er_seed_lanes(s->st.seed, j->view, pix, j->first + (uint32_t)k, &rng.s0, &rng.s1);
                     float o[4];
-                    single_scattering(s, x, y, &rng, o);
+                    const sample_id sid = { j->view, pix, j->first + (uint32_t)k };
+                    single_scattering(s, x, y, &rng, o, &sid);
                     acc[0] += o[0]; acc[1] += o[1]; acc[2] += o[2]; acc[3] += o[3];
                     if (j->out2) {
                         acc2[0] += o[0] * o[0]; acc2[1] += o[1] * o[1]; acc2[2] += o[2] * o[2]; acc2[3] += o[3] * o[3];

@@ -100,3 +100,21 @@ def test_delta_and_march_agree_on_alpha(oracle):
         vals.append(h.render_sum(128, nthreads=8)[..., 3] / 128)
         h.close()
     assert abs(vals[0].mean() - vals[1].mean()) < 0.02
+
+
+def test_stratified_light_samples_lower_rmse(oracle):
+    """settings.stratify (er_stratified_light): the light sample of each of a
+    pixel's samples from a per-pixel shifted lattice.  The estimate stays
+    unbiased and its RMSE against the FP64 reference drops (the first c3
+    view, 32 spp, four independent pixel streams)"""
+    import convergence as CV
+    sc = dict(S.rmse_views(names=["c3v0"]))["c3v0"]
+    ref = CV.load_reference("c3v0")
+    err = {}
+    for strat in (0, 1):
+        sc.tracer.settings.stratify = strat
+        h = OL.SceneHandle(oracle, sc)
+        mse = [CV.rmse((h.render_sum(32, view=v, nthreads=8)[..., :3] / 32).astype(np.float64), ref) ** 2 for v in (11, 12, 13, 14)]
+        h.close()
+        err[strat] = float(np.sqrt(np.mean(mse)))
+    assert 0.0 < err[1] < 0.9 * err[0], err

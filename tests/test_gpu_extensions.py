@@ -152,3 +152,32 @@ def test_persistent_stage_modes_bit_exact(env, oracle, mode):
     finally:
         r.close()
         h.close()
+
+
+@pytest.mark.parametrize("stages", [0, 1, 2], ids=["persistent-shadow", "persistent-both", "per-thread"])
+def test_stratified_light_samples_bit_exact(env, oracle, stages):
+    """settings.stratify on the GPU (wavefront stages in each mode, the
+    one-kernel path) gives the oracle's sums"""
+    torch, lib, rt = env
+    sc = two_light_scene(17)
+    sc.tracer.settings.free_flight = 1
+    sc.tracer.settings.mis = 1
+    sc.tracer.settings.stratify = 1
+    sc.tracer.settings.tune_stages = stages
+    h = OL.SceneHandle(oracle, sc)
+    cpu = h.render_sum(6, view=2, first=7, nthreads=4)
+    h.close()
+    for engine in (2, 1):
+        sc.tracer.settings.engine = engine
+        r = rt.Renderer(sc, lib)
+        try:
+            d = torch.zeros((sc.height, sc.width, 4), dtype=torch.float32, device="cuda")
+            r.trace_sum_device(d.data_ptr(), 6, 2, 7, 0, None)
+            torch.cuda.synchronize()
+            assert np.array_equal(bits(d.cpu().numpy()), bits(cpu)), engine
+        finally:
+            r.close()
+    sc.tracer.settings.stratify = 0
+    h = OL.SceneHandle(oracle, sc)
+    assert not np.array_equal(h.render_sum(6, view=2, first=7, nthreads=4), cpu)
+    h.close()
