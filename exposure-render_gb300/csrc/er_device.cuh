@@ -128,7 +128,7 @@ struct Params {
     int mis;
     float volume_ior;
     uint32_t seed;
-    int stratify;            /* multi-sample renders: light samples from er_stratified_light */
+    int stratify;            /* multi-sample renders: stratified dimensions from er_stratified_sample */
     /* lights (tracer's LightIDs resolved to light records) */
     int light_count;
     const Light* lights;     /* light_count entries, in LightIDs order; NULL entries are skipped */

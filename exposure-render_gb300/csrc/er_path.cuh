@@ -909,7 +909,7 @@ ER_D void dda_skip(const Params& P, Dda& d, int k, float e)
 /* SKIP: compile the empty-space skip (a grid without skip distances reads
    the same either way; the variant without it needs fewer registers) */
 template <bool WITH_NORMAL = true, bool SKIP = true>
-ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE)
+ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE, float u0 = -1.0f)
 {
     Isect Int; Int.invalid();
     intersect_box(R, vload(P.minp), vload(P.half_size), Int, false);
@@ -919,7 +919,8 @@ ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE
     if (!(t0 < t1)) return;
     Dda d;
     dda_init(P, R, t0, t1, d);
-    float tau = -er_logf(rng.get1());
+    const float ud = rng.get1();
+    float tau = -er_logf(u0 >= 0.0f ? u0 : ud);
     int guard = 0;
     while (!d.done) {
         const float e = dda_exit(d);
@@ -968,7 +969,7 @@ struct DeltaTracker {
     bool in_brick, done, hit;
 };
 
-ER_D void delta_begin(const Params& P, const Ray& R, Rng& rng, DeltaTracker& k)
+ER_D void delta_begin(const Params& P, const Ray& R, Rng& rng, DeltaTracker& k, float u0 = -1.0f)
 {
     k.done = true;
     k.hit = false;
@@ -979,7 +980,8 @@ ER_D void delta_begin(const Params& P, const Ray& R, Rng& rng, DeltaTracker& k)
     const float t1 = smin(Int.far_t, R.MaxT);
     if (!(t0 < t1)) return;
     dda_init(P, R, t0, t1, k.d);
-    k.tau = -er_logf(rng.get1());
+    const float ud = rng.get1();
+    k.tau = -er_logf(u0 >= 0.0f ? u0 : ud);
     k.guard = 0;
     k.in_brick = false;
     k.done = false;
@@ -1217,17 +1219,24 @@ struct Metro {               /* MetroSample::LargeStep - Source/sample.h:258-262
         film_uv = r.get2();
         lens_uv = r.get2();
     }
-    /* settings.stratify: the light sample of sample `index` of a pixel from
-       the per-pixel shifted lattice (after large_step, whose draws keep the
-       random stream unchanged) */
-    ER_D void stratify_light(const Params& P, uint32_t view, uint32_t pixel, uint32_t index)
+    float tau_u;             /* the stratified first free-flight draw, or < 0 */
+    /* settings.stratify: the light sample, the BSDF sample and the first
+       free-flight draw of sample `index` of a pixel from the per-pixel
+       shifted lattices of er_stratified_sample (after large_step, whose
+       draws keep the random stream unchanged) */
+    ER_D void stratify(const Params& P, uint32_t view, uint32_t pixel, uint32_t index)
     {
+        tau_u = -1.0f;
         if (!P.stratify) return;
-        float u, v, pick;
-        er_stratified_light(P.seed, view, pixel, index, &u, &v, &pick);
-        light_uvw.x = u;
-        light_uvw.y = v;
-        light_num = pick;
+        float u[7];
+        er_stratified_sample(P.seed, view, pixel, index, u);
+        light_uvw.x = u[0];
+        light_uvw.y = u[1];
+        light_num = u[2];
+        brdf_dir.x = u[3];
+        brdf_dir.y = u[4];
+        brdf_component = u[5];
+        tau_u = u[6];
     }
 };
 
@@ -1409,7 +1418,8 @@ ER_D float4 single_scattering(const Params& P, int x, int y, Rng& rng, uint32_t 
     c3 Lv = C3(0, 0, 0);
     Metro ms;
     ms.large_step(rng);
-    if (sample >= 0) ms.stratify_light(P, view, (uint32_t)y * (uint32_t)P.film[0] + (uint32_t)x, (uint32_t)sample);
+    ms.tau_u = -1.0f;
+    if (sample >= 0) ms.stratify(P, view, (uint32_t)y * (uint32_t)P.film[0] + (uint32_t)x, (uint32_t)sample);
     const Ray R = sample_camera(P, x, y, ms.film_uv, ms.lens_uv);
     Event se0, se1, se2, SE;
     se0.type = 0; se0.valid = false; se0.T = 0.0f; se0.Le = C3(0, 0, 0);
@@ -1418,7 +1428,7 @@ ER_D float4 single_scattering(const Params& P, int x, int y, Rng& rng, uint32_t 
     se2.type = 2; se2.valid = false; se2.T = 0.0f;
     ObjHit hit;
     hit.UV.x = 0.0f; hit.UV.y = 0.0f; hit.id = 0;
-    if (P.free_flight == 1) sample_volume_delta(P, R, rng, se0);
+    if (P.free_flight == 1) sample_volume_delta(P, R, rng, se0, ms.tau_u);
     else sample_volume(P, R, rng, se0);
     intersect_lights(P, R, se1, true);
     if (P.object_count > 0) intersect_objects(P, R, se2, hit);

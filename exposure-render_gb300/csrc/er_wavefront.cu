@@ -119,14 +119,14 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
             const int x = pix % P.film[0], y = pix / P.film[0];
             er_seed_lanes(P.seed, V.view_id, (uint32_t)pix, V.first + (uint32_t)s, &rng.s0, &rng.s1);
             ms.large_step(rng);
-            ms.stratify_light(P, V.view_id, (uint32_t)pix, V.first + (uint32_t)s);
+            ms.stratify(P, V.view_id, (uint32_t)pix, V.first + (uint32_t)s);
             const Ray R = sample_camera(P, x, y, ms.film_uv, ms.lens_uv);
             Event se0, se1;
             se0.type = 0; se0.valid = false; se0.T = 0.0f; se0.Le = C3(0, 0, 0);
             se0.P = V3(0, 0, 0); se0.N = V3(0, 0, 0); se0.Wo = V3(0, 0, 0);
             se1 = se0; se1.type = 1;
             /* the event normal (no RNG) is computed by the shade stage */
-            if (P.free_flight == 1) sample_volume_delta<false, SKIP>(P, R, rng, se0);
+            if (P.free_flight == 1) sample_volume_delta<false, SKIP>(P, R, rng, se0, ms.tau_u);
             else sample_volume<false>(P, R, rng, se0);
             intersect_lights(P, R, se1, true);
             SE = se0; SE.valid = false; SE.type = 0;
@@ -240,8 +240,9 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary_pt(const WfView* __res
             er_seed_lanes(P.seed, V.view_id, (uint32_t)pix, V.first + (uint32_t)s, &rng.s0, &rng.s1);
             Metro ms;
             ms.large_step(rng);
+            ms.stratify(P, V.view_id, (uint32_t)pix, V.first + (uint32_t)s);
             R = sample_camera(P, pix % P.film[0], pix / P.film[0], ms.film_uv, ms.lens_uv);
-            delta_begin(P, R, rng, k);
+            delta_begin(P, R, rng, k, ms.tau_u);
             tracking = true;
         }
         if (!__any_sync(0xffffffffu, tracking)) break;
@@ -299,7 +300,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary_pt(const WfView* __res
             er_seed_lanes(P.seed, V.view_id, local % npix, sidx, &r0.s0, &r0.s1);
             Metro ms;
             ms.large_step(r0);
-            ms.stratify_light(P, V.view_id, local % npix, sidx);
+            ms.stratify(P, V.view_id, local % npix, sidx);
             const bool obj = OBJ && SE.type == 2;
             float4* e = events + (size_t)slot * 5;
             e[0] = make_float4(u2f(i), u2f(rng.s0), u2f(rng.s1), ms.light_num);

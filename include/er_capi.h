@@ -221,9 +221,10 @@ typedef struct er_render_settings {
     int32_t tune_shade;           /* wavefront: resident 128-thread blocks per SM of the shade stage
                                      (2, 3, 4 or 6; 0 or other values: 2) */
     int32_t stratify;             /* 1: multi-sample renders (er_render_spp, er_trace_sum_device, batches) take
-                                     each sample's point on the light and light choice from a per-pixel
-                                     shifted rank-1 lattice over the sample index (er_stratified_light)
-                                     instead of the random stream; 0: the reference's draws */
+                                     each sample's point on the light, light choice, BSDF sample and first
+                                     delta-tracking draw from per-pixel shifted rank-1 lattices over the
+                                     sample index (er_stratified_sample in er_math.h) instead of the random
+                                     stream; 0: the reference's draws */
     int32_t tune_stages;          /* delta tracking: bits 0-1 which wavefront tracking stages run persistent
                                      lanes (ER_PERSISTENT_*; 0: the shadow stage only); bits 2 and 3
                                      (ER_TUNE_NO_SKIP_PRIMARY, ER_TUNE_NO_SKIP_SHADOW) turn empty-space

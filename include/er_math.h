@@ -340,26 +340,34 @@ ER_MATH_FN void er_seed_lanes(uint32_t seed, uint32_t view, uint32_t pixel, uint
     *lane1 = b;
 }
 
-/* Stratified light samples (er_render_settings.stratify): for sample
-   `sample` of `pixel` in `view`, the point on the light (u, v) comes from the
-   R2 sequence (generators 2^32/g and 2^32/g^2, g the plastic number) and the
-   light choice from the golden-ratio sequence, each shifted per pixel by a
-   hash of (seed, view, pixel) (a Cranley-Patterson rotation of a rank-1
-   lattice).  Successive samples of a pixel cover the light evenly; each
-   sample alone is uniform, so estimates stay unbiased.  Integer arithmetic,
-   23-bit mantissas: identical on every host and device. */
-ER_MATH_FN void er_stratified_light(uint32_t seed, uint32_t view, uint32_t pixel, uint32_t sample, float* u, float* v,
-                                    float* pick)
+/* Stratified sample dimensions (er_render_settings.stratify).  For sample
+   `sample` of `pixel` in `view`, each stratified dimension comes from a
+   rank-1 lattice over the sample index shifted per pixel and dimension by a
+   hash of (seed, view, pixel) (a Cranley-Patterson rotation): the R2
+   sequence (generators 2^32/g and 2^32/g^2, g the plastic number) for the
+   2D dimensions, the golden-ratio sequence for the 1D ones.  Successive
+   samples of a pixel cover each dimension evenly; each sample alone is
+   uniform, so estimates stay unbiased.  Integer arithmetic, 23-bit
+   mantissas in (0, 1): identical on every host and device.
+     out[0], out[1]: point on the light (MetroSample light u, v)
+     out[2]        : light choice
+     out[3], out[4]: BSDF direction
+     out[5]        : BSDF component
+     out[6]        : the first free-flight draw of delta tracking */
+ER_MATH_FN float er_lattice_unit(uint32_t x) { return ((float)(x >> 9) + 0.5f) * (1.0f / 8388608.0f); }
+
+ER_MATH_FN void er_stratified_sample(uint32_t seed, uint32_t view, uint32_t pixel, uint32_t sample, float out[7])
 {
     uint32_t h = er_hash32(seed * 0x9e3779b9u + 0x1b873593u);
     h = er_hash32(h ^ (view * 0x85ebca6bu));
     h = er_hash32(h + pixel);
-    const uint32_t a = er_hash32(h ^ 0x3c6ef372u) + sample * 3242174889u;
-    const uint32_t b = er_hash32(h ^ 0xa54ff53au) + sample * 2447445413u;
-    const uint32_t c = er_hash32(h ^ 0x510e527fu) + sample * 2654435769u;
-    *u = ((float)(a >> 9) + 0.5f) * (1.0f / 8388608.0f);
-    *v = ((float)(b >> 9) + 0.5f) * (1.0f / 8388608.0f);
-    *pick = ((float)(c >> 9) + 0.5f) * (1.0f / 8388608.0f);
+    out[0] = er_lattice_unit(er_hash32(h ^ 0x3c6ef372u) + sample * 3242174889u);
+    out[1] = er_lattice_unit(er_hash32(h ^ 0xa54ff53au) + sample * 2447445413u);
+    out[2] = er_lattice_unit(er_hash32(h ^ 0x510e527fu) + sample * 2654435769u);
+    out[3] = er_lattice_unit(er_hash32(h ^ 0x9b05688cu) + sample * 3242174889u);
+    out[4] = er_lattice_unit(er_hash32(h ^ 0x1f83d9abu) + sample * 2447445413u);
+    out[5] = er_lattice_unit(er_hash32(h ^ 0x5be0cd19u) + sample * 2654435769u);
+    out[6] = er_lattice_unit(er_hash32(h ^ 0xcbbb9d5du) + sample * 2654435769u);
 }
 
 #ifdef __cplusplus

@@ -342,7 +342,7 @@ public:
         float BilateralSigmaR;
         unsigned int Seed;
         int MajorantBrick;
-        bool Stratify;           /* multi-sample renders: light samples from a per-pixel shifted lattice */
+        bool Stratify;           /* multi-sample renders: light, BSDF and first free-flight samples from per-pixel shifted lattices */
     };
 
     TraversalSettings Traversal;

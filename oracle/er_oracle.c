@@ -151,6 +151,8 @@ struct or_scene {
     int n_bitmaps;
     int* bitmap_res;            /* 2 per bitmap */
     uint8_t** bitmap_pixels;
+    /* the stratified first free-flight draw of the current sample, or < 0 */
+    float tau_u;
     /* statistics */
     uint64_t lookups;
     uint64_t stat[OR_NSTATS];   /* work counters of the last render (render_stats) */
@@ -252,6 +254,7 @@ or_scene* ER_OR(scene_create)(const er_tracer_desc* t, const er_volume_desc* vol
     s->emission = t->emission;
     s->light_count = t->light_count;
     s->object_count = t->object_count > 0 ? t->object_count : 0;
+    s->tau_u = -1.0f;
     for (int i = 0; i < ER_MAX_INDICES; i++) s->light_idx[i] = t->light_ids[i];
 
     s->n_lights = n_lights;
@@ -1273,7 +1276,8 @@ static void sample_volume_delta(or_scene* s, ray_t R, rng_t* rng, scatter_event*
     if (!(t0 < t1)) return;
     dda_t d;
     dda_init(s, &R, t0, t1, &d);
-    float tau = -er_logf(rng_get1(rng));
+    const float u0 = rng_get1(rng);
+    float tau = -er_logf(s->tau_u >= 0.0f ? (float)s->tau_u : u0);
     int guard = 0;
     while (!d.done) {
         const float e = dda_exit(&d);
@@ -1705,7 +1709,8 @@ static void sample_ray(or_scene* s, ray_t R, rng_t* rng, scatter_event* nearest)
 /* SingleScattering - Source/singlescattering.h:76-102 */
 /* `sample` (view, pixel, sample index) identifies a sample of a
    multi-sample render, NULL for a frame; with settings.stratify the light
-   sample's (u, v) and light choice come from er_stratified_light (the
+   sample's (u, v), the light choice, the BSDF sample and the first
+   free-flight draw of delta tracking come from er_stratified_sample (the
    random stream still draws them first, so every later draw is unchanged) */
 typedef struct { uint32_t view, pixel, index; } sample_id;
 
@@ -1714,12 +1719,17 @@ static void single_scattering(or_scene* s, int x, int y, rng_t* rng, float out[4
     col3 Lv = C3(0, 0, 0);
     metro_sample ms;
     metro_large_step(&ms, rng);
+    s->tau_u = -1.0f;
     if (sample && s->st.stratify) {
-        desc_f32 u, v, pick;
-        er_stratified_light(s->st.seed, sample->view, sample->pixel, sample->index, &u, &v, &pick);
-        ms.light_uvw.x = u;
-        ms.light_uvw.y = v;
-        ms.light_num = pick;
+        desc_f32 u[7];
+        er_stratified_sample(s->st.seed, sample->view, sample->pixel, sample->index, u);
+        ms.light_uvw.x = u[0];
+        ms.light_uvw.y = u[1];
+        ms.light_num = u[2];
+        ms.brdf_dir.x = u[3];
+        ms.brdf_dir.y = u[4];
+        ms.brdf_component = u[5];
+        s->tau_u = u[6];
     }
     const ray_t R = sample_camera(s, x, y, ms.film_uv, ms.lens_uv);
     scatter_event SE;

@@ -103,8 +103,9 @@ def test_delta_and_march_agree_on_alpha(oracle):
 
 
 def test_stratified_light_samples_lower_rmse(oracle):
-    """settings.stratify (er_stratified_light): the light sample of each of a
-    pixel's samples from a per-pixel shifted lattice.  The estimate stays
+    """settings.stratify (er_stratified_sample): the light sample, BSDF sample
+    and first free-flight draw of each of a pixel's samples from per-pixel
+    shifted lattices.  The estimate stays
     unbiased and its RMSE against the FP64 reference drops (the first c3
     view, 32 spp, four independent pixel streams)"""
     import convergence as CV
