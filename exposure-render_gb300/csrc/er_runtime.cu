@@ -1608,6 +1608,20 @@ ER_API er_status er_batch_autotune(int32_t batch_id, void* stream, int32_t* tune
     }
     rs = er_batch_set_stages(batch_id, best);
     if (rs != ER_OK) return done(rs);
+    /* last the occupancy variants of the tracking stages under that mode */
+    const int pairs[][2] = {{4, 4}, {3, 3}, {3, 4}, {4, 3}, {2, 3}, {2, 2}};
+    int best_p = b->tune_primary, best_s = b->tune_shadow;
+    for (const auto& pr : pairs) {
+        if (pr[0] == best_p && pr[1] == best_s) continue;
+        rs = er_batch_set_tuning(batch_id, pr[0], pr[1]);
+        if (rs != ER_OK) return done(rs);
+        float r = 0.0f;
+        rs = time_batch(&r);
+        if (rs != ER_OK) return done(rs);
+        if (r > best_rate) { best_rate = r; best_p = pr[0]; best_s = pr[1]; }
+    }
+    rs = er_batch_set_tuning(batch_id, best_p, best_s);
+    if (rs != ER_OK) return done(rs);
     if (tune_stages) *tune_stages = best;
     if (msamples_per_s) *msamples_per_s = best_rate;
     return done(ER_OK);

@@ -437,7 +437,8 @@ ER_API er_status er_batch_set_stages(int32_t batch_id, int32_t tune_stages);
    times one launch of the whole batch per candidate, first each
    delta-tracking tracer's majorant brick in {1, 2, 4, 8} in turn (written
    into that tracer's settings, as er_autotune_tracer does), then eight
-   tune_stages candidates, keeping the fastest of each.  The views' sums are
+   tune_stages candidates, then six occupancy pairs of the tracking stages
+   (as er_batch_set_tuning), keeping the fastest of each.  The views' sums are
    rendered into (accumulating views accumulate), so reset them afterwards.
    Synchronous. */
 ER_API er_status er_batch_autotune(int32_t batch_id, void* stream, int32_t* tune_stages, float* msamples_per_s);
