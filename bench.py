@@ -670,8 +670,10 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
                    ("c3-batched-%d-views-3-blob-volumes" % len(views)), "views": len(views),
                    "samples_per_step": samples_per_step, "films": sorted({c.film_size[0] for _, c, _ in views}),
                    "spp_range": [min(s for _, _, s in views), max_spp], **describe_shading(scenes[0]),
+                   "free_flight": "delta+ratio tracking, majorant bricks per volume below",
                    "windows": info["windows"], "segments": info["segments"], "queue_bytes": info["queue_bytes"],
                    "autotune": tuned, "batch_autotune": batch_tune,
+                   "majorant_bricks": [r.tracer_desc.settings.majorant_brick for r in rs],
                    "l2": "volumes %d MiB in total; every step renders fresh samples" % (vol_bytes >> 20),
                    "parallelism": "replicas" if world > 1 else "single"},
         "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(vol_bytes),
