@@ -430,11 +430,14 @@ def run_ours(args, wl, rank, world, local_rank):
     plain = timed_plain({"free_flight": 0, "stratify": 0})
     ref_order = timed_plain({"free_flight": 0, "mis": 0, "apply_shading_type": 0, "bilateral": 0, "stratify": 0})
 
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers: the volume and the RGBA8
+    # estimate live in pinned host memory (BindVoxels' source, GetEstimate's target)
+    pinned_vol = torch.from_numpy(np.ascontiguousarray(scene.volume).view(np.int16)).pin_memory()
     vd = scene.volume_desc()
+    vd.voxels = ctypes.cast(ctypes.c_void_p(pinned_vol.data_ptr()), ctypes.POINTER(ctypes.c_uint16))
     vol_bytes = scene.volume.nbytes
     tr_bytes = ctypes.sizeof(r.tracer_desc)
-    out = np.empty((height, width, 4), dtype=np.uint8)
+    out = torch.empty((height, width, 4), dtype=torch.uint8, pin_memory=True)
     e2e_steps = max(1, min(args.steps, 3))
 
     def e2e_step():
@@ -444,7 +447,7 @@ def run_ours(args, wl, rank, world, local_rank):
         C.check(lib.er_bind_tracer(ctypes.byref(r.tracer_desc), ctypes.byref(tid)))
         C.check(lib.er_reset_accumulation(r.tracer_id))
         C.check(lib.er_render_spp(r.tracer_id, spp))
-        C.check(lib.er_get_estimate(r.tracer_id, out.ctypes.data))
+        C.check(lib.er_get_estimate(r.tracer_id, out.data_ptr()))
 
     e2e_step()
     torch.cuda.synchronize()
@@ -633,7 +636,10 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
     # end to end with host buffers: volumes bound from host memory, one batch
     # launch, every view's sums read back into pinned host memory
     host_sums = [torch.empty(d.shape, dtype=torch.float32, pin_memory=True) for d in sums]
+    pinned_vols = [torch.from_numpy(np.ascontiguousarray(sc.volume).view(np.int16)).pin_memory() for sc in scenes]
     vds = [sc.volume_desc() for sc in scenes]
+    for vd, pv in zip(vds, pinned_vols):
+        vd.voxels = ctypes.cast(ctypes.c_void_p(pv.data_ptr()), ctypes.POINTER(ctypes.c_uint16))
 
     def e2e_step():
         for r, vd in zip(rs, vds):
