@@ -761,6 +761,48 @@ ER_D void intersect_lights(const Params& P, const Ray& R, Event& RS, bool respec
     intersect_lights_slot(P, R, RS, respect_visibility, slot);
 }
 
+/* intersect_lights_slot without the emission: the nearest hit's (P, N, T,
+   Wo) in RS, its LightIDs index in `slot` and what its emission needs in
+   `lh`; light_emission gives the Le intersect_light would have, for the hits
+   that are used (the environment sphere's texture is not evaluated for the
+   rays whose volume event or chosen light wins).  Same operations, same
+   nearest hit. */
+struct LightHit {
+    v2 UV;
+    bool front;
+};
+
+ER_D void intersect_lights_geom(const Params& P, const Ray& R, Event& RS, bool respect_visibility, int& slot, LightHit& lh)
+{
+    float T = FLT_MAX;
+    for (int i = 0; i < P.light_count; i++) {
+        if (!P.light_valid[i]) continue;
+        const Light& L = P.lights[i];
+        if (respect_visibility && !L.visible) continue;
+        const Ray Rt = xform_ray(L.inv_tm, R);
+        Isect Int; Int.invalid();
+        intersect_shape(L, Rt, Int);
+        if (!Int.valid) continue;
+        Event local;
+        local.type = 1;
+        local.valid = true;
+        local.P = xform_point(L.tm, Int.P);
+        local.N = xform_vector(L.tm, Int.N);
+        local.T = vlen(vsub(local.P, R.O));
+        local.Wo = vneg(R.D);
+        local.Le = C3(0, 0, 0);
+        if (local.T < T) { RS = local; T = local.T; slot = i; lh.UV = Int.UV; lh.front = Int.front; }
+    }
+}
+
+/* the emission of a light hit (Source/lights.h:78-84) */
+ER_D c3 light_emission(const Params& P, const Light& L, const LightHit& lh)
+{
+    c3 Le = lh.front ? cscale(light_texture(P, L, lh.UV), L.multiplier) : C3(0, 0, 0);
+    if (L.unit == 1) Le = cdivs(Le, L.area);
+    return Le;
+}
+
 /* IntersectsLight - Source/lights.h:115-131 */
 ER_D bool intersects_light(const Params& P, const Ray& R)
 {
@@ -1339,8 +1381,10 @@ ER_D c3 estimate_direct_light(const Params& P, const Light& L, int slot, const M
     SE2.type = 1; SE2.valid = false; SE2.T = 0.0f; SE2.Le = C3(0, 0, 0);
     SE2.P = V3(0, 0, 0); SE2.N = V3(0, 0, 0); SE2.Wo = V3(0, 0, 0);
     int hit = -1;
-    intersect_lights_slot(P, R2, SE2, false, hit);
+    LightHit lh;
+    intersect_lights_geom(P, R2, SE2, false, hit, lh);
     if (!SE2.valid || P.light_ids[hit] != P.light_ids[slot]) return Ld;
+    SE2.Le = light_emission(P, P.lights[hit], lh);
     if (cblack(SE2.Le)) return Ld;
     const float Tr = visibility(P, SE.P, SE2.P, rng);
     if (Tr > 0.0f) {
@@ -1430,13 +1474,16 @@ ER_D float4 single_scattering(const Params& P, int x, int y, Rng& rng, uint32_t 
     hit.UV.x = 0.0f; hit.UV.y = 0.0f; hit.id = 0;
     if (P.free_flight == 1) sample_volume_delta(P, R, rng, se0, ms.tau_u);
     else sample_volume(P, R, rng, se0);
-    intersect_lights(P, R, se1, true);
+    int lslot = -1;
+    LightHit lh;
+    intersect_lights_geom(P, R, se1, true, lslot, lh);
     if (P.object_count > 0) intersect_objects(P, R, se2, hit);
     SE = se0; SE.valid = false; SE.type = 0;
     float T = FLT_MAX;
     if (se0.valid && se0.T < T) { SE = se0; T = se0.T; }
     if (se1.valid && se1.T < T) { SE = se1; T = se1.T; }
     if (se2.valid && se2.T < T) { SE = se2; T = se2.T; }
+    if (SE.valid && SE.type == 1) SE.Le = light_emission(P, P.lights[lslot], lh);
     if (SE.valid && SE.type == 0) Lv = cadd(Lv, uniform_sample_one_light(P, SE, rng, ms, hit));
     if (SE.valid && SE.type == 1) Lv = cadd(Lv, SE.Le);
     if (SE.valid && SE.type == 2) Lv = cadd(Lv, uniform_sample_one_light(P, SE, rng, ms, hit));

@@ -128,7 +128,9 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
             /* the event normal (no RNG) is computed by the shade stage */
             if (P.free_flight == 1) sample_volume_delta<false, SKIP>(P, R, rng, se0, ms.tau_u);
             else sample_volume<false>(P, R, rng, se0);
-            intersect_lights(P, R, se1, true);
+            int lslot = -1;
+            LightHit lh;
+            intersect_lights_geom(P, R, se1, true, lslot, lh);
             SE = se0; SE.valid = false; SE.type = 0;
             float T = FLT_MAX;
             if (se0.valid && se0.T < T) { SE = se0; T = se0.T; }
@@ -139,6 +141,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
                 intersect_objects(P, R, se2, hit);
                 if (se2.valid && se2.T < T) { SE = se2; T = se2.T; }
             }
+            if (SE.valid && SE.type == 1) SE.Le = light_emission(P, P.lights[lslot], lh);
             if (!SE.valid) {
                 results[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             } else if (SE.type == 1) {
@@ -269,7 +272,9 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary_pt(const WfView* __res
             SE.Wo = vneg(R.D);
         }
         const Event se0 = SE;
-        intersect_lights(P, R, se1, true);
+        int lslot = -1;
+        LightHit lh;
+        intersect_lights_geom(P, R, se1, true, lslot, lh);
         SE.valid = false; SE.type = 0;
         float T = FLT_MAX;
         if (se0.valid && se0.T < T) { SE = se0; T = se0.T; }
@@ -281,6 +286,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary_pt(const WfView* __res
             intersect_objects(P, R, se2, hit);
             if (se2.valid && se2.T < T) { SE = se2; T = se2.T; }
         }
+        if (SE.valid && SE.type == 1) SE.Le = light_emission(P, P.lights[lslot], lh);
         bool push = false;
         if (!SE.valid) {
             results[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -436,7 +442,9 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict
                         SE2.type = 1; SE2.valid = false; SE2.T = 0.0f; SE2.Le = C3(0, 0, 0);
                         SE2.P = V3(0, 0, 0); SE2.N = V3(0, 0, 0); SE2.Wo = V3(0, 0, 0);
                         int hit = -1;
-                        intersect_lights_slot(P, R2, SE2, false, hit);
+                        LightHit lh;
+                        intersect_lights_geom(P, R2, SE2, false, hit, lh);
+                        if (SE2.valid && P.light_ids[hit] == P.light_ids[idx]) SE2.Le = light_emission(P, P.lights[hit], lh);
                         if (SE2.valid && P.light_ids[hit] == P.light_ids[idx] && !cblack(SE2.Le)) {
                             const float LightPdf = vlen2(vsub(SE.P, SE2.P)) / (vabsdot(SE2.N, vneg(Wb)) * L.area);
                             const float w = power_heuristic(pb, LightPdf);
