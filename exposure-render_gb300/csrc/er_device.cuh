@@ -106,6 +106,9 @@ struct Params {
     float min_step;
     const float* sigma;      /* DensityScale * Opacity(I), I in [0, sigma_n) */
     int sigma_n;
+    const float4* shade_tab; /* per integer intensity I in [0, sigma_n), 3 records: (Diffuse1D(I), glossiness
+                                exponent 1e6 * Glossiness1D(I)^7), (Specular1D(I), Opacity1D(I)),
+                                (Emission1D(I), 0) */
     /* delta tracking: majorant per brick of `brick`^3 voxels */
     int free_flight;
     int brick;

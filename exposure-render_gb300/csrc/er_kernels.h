@@ -26,6 +26,8 @@ cudaError_t er_launch_trace_sum(const erd::Params& P, int spp, uint32_t view, ui
 /* the autofocus distance of film pixel (u, v) into out (one float) */
 cudaError_t er_launch_autofocus(const erd::Params& P, int u, int v, uint32_t lane0, uint32_t lane1, float* out, cudaStream_t s);
 cudaError_t er_launch_sigma_table(const erd::Plf* opacity, float density_scale, float* table, int n, cudaStream_t s);
+/* 3 float4 per integer intensity in [0, n): the shading transfer functions (erd::shade_tf) */
+cudaError_t er_launch_shade_table(const erd::Tfs* tfs, float4* tab, int n, cudaStream_t s);
 
 cudaError_t er_launch_post_frame(const float4* frame, float4* running, uchar4* rgba, int W, int H, int n_iter, float exposure,
                                  int filter, cudaStream_t s);

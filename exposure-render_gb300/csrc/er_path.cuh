@@ -83,6 +83,35 @@ ER_D float sigma_at(const Params& P, float I)
     return __ldg(P.sigma + i);
 }
 
+/* The transfer functions the shading reads at a scatter event, at its
+   intensity I.  I is an integer (GetIntensity returns an unsigned short,
+   Source/volume.h:131-138), so a per-tracer table built with the same
+   evaluations (k_shade_table) holds exactly the floats ctf_eval / plf_eval
+   give at I, without the node scans. */
+ER_D float opacity_at(const Params& P, float I)
+{
+    int i = (int)I;
+    i = i < 0 ? 0 : (i >= P.sigma_n ? P.sigma_n - 1 : i);
+    return __ldg(&P.shade_tab[3 * i + 1].w);
+}
+
+struct ShadeTF {
+    c3 Kd, Ks, Le;
+    float exponent, opacity;
+};
+
+ER_D void shade_tf(const Params& P, float I, ShadeTF& s)
+{
+    int i = (int)I;
+    i = i < 0 ? 0 : (i >= P.sigma_n ? P.sigma_n - 1 : i);
+    const float4 a = __ldg(P.shade_tab + 3 * i), b = __ldg(P.shade_tab + 3 * i + 1), c = __ldg(P.shade_tab + 3 * i + 2);
+    s.Kd = C3(a.x, a.y, a.z);
+    s.exponent = a.w;
+    s.Ks = C3(b.x, b.y, b.z);
+    s.opacity = b.w;
+    s.Le = C3(c.x, c.y, c.z);
+}
+
 /* ---- gradients: Source/volumes.h:31-114 ---- */
 
 ER_D v3 gdelta(const Params& P, int axis) { return V3(axis == 0 ? P.min_step : 0.0f, axis == 1 ? P.min_step : 0.0f, axis == 2 ? P.min_step : 0.0f); }
@@ -1216,7 +1245,7 @@ ER_D int select_shader_type(const Params& P, const Event& SE, float I, Rng& rng,
     case 2: {
         const float NGM = (gm >= 0.0f ? gm : gradient_magnitude(P, SE.P)) * P.gm_inv_max;
         const float Exponent = 25.0f * pow_c(P.gradient_factor, 3.0f) * NGM;
-        const float PdfBrdf = P.opacity_modulated ? plf_eval(P.tfs->opacity, I) * (1.0f - exp_c(-Exponent))
+        const float PdfBrdf = P.opacity_modulated ? opacity_at(P, I) * (1.0f - exp_c(-Exponent))
                                                   : 1.0f - exp_c(-Exponent);
         return rng.get1() <= PdfBrdf ? 0 : 1;
     }
@@ -1417,7 +1446,9 @@ ER_D c3 uniform_sample_one_light(const Params& P, const Event& SE, Rng& rng, con
 {
     c3 Ld = C3(0, 0, 0);
     const float I = get_intensity(P, SE.P);
-    Ld = cadd(Ld, ctf_eval(P.tfs->emission, I));
+    ShadeTF tf;
+    shade_tf(P, I, tf);
+    Ld = cadd(Ld, tf.Le);
     if (P.light_count <= 0) return Ld;
     const int idx = (int)floorf(ms.light_num * (float)P.light_count);
     if (idx < 0 || idx >= P.light_count || !P.light_valid[idx]) return Ld;
@@ -1427,8 +1458,7 @@ ER_D c3 uniform_sample_one_light(const Params& P, const Event& SE, Rng& rng, con
         object_shader(P, SE, hit, sh);
     } else {
         const int type = P.apply_shading_type ? select_shader_type(P, SE, I, rng) : 0;
-        shader_init(sh, type, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
-                    1000000.0f * pow_c(plf_eval(P.tfs->glossiness, I), 7.0f));
+        shader_init(sh, type, SE.N, SE.Wo, tf.Kd, tf.Ks, P.volume_ior, tf.exponent);
     }
     Ld = cadd(Ld, estimate_direct_light(P, L, idx, ms, SE, rng, sh));
     return cscale(Ld, (float)P.light_count);

@@ -7,6 +7,7 @@
  *   k_trace_sum   : `spp` counter-seeded samples per pixel in one launch,
  *                   summed in registers (one HBM write per pixel).
  *   k_sigma_table : DensityScale * Opacity1D(I) for every integer I.
+ *   k_shade_table : the shading transfer functions for every integer I.
  */
 #include "er_kernels.h"
 #include "er_path.cuh"
@@ -57,6 +58,19 @@ __global__ void k_sigma_table(const Plf* __restrict__ opacity, float density_sca
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     table[i] = density_scale * plf_eval(*opacity, (float)i);
+}
+
+/* the shading transfer functions at every integer intensity (shade_tf) */
+__global__ void k_shade_table(const Tfs* __restrict__ tfs, float4* __restrict__ tab, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float I = (float)i;
+    const c3 Kd = ctf_eval(tfs->diffuse, I), Ks = ctf_eval(tfs->specular, I), Le = ctf_eval(tfs->emission, I);
+    const float exponent = 1000000.0f * pow_c(plf_eval(tfs->glossiness, I), 7.0f);
+    tab[3 * i] = make_float4(Kd.r, Kd.g, Kd.b, exponent);
+    tab[3 * i + 1] = make_float4(Ks.r, Ks.g, Ks.b, plf_eval(tfs->opacity, I));
+    tab[3 * i + 2] = make_float4(Le.r, Le.g, Le.b, 0.0f);
 }
 
 /* ---- launchers ---- */
@@ -118,6 +132,12 @@ cudaError_t er_launch_trace_sum(const Params& P, int spp, uint32_t view, uint32_
     const dim3 b(16, 8);
     const dim3 g((P.film[0] + 15) / 16, (P.film[1] + 7) / 8);
     k_trace_sum<<<g, b, 0, s>>>(P, spp, view, first, sum, accumulate);
+    return cudaGetLastError();
+}
+
+cudaError_t er_launch_shade_table(const Tfs* tfs, float4* tab, int n, cudaStream_t s)
+{
+    k_shade_table<<<(n + 127) / 128, 128, 0, s>>>(tfs, tab, n);
     return cudaGetLastError();
 }
 

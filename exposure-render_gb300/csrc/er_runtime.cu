@@ -192,6 +192,7 @@ struct TracerItem {
     DevBuf<int> light_valid;
     DevBuf<erd::Texture> textures;
     DevBuf<float> sigma;
+    DevBuf<float4> shade_tab;      /* shading transfer functions per integer intensity */
     DevBuf<int> light_ids;
     DevBuf<float> majorant, rmq;   /* majorant: per brick, or -(distance to a non-empty brick) when empty */
     DevBuf<uint8_t> skip_tmp;
@@ -507,6 +508,9 @@ er_status build(TracerItem& t)
     ER_CUDA(er_launch_sigma_table(t.opacity.p, s.density_scale, t.sigma.p, n, st));
     P.sigma = t.sigma.p;
     P.sigma_n = n;
+    ER_CUDA(t.shade_tab.ensure(3 * (size_t)n));
+    ER_CUDA(er_launch_shade_table(t.tfs.p, t.shade_tab.p, n, st));
+    P.shade_tab = t.shade_tab.p;
     P.free_flight = s.free_flight;
     if (s.free_flight == ER_FREE_FLIGHT_DELTA) {
         int nb[3];

@@ -386,7 +386,9 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict
             SE.Wo = V3(e3.x, e3.y, e3.z);
             /* UniformSampleOneLight - Source/transport.h:115-156 */
             const float I = get_intensity(P, SE.P);
-            Le = cadd(C3(0, 0, 0), ctf_eval(P.tfs->emission, I));
+            ShadeTF tf;
+            shade_tf(P, I, tf);
+            Le = cadd(C3(0, 0, 0), tf.Le);
             bool early = P.light_count <= 0;
             int idx = 0;
             if (!early) {
@@ -403,8 +405,7 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict
                     object_shader(P, SE, hit, sh);
                 } else {
                     const int type = P.apply_shading_type ? select_shader_type(P, SE, I, rng, gm) : 0;
-                    shader_init(sh, type, SE.N, SE.Wo, ctf_eval(P.tfs->diffuse, I), ctf_eval(P.tfs->specular, I), P.volume_ior,
-                                1000000.0f * pow_c(plf_eval(P.tfs->glossiness, I), 7.0f));
+                    shader_init(sh, type, SE.N, SE.Wo, tf.Kd, tf.Ks, P.volume_ior, tf.exponent);
                 }
                 count = (float)P.light_count;
                 /* EstimateDirectLight - Source/transport.h:58-113, without the visibility terms */
