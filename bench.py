@@ -463,10 +463,10 @@ def run_ours(args, wl, rank, world, local_rank):
     if rank != 0:
         return
     conv = None
-    if world == 1 and not args.no_rmse and wl == "c2":
-        conv = convergence(lib, runtime, torch, ["c2"], {
-            "fast": {"free_flight": 1, "stratify": 1, "majorant_brick": r.tracer_desc.settings.majorant_brick},
-            "plain": {"free_flight": 0, "stratify": 0}})
+    if world == 1 and not args.no_rmse and wl in ("c1", "c2"):
+        conv = convergence(lib, runtime, torch, [wl], {
+            "fast": {"free_flight": 1, "mis": 1, "stratify": 1, "majorant_brick": r.tracer_desc.settings.majorant_brick},
+            "plain": {"free_flight": 0, "mis": 1, "stratify": 0}})
     peaks, peak_kind = measured_peaks()
     nthreads = os.cpu_count() or 1
     # work per sample of the measured configuration (oracle, whole field of view at 128^2)
@@ -498,7 +498,7 @@ def run_ours(args, wl, rank, world, local_rank):
         "reference_work_per_sample": ref_work,
         "plain": {"value": plain, "unit": "Msamples/s", "speedup": value / plain,
                   "what": "same workload and estimator, the reference's fixed-step march for free flight and shadows"},
-        "time_to_rmse": rmse_summary(conv, "c2", value, plain, width * height),
+        "time_to_rmse": rmse_summary(conv, wl, value, plain, width * height),
         "reference_order": {"value": ref_order, "unit": "Msamples/s",
                             "what": "reference live path (march, BRDF, light sampling), bit-exact with the reference"},
     }
