@@ -750,52 +750,12 @@ ER_D bool scatter_event_in_volume(const Params& P, const Ray& R, Rng& rng)
     return true;
 }
 
-/* IntersectLight - Source/lights.h:59-88 */
-ER_D void intersect_light(const Params& P, const Light& L, const Ray& R, Event& SE)
-{
-    const Ray Rt = xform_ray(L.inv_tm, R);
-    Isect Int; Int.invalid();
-    intersect_shape(L, Rt, Int);
-    if (Int.valid) {
-        SE.valid = true;
-        SE.P = xform_point(L.tm, Int.P);
-        SE.N = xform_vector(L.tm, Int.N);
-        SE.T = vlen(vsub(SE.P, R.O));
-        SE.Wo = vneg(R.D);
-        SE.Le = Int.front ? cscale(light_texture(P, L, Int.UV), L.multiplier) : C3(0, 0, 0);
-        if (L.unit == 1) SE.Le = cdivs(SE.Le, L.area);
-    }
-}
-
-/* IntersectLights - Source/lights.h:90-113; `slot` receives the LightIDs
-   index of the nearest hit (ScatterEvent::LightID) */
-ER_D void intersect_lights_slot(const Params& P, const Ray& R, Event& RS, bool respect_visibility, int& slot)
-{
-    float T = FLT_MAX;
-    for (int i = 0; i < P.light_count; i++) {
-        if (!P.light_valid[i]) continue;
-        const Light& L = P.lights[i];
-        if (respect_visibility && !L.visible) continue;
-        Event local;
-        local.type = 1; local.valid = false; local.T = 0.0f;
-        local.P = V3(0, 0, 0); local.N = V3(0, 0, 0); local.Wo = V3(0, 0, 0); local.Le = C3(0, 0, 0);
-        intersect_light(P, L, R, local);
-        if (local.valid && local.T < T) { RS = local; T = local.T; slot = i; }
-    }
-}
-
-ER_D void intersect_lights(const Params& P, const Ray& R, Event& RS, bool respect_visibility)
-{
-    int slot = -1;
-    intersect_lights_slot(P, R, RS, respect_visibility, slot);
-}
-
-/* intersect_lights_slot without the emission: the nearest hit's (P, N, T,
-   Wo) in RS, its LightIDs index in `slot` and what its emission needs in
-   `lh`; light_emission gives the Le intersect_light would have, for the hits
-   that are used (the environment sphere's texture is not evaluated for the
-   rays whose volume event or chosen light wins).  Same operations, same
-   nearest hit. */
+/* IntersectLight / IntersectLights - Source/lights.h:59-113, without the
+   emission: the nearest hit's (P, N, T, Wo) in RS, its LightIDs index in
+   `slot` (ScatterEvent::LightID) and what its emission needs in `lh`;
+   light_emission gives the Le IntersectLight computes, for the hits that are
+   used (the environment sphere's texture is not evaluated for the rays whose
+   volume event or chosen light wins).  Same operations, same nearest hit. */
 struct LightHit {
     v2 UV;
     bool front;
