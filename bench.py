@@ -879,18 +879,19 @@ def main():
     if args.impl == "reference":
         run_reference(args, args.workload, rank, world)
         return
-    if args.workload in ("c3", "c5"):
-        run_batched(args, rank, world, local_rank, args.workload)
-        return
-    if args.workload == "c4":
-        run_medium(args, rank, world, local_rank)
-        return
+    # replicas: one process per GPU; the process group carries only the
+    # barrier and the max-over-ranks timing of every workload
     if world > 1:
         import torch
         import torch.distributed as dist
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl")
-    run_ours(args, args.workload, rank, world, local_rank)
+    if args.workload in ("c3", "c5"):
+        run_batched(args, rank, world, local_rank, args.workload)
+    elif args.workload == "c4":
+        run_medium(args, rank, world, local_rank)
+    else:
+        run_ours(args, args.workload, rank, world, local_rank)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
