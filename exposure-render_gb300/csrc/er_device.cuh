@@ -64,6 +64,8 @@ struct Light {               /* ErLight + Shape (Source/erlight.h, Source/shape.
     int tex_const;           /* 1 when the light's texture does not vary over the surface (a uniform
                                 procedural texture, or none): tex_rgb is its value */
     float tex_rgb[3];
+    float inner_c[3];        /* sphere lights with a rigid transform: the centre in world space and */
+    float inner_r2;          /* (0.9 radius)^2 (< 0 otherwise): a segment with both ends inside cannot hit */
 };
 
 struct Object {              /* ErObject (Source/erobject.h:27-67) */

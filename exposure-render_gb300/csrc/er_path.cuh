@@ -798,6 +798,15 @@ ER_D bool intersects_light(const Params& P, const Ray& R)
     for (int i = 0; i < P.light_count; i++) {
         if (!P.light_valid[i]) continue;
         const Light& L = P.lights[i];
+        if (L.inner_r2 > 0.0f) {
+            /* a sphere (rigid transform) whose inner ball holds both ends of the
+               segment: the segment stays inside, 0.1 radius from the surface,
+               so the exact test below cannot find a root in [MinT, MaxT] */
+            const v3 c = vload(L.inner_c);
+            const v3 a = vsub(vadd(R.O, vscale(R.D, R.MinT)), c);
+            const v3 b = vsub(vadd(R.O, vscale(R.D, R.MaxT)), c);
+            if (vlen2(a) < L.inner_r2 && vlen2(b) < L.inner_r2) continue;
+        }
         const Ray Rt = xform_ray(L.inv_tm, R);
         Isect Int; Int.invalid();
         intersect_shape(L, Rt, Int);

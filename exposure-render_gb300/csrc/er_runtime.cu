@@ -543,6 +543,30 @@ er_status build(TracerItem& t)
         to_light(L[i], *it->second);
         valid[i] = 1;
     }
+    /* sphere lights with a rigid transform: the inner ball of the shadow
+       rays' occlusion early-out (intersects_light) */
+    for (int i = 0; i < lc; i++) {
+        erd::Light& l = L[i];
+        l.inner_r2 = -1.0f;
+        if (!valid[i] || l.type != ER_SHAPE_SPHERE || !(l.outer_radius > 0.0f)) continue;
+        /* the exact test maps the ray with InvTM: the sphere is centred where
+           InvTM sends a point to the origin, c = -R^T t for InvTM = (R, t) */
+        bool rigid = true;
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) {
+                double d = 0.0;
+                for (int k = 0; k < 3; k++) d += (double)l.inv_tm[k][r] * (double)l.inv_tm[k][c];
+                if (std::fabs(d - (r == c ? 1.0 : 0.0)) > 1e-5) rigid = false;
+            }
+        if (!rigid) continue;
+        for (int k = 0; k < 3; k++) {
+            double c = 0.0;
+            for (int r = 0; r < 3; r++) c -= (double)l.inv_tm[r][k] * (double)l.inv_tm[r][3];
+            l.inner_c[k] = (float)c;
+        }
+        const double ri = 0.9 * (double)l.outer_radius;
+        l.inner_r2 = (float)(ri * ri);
+    }
     /* lights whose texture is uniform (or unbound: black) get its value here,
        as EvaluateTexture computes it: colour * OutputLevel in float
        (Source/textures.h:63-111) */
