@@ -2162,6 +2162,26 @@ float ER_OR(gradient_magnitude_volume)(or_scene* s, uint16_t* gm)
 
 /* er_math functions on the host: fn 0 log, 1 exp, 2 sin, 3 cos, 4 tan,
    5 pow(x, y), 6 acos, 7 atan2(x, y) */
+/* IntersectsLight for one light shape and n segments (origin, unit
+   direction, MinT, MaxT: 8 floats each): 1 where the exact test of
+   Visible (Source/transport.h:46-56) finds the shape on the segment.  Test
+   infrastructure for the occlusion early-outs of the GPU shadow stage. */
+void ER_OR(segments_hit_shape)(const er_shape* shape, int32_t n, const float* seg, int32_t* hit)
+{
+    for (int i = 0; i < n; i++) {
+        const float* q = seg + 8 * (size_t)i;
+        ray_t R;
+        R.O = V3(q[0], q[1], q[2]);
+        R.D = V3(q[3], q[4], q[5]);
+        R.MinT = q[6];
+        R.MaxT = q[7];
+        const ray_t Rt = xform_ray(shape->inv_tm, &R);
+        isect_t Int; isect_invalid(&Int);
+        intersect_shape(shape, &Rt, &Int);
+        hit[i] = Int.valid ? 1 : 0;
+    }
+}
+
 void ER_OR(math_eval)(int32_t fn, int32_t n, const float* x, const float* y, float* out)
 {
     for (int i = 0; i < n; i++) {

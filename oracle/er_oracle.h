@@ -134,6 +134,8 @@ void ER_OR(bilateral)(const uint8_t* in, uint8_t* tmp, uint8_t* out, int32_t wid
 float ER_OR(gradient_magnitude_volume)(or_scene* scene, uint16_t* gm);
 /* include/er_math.h on the host: fn 0 log, 1 exp, 2 sin, 3 cos, 4 tan, 5 pow, 6 acos, 7 atan2 */
 void ER_OR(math_eval)(int32_t fn, int32_t n, const float* x, const float* y, float* out);
+/* IntersectsLight of one shape for n segments (O, D, MinT, MaxT: 8 floats each) */
+void ER_OR(segments_hit_shape)(const er_shape* shape, int32_t n, const float* seg, int32_t* hit);
 /* majorant grid of the delta tracker: ds * max sigma over each brick plus a one-voxel apron */
 void ER_OR(majorant_grid)(const uint16_t* vox, const int32_t* res, int32_t brick, const float* sigma, int32_t n, float ds, float* out);
 

@@ -40,6 +40,8 @@ class Oracle:
         f("scene_destroy", None, [c_void_p])
         f("scene_set_objects", None, [c_void_p, c_void_p, c_int32])
         f("scene_set_bitmaps", None, [c_void_p, c_void_p, c_int32])
+        if prefix != "ref_":
+            f("segments_hit_shape", None, [POINTER(C.er_shape), c_int32, c_void_p, c_void_p])
         f("render_frame", None, [c_void_p, c_void_p, c_void_p, c_int32])
         f("render_sum", None, [c_void_p, c_int32, c_uint32, c_uint32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_int32])
         if prefix != "ref_":

@@ -119,3 +119,46 @@ def test_stratified_light_samples_lower_rmse(oracle):
         h.close()
         err[strat] = float(np.sqrt(np.mean(mse)))
     assert 0.0 < err[1] < 0.9 * err[0], err
+
+
+def test_sphere_light_inner_ball_segments_never_hit(oracle):
+    """the premise of the GPU shadow stage's occlusion early-out for sphere
+    lights with a rigid InvTM: a segment whose two ends lie in the ball of
+    0.9 radius around the centre is never hit by IntersectsLight's exact test,
+    and segments that leave the sphere are (random rotations, translations,
+    radii)"""
+    import ctypes
+    rng = np.random.default_rng(9)
+    for trial in range(20):
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        w, x, y, z = q
+        Rm = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                       [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                       [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+        c = rng.uniform(-3, 3, size=3)
+        r = float(rng.uniform(0.2, 6.0))
+        tm = np.eye(4); tm[:3, :3] = Rm; tm[:3, 3] = c
+        inv = np.linalg.inv(tm)
+        sh = S.make_shape(C.SHAPE_SPHERE, (tm.tolist(), inv.tolist()), outer=r)
+
+        def segments(p0, p1):
+            d = p1 - p0
+            L = np.linalg.norm(d, axis=1, keepdims=True)
+            seg = np.concatenate([p0, d / L, np.zeros((len(p0), 1)), L], axis=1).astype(np.float32)
+            hit = np.zeros(len(p0), np.int32)
+            oracle.segments_hit_shape(ctypes.byref(sh), len(p0), OL.ptr(seg), OL.ptr(hit))
+            return hit
+
+        def ball(n, rad):
+            v = rng.normal(size=(n, 3))
+            v /= np.linalg.norm(v, axis=1, keepdims=True)
+            return c + v * (rad * rng.uniform(0.0, 1.0, size=(n, 1)) ** (1.0 / 3.0))
+
+        n = 4000
+        inside = segments(ball(n, 0.9 * r * 0.9999), ball(n, 0.9 * r * 0.9999))
+        assert inside.sum() == 0, trial
+        out = rng.normal(size=(n, 3))
+        far = c + out / np.linalg.norm(out, axis=1, keepdims=True) * 1.5 * r
+        crossing = segments(ball(n, 0.5 * r), far)
+        assert crossing.mean() > 0.99, trial
