@@ -63,6 +63,9 @@ def test_struct_layout_matches_c():
         src += f'printf("{s} %zu\\n", sizeof({s}));\n'
     src += 'printf("settings.seed %zu\\n", offsetof(er_render_settings, seed));\n'
     src += 'printf("tracer.volume_id %zu\\n", offsetof(er_tracer_desc, volume_id));\n'
+    src += 'printf("settings.stratify %zu\\n", offsetof(er_render_settings, stratify));\n'
+    src += 'printf("settings.tune_stages %zu\\n", offsetof(er_render_settings, tune_stages));\n'
+    src += 'printf("tune.tune_stages %zu\\n", offsetof(er_tune_result, tune_stages));\n'
     src += 'printf("batch.d_sum %zu\\n", offsetof(er_batch_view, d_sum_xyza));\nreturn 0;}\n'
     with tempfile.TemporaryDirectory() as d:
         c = os.path.join(d, "s.c")
@@ -76,3 +79,6 @@ def test_struct_layout_matches_c():
     assert int(got["settings.seed"]) == C.er_render_settings.seed.offset
     assert int(got["tracer.volume_id"]) == C.er_tracer_desc.volume_id.offset
     assert int(got["batch.d_sum"]) == C.er_batch_view.d_sum_xyza.offset
+    assert int(got["settings.stratify"]) == C.er_render_settings.stratify.offset
+    assert int(got["settings.tune_stages"]) == C.er_render_settings.tune_stages.offset
+    assert int(got["tune.tune_stages"]) == C.er_tune_result.tune_stages.offset
