@@ -336,20 +336,69 @@ def reference_path(scene):
     return out
 
 
+def batched_workload(wl, n_views=0):
+    """(scenes, views, workload name) of the batched workloads: c3, 64 orbit
+    views over three blob volumes; c5, 16 views of 2048^2 at 64 spp over the
+    1024x1024x512 volume"""
+    S = importlib.import_module("exposure-render_gb300.scenes")
+    if wl == "c5":
+        views = S.c5_views(n_views=n_views or 16)
+        return [S.scene_c5(S.c5_volume())], views, "c5-batched-%d-views-2048^2-1024x1024x512-volume" % len(views)
+    views = S.c3_views(n_views=n_views or 64)
+    return S.c3_scenes(), views, "c3-batched-%d-views-3-blob-volumes" % len(views)
+
+
+def batched_reference_rate(scenes, views, seconds_target=12.0, steps=1):
+    """Samples/s of the reference transport on the host cores over a batch of
+    views: the first view of each volume stands for that volume's views and is
+    timed on a centre crop at 1 spp (an equal share of `seconds_target`); the
+    batch's rate weights each volume by its views' samples,
+    sum(n_k) / sum(n_k / rate_k)."""
+    first, n = {}, {}
+    for k, cam, spp in views:
+        first.setdefault(k, cam)
+        n[k] = n.get(k, 0) + cam.film_size[0] * cam.film_size[1] * spp
+    seconds, kind, cores, crops = 0.0, None, None, []
+    for k in sorted(first):
+        sc = reference_path(scenes[k])
+        sc.tracer.camera = first[k]
+        rate, kind, cores, sample = cpu_reference_rate(sc, seconds_target=seconds_target / len(first), steps=steps)
+        seconds += n[k] / rate
+        crops.append("volume %d: %s" % (k, sample.split(" centre")[0]))
+    rate = sum(n.values()) / seconds
+    sample = "first view of each volume, centre crop x 1 spp per step (%s), weighted by the volume's samples" % ", ".join(crops)
+    return rate, kind, cores, sample
+
+
 def run_reference(args, wl, rank, world):
     if rank != 0:
         return
-    scene = reference_path(make_scene(wl))
-    shading = describe_shading(scene)
-    W = WORKLOADS[wl]
-    for _ in range(args.warmup):
-        cpu_reference_rate(scene, seconds_target=2.0, steps=1)
-    rate, kind, cores, sample = cpu_reference_rate(scene, seconds_target=10.0 * max(1, args.steps) / 3.0, steps=args.steps)
+    if wl == "c4":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no differentiable medium and no "
+                          "adjoint (its transport is forward only)"}), flush=True)
+        return
+    if wl in ("c3", "c5"):
+        scenes, views, name = batched_workload(wl, args.views)
+        shading = describe_shading(reference_path(scenes[0]))
+        for _ in range(args.warmup):
+            batched_reference_rate(scenes, views, seconds_target=2.0, steps=1)
+        rate, kind, cores, sample = batched_reference_rate(scenes, views, seconds_target=10.0 * max(1, args.steps) / 3.0,
+                                                           steps=args.steps)
+        config = {"workload": name, "views": len(views),
+                  "samples_per_step": sum(c.film_size[0] * c.film_size[1] * s for _, c, s in views), **shading}
+    else:
+        scene = reference_path(make_scene(wl))
+        shading = describe_shading(scene)
+        W = WORKLOADS[wl]
+        for _ in range(args.warmup):
+            cpu_reference_rate(scene, seconds_target=2.0, steps=1)
+        rate, kind, cores, sample = cpu_reference_rate(scene, seconds_target=10.0 * max(1, args.steps) / 3.0, steps=args.steps)
+        config = {"workload": W["name"], "film": list(W["film"]), "spp": W["spp"], **shading}
     line = {
         "impl": "reference", "metric": "Msamples/s", "value": rate / 1e6, "unit": "Msamples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": W["name"], "film": list(W["film"]), "spp": W["spp"], **shading},
+        "config": config,
         "cpu_baseline": {"value": rate / 1e6, "unit": "Msamples/s", "cores": cores, "kind": kind, "sample": sample},
         "e2e": {"value": rate / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -515,28 +564,22 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
     import torch
     torch.cuda.set_device(local_rank)
     runtime = importlib.import_module("exposure-render_gb300.runtime")
-    S = importlib.import_module("exposure-render_gb300.scenes")
     C = importlib.import_module("exposure-render_gb300.capi")
     lib = C.load_library()
     C.check(lib.er_set_device(local_rank))
     stream = torch.cuda.current_stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
     C.check(lib.er_set_stream(sp))
-    c5_vol = None
-    if wl == "c5":
-        t_gen = time.perf_counter()
-        c5_vol = S.c5_volume()
-        gen_s = time.perf_counter() - t_gen
-        scenes = [S.scene_c5(c5_vol)]
-    else:
-        scenes = S.c3_scenes()
+    t_gen = time.perf_counter()
+    scenes, views, wl_name = batched_workload(wl, args.views)
+    gen_s = time.perf_counter() - t_gen
+    c5_vol = scenes[0].volume if wl == "c5" else None
     for sc in scenes:
         sc.tracer.settings.seed = R.view_seed(1, rank)
     dist = None
     if world > 1:
         import torch.distributed as dist
     rs = [runtime.Renderer(sc, lib) for sc in scenes]
-    views = S.c5_views(n_views=args.views or 16) if wl == "c5" else S.c3_views(n_views=args.views or 64)
     # autotune each volume's tracer on one of its views (probe: 2 spp)
     tuned = []
     for k, r in enumerate(rs):
@@ -667,13 +710,14 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
         adjoint = c5_adjoint(args, lib, runtime, torch, stream, c5_vol)
     if rank != 0:
         return
+    # the reference transport on the host cores (rank 0 at N = 1 only)
+    cpu = batched_reference_rate(scenes, views) if world == 1 else None
     vol_bytes = sum(sc.volume.nbytes for sc in scenes)
     line = {
         "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": ("c5-batched-%d-views-2048^2-1024x1024x512-volume" % len(views)) if wl == "c5" else
-                   ("c3-batched-%d-views-3-blob-volumes" % len(views)), "views": len(views),
+        "config": {"workload": wl_name, "views": len(views),
                    "samples_per_step": samples_per_step, "films": sorted({c.film_size[0] for _, c, _ in views}),
                    "spp_range": [min(s for _, _, s in views), max_spp], **describe_shading(scenes[0]),
                    "free_flight": "delta+ratio tracking, majorant bricks per volume below",
@@ -682,6 +726,8 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
                    "majorant_bricks": [r.tracer_desc.settings.majorant_brick for r in rs],
                    "l2": "volumes %d MiB in total; every step renders fresh samples" % (vol_bytes >> 20),
                    "parallelism": "replicas" if world > 1 else "single"},
+        "cpu_baseline": ({"value": cpu[0] / 1e6, "unit": "Msamples/s", "cores": cpu[2], "kind": cpu[1], "sample": cpu[3]}
+                         if cpu else None),
         "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(vol_bytes),
                 "d2h_bytes_per_step": d2h_bytes},
         "clocks": clk.summary(),
