@@ -12,7 +12,7 @@ import importlib
 import os
 import subprocess
 import sys
-from ctypes import POINTER, c_double, c_float, c_int32, c_uint32, c_uint8, c_void_p
+from ctypes import POINTER, c_double, c_float, c_int32, c_uint32, c_void_p
 
 import numpy as np
 

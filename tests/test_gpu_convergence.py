@@ -3,7 +3,6 @@
 delta-tracking path and reaches 1e-2."""
 import importlib
 
-import numpy as np
 import pytest
 
 import convergence as CV

@@ -3,7 +3,6 @@ bit-exact with the CPU oracle, the path-replay adjoint against the oracle's
 adjoint and against central finite differences (h = 1e-3) of the binary64
 evaluation of the same samples, at the differentiable workload's size (128^3
 density, 64 opacity values, 256^2 x 32 spp)."""
-import ctypes
 import importlib
 
 import numpy as np
