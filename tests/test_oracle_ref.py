@@ -169,3 +169,126 @@ def test_bitmap_textures(oracle, ref):
     sc.tracer.settings.mis = 1
     c = OL.SceneHandle(oracle, sc)
     assert c.render_sum(2, nthreads=4)[..., :3].max() > 0
+
+
+def random_scene(seed):
+    """A scene on the reference's live path with every parameter drawn from a
+    seeded generator: a non-cubic blob volume with anisotropic spacing, random
+    unsorted transfer-function nodes, step factors, shadow settings and
+    gradient mode, an orbit camera (thin lens on odd seeds), and one to three
+    lights of random shape, orientation, size, sidedness, unit and texture
+    (uniform, checker or gradient with random offset, repeat and flips).
+    The volume's size is normalised: without NormalizeSize the reference
+    scales the spacing by 0 (Source/volume.h:106-114), an empty box, which
+    test_volume_without_normalize_size_is_empty covers."""
+    rng = np.random.default_rng(1000 + seed)
+    shape_zyx = tuple(int(v) for v in rng.integers(10, 26, size=3))
+    sc = S.scene_tiny(res=16, film=(22, 18), seed=3)
+    sc.volume = S.blob_volume(shape_zyx, n_blobs=5, seed=seed + 20)
+    sc.spacing = tuple(float(v) for v in rng.uniform(0.6, 1.8, size=3))
+    sc.normalize_size = 1
+    t = sc.tracer
+
+    def nodes(n, lo, hi):
+        return [(float(rng.uniform(0.0, 4500.0)), float(rng.uniform(lo, hi))) for _ in range(n)]
+
+    t.opacity = C.make_plf(nodes(int(rng.integers(2, 8)), 0.0, 1.0))
+    t.diffuse = C.make_color_tf([(p, tuple(float(x) for x in rng.uniform(0.1, 1.0, 3)))
+                                 for p, _ in nodes(int(rng.integers(1, 5)), 0, 1)])
+    t.specular = C.make_color_tf([(p, tuple(float(x) for x in rng.uniform(0.0, 0.5, 3)))
+                                  for p, _ in nodes(int(rng.integers(1, 4)), 0, 1)])
+    t.glossiness = C.make_plf(nodes(int(rng.integers(1, 4)), 0.05, 0.95))
+    t.emission = C.make_color_tf([(p, tuple(float(x) for x in rng.uniform(0.0, 0.3, 3)))
+                                  for p, _ in nodes(int(rng.integers(1, 3)), 0, 1)])
+    s = t.settings
+    s.density_scale = float(rng.uniform(20.0, 200.0))
+    s.step_factor_primary = float(rng.uniform(0.5, 2.0))
+    s.step_factor_shadow = float(rng.uniform(0.5, 3.0))
+    s.shadows = int(rng.integers(0, 2))
+    s.max_shadow_distance = float(rng.uniform(0.3, 1.5))
+    s.gradient_computation = int(rng.integers(0, 3))
+    s.seed = int(rng.integers(1, 1 << 30))
+    cam = S.orbit_camera(rng, (22, 18), radius=float(rng.uniform(1.6, 2.6)), fov=float(rng.uniform(25.0, 55.0)),
+                         exposure=float(rng.uniform(0.5, 2.0)))
+    if seed % 2:
+        cam.aperture_size = float(rng.uniform(0.01, 0.08))
+        cam.focal_distance = float(rng.uniform(1.0, 2.5))
+    t.camera = cam
+    sc.textures = []
+    for k in range(3):
+        kind = int(rng.integers(0, 3))
+        if kind == 0:
+            tex = S.uniform_texture(tuple(float(x) for x in rng.uniform(0.3, 1.0, 3)), level=float(rng.uniform(0.5, 2.0)))
+        elif kind == 1:
+            tex = S.checker_texture(tuple(float(x) for x in rng.uniform(0.0, 1.0, 3)),
+                                    tuple(float(x) for x in rng.uniform(0.0, 1.0, 3)),
+                                    level=float(rng.uniform(0.5, 2.0)), repeat=tuple(float(x) for x in rng.uniform(0.5, 4.0, 2)))
+        else:
+            tex = S.gradient_texture([(0.0, tuple(float(x) for x in rng.uniform(0, 1, 3))),
+                                      (float(rng.uniform(0.2, 0.8)), tuple(float(x) for x in rng.uniform(0, 1, 3))),
+                                      (1.0, tuple(float(x) for x in rng.uniform(0, 1, 3)))],
+                                     level=float(rng.uniform(0.5, 2.0)))
+        tex.offset[0], tex.offset[1] = (float(x) for x in rng.uniform(-0.5, 0.5, 2))
+        tex.flip[0], tex.flip[1] = (int(x) for x in rng.integers(0, 2, 2))
+        sc.textures.append(tex)
+    shapes = [C.SHAPE_PLANE, C.SHAPE_DISK, C.SHAPE_RING, C.SHAPE_BOX, C.SHAPE_SPHERE]
+    sc.lights = []
+    n_lights = int(rng.integers(1, 4))
+    for i in range(n_lights):
+        L = C.er_light_desc()
+        L.visible = int(rng.integers(0, 2))
+        d = rng.normal(size=3)
+        pos = tuple(float(x) for x in d / np.linalg.norm(d) * rng.uniform(0.9, 1.6))
+        up = tuple(float(x) for x in rng.normal(size=3))
+        st = shapes[int(rng.integers(0, len(shapes)))]
+        inner = float(rng.uniform(0.05, 0.15))
+        L.shape = S.make_shape(st, S.look_at_tm(pos, (0.0, 0.0, 0.0), up),
+                               size=tuple(float(x) for x in rng.uniform(0.2, 0.6, 3)),
+                               inner=inner, outer=inner + float(rng.uniform(0.1, 0.3)),
+                               one_sided=int(rng.integers(0, 2)) if st in (C.SHAPE_PLANE, C.SHAPE_DISK, C.SHAPE_RING) else 0)
+        L.texture_id = int(rng.integers(0, len(sc.textures)))
+        L.multiplier = float(rng.uniform(2.0, 30.0))
+        L.unit = int(rng.integers(0, 2))
+        sc.lights.append(L)
+        t.light_ids[i] = i
+    t.light_count = n_lights
+    return sc
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_random_scenes_bit_exact(oracle, ref, seed):
+    """seeded random scenes on the live path: sample sums and two stateful
+    frames equal the reference build bit for bit"""
+    sc = random_scene(seed)
+    a, b = OL.SceneHandle(oracle, sc), OL.SceneHandle(ref, sc)
+    try:
+        sa, sb = a.render_sum(3, nthreads=4), b.render_sum(3, nthreads=4)
+        assert np.array_equal(bits(sa), bits(sb))
+        assert np.isfinite(sa).all() and sa[..., 3].max() > 0
+        la = OL.initial_lanes(seed + 1, sc.width, sc.height)
+        lb = la.copy()
+        for _ in range(2):
+            assert np.array_equal(bits(a.render_frame(la, 4)), bits(b.render_frame(lb, 4)))
+            assert np.array_equal(la, lb)
+    finally:
+        a.close()
+        b.close()
+
+
+def test_volume_without_normalize_size_is_empty(oracle, ref):
+    """ErVolume without NormalizeSize: Volume's copy leaves Scale at 0 and
+    multiplies the spacing by it (Source/volume.h:106-114), so the box has
+    size 0 and no camera ray meets the volume; both builds render an empty,
+    finite image, bit for bit"""
+    sc = random_scene(0)
+    sc.normalize_size = 0
+    for L in sc.lights:
+        L.visible = 0
+    a, b = OL.SceneHandle(oracle, sc), OL.SceneHandle(ref, sc)
+    try:
+        sa, sb = a.render_sum(2, nthreads=4), b.render_sum(2, nthreads=4)
+        assert np.array_equal(bits(sa), bits(sb))
+        assert np.isfinite(sa).all() and not sa.any()
+    finally:
+        a.close()
+        b.close()
