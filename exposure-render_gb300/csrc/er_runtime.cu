@@ -1106,6 +1106,11 @@ ER_API er_status er_bind_volume(const er_volume_desc* d, int32_t* id)
     if (!d || !d->voxels) return fail(ER_ERR_INVALID_ARGUMENT, "volume descriptor or voxel pointer is NULL");
     for (int i = 0; i < 3; i++)
         if (d->resolution[i] <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "volume resolution must be positive");
+    /* a zero, negative or non-finite spacing gives a degenerate box whose
+       fixed-step marches take steps of zero or NaN length */
+    for (int i = 0; i < 3; i++)
+        if (!(d->spacing[i] > 0.0f) || !std::isfinite(d->spacing[i]))
+            return fail(ER_ERR_INVALID_ARGUMENT, "volume spacing must be finite and positive");
     if (!d->normalize_size)
         return fail(ER_ERR_INVALID_ARGUMENT, "normalize_size = 0 collapses the volume to zero size (Source/volume.h:106-117 leaves Scale = 0)");
     Context& C = ctx();

@@ -82,3 +82,66 @@ def test_struct_layout_matches_c():
     assert int(got["settings.stratify"]) == C.er_render_settings.stratify.offset
     assert int(got["settings.tune_stages"]) == C.er_render_settings.tune_stages.offset
     assert int(got["tune.tune_stages"]) == C.er_tune_result.tune_stages.offset
+
+
+@pytest.mark.parametrize("case", ["null", "resolution", "spacing-zero", "spacing-negative", "spacing-nan", "spacing-inf",
+                                  "no-normalize"])
+def test_bind_volume_rejects_degenerate_descriptors(case):
+    """er_bind_volume refuses, before any device work, a descriptor whose box
+    would be degenerate: a zero, negative or non-finite spacing, or
+    normalize_size = 0 (the reference then scales the spacing by 0,
+    Source/volume.h:106-114)"""
+    import numpy as np
+    L = C.load_library()
+    vox = np.zeros((4, 4, 4), dtype=np.uint16)
+    d = C.er_volume_desc()
+    for i in range(3):
+        d.resolution[i] = 4
+        d.spacing[i] = 1.0
+    d.normalize_size = 1
+    d.voxels = vox.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16))
+    if case == "null":
+        d.voxels = None
+    elif case == "resolution":
+        d.resolution[1] = 0
+    elif case == "no-normalize":
+        d.normalize_size = 0
+    else:
+        d.spacing[2] = {"spacing-zero": 0.0, "spacing-negative": -1.0, "spacing-nan": float("nan"),
+                        "spacing-inf": float("inf")}[case]
+    vid = ctypes.c_int32(-1)
+    assert L.er_bind_volume(ctypes.byref(d), ctypes.byref(vid)) == C.ER_ERR_INVALID_ARGUMENT
+    assert vid.value == -1
+    msg = L.er_last_error_message().decode()
+    assert {"null": "NULL", "resolution": "resolution", "no-normalize": "normalize_size"}.get(case, "spacing") in msg
+
+
+@pytest.mark.parametrize("case", ["step-primary-zero", "step-shadow-nan", "density-zero", "density-inf", "film-zero",
+                                  "film-huge", "lights-negative"])
+def test_bind_tracer_rejects_invalid_settings(case):
+    """er_bind_tracer refuses, before any device work, settings under which a
+    march would take steps of zero or NaN length, and out-of-range films and
+    light counts"""
+    L = C.load_library()
+    t = OL.PKG.scenes.c1_tracer((16, 16))
+    s = t.settings
+    if case == "step-primary-zero":
+        s.step_factor_primary = 0.0
+    elif case == "step-shadow-nan":
+        s.step_factor_shadow = float("nan")
+    elif case == "density-zero":
+        s.density_scale = 0.0
+    elif case == "density-inf":
+        s.density_scale = float("inf")
+    elif case == "film-zero":
+        t.camera.film_size[0] = 0
+    elif case == "film-huge":
+        t.camera.film_size[1] = 40000
+    else:
+        t.light_count = -1
+    tid = ctypes.c_int32(-1)
+    assert L.er_bind_tracer(ctypes.byref(t), ctypes.byref(tid)) == C.ER_ERR_INVALID_ARGUMENT
+    assert tid.value == -1
+    msg = L.er_last_error_message().decode()
+    assert {"step": "step factors", "density": "density_scale", "film": "film size",
+            "lights": "light_count"}[case.split("-")[0]] in msg
