@@ -54,7 +54,8 @@ def make_scene(wl):
     S = importlib.import_module("exposure-render_gb300.scenes")
     if wl == "c2":
         return S.scene_c2(res=512, film=WORKLOADS[wl]["film"], spp=WORKLOADS[wl]["spp"])
-    return S.scene_c1(res=128, film=WORKLOADS[wl]["film"], spp=WORKLOADS[wl]["spp"])
+    # c1 is specified with the isotropic phase function at every volume event
+    return S.scene_c1(res=128, film=WORKLOADS[wl]["film"], spp=WORKLOADS[wl]["spp"], phase=True)
 
 
 def describe_shading(scene):
@@ -212,12 +213,16 @@ def stage_bytes(w):
 
 
 def stage_roofline(work, ref_work, stage_ms, stage_launches, samples, peaks, peak_kind, wl):
-    """roofline of the transport: the reference estimator's algorithmic bytes
-    per sample (16 per lookup of the fixed-step march + 32 for the float4
-    accumulate) over the wavefront window's time (its four stage launches);
-    a fraction above 1 means fewer lookups than the reference needs.  The
-    stages' own bytes (this estimator's lookups and queue records) are
-    reported per stage."""
+    """roofline of the dominant wavefront stage: its own algorithmic bytes
+    per sample (this estimator's volume lookups at 16 B, majorant reads at
+    4 B, the queue records it reads and writes) times the samples of one
+    launch, over that stage's average launch time from CUDA events on the
+    launching stream, against the measured HBM copy bandwidth.  `traffic`
+    is the stage's measured DRAM bytes per launch (ncu, profiles/), so
+    traffic / algorithmic bytes says how much of the gather the caches
+    absorb.  The reference estimator's bytes over the whole window (its
+    fixed-step march makes far more lookups) are kept apart as
+    `reference_equivalent`: a throughput figure, not a roofline."""
     names = ("primary", "shade", "shadow", "reduce")
     bps = stage_bytes(work)
     total = float(sum(stage_ms)) or 1.0
@@ -227,19 +232,24 @@ def stage_roofline(work, ref_work, stage_ms, stage_launches, samples, peaks, pea
         stages[n] = {"ms": t, "share": t / total, "launches": int(stage_launches[i]),
                      "bytes_per_sample": bps[n], "achieved_gbs": (bps[n] * samples / (t / 1e3) / 1e9) if t > 0 else None}
     top = max(names, key=lambda n: stages[n]["ms"])
-    windows = max(int(stage_launches[0]), 1)
-    b_ref = BYTES_PER_LOOKUP * ref_work["lookups"] + 32.0
-    achieved = b_ref * samples / (total / 1e3) / 1e9
+    launches = max(int(stages[top]["launches"]), 1)
+    top_ms = stages[top]["ms"] / launches
+    alg = bps[top] * samples / launches
+    achieved = alg / (top_ms / 1e3) / 1e9
     traffic = profile_traffic(wl)
+    b_ref = BYTES_PER_LOOKUP * ref_work["lookups"] + 32.0
+    ref_gbs = b_ref * samples / (total / 1e3) / 1e9
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-        "peak_source": peak_kind, "kernel": "wavefront window (k_wf_primary + k_wf_shade + k_wf_shadow + k_wf_reduce)",
-        "avg_launch_ms": total / windows, "algorithmic_bytes_per_launch": b_ref * samples / windows,
-        "basis": "reference estimator: %.1f lookups/sample (fixed-step march, oracle) x 16 B + 32 B" % ref_work["lookups"],
-        "traffic": (traffic.get("window") if traffic else None),
-        "dominant_stage": {"kernel": "k_wf_" + top, "bytes_per_sample": bps[top], "achieved_gbs": stages[top]["achieved_gbs"],
-                           "frac": (stages[top]["achieved_gbs"] or 0.0) / peaks["hbm_gbs"],
-                           "traffic": (traffic.get(top) if traffic else None)},
+        "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured" else peak_kind,
+        "kernel": "k_wf_" + top, "avg_launch_ms": top_ms, "algorithmic_bytes_per_launch": alg,
+        "basis": "%.1f B/sample of this stage (lookups x 16 B + majorant reads x 4 B + queue records, oracle work counts)"
+                 " x %d samples per launch" % (bps[top], samples // launches),
+        "traffic": (traffic.get(top) if traffic else None),
+        "traffic_source": (traffic.get("note") if traffic else None),
+        "reference_equivalent": {"gbs": ref_gbs, "what": "the reference estimator's algorithmic bytes (%.1f lookups/sample of the "
+                                 "fixed-step march x 16 B + 32 B) per wavefront-window time: throughput in the reference's "
+                                 "currency, not a bandwidth" % ref_work["lookups"]},
     }
     return roofline, stages
 
@@ -280,6 +290,93 @@ def convergence(lib, runtime, torch, names, patches, max_spp=4096, target=1e-2):
         res["reference_spp"] = int(ref["spp"])
         out[name] = res
         r.close()
+    return out
+
+
+FILM_SCHEDULE = (8, 16, 32, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048)
+
+
+def film_convergence(lib, torch, r, patches, ref_patch, ref_spp, target=1e-2, budget_s=45.0, stream=None):
+    """Samples per pixel to image RMSE `target` at the workload's own film.
+
+    The converged image is the unbiased estimator (`ref_patch`: delta
+    tracking, ratio-tracked shadows, full MIS) rendered on the GPU at
+    `ref_spp` from its own random stream (view 97), as two independent
+    halves whose difference gives its own noise (subtracted in quadrature,
+    as for the FP64 references).  That estimator's convergence to the FP64
+    oracle is checked on 128^2 views of the same workloads
+    (tests/test_gpu_convergence.py, and `fp64_128` below).  Each
+    configuration of `patches` then renders from view 0 along FILM_SCHEDULE
+    until its RMSE reaches `target` (or `budget_s` of rendering is spent)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import convergence as CV
+    W, H = r.width, r.height
+    d = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+
+    def apply(patch):
+        for k, v in patch.items():
+            setattr(r.tracer_desc.settings, k, v)
+        r.rebind_tracer()
+
+    def accumulate(acc, spp, view, first, chunk=64):
+        n = 0
+        while n < spp:
+            c = min(chunk, spp - n)
+            r.trace_sum_device(d.data_ptr(), c, view, first + n, 0, stream)
+            acc += d.double()
+            n += c
+
+    saved = {k: getattr(r.tracer_desc.settings, k) for p in [ref_patch, *patches.values()] for k in p}
+    apply(ref_patch)
+    half = ref_spp // 2
+    a = torch.zeros((H, W, 4), dtype=torch.float64, device="cuda")
+    b = torch.zeros((H, W, 4), dtype=torch.float64, device="cuda")
+    t0 = time.perf_counter()
+    accumulate(a, half, 97, 0)
+    accumulate(b, half, 97, half)
+    torch.cuda.synchronize()
+    ref_s = time.perf_counter() - t0
+    e = float(r.tracer_desc.camera.exposure)
+    an, bn = (a / half).cpu().numpy(), (b / half).cpu().numpy()
+    diff = CV.tonemap_rgb(an, e) - CV.tonemap_rgb(bn, e)
+    ref = {"mean_xyz": 0.5 * (an + bn)[..., :3], "exposure": e, "noise2": float(np.mean(diff * diff)) / 4.0}
+    del a, b, an, bn
+    out = {"reference": {"spp": 2 * half, "noise": float(np.sqrt(ref["noise2"])), "seconds": ref_s, "film": [W, H],
+                         "what": "the unbiased estimator (delta tracking, ratio-tracked shadows, full MIS) at the "
+                                 "workload's film, GPU, own random stream"}}
+    for label, patch in patches.items():
+        apply(patch)
+        acc = torch.zeros((H, W, 4), dtype=torch.float64, device="cuda")
+        n, spps, errs, spent = 0, [], [], 0.0
+        for m in FILM_SCHEDULE:
+            t1 = time.perf_counter()
+            accumulate(acc, m - n, 0, n)
+            torch.cuda.synchronize()
+            spent += time.perf_counter() - t1
+            n = m
+            err = CV.rmse((acc / n).cpu().numpy(), ref)
+            spps.append(n)
+            errs.append(err)
+            if err <= target or spent > budget_s:
+                break
+        out[label] = {"spp": spps, "rmse": errs, "spp_to_target": CV.spp_to_rmse(spps, errs, target)}
+        del acc
+    apply(saved)
+    return out
+
+
+def film_rmse_summary(fc, fast_value, plain_value, npix, target=1e-2):
+    """time to image RMSE `target` at the workload's own film from the
+    measured samples-to-target and the measured rates of each path"""
+    if not fc:
+        return None
+    f, p = fc["fast"]["spp_to_target"], fc["plain"]["spp_to_target"]
+    out = {"target": target, "reference": fc["reference"],
+           "fast": {"spp": f, "seconds": f * npix / (fast_value * 1e6) if f else None, "curve": [fc["fast"]["spp"], fc["fast"]["rmse"]]},
+           "plain": {"spp": p, "seconds": p * npix / (plain_value * 1e6) if p else None,
+                     "curve": [fc["plain"]["spp"], fc["plain"]["rmse"]]}}
+    if f and p:
+        out["speedup_equal_rmse"] = out["plain"]["seconds"] / out["fast"]["seconds"]
     return out
 
 
@@ -368,6 +465,29 @@ def batched_reference_rate(scenes, views, seconds_target=12.0, steps=1):
     rate = sum(n.values()) / seconds
     sample = "first view of each volume, centre crop x 1 spp per step (%s), weighted by the volume's samples" % ", ".join(crops)
     return rate, kind, cores, sample
+
+
+def batched_work(scenes, views, settings_of, nthreads, spp=2, reference=False):
+    """Per-sample work counters of a batch: the oracle's counts on the first
+    view of each volume (whole field of view at 128^2, that volume's tracer
+    settings, or the reference estimator's), weighted by the samples of the
+    volume's views."""
+    import copy
+    first, n = {}, {}
+    for k, cam, s in views:
+        first.setdefault(k, cam)
+        n[k] = n.get(k, 0) + cam.film_size[0] * cam.film_size[1] * s
+    total = float(sum(n.values()))
+    out = {}
+    for k in sorted(first):
+        sc = copy.copy(reference_path(scenes[k]) if reference else scenes[k])
+        C = importlib.import_module("exposure-render_gb300.capi")
+        sc.tracer = C.er_tracer_desc.from_buffer_copy(sc.tracer)
+        sc.tracer.camera = first[k]
+        w = oracle_work(sc, sc.tracer.settings if reference else settings_of(k), nthreads, spp=spp)
+        for key, v in w.items():
+            out[key] = out.get(key, 0.0) + v * n[k] / total
+    return out
 
 
 def run_reference(args, wl, rank, world):
@@ -512,10 +632,18 @@ def run_ours(args, wl, rank, world, local_rank):
     if rank != 0:
         return
     conv = None
+    rmse_name = {"c1": "c1p"}.get(wl, wl)      # the FP64 view with the workload's shading
     if world == 1 and not args.no_rmse and wl in ("c1", "c2"):
-        conv = convergence(lib, runtime, torch, [wl], {
+        conv = convergence(lib, runtime, torch, [rmse_name], {
             "fast": {"free_flight": 1, "mis": 1, "stratify": 1, "majorant_brick": r.tracer_desc.settings.majorant_brick},
             "plain": {"free_flight": 0, "mis": 1, "stratify": 0}})
+    film_conv = None
+    if world == 1 and not args.no_rmse and wl in ("c1", "c2"):
+        film_conv = film_convergence(
+            lib, torch, r,
+            {"fast": {"free_flight": 1, "mis": 1, "stratify": 1}, "plain": {"free_flight": 0, "mis": 1, "stratify": 0}},
+            {"free_flight": 1, "mis": 1, "stratify": 0}, 8192 if wl == "c2" else 16384,
+            stream=ctypes.c_void_p(stream.cuda_stream))
     peaks, peak_kind = measured_peaks()
     nthreads = os.cpu_count() or 1
     # work per sample of the measured configuration (oracle, whole field of view at 128^2)
@@ -547,7 +675,10 @@ def run_ours(args, wl, rank, world, local_rank):
         "reference_work_per_sample": ref_work,
         "plain": {"value": plain, "unit": "Msamples/s", "speedup": value / plain,
                   "what": "same workload and estimator, the reference's fixed-step march for free flight and shadows"},
-        "time_to_rmse": rmse_summary(conv, wl, value, plain, width * height),
+        "time_to_rmse": film_rmse_summary(film_conv, value, plain, width * height),
+        "time_to_rmse_fp64_128": (dict(rmse_summary(conv, rmse_name, value, plain, width * height) or {},
+                                       note="samples per pixel to RMSE 1e-2 measured on a 128^2 view against the FP64 "
+                                            "oracle, times the workload's pixels") if conv else None),
         "reference_order": {"value": ref_order, "unit": "Msamples/s",
                             "what": "reference live path (march, BRDF, light sampling), bit-exact with the reference"},
     }
@@ -650,24 +781,29 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
         b.close()
     seq_value = samples_per_step / (ms_seq / 1e3) / 1e6
 
-    # plain: the reference estimator (fixed-step march, light sampling, BRDF),
-    # one frame of 1 spp per call (RenderEstimate), one view at a time
+    # plain: the single-view GPU path at its best - each view's full spp in
+    # one er_trace_sum_device call (the wavefront stages, as c2's plain path),
+    # one view at a time - with the same estimator except the reference's
+    # fixed-step march for free flight and shadows and no stratification
     plain_samples, plain_ms = 0, 0.0
-    n_plain = args.plain_views if args.plain_views is not None else (4 if wl == "c5" else 16)
-    for (k, cam, spp) in views[:n_plain]:
+    n_plain = args.plain_views if args.plain_views is not None else (2 if wl == "c5" else len(views))
+    plain_sum = torch.zeros((max(c.film_size[1] for _, c, _ in views), max(c.film_size[0] for _, c, _ in views), 4),
+                            dtype=torch.float32, device="cuda")
+    for i, (k, cam, spp) in enumerate(views[:n_plain]):
         r = rs[k]
         saved = C.er_tracer_desc.from_buffer_copy(r.tracer_desc)
         r.tracer_desc.camera = cam
         r.tracer_desc.settings.free_flight = 0
         r.tracer_desc.settings.stratify = 0
         r.rebind_tracer()
-        C.check(lib.er_reset_accumulation(r.tracer_id))
-        r.render_estimate()
-        torch.cuda.synchronize()
-        plain_ms += timed(r.render_estimate, 2)
-        plain_samples += 2 * cam.film_size[0] * cam.film_size[1]
+        if i == 0:
+            r.trace_sum_device(plain_sum.data_ptr(), 1, i, 0, 0, sp)      # warm-up
+            torch.cuda.synchronize()
+        plain_ms += timed(lambda: r.trace_sum_device(plain_sum.data_ptr(), spp, i, 0, 0, sp), 1)
+        plain_samples += spp * cam.film_size[0] * cam.film_size[1]
         ctypes.memmove(ctypes.byref(r.tracer_desc), ctypes.byref(saved), ctypes.sizeof(saved))
         r.rebind_tracer()
+    del plain_sum
     plain_value = plain_samples / (plain_ms / 1e3) / 1e6
 
     # equal-RMSE comparison on the first view of each volume (128^2, FP64 references)
@@ -713,6 +849,12 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
     # the reference transport on the host cores (rank 0 at N = 1 only)
     cpu = batched_reference_rate(scenes, views) if world == 1 else None
     vol_bytes = sum(sc.volume.nbytes for sc in scenes)
+    # roofline of the dominant stage of the profiled launch (one pass of the batch)
+    peaks, peak_kind = measured_peaks()
+    nthreads = os.cpu_count() or 1
+    work = batched_work(scenes, views, lambda k: rs[k].tracer_desc.settings, nthreads)
+    ref_work = batched_work(scenes, views, None, nthreads, spp=1, reference=True)
+    roofline, stages = stage_roofline(work, ref_work, stage_ms, stage_launches, samples_per_step, peaks, peak_kind, wl)
     line = {
         "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -732,12 +874,14 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
                 "d2h_bytes_per_step": d2h_bytes},
         "clocks": clk.summary(),
         "gpu_launches": args.steps * (4 * info["windows"]),
-        "stages": {n: {"ms": float(stage_ms[i]), "share": float(stage_ms[i] / max(stage_ms.sum(), 1e-9)),
-                       "launches": int(stage_launches[i])} for i, n in enumerate(("primary", "shade", "shadow", "reduce"))},
+        "roofline": roofline,
+        "stages": stages,
+        "work_per_sample": work,
         "profiled_pass_ms": prof_ms,
         "one_batch_per_view": {"value": seq_value, "unit": "Msamples/s", "speedup": value / seq_value},
         "plain": {"value": plain_value, "unit": "Msamples/s", "speedup": value / plain_value, "views": n_plain,
-                  "what": "reference estimator (march, light sampling, BRDF), 1 spp per RenderEstimate, one view at a time"},
+                  "what": "same estimator with the fixed-step march and no stratification, each view's full spp in one "
+                          "er_trace_sum_device call, one view at a time"},
         "equal_rmse": batched_rmse_summary(conv, value, plain_value) if wl == "c3" else
         {"throughput_ratio": value / plain_value, "note": "no FP64 reference of the c5 volume: samples-to-RMSE ratios are measured on c2 and c3"},
     }
@@ -907,7 +1051,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3", "c4", "c5"])
     ap.add_argument("--views", type=int, default=0, help="c3/c5: number of views (0: 64 for c3, 16 for c5)")
-    ap.add_argument("--plain-views", type=int, default=None, help="c3/c5: views timed on the plain one-view path (16 / 4)")
+    ap.add_argument("--plain-views", type=int, default=None, help="c3/c5: views timed on the plain one-view path (all / 2)")
     ap.add_argument("--film", type=int, default=0, help="square film edge (smaller profiling cases; 0 = the workload's)")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel (0 = the workload's)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default settings)")

@@ -96,6 +96,14 @@ struct Bitmap {              /* Bitmap (Source/bitmap.h): RGBA8, row-major */
     int res[2];
 };
 
+struct Clip {                /* ErClippingObject (Source/erclippingobject.h:27-58): Shape + Invert */
+    float inv_tm[3][4];
+    int type;
+    float size[3];
+    float outer_radius;
+    int invert;
+};
+
 struct Params {
     /* volume (Source/volume.h:140-149) */
     const uint16_t* vox;
@@ -149,6 +157,13 @@ struct Params {
     int n_bitmaps;
     const Tfs* tfs;
     int* err;                /* device error word (bit 0: a march exceeded its step budget) */
+    /* clipping objects: the tracer's ClippingObjectIDs resolved to their shapes */
+    int clip_count;
+    const Clip* clips;
+    /* 1 for a volume bound without NormalizeSize: Volume's copy scales the
+       spacing by 0 (Source/volume.h:106-117), so its box has no extent and
+       no ray meets the volume */
+    int box_empty;
 };
 
 /* ------------------------------------------------------------------ */

@@ -130,7 +130,7 @@ ER_D void dm_scatter(const DmParams& M, const DmLookup<float>& k, const DmTf<flo
 ER_D bool dm_segment(const Params& P, const Ray& R, float& t0, float& t1)
 {
     Isect Int; Int.invalid();
-    intersect_box(R, vload(P.minp), vload(P.half_size), Int, false);
+    intersect_volume(P, R, Int);
     if (!Int.valid) return false;
     t0 = smax(Int.near_t, R.MinT);
     t1 = smin(Int.far_t, R.MaxT);

@@ -305,6 +305,59 @@ ER_D void intersect_box(const Ray& R, v3 mn, v3 mx, Isect& I, bool full)
     }
 }
 
+/* The volume's bounding box (Source/raymarching.h:32-36 and :75-79 intersect
+   it first).  A volume bound without NormalizeSize has no extent
+   (Source/volume.h:106-117 scales its spacing by 0): no ray meets it. */
+ER_D void intersect_volume(const Params& P, const Ray& R, Isect& I)
+{
+    if (P.box_empty) return;
+    intersect_box(R, vload(P.minp), vload(P.half_size), I, false);
+}
+
+/* Clipping objects (ErClippingObject, Source/erclippingobject.h:27-58: a
+   Shape and Invert; bound by BindClippingObject, Source/core.cu:96-104, and
+   listed in the tracer's ClippingObjectIDs, Source/ertracer.h:100-116).  The
+   reference binds them but no transport code reads them; here a point of the
+   volume is clipped - its extinction counts as zero in free flight and in
+   shadow rays - when it lies inside a clipping object's shape, or outside it
+   when Invert is set; with several objects, any one of them clips.  Inside
+   is tested in the shape's local frame (InvTM) with the reference's
+   predicates: InsidePlane z > 0 (Source/plane.h:90-93; also for disks and
+   rings, which have no predicate of their own), InsideBox open slabs of
+   Size (Source/box.h:116-120), InsideSphere Length < OuterRadius
+   (Source/sphere.h:147-150), InsideCylinder radial distance in x/z below
+   OuterRadius and |y| below half of Size[2] (Source/cylinder.h:96-99, with
+   the height Shape::Update uses, Source/shape.h:100). */
+ER_D bool clipped(const Params& P, v3 p)
+{
+    for (int i = 0; i < P.clip_count; i++) {
+        const Clip& c = P.clips[i];
+        const v3 q = xform_point(c.inv_tm, p);
+        bool in;
+        switch (c.type) {
+        case 0: case 1: case 2: in = q.z > 0.0f; break;
+        case 3: {
+            const float h0 = 0.5f * c.size[0], h1 = 0.5f * c.size[1], h2 = 0.5f * c.size[2];
+            in = q.x > -h0 && q.x < h0 && q.y > -h1 && q.y < h1 && q.z > -h2 && q.z < h2;
+            break;
+        }
+        case 4: in = vlen(q) < c.outer_radius; break;
+        case 5: in = sqrtf((q.x * q.x) + (q.z * q.z)) < c.outer_radius && fabsf(q.y) < (0.5f * c.size[2]); break;
+        default: in = false; break;
+        }
+        if (in != (c.invert != 0)) return true;
+    }
+    return false;
+}
+
+/* DensityScale * Opacity1D(I(p)) at a point of a free-flight or shadow
+   march, zero where a clipping object removes the volume (no lookup) */
+ER_D float sigma_point(const Params& P, v3 p)
+{
+    if (P.clip_count > 0 && clipped(P, p)) return 0.0f;
+    return sigma_at(P, get_intensity(P, p));
+}
+
 /* IntersectPlane(R, OneSided, Int) - Source/plane.h:41-62 */
 ER_D void intersect_plane_inf(const Ray& R, int one_sided, Isect& I)
 {
@@ -699,7 +752,7 @@ template <bool WITH_NORMAL = true>
 ER_D void sample_volume(const Params& P, const Ray& R, Rng& rng, Event& SE)
 {
     Isect Int; Int.invalid();
-    intersect_box(R, vload(P.minp), vload(P.half_size), Int, false);
+    intersect_volume(P, R, Int);
     if (!Int.valid) return;
     float MinT = smax(Int.near_t, R.MinT);
     const float MaxT = smin(Int.far_t, R.MaxT);
@@ -713,8 +766,7 @@ ER_D void sample_volume(const Params& P, const Ray& R, Rng& rng, Event& SE)
         Ps = vadd(R.O, vscale(R.D, MinT));
         if (MinT >= MaxT) return;
         if (--budget < 0) { atomicOr(P.err, 1); return; }
-        const float I = get_intensity(P, Ps);
-        const float SigmaT = sigma_at(P, I);
+        const float SigmaT = sigma_point(P, Ps);
         Sum += SigmaT * StepSize;
         MinT += StepSize;
     }
@@ -730,7 +782,7 @@ ER_D void sample_volume(const Params& P, const Ray& R, Rng& rng, Event& SE)
 ER_D bool scatter_event_in_volume(const Params& P, const Ray& R, Rng& rng)
 {
     Isect Int; Int.invalid();
-    intersect_box(R, vload(P.minp), vload(P.half_size), Int, false);
+    intersect_volume(P, R, Int);
     if (!Int.valid) return false;
     float MinT = smax(Int.near_t, R.MinT);
     const float MaxT = smin(Int.far_t, R.MaxT);
@@ -743,8 +795,7 @@ ER_D bool scatter_event_in_volume(const Params& P, const Ray& R, Rng& rng)
         const v3 Ps = vadd(R.O, vscale(R.D, MinT));
         if (MinT > MaxT) return false;
         if (--budget < 0) { atomicOr(P.err, 1); return false; }
-        const float I = get_intensity(P, Ps);
-        Sum += sigma_at(P, I) * StepSize;
+        Sum += sigma_point(P, Ps) * StepSize;
         MinT += StepSize;
     }
     return true;
@@ -952,7 +1003,7 @@ template <bool WITH_NORMAL = true, bool SKIP = true>
 ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE, float u0 = -1.0f)
 {
     Isect Int; Int.invalid();
-    intersect_box(R, vload(P.minp), vload(P.half_size), Int, false);
+    intersect_volume(P, R, Int);
     if (!Int.valid) return;
     const float t0 = smax(Int.near_t, R.MinT);
     const float t1 = smin(Int.far_t, R.MaxT);
@@ -976,7 +1027,7 @@ ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE
                 }
                 t = t + dt;
                 const v3 Pt = vadd(R.O, vscale(R.D, t));
-                const float sig = P.density_scale * sigma_at(P, get_intensity(P, Pt));
+                const float sig = P.density_scale * sigma_point(P, Pt);
                 if (rng.get1() * mu < sig) {
                     SE.valid = true;
                     SE.T = t;
@@ -1014,7 +1065,7 @@ ER_D void delta_begin(const Params& P, const Ray& R, Rng& rng, DeltaTracker& k, 
     k.done = true;
     k.hit = false;
     Isect Int; Int.invalid();
-    intersect_box(R, vload(P.minp), vload(P.half_size), Int, false);
+    intersect_volume(P, R, Int);
     if (!Int.valid) return;
     const float t0 = smax(Int.near_t, R.MinT);
     const float t1 = smin(Int.far_t, R.MaxT);
@@ -1041,7 +1092,7 @@ ER_D void delta_step(const Params& P, const Ray& R, Rng& rng, DeltaTracker& k)
         if (k.t + dt < k.e) {
             k.t = k.t + dt;
             const v3 Pt = vadd(R.O, vscale(R.D, k.t));
-            const float sig = P.density_scale * sigma_at(P, get_intensity(P, Pt));
+            const float sig = P.density_scale * sigma_point(P, Pt);
             if (rng.get1() * k.mu < sig) { k.hit = true; k.done = true; return; }
             if (++k.guard > ER_DELTA_MAX_COLLISIONS) { atomicOr(P.err, 2); k.done = true; return; }
             k.tau = -er_logf(rng.get1());
@@ -1080,7 +1131,7 @@ ER_D void ratio_begin(const Params& P, const Ray& R, Rng& rng, RatioTracker& k)
     k.Tr = 1.0f;
     k.done = true;
     Isect Int; Int.invalid();
-    intersect_box(R, vload(P.minp), vload(P.half_size), Int, false);
+    intersect_volume(P, R, Int);
     if (!Int.valid) return;
     const float t0 = smax(Int.near_t, R.MinT);
     const float t1 = smin(Int.far_t, R.MaxT);
@@ -1106,7 +1157,7 @@ ER_D void ratio_step(const Params& P, const Ray& R, Rng& rng, RatioTracker& k)
         if (k.t + dt < k.e) {
             k.t = k.t + dt;
             const v3 Pt = vadd(R.O, vscale(R.D, k.t));
-            const float sig = P.density_scale * sigma_at(P, get_intensity(P, Pt));
+            const float sig = P.density_scale * sigma_point(P, Pt);
             k.Tr = k.Tr * (1.0f - sig / k.mu);
             if (k.Tr <= 0.0f) { k.Tr = 0.0f; k.done = true; return; }
             if (k.Tr < 0.1f) {
@@ -1136,7 +1187,7 @@ template <bool SKIP = true>
 ER_D float transmittance_ratio(const Params& P, const Ray& R, Rng& rng)
 {
     Isect Int; Int.invalid();
-    intersect_box(R, vload(P.minp), vload(P.half_size), Int, false);
+    intersect_volume(P, R, Int);
     if (!Int.valid) return 1.0f;
     const float t0 = smax(Int.near_t, R.MinT);
     const float t1 = smin(Int.far_t, R.MaxT);
@@ -1160,7 +1211,7 @@ ER_D float transmittance_ratio(const Params& P, const Ray& R, Rng& rng)
                 }
                 t = t + dt;
                 const v3 Pt = vadd(R.O, vscale(R.D, t));
-                const float sig = P.density_scale * sigma_at(P, get_intensity(P, Pt));
+                const float sig = P.density_scale * sigma_point(P, Pt);
                 Tr = Tr * (1.0f - sig / mu);
                 if (Tr <= 0.0f) return 0.0f;
                 if (Tr < 0.1f) {

@@ -164,6 +164,7 @@ struct VolumeItem {
     int normalize;
     uint16_t vmax = 0;
     uint64_t signature = 0;        /* sampled content hash (tuning cache key) */
+    uint64_t edits = 0;            /* region edits from device voxels (folded into the signature) */
     DevBuf<uint16_t> vox;
     DevBuf<uint2> quad;            /* corner quads (NULL when they do not fit in memory) */
     DevBuf<unsigned int> gm_max_bits;
@@ -188,6 +189,7 @@ struct TracerItem {
     DevBuf<erd::Plf> opacity;
     DevBuf<erd::Light> lights;
     DevBuf<erd::Object> objects;
+    DevBuf<erd::Clip> clips;
     DevBuf<erd::Bitmap> bitmaps;
     DevBuf<int> light_valid;
     DevBuf<erd::Texture> textures;
@@ -457,8 +459,10 @@ er_status build(TracerItem& t)
         return fail(ER_ERR_INVALID_ARGUMENT, "mis %d is not an ER_MIS_* value", d.settings.mis);
     const int brick = d.settings.majorant_brick > 0 ? d.settings.majorant_brick : 8;
     if (brick > 64) return fail(ER_ERR_INVALID_ARGUMENT, "majorant_brick %d out of range [1, 64]", brick);
+    /* a volume bound without NormalizeSize has an empty box: no scatter
+       event reads the gradient-magnitude range */
     const bool needs_gm = d.settings.apply_shading_type && d.settings.shading_type >= ER_SHADING_HYBRID &&
-                          d.settings.shading_type <= ER_SHADING_THRESHOLD;
+                          d.settings.shading_type <= ER_SHADING_THRESHOLD && v.normalize;
     if (needs_gm && v.gm_max < 0.0f) {
         /* GradientMagnitudeRange of the shader switch: maximum voxel-centre
            gradient magnitude (Source/gradientmagnitude.cuh:46-71) */
@@ -619,6 +623,30 @@ er_status build(TracerItem& t)
         ER_CUDA(cudaMemcpyAsync(t.objects.p, O.data(), O.size() * sizeof(erd::Object), cudaMemcpyHostToDevice, st));
         P.objects = t.objects.p;
     }
+    /* clipping objects named by ClippingObjectIDs (Source/ertracer.h:100-116);
+       IDs that name no bound clipping object are skipped */
+    std::vector<erd::Clip> K;
+    const int cc = std::min(std::max(d.clipping_object_count, 0), ER_MAX_INDICES);
+    for (int i = 0; i < cc; i++) {
+        auto it = C.clipping.items.find(d.clipping_object_ids[i]);
+        if (d.clipping_object_ids[i] < 0 || it == C.clipping.items.end()) continue;
+        erd::Clip k;
+        memset(&k, 0, sizeof(k));
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 4; c++) k.inv_tm[r][c] = it->second->shape.inv_tm[r][c];
+        k.type = it->second->shape.type;
+        for (int c = 0; c < 3; c++) k.size[c] = it->second->shape.size[c];
+        k.outer_radius = it->second->shape.outer_radius;
+        k.invert = it->second->invert ? 1 : 0;
+        K.push_back(k);
+    }
+    P.clip_count = (int)K.size();
+    if (!K.empty()) {
+        ER_CUDA(t.clips.ensure(K.size()));
+        ER_CUDA(cudaMemcpyAsync(t.clips.p, K.data(), K.size() * sizeof(erd::Clip), cudaMemcpyHostToDevice, st));
+        P.clips = t.clips.p;
+    }
+    P.box_empty = v.normalize ? 0 : 1;
     /* textures indexed by texture ID; unbound IDs evaluate to black */
     const int ntex = max_tex + 1;
     std::vector<erd::Texture> T((size_t)std::max(ntex, 1));
@@ -1111,8 +1139,9 @@ ER_API er_status er_bind_volume(const er_volume_desc* d, int32_t* id)
     for (int i = 0; i < 3; i++)
         if (!(d->spacing[i] > 0.0f) || !std::isfinite(d->spacing[i]))
             return fail(ER_ERR_INVALID_ARGUMENT, "volume spacing must be finite and positive");
-    if (!d->normalize_size)
-        return fail(ER_ERR_INVALID_ARGUMENT, "normalize_size = 0 collapses the volume to zero size (Source/volume.h:106-117 leaves Scale = 0)");
+    /* normalize_size = 0 is accepted: as in the reference, Volume's copy then
+       scales the spacing by 0 (Source/volume.h:106-117), the volume has no
+       extent and renders show only the lights and objects (box_empty) */
     Context& C = ctx();
     bool is_new = false;
     er_status st = reserve_id(C.volumes, id, &is_new);
@@ -1175,8 +1204,18 @@ static er_status update_volume_region(int32_t id, const int32_t* offset, const i
     if (us != ER_OK) return us;
     if (bmax > v.vmax) v.vmax = (uint16_t)bmax;
     v.gm_max = -1.0f;
+    /* tuning-cache signature: the edit's box, its contents (every 61st of
+       the host voxels, as er_bind_volume samples a whole volume) and, for
+       device voxels the host cannot read, the volume's edit count */
     v.signature = fnv1a(v.signature, offset, 3 * sizeof(int32_t));
     v.signature = fnv1a(v.signature, size, 3 * sizeof(int32_t));
+    const size_t n = (size_t)size[0] * size[1] * size[2];
+    if (kind == cudaMemcpyHostToDevice) {
+        for (size_t i = 0; i < n; i += 61) v.signature = fnv1a(v.signature, &voxels[i], sizeof(uint16_t));
+    } else {
+        v.edits++;
+        v.signature = fnv1a(v.signature, &v.edits, sizeof(v.edits));
+    }
     C.version++;
     return ER_OK;
 }

@@ -237,8 +237,11 @@ cudaError_t er_launch_box_quads_max(const uint16_t* vox, const int res[3], const
  * Set-up: the first call on a device, with that device current, resolves the
  * arrays' device addresses with cudaGetSymbolAddress (the host-side names of
  * __device__ arrays are not device addresses).  Make that first call before
- * any stream capture.
+ * any stream capture.  The addresses belong to the device's current context;
+ * when that context is replaced (cudaDeviceReset, then new work), the next
+ * call sees a new context ID and resolves them again.
  */
+#include <cuda.h>
 #include <mutex>
 
 #define ER_NOALLOC_MAX_BRICKS (1u << 20)
@@ -253,6 +256,7 @@ namespace {
 struct NoallocScratch {
     uint32_t* minmax;
     float* rmq;
+    unsigned long long ctx_id;     /* context the addresses belong to (0: unknown) */
     bool ready;
 };
 
@@ -260,20 +264,62 @@ struct NoallocScratch {
 std::mutex g_noalloc_mutex;
 NoallocScratch g_noalloc[ER_NOALLOC_MAX_DEVICES];
 
-/* device addresses of the scratch arrays on the current device (set up once) */
+/* The driver's cuCtxGetCurrent and cuCtxGetId, looked up through the runtime
+   (the library does not link libcuda).  A context's ID is unique for the
+   life of the process, so a device whose context was destroyed and made
+   again (cudaDeviceReset) shows a new ID, and the arrays' addresses, which
+   belong to the module loaded into the old context, are resolved again. */
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+bool g_ctx_fns_looked_up = false;
+
+/* ID of the current context, 0 when it cannot be read */
+unsigned long long current_context_id()
+{
+    if (!g_ctx_fns_looked_up) {
+        g_ctx_fns_looked_up = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_get_current = (CtxGetCurrentFn)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_get_id = (CtxGetIdFn)f;
+        cudaGetLastError();
+    }
+    if (!g_ctx_get_current || !g_ctx_get_id) return 0;
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_get_current(&c) != CUDA_SUCCESS || !c) return 0;
+    if (g_ctx_get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+/* device addresses of the scratch arrays in the current device's context:
+   resolved once per context (the first call on a device, and again after
+   its context was replaced); every call when the context ID cannot be read */
 cudaError_t noalloc_scratch(int device, NoallocScratch* out)
 {
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     NoallocScratch& s = g_noalloc[device];
-    if (!s.ready) {
+    const unsigned long long id = current_context_id();
+    if (!s.ready || id == 0 || id != s.ctx_id) {
         void* a = nullptr;
         void* b = nullptr;
+        s.ready = false;
         cudaError_t e = cudaGetSymbolAddress(&a, g_noalloc_minmax);
         if (e != cudaSuccess) return e;
         e = cudaGetSymbolAddress(&b, g_noalloc_rmq);
         if (e != cudaSuccess) return e;
         s.minmax = (uint32_t*)a;
         s.rmq = (float*)b;
+        /* the first runtime call above makes the primary context current
+           when nothing had: read the ID again */
+        s.ctx_id = id ? id : current_context_id();
         s.ready = true;
     }
     *out = s;

@@ -61,6 +61,13 @@ class Renderer:
             i = c_int32(-1)
             C.check(self.lib.er_bind_object(byref(oc), byref(i)))
             self.object_ids.append(i.value)
+        # BindClippingObject (Source/exposurerender.h:36): clipping object i of
+        # the scene; the tracer's clipping_object_ids index this list
+        self.clipping_ids = []
+        for k in getattr(scene, "clipping_objects", []):
+            i = c_int32(-1)
+            C.check(self.lib.er_bind_clipping_object(byref(k), byref(i)))
+            self.clipping_ids.append(i.value)
         vd = scene.volume_desc()
         vid = c_int32(-1)
         C.check(self.lib.er_bind_volume(byref(vd), byref(vid)))
@@ -74,6 +81,9 @@ class Renderer:
         for k in range(t.object_count):
             src = scene.tracer.object_ids[k]
             t.object_ids[k] = self.object_ids[src] if 0 <= src < len(self.object_ids) else -1
+        for k in range(max(0, min(t.clipping_object_count, C.ER_MAX_INDICES))):
+            src = scene.tracer.clipping_object_ids[k]
+            t.clipping_object_ids[k] = self.clipping_ids[src] if 0 <= src < len(self.clipping_ids) else -1
         self.tracer_desc = t
         tid = c_int32(-1)
         C.check(self.lib.er_bind_tracer(byref(t), byref(tid)))
@@ -158,7 +168,9 @@ class Renderer:
             lib.er_unbind_texture(i)
         for i in self.bitmap_ids:
             lib.er_unbind_bitmap(i)
-        self.bitmap_ids = []
+        for i in getattr(self, "clipping_ids", []):
+            lib.er_unbind_clipping_object(i)
+        self.bitmap_ids, self.clipping_ids = [], []
         self.light_ids, self.texture_ids, self.object_ids = [], [], []
 
 

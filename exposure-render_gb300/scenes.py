@@ -38,6 +38,7 @@ class Scene:
     spp: int = 1
     objects: list = field(default_factory=list)     # er_object_desc, object i has ID i
     bitmaps: list = field(default_factory=list)     # uint8 (H, W, 4) RGBA arrays, bitmap i has ID i
+    clipping_objects: list = field(default_factory=list)   # er_clipping_object_desc, clipping object i has ID i
 
     @property
     def width(self) -> int:
@@ -442,13 +443,17 @@ def density_subblock(volume, size=256, lo=800.0, hi=3000.0) -> np.ndarray:
 
 def rmse_views(film=128, names=None) -> list:
     """(name, Scene) of the views whose converged images the FP64 oracle
-    provides: the c1 scene, the first view of each c3 volume, and c2 - all
-    at a film of `film`^2 with each workload's camera and settings.  `names`
-    restricts the list (and the volumes generated)."""
-    want = set(names) if names else {"c1", "c3v0", "c3v1", "c3v2", "c2"}
+    provides: the c1 scene with the BRDF at every volume event (the
+    reference's live shading) and with the isotropic phase function (c1p,
+    the c1 workload's shading), the first view of each c3 volume, and c2 -
+    all at a film of `film`^2 with each workload's camera and settings.
+    `names` restricts the list (and the volumes generated)."""
+    want = set(names) if names else {"c1", "c1p", "c3v0", "c3v1", "c3v2", "c2"}
     out = []
     if "c1" in want:
         out.append(("c1", scene_c1(res=128, film=(film, film))))
+    if "c1p" in want:
+        out.append(("c1p", scene_c1(res=128, film=(film, film), phase=True)))
     c3 = [k for k in range(3) if f"c3v{k}" in want]
     if c3:
         views = c3_views()
@@ -596,3 +601,47 @@ def scene_bitmaps(res=32, film=(48, 40), spp=4, seed=3) -> Scene:
     sc.objects[1].specular_texture_id = 5
     sc.lights[0].texture_id = 4
     return sc
+
+
+# ---------------------------------------------------------------------------
+# clipping objects (ErClippingObject: a shape that removes part of the volume)
+# ---------------------------------------------------------------------------
+
+def make_clipping_object(shape, invert=0) -> C.er_clipping_object_desc:
+    k = C.er_clipping_object_desc()
+    k.shape = shape
+    k.invert = invert
+    return k
+
+
+def scene_clipped(res=32, film=(48, 40), spp=4, seed=3) -> Scene:
+    """The tiny blob scene cut by three clipping objects: a tilted plane
+    (the half-space on its +z side is removed), a sphere with Invert set
+    (only the volume inside it is kept) and a box that removes a corner."""
+    sc = scene_tiny(res=res, film=film, spp=spp, seed=seed)
+    plane = make_shape(C.SHAPE_PLANE, look_at_tm((0.05, 0.0, 0.1), (0.35, 0.2, 1.1), (0.0, 1.0, 0.0)), size=(1.0, 1.0, 0.0))
+    ball = make_shape(C.SHAPE_SPHERE, look_at_tm((0.0, 0.05, -0.05), (0.0, 0.05, 0.95), (0.0, 1.0, 0.0)), outer=0.42)
+    box = make_shape(C.SHAPE_BOX, look_at_tm((-0.3, -0.25, -0.3), (0.2, 0.25, 0.7), (0.0, 0.0, 1.0)), size=(0.35, 0.3, 0.4))
+    sc.clipping_objects = [make_clipping_object(plane), make_clipping_object(ball, invert=1), make_clipping_object(box)]
+    sc.tracer.clipping_object_count = 3
+    for i in range(3):
+        sc.tracer.clipping_object_ids[i] = i
+    return sc
+
+
+def lattice_volume(shape_zyx, period=96.0, seed=13, noise=40.0) -> np.ndarray:
+    """A volume filled everywhere: 1200 + 900 sin(2 pi x / p) sin(2 pi y / p)
+    sin(2 pi z / p) plus uniform noise in [0, noise), uint16, x fastest (the
+    large-index tests need voxels that matter in every slice).  Built slab by
+    slab in float32."""
+    Z, Y, X = shape_zyx
+    rng = np.random.default_rng(seed)
+    sx = np.sin(2.0 * np.pi * np.arange(X, dtype=np.float32) / np.float32(period)).astype(np.float32)
+    sy = np.sin(2.0 * np.pi * np.arange(Y, dtype=np.float32) / np.float32(period)).astype(np.float32)
+    sxy = (sy[:, None] * sx[None, :]) * np.float32(900.0)
+    out = np.empty((Z, Y, X), dtype=np.uint16)
+    for z in range(Z):
+        sz = np.float32(np.sin(2.0 * np.pi * z / period))
+        v = np.float32(1200.0) + sxy * sz + rng.random(size=(Y, X), dtype=np.float32) * np.float32(noise)
+        out[z] = v.astype(np.uint16)
+    return out

@@ -585,8 +585,10 @@ ER_API er_status er_build_majorant_device(const uint16_t* d_voxels, const int32_
    in static device arrays sized for at most 2^20 bricks and 65536 sigma
    entries (8.25 MiB per GPU, held until exit); larger inputs are rejected
    with ER_ERR_INVALID_ARGUMENT.  The first call on a device resolves the
-   arrays' addresses (make it before any stream capture); calls that overlap
-   on the GPU share the arrays and race.  No counterpart in the reference. */
+   arrays' addresses (make it before any stream capture), and the first call
+   after the device's context was replaced (cudaDeviceReset) resolves them
+   again; calls that overlap on the GPU share the arrays and race.  No
+   counterpart in the reference. */
 ER_API er_status er_build_majorant_device_noalloc(const uint16_t* d_voxels, const int32_t resolution[3], int32_t brick,
                                                   const float* d_sigma, int32_t sigma_count, float density_scale, float* d_majorant,
                                                   void* stream);

@@ -151,6 +151,12 @@ struct or_scene {
     int n_bitmaps;
     int* bitmap_res;            /* 2 per bitmap */
     uint8_t** bitmap_pixels;
+    /* clipping objects named by the tracer's ClippingObjectIDs, resolved
+       (scene_set_clipping_objects) */
+    int n_clips;
+    er_clipping_object_desc* clips;
+    int clip_ids_count;
+    int clip_ids[ER_MAX_INDICES];
     /* the stratified first free-flight draw of the current sample, or < 0 */
     float tau_u;
     /* statistics */
@@ -180,6 +186,7 @@ struct or_scene {
 static double g_lookups_per_sample = 0.0;
 static double g_stats[OR_NSTATS];
 static void prepare_extensions(or_scene* s);
+static int clipped(const or_scene* s, v3 p);
 
 /* Shape::Update (Source/shape.h:92-103) with the area helpers :27-55 */
 static float shape_area(const er_shape* s)
@@ -256,6 +263,8 @@ or_scene* ER_OR(scene_create)(const er_tracer_desc* t, const er_volume_desc* vol
     s->object_count = t->object_count > 0 ? t->object_count : 0;
     s->tau_u = -1.0f;
     for (int i = 0; i < ER_MAX_INDICES; i++) s->light_idx[i] = t->light_ids[i];
+    s->clip_ids_count = t->clipping_object_count < 0 ? 0 : (t->clipping_object_count > ER_MAX_INDICES ? ER_MAX_INDICES : t->clipping_object_count);
+    for (int i = 0; i < ER_MAX_INDICES; i++) s->clip_ids[i] = t->clipping_object_ids[i];
 
     s->n_lights = n_lights;
     s->lights = (or_light*)calloc(n_lights > 0 ? (size_t)n_lights : 1u, sizeof(or_light));
@@ -276,6 +285,7 @@ void ER_OR(scene_destroy)(or_scene* s)
     free(s->lights);
     free(s->textures);
     free(s->objects);
+    free(s->clips);
     for (int i = 0; i < s->n_bitmaps; i++) free(s->bitmap_pixels[i]);
     free(s->bitmap_pixels);
     free(s->bitmap_res);
@@ -1028,8 +1038,7 @@ static void sample_volume(or_scene* s, ray_t R, rng_t* rng, scatter_event* SE)
     while (Sum < S) {
         Ps = vadd(R.O, vscale(R.D, MinT));
         if (MinT >= MaxT) return;
-        const float I = get_intensity(s, Ps);
-        const float SigmaT = s->st.density_scale * plf_eval(&s->opacity, I);
+        const float SigmaT = (s->n_clips && clipped(s, Ps)) ? 0.0f : s->st.density_scale * plf_eval(&s->opacity, get_intensity(s, Ps));
         Sum += SigmaT * StepSize;
         MinT += StepSize;
     }
@@ -1057,8 +1066,7 @@ static int scatter_event_in_volume(or_scene* s, ray_t R, rng_t* rng)
     while (Sum < S) {
         const v3 Ps = vadd(R.O, vscale(R.D, MinT));
         if (MinT > MaxT) return 0;
-        const float I = get_intensity(s, Ps);
-        const float SigmaT = s->st.density_scale * plf_eval(&s->opacity, I);
+        const float SigmaT = (s->n_clips && clipped(s, Ps)) ? 0.0f : s->st.density_scale * plf_eval(&s->opacity, get_intensity(s, Ps));
         Sum += SigmaT * StepSize;
         MinT += StepSize;
     }
@@ -1188,6 +1196,58 @@ void ER_OR(scene_set_objects)(or_scene* s, const er_object_desc* objects, int32_
     }
 }
 
+/* BindClippingObject for the scene: clipping object i of `clips` has ID i;
+   the tracer's ClippingObjectIDs (Source/ertracer.h:100-116) name the ones
+   applied, IDs without a clipping object are skipped */
+void ER_OR(scene_set_clipping_objects)(or_scene* s, const er_clipping_object_desc* clips, int32_t n)
+{
+    free(s->clips);
+    s->clips = NULL;
+    s->n_clips = 0;
+    if (n <= 0) return;
+    s->clips = (er_clipping_object_desc*)malloc(sizeof(er_clipping_object_desc) * (size_t)ER_MAX_INDICES);
+    for (int i = 0; i < s->clip_ids_count; i++) {
+        const int id = s->clip_ids[i];
+        if (id < 0 || id >= n) continue;
+        s->clips[s->n_clips++] = clips[id];
+    }
+}
+
+/* Clipping objects: ErClippingObject is a Shape and Invert
+   (Source/erclippingobject.h:27-58), bound (Source/core.cu:96-104) but read
+   by no transport code of the reference.  Here a point of the volume is
+   clipped - its extinction counts as zero in free flight and shadow rays,
+   and no lookup is made - when it lies inside a clipping object's shape
+   (outside it when Invert is set); any one object clips.  Inside is tested
+   in the shape's local frame (InvTM) with the reference's predicates:
+   InsidePlane (Source/plane.h:90-93, also for disks and rings), InsideBox
+   (Source/box.h:116-120), InsideSphere (Source/sphere.h:147-150) and
+   InsideCylinder (Source/cylinder.h:96-99) with radius OuterRadius and
+   height Size[2] (the height Shape::Update uses, Source/shape.h:100). */
+static int clipped(const or_scene* s, v3 p)
+{
+    for (int i = 0; i < s->n_clips; i++) {
+        const er_clipping_object_desc* c = &s->clips[i];
+        const v3 q = xform_point(c->shape.inv_tm, p);
+        int in;
+        switch (c->shape.type) {
+        case ER_SHAPE_PLANE: case ER_SHAPE_DISK: case ER_SHAPE_RING: in = q.z > 0.0f; break;
+        case ER_SHAPE_BOX: {
+            const float h0 = 0.5f * c->shape.size[0], h1 = 0.5f * c->shape.size[1], h2 = 0.5f * c->shape.size[2];
+            in = q.x > -h0 && q.x < h0 && q.y > -h1 && q.y < h1 && q.z > -h2 && q.z < h2;
+            break;
+        }
+        case ER_SHAPE_SPHERE: in = vlen(q) < c->shape.outer_radius; break;
+        case ER_SHAPE_CYLINDER:
+            in = sqrtf((q.x * q.x) + (q.z * q.z)) < c->shape.outer_radius && fabsf(q.y) < (0.5f * c->shape.size[2]);
+            break;
+        default: in = 0; break;
+        }
+        if (in != (c->invert != 0)) return 1;
+    }
+    return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* extension estimators (settings fields apply_shading_type, mis,        */
 /* free_flight of er_capi.h).  The reference has no live code for these; */
@@ -1293,7 +1353,7 @@ static void sample_volume_delta(or_scene* s, ray_t R, rng_t* rng, scatter_event*
                 }
                 t = t + dt;
                 const v3 P = vadd(R.O, vscale(R.D, t));
-                const float sig = s->st.density_scale * sigma_lookup(s, get_intensity(s, P));
+                const float sig = (s->n_clips && clipped(s, P)) ? 0.0f : s->st.density_scale * sigma_lookup(s, get_intensity(s, P));
                 if (rng_get1(rng) * mu < sig) {
                     SE->valid = 1;
                     SE->T = t;
@@ -1340,7 +1400,7 @@ static float transmittance_ratio(or_scene* s, ray_t R, rng_t* rng)
                 }
                 t = t + dt;
                 const v3 P = vadd(R.O, vscale(R.D, t));
-                const float sig = s->st.density_scale * sigma_lookup(s, get_intensity(s, P));
+                const float sig = (s->n_clips && clipped(s, P)) ? 0.0f : s->st.density_scale * sigma_lookup(s, get_intensity(s, P));
                 Tr = Tr * (1.0f - sig / mu);
                 if (Tr <= 0.0f) return 0.0f;
                 if (Tr < 0.1f) {

@@ -49,6 +49,9 @@ void ER_OR(scene_destroy)(or_scene* scene);
 /* BindObject for the scene: object i of `objects` is the i-th bound object
    (gpObjects[i]); the tracer's object_count says how many are intersected */
 void ER_OR(scene_set_objects)(or_scene* scene, const er_object_desc* objects, int32_t n);
+/* BindClippingObject for the scene: clipping object i has ID i; the
+   tracer's clipping_object_ids name the ones applied to the volume */
+void ER_OR(scene_set_clipping_objects)(or_scene* scene, const er_clipping_object_desc* clips, int32_t n);
 /* BindBitmap for the scene: bitmap i is gpBitmaps[i] (ErTexture::BitmapID) */
 void ER_OR(scene_set_bitmaps)(or_scene* scene, const er_bitmap_desc* bitmaps, int32_t n);
 

@@ -42,6 +42,7 @@ class Oracle:
         f("scene_set_bitmaps", None, [c_void_p, c_void_p, c_int32])
         if prefix != "ref_":
             f("segments_hit_shape", None, [POINTER(C.er_shape), c_int32, c_void_p, c_void_p])
+            f("scene_set_clipping_objects", None, [c_void_p, c_void_p, c_int32])
         f("render_frame", None, [c_void_p, c_void_p, c_void_p, c_int32])
         f("render_sum", None, [c_void_p, c_int32, c_uint32, c_uint32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_int32])
         if prefix != "ref_":
@@ -129,6 +130,12 @@ class SceneHandle:
         if objs:
             self.oa = (C.er_object_desc * len(objs))(*objs)
             orc.scene_set_objects(self.h, ctypes.cast(self.oa, c_void_p), len(objs))
+        clips = getattr(scene, "clipping_objects", [])
+        if clips:
+            if orc.p == "ref_":
+                raise ValueError("the reference build does not apply clipping objects")
+            self.ca = (C.er_clipping_object_desc * len(clips))(*clips)
+            orc.scene_set_clipping_objects(self.h, ctypes.cast(self.ca, c_void_p), len(clips))
 
     def close(self):
         if self.h:

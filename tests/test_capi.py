@@ -84,13 +84,12 @@ def test_struct_layout_matches_c():
     assert int(got["tune.tune_stages"]) == C.er_tune_result.tune_stages.offset
 
 
-@pytest.mark.parametrize("case", ["null", "resolution", "spacing-zero", "spacing-negative", "spacing-nan", "spacing-inf",
-                                  "no-normalize"])
+@pytest.mark.parametrize("case", ["null", "resolution", "spacing-zero", "spacing-negative", "spacing-nan", "spacing-inf"])
 def test_bind_volume_rejects_degenerate_descriptors(case):
     """er_bind_volume refuses, before any device work, a descriptor whose box
-    would be degenerate: a zero, negative or non-finite spacing, or
-    normalize_size = 0 (the reference then scales the spacing by 0,
-    Source/volume.h:106-114)"""
+    would be degenerate: a zero, negative or non-finite spacing.
+    normalize_size = 0 is accepted as the reference accepts it (its box then
+    has no extent, Source/volume.h:106-114; tests/test_gpu_clipping.py)."""
     import numpy as np
     L = C.load_library()
     vox = np.zeros((4, 4, 4), dtype=np.uint16)
@@ -104,8 +103,6 @@ def test_bind_volume_rejects_degenerate_descriptors(case):
         d.voxels = None
     elif case == "resolution":
         d.resolution[1] = 0
-    elif case == "no-normalize":
-        d.normalize_size = 0
     else:
         d.spacing[2] = {"spacing-zero": 0.0, "spacing-negative": -1.0, "spacing-nan": float("nan"),
                         "spacing-inf": float("inf")}[case]
@@ -113,7 +110,7 @@ def test_bind_volume_rejects_degenerate_descriptors(case):
     assert L.er_bind_volume(ctypes.byref(d), ctypes.byref(vid)) == C.ER_ERR_INVALID_ARGUMENT
     assert vid.value == -1
     msg = L.er_last_error_message().decode()
-    assert {"null": "NULL", "resolution": "resolution", "no-normalize": "normalize_size"}.get(case, "spacing") in msg
+    assert {"null": "NULL", "resolution": "resolution"}.get(case, "spacing") in msg
 
 
 @pytest.mark.parametrize("case", ["step-primary-zero", "step-shadow-nan", "density-zero", "density-inf", "film-zero",

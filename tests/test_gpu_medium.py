@@ -132,12 +132,19 @@ def test_c4_adjoint_matches_finite_differences(torch, lib, pkg):
         dsum = 2.0 * (s.double() / spp - target) / spp / target.numel()
         g_rho, g_tf = m.adjoint(rho, tf, spp, dsum.float(), smp)
         C.check(lib.er_synchronize())
+        # 32 parameters drawn uniformly among those the loss depends on (a
+        # non-zero gradient, however small): up to 16 opacity values, the rest
+        # voxels.  The error is relative to the finite difference, with a floor
+        # of 1e-4 of the largest gradient of the parameter's kind (float
+        # atomics sum many samples' contributions, which cancel in the
+        # smallest gradients)
         rng = np.random.default_rng(11)
         gt = g_tf.cpu().numpy()
-        live_tf = np.flatnonzero(np.abs(gt) > 1e-3 * np.abs(gt).max())
+        live_tf = np.flatnonzero(gt != 0.0)
         tf_idx = rng.choice(live_tf, min(16, len(live_tf)), replace=False)
         gr = g_rho.cpu().numpy().ravel()
-        rho_idx = rng.choice(np.flatnonzero(np.abs(gr) > 1e-2 * np.abs(gr).max()), 32 - len(tf_idx), replace=False)
+        rho_idx = rng.choice(np.flatnonzero(gr != 0.0), 32 - len(tf_idx), replace=False)
+        floor = {"tf": 1e-4 * float(np.abs(gt).max()), "rho": 1e-4 * float(np.abs(gr).max())}
         h = 1e-3
         worst = 0.0
         for kind, idx in [("tf", i) for i in tf_idx] + [("rho", i) for i in rho_idx]:
@@ -151,7 +158,7 @@ def test_c4_adjoint_matches_finite_differences(torch, lib, pkg):
             else:
                 fd = (loss64(p, tf) - loss64(q, tf)) / (2 * h)
                 adj = float(gr[idx])
-            rel = abs(adj - fd) / abs(fd)
+            rel = abs(adj - fd) / max(abs(fd), floor[kind])
             worst = max(worst, rel)
             assert rel <= 1e-3, (kind, int(idx), adj, fd, rel)
         print(f"worst relative error over 32 parameters: {worst:.2e}")
