@@ -896,17 +896,27 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
 
 
 def c5_adjoint(args, lib, runtime, torch, stream, vol, film=(2048, 2048), spp=8, size=256):
-    """c5's adjoint: the differentiable medium on the centred 256^3 block of
-    the c5 volume (a float density window) with a 64-value opacity spline, one
-    2048^2 view at 8 spp; forward, adjoint with the forward's samples kept,
-    and adjoint with seed-replay recomputation (nothing kept)"""
+    """c5's adjoint: the differentiable tracer model (64-node opacity PLF
+    with its node values as parameters, colour TFs, hybrid shading; --medium
+    spline: the B-spline medium) on the centred 256^3 block of the c5 volume
+    (a float intensity window), one 2048^2 view at 8 spp; forward, adjoint
+    with the forward's samples kept, and adjoint with seed-replay
+    recomputation (nothing kept)"""
     medium = importlib.import_module("exposure-render_gb300.medium")
     S = importlib.import_module("exposure-render_gb300.scenes")
-    rho = torch.from_numpy(S.density_subblock(vol, size)).cuda()
-    tf = torch.from_numpy(S.ramp_opacity(64)).cuda()
-    sc = S.medium_scene(res=(size, size, size), film=film)
-    r = runtime.Renderer(sc, lib)
-    m = medium.Medium(r, rho, tf, 40.0, albedo=(0.8, 0.7, 0.6), nee_probability=0.5, brick=8)
+    rho_np = S.density_subblock(vol, size)
+    rho = torch.from_numpy(rho_np).cuda()
+    if args.medium == "tracer":
+        sc = S.tf_medium_scene(res=(size, size, size), film=film, n_nodes=64)
+        r = runtime.Renderer(sc, lib)
+        tf = torch.from_numpy(S.plf_node_values(sc.tracer.opacity)).cuda()
+        m = medium.Medium(r, rho, tf, 40.0, nee_probability=0.5, brick=8, model="tracer",
+                          gradient_magnitude_inv=S.gradient_magnitude_range(rho_np))
+    else:
+        tf = torch.from_numpy(S.ramp_opacity(64)).cuda()
+        sc = S.medium_scene(res=(size, size, size), film=film)
+        r = runtime.Renderer(sc, lib)
+        m = medium.Medium(r, rho, tf, 40.0, albedo=(0.8, 0.7, 0.6), nee_probability=0.5, brick=8)
     target = torch.zeros((film[1], film[0], 3), device="cuda")
 
     def timed(fn, steps):
@@ -941,8 +951,9 @@ def c5_adjoint(args, lib, runtime, torch, stream, vol, film=(2048, 2048), spp=8,
     br_ms = timed(bwd_recompute, 1)
     # the adjoints gather with atomics, so the two agree to float summation order
     rel = max(float((state["g"][i] - state["g2"][i]).norm() / max(float(state["g"][i].norm()), 1e-30)) for i in range(2))
-    out = {"what": "differentiable medium on the centred %d^3 block of the c5 volume, 64 opacity values, %dx%d x %d spp"
-                   % (size, film[0], film[1], spp),
+    out = {"what": "%s on the centred %d^3 block of the c5 volume, %dx%d x %d spp"
+                   % ("the differentiable tracer model (64-node opacity PLF, colour TFs, hybrid shading)" if args.medium == "tracer"
+                      else "the B-spline medium (64 opacity values)", size, film[0], film[1], spp),
            "samples": film[0] * film[1] * spp, "forward_ms": f_ms, "adjoint_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
            "adjoint_recompute_ms": br_ms, "adjoint_recompute_over_forward": br_ms / f_ms,
            "forward_msamples_per_s": film[0] * film[1] * spp / (f_ms / 1e3) / 1e6,
@@ -954,10 +965,13 @@ def c5_adjoint(args, lib, runtime, torch, stream, vol, film=(2048, 2048), spp=8,
 
 
 def run_medium(args, rank, world, local_rank):
-    """c4: differentiable medium, 128^3 float density + 64 opacity values,
-    256^2 x 32 spp; forward (every sample kept) and path-replay adjoint of an
-    L2 image loss against a target rendered at 1024 spp from parameters
-    perturbed by N(0, 0.05)"""
+    """c4: the differentiable tracer model (ER_MEDIUM_TRACER: the tracer's
+    64-node opacity PLF with its node values as parameters, its colour
+    transfer functions and hybrid BRDF/phase shading) over a 128^3 float
+    intensity grid, 256^2 x 32 spp; forward (every sample kept) and
+    path-replay adjoint of an L2 image loss against a target rendered at
+    1024 spp from parameters perturbed by N(0, 0.05).  --medium spline
+    runs the B-spline/isotropic medium instead."""
     import torch
     torch.cuda.set_device(local_rank)
     runtime = importlib.import_module("exposure-render_gb300.runtime")
@@ -969,15 +983,22 @@ def run_medium(args, rank, world, local_rank):
     stream = torch.cuda.current_stream()
     C.check(lib.er_set_stream(ctypes.c_void_p(stream.cuda_stream)))
     res, film, spp = (128, 128, 128), (256, 256), 32
-    sc = S.medium_scene(res=res, film=film)
+    tracer_model = args.medium == "tracer"
+    sc = S.tf_medium_scene(res=res, film=film, n_nodes=64) if tracer_model else S.medium_scene(res=res, film=film)
     sc.tracer.settings.seed = R.view_seed(1, rank)
     dist = None
     if world > 1:
         import torch.distributed as dist
     r = runtime.Renderer(sc, lib)
-    rho = torch.from_numpy(S.blob_density(res, n_blobs=10, seed=40)).cuda()
-    tf = torch.from_numpy(S.ramp_opacity(64)).cuda()
-    m = medium.Medium(r, rho, tf, 40.0, albedo=(0.8, 0.7, 0.6), nee_probability=0.5, brick=8)
+    rho_np = S.blob_density(res, n_blobs=10, seed=40)
+    rho = torch.from_numpy(rho_np).cuda()
+    if tracer_model:
+        tf = torch.from_numpy(S.plf_node_values(sc.tracer.opacity)).cuda()
+        m = medium.Medium(r, rho, tf, 40.0, nee_probability=0.5, brick=8, model="tracer",
+                          gradient_magnitude_inv=S.gradient_magnitude_range(rho_np))
+    else:
+        tf = torch.from_numpy(S.ramp_opacity(64)).cuda()
+        m = medium.Medium(r, rho, tf, 40.0, albedo=(0.8, 0.7, 0.6), nee_probability=0.5, brick=8)
     gen = torch.Generator(device="cuda").manual_seed(7)
     rho_t = (rho + 0.05 * torch.randn(rho.shape, device="cuda", generator=gen)).contiguous()
     tf_t = (tf + 0.05 * torch.randn(tf.shape, device="cuda", generator=gen)).contiguous()
@@ -1028,8 +1049,11 @@ def run_medium(args, rank, world, local_rank):
         "metric": "Msamples/s", "value": R.whole_job_rate(samples, f_ms / 1e3, world) / 1e6, "unit": "Msamples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": f_ms + b_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "c4-differentiable-128^3-density-64-opacity-256^2-32spp", "scale": 40.0, "nee_probability": 0.5,
+        "config": {"workload": "c4-differentiable-128^3-grid-64-node-opacity-256^2-32spp", "scale": 40.0, "nee_probability": 0.5,
                    "majorant_brick": 8, "loss": "mean squared error vs 1024-spp target of perturbed parameters",
+                   "model": ("the tracer's transfer functions: 64-node opacity PLF (node values are parameters), colour TFs, "
+                             "hybrid BRDF/phase shading (expected value over the shader choice), float intensity grid"
+                             if tracer_model else "B-spline opacity (64 values), isotropic phase, float density grid"),
                    "parallelism": "replicas" if world > 1 else "single"},
         "forward_ms": f_ms, "adjoint_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
         "adjoint_recompute_ms": br_ms, "adjoint_recompute_over_forward": br_ms / f_ms,
@@ -1056,6 +1080,8 @@ def main():
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel (0 = the workload's)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default settings)")
     ap.add_argument("--no-rmse", action="store_true", help="skip the time-to-RMSE measurement")
+    ap.add_argument("--medium", default="tracer", choices=["tracer", "spline"],
+                    help="c4/c5 adjoint: the tracer's transfer functions and shading, or the B-spline medium")
     args = ap.parse_args()
     if (args.film or args.spp) and args.workload in WORKLOADS:
         W = dict(WORKLOADS[args.workload])

@@ -210,7 +210,12 @@ class er_medium_desc(Structure):
         ("nee_probability", c_float),
         ("d_majorant", c_void_p),
         ("brick", c_int32),
+        ("model", c_int32),
+        ("gradient_magnitude_inv", c_float),
     ]
+
+
+ER_MEDIUM_SPLINE, ER_MEDIUM_TRACER = 0, 1
 
 
 class er_tune_result(Structure):

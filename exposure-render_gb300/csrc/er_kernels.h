@@ -47,11 +47,14 @@ cudaError_t er_launch_empty_skip(float* majorant, const int nb[3], uint8_t* tmp,
 /* the differentiable medium (er_medium.cu) */
 struct DmParams {
     const float* rho;    /* density grid, the tracer volume's resolution, x fastest */
-    const float* tf;     /* tf_n opacity B-spline values */
+    const float* tf;     /* tf_n opacity B-spline values (model 0) or opacity node values (model 1) */
     int tf_n;
     float scale;         /* sigma = scale * opacity */
     float albedo[3];
     float q;             /* next-event probability per collision */
+    int model;           /* 0: B-spline opacity, isotropic albedo; 1: the tracer's transfer functions and shading */
+    int emissive;        /* model 1: the tracer's emission TF is not zero everywhere */
+    float gm_inv;        /* model 1, hybrid: 1 / gradient-magnitude range (a constant) */
 };
 cudaError_t er_launch_dm_forward(const erd::Params& P, const DmParams& M, int spp, uint32_t view, uint32_t first, float* samples,
                                  float* sum, cudaStream_t s);
@@ -59,8 +62,10 @@ cudaError_t er_launch_dm_forward64(const erd::Params& P, const DmParams& M, int 
                                    double* sum, cudaStream_t s);
 cudaError_t er_launch_dm_adjoint(const erd::Params& P, const DmParams& M, int spp, uint32_t view, uint32_t first, const float* dimg,
                                  const float* fwd, float* g_rho, float* g_tf, cudaStream_t s);
-cudaError_t er_launch_dm_majorant(const float* rho, const int res[3], int B, const float* tf, int n, float scale, float margin,
-                                  float floor_, float* out, cudaStream_t s);
+/* plf: NULL for model 0 (B-spline values tf); model 1: the tracer's opacity
+   PLF (device), whose node values are tf */
+cudaError_t er_launch_dm_majorant(const float* rho, const int res[3], int B, const float* tf, int n, const erd::Plf* plf, float scale,
+                                  float margin, float floor_, float* out, cudaStream_t s);
 
 /* corner quads of a uint16 volume (8 bytes per voxel) */
 cudaError_t er_launch_quads(const uint16_t* vox, const int res[3], uint2* quad, cudaStream_t s);

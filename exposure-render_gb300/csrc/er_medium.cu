@@ -82,13 +82,87 @@ ER_D void dm_density(const Params& P, const DmParams& M, v3 p, DmLookup<Real>& k
 template <typename Real>
 struct DmTf {
     Real alpha, dalpha;
-    int i0;
+    int i0, nb;          /* the nb parameters the opacity depends on, from i0 */
     Real b[4];
 };
 
+/* PiecewiseLinearFunction::Evaluate (Source/plf.h:68-91) with the node
+   values `vals` at the positions of p: the value, the segment's slope d/dx
+   (0 where it clamps), and the one or two values it blends with their
+   weights (none at x equal to the last node, where Evaluate returns 0) */
 template <typename Real>
-ER_D void dm_opacity(const DmParams& M, Real rho, DmTf<Real>& o)
+ER_D Real dm_plf(const Plf& p, const float* vals, Real x, int& i0, int& nb, Real* b, Real& slope)
 {
+    const int n = p.count;
+    slope = 0.0f;
+    nb = 0;
+    i0 = 0;
+    if (n <= 0) return 0.0f;
+    if (x < (Real)p.range0) { nb = 1; b[0] = 1.0f; return (Real)__ldg(vals); }
+    if (x > (Real)p.range1) { nb = 1; i0 = n - 1; b[0] = 1.0f; return (Real)__ldg(vals + n - 1); }
+    for (int i = 1; i < n; i++) {
+        const Real P1 = p.pos[i - 1];
+        const Real P2 = p.pos[i];
+        const Real DeltaP = P2 - P1;
+        const Real LerpT = (x - P1) / DeltaP;
+        if (x >= P1 && x < P2) {
+            const Real v0 = __ldg(vals + i - 1), v1 = __ldg(vals + i);
+            i0 = i - 1;
+            nb = 2;
+            b[0] = (Real)1.0f - LerpT;
+            b[1] = LerpT;
+            slope = (v1 - v0) / DeltaP;
+            return v0 + LerpT * (v1 - v0);
+        }
+    }
+    return 0.0f;
+}
+
+/* a transfer function of the tracer (its own node values) at x, and its slope */
+template <typename Real>
+ER_D Real dm_tf_value(const Plf& p, Real x)
+{
+    if constexpr (sizeof(Real) == sizeof(float)) {
+        return plf_eval(p, x);
+    } else {
+        const int n = p.count;
+        if (n <= 0) return 0.0;
+        if (x < (Real)p.range0) return p.val[0];
+        if (x > (Real)p.range1) return p.val[n - 1];
+        for (int i = 1; i < n; i++) {
+            const Real P1 = p.pos[i - 1], P2 = p.pos[i];
+            const Real LerpT = (x - P1) / (P2 - P1);
+            if (x >= P1 && x < P2) return (Real)p.val[i - 1] + LerpT * ((Real)p.val[i] - (Real)p.val[i - 1]);
+        }
+        return 0.0;
+    }
+}
+
+ER_D float dm_tf_slope(const Plf& p, float x)
+{
+    if (p.count <= 0 || x < p.range0 || x > p.range1) return 0.0f;
+    for (int i = 1; i < p.count; i++) {
+        const float P1 = p.pos[i - 1], P2 = p.pos[i];
+        if (x >= P1 && x < P2) return (p.val[i] - p.val[i - 1]) / (P2 - P1);
+    }
+    return 0.0f;
+}
+
+ER_D float dm_pow(float x, float y) { return er_powf(x, y); }
+ER_D double dm_pow(double x, double y) { return pow(x, y); }
+ER_D float dm_exp(float x) { return er_expf(x); }
+ER_D double dm_exp(double x) { return exp(x); }
+ER_D float dm_sqrt(float x) { return sqrtf(x); }
+ER_D double dm_sqrt(double x) { return sqrt(x); }
+
+template <typename Real, int MODEL>
+ER_D void dm_opacity(const Params& P, const DmParams& M, Real rho, DmTf<Real>& o)
+{
+    if (MODEL == 1) {
+        o.alpha = dm_plf<Real>(P.tfs->opacity, M.tf, rho, o.i0, o.nb, o.b, o.dalpha);
+        return;
+    }
+    o.nb = 4;
     const int n = M.tf_n;
     const Real du = (Real)(n - 5);
     Real u = (Real)2.0f + rho * du;
@@ -118,12 +192,279 @@ ER_D void dm_scatter(const DmParams& M, const DmLookup<float>& k, const DmTf<flo
     const float as = a * M.scale;
     if (s_tf) {
 #pragma unroll
-        for (int j = 0; j < 4; j++) atomicAdd(s_tf + o.i0 + j, as * o.b[j]);
+        for (int j = 0; j < 4; j++)
+            if (j < o.nb) atomicAdd(s_tf + o.i0 + j, as * o.b[j]);
     }
     if (g_rho && o.dalpha != 0.0f) {
         const float ar = as * o.dalpha;
 #pragma unroll
         for (int c = 0; c < 8; c++) atomicAdd(g_rho + k.idx[c], ar * k.w[c]);
+    }
+}
+
+ER_D void dm_scatter_rho(const DmLookup<float>& k, float a, float* g_rho)
+{
+    if (!g_rho || a == 0.0f) return;
+#pragma unroll
+    for (int c = 0; c < 8; c++) atomicAdd(g_rho + k.idx[c], a * k.w[c]);
+}
+
+/* ---- model 1: the tracer's shading at a tentative collision ----------
+   At the grid's float intensity I: Kd = Diffuse1D(I), Ks = Specular1D(I),
+   exponent = 1e6 Glossiness1D(I)^7 and the volume IOR
+   (Source/transport.h:136-139, Source/utilities.h:28-31); the normal from
+   central differences of the grid at +-MinStep (Source/volumes.h:31-91);
+   the BRDF (also without apply_shading_type, as the live reference),
+   isotropic phase, or hybrid (Source/scatterevent.h:155-212) with its
+   random shader choice replaced by the expected value P_brdf BRDF +
+   (1 - P_brdf) phase, so that samples stay smooth in the parameters.  The
+   next-event estimate is S(Wo, Wi) Li LightCount / (LightPdf q), S = F
+   |Wi . N| for the BRDF and F for the phase function (Source/transport.h:
+   58-84 without the MIS weight: the estimator samples lights only). */
+template <typename Real>
+struct DmShade {
+    Real Kd[3], Ks[3];
+    Real gl, e;          /* Glossiness1D(I) and its exponent */
+    int type;            /* 0 BRDF, 1 isotropic phase, 2 hybrid (expected value) */
+    Real g6[6];          /* I(P - d), I(P + d) per axis, d = MinStep */
+    Real N[3];
+    Real gm, pb;         /* gradient magnitude, probability of the BRDF */
+};
+
+template <typename Real>
+ER_D void dm_shade_prepare(const Params& P, const DmParams& M, v3 Pt, Real I, const DmTf<Real>& o, DmShade<Real>& h)
+{
+    const Tfs& T = *P.tfs;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        h.Kd[c] = dm_tf_value<Real>(T.diffuse[c], I);
+        h.Ks[c] = dm_tf_value<Real>(T.specular[c], I);
+    }
+    h.gl = dm_tf_value<Real>(T.glossiness, I);
+    h.e = (Real)1000000.0f * dm_pow(h.gl, (Real)7.0f);
+    h.type = !P.apply_shading_type ? 0 : (P.shading_type == 1 ? 1 : (P.shading_type == 2 ? 2 : 0));
+    h.pb = h.type == 0 ? (Real)1.0f : (Real)0.0f;
+    h.gm = 0.0f;
+    h.N[0] = h.N[1] = h.N[2] = 0.0f;
+    if (h.type == 1) return;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const v3 d = gdelta(P, i);
+        DmLookup<Real> a, b;
+        dm_density<Real>(P, M, vsub(Pt, d), a);
+        dm_density<Real>(P, M, vadd(Pt, d), b);
+        h.g6[2 * i] = a.rho;
+        h.g6[2 * i + 1] = b.rho;
+    }
+    /* Normalize(V) = V / Length(V) (Source/vector.h:469-475) */
+    const Real gx = h.g6[0] - h.g6[1], gy = h.g6[2] - h.g6[3], gz = h.g6[4] - h.g6[5];
+    const Real L = dm_sqrt(gx * gx + gy * gy + gz * gz);
+    h.N[0] = gx / L; h.N[1] = gy / L; h.N[2] = gz / L;
+    if (h.type != 2) return;
+    Real sum = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        Real D = h.g6[2 * i] - h.g6[2 * i + 1];
+        D *= (Real)(0.5f / P.spacing[i]);
+        sum += D * D;
+    }
+    h.gm = dm_sqrt(sum);
+    const Real NGM = h.gm * (Real)M.gm_inv;
+    const Real Exponent = (Real)25.0f * dm_pow((Real)P.gradient_factor, (Real)3.0f) * NGM;
+    h.pb = P.opacity_modulated ? o.alpha * ((Real)1.0f - dm_exp(-Exponent)) : (Real)1.0f - dm_exp(-Exponent);
+}
+
+/* binary64 copies of the BRDF's functions (Source/shader.h), for the
+   binary64 evaluation of the estimator; the float path calls er_path.cuh's */
+struct dv3 { double x, y, z; };
+ER_D dv3 DV3(double x, double y, double z) { dv3 r; r.x = x; r.y = y; r.z = z; return r; }
+ER_D double ddot(dv3 a, dv3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+ER_D dv3 dcross(dv3 a, dv3 b) { return DV3((a.y * b.z) - (a.z * b.y), (a.z * b.x) - (a.x * b.z), (a.x * b.y) - (a.y * b.x)); }
+ER_D dv3 dnorm(dv3 a) { const double L = sqrt(ddot(a, a)); return DV3(a.x / L, a.y / L, a.z / L); }
+
+ER_D double dm_fresnel64(double ei_, double et_, double cosi)
+{
+    cosi = cosi < -1.0 ? -1.0 : (cosi > 1.0 ? 1.0 : cosi);
+    const bool entering = cosi > 0.0;
+    double ei = ei_, et = et_;
+    if (!entering) { const double t = ei; ei = et; et = t; }
+    const double s2 = 1.0 - cosi * cosi;
+    const double sint = ei / et * sqrt(s2 > 0.0 ? s2 : 0.0);
+    if (sint >= 1.0) return 1.0;
+    const double c2 = 1.0 - sint * sint;
+    const double cost = sqrt(c2 > 0.0 ? c2 : 0.0);
+    const double ci = fabs(cosi);
+    const double Rparl = ((et * ci) - (ei * cost)) / ((et * ci) + (ei * cost));
+    const double Rperp = ((ei * ci) - (et * cost)) / ((ei * ci) + (et * cost));
+    return (Rparl * Rparl + Rperp * Rperp) / 2.0;
+}
+
+/* BRDF::F (Lambertian + microfacet) times |Wi . N|, per channel, binary64 */
+ER_D void dm_brdf64(const DmShade<double>& h, double ior, v3 Wo_, v3 Wi_, double out[3])
+{
+    const dv3 N = DV3(h.N[0], h.N[1], h.N[2]);
+    const dv3 Wo = DV3(Wo_.x, Wo_.y, Wo_.z), Wi = DV3(Wi_.x, Wi_.y, Wi_.z);
+    const dv3 Nn = dnorm(N);
+    const dv3 Nu = dnorm(dcross(N, Wo));
+    const dv3 Nv = dnorm(dcross(N, Nu));
+    const dv3 Wol = DV3(ddot(Wo, Nu), ddot(Wo, Nv), ddot(Wo, Nn));
+    const dv3 Wil = DV3(ddot(Wi, Nu), ddot(Wi, Nv), ddot(Wi, Nn));
+    double m = 0.0;
+    const double co = fabs(Wol.z), ci = fabs(Wil.z);
+    dv3 Wh = DV3(Wil.x + Wol.x, Wil.y + Wol.y, Wil.z + Wol.z);
+    if (ci != 0.0 && co != 0.0 && !(Wh.x == 0.0 && Wh.y == 0.0 && Wh.z == 0.0)) {
+        Wh = dnorm(Wh);
+        const double F = dm_fresnel64(1.0, ior, ddot(Wil, Wh));
+        const double NdotWh = fabs(Wh.z);
+        const double WOdotWh = fabs(ddot(Wol, Wh));
+        const double g1 = 2.0 * NdotWh * co / WOdotWh, g2 = 2.0 * NdotWh * ci / WOdotWh;
+        const double gmin = (g2 < g1) ? g2 : g1;
+        const double G = (gmin < 1.0) ? gmin : 1.0;
+        const double D = (h.e + 2.0) * 0.15915494309189533577 * pow(NdotWh, h.e);
+        m = D * G * F / (4.0 * ci * co);
+    }
+    const double cosw = fabs(ddot(Wi, Nn));
+    for (int c = 0; c < 3; c++) out[c] = (h.Kd[c] * 0.31830988618379067154 + h.Ks[c] * m) * cosw;
+}
+
+/* S(Wo, Wi) per channel, and its BRDF and phase parts */
+template <typename Real>
+ER_D void dm_shade_eval(const Params& P, const DmShade<Real>& h, v3 Wo, v3 Wi, Real S[3], Real Sb[3], Real Sp[3])
+{
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        Sp[c] = h.Kd[c] * (Real)ER_INV_PI_F;
+        Sb[c] = 0.0f;
+    }
+    if (h.type != 1) {
+        if constexpr (sizeof(Real) == sizeof(float)) {
+            Shader sh;
+            shader_init(sh, 0, V3(h.N[0], h.N[1], h.N[2]), Wo, C3(h.Kd[0], h.Kd[1], h.Kd[2]), C3(h.Ks[0], h.Ks[1], h.Ks[2]),
+                        P.volume_ior, h.e);
+            const c3 f = cscale(shader_f(sh, Wo, Wi), vabsdot(Wi, V3(h.N[0], h.N[1], h.N[2])));
+            Sb[0] = f.r; Sb[1] = f.g; Sb[2] = f.b;
+        } else {
+            dm_brdf64(h, (double)P.volume_ior, Wo, Wi, Sb);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+        S[c] = h.type == 1 ? Sp[c] : (h.type == 0 ? Sb[c] : Sb[c] * h.pb + Sp[c] * ((Real)1.0f - h.pb));
+}
+
+ER_D float dm_sgn(float x) { return x < 0.0f ? -1.0f : 1.0f; }
+
+/* adjoint of S: aS = dLoss/dS; adds dLoss/dI to aI, dLoss/d(opacity at I)
+   through the hybrid's modulation to aop, and returns dLoss/d(each of the
+   six gradient lookups) in ag.  The microfacet term depends on the normal
+   only through a = Wh.N, b = Wo.N and c = Wi.N (the Fresnel term and
+   |Wo.Wh| do not). */
+ER_D void dm_shade_adjoint(const Params& P, const DmParams& M, const DmShade<float>& h, const DmTf<float>& o, float I, v3 Wo, v3 Wi,
+                           const float aS[3], float& aI, float& aop, float ag[6])
+{
+#pragma unroll
+    for (int i = 0; i < 6; i++) ag[i] = 0.0f;
+    float S[3], Sb[3], Sp[3];
+    dm_shade_eval<float>(P, h, Wo, Wi, S, Sb, Sp);
+    float aSb[3] = { aS[0], aS[1], aS[2] }, aSp[3] = { aS[0], aS[1], aS[2] };
+    float angm = 0.0f;
+    const Tfs& T = *P.tfs;
+    if (h.type == 2) {
+        const float apb = aS[0] * (Sb[0] - Sp[0]) + aS[1] * (Sb[1] - Sp[1]) + aS[2] * (Sb[2] - Sp[2]);
+        const float GF3 = er_powf(P.gradient_factor, 3.0f);
+        const float ex = er_expf(-25.0f * GF3 * h.gm * M.gm_inv);
+        const float mod = P.opacity_modulated ? o.alpha : 1.0f;
+        if (P.opacity_modulated) aop += apb * (1.0f - ex);
+        angm = apb * mod * ex * 25.0f * GF3;
+#pragma unroll
+        for (int c = 0; c < 3; c++) { aSb[c] = aS[c] * h.pb; aSp[c] = aS[c] * (1.0f - h.pb); }
+    }
+    if (h.type != 0) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) aI += aSp[c] * dm_tf_slope(T.diffuse[c], I) * ER_INV_PI_F;
+    }
+    if (h.type == 1) return;
+    /* BRDF: Sb = (Kd / pi + Ks m(a, b, c, e)) |c| */
+    const v3 N = V3(h.N[0], h.N[1], h.N[2]);
+    const v3 Wsum = vadd(Wi, Wo);
+    const float b = vdot(Wo, N), c = vdot(Wi, N);
+    const float ab = fabsf(b), ac = fabsf(c);
+    float m = 0.0f, dmda = 0.0f, dmdb = 0.0f, dmdc = 0.0f, dmde = 0.0f;
+    v3 Wh = V3(0.0f, 0.0f, 0.0f);
+    if (ab > 0.0f && ac > 0.0f && !(Wsum.x == 0.0f && Wsum.y == 0.0f && Wsum.z == 0.0f)) {
+        Wh = vnorm(Wsum);
+        const float a = vdot(Wh, N), aa = fabsf(a);
+        const float k = vabsdot(Wo, Wh);
+        const float F = fresnel_eval(1.0f, P.volume_ior, vdot(Wi, Wh));
+        const float D = (h.e + 2.0f) * ER_INV_TWO_PI_F * er_powf(aa, h.e);
+        const float g1 = 2.0f * aa * ab / k, g2 = 2.0f * aa * ac / k;
+        const float gmin = (g2 < g1) ? g2 : g1;
+        float G = 1.0f, dGda = 0.0f, dGdb = 0.0f, dGdc = 0.0f;
+        if (gmin < 1.0f) {
+            G = gmin;
+            if (g2 < g1) { dGda = 2.0f * ac / k * dm_sgn(a); dGdc = 2.0f * aa / k * dm_sgn(c); }
+            else { dGda = 2.0f * ab / k * dm_sgn(a); dGdb = 2.0f * aa / k * dm_sgn(b); }
+        }
+        const float den = 4.0f * ac * ab;
+        m = D * G * F / den;
+        const float dDda = aa > 0.0f ? D * h.e / aa * dm_sgn(a) : 0.0f;
+        dmda = (dDda * G + D * dGda) * F / den;
+        dmdb = D * F / (4.0f * ac) * (dGdb / ab - G * dm_sgn(b) / (ab * ab));
+        dmdc = D * F / (4.0f * ab) * (dGdc / ac - G * dm_sgn(c) / (ac * ac));
+        dmde = aa > 0.0f ? m * (1.0f / (h.e + 2.0f) + er_logf(aa)) : 0.0f;
+    }
+    /* through I: Kd', Ks' and the exponent's 7e6 gl^6 gl' */
+    const float dedI = 7000000.0f * er_powf(h.gl, 6.0f) * dm_tf_slope(T.glossiness, I);
+    float ks_dot = 0.0f, f_dot = 0.0f;
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) {
+        aI += aSb[ch] * (dm_tf_slope(T.diffuse[ch], I) * ER_INV_PI_F + dm_tf_slope(T.specular[ch], I) * m + h.Ks[ch] * dmde * dedI) * ac;
+        ks_dot += aSb[ch] * h.Ks[ch];
+        f_dot += aSb[ch] * (h.Kd[ch] * ER_INV_PI_F + h.Ks[ch] * m);
+    }
+    /* through the normal N = g / |g|, g = (I(P - d) - I(P + d)) per axis */
+    v3 aN = vscale(vadd(vadd(vscale(Wh, dmda), vscale(Wo, dmdb)), vscale(Wi, dmdc)), ks_dot * ac);
+    aN = vadd(aN, vscale(Wi, f_dot * dm_sgn(c)));
+    const v3 gv = V3(h.g6[0] - h.g6[1], h.g6[2] - h.g6[3], h.g6[4] - h.g6[5]);
+    const float glen = vlen(gv);
+    float aG[3] = { 0.0f, 0.0f, 0.0f };
+    if (glen > 0.0f) {
+        const float an = vdot(aN, N);
+        aG[0] = (aN.x - an * N.x) / glen;
+        aG[1] = (aN.y - an * N.y) / glen;
+        aG[2] = (aN.z - an * N.z) / glen;
+    }
+    if (h.type == 2 && h.gm > 0.0f) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const float hi = 0.5f / P.spacing[i];
+            aG[i] += angm * M.gm_inv * vget(gv, i) * hi * hi / h.gm;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        ag[2 * i] = aG[i];
+        ag[2 * i + 1] = -aG[i];
+    }
+}
+
+/* the six gradient lookups' adjoints into the density gradient */
+ER_D void dm_scatter_gradient_lookups(const Params& P, const DmParams& M, v3 Pt, const float ag[6], float* g_rho)
+{
+    if (!g_rho) return;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const v3 d = gdelta(P, i);
+        if (ag[2 * i] != 0.0f) {
+            DmLookup<float> a;
+            dm_density<float>(P, M, vsub(Pt, d), a);
+            dm_scatter_rho(a, ag[2 * i], g_rho);
+        }
+        if (ag[2 * i + 1] != 0.0f) {
+            DmLookup<float> b;
+            dm_density<float>(P, M, vadd(Pt, d), b);
+            dm_scatter_rho(b, ag[2 * i + 1], g_rho);
+        }
     }
 }
 
@@ -138,7 +479,7 @@ ER_D bool dm_segment(const Params& P, const Ray& R, float& t0, float& t1)
 }
 
 /* ratio-tracked shadow transmittance; ADJ scatters -a_scale / (mu - sigma) */
-template <bool ADJ, typename Real = float>
+template <bool ADJ, int MODEL, typename Real = float>
 ER_D Real dm_shadow(const Params& P, const DmParams& M, v3 P1, v3 P2, Rng& rng, float a_scale, float* g_rho, float* s_tf)
 {
     if (!P.shadows) return 1.0f;
@@ -172,7 +513,7 @@ ER_D Real dm_shadow(const Params& P, const DmParams& M, v3 P1, v3 P2, Rng& rng, 
                 DmLookup<Real> k;
                 dm_density(P, M, Pt, k);
                 DmTf<Real> o;
-                dm_opacity(M, k.rho, o);
+                dm_opacity<Real, MODEL>(P, M, k.rho, o);
                 const Real sig = (Real)M.scale * o.alpha;
                 if constexpr (ADJ) dm_scatter(M, k, o, -a_scale / (mu - sig), g_rho, s_tf);
                 Tr = Tr * ((Real)1.0f - sig / (Real)mu);
@@ -185,8 +526,11 @@ ER_D Real dm_shadow(const Params& P, const DmParams& M, v3 P1, v3 P2, Rng& rng, 
     return Tr;
 }
 
-/* next-event estimate at Pt without the collision weight and the shadow */
-ER_D c3 dm_nee(const Params& P, const DmParams& M, v3 Pt, Rng& rng, v3& S, bool& has)
+/* next-event estimate at Pt without the collision weight and the shadow:
+   model 0 returns it (albedo, isotropic phase); model 1 returns the light
+   sample's direction Wi and Li LightCount / (LightPdf q) in LiK, which the
+   caller multiplies by the shading */
+ER_D c3 dm_nee(const Params& P, const DmParams& M, v3 Pt, Rng& rng, v3& S, bool& has, v3& Wi_out, c3& LiK)
 {
     has = false;
     const float pick = rng.get1();
@@ -208,6 +552,11 @@ ER_D c3 dm_nee(const Params& P, const DmParams& M, v3 Pt, Rng& rng, v3& S, bool&
     const float LightPdf = vlen2(vsub(Pt, SS.P)) / (vabsdot(SS.N, vneg(Wi)) * L.area);
     if (!(LightPdf > 0.0f)) return C3(0, 0, 0);
     has = true;
+    if (M.model == 1) {
+        Wi_out = Wi;
+        LiK = cscale(Li, (float)P.light_count / (LightPdf * M.q));
+        return LiK;
+    }
     return cscale(cmul(C3(M.albedo[0], M.albedo[1], M.albedo[2]), Li), DM_INV_4PI * (float)P.light_count / (LightPdf * M.q));
 }
 
@@ -219,18 +568,24 @@ ER_D void dm_shadow_stream(uint32_t seed, uint32_t view, uint32_t pix, uint32_t 
 }
 
 /* one tentative collision of the camera ray, as the walker hands it over */
+template <typename Real>
 struct DmHit {
     v3 Pt;
     float mu;
     bool nee, has;       /* next-event estimate drawn here; it found a light sample */
     uint32_t k_nee;      /* index of the estimate along the ray (its shadow stream) */
-    c3 A0;               /* unshadowed next-event estimate */
+    Real A0[3];          /* unshadowed next-event estimate */
     v3 S;                /* light sample point */
+    Real Le[3];          /* model 1: the emission at the collision */
+    v3 Wo;               /* model 1: minus the camera ray's direction */
+    v3 Wi;               /* model 1: light sample direction */
+    c3 LiK;              /* model 1: Li LightCount / (LightPdf q) */
 };
 
 /* the camera ray's tentative collisions in order; visit(hit, lookup,
-   opacity, sigma, w, T) sees each with the throughput T before it */
-template <typename Real, typename Visit>
+   opacity, sigma, w, T, shading) sees each with the throughput T before
+   it (shading: model 1's, prepared where a next-event estimate is drawn) */
+template <typename Real, int MODEL, typename Visit>
 ER_D void dm_walk(const Params& P, const DmParams& M, int x, int y, Rng& rng, Visit& visit)
 {
     const v2 film_uv = rng.get2();
@@ -257,23 +612,42 @@ ER_D void dm_walk(const Params& P, const DmParams& M, int x, int y, Rng& rng, Vi
                     break;
                 }
                 t = t + dt;
-                DmHit h;
+                DmHit<Real> h;
                 h.Pt = vadd(R.O, vscale(R.D, t));
                 h.mu = mu;
+                h.Wo = vneg(R.D);
                 DmLookup<Real> k;
                 dm_density(P, M, h.Pt, k);
                 DmTf<Real> o;
-                dm_opacity(M, k.rho, o);
+                dm_opacity<Real, MODEL>(P, M, k.rho, o);
                 const Real sig = (Real)M.scale * o.alpha;
                 if (!(sig < (Real)mu)) atomicOr(P.err, 4);   /* the majorant no longer bounds sigma */
                 const Real w = sig / (Real)mu;
+                DmShade<Real> sd;
+                sd.type = -1;
+#pragma unroll
+                for (int c = 0; c < 3; c++) h.Le[c] = 0.0f;
+                if (MODEL == 1 && M.emissive) {
+#pragma unroll
+                    for (int c = 0; c < 3; c++) h.Le[c] = dm_tf_value<Real>(P.tfs->emission[c], k.rho);
+                }
                 h.has = false;
                 h.nee = rng.get1() < M.q;
                 if (h.nee) {
-                    h.A0 = dm_nee(P, M, h.Pt, rng, h.S, h.has);
+                    if (MODEL == 1) dm_shade_prepare<Real>(P, M, h.Pt, k.rho, o, sd);
+                    const c3 a0 = dm_nee(P, M, h.Pt, rng, h.S, h.has, h.Wi, h.LiK);
+                    if (MODEL == 1 && h.has) {
+                        Real S[3], Sb[3], Sp[3];
+                        dm_shade_eval<Real>(P, sd, h.Wo, h.Wi, S, Sb, Sp);
+                        h.A0[0] = S[0] * (Real)a0.r;
+                        h.A0[1] = S[1] * (Real)a0.g;
+                        h.A0[2] = S[2] * (Real)a0.b;
+                    } else {
+                        h.A0[0] = a0.r; h.A0[1] = a0.g; h.A0[2] = a0.b;
+                    }
                     h.k_nee = nee++;
                 }
-                visit(h, k, o, sig, w, T);
+                visit(h, k, o, sig, w, T, sd);
                 T = T * ((Real)1.0f - w);
                 if (++guard > ER_DELTA_MAX_COLLISIONS) { atomicOr(P.err, 2); return; }
                 tau = -er_logf(rng.get1());
@@ -306,6 +680,7 @@ struct DmJobs {
     uint32_t* cnt;     /* per item: jobs */
     uint32_t* total;   /* jobs of the window */
     uint32_t cap;      /* job slots */
+    float4* E;         /* model 1: per item, the emission summed along the walk (NULL for model 0) */
 };
 
 struct DmWindow {
@@ -324,6 +699,7 @@ ER_D void dm_item(const Params& P, const DmWindow& W, uint32_t i, uint32_t& pix,
     y = (int)(pix / (uint32_t)P.film[0]);
 }
 
+template <int MODEL>
 __global__ void __launch_bounds__(256) k_dm_count(const Params P, const DmParams M, const DmWindow W, DmJobs J)
 {
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -336,8 +712,9 @@ __global__ void __launch_bounds__(256) k_dm_count(const Params P, const DmParams
             dm_item(P, W, i, pix, sample, x, y);
             Rng rng;
             er_seed_lanes(P.seed, W.view, pix, sample, &rng.s0, &rng.s1);
-            auto count = [&](const DmHit& h, const DmLookup<float>&, const DmTf<float>&, float, float, float) { n += h.has ? 1u : 0u; };
-            dm_walk<float>(P, M, x, y, rng, count);
+            auto count = [&](const DmHit<float>& h, const DmLookup<float>&, const DmTf<float>&, float, float, float,
+                             const DmShade<float>&) { n += h.has ? 1u : 0u; };
+            dm_walk<float, MODEL>(P, M, x, y, rng, count);
         }
         /* warp-aggregated reservation of the item's job slots */
         const int lane = threadIdx.x & 31;
@@ -356,6 +733,7 @@ __global__ void __launch_bounds__(256) k_dm_count(const Params P, const DmParams
     }
 }
 
+template <int MODEL>
 __global__ void __launch_bounds__(256) k_dm_jobs(const Params P, const DmParams M, const DmWindow W, DmJobs J)
 {
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -367,18 +745,23 @@ __global__ void __launch_bounds__(256) k_dm_jobs(const Params P, const DmParams 
         er_seed_lanes(P.seed, W.view, pix, sample, &rng.s0, &rng.s1);
         uint32_t j = J.off[i];
         const uint32_t end = j + J.cnt[i];
-        auto write = [&](const DmHit& h, const DmLookup<float>&, const DmTf<float>&, float, float w, float T) {
+        c3 E = C3(0, 0, 0);
+        auto write = [&](const DmHit<float>& h, const DmLookup<float>&, const DmTf<float>&, float, float w, float T,
+                         const DmShade<float>&) {
+            if (MODEL == 1) E = cadd(E, cscale(C3(h.Le[0], h.Le[1], h.Le[2]), T * w));
             if (!h.has || j >= end || j >= J.cap) return;
             J.P[j] = make_float4(h.Pt.x, h.Pt.y, h.Pt.z, T * w);
             J.S[j] = make_float4(h.S.x, h.S.y, h.S.z, 0.0f);
-            J.A[j] = make_float4(h.A0.r, h.A0.g, h.A0.b, 0.0f);
+            J.A[j] = make_float4(h.A0[0], h.A0[1], h.A0[2], 0.0f);
             J.id[j] = make_uint2(i, h.k_nee);
             j++;
         };
-        dm_walk<float>(P, M, x, y, rng, write);
+        dm_walk<float, MODEL>(P, M, x, y, rng, write);
+        if (J.E) J.E[i] = make_float4(E.r, E.g, E.b, 0.0f);
     }
 }
 
+template <int MODEL>
 __global__ void __launch_bounds__(256) k_dm_shadow(const Params P, const DmParams M, const DmWindow W, DmJobs J)
 {
     const uint32_t n = min(*J.total, J.cap);
@@ -391,7 +774,7 @@ __global__ void __launch_bounds__(256) k_dm_shadow(const Params P, const DmParam
         Rng sh;
         dm_shadow_stream(P.seed, W.view, pix, sample, id.y, sh);
         const float4 p = J.P[j], s = J.S[j];
-        const float Tr = dm_shadow<false>(P, M, V3(p.x, p.y, p.z), V3(s.x, s.y, s.z), sh, 0.0f, nullptr, nullptr);
+        const float Tr = dm_shadow<false, MODEL>(P, M, V3(p.x, p.y, p.z), V3(s.x, s.y, s.z), sh, 0.0f, nullptr, nullptr);
         J.A[j].w = Tr;
     }
 }
@@ -409,6 +792,11 @@ __global__ void k_dm_gather(const DmWindow W, const DmJobs J, uint64_t base, flo
         const float Tw = J.P[j].w;
         const c3 A = cscale(C3(a.x, a.y, a.z), a.w);
         L = cadd(L, cscale(A, Tw));
+    }
+    if (J.E) {
+        /* model 1: the emission after the next-event estimates */
+        const float4 e = J.E[i];
+        L = cadd(L, C3(e.x, e.y, e.z));
     }
     const uint64_t q = 3 * (base + i);
     samples[q] = L.r;
@@ -435,6 +823,7 @@ ER_D void dm_tf_flush(const DmParams& M, const float* row, float* g_tf)
         if (row[j] != 0.0f) atomicAdd(g_tf + j, row[j]);
 }
 
+template <int MODEL>
 __global__ void __launch_bounds__(256) k_dm_adj_primary(const Params P, const DmParams M, const DmWindow W, DmJobs J, uint64_t base,
                                                         const float* __restrict__ dimg, const float* __restrict__ fwd,
                                                         float* __restrict__ g_rho, float* __restrict__ g_tf)
@@ -455,28 +844,57 @@ __global__ void __launch_bounds__(256) k_dm_adj_primary(const Params P, const Dm
         er_seed_lanes(P.seed, W.view, pix, sample, &rng.s0, &rng.s1);
         uint32_t j = J.off[i];
         const uint32_t end = j + J.cnt[i];
-        c3 L = C3(0, 0, 0);
-        auto adj = [&](const DmHit& h, const DmLookup<float>& k, const DmTf<float>& o, float sig, float w, float T) {
+        c3 L = C3(0, 0, 0), E = C3(0, 0, 0);
+        auto adj = [&](const DmHit<float>& h, const DmLookup<float>& k, const DmTf<float>& o, float sig, float w, float T,
+                       const DmShade<float>& sd) {
             c3 A = C3(0, 0, 0);
+            float Tr = 0.0f;
+            bool shaded = false;
             if (h.has && j < end && j < J.cap) {
                 const float4 a = J.A[j];
+                Tr = a.w;
                 A = cscale(C3(a.x, a.y, a.z), a.w);
                 const c3 c = cscale(A, T * w);
                 L = cadd(L, c);
                 J.S[j].w = g.r * c.r + g.g * c.g + g.b * c.b;
                 j++;
+                shaded = MODEL == 1;
             }
-            /* dL/dsigma = T A / mu - (Ltot - L_<=k) / (mu - sigma) */
-            const c3 rest = csub(Lt, L);
-            const c3 dLds = csub(cscale(A, T / h.mu), cdivs(rest, h.mu - sig));
+            /* dL/dsigma = T A / mu - (Ltot - L_<=k) / (mu - sigma), A the
+               collision's whole contribution before T w */
+            const c3 Le = C3(h.Le[0], h.Le[1], h.Le[2]);
+            if (MODEL == 1) E = cadd(E, cscale(Le, T * w));
+            const c3 Ak = MODEL == 1 ? cadd(Le, A) : A;
+            const c3 rest = csub(Lt, MODEL == 1 ? cadd(L, E) : L);
+            const c3 dLds = csub(cscale(Ak, T / h.mu), cdivs(rest, h.mu - sig));
             const float a = g.r * dLds.r + g.g * dLds.g + g.b * dLds.b;
-            if (a != 0.0f) dm_scatter(M, k, o, a, g_rho, s_tf);
+            if (MODEL == 1) {
+                /* through the emission and shading at I, and the hybrid's
+                   opacity modulation */
+                const c3 gA = cscale(g, T * w);
+                float aI = 0.0f, aop = 0.0f;
+                if (M.emissive)
+                    aI += gA.r * dm_tf_slope(P.tfs->emission[0], k.rho) + gA.g * dm_tf_slope(P.tfs->emission[1], k.rho) +
+                          gA.b * dm_tf_slope(P.tfs->emission[2], k.rho);
+                if (shaded) {
+                    float ag[6];
+                    const float aS[3] = { gA.r * Tr * h.LiK.r, gA.g * Tr * h.LiK.g, gA.b * Tr * h.LiK.b };
+                    dm_shade_adjoint(P, M, sd, o, k.rho, h.Wo, h.Wi, aS, aI, aop, ag);
+                    if (sd.type != 1) dm_scatter_gradient_lookups(P, M, h.Pt, ag, g_rho);
+                }
+                dm_scatter_rho(k, aI, g_rho);
+                const float at = a + aop / M.scale;
+                if (at != 0.0f) dm_scatter(M, k, o, at, g_rho, s_tf);
+            } else if (a != 0.0f) {
+                dm_scatter(M, k, o, a, g_rho, s_tf);
+            }
         };
-        dm_walk<float>(P, M, x, y, rng, adj);
+        dm_walk<float, MODEL>(P, M, x, y, rng, adj);
     }
     if (g_tf) dm_tf_flush(M, row, g_tf);
 }
 
+template <int MODEL>
 __global__ void __launch_bounds__(256) k_dm_adj_shadow(const Params P, const DmParams M, const DmWindow W, DmJobs J,
                                                        float* __restrict__ g_rho, float* __restrict__ g_tf)
 {
@@ -495,13 +913,14 @@ __global__ void __launch_bounds__(256) k_dm_adj_shadow(const Params P, const DmP
         Rng sh;
         dm_shadow_stream(P.seed, W.view, pix, sample, id.y, sh);
         const float4 p = J.P[j], s = J.S[j];
-        dm_shadow<true>(P, M, V3(p.x, p.y, p.z), V3(s.x, s.y, s.z), sh, gc, g_rho, s_tf);
+        dm_shadow<true, MODEL>(P, M, V3(p.x, p.y, p.z), V3(s.x, s.y, s.z), sh, gc, g_rho, s_tf);
     }
     if (g_tf) dm_tf_flush(M, row, g_tf);
 }
 
 /* the binary64 evaluation: one thread per sample, every medium-dependent
    quantity in double */
+template <int MODEL>
 __global__ void __launch_bounds__(256) k_dm_forward64(const Params P, const DmParams M, int spp, uint32_t view, uint32_t first,
                                                       uint32_t npix, double* __restrict__ samples)
 {
@@ -514,19 +933,26 @@ __global__ void __launch_bounds__(256) k_dm_forward64(const Params P, const DmPa
         er_seed_lanes(P.seed, view, pix, first + s, &rng.s0, &rng.s1);
         const int x = (int)(pix % (uint32_t)P.film[0]), y = (int)(pix / (uint32_t)P.film[0]);
         double L0 = 0.0, L1 = 0.0, L2 = 0.0;
-        auto acc = [&](const DmHit& h, const DmLookup<double>&, const DmTf<double>&, double, double w, double T) {
+        double E0 = 0.0, E1 = 0.0, E2 = 0.0;
+        auto acc = [&](const DmHit<double>& h, const DmLookup<double>&, const DmTf<double>&, double, double w, double T,
+                       const DmShade<double>&) {
+            if (MODEL == 1) {
+                E0 += h.Le[0] * T * w;
+                E1 += h.Le[1] * T * w;
+                E2 += h.Le[2] * T * w;
+            }
             if (!h.has) return;
             Rng sh;
             dm_shadow_stream(P.seed, view, pix, first + s, h.k_nee, sh);
-            const double Tr = dm_shadow<false, double>(P, M, h.Pt, h.S, sh, 0.0f, nullptr, nullptr);
-            L0 += (double)h.A0.r * Tr * T * w;
-            L1 += (double)h.A0.g * Tr * T * w;
-            L2 += (double)h.A0.b * Tr * T * w;
+            const double Tr = dm_shadow<false, MODEL, double>(P, M, h.Pt, h.S, sh, 0.0f, nullptr, nullptr);
+            L0 += h.A0[0] * Tr * T * w;
+            L1 += h.A0[1] * Tr * T * w;
+            L2 += h.A0[2] * Tr * T * w;
         };
-        dm_walk<double>(P, M, x, y, rng, acc);
-        samples[3 * i] = L0;
-        samples[3 * i + 1] = L1;
-        samples[3 * i + 2] = L2;
+        dm_walk<double, MODEL>(P, M, x, y, rng, acc);
+        samples[3 * i] = L0 + E0;
+        samples[3 * i + 1] = L1 + E1;
+        samples[3 * i + 2] = L2 + E2;
     }
 }
 
@@ -567,7 +993,8 @@ __global__ void k_dm_reduce(const float* __restrict__ samples, int spp, uint32_t
    brick's density range (1-voxel apron) covers, times margin, plus floor;
    one warp per brick */
 __global__ void k_dm_majorant(const float* __restrict__ rho, int rx, int ry, int rz, int B, int nbx, int nby, int nbz,
-                              const float* __restrict__ tf, int n, float scale, float margin, float floor_, float* __restrict__ out)
+                              const float* __restrict__ tf, int n, const Plf* plf, float scale, float margin, float floor_,
+                              float* __restrict__ out)
 {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -592,6 +1019,17 @@ __global__ void k_dm_majorant(const float* __restrict__ rho, int rx, int ry, int
         hi = b > hi ? b : hi;
     }
     if (lane != 0) return;
+    if (plf) {
+        /* model 1: the opacity PLF's maximum over [lo, hi] - its values at
+           both ends and at the nodes inside */
+        int i0, nb;
+        float b[2], sl;
+        float vmax = fmaxf(dm_plf<float>(*plf, tf, lo, i0, nb, b, sl), dm_plf<float>(*plf, tf, hi, i0, nb, b, sl));
+        for (int i = 0; i < plf->count; i++)
+            if (plf->pos[i] >= lo && plf->pos[i] <= hi) vmax = fmaxf(vmax, __ldg(tf + i));
+        out[warp] = scale * (fmaxf(vmax, 0.0f) * margin + floor_);
+        return;
+    }
     float u0 = 2.0f + lo * (float)(n - 5), u1 = 2.0f + hi * (float)(n - 5);
     u0 = fminf(fmaxf(u0, 1.0f), (float)(n - 2));
     u1 = fminf(fmaxf(u1, 1.0f), (float)(n - 2));
@@ -622,10 +1060,11 @@ struct DmWorkspace {
     float4 *P = nullptr, *S = nullptr, *A = nullptr;
     uint2* id = nullptr;
     uint32_t *off = nullptr, *cnt = nullptr, *total = nullptr, *host_total = nullptr;
+    float4* E = nullptr;       /* model 1: per item emission sums */
     size_t cap = 0, item_cap = 0;
     ~DmWorkspace()
     {
-        cudaFree(P); cudaFree(S); cudaFree(A); cudaFree(id); cudaFree(off); cudaFree(cnt); cudaFree(total);
+        cudaFree(P); cudaFree(S); cudaFree(A); cudaFree(id); cudaFree(off); cudaFree(cnt); cudaFree(total); cudaFree(E);
         if (host_total) cudaFreeHost(host_total);
     }
     cudaError_t ensure_items(size_t n)
@@ -636,10 +1075,12 @@ struct DmWorkspace {
             if (e != cudaSuccess) return e;
         }
         if (n <= item_cap) return cudaSuccess;
-        cudaFree(off); cudaFree(cnt);
+        cudaFree(off); cudaFree(cnt); cudaFree(E);
         off = cnt = nullptr;
+        E = nullptr;
         cudaError_t e = cudaMalloc(&off, n * sizeof(uint32_t));
         if (e == cudaSuccess) e = cudaMalloc(&cnt, n * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc(&E, n * sizeof(float4));
         item_cap = e == cudaSuccess ? n : 0;
         return e;
     }
@@ -691,24 +1132,30 @@ static cudaError_t dm_windows(const Params& P, const DmParams& M, int spp, uint3
         W.first = first;
         DmJobs J;
         J.P = ws.P; J.S = ws.S; J.A = ws.A; J.id = ws.id; J.off = ws.off; J.cnt = ws.cnt; J.total = ws.total;
+        J.E = M.model == 1 ? ws.E : nullptr;
         J.cap = (uint32_t)ws.cap;
         if ((e = cudaMemsetAsync(ws.total, 0, sizeof(uint32_t), s)) != cudaSuccess) return e;
-        k_dm_count<<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
+        if (M.model == 1) k_dm_count<1><<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
+        else k_dm_count<0><<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
         if ((e = cudaMemcpyAsync(ws.host_total, ws.total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
         const uint32_t njobs = *ws.host_total;
         if ((e = ws.ensure_jobs(njobs)) != cudaSuccess) return e;
         J.P = ws.P; J.S = ws.S; J.A = ws.A; J.id = ws.id; J.cap = (uint32_t)ws.cap;
         const uint64_t base = (uint64_t)s0 * npix;
-        k_dm_jobs<<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
-        if (njobs) k_dm_shadow<<<grid_for(njobs, 16), 256, 0, s>>>(P, M, W, J);
+        if (M.model == 1) k_dm_jobs<1><<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
+        else k_dm_jobs<0><<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
+        if (njobs && M.model == 1) k_dm_shadow<1><<<grid_for(njobs, 16), 256, 0, s>>>(P, M, W, J);
+        else if (njobs) k_dm_shadow<0><<<grid_for(njobs, 16), 256, 0, s>>>(P, M, W, J);
         if (!dimg || samples) {
             /* forward values: written by the forward, read by the adjoint */
             if (!dimg) k_dm_gather<<<(W.items + 255) / 256, 256, 0, s>>>(W, J, base, samples);
         }
         if (dimg) {
-            k_dm_adj_primary<<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J, base, dimg, samples, g_rho, g_tf);
-            if (njobs) k_dm_adj_shadow<<<grid_for(njobs, 16), 256, 0, s>>>(P, M, W, J, g_rho, g_tf);
+            if (M.model == 1) k_dm_adj_primary<1><<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J, base, dimg, samples, g_rho, g_tf);
+            else k_dm_adj_primary<0><<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J, base, dimg, samples, g_rho, g_tf);
+            if (njobs && M.model == 1) k_dm_adj_shadow<1><<<grid_for(njobs, 16), 256, 0, s>>>(P, M, W, J, g_rho, g_tf);
+            else if (njobs) k_dm_adj_shadow<0><<<grid_for(njobs, 16), 256, 0, s>>>(P, M, W, J, g_rho, g_tf);
         }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
@@ -729,7 +1176,8 @@ cudaError_t er_launch_dm_forward64(const Params& P, const DmParams& M, int spp, 
                                    double* sum, cudaStream_t s)
 {
     const uint32_t npix = (uint32_t)P.film[0] * (uint32_t)P.film[1];
-    k_dm_forward64<<<grid_for((uint64_t)spp * npix, 32), 256, 0, s>>>(P, M, spp, view, first, npix, samples);
+    if (M.model == 1) k_dm_forward64<1><<<grid_for((uint64_t)spp * npix, 32), 256, 0, s>>>(P, M, spp, view, first, npix, samples);
+    else k_dm_forward64<0><<<grid_for((uint64_t)spp * npix, 32), 256, 0, s>>>(P, M, spp, view, first, npix, samples);
     k_dm_reduce64<<<(npix + 255) / 256, 256, 0, s>>>(samples, spp, npix, sum);
     return cudaGetLastError();
 }
@@ -754,12 +1202,12 @@ cudaError_t er_launch_dm_adjoint(const Params& P, const DmParams& M, int spp, ui
     return e;
 }
 
-cudaError_t er_launch_dm_majorant(const float* rho, const int res[3], int B, const float* tf, int n, float scale, float margin,
-                                  float floor_, float* out, cudaStream_t s)
+cudaError_t er_launch_dm_majorant(const float* rho, const int res[3], int B, const float* tf, int n, const erd::Plf* plf, float scale,
+                                  float margin, float floor_, float* out, cudaStream_t s)
 {
     const int nbx = (res[0] + B - 1) / B, nby = (res[1] + B - 1) / B, nbz = (res[2] + B - 1) / B;
     const long long warps = (long long)nbx * nby * nbz;
     const unsigned blocks = (unsigned)((warps * 32 + 255) / 256);
-    k_dm_majorant<<<blocks, 256, 0, s>>>(rho, res[0], res[1], res[2], B, nbx, nby, nbz, tf, n, scale, margin, floor_, out);
+    k_dm_majorant<<<blocks, 256, 0, s>>>(rho, res[0], res[1], res[2], B, nbx, nby, nbz, tf, n, plf, scale, margin, floor_, out);
     return cudaGetLastError();
 }

@@ -1834,8 +1834,23 @@ static er_status medium_params(int32_t tracer_id, const er_medium_desc* m, erd::
     TracerItem* t = find_tracer(tracer_id);
     if (!t) return fail(ER_ERR_INVALID_ID, "resource item with ID:%d does not exist", tracer_id);
     if (!m || !m->d_density || !m->d_opacity) return fail(ER_ERR_INVALID_ARGUMENT, "medium descriptor or its buffers are NULL");
-    if (m->n_opacity < 6 || m->n_opacity > ER_MAX_TF_NODES)
+    if (m->model != ER_MEDIUM_SPLINE && m->model != ER_MEDIUM_TRACER)
+        return fail(ER_ERR_INVALID_ARGUMENT, "model %d is not an ER_MEDIUM_* value", m->model);
+    const er_render_settings& ts = t->d.settings;
+    const int shading = !ts.apply_shading_type ? ER_SHADING_BRDF_ONLY : ts.shading_type;
+    if (m->model == ER_MEDIUM_TRACER) {
+        if (m->n_opacity != t->d.opacity.count || m->n_opacity < 1)
+            return fail(ER_ERR_INVALID_ARGUMENT, "n_opacity %d is not the tracer's opacity node count %d", m->n_opacity,
+                        t->d.opacity.count);
+        if (shading != ER_SHADING_BRDF_ONLY && shading != ER_SHADING_PHASE_ONLY && shading != ER_SHADING_HYBRID)
+            return fail(ER_ERR_UNSUPPORTED, "the differentiable tracer model supports the BRDF, phase and hybrid shaders");
+        if (shading != ER_SHADING_PHASE_ONLY && ts.gradient_computation != ER_GRADIENT_CENTRAL)
+            return fail(ER_ERR_UNSUPPORTED, "the differentiable tracer model takes normals from central differences");
+        if (shading == ER_SHADING_HYBRID && !(m->gradient_magnitude_inv > 0.0f && std::isfinite(m->gradient_magnitude_inv)))
+            return fail(ER_ERR_INVALID_ARGUMENT, "the hybrid shader needs a finite positive gradient_magnitude_inv");
+    } else if (m->n_opacity < 6 || m->n_opacity > ER_MAX_TF_NODES) {
         return fail(ER_ERR_INVALID_ARGUMENT, "n_opacity %d out of range [6, %d]", m->n_opacity, ER_MAX_TF_NODES);
+    }
     if (m->brick < 1 || m->brick > 64) return fail(ER_ERR_INVALID_ARGUMENT, "brick %d out of range [1, 64]", m->brick);
     if (!(m->nee_probability > 0.0f && m->nee_probability <= 1.0f))
         return fail(ER_ERR_INVALID_ARGUMENT, "nee_probability must lie in (0, 1]");
@@ -1852,6 +1867,13 @@ static er_status medium_params(int32_t tracer_id, const er_medium_desc* m, erd::
     M.scale = m->scale;
     for (int i = 0; i < 3; i++) M.albedo[i] = m->albedo[i];
     M.q = m->nee_probability;
+    M.model = m->model;
+    M.gm_inv = m->model == ER_MEDIUM_TRACER ? m->gradient_magnitude_inv : 0.0f;
+    M.emissive = 0;
+    if (m->model == ER_MEDIUM_TRACER)
+        for (int c = 0; c < 3; c++)
+            for (int i = 0; i < t->d.emission.plf[c].count; i++)
+                if (t->d.emission.plf[c].value[i] != 0.0f) M.emissive = 1;
     *tp = t;
     return ER_OK;
 }
@@ -1871,7 +1893,12 @@ ER_API er_status er_medium_majorant(int32_t tracer_id, const er_medium_desc* med
     if (!(margin >= 1.0f) || !(floor_ >= 0.0f)) return fail(ER_ERR_INVALID_ARGUMENT, "margin must be >= 1 and floor >= 0");
     if ((long long)P.nb[0] * P.nb[1] * P.nb[2] > (1ll << 26))
         return fail(ER_ERR_INVALID_ARGUMENT, "%d x %d x %d bricks exceed the majorant build's 2^26", P.nb[0], P.nb[1], P.nb[2]);
-    ER_CUDA(er_launch_dm_majorant(M.rho, P.res, P.brick, M.tf, M.tf_n, M.scale, margin, floor_, d_majorant, (cudaStream_t)stream));
+    /* model 1 reads the tracer's opacity PLF (device) for its node positions */
+    const erd::Plf* plf = M.model == ER_MEDIUM_TRACER
+                              ? reinterpret_cast<const erd::Plf*>(reinterpret_cast<const char*>(t->tfs.p) + offsetof(erd::Tfs, opacity))
+                              : nullptr;
+    ER_CUDA(er_launch_dm_majorant(M.rho, P.res, P.brick, M.tf, M.tf_n, plf, M.scale, margin, floor_, d_majorant,
+                                  (cudaStream_t)stream));
     return ER_OK;
 }
 

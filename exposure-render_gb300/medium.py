@@ -1,11 +1,22 @@
 """Differentiable medium over the C ABI (er_medium_*): a float density grid
-and opacity B-spline values rendered by a bound tracer's camera and lights,
-with gradients from the path-replay adjoint kernel behind a
+and opacity parameters rendered by a bound tracer's camera and lights, with
+gradients from the path-replay adjoint kernel behind a
 torch.autograd.Function.
 
     m = Medium(renderer, density, opacity, scale=40.0)        # majorant built once
     img = m(density, opacity, spp=32)                          # (H, W, 3) mean, differentiable
     loss = ((img - target) ** 2).mean(); loss.backward()       # density.grad, opacity.grad
+
+model="spline" (C.ER_MEDIUM_SPLINE): opacity holds B-spline values over the
+density, isotropic phase with `albedo`.  model="tracer" (C.ER_MEDIUM_TRACER):
+the grid holds intensities in the tracer's transfer-function domain and
+opacity holds the values of the tracer's opacity nodes (at the tracer's node
+positions); diffuse, specular, glossiness and emission are the tracer's, the
+shading its BRDF / phase / hybrid (the hybrid as the expected value over its
+shader choice) - the transport model of the tracer, with its opacity nodes
+and intensity grid as the parameters.  `gradient_magnitude_inv` normalises
+the hybrid switch (a constant of the estimator: 1 / the grid's largest
+gradient magnitude when the Medium is made, by default).
 
 The majorant grid is fixed when the Medium is made (or on rebuild_majorant):
 the estimator's random numbers then do not depend on the medium, so for a
@@ -28,9 +39,17 @@ from . import capi as C
 class Medium:
     def __init__(self, renderer, density: torch.Tensor, opacity: torch.Tensor, scale: float,
                  albedo=(0.8, 0.8, 0.8), nee_probability: float = 0.5, brick: int = 8, margin: float = 1.25,
-                 floor: float = 1e-3, keep_samples: bool = True):
+                 floor: float = 1e-3, keep_samples: bool = True, model: str = "spline", gradient_magnitude_inv: float = None):
         self.r = renderer
         self.lib = renderer.lib
+        self.model = {"spline": C.ER_MEDIUM_SPLINE, "tracer": C.ER_MEDIUM_TRACER}[model]
+        self.gm_inv = 0.0
+        if self.model == C.ER_MEDIUM_TRACER:
+            if gradient_magnitude_inv is None:
+                from . import scenes
+                v = renderer.scene
+                gradient_magnitude_inv = scenes.gradient_magnitude_range(density.detach().cpu().numpy(), v.spacing)
+            self.gm_inv = float(gradient_magnitude_inv)
         self.scale = float(scale)
         self.albedo = tuple(float(a) for a in albedo)
         self.q = float(nee_probability)
@@ -61,6 +80,8 @@ class Medium:
         d.nee_probability = self.q
         d.d_majorant = self.majorant.data_ptr()
         d.brick = self.brick
+        d.model = self.model
+        d.gradient_magnitude_inv = self.gm_inv
         return d
 
     def rebuild_majorant(self, density, opacity, margin=1.25, floor=1e-3):

@@ -645,3 +645,100 @@ def lattice_volume(shape_zyx, period=96.0, seed=13, noise=40.0) -> np.ndarray:
         v = np.float32(1200.0) + sxy * sz + rng.random(size=(Y, X), dtype=np.float32) * np.float32(noise)
         out[z] = v.astype(np.uint16)
     return out
+
+
+# ---------------------------------------------------------------------------
+# the differentiable product estimator: the tracer's transfer functions and
+# shading over a float intensity grid (medium model 1)
+# ---------------------------------------------------------------------------
+
+def tf_medium_tracer(film=(256, 256), n_nodes=64, shading=C.SHADING_HYBRID, glossiness=0.3, emission=0.0):
+    """The c1 camera and light with transfer functions over intensities in
+    [0, 1]: an n-node opacity PLF (positions i / (n - 1), a ramp from 0.15 to
+    0.7 as the values), a diffuse colour ramp, a constant specular colour and
+    glossiness (exponent 1e6 g^7), an optional emission bump, and the given
+    shader (BRDF, phase or hybrid, opacity-modulated)."""
+    t = c1_tracer(film)
+    pos = np.arange(n_nodes, dtype=np.float64) / (n_nodes - 1)
+    vals = np.clip((pos - 0.15) / (0.7 - 0.15), 0.0, 1.0)
+    t.opacity = C.make_plf([(float(p), float(v)) for p, v in zip(pos, vals)])
+    t.diffuse = C.make_color_tf([(0.0, (0.9, 0.5, 0.3)), (0.4, (0.8, 0.7, 0.5)), (1.0, (0.6, 0.8, 0.9))])
+    t.specular = C.make_color_tf([(0.0, (0.25, 0.25, 0.25)), (1.0, (0.35, 0.3, 0.3))])
+    t.glossiness = C.make_plf([(0.0, glossiness), (1.0, glossiness)])
+    t.emission = C.make_color_tf([(0.0, (0.0, 0.0, 0.0)), (0.45, (0.0, 0.0, 0.0)), (0.6, (emission, 0.6 * emission, 0.2 * emission)),
+                                  (0.75, (0.0, 0.0, 0.0)), (1.0, (0.0, 0.0, 0.0))])
+    t.settings.apply_shading_type = 1
+    t.settings.shading_type = shading
+    t.settings.opacity_modulated = 1
+    return t
+
+
+def tf_medium_scene(res=(128, 128, 128), film=(256, 256), n_nodes=64, shading=C.SHADING_HYBRID, glossiness=0.3, emission=0.0,
+                    two_lights=True) -> Scene:
+    """tf_medium_tracer around a zero volume of the grid's resolution (the
+    volume gives the grid its placement), with the c1 area light and, with
+    two_lights, a small sphere light beside the volume"""
+    lights, textures = c1_lights()
+    t = tf_medium_tracer(film, n_nodes, shading, glossiness, emission)
+    if two_lights:
+        L = C.er_light_desc()
+        L.visible = 0
+        L.shape = make_shape(C.SHAPE_SPHERE, look_at_tm((-0.9, -0.6, 0.3), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0)), outer=0.15)
+        L.texture_id = 0
+        L.multiplier = 6.0
+        L.unit = C.UNIT_POWER
+        lights.append(L)
+        t.light_count = 2
+        t.light_ids[1] = 1
+    return Scene("tf_medium", np.zeros(res, dtype=np.uint16), tracer=t, lights=lights, textures=textures, spp=32)
+
+
+def plf_node_values(plf) -> np.ndarray:
+    return np.array([plf.value[i] for i in range(plf.count)], dtype=np.float32)
+
+
+def plf_majorant(rho, plf, values, scale, brick=8, margin=1.25, floor=1e-3) -> np.ndarray:
+    """per-brick upper bound of sigma = scale * PLF(rho) with the node
+    values `values` at the positions of `plf`: the PLF's maximum over the
+    brick's density range (1-voxel apron) - its values at both ends and at
+    the nodes inside - times `margin`, plus `floor` * scale.  Shape
+    (nbz, nby, nbx), float32."""
+    n = plf.count
+    pos = np.array([plf.position[i] for i in range(n)], dtype=np.float64)
+    vals = np.asarray(values, dtype=np.float64)
+
+    def ev(x):
+        if x < pos[0]:
+            return vals[0]
+        if x > pos[-1]:
+            return vals[-1]
+        return float(np.interp(x, pos, vals))
+    Z, Y, X = rho.shape
+    nb = [(d + brick - 1) // brick for d in (Z, Y, X)]
+    out = np.zeros(nb, dtype=np.float32)
+    for bz in range(nb[0]):
+        for by in range(nb[1]):
+            for bx in range(nb[2]):
+                sl = rho[max(bz * brick - 1, 0):min((bz + 1) * brick + 1, Z),
+                         max(by * brick - 1, 0):min((by + 1) * brick + 1, Y),
+                         max(bx * brick - 1, 0):min((bx + 1) * brick + 1, X)]
+                lo, hi = float(sl.min()), float(sl.max())
+                inside = vals[(pos >= lo) & (pos <= hi)]
+                vmax = max(ev(lo), ev(hi), float(inside.max()) if inside.size else -np.inf)
+                out[bz, by, bx] = scale * (max(vmax, 0.0) * margin + floor)
+    return out
+
+
+def gradient_magnitude_range(rho, spacing=(1.0, 1.0, 1.0)) -> float:
+    """1 / the largest central-difference gradient magnitude of a float grid
+    at its voxel centres (the hybrid shader's normalisation), with the
+    normalised volume's spacing (longest axis 1)"""
+    Z, Y, X = rho.shape
+    phys = np.array([X * spacing[0], Y * spacing[1], Z * spacing[2]], dtype=np.float64)
+    sp = np.array(spacing, dtype=np.float64) / phys.max()
+    r = np.pad(rho.astype(np.float64), 1, mode="edge")
+    gx = (r[1:-1, 1:-1, :-2] - r[1:-1, 1:-1, 2:]) * 0.5 / sp[0]
+    gy = (r[1:-1, :-2, 1:-1] - r[1:-1, 2:, 1:-1]) * 0.5 / sp[1]
+    gz = (r[:-2, 1:-1, 1:-1] - r[2:, 1:-1, 1:-1]) * 0.5 / sp[2]
+    m = float(np.sqrt(gx * gx + gy * gy + gz * gz).max())
+    return 1.0 / m if m > 0.0 else 0.0

@@ -465,14 +465,32 @@ ER_API er_status er_batch_destroy(int32_t batch_id);
    error word (ER_ERR_TIMEOUT at the next synchronising call). */
 typedef struct er_medium_desc {
     const float* d_density;       /* device, the tracer volume's resolution, x fastest */
-    const float* d_opacity;       /* device, n_opacity B-spline values */
-    int32_t n_opacity;            /* 6 .. ER_MAX_TF_NODES */
+    const float* d_opacity;       /* device, n_opacity B-spline values (ER_MEDIUM_SPLINE) or the values of
+                                     the tracer's opacity nodes (ER_MEDIUM_TRACER) */
+    int32_t n_opacity;            /* 6 .. ER_MAX_TF_NODES (spline); the tracer's opacity node count (tracer) */
     float scale;                  /* sigma = scale * opacity */
-    float albedo[3];
+    float albedo[3];              /* ER_MEDIUM_SPLINE only */
     float nee_probability;        /* (0, 1] */
     const float* d_majorant;      /* device, one float per brick of brick^3 voxels (x fastest) */
     int32_t brick;                /* 1 .. 64 */
+    int32_t model;                /* ER_MEDIUM_SPLINE (0) or ER_MEDIUM_TRACER (1) */
+    float gradient_magnitude_inv; /* ER_MEDIUM_TRACER with the hybrid shader: 1 / the gradient-magnitude range
+                                     that normalises the shader switch (a constant of the estimator) */
 } er_medium_desc;
+
+/* Models of the differentiable medium.  ER_MEDIUM_SPLINE: the B-spline
+   opacity and isotropic albedo above.  ER_MEDIUM_TRACER: the bound tracer's
+   own transfer functions and shading over the float grid, read as
+   intensities - sigma = scale * Opacity1D(I) with the tracer's opacity node
+   positions and d_opacity's node values (the parameters), and at each
+   next-event estimate Diffuse1D/Specular1D/Glossiness1D(I) with the BRDF
+   (normal from central differences of the grid), the isotropic phase
+   function, or the hybrid switch of the settings (Source/scatterevent.h:
+   155-212) as the expected value over its random choice; Emission1D(I) at
+   every collision.  The tracer's gradient_computation must be central
+   differences; shading types other than BRDF, phase and hybrid are
+   refused (ER_ERR_UNSUPPORTED). */
+enum { ER_MEDIUM_SPLINE = 0, ER_MEDIUM_TRACER = 1 };
 
 /* Per-brick majorant of a medium into d_majorant: scale * (max opacity
    control value over the spline segments of the brick's density range with

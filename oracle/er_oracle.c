@@ -181,6 +181,12 @@ struct or_scene {
     float dm_scale;
     col3 dm_albedo;
     float dm_q;
+    /* dm_set_model: 0 the B-spline opacity and isotropic albedo above; 1 the
+       tracer's transfer functions and shading, with tf_val the values of the
+       tracer's opacity nodes (at its node positions) */
+    int dm_model;
+    int dm_emissive;          /* model 1: the emission TF is not zero everywhere */
+    float dm_gm_inv;          /* model 1, hybrid shading: 1 / gradient-magnitude range (a fixed constant) */
 };
 
 static double g_lookups_per_sample = 0.0;
@@ -2364,11 +2370,60 @@ static void dm_density(or_scene* s, v3 P, dm_lookup* k)
     k->rho = r;
 }
 
-/* opacity spline: value, d alpha / d rho, first control index and weights */
-typedef struct { float alpha, dalpha; int i0; float b[4]; } dm_tf;
+/* opacity: value, d alpha / d rho, the nb parameters it depends on (first
+   index i0) and their weights */
+typedef struct { float alpha, dalpha; int i0, nb; float b[4]; } dm_tf;
+
+/* PiecewiseLinearFunction::Evaluate (Source/plf.h:68-91) with the node
+   values `vals` at the positions of `p`: the value, the slope d/dx of the
+   segment (0 where it clamps) and the two values it blends (i0 and i0 + 1
+   with weights b[0], b[1]; one value where it clamps; none for the x equal
+   to the last node, where Evaluate returns 0) */
+static float dm_plf(const er_plf* p, const float* vals, float x, int* i0, int* nb, float* b, float* slope)
+{
+    const int n = p->count;
+    *slope = 0.0f;
+    *nb = 0;
+    *i0 = 0;
+    if (n <= 0) return 0.0f;
+    if (x < p->node_range[0]) { *nb = 1; b[0] = 1.0f; return vals[0]; }
+    if (x > p->node_range[1]) { *nb = 1; *i0 = n - 1; b[0] = 1.0f; return vals[n - 1]; }
+    for (int i = 1; i < n; i++) {
+        const float P1 = p->position[i - 1];
+        const float P2 = p->position[i];
+        const float DeltaP = P2 - P1;
+        const float LerpT = (x - P1) / DeltaP;
+        if (x >= P1 && x < P2) {
+            *i0 = i - 1;
+            *nb = 2;
+            b[0] = 1.0f - LerpT;
+            b[1] = LerpT;
+            *slope = (vals[i] - vals[i - 1]) / DeltaP;
+            return vals[i - 1] + LerpT * (vals[i] - vals[i - 1]);
+        }
+    }
+    return 0.0f;
+}
+
+/* d/dx of a transfer function of the tracer (its own node values) */
+static float plf_slope(const er_plf* p, float x)
+{
+    if (p->count <= 0 || x < p->node_range[0] || x > p->node_range[1]) return 0.0f;
+    for (int i = 1; i < p->count; i++) {
+        const float P1 = p->position[i - 1];
+        const float P2 = p->position[i];
+        if (x >= P1 && x < P2) return (p->value[i] - p->value[i - 1]) / (P2 - P1);
+    }
+    return 0.0f;
+}
 
 static void dm_opacity(const or_scene* s, float rho, dm_tf* o)
 {
+    if (s->dm_model == 1) {
+        o->alpha = dm_plf(&s->opacity, s->tf_val, rho, &o->i0, &o->nb, o->b, &o->dalpha);
+        return;
+    }
+    o->nb = 4;
     const int n = s->tf_n;
     const float du = (float)(n - 5);
     float u = 2.0f + rho * du;
@@ -2397,11 +2452,200 @@ static void dm_scatter(const or_scene* s, const dm_lookup* k, const dm_tf* o, fl
 {
     const float as = a * s->dm_scale;
     if (g_tf)
-        for (int j = 0; j < 4; j++) g_tf[o->i0 + j] += as * o->b[j];
+        for (int j = 0; j < o->nb; j++) g_tf[o->i0 + j] += as * o->b[j];
     if (g_rho && o->dalpha != 0.0f) {
         const float ar = as * o->dalpha;
         for (int c = 0; c < 8; c++) g_rho[k->idx[c]] += ar * k->w[c];
     }
+}
+
+static void dm_scatter_rho(const dm_lookup* k, float a, float* g_rho)
+{
+    if (!g_rho || a == 0.0f) return;
+    for (int c = 0; c < 8; c++) g_rho[k->idx[c]] += a * k->w[c];
+}
+
+/* ---- model 1: the tracer's shading at a tentative collision ----------
+   At intensity I (the float grid's trilinear value): Kd = Diffuse1D(I),
+   Ks = Specular1D(I), exponent = 1e6 Glossiness1D(I)^7, IOR of the volume
+   BRDF (Source/transport.h:136-139, Source/utilities.h:28-31); the normal
+   from central differences of the grid at +-MinStep (Source/volumes.h:31-
+   91); the shader chosen by the settings: BRDF (also without
+   apply_shading_type, as the live reference), isotropic phase, or hybrid
+   (Source/scatterevent.h:155-212), whose random choice between the two is
+   replaced by its expected value, P_brdf * BRDF + (1 - P_brdf) * phase, so
+   that a sample stays smooth in the parameters.  The next-event estimate is
+   S(Wo, Wi) Li LightCount / (LightPdf q): S = F |Wi . N| for the BRDF, F
+   for the phase function (Source/transport.h:58-84 without the MIS
+   weight, which a light-sampling-only estimator does not need). */
+typedef struct {
+    col3 Kd, Ks;
+    float gl, e;        /* Glossiness1D(I) and the exponent */
+    int type;           /* 0 BRDF, 1 isotropic phase, 2 hybrid (expected value) */
+    dm_lookup g[6];     /* I(P - d), I(P + d) per axis, d = MinStep */
+    v3 N;
+    float gm, pb;       /* gradient magnitude, probability of the BRDF */
+} dm_shade_t;
+
+static void dm_shade_prepare(or_scene* s, v3 P, const dm_lookup* k, const dm_tf* o, dm_shade_t* h)
+{
+    const float I = k->rho;
+    h->Kd = ctf_eval(&s->diffuse, I);
+    h->Ks = ctf_eval(&s->specular, I);
+    h->gl = plf_eval(&s->glossiness, I);
+    h->e = glossiness_exponent(h->gl);
+    h->type = !s->st.apply_shading_type ? 0 : (s->st.shading_type == ER_SHADING_PHASE_ONLY ? 1 : (s->st.shading_type == ER_SHADING_HYBRID ? 2 : 0));
+    h->pb = h->type == 0 ? 1.0f : 0.0f;
+    h->gm = 0.0f;
+    h->N = V3(0.0f, 0.0f, 0.0f);
+    if (h->type == 1) return;
+    const v3 d[3] = { s->gdx, s->gdy, s->gdz };
+    for (int i = 0; i < 3; i++) {
+        dm_density(s, vsub(P, d[i]), &h->g[2 * i]);
+        dm_density(s, vadd(P, d[i]), &h->g[2 * i + 1]);
+    }
+    h->N = vnorm(V3(h->g[0].rho - h->g[1].rho, h->g[2].rho - h->g[3].rho, h->g[4].rho - h->g[5].rho));
+    if (h->type != 2) return;
+    float sum = 0.0f;
+    for (int i = 0; i < 3; i++) {
+        float D = h->g[2 * i].rho - h->g[2 * i + 1].rho;
+        D *= 0.5f / vget(s->spacing, i);
+        sum += D * D;
+    }
+    h->gm = sqrtf(sum);
+    const float NGM = h->gm * s->dm_gm_inv;
+    const float Exponent = 25.0f * er_powf(s->st.gradient_factor, 3.0f) * NGM;
+    h->pb = s->st.opacity_modulated ? o->alpha * (1.0f - er_expf(-Exponent)) : 1.0f - er_expf(-Exponent);
+}
+
+static inline float dm_ior(const or_scene* s) { return s->st.volume_ior > 0.0f ? s->st.volume_ior : 15.0f; }
+
+/* S(Wo, Wi), and the BRDF and phase parts */
+static col3 dm_shade_eval(const or_scene* s, const dm_shade_t* h, v3 Wo, v3 Wi, col3* Sb_out, col3* Sp_out)
+{
+    const col3 Sp = cscale(h->Kd, INV_PI_F);
+    col3 Sb = C3(0.0f, 0.0f, 0.0f);
+    if (h->type != 1) {
+        shader_t sh;
+        shader_init(&sh, 0, h->N, Wo, h->Kd, h->Ks, dm_ior(s), h->e);
+        Sb = cscale(shader_f(&sh, Wo, Wi), vabsdot(Wi, h->N));
+    }
+    if (Sb_out) *Sb_out = Sb;
+    if (Sp_out) *Sp_out = Sp;
+    if (h->type == 1) return Sp;
+    if (h->type == 0) return Sb;
+    return cadd(cscale(Sb, h->pb), cscale(Sp, 1.0f - h->pb));
+}
+
+static inline float sgnf(float x) { return x < 0.0f ? -1.0f : 1.0f; }
+
+/* adjoint of S: aS = dLoss/dS; adds dLoss/dI to *aI, dLoss/d(opacity at
+   I) through the hybrid's modulation to *aop, and dLoss/d(each of the six
+   gradient lookups) to ag[6].  The microfacet term depends on the normal
+   only through a = Wh.N, b = Wo.N, c = Wi.N (the Fresnel term and |Wo.Wh|
+   do not). */
+static void dm_shade_adjoint(const or_scene* s, const dm_shade_t* h, const dm_tf* o, float I, v3 Wo, v3 Wi, col3 aS, float* aI, float* aop,
+                             float ag[6])
+{
+    for (int i = 0; i < 6; i++) ag[i] = 0.0f;
+    col3 Sb, Sp;
+    dm_shade_eval(s, h, Wo, Wi, &Sb, &Sp);
+    col3 aSb = aS, aSp = aS;
+    float angm = 0.0f;
+    if (h->type == 2) {
+        const float apb = aS.c[0] * (Sb.c[0] - Sp.c[0]) + aS.c[1] * (Sb.c[1] - Sp.c[1]) + aS.c[2] * (Sb.c[2] - Sp.c[2]);
+        const float GF3 = er_powf(s->st.gradient_factor, 3.0f);
+        const float ex = er_expf(-25.0f * GF3 * h->gm * s->dm_gm_inv);
+        const float mod = s->st.opacity_modulated ? o->alpha : 1.0f;
+        if (s->st.opacity_modulated) *aop += apb * (1.0f - ex);
+        angm = apb * mod * ex * 25.0f * GF3;
+        aSb = cscale(aS, h->pb);
+        aSp = cscale(aS, 1.0f - h->pb);
+    }
+    if (h->type != 0) {
+        for (int c = 0; c < 3; c++) *aI += aSp.c[c] * plf_slope(&s->diffuse.plf[c], I) * INV_PI_F;
+    }
+    if (h->type == 1) return;
+    /* BRDF: Sb = (Kd / pi + Ks m(a, b, c, e)) |c| */
+    const v3 N = h->N;
+    const v3 Wsum = vadd(Wi, Wo);
+    const float b = vdot(Wo, N), c = vdot(Wi, N);
+    const float ab = fabsf(b), ac = fabsf(c);
+    float m = 0.0f, dmda = 0.0f, dmdb = 0.0f, dmdc = 0.0f, dmde = 0.0f;
+    v3 Wh = V3(0.0f, 0.0f, 0.0f);
+    if (ab > 0.0f && ac > 0.0f && !(Wsum.x == 0.0f && Wsum.y == 0.0f && Wsum.z == 0.0f)) {
+        Wh = vnorm(Wsum);
+        const float a = vdot(Wh, N), aa = fabsf(a);
+        const float k = vabsdot(Wo, Wh);
+        const float F = fresnel_eval(1.0f, dm_ior(s), vdot(Wi, Wh));
+        const float D = (h->e + 2.0f) * INV_TWO_PI_F * er_powf(aa, h->e);
+        const float g1 = 2.0f * aa * ab / k, g2 = 2.0f * aa * ac / k;
+        const float gmin = (g2 < g1) ? g2 : g1;
+        float G = 1.0f, dGda = 0.0f, dGdb = 0.0f, dGdc = 0.0f;
+        if (gmin < 1.0f) {
+            G = gmin;
+            if (g2 < g1) { dGda = 2.0f * ac / k * sgnf(a); dGdc = 2.0f * aa / k * sgnf(c); }
+            else { dGda = 2.0f * ab / k * sgnf(a); dGdb = 2.0f * aa / k * sgnf(b); }
+        }
+        const float den = 4.0f * ac * ab;
+        m = D * G * F / den;
+        const float dDda = aa > 0.0f ? D * h->e / aa * sgnf(a) : 0.0f;
+        dmda = (dDda * G + D * dGda) * F / den;
+        dmdb = D * F / (4.0f * ac) * (dGdb / ab - G * sgnf(b) / (ab * ab));
+        dmdc = D * F / (4.0f * ab) * (dGdc / ac - G * sgnf(c) / (ac * ac));
+        dmde = aa > 0.0f ? m * (1.0f / (h->e + 2.0f) + er_logf(aa)) : 0.0f;
+    }
+    /* through I: Kd', Ks' and the exponent's 7e6 gl^6 gl' */
+    const float gls = plf_slope(&s->glossiness, I);
+    const float dedI = 7000000.0f * er_powf(h->gl, 6.0f) * gls;
+    float ks_dot = 0.0f, f_dot = 0.0f;
+    for (int ch = 0; ch < 3; ch++) {
+        const float kd_s = plf_slope(&s->diffuse.plf[ch], I), ks_s = plf_slope(&s->specular.plf[ch], I);
+        *aI += aSb.c[ch] * (kd_s * INV_PI_F + ks_s * m + h->Ks.c[ch] * dmde * dedI) * ac;
+        ks_dot += aSb.c[ch] * h->Ks.c[ch];
+        f_dot += aSb.c[ch] * (h->Kd.c[ch] * INV_PI_F + h->Ks.c[ch] * m);
+    }
+    /* through the normal */
+    v3 aN = vscale(vadd(vadd(vscale(Wh, dmda), vscale(Wo, dmdb)), vscale(Wi, dmdc)), ks_dot * ac);
+    aN = vadd(aN, vscale(Wi, f_dot * sgnf(c)));
+    const v3 gv = V3(h->g[0].rho - h->g[1].rho, h->g[2].rho - h->g[3].rho, h->g[4].rho - h->g[5].rho);
+    const float glen = vlen(gv);
+    float aG[3] = { 0.0f, 0.0f, 0.0f };
+    if (glen > 0.0f) {
+        const float an = vdot(aN, N);
+        aG[0] = (aN.x - an * N.x) / glen;
+        aG[1] = (aN.y - an * N.y) / glen;
+        aG[2] = (aN.z - an * N.z) / glen;
+    }
+    if (h->type == 2 && h->gm > 0.0f) {
+        for (int i = 0; i < 3; i++) {
+            const float hi = 0.5f / vget(s->spacing, i);
+            aG[i] += angm * s->dm_gm_inv * vget(gv, i) * hi * hi / h->gm;
+        }
+    }
+    for (int i = 0; i < 3; i++) {
+        ag[2 * i] = aG[i];
+        ag[2 * i + 1] = -aG[i];
+    }
+}
+
+/* model 1: the emission TF of the tracer at I and its slope per channel */
+static col3 dm_emission(const or_scene* s, float I)
+{
+    return s->dm_emissive ? ctf_eval(&s->emission, I) : C3(0.0f, 0.0f, 0.0f);
+}
+
+/* the model of the differentiable medium (the dm_model field); gm_inv is
+   the hybrid shader's 1 / gradient-magnitude range, a constant of the
+   estimator */
+void ER_OR(dm_set_model)(or_scene* s, int32_t model, float gm_inv)
+{
+    s->dm_model = model;
+    s->dm_gm_inv = gm_inv;
+    s->dm_emissive = 0;
+    for (int c = 0; c < 3; c++)
+        for (int i = 0; i < s->emission.plf[c].count; i++)
+            if (s->emission.plf[c].value[i] != 0.0f) s->dm_emissive = 1;
 }
 
 /* the ray's box segment, as the delta tracker clips it */
@@ -2472,7 +2716,8 @@ static float dm_shadow(or_scene* s, v3 P1, v3 P2, rng_t* rng, float a_scale, flo
 /* next-event estimate at P (without the collision weight): one uniformly
    picked light, isotropic phase, albedo, ratio-tracked shadow; the light
    sample is written to *S for the adjoint's shadow replay */
-static col3 dm_nee(or_scene* s, v3 P, rng_t* rng, v3* S, float* unshadowed_scale)
+static col3 dm_nee(or_scene* s, v3 P, rng_t* rng, v3* S, float* unshadowed_scale, const dm_shade_t* h, v3 Wo, v3* Wi_out,
+                   col3* LiK)
 {
     *unshadowed_scale = 0.0f;
     const float pick = rng_get1(rng);
@@ -2494,8 +2739,14 @@ static col3 dm_nee(or_scene* s, v3 P, rng_t* rng, v3* S, float* unshadowed_scale
     if (cblack(Li)) return C3(0, 0, 0);
     const float LightPdf = vlen2(vsub(P, SS.P)) / (vabsdot(SS.N, vneg(Wi)) * L->area);
     if (!(LightPdf > 0.0f)) return C3(0, 0, 0);
-    const col3 c = cscale(cmul(s->dm_albedo, Li), DM_INV_4PI * (float)s->light_count / (LightPdf * s->dm_q));
     *unshadowed_scale = 1.0f;
+    if (s->dm_model == 1) {
+        /* the tracer's shading (model 1) */
+        *Wi_out = Wi;
+        *LiK = cscale(Li, (float)s->light_count / (LightPdf * s->dm_q));
+        return cmul(dm_shade_eval(s, h, Wo, Wi, NULL, NULL), *LiK);
+    }
+    const col3 c = cscale(cmul(s->dm_albedo, Li), DM_INV_4PI * (float)s->light_count / (LightPdf * s->dm_q));
     return c;
 }
 
@@ -2506,6 +2757,7 @@ static col3 dm_sample(or_scene* s, int x, int y, uint32_t view, uint32_t pix, ui
 {
     uint32_t nee = 0;
     col3 L = C3(0, 0, 0);
+    col3 E = C3(0, 0, 0);     /* model 1: emission, summed apart from the next-event estimates */
     const v2 film_uv = rng_get2(rng);
     const v2 lens_uv = rng_get2(rng);
     const ray_t R = sample_camera(s, x, y, film_uv, lens_uv);
@@ -2536,16 +2788,26 @@ static col3 dm_sample(or_scene* s, int x, int y, uint32_t view, uint32_t pix, ui
                 const float sig = s->dm_scale * o.alpha;
                 const float w = sig / mu;
                 col3 A = C3(0, 0, 0);
+                /* model 1: the tracer's emission at every collision and its
+                   shading at the next-event estimates */
+                const col3 Le = s->dm_model == 1 ? dm_emission(s, k.rho) : C3(0, 0, 0);
+                dm_shade_t sd;
+                v3 Wi = V3(0, 0, 0);
+                col3 LiK = C3(0, 0, 0);
+                float Tr = 0.0f;
+                int shaded = 0;
                 if (rng_get1(rng) < s->dm_q) {
                     v3 S;
                     float has;
-                    const col3 A0 = dm_nee(s, P, rng, &S, &has);
+                    if (s->dm_model == 1) dm_shade_prepare(s, P, &k, &o, &sd);
+                    const col3 A0 = dm_nee(s, P, rng, &S, &has, &sd, vneg(R.D), &Wi, &LiK);
                     const uint32_t k_nee = nee++;
                     if (has != 0.0f) {
                         rng_t sh;
                         dm_shadow_stream(s->st.seed, view, pix, sample, k_nee, &sh);
-                        const float Tr = dm_shadow(s, P, S, &sh, 0.0f, NULL, NULL);
+                        Tr = dm_shadow(s, P, S, &sh, 0.0f, NULL, NULL);
                         A = cscale(A0, Tr);
+                        shaded = s->dm_model == 1;
                         if (g) {
                             /* the adjoint replay of the same segment */
                             const col3 c = cscale(A, T * w);
@@ -2559,12 +2821,34 @@ static col3 dm_sample(or_scene* s, int x, int y, uint32_t view, uint32_t pix, ui
                 }
                 const col3 c = cscale(A, T * w);
                 L = cadd(L, c);
+                if (s->dm_model == 1) E = cadd(E, cscale(Le, T * w));
                 if (g) {
-                    /* dL/dsigma = T A / mu - (Ltot - L_<=k) / (mu - sigma) */
-                    const col3 rest = csub(Ltot, L);
-                    const col3 dLds = csub(cscale(A, T / mu), cdivs(rest, mu - sig));
+                    /* dL/dsigma = T A / mu - (Ltot - L_<=k) / (mu - sigma), A the
+                       collision's whole contribution before T w */
+                    const col3 Ak = s->dm_model == 1 ? cadd(Le, A) : A;
+                    const col3 rest = csub(Ltot, s->dm_model == 1 ? cadd(L, E) : L);
+                    const col3 dLds = csub(cscale(Ak, T / mu), cdivs(rest, mu - sig));
                     const float a = g->c[0] * dLds.c[0] + g->c[1] * dLds.c[1] + g->c[2] * dLds.c[2];
-                    if (a != 0.0f) dm_scatter(s, &k, &o, a, g_rho, g_tf);
+                    if (s->dm_model == 1) {
+                        /* through the shading and emission at I, and the hybrid's
+                           opacity modulation */
+                        const col3 gA = cscale(*g, T * w);
+                        float aI = 0.0f, aop = 0.0f;
+                        if (s->dm_emissive)
+                            for (int ch = 0; ch < 3; ch++) aI += gA.c[ch] * plf_slope(&s->emission.plf[ch], k.rho);
+                        if (shaded) {
+                            float ag[6];
+                            const col3 aS = cmul(cscale(gA, Tr), LiK);
+                            dm_shade_adjoint(s, &sd, &o, k.rho, vneg(R.D), Wi, aS, &aI, &aop, ag);
+                            if (sd.type != 1)
+                                for (int i = 0; i < 6; i++) dm_scatter_rho(&sd.g[i], ag[i], g_rho);
+                        }
+                        dm_scatter_rho(&k, aI, g_rho);
+                        const float at = a + aop / s->dm_scale;
+                        if (at != 0.0f) dm_scatter(s, &k, &o, at, g_rho, g_tf);
+                    } else if (a != 0.0f) {
+                        dm_scatter(s, &k, &o, a, g_rho, g_tf);
+                    }
                 }
                 T = T * (1.0f - w);
                 tau = -er_logf(rng_get1(rng));
@@ -2572,7 +2856,7 @@ static col3 dm_sample(or_scene* s, int x, int y, uint32_t view, uint32_t pix, ui
         }
         dda_advance(s, &d, e);
     }
-    return L;
+    return s->dm_model == 1 ? cadd(L, E) : L;
 }
 
 typedef struct {

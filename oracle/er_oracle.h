@@ -94,6 +94,14 @@ void ER_OR(render_stats)(double* out);
    float buffer is double. */
 void ER_OR(dm_attach)(or_scene* scene, const float* rho, const float* tf_val, int32_t tf_n, float scale, const float* albedo,
                       float q, const float* majorant, int32_t brick);
+/* Model of the medium (after dm_attach): 0 the B-spline opacity and
+   isotropic albedo; 1 the tracer's transfer functions - the opacity PLF at
+   the tracer's node positions with the node values tf_val (tf_n = the
+   tracer's opacity node count), Diffuse/Specular/Glossiness/Emission of the
+   tracer at the grid's float intensity - and its BRDF / phase / hybrid
+   shading (the hybrid as the expected value over its shader choice); gm_inv
+   is the hybrid's 1 / gradient-magnitude range, a constant. */
+void ER_OR(dm_set_model)(or_scene* scene, int32_t model, float gm_inv);
 void ER_OR(dm_render)(or_scene* scene, int32_t spp, uint32_t view, uint32_t first, float* sum, float* samples, int32_t nthreads);
 void ER_OR(dm_adjoint)(or_scene* scene, int32_t spp, uint32_t view, uint32_t first, const float* dimg, const float* fwd,
                        float* g_rho, float* g_tf, int32_t nthreads);

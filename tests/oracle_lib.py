@@ -53,6 +53,7 @@ class Oracle:
         if prefix != "ref_":
             f("dm_attach", None, [c_void_p, c_void_p, c_void_p, c_int32, self._real_c(prefix), c_void_p,
                                   self._real_c(prefix), c_void_p, c_int32])
+            f("dm_set_model", None, [c_void_p, c_int32, self._real_c(prefix)])
             f("dm_render", None, [c_void_p, c_int32, c_uint32, c_uint32, c_void_p, c_void_p, c_int32])
             f("dm_adjoint", None, [c_void_p, c_int32, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p, c_int32])
         # the FP64 build takes double buffers wherever the float build takes float
@@ -170,9 +171,11 @@ class SceneHandle:
 
 class MediumHandle(SceneHandle):
     """An oracle scene with a differentiable medium attached: `rho` (Z, Y, X)
-    float density, `tf` opacity B-spline values, fixed `majorant` grid."""
+    float density, `tf` opacity B-spline values (model 0) or the values of
+    the tracer's opacity nodes (model 1, the tracer's transfer functions and
+    shading), fixed `majorant` grid."""
 
-    def __init__(self, orc: Oracle, scene, rho, tf, scale, albedo, q, majorant, brick):
+    def __init__(self, orc: Oracle, scene, rho, tf, scale, albedo, q, majorant, brick, model=0, gm_inv=0.0):
         super().__init__(orc, scene)
         r = orc.real
         self.rho = np.ascontiguousarray(rho, dtype=r)
@@ -180,6 +183,7 @@ class MediumHandle(SceneHandle):
         self.albedo = np.ascontiguousarray(albedo, dtype=r)
         self.maj = np.ascontiguousarray(majorant, dtype=r)
         orc.dm_attach(self.h, ptr(self.rho), ptr(self.tf), len(self.tf), scale, ptr(self.albedo), q, ptr(self.maj), brick)
+        orc.dm_set_model(self.h, model, gm_inv)
 
     def render(self, spp, view=0, first=0, keep_samples=False, nthreads=8):
         W, H = self.scene.width, self.scene.height
