@@ -20,8 +20,10 @@ e2e   : the same metric through the C ABI a user calls, with host buffers:
         reference build in oracle/_ref when it exists for this machine, else
         the C restatement of oracle/), all threads, each step a bounded
         sample (a film crop at 1 spp) of the same workload.
-Multi-GPU (torchrun): independent replicas, one view per rank, no data-path
-collective; value = all ranks' samples / max time.
+Multi-GPU (torchrun): c1/c2/c3/c5 render one set of images over all ranks,
+each rank its own sample ranges of every view, with the per-pixel sums
+all-reduced each step (the path's one exchange); c4 runs independent
+replicas.  value = all ranks' samples / max time (weak scaling).
 """
 from __future__ import annotations
 
@@ -539,7 +541,10 @@ def run_ours(args, wl, rank, world, local_rank):
     scene.tracer.settings.mis = 1                        # stratified light samples
     scene.tracer.settings.stratify = 1
     shading = describe_shading(scene)
-    scene.tracer.settings.seed = R.view_seed(1, rank)    # one replica view per rank
+    # one image over all ranks: the same seed and view, and in step k rank r
+    # renders the sample range [(k world + r) spp, (k world + r + 1) spp) of
+    # the view's stream; the per-pixel sums are all-reduced every step
+    scene.tracer.settings.seed = R.view_seed(1, 0)
     r = runtime.Renderer(scene, lib)
     spp = W["spp"]
     width, height = scene.width, scene.height
@@ -547,13 +552,13 @@ def run_ours(args, wl, rank, world, local_rank):
     C.check(lib.er_set_stream(ctypes.c_void_p(stream.cuda_stream)))
     tuned = r.autotune(2) if not args.no_tune else None     # majorant brick and stage occupancy
     d_sum = torch.zeros((height, width, 4), dtype=torch.float32, device="cuda")
-
-    def step(k):
-        r.trace_sum_device(d_sum.data_ptr(), spp, rank, k * spp, 0, ctypes.c_void_p(stream.cuda_stream))
-
     dist = None
     if world > 1:
         import torch.distributed as dist
+
+    def step(k):
+        r.trace_sum_device(d_sum.data_ptr(), spp, 0, (k * world + rank) * spp, 0, ctypes.c_void_p(stream.cuda_stream))
+        R.sum_over_ranks(d_sum, dist)
     for k in range(args.warmup):
         step(k)
     torch.cuda.synchronize()
@@ -662,7 +667,8 @@ def run_ours(args, wl, rank, world, local_rank):
                    "autotune": tuned,
                    "l2": "inputs larger than L2 (volume %d MiB)" % (vol_bytes >> 20) if vol_bytes > (129 << 20) else
                    "volume fits in L2 (%d MiB); transport re-reads it from L2" % (vol_bytes >> 20),
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "parallelism": "sample ranges of one image per rank, per-pixel sums all-reduced each step" if world > 1
+                   else "single"},
         "roofline": roofline,
         "cpu_baseline": ({"value": cpu_rate / 1e6, "unit": "Msamples/s", "cores": cores, "kind": kind, "sample": sample}
                          if cpu_rate else None),
@@ -705,8 +711,11 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
     scenes, views, wl_name = batched_workload(wl, args.views)
     gen_s = time.perf_counter() - t_gen
     c5_vol = scenes[0].volume if wl == "c5" else None
+    # every rank renders every view, from its own sample range of each view's
+    # stream (step k, rank r: the range k world + r), and the views' sums are
+    # all-reduced each step: one set of images over all ranks
     for sc in scenes:
-        sc.tracer.settings.seed = R.view_seed(1, rank)
+        sc.tracer.settings.seed = R.view_seed(1, 0)
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -719,7 +728,13 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
             r.tracer_desc.camera = cams[0]
             r.rebind_tracer()
             tuned.append(r.autotune(2))
-    sums = [torch.zeros((cam.film_size[1], cam.film_size[0], 4), dtype=torch.float32, device="cuda") for _, cam, _ in views]
+    # the views' sums in one buffer (one all-reduce per step)
+    sizes = [cam.film_size[1] * cam.film_size[0] * 4 for _, cam, _ in views]
+    flat = torch.zeros(sum(sizes), dtype=torch.float32, device="cuda")
+    sums, o = [], 0
+    for (_, cam, _), n in zip(views, sizes):
+        sums.append(flat[o:o + n].view(cam.film_size[1], cam.film_size[0], 4))
+        o += n
     table = [(rs[k].tracer_id, spp, d.data_ptr(), cam) for (k, cam, spp), d in zip(views, sums)]
     samples_per_step = sum(cam.film_size[0] * cam.film_size[1] * spp for _, cam, spp in views)
     max_spp = max(spp for _, _, spp in views)
@@ -747,9 +762,12 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
         return a.elapsed_time(b)
 
     def step():
-        batch.advance(max_spp, sp)       # fresh samples every step
+        batch.advance(world * max_spp, sp)      # fresh samples every step
         batch.launch(sp)
+        R.sum_over_ranks(flat, dist)
 
+    if rank:
+        batch.advance(rank * max_spp, sp)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -867,7 +885,7 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
                    "autotune": tuned, "batch_autotune": batch_tune,
                    "majorant_bricks": [r.tracer_desc.settings.majorant_brick for r in rs],
                    "l2": "volumes %d MiB in total; every step renders fresh samples" % (vol_bytes >> 20),
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "parallelism": "sample ranges of every view per rank, sums all-reduced each step" if world > 1 else "single"},
         "cpu_baseline": ({"value": cpu[0] / 1e6, "unit": "Msamples/s", "cores": cpu[2], "kind": cpu[1], "sample": cpu[3]}
                          if cpu else None),
         "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": int(vol_bytes),
@@ -1054,7 +1072,7 @@ def run_medium(args, rank, world, local_rank):
                    "model": ("the tracer's transfer functions: 64-node opacity PLF (node values are parameters), colour TFs, "
                              "hybrid BRDF/phase shading (expected value over the shader choice), float intensity grid"
                              if tracer_model else "B-spline opacity (64 values), isotropic phase, float density grid"),
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "parallelism": "independent replicas (own seeds)" if world > 1 else "single"},
         "forward_ms": f_ms, "adjoint_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
         "adjoint_recompute_ms": br_ms, "adjoint_recompute_over_forward": br_ms / f_ms,
         "loss": loss, "grad_norm": {"density": float(state["g"][0].norm()), "opacity": float(state["g"][1].norm())},

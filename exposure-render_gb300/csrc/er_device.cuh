@@ -108,6 +108,9 @@ struct Params {
     /* volume (Source/volume.h:140-149) */
     const uint16_t* vox;
     const uint2* quad;       /* per voxel (x, y, z): the x/y 2x2 corner quad at z, packed uint16 pairs, or NULL */
+    int qb_nbx;              /* quads in 8^3 bricks (brick-major, x fastest inside a brick): bricks along x;
+                                0: quads x fastest over the whole volume */
+    unsigned long long qb_slab;  /* bricked quads: entries per z-slab of bricks (nbx * nby * 512) */
     int res[3];
     float minp[3];
     float inv_size[3];
@@ -165,6 +168,18 @@ struct Params {
        no ray meets the volume */
     int box_empty;
 };
+
+/* index of voxel (x, y, z)'s corner quad: x fastest over the volume, or in
+   8^3 bricks (brick-major, x fastest inside a brick) when nbx > 0, which
+   keeps a trilinear lookup's two z-slices 512 bytes apart instead of a whole
+   slice */
+__host__ __device__ __forceinline__ size_t quad_index(int x, int y, int z, int rx, int ry, int nbx, unsigned long long slab)
+{
+    if (nbx > 0)
+        return (size_t)(z >> 3) * (size_t)slab + ((size_t)(y >> 3) * (size_t)nbx + (size_t)(x >> 3)) * 512u +
+               (size_t)(((z & 7) << 6) | ((y & 7) << 3) | (x & 7));
+    return (size_t)z * (size_t)rx * (size_t)ry + (size_t)y * (size_t)rx + (size_t)x;
+}
 
 /* ------------------------------------------------------------------ */
 /* vector algebra in the order of Source/vector.h                       */

@@ -67,12 +67,10 @@ cudaError_t er_launch_dm_adjoint(const erd::Params& P, const DmParams& M, int sp
 cudaError_t er_launch_dm_majorant(const float* rho, const int res[3], int B, const float* tf, int n, const erd::Plf* plf, float scale,
                                   float margin, float floor_, float* out, cudaStream_t s);
 
-/* corner quads of a uint16 volume (8 bytes per voxel) */
-cudaError_t er_launch_quads(const uint16_t* vox, const int res[3], uint2* quad, cudaStream_t s);
-/* corner quads (quad may be NULL) and atomicMax of the voxel values over the
-   box [lo, lo + n) */
-cudaError_t er_launch_box_quads_max(const uint16_t* vox, const int res[3], const int lo[3], const int n[3], uint2* quad,
-                                    unsigned int* vmax, cudaStream_t s);
+/* corner quads (quad may be NULL; laid out by quad_index with qb_nbx,
+   qb_slab) and atomicMax of the voxel values over the box [lo, lo + n) */
+cudaError_t er_launch_box_quads_max(const uint16_t* vox, const int res[3], const int lo[3], const int n[3], uint2* quad, int qb_nbx,
+                                    unsigned long long qb_slab, unsigned int* vmax, cudaStream_t s);
 
 /* sets the text returned by er_last_error_message() on this thread */
 void er_internal_set_error(const char* message);

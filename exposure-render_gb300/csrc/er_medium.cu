@@ -256,10 +256,12 @@ ER_D void dm_shade_prepare(const Params& P, const DmParams& M, v3 Pt, Real I, co
         h.g6[2 * i] = a.rho;
         h.g6[2 * i + 1] = b.rho;
     }
-    /* Normalize(V) = V / Length(V) (Source/vector.h:469-475) */
+    /* Normalize(V) = V / Length(V) (Source/vector.h:469-475); where the grid
+       is flat the normal is undefined and the BRDF term is taken as 0 (the
+       hybrid's P_brdf is 0 there anyway) */
     const Real gx = h.g6[0] - h.g6[1], gy = h.g6[2] - h.g6[3], gz = h.g6[4] - h.g6[5];
     const Real L = dm_sqrt(gx * gx + gy * gy + gz * gz);
-    h.N[0] = gx / L; h.N[1] = gy / L; h.N[2] = gz / L;
+    if (L > (Real)0.0f) { h.N[0] = gx / L; h.N[1] = gy / L; h.N[2] = gz / L; }
     if (h.type != 2) return;
     Real sum = 0.0f;
 #pragma unroll
@@ -336,7 +338,7 @@ ER_D void dm_shade_eval(const Params& P, const DmShade<Real>& h, v3 Wo, v3 Wi, R
         Sp[c] = h.Kd[c] * (Real)ER_INV_PI_F;
         Sb[c] = 0.0f;
     }
-    if (h.type != 1) {
+    if (h.type != 1 && !(h.N[0] == (Real)0.0f && h.N[1] == (Real)0.0f && h.N[2] == (Real)0.0f)) {
         if constexpr (sizeof(Real) == sizeof(float)) {
             Shader sh;
             shader_init(sh, 0, V3(h.N[0], h.N[1], h.N[2]), Wo, C3(h.Kd[0], h.Kd[1], h.Kd[2]), C3(h.Ks[0], h.Ks[1], h.Ks[2]),

@@ -56,10 +56,20 @@ ER_D float get_intensity(const Params& P, v3 p)
     if (P.quad && vx >= 0 && vx < P.res[0] - 1 && vy >= 0 && vy < P.res[1] - 1) {
         /* the same eight corners from two 8-byte quad loads (no x/y clamping
            needed inside the volume; z clamps per corner) */
-        const size_t slice = (size_t)P.res[0] * (size_t)P.res[1];
-        const size_t xy = (size_t)vy * (size_t)P.res[0] + (size_t)vx;
-        const uint2 a = __ldg(P.quad + (size_t)iclamp(vz, 0, P.res[2] - 1) * slice + xy);
-        const uint2 b = __ldg(P.quad + (size_t)iclamp(vz + 1, 0, P.res[2] - 1) * slice + xy);
+        const int z0 = iclamp(vz, 0, P.res[2] - 1), z1 = iclamp(vz + 1, 0, P.res[2] - 1);
+        size_t i0, i1;
+        if (P.qb_nbx > 0) {
+            const size_t xy = ((size_t)(vy >> 3) * (size_t)P.qb_nbx + (size_t)(vx >> 3)) * 512u + (size_t)(((vy & 7) << 3) | (vx & 7));
+            i0 = (size_t)(z0 >> 3) * (size_t)P.qb_slab + xy + (size_t)((z0 & 7) << 6);
+            i1 = (size_t)(z1 >> 3) * (size_t)P.qb_slab + xy + (size_t)((z1 & 7) << 6);
+        } else {
+            const size_t slice = (size_t)P.res[0] * (size_t)P.res[1];
+            const size_t xy = (size_t)vy * (size_t)P.res[0] + (size_t)vx;
+            i0 = (size_t)z0 * slice + xy;
+            i1 = (size_t)z1 * slice + xy;
+        }
+        const uint2 a = __ldg(P.quad + i0);
+        const uint2 b = __ldg(P.quad + i1);
         const float q00 = lerp_u16(dx, (float)(a.x & 0xffffu), (float)(a.x >> 16));
         const float q10 = lerp_u16(dx, (float)(a.y & 0xffffu), (float)(a.y >> 16));
         const float q01 = lerp_u16(dx, (float)(b.x & 0xffffu), (float)(b.x >> 16));

@@ -167,6 +167,8 @@ struct VolumeItem {
     uint64_t edits = 0;            /* region edits from device voxels (folded into the signature) */
     DevBuf<uint16_t> vox;
     DevBuf<uint2> quad;            /* corner quads (NULL when they do not fit in memory) */
+    int qb_nbx = 0;                /* quads in 8^3 bricks: bricks along x (0: x fastest) */
+    unsigned long long qb_slab = 0;
     DevBuf<unsigned int> gm_max_bits;
     DevBuf<unsigned int> box_max;  /* largest voxel of an uploaded box */
     float gm_max = -1.0f;          /* lazily computed maximum gradient magnitude */
@@ -362,6 +364,8 @@ void volume_geometry(const VolumeItem& v, erd::Params& P)
     P.min_step = smin_h(sp[0], smin_h(sp[1], sp[2]));
     P.vox = v.vox.p;
     P.quad = v.quad.p;
+    P.qb_nbx = v.qb_nbx;
+    P.qb_slab = v.qb_slab;
 }
 
 /* Camera::Update - Source/camera.h:61-96 */
@@ -1122,7 +1126,7 @@ er_status upload_box(VolumeItem& v, const int lo[3], const int n[3], const uint1
     int qn[3] = { n[0] + (lo[0] - qlo[0]), n[1] + (lo[1] - qlo[1]), n[2] };
     ER_CUDA(v.box_max.ensure(1));
     ER_CUDA(cudaMemsetAsync(v.box_max.p, 0, sizeof(unsigned int), s));
-    ER_CUDA(er_launch_box_quads_max(v.vox.p, v.res, qlo, qn, v.quad.p, v.box_max.p, s));
+    ER_CUDA(er_launch_box_quads_max(v.vox.p, v.res, qlo, qn, v.quad.p, v.qb_nbx, v.qb_slab, v.box_max.p, s));
     ER_CUDA(cudaMemcpyAsync(box_max, v.box_max.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
     ER_CUDA(cudaStreamSynchronize(s));
     return ER_OK;
@@ -1162,9 +1166,18 @@ ER_API er_status er_bind_volume(const er_volume_desc* d, int32_t* id)
         fresh.reset(new VolumeItem());
         v = fresh.get();
         ER_CUDA(v->vox.ensure(n));
-        /* corner quads for the transport's lookups; without room for them the
+        /* corner quads for the transport's lookups, x fastest or (environment
+           ER_QUAD_LAYOUT=bricked) in 8^3 bricks; without room for them the
            kernels read the plain voxels (same values, more loads) */
-        if (v->quad.ensure(n) != cudaSuccess) cudaGetLastError();
+        const char* layout = getenv("ER_QUAD_LAYOUT");
+        size_t nq = n;
+        if (layout && strcmp(layout, "bricked") == 0) {
+            const int nb[3] = { (d->resolution[0] + 7) / 8, (d->resolution[1] + 7) / 8, (d->resolution[2] + 7) / 8 };
+            v->qb_nbx = nb[0];
+            v->qb_slab = (unsigned long long)nb[0] * (unsigned long long)nb[1] * 512ull;
+            nq = (size_t)v->qb_slab * (size_t)nb[2];
+        }
+        if (v->quad.ensure(nq) != cudaSuccess) cudaGetLastError();
     }
     for (int i = 0; i < 3; i++) { v->res[i] = d->resolution[i]; v->spacing[i] = d->spacing[i]; }
     v->normalize = d->normalize_size;

@@ -151,32 +151,13 @@ cudaError_t er_launch_empty_skip(float* majorant, const int nb[3], uint8_t* tmp,
 
 /* corner quads: for voxel (x, y, z) the intensities at (x, y), (x+1, y),
    (x, y+1), (x+1, y+1) of slice z, packed as two uint16 pairs, so that a
-   trilinear lookup reads two 8-byte words instead of eight 2-byte ones */
-__global__ void k_quads(const uint16_t* __restrict__ vox, int rx, int ry, int rz, uint2* __restrict__ quad)
-{
-    const size_t n = (size_t)rx * ry * rz;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const int x = (int)(i % rx), y = (int)((i / rx) % ry);
-        const size_t z0 = i - (size_t)y * rx - x;
-        const int x1 = x + 1 < rx ? x + 1 : rx - 1, y1 = y + 1 < ry ? y + 1 : ry - 1;
-        const uint32_t v00 = vox[z0 + (size_t)y * rx + x], v10 = vox[z0 + (size_t)y * rx + x1];
-        const uint32_t v01 = vox[z0 + (size_t)y1 * rx + x], v11 = vox[z0 + (size_t)y1 * rx + x1];
-        quad[i] = make_uint2(v00 | (v10 << 16), v01 | (v11 << 16));
-    }
-}
-
-cudaError_t er_launch_quads(const uint16_t* vox, const int res[3], uint2* quad, cudaStream_t s)
-{
-    k_quads<<<2048, 256, 0, s>>>(vox, res[0], res[1], res[2], quad);
-    return cudaGetLastError();
-}
-
-/* the corner quads of the voxels in the box [lo, lo + n) (a region edit
-   changes the quads of the voxels one below it in x and y as well) and the
-   largest voxel value in the box */
+   trilinear lookup reads two 8-byte words instead of eight 2-byte ones;
+   stored x fastest or in 8^3 bricks (quad_index, er_device.cuh).  This
+   kernel writes the quads of the voxels in the box [lo, lo + n) (a region
+   edit changes the quads of the voxels one below it in x and y as well) and
+   finds the largest voxel value in the box. */
 __global__ void k_box_quads_max(const uint16_t* __restrict__ vox, int rx, int ry, int x0, int y0, int z0, int nx, int ny, int nz,
-                                uint2* __restrict__ quad, unsigned int* __restrict__ vmax)
+                                uint2* __restrict__ quad, int qb_nbx, unsigned long long qb_slab, unsigned int* __restrict__ vmax)
 {
     const size_t n = (size_t)nx * ny * nz;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -187,7 +168,7 @@ __global__ void k_box_quads_max(const uint16_t* __restrict__ vox, int rx, int ry
         const int x1 = x + 1 < rx ? x + 1 : rx - 1, y1 = y + 1 < ry ? y + 1 : ry - 1;
         const uint32_t v00 = vox[zb + (size_t)y * rx + x], v10 = vox[zb + (size_t)y * rx + x1];
         const uint32_t v01 = vox[zb + (size_t)y1 * rx + x], v11 = vox[zb + (size_t)y1 * rx + x1];
-        if (quad) quad[zb + (size_t)y * rx + x] = make_uint2(v00 | (v10 << 16), v01 | (v11 << 16));
+        if (quad) quad[erd::quad_index(x, y, z, rx, ry, qb_nbx, qb_slab)] = make_uint2(v00 | (v10 << 16), v01 | (v11 << 16));
         m = v00 > m ? v00 : m;
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -197,14 +178,15 @@ __global__ void k_box_quads_max(const uint16_t* __restrict__ vox, int rx, int ry
     if ((threadIdx.x & 31) == 0 && m) atomicMax(vmax, m);
 }
 
-cudaError_t er_launch_box_quads_max(const uint16_t* vox, const int res[3], const int lo[3], const int n[3], uint2* quad,
-                                    unsigned int* vmax, cudaStream_t s)
+cudaError_t er_launch_box_quads_max(const uint16_t* vox, const int res[3], const int lo[3], const int n[3], uint2* quad, int qb_nbx,
+                                    unsigned long long qb_slab, unsigned int* vmax, cudaStream_t s)
 {
     const size_t total = (size_t)n[0] * n[1] * n[2];
     if (total == 0) return cudaSuccess;
     size_t blocks = (total + 255) / 256;
     if (blocks > 4096) blocks = 4096;
-    k_box_quads_max<<<(unsigned)blocks, 256, 0, s>>>(vox, res[0], res[1], lo[0], lo[1], lo[2], n[0], n[1], n[2], quad, vmax);
+    k_box_quads_max<<<(unsigned)blocks, 256, 0, s>>>(vox, res[0], res[1], lo[0], lo[1], lo[2], n[0], n[1], n[2], quad, qb_nbx, qb_slab,
+                                                     vmax);
     return cudaGetLastError();
 }
 

@@ -2504,7 +2504,12 @@ static void dm_shade_prepare(or_scene* s, v3 P, const dm_lookup* k, const dm_tf*
         dm_density(s, vsub(P, d[i]), &h->g[2 * i]);
         dm_density(s, vadd(P, d[i]), &h->g[2 * i + 1]);
     }
-    h->N = vnorm(V3(h->g[0].rho - h->g[1].rho, h->g[2].rho - h->g[3].rho, h->g[4].rho - h->g[5].rho));
+    /* Normalize(V) = V / Length(V) (Source/vector.h:469-475); where the
+       grid is flat the normal is undefined and the BRDF term is taken as 0
+       (the hybrid's P_brdf is 0 there anyway) */
+    const v3 gv = V3(h->g[0].rho - h->g[1].rho, h->g[2].rho - h->g[3].rho, h->g[4].rho - h->g[5].rho);
+    const float L = vlen(gv);
+    if (L > 0.0f) h->N = V3(gv.x / L, gv.y / L, gv.z / L);
     if (h->type != 2) return;
     float sum = 0.0f;
     for (int i = 0; i < 3; i++) {
@@ -2525,7 +2530,7 @@ static col3 dm_shade_eval(const or_scene* s, const dm_shade_t* h, v3 Wo, v3 Wi, 
 {
     const col3 Sp = cscale(h->Kd, INV_PI_F);
     col3 Sb = C3(0.0f, 0.0f, 0.0f);
-    if (h->type != 1) {
+    if (h->type != 1 && !(h->N.x == 0.0f && h->N.y == 0.0f && h->N.z == 0.0f)) {
         shader_t sh;
         shader_init(&sh, 0, h->N, Wo, h->Kd, h->Ks, dm_ior(s), h->e);
         Sb = cscale(shader_f(&sh, Wo, Wi), vabsdot(Wi, h->N));
