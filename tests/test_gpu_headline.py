@@ -215,3 +215,27 @@ def test_majorant_grid_beyond_2e30_bricks(torch, lib, big_volume):
         nonempty = expect > 0.0
         assert np.array_equal(got[nonempty], expect[nonempty]), f"slab {z}"
         assert (got[~nonempty] <= 0.0).all(), f"slab {z}"
+
+
+def test_c2_bricked_quad_layout(torch, lib, runtime, oracle, c2, monkeypatch):
+    """The corner quads in 8^3 bricks (ER_QUAD_LAYOUT=bricked at bind time)
+    read the same intensities: the c2 fast path's crops stay bit-exact, and
+    the whole film equals the x-fastest layout's"""
+    sc = S.Scene(c2.name, c2.volume, tracer=C.er_tracer_desc.from_buffer_copy(c2.tracer), lights=c2.lights, textures=c2.textures)
+    s = sc.tracer.settings
+    s.free_flight, s.mis, s.stratify, s.majorant_brick = 1, 1, 1, 8
+    r = runtime.Renderer(sc, lib)
+    try:
+        flat = dev_sum(torch, r, 2, view=4)
+    finally:
+        r.close()
+    monkeypatch.setenv("ER_QUAD_LAYOUT", "bricked")
+    r = runtime.Renderer(sc, lib)
+    h = OL.SceneHandle(oracle, sc)
+    try:
+        bricked = dev_sum(torch, r, 2, view=4)
+        assert np.array_equal(bits(bricked), bits(flat))
+        compare_crops(bricked, h, 2, C2_CROPS[:2], view=4)
+    finally:
+        r.close()
+        h.close()
