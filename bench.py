@@ -982,6 +982,43 @@ def c5_adjoint(args, lib, runtime, torch, stream, vol, film=(2048, 2048), spp=8,
     return out
 
 
+def medium_cpu_rate(sc, rho, tf, m, seconds_target=10.0):
+    """forward samples/s of the same differentiable estimator in the CPU
+    oracle (the reference has no differentiable path; kind "port"), all host
+    threads, on a film crop of the workload's camera (the oracle renders
+    whole films: the camera's film is shrunk, which keeps the field of view),
+    with the forward+adjoint time ratio of the same run"""
+    import copy
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as OL
+    C = importlib.import_module("exposure-render_gb300.capi")
+    orc = OL.load_oracle()
+    nthreads = os.cpu_count() or 1
+    maj = m.majorant.cpu().numpy()
+
+    def run(side, spp):
+        s2 = copy.copy(sc)
+        s2.tracer = C.er_tracer_desc.from_buffer_copy(sc.tracer)
+        s2.tracer.camera.film_size[0] = s2.tracer.camera.film_size[1] = side
+        h = OL.MediumHandle(orc, s2, rho, tf, m.scale, np.array(m.albedo), m.q, maj, m.brick, model=m.model, gm_inv=m.gm_inv)
+        t0 = time.perf_counter()
+        img, smp = h.render(spp, keep_samples=True, nthreads=nthreads)
+        t1 = time.perf_counter()
+        h.adjoint(spp, np.ones_like(img) * 1e-3, smp, nthreads=nthreads)
+        t2 = time.perf_counter()
+        h.close()
+        return side * side * spp / max(t1 - t0, 1e-6), (t2 - t1) / max(t1 - t0, 1e-6)
+
+    side = 32
+    rate, _ = run(side, 2)
+    side = int(max(32, min(256, np.sqrt(rate * seconds_target / 4.0))))
+    rate, ratio = run(side, 4)
+    return {"value": rate / 1e6, "unit": "Msamples/s", "cores": nthreads, "kind": "port",
+            "sample": "%dx%d film of the workload's camera x 4 spp, forward (the oracle's float restatement of the same "
+                      "estimator; the reference has no differentiable path)" % (side, side),
+            "adjoint_over_forward": ratio}
+
+
 def run_medium(args, rank, world, local_rank):
     """c4: the differentiable tracer model (ER_MEDIUM_TRACER: the tracer's
     64-node opacity PLF with its node values as parameters, its colour
@@ -1063,6 +1100,7 @@ def run_medium(args, rank, world, local_rank):
     loss = float(((state["s"] / spp - target) ** 2).mean())
     if rank != 0:
         return
+    cpu = medium_cpu_rate(sc, rho_np, tf.cpu().numpy(), m) if world == 1 else None
     line = {
         "metric": "Msamples/s", "value": R.whole_job_rate(samples, f_ms / 1e3, world) / 1e6, "unit": "Msamples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": f_ms + b_ms, "higher_is_better": True, "scaling": "weak",
@@ -1076,6 +1114,7 @@ def run_medium(args, rank, world, local_rank):
         "forward_ms": f_ms, "adjoint_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
         "adjoint_recompute_ms": br_ms, "adjoint_recompute_over_forward": br_ms / f_ms,
         "loss": loss, "grad_norm": {"density": float(state["g"][0].norm()), "opacity": float(state["g"][1].norm())},
+        "cpu_baseline": cpu,
         "clocks": clk.summary(),
         # per window of 2^21 items: forward count, jobs, shadow, gather (+ one reduce per step);
         # adjoint count, jobs, shadow, primary replay, shadow replay
