@@ -298,7 +298,7 @@ def convergence(lib, runtime, torch, names, patches, max_spp=4096, target=1e-2):
 FILM_SCHEDULE = (8, 16, 32, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048)
 
 
-def film_convergence(lib, torch, r, patches, ref_patch, ref_spp, target=1e-2, budget_s=45.0, stream=None):
+def film_convergence(lib, torch, r, patches, ref_patch, ref_spp, target=1e-2, budget_s=45.0, stream=None, film=None):
     """Samples per pixel to image RMSE `target` at the workload's own film.
 
     The converged image is the unbiased estimator (`ref_patch`: delta
@@ -309,10 +309,12 @@ def film_convergence(lib, torch, r, patches, ref_patch, ref_spp, target=1e-2, bu
     oracle is checked on 128^2 views of the same workloads
     (tests/test_gpu_convergence.py, and `fp64_128` below).  Each
     configuration of `patches` then renders from view 0 along FILM_SCHEDULE
-    until its RMSE reaches `target` (or `budget_s` of rendering is spent)."""
+    until its RMSE reaches `target` (or `budget_s` of rendering is spent).
+    `film`: (W, H) of the bound tracer's camera when it differs from the
+    scene's."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import convergence as CV
-    W, H = r.width, r.height
+    W, H = film if film else (r.width, r.height)
     d = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
 
     def apply(patch):
@@ -409,7 +411,9 @@ def batched_rmse_summary(conv, value, plain_value, target=1e-2):
     for name, c in conv.items():
         f, p = c["fast"]["spp_to_target"], c["plain"]["spp_to_target"]
         per[name] = {"fast_spp": f, "plain_spp": p, "plain_rmse_at_max_spp": c["plain"]["rmse"][-1],
-                     "reference_noise": c["reference_noise"]}
+                     "reference_noise": c["reference_noise"] if "reference_noise" in c else c["reference"]["noise"]}
+        if "reference" in c and isinstance(c["reference"], dict):
+            per[name]["film"] = c["reference"]["film"]
         if f and p:
             ratios.append(p / f)
     out = {"target": target, "views": per, "throughput_ratio": value / plain_value}
@@ -824,11 +828,24 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
     del plain_sum
     plain_value = plain_samples / (plain_ms / 1e3) / 1e6
 
-    # equal-RMSE comparison on the first view of each volume (128^2, FP64 references)
-    conv = None
+    # equal-RMSE comparison on the first view of each volume: at 128^2 against
+    # the FP64 references, and at each view's own film against a converged
+    # GPU render of the unbiased estimator
+    conv, film_conv = None, None
     if world == 1 and not args.no_rmse and wl == "c3":
         conv = convergence(lib, runtime, torch, ["c3v0", "c3v1", "c3v2"],
                            {"fast": {"free_flight": 1, "stratify": 1}, "plain": {"free_flight": 0, "stratify": 0}})
+        film_conv = {}
+        for k, r in enumerate(rs):
+            cam = [c for (kk, c, _) in views if kk == k][0]
+            saved = C.er_tracer_desc.from_buffer_copy(r.tracer_desc)
+            r.tracer_desc.camera = cam
+            r.rebind_tracer()
+            film_conv["c3v%d" % k] = film_convergence(
+                lib, torch, r, {"fast": {"free_flight": 1, "stratify": 1}, "plain": {"free_flight": 0, "stratify": 0}},
+                {"free_flight": 1, "stratify": 0}, 8192, budget_s=30.0, stream=sp, film=(cam.film_size[0], cam.film_size[1]))
+            ctypes.memmove(ctypes.byref(r.tracer_desc), ctypes.byref(saved), ctypes.sizeof(saved))
+            r.rebind_tracer()
 
     # end to end with host buffers: volumes bound from host memory, one batch
     # launch, every view's sums read back into pinned host memory
@@ -900,8 +917,10 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
         "plain": {"value": plain_value, "unit": "Msamples/s", "speedup": value / plain_value, "views": n_plain,
                   "what": "same estimator with the fixed-step march and no stratification, each view's full spp in one "
                           "er_trace_sum_device call, one view at a time"},
-        "equal_rmse": batched_rmse_summary(conv, value, plain_value) if wl == "c3" else
+        "equal_rmse": batched_rmse_summary(film_conv, value, plain_value) if wl == "c3" else
         {"throughput_ratio": value / plain_value, "note": "no FP64 reference of the c5 volume: samples-to-RMSE ratios are measured on c2 and c3"},
+        "equal_rmse_fp64_128": (dict(batched_rmse_summary(conv, value, plain_value) or {},
+                                     note="samples to RMSE 1e-2 on 128^2 views against the FP64 oracle") if conv else None),
     }
     if wl == "c5":
         line["volume_generation_s"] = gen_s
