@@ -56,12 +56,15 @@ struct DmParams {
     int emissive;        /* model 1: the tracer's emission TF is not zero everywhere */
     float gm_inv;        /* model 1, hybrid: 1 / gradient-magnitude range (a constant) */
 };
+/* key: nonzero name of the walk (tracer build, medium, spp, view, first
+   sample); an adjoint with the key and stream of the last one-window call
+   replays against that call's kept shadow jobs */
 cudaError_t er_launch_dm_forward(const erd::Params& P, const DmParams& M, int spp, uint32_t view, uint32_t first, float* samples,
-                                 float* sum, cudaStream_t s);
+                                 float* sum, uint64_t key, cudaStream_t s);
 cudaError_t er_launch_dm_forward64(const erd::Params& P, const DmParams& M, int spp, uint32_t view, uint32_t first, double* samples,
                                    double* sum, cudaStream_t s);
 cudaError_t er_launch_dm_adjoint(const erd::Params& P, const DmParams& M, int spp, uint32_t view, uint32_t first, const float* dimg,
-                                 const float* fwd, float* g_rho, float* g_tf, cudaStream_t s);
+                                 const float* fwd, float* g_rho, float* g_tf, uint64_t key, cudaStream_t s);
 /* plf: NULL for model 0 (B-spline values tf); model 1: the tracer's opacity
    PLF (device), whose node values are tf */
 cudaError_t er_launch_dm_majorant(const float* rho, const int res[3], int B, const float* tf, int n, const erd::Plf* plf, float scale,

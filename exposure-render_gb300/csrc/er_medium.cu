@@ -1064,6 +1064,11 @@ struct DmWorkspace {
     uint32_t *off = nullptr, *cnt = nullptr, *total = nullptr, *host_total = nullptr;
     float4* E = nullptr;       /* model 1: per item emission sums */
     size_t cap = 0, item_cap = 0;
+    /* the call whose jobs the arrays hold (dm_windows): 0 = none, or not
+       reusable (several windows, or a failed call) */
+    uint64_t key = 0;
+    cudaStream_t key_stream = nullptr;
+    uint32_t kept_jobs = 0;    /* the kept walk's job count */
     ~DmWorkspace()
     {
         cudaFree(P); cudaFree(S); cudaFree(A); cudaFree(id); cudaFree(off); cudaFree(cnt); cudaFree(total); cudaFree(E);
@@ -1115,9 +1120,14 @@ static DmWorkspace& dm_workspace()
 
 /* the four forward stages (and the two adjoint stages when dimg != NULL)
    over windows of whole sample rows; synchronises once per window to size
-   the job storage */
+   the job storage.  key (nonzero) names the walk: tracer build, medium
+   buffers and values, spp, view, first sample.  When the whole call is one
+   window, the job arrays keep that walk's jobs after the call; an adjoint
+   whose key and stream match the last call's skips the count, jobs and
+   shadow stages and replays against the kept jobs (the same kernels would
+   write the same jobs, in an order only the slot atomics decide). */
 static cudaError_t dm_windows(const Params& P, const DmParams& M, int spp, uint32_t view, uint32_t first, float* samples,
-                              const float* dimg, float* g_rho, float* g_tf, cudaStream_t s)
+                              const float* dimg, float* g_rho, float* g_tf, uint64_t key, cudaStream_t s)
 {
     DmWorkspace& ws = dm_workspace();
     const uint32_t npix = (uint32_t)P.film[0] * (uint32_t)P.film[1];
@@ -1125,6 +1135,9 @@ static cudaError_t dm_windows(const Params& P, const DmParams& M, int spp, uint3
     if (rows < 1) rows = 1;
     cudaError_t e = ws.ensure_items((size_t)rows * npix);
     if (e != cudaSuccess) return e;
+    const bool one_window = (uint32_t)spp <= rows;
+    const bool reuse = dimg && one_window && key != 0 && ws.key == key && ws.key_stream == s;
+    ws.key = 0;
     for (uint32_t s0 = 0; s0 < (uint32_t)spp; s0 += rows) {
         DmWindow W;
         W.npix = npix;
@@ -1136,19 +1149,23 @@ static cudaError_t dm_windows(const Params& P, const DmParams& M, int spp, uint3
         J.P = ws.P; J.S = ws.S; J.A = ws.A; J.id = ws.id; J.off = ws.off; J.cnt = ws.cnt; J.total = ws.total;
         J.E = M.model == 1 ? ws.E : nullptr;
         J.cap = (uint32_t)ws.cap;
-        if ((e = cudaMemsetAsync(ws.total, 0, sizeof(uint32_t), s)) != cudaSuccess) return e;
-        if (M.model == 1) k_dm_count<1><<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
-        else k_dm_count<0><<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
-        if ((e = cudaMemcpyAsync(ws.host_total, ws.total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
-        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-        const uint32_t njobs = *ws.host_total;
-        if ((e = ws.ensure_jobs(njobs)) != cudaSuccess) return e;
-        J.P = ws.P; J.S = ws.S; J.A = ws.A; J.id = ws.id; J.cap = (uint32_t)ws.cap;
         const uint64_t base = (uint64_t)s0 * npix;
-        if (M.model == 1) k_dm_jobs<1><<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
-        else k_dm_jobs<0><<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
-        if (njobs && M.model == 1) k_dm_shadow<1><<<grid_for(njobs, 16), 256, 0, s>>>(P, M, W, J);
-        else if (njobs) k_dm_shadow<0><<<grid_for(njobs, 16), 256, 0, s>>>(P, M, W, J);
+        uint32_t njobs = ws.kept_jobs;
+        if (!reuse) {
+            if ((e = cudaMemsetAsync(ws.total, 0, sizeof(uint32_t), s)) != cudaSuccess) return e;
+            if (M.model == 1) k_dm_count<1><<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
+            else k_dm_count<0><<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
+            if ((e = cudaMemcpyAsync(ws.host_total, ws.total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
+            if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+            njobs = *ws.host_total;
+            if ((e = ws.ensure_jobs(njobs)) != cudaSuccess) return e;
+            J.P = ws.P; J.S = ws.S; J.A = ws.A; J.id = ws.id; J.cap = (uint32_t)ws.cap;
+            if (M.model == 1) k_dm_jobs<1><<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
+            else k_dm_jobs<0><<<grid_for(W.items, 16), 256, 0, s>>>(P, M, W, J);
+            if (njobs && M.model == 1) k_dm_shadow<1><<<grid_for(njobs, 16), 256, 0, s>>>(P, M, W, J);
+            else if (njobs) k_dm_shadow<0><<<grid_for(njobs, 16), 256, 0, s>>>(P, M, W, J);
+            ws.kept_jobs = njobs;
+        }
         if (!dimg || samples) {
             /* forward values: written by the forward, read by the adjoint */
             if (!dimg) k_dm_gather<<<(W.items + 255) / 256, 256, 0, s>>>(W, J, base, samples);
@@ -1161,13 +1178,17 @@ static cudaError_t dm_windows(const Params& P, const DmParams& M, int spp, uint3
         }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
+    if (one_window && key != 0) {
+        ws.key = key;
+        ws.key_stream = s;
+    }
     return cudaSuccess;
 }
 
 cudaError_t er_launch_dm_forward(const Params& P, const DmParams& M, int spp, uint32_t view, uint32_t first, float* samples,
-                                 float* sum, cudaStream_t s)
+                                 float* sum, uint64_t key, cudaStream_t s)
 {
-    cudaError_t e = dm_windows(P, M, spp, view, first, samples, nullptr, nullptr, nullptr, s);
+    cudaError_t e = dm_windows(P, M, spp, view, first, samples, nullptr, nullptr, nullptr, key, s);
     if (e != cudaSuccess) return e;
     const uint32_t npix = (uint32_t)P.film[0] * (uint32_t)P.film[1];
     if (sum) k_dm_reduce<<<(npix + 255) / 256, 256, 0, s>>>(samples, spp, npix, sum);
@@ -1187,7 +1208,7 @@ cudaError_t er_launch_dm_forward64(const Params& P, const DmParams& M, int spp, 
 /* fwd: the forward samples (spp * npix * 3); without them a scratch buffer
    receives the recomputed values window by window */
 cudaError_t er_launch_dm_adjoint(const Params& P, const DmParams& M, int spp, uint32_t view, uint32_t first, const float* dimg,
-                                 const float* fwd, float* g_rho, float* g_tf, cudaStream_t s)
+                                 const float* fwd, float* g_rho, float* g_tf, uint64_t key, cudaStream_t s)
 {
     float* samples = const_cast<float*>(fwd);
     float* scratch = nullptr;
@@ -1195,11 +1216,11 @@ cudaError_t er_launch_dm_adjoint(const Params& P, const DmParams& M, int spp, ui
     if (!fwd) {
         cudaError_t e = cudaMallocAsync(&scratch, (size_t)spp * npix * 3 * sizeof(float), s);
         if (e != cudaSuccess) return e;
-        e = dm_windows(P, M, spp, view, first, scratch, nullptr, nullptr, nullptr, s);
+        e = dm_windows(P, M, spp, view, first, scratch, nullptr, nullptr, nullptr, key, s);
         if (e != cudaSuccess) { cudaFreeAsync(scratch, s); return e; }
         samples = scratch;
     }
-    cudaError_t e = dm_windows(P, M, spp, view, first, samples, dimg, g_rho, g_tf, s);
+    cudaError_t e = dm_windows(P, M, spp, view, first, samples, dimg, g_rho, g_tf, key, s);
     if (scratch) cudaFreeAsync(scratch, s);
     return e;
 }

@@ -989,26 +989,61 @@ ER_D float dda_majorant(const Params& P, const Dda& d)
 
 #define ER_DELTA_MAX_COLLISIONS 1048576
 
-/* Empty-space skip.  An empty brick of the tracker's majorant grid holds
+/* Empty-space jump.  An empty brick of the tracker's majorant grid holds
    -k, k the Chebyshev distance in bricks to the nearest non-empty brick
-   (er_volume.cu k_skip_pass), so every brick within k-1 of it is empty.
-   dda_skip steps the DDA through that cube of empty bricks without reading
-   their majorants: each step is the exit and advance that brick-by-brick
-   tracking makes in an empty brick (which draws nothing and leaves tau
-   alone), so the DDA leaves the cube with exactly the face times and brick
-   indices of plain stepping and renders are bit-identical with or without
-   the skip; only the dependent majorant loads are saved. */
-ER_D void dda_skip(const Params& P, Dda& d, int k, float e)
+   (er_volume.cu k_skip_pass), so the cube of bricks within k-1 of it is
+   empty: nothing is drawn and tau is unchanged while the ray crosses it.
+   dda_jump moves the DDA to the cube's exit in one step.  The exit face of
+   each axis is k-1 bricks past its next face (time next + (k-1) * delta);
+   the earliest of the three (ties to x, then y, as dda_advance) is the exit
+   time te, that axis moves k bricks, and each other axis moves past the m
+   faces it crosses before te, m = floor((te - next) / delta) + 1 (at most
+   k).  The oracle makes the same float operations (oracle/er_oracle.c
+   dda_jump), so the face times after a jump are those of the oracle, not
+   those of k-1 brick-by-brick advances (a sum of deltas rounds
+   differently); the segment [t, te] lies in empty bricks either way. */
+ER_D void dda_jump(const Params& P, Dda& d, int k)
 {
-    const int x0 = d.bx, y0 = d.by, z0 = d.bz, r = k - 1;
-    dda_advance(P, d, e);
-    while (!d.done && abs(d.bx - x0) <= r && abs(d.by - y0) <= r && abs(d.bz - z0) <= r) dda_advance(P, d, dda_exit(d));
+    const float r = (float)(k - 1);
+    const float fx = d.sx != 0 ? d.nx + r * d.dx : FLT_MAX;
+    const float fy = d.sy != 0 ? d.ny + r * d.dy : FLT_MAX;
+    const float fz = d.sz != 0 ? d.nz + r * d.dz : FLT_MAX;
+    const bool ax = !(fy < fx) && !(fz < fx);
+    const bool ay = !ax && !(fz < fy);
+    const float te = ax ? fx : (ay ? fy : fz);
+    if (te >= d.tmax) { d.done = true; d.t = te; return; }
+    int m;
+    if (ax) { d.bx += d.sx * k; d.nx = fx + d.dx; }
+    else if (d.nx < te) {
+        m = (int)((te - d.nx) / d.dx) + 1;
+        m = m > k ? k : m;
+        d.bx += d.sx * m;
+        d.nx = d.nx + (float)m * d.dx;
+    }
+    if (ay) { d.by += d.sy * k; d.ny = fy + d.dy; }
+    else if (d.ny < te) {
+        m = (int)((te - d.ny) / d.dy) + 1;
+        m = m > k ? k : m;
+        d.by += d.sy * m;
+        d.ny = d.ny + (float)m * d.dy;
+    }
+    if (!ax && !ay) { d.bz += d.sz * k; d.nz = fz + d.dz; }
+    else if (d.nz < te) {
+        m = (int)((te - d.nz) / d.dz) + 1;
+        m = m > k ? k : m;
+        d.bz += d.sz * m;
+        d.nz = d.nz + (float)m * d.dz;
+    }
+    if (d.bx < 0 || d.bx >= P.nb[0] || d.by < 0 || d.by >= P.nb[1] || d.bz < 0 || d.bz >= P.nb[2]) d.done = true;
+    d.t = te;
 }
 
 /* Delta tracking of the primary ray: sigma_t = DensityScale^2 * Opacity(I),
    the extinction the reference's march integrates (Source/raymarching.h:45,64-66) */
-/* SKIP: compile the empty-space skip (a grid without skip distances reads
-   the same either way; the variant without it needs fewer registers) */
+/* SKIP: compile the empty-space jump.  Every delta-tracking caller passes
+   true (the tracker's grid carries skip distances, and the jump sets the
+   face times the tracker continues from); false compiles the stages of the
+   fixed-step march, which never run this tracker, with fewer registers. */
 template <bool WITH_NORMAL = true, bool SKIP = true>
 ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE, float u0 = -1.0f)
 {
@@ -1051,7 +1086,7 @@ ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE
                 tau = -er_logf(rng.get1());
             }
         } else if (SKIP && mu <= -2.0f) {
-            dda_skip(P, d, (int)(-mu), e);
+            dda_jump(P, d, (int)(-mu));
             continue;
         }
         dda_advance(P, d, e);
@@ -1111,7 +1146,7 @@ ER_D void delta_step(const Params& P, const Ray& R, Rng& rng, DeltaTracker& k)
         k.tau = k.tau - k.mu * (k.e - k.t);
         if (k.tau < 0.0f) k.tau = 0.0f;
     } else if (SKIP && k.mu <= -2.0f) {
-        dda_skip(P, k.d, (int)(-k.mu), k.e);
+        dda_jump(P, k.d, (int)(-k.mu));
         k.in_brick = false;
         if (k.d.done) k.done = true;
         return;
@@ -1181,7 +1216,7 @@ ER_D void ratio_step(const Params& P, const Ray& R, Rng& rng, RatioTracker& k)
         k.tau = k.tau - k.mu * (k.e - k.t);
         if (k.tau < 0.0f) k.tau = 0.0f;
     } else if (SKIP && k.mu <= -2.0f) {
-        dda_skip(P, k.d, (int)(-k.mu), k.e);
+        dda_jump(P, k.d, (int)(-k.mu));
         k.in_brick = false;
         if (k.d.done) k.done = true;
         return;
@@ -1232,7 +1267,7 @@ ER_D float transmittance_ratio(const Params& P, const Ray& R, Rng& rng)
                 tau = -er_logf(rng.get1());
             }
         } else if (SKIP && mu <= -2.0f) {
-            dda_skip(P, d, (int)(-mu), e);
+            dda_jump(P, d, (int)(-mu));
             continue;
         }
         dda_advance(P, d, e);

@@ -207,6 +207,7 @@ struct TracerItem {
     DevBuf<float4> tune_sum;       /* probe renders of the autotuner */
     erd::Params P;
     uint64_t built_version = 0;
+    uint64_t build_serial = 0;     /* distinct for every build of any tracer */
     bool built = false;
 };
 
@@ -423,11 +424,15 @@ er_status init_lanes(TracerItem& t)
     return ER_OK;
 }
 
-/* which tracking stages run persistent lanes (ER_PERSISTENT_*; delta tracking only) */
+/* which tracking stages run persistent lanes (ER_PERSISTENT_*; delta
+   tracking only).  Delta-tracking stages always compile the empty-space
+   jump: it sets the face times the tracker continues from, so every path
+   (and the oracle) takes it; the ER_TUNE_NO_SKIP_* bits are accepted and
+   ignored. */
 void persistent_stages(int mode, bool all_delta, WavefrontBuffers& B)
 {
-    B.skip_primary = all_delta && !(mode & ER_TUNE_NO_SKIP_PRIMARY);
-    B.skip_shadow = all_delta && !(mode & ER_TUNE_NO_SKIP_SHADOW);
+    B.skip_primary = all_delta;
+    B.skip_shadow = all_delta;
     mode &= 3;
     B.pt_primary = all_delta && (mode == ER_PERSISTENT_BOTH || mode == ER_PERSISTENT_PRIMARY);
     B.pt_shadow = all_delta && (mode == ER_PERSISTENT_SHADOW || mode == ER_PERSISTENT_BOTH);
@@ -686,6 +691,8 @@ er_status build(TracerItem& t)
     t.P = P;
     t.built = true;
     t.built_version = C.version;
+    static uint64_t serial = 0;
+    t.build_serial = ++serial;
     return ER_OK;
 }
 
@@ -1678,10 +1685,8 @@ ER_API er_status er_batch_autotune(int32_t batch_id, void* stream, int32_t* tune
         t->built = false;
         ctx().version++;
     }
-    /* then the tracking stages' persistent-lane mode and empty-space skips */
-    const int candidates[] = {ER_PERSISTENT_BOTH, ER_PERSISTENT_BOTH | ER_TUNE_NO_SKIP_SHADOW, ER_PERSISTENT_BOTH | ER_TUNE_NO_SKIP,
-                              ER_PERSISTENT_SHADOW, ER_PERSISTENT_SHADOW | ER_TUNE_NO_SKIP_SHADOW, ER_PERSISTENT_SHADOW | ER_TUNE_NO_SKIP,
-                              ER_PERSISTENT_NONE | ER_TUNE_NO_SKIP_SHADOW, ER_PERSISTENT_NONE | ER_TUNE_NO_SKIP};
+    /* then the tracking stages' persistent-lane mode */
+    const int candidates[] = {ER_PERSISTENT_BOTH, ER_PERSISTENT_SHADOW, ER_PERSISTENT_NONE, ER_PERSISTENT_PRIMARY};
     int best = b->tune_stages;
     for (int c : candidates) {
         rs = er_batch_set_stages(batch_id, c);
@@ -1768,27 +1773,23 @@ ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tun
         r.tune_stages = s.tune_stages;
         for (int b : bricks) {
             if (!delta && b != r.majorant_brick) continue;
-            const int skips[] = {0, ER_TUNE_NO_SKIP_SHADOW, ER_TUNE_NO_SKIP};
-            for (int si = 0; si < (delta ? 3 : 1); si++) {
-                s.majorant_brick = b;
-                s.tune_stages = base_stages | skips[si];
-                float m = 0.0f;
-                st = time_probe(*t, probe_spp, &m);
-                if (st != ER_OK) {
-                    /* a brick size whose grid does not fit (memory, launch limits) is
-                       skipped; a fault that poisons the context ends the sweep */
-                    if (cudaDeviceSynchronize() != cudaSuccess) { s = saved; t->built = false; return st; }
-                    cudaGetLastError();
-                    continue;
-                }
-                r.candidates++;
-                if (m > r.msamples_per_s) { r.msamples_per_s = m; r.majorant_brick = b; r.tune_stages = s.tune_stages; }
+            s.majorant_brick = b;
+            s.tune_stages = base_stages;
+            float m = 0.0f;
+            st = time_probe(*t, probe_spp, &m);
+            if (st != ER_OK) {
+                /* a brick size whose grid does not fit (memory, launch limits) is
+                   skipped; a fault that poisons the context ends the sweep */
+                if (cudaDeviceSynchronize() != cudaSuccess) { s = saved; t->built = false; return st; }
+                cudaGetLastError();
+                continue;
             }
+            r.candidates++;
+            if (m > r.msamples_per_s) { r.msamples_per_s = m; r.majorant_brick = b; r.tune_stages = s.tune_stages; }
         }
         if (r.msamples_per_s < 0.0f) { s = saved; t->built = false; return fail(ER_ERR_CUDA, "no majorant brick size could be timed"); }
         s.majorant_brick = r.majorant_brick;
         s.tune_stages = r.tune_stages;
-        const int skip_bit = r.tune_stages & ER_TUNE_NO_SKIP;
         if (wavefront) {
             /* occupancy pairs, with persistent-lane tracking stages or not (delta tracking) */
             const int variants[][2] = {{4, 4}, {3, 3}, {3, 4}, {4, 3}, {2, 3}, {3, 2}, {2, 2}, {2, 4}};
@@ -1797,7 +1798,7 @@ ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tun
             const int* modes = delta ? modes_delta : modes_march;
             const int n_modes = delta ? 3 : 1;
             for (int mi = 0; mi < n_modes; mi++) {
-                s.tune_stages = modes[mi] | skip_bit;
+                s.tune_stages = modes[mi];
                 for (const auto& vv : variants) {
                     s.tune_primary = vv[0];
                     s.tune_shadow = vv[1];
@@ -1809,7 +1810,7 @@ ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tun
                         r.msamples_per_s = m;
                         r.tune_primary = vv[0];
                         r.tune_shadow = vv[1];
-                        r.tune_stages = modes[mi] | skip_bit;
+                        r.tune_stages = modes[mi];
                     }
                 }
             }
@@ -1915,6 +1916,28 @@ ER_API er_status er_medium_majorant(int32_t tracer_id, const er_medium_desc* med
     return ER_OK;
 }
 
+/* names one walk of the differentiable medium (the tracer's build, the
+   medium's buffers and values, spp, view, first sample, and the buffer of
+   its samples): an adjoint with the key of the forward just before it
+   replays against that forward's shadow jobs (er_medium.cu dm_windows) */
+static uint64_t medium_walk_key(const TracerItem* t, const er_medium_desc* m, int32_t spp, uint32_t view, uint32_t first,
+                                const float* samples)
+{
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        for (size_t i = 0; i < n; i++) h = (h ^ b[i]) * 1099511628211ull;
+    };
+    const uintptr_t ptrs[4] = {(uintptr_t)m->d_density, (uintptr_t)m->d_opacity, (uintptr_t)m->d_majorant, (uintptr_t)samples};
+    const int32_t ints[6] = {m->n_opacity, m->brick, m->model, spp, (int32_t)view, (int32_t)first};
+    const float fl[6] = {m->scale, m->albedo[0], m->albedo[1], m->albedo[2], m->nee_probability, m->gradient_magnitude_inv};
+    mix(&t->build_serial, sizeof(t->build_serial));
+    mix(ptrs, sizeof(ptrs));
+    mix(ints, sizeof(ints));
+    mix(fl, sizeof(fl));
+    return h ? h : 1;
+}
+
 ER_API er_status er_medium_render(int32_t tracer_id, const er_medium_desc* medium, int32_t spp, uint32_t view,
                                   uint32_t first_sample, float* d_samples, float* d_sum_rgb, void* stream)
 {
@@ -1925,7 +1948,8 @@ ER_API er_status er_medium_render(int32_t tracer_id, const er_medium_desc* mediu
     er_status st = medium_params(tracer_id, medium, P, M, &t);
     if (st != ER_OK) return st;
     if (!medium->d_majorant || !d_samples || spp <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "invalid majorant, samples buffer or spp");
-    ER_CUDA(er_launch_dm_forward(P, M, spp, view, first_sample, d_samples, d_sum_rgb, (cudaStream_t)stream));
+    ER_CUDA(er_launch_dm_forward(P, M, spp, view, first_sample, d_samples, d_sum_rgb,
+                                 medium_walk_key(t, medium, spp, view, first_sample, d_samples), (cudaStream_t)stream));
     return ER_OK;
 }
 
@@ -1956,7 +1980,7 @@ ER_API er_status er_medium_adjoint(int32_t tracer_id, const er_medium_desc* medi
     if (st != ER_OK) return st;
     if (!medium->d_majorant || !d_dloss_dsum || spp <= 0) return fail(ER_ERR_INVALID_ARGUMENT, "invalid majorant, dLoss buffer or spp");
     ER_CUDA(er_launch_dm_adjoint(P, M, spp, view, first_sample, d_dloss_dsum, d_samples, d_grad_density, d_grad_opacity,
-                                 (cudaStream_t)stream));
+                                 medium_walk_key(t, medium, spp, view, first_sample, d_samples), (cudaStream_t)stream));
     return ER_OK;
 }
 

@@ -111,7 +111,7 @@ cudaError_t er_launch_majorant(const uint16_t* vox, const int res[3], int B, con
    passes (x: nearest non-empty along the row; y and z: min over offsets of
    max(offset, previous pass)).  The last pass writes -dist into the empty
    bricks of the majorant grid: a tracker in such a brick knows every brick
-   within dist-1 of it is empty too (er_path.cuh dda_skip). */
+   within dist-1 of it is empty too (er_path.cuh dda_jump). */
 #define ER_SKIP_CAP 32
 
 __global__ void k_skip_pass(const float* __restrict__ majorant, const uint8_t* __restrict__ in, uint8_t* __restrict__ out,

@@ -227,8 +227,7 @@ typedef struct er_render_settings {
                                      stream; 0: the reference's draws */
     int32_t tune_stages;          /* delta tracking: bits 0-1 which wavefront tracking stages run persistent
                                      lanes (ER_PERSISTENT_*; 0: the shadow stage only); bits 2 and 3
-                                     (ER_TUNE_NO_SKIP_PRIMARY, ER_TUNE_NO_SKIP_SHADOW) turn empty-space
-                                     skipping off in the free-flight and shadow stages */
+                                     (ER_TUNE_NO_SKIP_*) are accepted and ignored */
 } er_render_settings;
 
 /* tune_stages bits 0-1: the persistent-lane stages keep every warp's lanes
@@ -240,11 +239,11 @@ enum {
     ER_PERSISTENT_NONE = 2,
     ER_PERSISTENT_PRIMARY = 3
 };
-/* tune_stages bits 2, 3: no empty-space skipping in the free-flight or the
-   shadow stage.  With skipping, each empty majorant brick stores its
-   distance to the nearest non-empty brick and the trackers cross the empty
-   bricks around it without reading their majorants; images are
-   bit-identical either way. */
+/* tune_stages bits 2, 3: accepted for compatibility, no effect.  Each
+   empty majorant brick stores its Chebyshev distance k to the nearest
+   non-empty brick, and every delta/ratio tracker jumps in one step to the
+   exit of the cube of empty bricks of half-width k-1 around it; the jump
+   sets the face times the tracker continues from, so it is not optional. */
 #define ER_TUNE_NO_SKIP_PRIMARY 4
 #define ER_TUNE_NO_SKIP_SHADOW 8
 #define ER_TUNE_NO_SKIP (ER_TUNE_NO_SKIP_PRIMARY | ER_TUNE_NO_SKIP_SHADOW)
@@ -428,8 +427,8 @@ ER_API er_status er_batch_advance(int32_t batch_id, uint32_t samples, void* stre
    or 8 resident blocks of 256 threads per SM; 0 keeps the current value).
    Without this call a batch uses the settings of its first view's tracer. */
 ER_API er_status er_batch_set_tuning(int32_t batch_id, int32_t tune_primary, int32_t tune_shadow);
-/* The tracking stages' persistent-lane mode and empty-space skips of a batch
-   (tune_stages of er_render_settings: ER_PERSISTENT_* | ER_TUNE_NO_SKIP_*).
+/* The tracking stages' persistent-lane mode of a batch (tune_stages of
+   er_render_settings: ER_PERSISTENT_*; ER_TUNE_NO_SKIP_* bits ignored).
    Without this call (or er_batch_autotune) a batch uses its first view's
    tracer's value. */
 ER_API er_status er_batch_set_stages(int32_t batch_id, int32_t tune_stages);
@@ -511,7 +510,13 @@ ER_API er_status er_medium_render_f64(int32_t tracer_id, const er_medium_desc* m
 /* Path-replay adjoint: given dLoss/d(pixel sum) (W*H*3) and the forward
    samples (NULL: each thread recomputes its sample first), adds
    dLoss/d(density) (grid) and dLoss/d(opacity values) to the gradient
-   buffers (either may be NULL). */
+   buffers (either may be NULL).  d_samples must hold the forward of the
+   parameter values the buffers hold now.  When the last er_medium_render or
+   er_medium_adjoint call on this device was on the same stream with the
+   same tracer (not rebuilt since), medium descriptor, spp, view, first
+   sample and samples buffer, and covered at most 2^21 samples, the adjoint
+   replays against the shadow jobs that call kept instead of walking and
+   shadowing every path again. */
 ER_API er_status er_medium_adjoint(int32_t tracer_id, const er_medium_desc* medium, int32_t spp, uint32_t view,
                                    uint32_t first_sample, const float* d_dloss_dsum, const float* d_samples,
                                    float* d_grad_density, float* d_grad_opacity, void* stream);
@@ -528,7 +533,7 @@ typedef struct er_tune_result {
     float msamples_per_s;     /* probe throughput of the chosen configuration */
     int32_t candidates;       /* configurations timed */
     int32_t tune_shade;       /* occupancy variant of the shade stage */
-    int32_t tune_stages;      /* tune_stages of the chosen configuration (ER_PERSISTENT_*, ER_TUNE_NO_SKIP_*) */
+    int32_t tune_stages;      /* tune_stages of the chosen configuration (ER_PERSISTENT_*) */
 } er_tune_result;
 
 /* Times probe renders of a bound tracer (probe_spp samples per pixel of its

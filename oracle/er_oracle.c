@@ -1325,6 +1325,40 @@ static inline float dda_majorant(or_scene* s, const dda_t* d)
     return s->majorant[((size_t)d->b[2] * (size_t)s->nb[1] + (size_t)d->b[1]) * (size_t)s->nb[0] + (size_t)d->b[0]];
 }
 
+/* Empty-space jump (exposure-render_gb300/csrc/er_path.cuh dda_jump): an
+   empty brick holding -k (k >= 2, its Chebyshev distance in bricks to the
+   nearest non-empty brick, see empty_skip_distances) lies in a cube of
+   empty bricks of half-width k-1; the DDA moves to that cube's exit in one
+   step.  Exit face per axis at next + (k-1) * delta; the earliest (ties to
+   x, then y) moves its axis k bricks, each other axis moves past the
+   floor((te - next) / delta) + 1 faces (at most k) it crosses before te.
+   The same float operations as the GPU, in the same order. */
+static inline void dda_jump(const or_scene* s, dda_t* d, int k)
+{
+    const float r = (float)(k - 1);
+    float f[3];
+    for (int i = 0; i < 3; i++) f[i] = d->step[i] != 0 ? d->tnext[i] + r * d->tdelta[i] : FLT_MAX;
+    int a = 0;
+    if (f[1] < f[a]) a = 1;
+    if (f[2] < f[a]) a = 2;
+    const float te = f[a];
+    if (te >= d->tmax) { d->done = 1; d->t = te; return; }
+    for (int i = 0; i < 3; i++) {
+        if (i == a) {
+            d->b[i] += d->step[i] * k;
+            d->tnext[i] = f[i] + d->tdelta[i];
+        } else if (d->tnext[i] < te) {
+            int m = (int)((te - d->tnext[i]) / d->tdelta[i]) + 1;
+            m = m > k ? k : m;
+            d->b[i] += d->step[i] * m;
+            d->tnext[i] = d->tnext[i] + (float)m * d->tdelta[i];
+        }
+    }
+    for (int i = 0; i < 3; i++)
+        if (d->b[i] < 0 || d->b[i] >= s->nb[i]) d->done = 1;
+    d->t = te;
+}
+
 #define ER_DELTA_MAX_COLLISIONS 1048576
 
 /* Delta tracking of the primary ray.  sigma_t(x) = DensityScale *
@@ -1373,6 +1407,9 @@ static void sample_volume_delta(or_scene* s, ray_t R, rng_t* rng, scatter_event*
                 if (++guard > ER_DELTA_MAX_COLLISIONS) return;
                 tau = -er_logf(rng_get1(rng));
             }
+        } else if (mu <= -2.0f) {
+            dda_jump(s, &d, (int)(-mu));
+            continue;
         }
         dda_advance(s, &d, e);
     }
@@ -1416,6 +1453,9 @@ static float transmittance_ratio(or_scene* s, ray_t R, rng_t* rng)
                 if (++guard > ER_DELTA_MAX_COLLISIONS) return Tr;
                 tau = -er_logf(rng_get1(rng));
             }
+        } else if (mu <= -2.0f) {
+            dda_jump(s, &d, (int)(-mu));
+            continue;
         }
         dda_advance(s, &d, e);
     }
@@ -1685,6 +1725,45 @@ static float gradient_magnitude_max_threaded(or_scene* s, int nthreads)
     return mx;
 }
 
+/* Empty-space distances (exposure-render_gb300/csrc/er_volume.cu
+   k_skip_pass): for each empty brick (majorant 0) the Chebyshev distance
+   in bricks to the nearest non-empty brick, capped at 32, by three 1D
+   passes -- x: distance to the nearest non-empty brick of the row (0 for a
+   non-empty brick, 32 when none is within 31); y, then z: the minimum over
+   offsets o of max(|o|, previous pass at o).  Empty bricks then hold minus
+   that distance. */
+#define ER_SKIP_CAP 32
+static void empty_skip_distances(float* majorant, const int nb[3])
+{
+    const size_t total = (size_t)nb[0] * nb[1] * nb[2];
+    uint8_t* a = (uint8_t*)malloc(total);
+    uint8_t* b = (uint8_t*)malloc(total);
+    for (int axis = 0; axis < 3; axis++) {
+        const uint8_t* in = axis == 1 ? a : b;
+        uint8_t* out = axis == 1 ? b : a;
+        const size_t step = axis == 0 ? 1 : (axis == 1 ? (size_t)nb[0] : (size_t)nb[0] * nb[1]);
+        for (size_t i = 0; i < total; i++) {
+            const int c0[3] = { (int)(i % nb[0]), (int)((i / nb[0]) % nb[1]), (int)(i / ((size_t)nb[0] * nb[1])) };
+            int best = ER_SKIP_CAP;
+            for (int o = -(ER_SKIP_CAP - 1); o <= ER_SKIP_CAP - 1; o++) {
+                const int c = c0[axis] + o;
+                if (c < 0 || c >= nb[axis]) continue;
+                const int ao = o < 0 ? -o : o;
+                if (ao >= best) continue;
+                const size_t j = (size_t)((long long)i + (long long)o * (long long)step);
+                const int v = axis == 0 ? (majorant[j] > 0.0f ? 0 : ER_SKIP_CAP) : (int)in[j];
+                const int dd = v > ao ? v : ao;
+                best = dd < best ? dd : best;
+            }
+            out[i] = (uint8_t)best;
+        }
+    }
+    for (size_t i = 0; i < total; i++)
+        if (!(majorant[i] > 0.0f)) majorant[i] = -(float)a[i];
+    free(a);
+    free(b);
+}
+
 static void prepare_extensions(or_scene* s)
 {
     const size_t n = (size_t)s->res[0] * (size_t)s->res[1] * (size_t)s->res[2];
@@ -1723,6 +1802,7 @@ static void prepare_extensions(or_scene* s)
                     for (int i = vlo; i <= (int)vhi; i++) m = s->sigma[i] > m ? s->sigma[i] : m;
                     s->majorant[((size_t)bz * s->nb[1] + by) * s->nb[0] + bx] = s->st.density_scale * m;
                 }
+        empty_skip_distances(s->majorant, s->nb);
     }
     s->gm_inv_max = 0.0f;
     s->gm_ready = 0;

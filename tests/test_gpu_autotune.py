@@ -56,9 +56,9 @@ def test_autotune_delta_sweep_and_cache(torch, lib, runtime, oracle, cache):
         assert first["tune_shade"] in (2, 3, 4, 6)
         assert first["tune_stages"] & 3 in (C.PERSISTENT_SHADOW, C.PERSISTENT_BOTH, C.PERSISTENT_NONE)
         assert first["tune_stages"] & ~(3 | C.TUNE_NO_SKIP) == 0
-        # bricks with empty-space skipping in both, one or neither tracking stage, occupancy pairs under
-        # three persistent-lane modes, shade variants
-        assert first["candidates"] == 3 * 5 + 3 * 8 + 4 and not first["from_cache"] and first["msamples_per_s"] > 0
+        # five brick sizes (the empty-space jump always on), occupancy pairs under three persistent-lane
+        # modes, shade variants
+        assert first["candidates"] == 5 + 3 * 8 + 4 and not first["from_cache"] and first["msamples_per_s"] > 0
         assert cache.exists() and len(cache.read_text().splitlines()) == 1
         again = r.autotune(2)
         assert again["from_cache"] and again["candidates"] == 0

@@ -129,9 +129,9 @@ def test_majorant_grid_device_bit_exact(env, oracle, shape, brick):
 @pytest.mark.parametrize("mode", [0, 1, 2, 3, 0 | 12, 1 | 12, 1 | 8, 2 | 4], ids=["shadow", "both", "none", "primary", "shadow-noskip",
                                                                         "both-noskip", "both-skip-primary", "none-skip-shadow"])
 def test_persistent_stage_modes_bit_exact(env, oracle, mode):
-    """every persistent-lane mode of the delta-tracking stages, with and
-    without empty-space skipping (tune_stages), gives the oracle's sums with
-    the hybrid shader and full MIS"""
+    """every persistent-lane mode of the delta-tracking stages (tune_stages;
+    the ER_TUNE_NO_SKIP_* bits are accepted and ignored) gives the oracle's
+    sums with the hybrid shader and full MIS"""
     torch, lib, rt = env
     sc = two_light_scene(13)
     sc.tracer.settings.free_flight = 1
@@ -181,3 +181,38 @@ def test_stratified_light_samples_bit_exact(env, oracle, stages):
     h = OL.SceneHandle(oracle, sc)
     assert not np.array_equal(h.render_sum(6, view=2, first=7, nthreads=4), cpu)
     h.close()
+
+
+def sparse_scene(film=(40, 32)):
+    """80^3 voxels, empty but for two small dense boxes: empty-space
+    distances run up to the 32-brick cap at 1^3 and 2^3 bricks"""
+    vol = np.zeros((80, 80, 80), dtype=np.uint16)
+    vol[10:30, 8:28, 12:34] = 3000
+    vol[50:66, 54:72, 44:60] = 2200
+    lights, textures = S.c1_lights()
+    return S.Scene("sparse", vol, tracer=S.c1_tracer(film), lights=lights, textures=textures)
+
+
+@pytest.mark.parametrize("brick,stages,engine", [(1, 0, 0), (1, 1, 0), (1, 2, 0), (2, 0, 0), (2, 1, 0), (2, 3, 0), (1, 0, 1), (2, 0, 1)],
+                         ids=["b1-persistent-shadow", "b1-persistent-both", "b1-per-thread", "b2-persistent-shadow",
+                              "b2-persistent-both", "b2-persistent-primary", "b1-one-kernel", "b2-one-kernel"])
+def test_empty_space_jump_bit_exact(env, oracle, brick, stages, engine):
+    """delta and ratio tracking that jump across cubes of empty bricks (the
+    wavefront stages in each persistent-lane mode and the one-kernel path)
+    give the oracle's sums bit for bit"""
+    torch, lib, rt = env
+    sc = sparse_scene()
+    s = sc.tracer.settings
+    s.free_flight, s.mis, s.majorant_brick, s.tune_stages, s.engine = 1, 1, brick, stages, engine
+    r = rt.Renderer(sc, lib)
+    h = OL.SceneHandle(oracle, sc)
+    try:
+        d = torch.zeros((sc.height, sc.width, 4), dtype=torch.float32, device="cuda")
+        r.trace_sum_device(d.data_ptr(), 4, 2, 1, 0, None)
+        torch.cuda.synchronize()
+        cpu = h.render_sum(4, view=2, first=1, nthreads=4)
+        assert np.array_equal(bits(d.cpu().numpy()), bits(cpu))
+        assert cpu[..., 3].sum() > 0
+    finally:
+        r.close()
+        h.close()

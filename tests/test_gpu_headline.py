@@ -91,8 +91,8 @@ def test_c2_reference_order_crops(torch, lib, runtime, oracle, c2):
 def test_c2_fast_path_crops(torch, lib, runtime, oracle, c2, stages):
     """The benchmark's estimator on the c2 workload: delta tracking over 8^3
     majorant bricks, ratio-tracked shadows, hybrid shader, full MIS,
-    stratified samples (the per-thread and persistent-lane stages, with and
-    without empty-space skipping)"""
+    stratified samples (the per-thread and persistent-lane stages; the
+    ER_TUNE_NO_SKIP_* bits are accepted and ignored)"""
     sc = S.Scene(c2.name, c2.volume, tracer=C.er_tracer_desc.from_buffer_copy(c2.tracer), lights=c2.lights, textures=c2.textures)
     s = sc.tracer.settings
     s.free_flight, s.mis, s.stratify, s.majorant_brick, s.tune_stages = 1, 1, 1, 8, stages

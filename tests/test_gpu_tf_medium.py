@@ -88,6 +88,28 @@ def test_forward_bit_exact_and_adjoint_matches_oracle(torch, lib, pkg, oracle, s
         r.close()
 
 
+def test_adjoint_on_kept_jobs_matches_a_fresh_walk(torch, lib, pkg):
+    """An adjoint right after its forward replays against the job list the
+    forward kept; after another walk (here view 3) the same adjoint call
+    runs the count, jobs and shadow stages again.  Both give the same
+    gradients up to the order of the atomic sums."""
+    sc, r, m, rho, vals = make(torch, lib, pkg, (16, 16, 16), 12, (24, 20), 30.0, 4)
+    try:
+        spp = 4
+        smp, s = m.render_samples(rho, vals, spp)
+        dimg = torch.from_numpy(np.random.default_rng(5).normal(size=tuple(s.shape)).astype(np.float32)).cuda()
+        k_rho, k_tf = m.adjoint(rho, vals, spp, dimg, smp)
+        m.render_samples(rho, vals, spp, view=3)
+        f_rho, f_tf = m.adjoint(rho, vals, spp, dimg, smp)
+        k2_rho, k2_tf = m.adjoint(rho, vals, spp, dimg, smp)      # kept again after the fresh walk
+        torch.cuda.synchronize()
+        assert float(f_tf.abs().max()) > 0 and float(f_rho.abs().max()) > 0
+        for a, b in ((k_tf, f_tf), (k_rho, f_rho), (k2_tf, f_tf), (k2_rho, f_rho)):
+            assert torch.allclose(a, b, rtol=1e-5, atol=1e-6 * float(b.abs().max()))
+    finally:
+        r.close()
+
+
 def test_binary64_tracks_float_and_the_oracle(torch, lib, pkg):
     """The GPU's binary64 evaluation (every medium-dependent quantity in
     double; the camera and light geometry stays float) against its float
@@ -97,13 +119,24 @@ def test_binary64_tracks_float_and_the_oracle(torch, lib, pkg):
     try:
         s64 = m.render_sums64(rho, vals, 4).cpu().numpy()
         _, s32 = m.render_samples(rho, vals, 4)
-        assert np.allclose(s32.cpu().numpy(), s64, rtol=1e-4, atol=1e-6 * np.abs(s64).max())
+        s32 = s32.cpu().numpy()
+        # a collision or roulette decision whose threshold falls between the
+        # float and the double value takes another path: such pixels differ
+        # by a whole sample; every other pixel agrees to float rounding
+        close = np.isclose(s32, s64, rtol=1e-4, atol=1e-6 * np.abs(s64).max()).all(-1)
+        flips = int((~close).sum())
+        assert flips <= max(2, close.size // 100), (flips, float(np.abs(s32 - s64).max()))
+        assert abs(float(s32.sum()) - float(s64.sum())) <= 2e-2 * float(np.abs(s64).sum()), (s32.sum(), s64.sum())
         f64 = OL.load_fp64()
         h = OL.MediumHandle(f64, sc, rho.cpu().numpy(), vals.cpu().numpy(), 30.0, np.array([0.8, 0.8, 0.8]), 0.5,
                             m.majorant.cpu().numpy(), 4, model=1, gm_inv=m.gm_inv)
         ref = h.render(4, nthreads=4)
         h.close()
-        assert np.abs(s64 - ref).max() <= 1e-3 * np.abs(ref).max()
+        # the geometry (float on the GPU, double in the oracle) moves the
+        # collision points by float rounding: pixels agree to 1e-3 of the
+        # image's largest value but for the rare decision flips
+        near = (np.abs(s64 - ref) <= 1e-3 * np.abs(ref).max()).all(-1)
+        assert int((~near).sum()) <= max(2, near.size // 100), (int((~near).sum()), float(np.abs(s64 - ref).max()))
     finally:
         r.close()
 
