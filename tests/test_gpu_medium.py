@@ -91,8 +91,11 @@ def test_autograd_function(torch, lib, pkg):
         smp, s = m.render_samples(rho, tf, spp)
         dsum = 2.0 * (s / spp - target) / spp
         g_rho, g_tf = m.adjoint(rho, tf, spp, dsum, smp)
-        assert torch.allclose(tf_p.grad, g_tf, rtol=1e-5, atol=1e-7 * float(g_tf.abs().max()))
-        assert torch.allclose(rho_p.grad, g_rho, rtol=1e-5, atol=1e-7 * float(g_rho.abs().max()))
+        # two walks of the same samples: the gradients agree up to the order
+        # of the atomic sums (a density entry that sums terms of both signs
+        # keeps ~1e-7 of the largest gradient from that order)
+        assert torch.allclose(tf_p.grad, g_tf, rtol=1e-5, atol=1e-6 * float(g_tf.abs().max()))
+        assert torch.allclose(rho_p.grad, g_rho, rtol=1e-5, atol=1e-6 * float(g_rho.abs().max()))
     finally:
         r.close()
 
