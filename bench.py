@@ -451,25 +451,38 @@ def batched_workload(wl, n_views=0):
     return S.c3_scenes(), views, "c3-batched-%d-views-3-blob-volumes" % len(views)
 
 
-def batched_reference_rate(scenes, views, seconds_target=12.0, steps=1):
+def batched_reference_rate(scenes, views, seconds_target=12.0, steps=1, per_volume=4):
     """Samples/s of the reference transport on the host cores over a batch of
-    views: the first view of each volume stands for that volume's views and is
-    timed on a centre crop at 1 spp (an equal share of `seconds_target`); the
-    batch's rate weights each volume by its views' samples,
-    sum(n_k) / sum(n_k / rate_k)."""
-    first, n = {}, {}
+    views: up to `per_volume` views of each volume, spread over its orbit,
+    each timed on a centre crop at 1 spp (equal shares of `seconds_target`);
+    a volume's rate is the harmonic mean of its timed views' rates (each
+    stands for an equal share of the volume's samples), and the batch's rate
+    weights the volumes by their views' samples, sum(n_k) / sum(n_k / rate_k).
+    Returns the per-view spread with the rate."""
+    cams, n = {}, {}
     for k, cam, spp in views:
-        first.setdefault(k, cam)
+        cams.setdefault(k, []).append(cam)
         n[k] = n.get(k, 0) + cam.film_size[0] * cam.film_size[1] * spp
-    seconds, kind, cores, crops = 0.0, None, None, []
-    for k in sorted(first):
-        sc = reference_path(scenes[k])
-        sc.tracer.camera = first[k]
-        rate, kind, cores, sample = cpu_reference_rate(sc, seconds_target=seconds_target / len(first), steps=steps)
-        seconds += n[k] / rate
-        crops.append("volume %d: %s" % (k, sample.split(" centre")[0]))
+    picks = {}
+    for k, cs in cams.items():
+        m = min(per_volume, len(cs))
+        picks[k] = [cs[(i * len(cs)) // m] for i in range(m)]
+    n_timed = sum(len(v) for v in picks.values())
+    seconds, kind, cores, crops, rates = 0.0, None, None, [], []
+    for k in sorted(picks):
+        inv = 0.0
+        for cam in picks[k]:
+            sc = reference_path(scenes[k])
+            sc.tracer.camera = cam
+            rate, kind, cores, sample = cpu_reference_rate(sc, seconds_target=seconds_target / n_timed, steps=steps)
+            inv += 1.0 / rate
+            rates.append(rate)
+        seconds += n[k] * inv / len(picks[k])
+        crops.append("volume %d: %d views, %s" % (k, len(picks[k]), sample.split(" centre")[0]))
     rate = sum(n.values()) / seconds
-    sample = "first view of each volume, centre crop x 1 spp per step (%s), weighted by the volume's samples" % ", ".join(crops)
+    sample = ("views spread over each volume's orbit, centre crop x 1 spp per step (%s); harmonic mean per volume, "
+              "weighted by the volume's samples; per-view rates %.3g .. %.3g Msamples/s"
+              % ("; ".join(crops), min(rates) / 1e6, max(rates) / 1e6))
     return rate, kind, cores, sample
 
 
@@ -843,7 +856,7 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
         r.rebind_tracer()
         film_conv = {"c5v0": film_convergence(
             lib, torch, r, {"fast": {"free_flight": 1, "stratify": 1}, "plain": {"free_flight": 0, "stratify": 0}},
-            {"free_flight": 1, "stratify": 0}, 4096, budget_s=30.0, stream=sp, film=(cam.film_size[0], cam.film_size[1]))}
+            {"free_flight": 1, "stratify": 0}, 4096, budget_s=75.0, stream=sp, film=(cam.film_size[0], cam.film_size[1]))}
         ctypes.memmove(ctypes.byref(r.tracer_desc), ctypes.byref(saved), ctypes.sizeof(saved))
         r.rebind_tracer()
     if world == 1 and not args.no_rmse and wl == "c3":

@@ -41,12 +41,9 @@ ER_D float lerp_u16(float t, float a, float b)
     return truncf(r);
 }
 
-ER_D float get_intensity(const Params& P, v3 p)
+/* the trilinear lookup at local voxel coordinates (Lx, Ly, Lz) */
+ER_D float get_intensity_local(const Params& P, float Lx, float Ly, float Lz)
 {
-    const v3 off = V3(p.x - P.minp[0], p.y - P.minp[1], p.z - P.minp[2]);
-    const float Lx = off.x * P.inv_size[0] * (float)P.res[0];
-    const float Ly = off.y * P.inv_size[1] * (float)P.res[1];
-    const float Lz = off.z * P.inv_size[2] * (float)P.res[2];
     const int vx = (int)floorf(Lx);
     const int vy = (int)floorf(Ly);
     const int vz = (int)floorf(Lz);
@@ -83,6 +80,21 @@ ER_D float get_intensity(const Params& P, v3 p)
     const float d0 = lerp_u16(dy, d00, d10);
     const float d1 = lerp_u16(dy, d01, d11);
     return lerp_u16(dz, d0, d1);
+}
+
+ER_D void local_coords(const Params& P, v3 p, float& Lx, float& Ly, float& Lz)
+{
+    const v3 off = V3(p.x - P.minp[0], p.y - P.minp[1], p.z - P.minp[2]);
+    Lx = off.x * P.inv_size[0] * (float)P.res[0];
+    Ly = off.y * P.inv_size[1] * (float)P.res[1];
+    Lz = off.z * P.inv_size[2] * (float)P.res[2];
+}
+
+ER_D float get_intensity(const Params& P, v3 p)
+{
+    float Lx, Ly, Lz;
+    local_coords(P, p, Lx, Ly, Lz);
+    return get_intensity_local(P, Lx, Ly, Lz);
 }
 
 /* DensityScale * Opacity1D.Evaluate(I) from the integer-intensity table */
@@ -366,6 +378,26 @@ ER_D float sigma_point(const Params& P, v3 p)
 {
     if (P.clip_count > 0 && clipped(P, p)) return 0.0f;
     return sigma_at(P, get_intensity(P, p));
+}
+
+/* sigma_point at a tentative collision of a tracker in majorant brick
+   (bx, by, bz): the local coordinates are clamped to the brick's extent
+   [b B, (b + 1) B] per axis before the lookup, so that it blends only
+   voxels of the brick's footprint (b B .. (b + 1) B), whose maximum the
+   brick's majorant bounds.  The clamp moves a point only when float
+   rounding put it outside its DDA brick (a distance of a few ulps). */
+ER_D float sigma_point_in_brick(const Params& P, v3 p, int bx, int by, int bz)
+{
+    if (P.clip_count > 0 && clipped(P, p)) return 0.0f;
+    float Lx, Ly, Lz;
+    local_coords(P, p, Lx, Ly, Lz);
+    const float B = (float)P.brick;
+    const float x0 = (float)bx * B, y0 = (float)by * B, z0 = (float)bz * B;
+    const float x1 = x0 + B, y1 = y0 + B, z1 = z0 + B;
+    Lx = Lx < x0 ? x0 : (x1 < Lx ? x1 : Lx);
+    Ly = Ly < y0 ? y0 : (y1 < Ly ? y1 : Ly);
+    Lz = Lz < z0 ? z0 : (z1 < Lz ? z1 : Lz);
+    return sigma_at(P, get_intensity_local(P, Lx, Ly, Lz));
 }
 
 /* IntersectPlane(R, OneSided, Int) - Source/plane.h:41-62 */
@@ -1072,7 +1104,7 @@ ER_D void sample_volume_delta(const Params& P, const Ray& R, Rng& rng, Event& SE
                 }
                 t = t + dt;
                 const v3 Pt = vadd(R.O, vscale(R.D, t));
-                const float sig = P.density_scale * sigma_point(P, Pt);
+                const float sig = P.density_scale * sigma_point_in_brick(P, Pt, d.bx, d.by, d.bz);
                 if (rng.get1() * mu < sig) {
                     SE.valid = true;
                     SE.T = t;
@@ -1137,7 +1169,7 @@ ER_D void delta_step(const Params& P, const Ray& R, Rng& rng, DeltaTracker& k)
         if (k.t + dt < k.e) {
             k.t = k.t + dt;
             const v3 Pt = vadd(R.O, vscale(R.D, k.t));
-            const float sig = P.density_scale * sigma_point(P, Pt);
+            const float sig = P.density_scale * sigma_point_in_brick(P, Pt, k.d.bx, k.d.by, k.d.bz);
             if (rng.get1() * k.mu < sig) { k.hit = true; k.done = true; return; }
             if (++k.guard > ER_DELTA_MAX_COLLISIONS) { atomicOr(P.err, 2); k.done = true; return; }
             k.tau = -er_logf(rng.get1());
@@ -1202,7 +1234,7 @@ ER_D void ratio_step(const Params& P, const Ray& R, Rng& rng, RatioTracker& k)
         if (k.t + dt < k.e) {
             k.t = k.t + dt;
             const v3 Pt = vadd(R.O, vscale(R.D, k.t));
-            const float sig = P.density_scale * sigma_point(P, Pt);
+            const float sig = P.density_scale * sigma_point_in_brick(P, Pt, k.d.bx, k.d.by, k.d.bz);
             k.Tr = k.Tr * (1.0f - sig / k.mu);
             if (k.Tr <= 0.0f) { k.Tr = 0.0f; k.done = true; return; }
             if (k.Tr < 0.1f) {
@@ -1256,7 +1288,7 @@ ER_D float transmittance_ratio(const Params& P, const Ray& R, Rng& rng)
                 }
                 t = t + dt;
                 const v3 Pt = vadd(R.O, vscale(R.D, t));
-                const float sig = P.density_scale * sigma_point(P, Pt);
+                const float sig = P.density_scale * sigma_point_in_brick(P, Pt, d.bx, d.by, d.bz);
                 Tr = Tr * (1.0f - sig / mu);
                 if (Tr <= 0.0f) return 0.0f;
                 if (Tr < 0.1f) {

@@ -1,19 +1,23 @@
 /*
  * er_volume.cu - per-volume pre-passes of the delta tracker.
  *
- *   k_brick_minmax : min and max voxel of every brick's footprint (the
- *                    brick^3 voxels plus a one-voxel apron on each side,
- *                    which covers every corner a trilinear lookup inside the
- *                    brick can touch, Source/buffer3d.h:222-242).  One warp
- *                    per brick, coalesced reads along x.
+ *   k_brick_minmax : min and max voxel of every brick's footprint: voxels
+ *                    b B .. (b + 1) B per axis, every corner a trilinear
+ *                    lookup (Source/buffer3d.h:222-242) at local coordinates
+ *                    in [b B, (b + 1) B] can blend with a nonzero weight (the
+ *                    trackers clamp their lookups to that range,
+ *                    er_path.cuh sigma_point_in_brick).  One warp per brick,
+ *                    coalesced reads along x.
  *   k_rmq_level    : level k of a sparse table of running maxima over the
  *                    sigma table (sigma[I] = DensityScale * Opacity(I)).
  *   k_majorant     : majorant[brick] = DensityScale * max sigma[lo..hi].
  *
  * A lookup inside a brick is a truncated trilinear blend of voxels in
- * [lo, hi], so its integer intensity lies in [lo, hi] and its extinction
- * DensityScale * sigma[I] is bounded by the brick's majorant exactly (max of
- * the same floats, one multiply).  The CPU oracle builds the same grid by
+ * [lo, hi]; float rounding of a blend (1 - t) a + t b can fall just below
+ * min(a, b), which the truncation turns into one intensity less, so its
+ * integer intensity lies in [lo - 1, hi] and its extinction
+ * DensityScale * sigma[I] is bounded by the max over that range exactly
+ * (max of the same floats, one multiply).  The CPU oracle builds the same grid by
  * brute force; the tests compare them bit for bit through the rendered paths.
  */
 #include <cuda_runtime.h>
@@ -32,10 +36,8 @@ __global__ void k_brick_minmax(const uint16_t* __restrict__ vox, int rx, int ry,
     /* one warp per brick, grid-stride over the bricks (2^27 at 1^3 bricks of 512^3) */
     for (long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < total; warp += nwarps) {
     const int bx = (int)(warp % nbx), by = (int)((warp / nbx) % nby), bz = (int)(warp / ((long long)nbx * nby));
-    int x0 = bx * B - 1, x1 = (bx + 1) * B + 1;
-    int y0 = by * B - 1, y1 = (by + 1) * B + 1;
-    int z0 = bz * B - 1, z1 = (bz + 1) * B + 1;
-    x0 = x0 < 0 ? 0 : x0; y0 = y0 < 0 ? 0 : y0; z0 = z0 < 0 ? 0 : z0;
+    const int x0 = bx * B, y0 = by * B, z0 = bz * B;
+    int x1 = (bx + 1) * B, y1 = (by + 1) * B, z1 = (bz + 1) * B;
     x1 = x1 > rx - 1 ? rx - 1 : x1; y1 = y1 > ry - 1 ? ry - 1 : y1; z1 = z1 > rz - 1 ? rz - 1 : z1;
     const int wx = x1 - x0 + 1;
     const int rows = (y1 - y0 + 1) * (z1 - z0 + 1);
@@ -76,8 +78,8 @@ __global__ void k_majorant(const uint32_t* __restrict__ minmax, const float* __r
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= total) return;
     const uint32_t mm = minmax[i];
-    int lo = (int)(mm & 0xffffu), hi = (int)(mm >> 16);
-    lo = lo > n - 1 ? n - 1 : lo;
+    int lo = (int)(mm & 0xffffu) - 1, hi = (int)(mm >> 16);
+    lo = lo < 0 ? 0 : (lo > n - 1 ? n - 1 : lo);
     hi = hi > n - 1 ? n - 1 : hi;
     const int len = hi - lo + 1;
     int k = 31 - __clz(len);

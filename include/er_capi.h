@@ -594,7 +594,10 @@ ER_API er_status er_gradient_magnitude(int32_t volume_id, uint16_t* d_gm_or_null
    d_voxels (x-fastest uint16, resolution[0]*[1]*[2]), d_sigma (sigma_count
    floats, sigma[I] = density_scale * Opacity(I), covering every voxel value),
    d_majorant receives ceil(res/brick) per axis floats, x fastest:
-   density_scale * max sigma over each brick's voxels plus a one-voxel apron.
+   density_scale * max sigma[lo - 1 .. hi], lo and hi the smallest and largest
+   voxel of the brick's footprint (voxels b*brick .. (b+1)*brick per axis,
+   the corners a lookup clamped to the brick blends; lo - 1 because the
+   truncated blend can round to one below its smallest corner).
    The design precedent is the commented macrocell tracker of
    Source/raymarching.h:115-273 (per-cell maximum extinction).  Scratch space
    (per-brick min/max, range-max table) is allocated by the library. */

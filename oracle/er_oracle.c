@@ -403,12 +403,10 @@ static inline float lerp_u16(float t, float a, float b)
 
 /* GetIntensity (Source/volumes.h:26-29) -> Volume::operator() (Source/volume.h:131-138)
    -> Buffer3D<unsigned short>::operator()(Vec3f) (Source/buffer3d.h:222-242) */
-static inline float get_intensity(or_scene* s, v3 P)
+/* the trilinear lookup at local voxel coordinates L */
+static inline float get_intensity_local(or_scene* s, v3 L)
 {
     s->lookups++;
-    const v3 off = vsub(P, s->minp);
-    const v3 L = V3(off.x * s->inv_size.x * (float)s->res[0], off.y * s->inv_size.y * (float)s->res[1],
-                    off.z * s->inv_size.z * (float)s->res[2]);
     const int vx = (int)floorf(L.x);
     const int vy = (int)floorf(L.y);
     const int vz = (int)floorf(L.z);
@@ -422,6 +420,18 @@ static inline float get_intensity(or_scene* s, v3 P)
     const float d0 = lerp_u16(dy, d00, d10);
     const float d1 = lerp_u16(dy, d01, d11);
     return lerp_u16(dz, d0, d1);
+}
+
+static inline v3 local_coords(const or_scene* s, v3 P)
+{
+    const v3 off = vsub(P, s->minp);
+    return V3(off.x * s->inv_size.x * (float)s->res[0], off.y * s->inv_size.y * (float)s->res[1],
+              off.z * s->inv_size.z * (float)s->res[2]);
+}
+
+static inline float get_intensity(or_scene* s, v3 P)
+{
+    return get_intensity_local(s, local_coords(s, P));
 }
 
 /* GradientCD / GradientFD / GradientFiltered / Gradient - Source/volumes.h:31-86 */
@@ -1359,6 +1369,24 @@ static inline void dda_jump(const or_scene* s, dda_t* d, int k)
     d->t = te;
 }
 
+/* extinction at a tentative collision of a tracker in DDA brick b
+   (exposure-render_gb300/csrc/er_path.cuh sigma_point_in_brick): the local
+   coordinates are clamped to [b B, (b + 1) B] per axis before the lookup, so
+   that it blends only voxels of the brick's footprint, which the majorant
+   bounds; zero where a clipping object removes the volume */
+static inline float sigma_in_brick(or_scene* s, v3 P, const dda_t* d)
+{
+    if (s->n_clips && clipped(s, P)) return 0.0f;
+    v3 L = local_coords(s, P);
+    const float B = (float)s->brick;
+    const float x0 = (float)d->b[0] * B, y0 = (float)d->b[1] * B, z0 = (float)d->b[2] * B;
+    const float x1 = x0 + B, y1 = y0 + B, z1 = z0 + B;
+    L.x = L.x < x0 ? x0 : (x1 < L.x ? x1 : L.x);
+    L.y = L.y < y0 ? y0 : (y1 < L.y ? y1 : L.y);
+    L.z = L.z < z0 ? z0 : (z1 < L.z ? z1 : L.z);
+    return s->st.density_scale * sigma_lookup(s, get_intensity_local(s, L));
+}
+
 #define ER_DELTA_MAX_COLLISIONS 1048576
 
 /* Delta tracking of the primary ray.  sigma_t(x) = DensityScale *
@@ -1393,7 +1421,7 @@ static void sample_volume_delta(or_scene* s, ray_t R, rng_t* rng, scatter_event*
                 }
                 t = t + dt;
                 const v3 P = vadd(R.O, vscale(R.D, t));
-                const float sig = (s->n_clips && clipped(s, P)) ? 0.0f : s->st.density_scale * sigma_lookup(s, get_intensity(s, P));
+                const float sig = sigma_in_brick(s, P, &d);
                 if (rng_get1(rng) * mu < sig) {
                     SE->valid = 1;
                     SE->T = t;
@@ -1443,7 +1471,7 @@ static float transmittance_ratio(or_scene* s, ray_t R, rng_t* rng)
                 }
                 t = t + dt;
                 const v3 P = vadd(R.O, vscale(R.D, t));
-                const float sig = (s->n_clips && clipped(s, P)) ? 0.0f : s->st.density_scale * sigma_lookup(s, get_intensity(s, P));
+                const float sig = sigma_in_brick(s, P, &d);
                 Tr = Tr * (1.0f - sig / mu);
                 if (Tr <= 0.0f) return 0.0f;
                 if (Tr < 0.1f) {
@@ -1781,13 +1809,13 @@ static void prepare_extensions(or_scene* s)
         for (int bz = 0; bz < s->nb[2]; bz++)
             for (int by = 0; by < s->nb[1]; by++)
                 for (int bx = 0; bx < s->nb[0]; bx++) {
-                    /* voxel footprint of the brick plus a one-voxel apron on both sides */
+                    /* voxel footprint of the brick: b B .. (b + 1) B per axis
+                       (the trackers clamp their lookups to [b B, (b + 1) B]) */
                     int lo[3], hi[3];
                     const int b[3] = { bx, by, bz };
                     for (int i = 0; i < 3; i++) {
-                        lo[i] = b[i] * B - 1;
-                        hi[i] = (b[i] + 1) * B + 1;
-                        lo[i] = lo[i] < 0 ? 0 : lo[i];
+                        lo[i] = b[i] * B;
+                        hi[i] = (b[i] + 1) * B;
                         hi[i] = hi[i] > s->res[i] - 1 ? s->res[i] - 1 : hi[i];
                     }
                     uint16_t vlo = 65535, vhi = 0;
@@ -1798,8 +1826,10 @@ static void prepare_extensions(or_scene* s)
                                 vlo = v < vlo ? v : vlo;
                                 vhi = v > vhi ? v : vhi;
                             }
+                    /* a truncated blend can land one intensity below the
+                       smallest corner (float rounding of (1 - t) a + t b) */
                     float m = 0.0f;
-                    for (int i = vlo; i <= (int)vhi; i++) m = s->sigma[i] > m ? s->sigma[i] : m;
+                    for (int i = vlo > 0 ? (int)vlo - 1 : 0; i <= (int)vhi; i++) m = s->sigma[i] > m ? s->sigma[i] : m;
                     s->majorant[((size_t)bz * s->nb[1] + by) * s->nb[0] + bx] = s->st.density_scale * m;
                 }
         empty_skip_distances(s->majorant, s->nb);
@@ -2357,9 +2387,8 @@ void ER_OR(majorant_grid)(const uint16_t* vox, const int32_t* res, int32_t B, co
                 int lo[3], hi[3];
                 const int b[3] = { bx, by, bz };
                 for (int i = 0; i < 3; i++) {
-                    lo[i] = b[i] * B - 1;
-                    hi[i] = (b[i] + 1) * B + 1;
-                    lo[i] = lo[i] < 0 ? 0 : lo[i];
+                    lo[i] = b[i] * B;
+                    hi[i] = (b[i] + 1) * B;
                     hi[i] = hi[i] > res[i] - 1 ? res[i] - 1 : hi[i];
                 }
                 int vlo = 65535, vhi = 0;
@@ -2370,7 +2399,8 @@ void ER_OR(majorant_grid)(const uint16_t* vox, const int32_t* res, int32_t B, co
                             vlo = v < vlo ? v : vlo;
                             vhi = v > vhi ? v : vhi;
                         }
-                vlo = vlo > n - 1 ? n - 1 : vlo;
+                vlo = vlo - 1;
+                vlo = vlo < 0 ? 0 : (vlo > n - 1 ? n - 1 : vlo);
                 vhi = vhi > n - 1 ? n - 1 : vhi;
                 float m = 0.0f;
                 for (int i = vlo; i <= vhi; i++) m = sigma[i] > m ? sigma[i] : m;

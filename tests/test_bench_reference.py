@@ -52,16 +52,17 @@ class Cam:
 
 
 def test_batched_reference_rate_weighting(monkeypatch):
-    """each volume's rate is measured on its first view, and the batch's rate
-    is its samples over the time each volume's samples take at that rate"""
+    """each volume's rate is the harmonic mean of views spread over its orbit
+    (here both of its views), and the batch's rate is its samples over the
+    time each volume's samples take at that rate"""
     bench = load_bench()
-    rates = {0: 100.0, 1: 400.0}
+    rates = {8: 100.0, 4: 300.0, 16: 400.0, 32: 200.0}
     seen = []
 
     def fake_rate(scene, seconds_target=12.0, nthreads=None, steps=1):
         k = scene.tracer.camera.film_size[0]          # the view's film width names the volume here
         seen.append((k, seconds_target, steps))
-        return rates[0 if k == 8 else 1], "port", 3, "16x16 centre crop x 1 spp per step"
+        return rates[k], "port", 3, "16x16 centre crop x 1 spp per step"
 
     class Tracer:
         camera = None
@@ -76,8 +77,11 @@ def test_batched_reference_rate_weighting(monkeypatch):
     views = [(0, Cam(8, 8), 10), (1, Cam(16, 16), 2), (0, Cam(4, 4), 5), (1, Cam(32, 32), 1)]
     rate, kind, cores, sample = bench.batched_reference_rate([None, None], views, seconds_target=6.0, steps=2)
     n0, n1 = 8 * 8 * 10 + 4 * 4 * 5, 16 * 16 * 2 + 32 * 32 * 1
-    assert rate == pytest.approx((n0 + n1) / (n0 / 100.0 + n1 / 400.0))
+    t0 = n0 * (1 / 100.0 + 1 / 300.0) / 2
+    t1 = n1 * (1 / 400.0 + 1 / 200.0) / 2
+    assert rate == pytest.approx((n0 + n1) / (t0 + t1))
     assert (kind, cores) == ("port", 3)
-    assert [s[0] for s in seen] == [8, 16]                # first view of each volume, in volume order
-    assert all(s[1] == pytest.approx(3.0) and s[2] == 2 for s in seen)
-    assert "volume 0: 16x16" in sample and "volume 1: 16x16" in sample
+    assert [s[0] for s in seen] == [8, 4, 16, 32]         # every view of each volume (two each), in volume order
+    assert all(s[1] == pytest.approx(1.5) and s[2] == 2 for s in seen)
+    assert "100 .. 400" not in sample and "0.0001 .. 0.0004" in sample
+    assert "volume 0: 2 views, 16x16" in sample and "volume 1: 2 views, 16x16" in sample

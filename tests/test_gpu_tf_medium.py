@@ -122,8 +122,9 @@ def test_binary64_tracks_float_and_the_oracle(torch, lib, pkg):
         s32 = s32.cpu().numpy()
         # a collision or roulette decision whose threshold falls between the
         # float and the double value takes another path: such pixels differ
-        # by a whole sample; every other pixel agrees to float rounding
-        close = np.isclose(s32, s64, rtol=1e-4, atol=1e-6 * np.abs(s64).max()).all(-1)
+        # by a whole sample; every other pixel agrees to float rounding of
+        # its path (products of transmittances: ~1e-4 of the image's peak)
+        close = np.isclose(s32, s64, rtol=1e-4, atol=2e-4 * np.abs(s64).max()).all(-1)
         flips = int((~close).sum())
         assert flips <= max(2, close.size // 100), (flips, float(np.abs(s32 - s64).max()))
         assert abs(float(s32.sum()) - float(s64.sum())) <= 2e-2 * float(np.abs(s64).sum()), (s32.sum(), s64.sum())
