@@ -120,7 +120,8 @@ struct WavefrontBuffers {
     float4* events;      /* 5 * max_items */
     float4* jobs;        /* 6 * max_items */
     float4* partial;     /* 2 * max_npix: sums of a view cut by a window boundary */
-    uint32_t* counters;  /* 4: events, shadow jobs, items and jobs taken by the persistent stages */
+    float4* records;     /* 5 * max_items when sort_shade: shading records by shader (BRDF from the front, phase from the back) */
+    uint32_t* counters;  /* 6: events, shadow jobs, items and jobs taken by the persistent stages, BRDF and phase records */
     int tune_primary;    /* resident blocks per SM targeted by the primary stage (2, 3, 4, 6, 8) */
     int tune_shadow;     /* same for the shadow stage */
     int tune_shade;      /* resident 128-thread blocks per SM of the shade stage (2, 3, 4, 6) */
@@ -130,6 +131,8 @@ struct WavefrontBuffers {
     int pt_shadow;       /* the persistent-lane shadow stage runs (every view delta-tracks) */
     int skip_primary;    /* the free-flight stage compiles the empty-space skip */
     int skip_shadow;     /* the shadow stage compiles the empty-space skip */
+    int sort_shade;      /* a view's shader switch mixes BRDF and phase events: the shade stage runs as
+                            k_wf_classify + k_wf_shade_sorted (records must be allocated) */
 };
 
 /* cuts the items of views (npix[v] * spp[v] each) into windows of whole

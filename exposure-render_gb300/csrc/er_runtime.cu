@@ -106,7 +106,7 @@ constexpr size_t kWindowCap = (size_t)8 << 20;
 
 /* queues of the wavefront stages, grown to the largest plan seen */
 struct WfQueues {
-    DevBuf<float4> results, events, jobs, partial;
+    DevBuf<float4> results, events, jobs, partial, records;
     DevBuf<uint32_t> counters;
     cudaError_t ensure(const WavefrontPlan& plan, WavefrontBuffers& B)
     {
@@ -115,11 +115,13 @@ struct WfQueues {
         if ((e = events.ensure(5 * plan.max_items)) != cudaSuccess) return e;
         if ((e = jobs.ensure(6 * plan.max_items)) != cudaSuccess) return e;
         if ((e = partial.ensure(2 * (size_t)plan.max_npix)) != cudaSuccess) return e;
-        if ((e = counters.ensure(4)) != cudaSuccess) return e;
+        if ((e = counters.ensure(6)) != cudaSuccess) return e;
         B.results = results.p;
         B.events = events.p;
         B.jobs = jobs.p;
         B.partial = partial.p;
+        B.records = nullptr;
+        B.sort_shade = 0;
         B.counters = counters.p;
         B.tune_primary = 4;
         B.tune_shadow = 4;
@@ -131,7 +133,25 @@ struct WfQueues {
         B.skip_shadow = 0;
         return cudaSuccess;
     }
+    /* the shading records of the sorted shade stage, when a view mixes shaders */
+    cudaError_t ensure_sorted(const WavefrontPlan& plan, bool mixed, WavefrontBuffers& B)
+    {
+        B.sort_shade = 0;
+        if (!mixed) return cudaSuccess;
+        cudaError_t e = records.ensure(5 * plan.max_items);
+        if (e != cudaSuccess) return e;
+        B.records = records.p;
+        B.sort_shade = 1;
+        return cudaSuccess;
+    }
 };
+
+/* the shader switch picks BRDF or phase per event (hybrid, modulation,
+   threshold), so the sorted shade stage pays */
+bool mixes_shaders(const erd::Params& P)
+{
+    return P.apply_shading_type && P.shading_type >= ER_SHADING_HYBRID && P.shading_type <= ER_SHADING_THRESHOLD;
+}
 
 float smin_h(float a, float b) { return (b < a) ? b : a; }
 float smax_h(float a, float b) { return (a < b) ? b : a; }
@@ -746,6 +766,7 @@ er_status trace_sum(TracerItem& t, int spp, uint32_t view, uint32_t first, float
     B.tune_shade = t.d.settings.tune_shade > 0 ? t.d.settings.tune_shade : 2;
     B.objects = t.P.object_count > 0;
     persistent_stages(t.d.settings.tune_stages, t.P.free_flight == ER_FREE_FLIGHT_DELTA, B);
+    ER_CUDA(t.wf.ensure_sorted(plan, mixes_shaders(t.P), B));
     WfView V;
     memset(&V, 0, sizeof(V));
     V.P = t.P;
@@ -840,12 +861,14 @@ er_status batch_plan(BatchItem& b)
     b.B.tune_shadow = b.tune_shadow;
     b.B.tune_shade = b.tune_shade;
     b.B.objects = 0;
-    bool all_delta = true;
+    bool all_delta = true, mixed = false;
     for (const WfView& hv : b.host_views) {
         b.B.objects |= hv.P.object_count > 0;
         all_delta = all_delta && hv.P.free_flight == ER_FREE_FLIGHT_DELTA;
+        mixed = mixed || mixes_shaders(hv.P);
     }
     persistent_stages(b.tune_stages, all_delta, b.B);
+    ER_CUDA(b.wf.ensure_sorted(b.plan, mixed, b.B));
     if (b.flags & ER_BATCH_GRAPH) {
         if (!b.capture_stream) ER_CUDA(cudaStreamCreateWithFlags(&b.capture_stream, cudaStreamNonBlocking));
         ER_CUDA(cudaStreamBeginCapture(b.capture_stream, cudaStreamCaptureModeThreadLocal));

@@ -476,6 +476,212 @@ __global__ void __launch_bounds__(128, MINB) k_wf_shade(const WfView* __restrict
     }
 }
 
+/* ---- stage 2 sorted by shader: classification, then shading ---- */
+
+/* When a launch's shader switch mixes BRDF and phase events (hybrid,
+   modulation and threshold shading), the shade stage runs as two kernels:
+   k_wf_classify does the part every event shares (normal and gradient
+   magnitude from the six central-difference lookups, intensity, transfer
+   functions, light choice, the shader switch with its random draw) and
+   appends a shading record to the queue of its shader - BRDF records from
+   the front of the record buffer, phase records from its back - and
+   k_wf_shade_sorted shades the records in that order, so a warp evaluates
+   one shader instead of both.  The operations and random draws are those of
+   k_wf_shade, in the same order: the sums are bit-identical.
+
+   record (5 float4): (sample, rng.s0, rng.s1, view), (P, I | light << 16 |
+   shader << 28), (N, brdf_component), (Wo, brdf_dir.x), (light_uvw,
+   brdf_dir.y); I is an integer intensity (< 2^16), light < 2^12 */
+template <bool ONE>
+__global__ void __launch_bounds__(128, 6) k_wf_classify(const WfView* __restrict__ views, const WfView one, const float4* __restrict__ events,
+                                                        const uint32_t* __restrict__ n_events, float4* __restrict__ results,
+                                                        float4* __restrict__ records, uint32_t cap, uint32_t* __restrict__ n_records)
+{
+    const uint32_t n = *n_events;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t e_i = base + threadIdx.x;
+        bool push = false;
+        int type = 0, idx = 0;
+        uint32_t sample = 0, v = 0;
+        float I = 0.0f;
+        Rng rng;
+        rng.s0 = 0u;
+        rng.s1 = 0u;
+        Event SE;
+        Metro ms;
+        if (e_i < n) {
+            const float4* e = events + (size_t)e_i * 5;
+            const float4 e0 = e[0], e1 = e[1], e2 = e[2], e3 = e[3], e4 = e[4];
+            sample = f2u(e0.x);
+            rng.s0 = f2u(e0.y);
+            rng.s1 = f2u(e0.z);
+            v = f2u(e4.w);
+            const Params& P = view_of<ONE>(views, one, v).P;
+            ms.light_num = e0.w;
+            ms.brdf_component = e1.w;
+            ms.brdf_dir.x = e2.w;
+            ms.brdf_dir.y = e3.w;
+            ms.light_uvw = V3(e4.x, e4.y, e4.z);
+            SE.type = 0; SE.valid = true; SE.T = 0.0f; SE.Le = C3(0, 0, 0);
+            SE.P = V3(e1.x, e1.y, e1.z);
+            float gm = -1.0f;
+            if (P.gradient_mode == 1) {
+                Grad6 g6;
+                gradient_samples(P, SE.P, g6);
+                SE.N = vnorm(gradient_cd6(g6));
+                if (P.apply_shading_type && P.shading_type >= 2 && P.shading_type <= 4) gm = gradient_magnitude6(P, g6);
+            } else {
+                SE.N = normalized_gradient(P, SE.P);
+            }
+            SE.Wo = V3(e3.x, e3.y, e3.z);
+            I = get_intensity(P, SE.P);
+            ShadeTF tf;
+            shade_tf(P, I, tf);
+            bool early = P.light_count <= 0;
+            if (!early) {
+                idx = (int)floorf(ms.light_num * (float)P.light_count);
+                early = idx < 0 || idx >= P.light_count || !P.light_valid[idx];
+            }
+            if (early) {
+                const c3 Lv = cadd(C3(0, 0, 0), cadd(C3(0, 0, 0), tf.Le));
+                results[sample] = make_float4(Lv.r, Lv.g, Lv.b, 1.0f);
+            } else {
+                type = P.apply_shading_type ? select_shader_type(P, SE, I, rng, gm) : 0;
+                push = true;
+            }
+        }
+        const uint32_t s_brdf = queue_slot(push && type == 0, n_records);
+        const uint32_t s_phase = queue_slot(push && type != 0, n_records + 1);
+        if (push) {
+            float4* r = records + (size_t)(type == 0 ? s_brdf : cap - 1u - s_phase) * 5;
+            r[0] = make_float4(u2f(sample), u2f(rng.s0), u2f(rng.s1), u2f(v));
+            r[1] = make_float4(SE.P.x, SE.P.y, SE.P.z, u2f((uint32_t)I | ((uint32_t)idx << 16) | ((uint32_t)type << 28)));
+            r[2] = make_float4(SE.N.x, SE.N.y, SE.N.z, ms.brdf_component);
+            r[3] = make_float4(SE.Wo.x, SE.Wo.y, SE.Wo.z, ms.brdf_dir.x);
+            r[4] = make_float4(ms.light_uvw.x, ms.light_uvw.y, ms.light_uvw.z, ms.brdf_dir.y);
+        }
+    }
+}
+
+/* MINB: resident 128-thread blocks per SM, as k_wf_shade */
+template <bool ONE, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_wf_shade_sorted(const WfView* __restrict__ views, const WfView one,
+                                                               const float4* __restrict__ records, uint32_t cap,
+                                                               const uint32_t* __restrict__ n_records, float4* __restrict__ results,
+                                                               float4* __restrict__ jobs, uint32_t* __restrict__ n_jobs)
+{
+    const uint32_t nb = n_records[0];
+    const uint32_t n = nb + n_records[1];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        bool push = false;
+        uint32_t sample = 0, flags = 0, v = 0;
+        Rng rng;
+        rng.s0 = 0u;
+        rng.s1 = 0u;
+        Event SE;
+        c3 Le = C3(0, 0, 0), c1 = C3(0, 0, 0), c2 = C3(0, 0, 0);
+        v3 S1 = V3(0, 0, 0), S2 = V3(0, 0, 0);
+        float count = 0.0f;
+        if (i < n) {
+            const float4* r = records + (size_t)(i < nb ? i : cap - 1u - (i - nb)) * 5;
+            const float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3], r4 = r[4];
+            sample = f2u(r0.x);
+            rng.s0 = f2u(r0.y);
+            rng.s1 = f2u(r0.z);
+            v = f2u(r0.w);
+            const Params& P = view_of<ONE>(views, one, v).P;
+            const uint32_t meta = f2u(r1.w);
+            const float I = (float)(meta & 0xffffu);
+            const int idx = (int)((meta >> 16) & 0xfffu);
+            const int type = (int)(meta >> 28);
+            Metro ms;
+            ms.brdf_component = r2.w;
+            ms.brdf_dir.x = r3.w;
+            ms.brdf_dir.y = r4.w;
+            ms.light_uvw = V3(r4.x, r4.y, r4.z);
+            SE.type = 0; SE.valid = true; SE.T = 0.0f; SE.Le = C3(0, 0, 0);
+            SE.P = V3(r1.x, r1.y, r1.z);
+            SE.N = V3(r2.x, r2.y, r2.z);
+            SE.Wo = V3(r3.x, r3.y, r3.z);
+            ShadeTF tf;
+            shade_tf(P, I, tf);
+            Le = cadd(C3(0, 0, 0), tf.Le);
+            {
+                const Light& L = P.lights[idx];
+                Shader sh;
+                shader_init(sh, type, SE.N, SE.Wo, tf.Kd, tf.Ks, P.volume_ior, tf.exponent);
+                count = (float)P.light_count;
+                /* EstimateDirectLight - Source/transport.h:58-113, without the visibility terms */
+                v3 Wi;
+                c3 Li;
+                Surf SS;
+                sample_light(P, L, ms.light_uvw, SS, SE, Wi, Li);
+                const c3 F = shader_f(sh, SE.Wo, Wi);
+                const bool full = P.mis == 1;
+                const float BsdfPdf = full ? mis_bsdf_pdf(sh, SE.Wo, Wi) : shader_pdf(sh, SE.Wo, Wi);
+                if (!cblack(Li) && !cblack(F) && BsdfPdf > 0.0f) {
+                    const float LightPdf = vlen2(vsub(SE.P, SS.P)) / (vabsdot(SS.N, vneg(Wi)) * L.area);
+                    if (full) {
+                        const float w = power_heuristic(LightPdf, BsdfPdf);
+                        c1 = cscale(cmul(F, Li), sh.type == 0 ? vabsdot(Wi, SE.N) * w / LightPdf : w / LightPdf);
+                    } else if (sh.type == 0) {
+                        c1 = cscale(cmul(F, Li), vabsdot(Wi, SE.N) * power_heuristic(LightPdf, BsdfPdf) / LightPdf);
+                    } else {
+                        c1 = cdivs(cmul(F, Li), LightPdf);
+                    }
+                    S1 = SS.P;
+                    flags |= WF_RAY1;
+                }
+                if (full) {
+                    const v3 Wb = sample_bsdf_dir(sh, SE.Wo, ms);
+                    const c3 Fb = shader_f(sh, SE.Wo, Wb);
+                    const float pb = mis_bsdf_pdf(sh, SE.Wo, Wb);
+                    if (!cblack(Fb) && pb > 0.0f) {
+                        Ray R2;
+                        R2.O = SE.P;
+                        R2.D = Wb;
+                        R2.MinT = 0.0f;
+                        R2.MaxT = 1000000.0f;
+                        Event SE2;
+                        SE2.type = 1; SE2.valid = false; SE2.T = 0.0f; SE2.Le = C3(0, 0, 0);
+                        SE2.P = V3(0, 0, 0); SE2.N = V3(0, 0, 0); SE2.Wo = V3(0, 0, 0);
+                        int hit = -1;
+                        LightHit lh;
+                        intersect_lights_geom(P, R2, SE2, false, hit, lh);
+                        if (SE2.valid && P.light_ids[hit] == P.light_ids[idx]) SE2.Le = light_emission(P, P.lights[hit], lh);
+                        if (SE2.valid && P.light_ids[hit] == P.light_ids[idx] && !cblack(SE2.Le)) {
+                            const float LightPdf = vlen2(vsub(SE.P, SE2.P)) / (vabsdot(SE2.N, vneg(Wb)) * L.area);
+                            const float w = power_heuristic(pb, LightPdf);
+                            c2 = cscale(cmul(Fb, SE2.Le), sh.type == 0 ? vabsdot(Wb, SE.N) * w / pb : w / pb);
+                            S2 = SE2.P;
+                            flags |= WF_RAY2;
+                        }
+                    }
+                }
+                if (flags == 0) {
+                    const c3 Lv = cadd(C3(0, 0, 0), cscale(cadd(Le, C3(0, 0, 0)), count));
+                    results[sample] = make_float4(Lv.r, Lv.g, Lv.b, 1.0f);
+                } else {
+                    push = true;
+                }
+            }
+        }
+        const uint32_t slot = queue_slot(push, n_jobs);
+        if (push) {
+            float4* j = jobs + (size_t)slot * 6;
+            j[0] = make_float4(u2f(sample), u2f(rng.s0), u2f(rng.s1), u2f(flags));
+            j[1] = make_float4(SE.P.x, SE.P.y, SE.P.z, count);
+            j[2] = make_float4(S1.x, S1.y, S1.z, Le.r);
+            j[3] = make_float4(c1.r, c1.g, c1.b, Le.g);
+            j[4] = make_float4(S2.x, S2.y, S2.z, Le.b);
+            j[5] = make_float4(c2.r, c2.g, c2.b, u2f(v));
+        }
+    }
+}
+
 /* ---- stage 3: shadow segments and the sample's sum ---- */
 
 template <int MINB, bool ONE, bool OBJ, bool SKIP>
@@ -774,7 +980,7 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         const WfSegment one_seg = plan.segs[s0];
         float4* p_in = B.partial + (size_t)((w + 1) & 1) * plan.max_npix;
         float4* p_out = B.partial + (size_t)(w & 1) * plan.max_npix;
-        cudaError_t e = cudaMemsetAsync(B.counters, 0, 4 * sizeof(uint32_t), s);
+        cudaError_t e = cudaMemsetAsync(B.counters, 0, 6 * sizeof(uint32_t), s);
         if (e != cudaSuccess) return e;
         const uint32_t g1 = (items + 255) / 256 < (uint32_t)sm * 64 ? (items + 255) / 256 : (uint32_t)sm * 64;
         cudaEvent_t t0 = stage_begin(s);
@@ -817,13 +1023,26 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         stage_end(t0, 0, s);
         t0 = stage_begin(s);
 #define ER_SHADE(M, O) k_wf_shade<ONE, M, O><<<sm * 16, 128, 0, s>>>(d_views, one, B.events, B.counters, B.results, B.jobs, B.counters + 1)
+#define ER_SORTED(M) k_wf_shade_sorted<ONE, M><<<sm * 16, 128, 0, s>>>(d_views, one, B.records, cap, B.counters + 4, B.results, B.jobs, \
+                                                                    B.counters + 1)
+        const uint32_t cap = (uint32_t)plan.max_items;
         if (B.objects) ER_SHADE(2, true);
-        else switch (B.tune_shade) {
+        else if (B.sort_shade) {
+            /* shader switch mixing BRDF and phase events: classify, then shade by shader */
+            k_wf_classify<ONE><<<sm * 16, 128, 0, s>>>(d_views, one, B.events, B.counters, B.results, B.records, cap, B.counters + 4);
+            switch (B.tune_shade) {
+            case 3: ER_SORTED(3); break;
+            case 4: ER_SORTED(4); break;
+            case 6: ER_SORTED(6); break;
+            default: ER_SORTED(2); break;
+            }
+        } else switch (B.tune_shade) {
         case 3: ER_SHADE(3, false); break;
         case 4: ER_SHADE(4, false); break;
         case 6: ER_SHADE(6, false); break;
         default: ER_SHADE(2, false); break;
         }
+#undef ER_SORTED
 #undef ER_SHADE
         stage_end(t0, 1, s);
         t0 = stage_begin(s);

@@ -216,3 +216,27 @@ def test_empty_space_jump_bit_exact(env, oracle, brick, stages, engine):
     finally:
         r.close()
         h.close()
+
+
+@pytest.mark.parametrize("shading", [2, 3, 4], ids=["hybrid", "modulation", "threshold"])
+@pytest.mark.parametrize("tune_shade", [2, 3, 4, 6])
+def test_sorted_shade_stage_bit_exact(env, oracle, shading, tune_shade):
+    """a shader switch that mixes BRDF and phase events runs the shade stage
+    as classification + shading sorted by shader (k_wf_classify,
+    k_wf_shade_sorted) in every occupancy variant: the oracle's sums"""
+    torch, lib, rt = env
+    sc = two_light_scene(17)
+    s = sc.tracer.settings
+    s.free_flight, s.mis, s.apply_shading_type, s.shading_type, s.tune_shade = 1, 1, 1, shading, tune_shade
+    r = rt.Renderer(sc, lib)
+    h = OL.SceneHandle(oracle, sc)
+    try:
+        d = torch.zeros((sc.height, sc.width, 4), dtype=torch.float32, device="cuda")
+        r.trace_sum_device(d.data_ptr(), 6, 4, 3, 0, None)
+        torch.cuda.synchronize()
+        cpu = h.render_sum(6, view=4, first=3, nthreads=4)
+        assert np.array_equal(bits(d.cpu().numpy()), bits(cpu))
+        assert cpu[..., 3].sum() > 0
+    finally:
+        r.close()
+        h.close()

@@ -215,8 +215,9 @@ def test_autograd_function(torch, lib, pkg):
         smp, s = m.render_samples(rho, vals, spp)
         dsum = 2.0 * (s / spp - target) / spp
         g_rho, g_tf = m.adjoint(rho, vals, spp, dsum, smp)
-        assert torch.allclose(v_p.grad, g_tf, rtol=1e-5, atol=1e-7 * float(g_tf.abs().max()))
-        assert torch.allclose(rho_p.grad, g_rho, rtol=1e-5, atol=1e-7 * float(g_rho.abs().max()))
+        # two walks of the same samples: equal up to the order of the atomic sums
+        assert torch.allclose(v_p.grad, g_tf, rtol=1e-5, atol=1e-6 * float(g_tf.abs().max()))
+        assert torch.allclose(rho_p.grad, g_rho, rtol=1e-5, atol=1e-6 * float(g_rho.abs().max()))
     finally:
         r.close()
 
