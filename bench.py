@@ -298,7 +298,8 @@ def convergence(lib, runtime, torch, names, patches, max_spp=4096, target=1e-2):
 FILM_SCHEDULE = (8, 16, 32, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048)
 
 
-def film_convergence(lib, torch, r, patches, ref_patch, ref_spp, target=1e-2, budget_s=45.0, stream=None, film=None):
+def film_convergence(lib, torch, r, patches, ref_patch, ref_spp, target=1e-2, budget_s=45.0, stream=None, film=None,
+                     unbiased=("fast",)):
     """Samples per pixel to image RMSE `target` at the workload's own film.
 
     The converged image is the unbiased estimator (`ref_patch`: delta
@@ -311,7 +312,9 @@ def film_convergence(lib, torch, r, patches, ref_patch, ref_spp, target=1e-2, bu
     configuration of `patches` then renders from view 0 along FILM_SCHEDULE
     until its RMSE reaches `target` (or `budget_s` of rendering is spent).
     `film`: (W, H) of the bound tracer's camera when it differs from the
-    scene's."""
+    scene's.  `unbiased`: the configurations with the reference's
+    expectation, whose samples-to-target come from a fit of the whole curve
+    (the others, such as the biased fixed-step march, from the crossing)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import convergence as CV
     W, H = film if film else (r.width, r.height)
@@ -363,7 +366,18 @@ def film_convergence(lib, torch, r, patches, ref_patch, ref_spp, target=1e-2, bu
             errs.append(err)
             if err <= target or spent > budget_s:
                 break
-        out[label] = {"spp": spps, "rmse": errs, "spp_to_target": CV.spp_to_rmse(spps, errs, target)}
+        crossing = CV.spp_to_rmse(spps, errs, target)
+        out[label] = {"spp": spps, "rmse": errs, "spp_to_target": crossing}
+        if label in unbiased:
+            # an estimator with the reference's expectation converges as
+            # rmse^2 = var / n: every schedule point from 32 spp on implies
+            # n (rmse / target)^2; their geometric mean is far less noisy than
+            # the crossing of two points when rare bright samples dominate
+            implied = [n_ * (e_ / target) ** 2 for n_, e_ in zip(spps, errs) if n_ >= 32 and e_ > 0]
+            if implied:
+                out[label]["spp_to_target"] = float(np.exp(np.mean(np.log(implied))))
+                out[label]["spp_to_target_crossing"] = crossing
+                out[label]["method"] = "geometric mean of n (rmse_n / target)^2 over the points n >= 32"
         del acc
     apply(saved)
     return out
@@ -376,7 +390,8 @@ def film_rmse_summary(fc, fast_value, plain_value, npix, target=1e-2):
         return None
     f, p = fc["fast"]["spp_to_target"], fc["plain"]["spp_to_target"]
     out = {"target": target, "reference": fc["reference"],
-           "fast": {"spp": f, "seconds": f * npix / (fast_value * 1e6) if f else None, "curve": [fc["fast"]["spp"], fc["fast"]["rmse"]]},
+           "fast": {"spp": f, "seconds": f * npix / (fast_value * 1e6) if f else None, "curve": [fc["fast"]["spp"], fc["fast"]["rmse"]],
+                    "spp_crossing": fc["fast"].get("spp_to_target_crossing"), "method": fc["fast"].get("method", "crossing")},
            "plain": {"spp": p, "seconds": p * npix / (plain_value * 1e6) if p else None,
                      "curve": [fc["plain"]["spp"], fc["plain"]["rmse"]]}}
     if f and p:
@@ -414,6 +429,9 @@ def batched_rmse_summary(conv, value, plain_value, target=1e-2):
                      "reference_noise": c["reference_noise"] if "reference_noise" in c else c["reference"]["noise"]}
         if "reference" in c and isinstance(c["reference"], dict):
             per[name]["film"] = c["reference"]["film"]
+            per[name]["curves"] = {k: [c[k]["spp"], c[k]["rmse"]] for k in ("fast", "plain")}
+            if "spp_to_target_crossing" in c["fast"]:
+                per[name]["fast_spp_crossing"] = c["fast"]["spp_to_target_crossing"]
         if f and p:
             ratios.append(p / f)
     out = {"target": target, "views": per, "throughput_ratio": value / plain_value}

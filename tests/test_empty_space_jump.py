@@ -56,3 +56,45 @@ def test_jump_float_and_binary64_agree():
     assert noisy.sum() > 50
     z = (ma - mb)[noisy] / np.sqrt(v[noisy] / n)
     assert np.mean(z * z) < 1.5
+
+
+def test_majorant_brick_size_does_not_change_the_image():
+    """Delta and ratio tracking are unbiased for any majorant that bounds the
+    extinction of every lookup they make; the majorant of a brick covers only
+    the voxels a lookup clamped to that brick blends.  If a brick's bound
+    missed a lookup, the tight 1^3 bricks (a 2^3-voxel footprint each) would
+    render another image than 8^3 bricks: the c3 96^3 blob volume, 48^2
+    film, independent streams, per-pixel and whole-image z-tests."""
+    import importlib.util
+    import os
+    spec = importlib.util.spec_from_file_location("bench_for_test", os.path.join(OL.ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    scenes, views, _ = bench.batched_workload("c3", 0)
+    cam = [c for (k, c, _) in views if k == 0][0]
+    f32 = OL.load_oracle()
+    n = 512
+    out = []
+    for brick, view in ((1, 1), (8, 2)):
+        sc = scenes[0]
+        t = C.er_tracer_desc.from_buffer_copy(sc.tracer)
+        t.camera = cam
+        t.camera.film_size[0] = t.camera.film_size[1] = 48
+        t.settings.free_flight, t.settings.mis, t.settings.majorant_brick, t.settings.stratify = 1, 1, brick, 0
+        sc.tracer = t
+        h = OL.SceneHandle(f32, sc)
+        try:
+            out.append(h.render_moments(n, view=view, nthreads=os.cpu_count() or 4))
+        finally:
+            h.close()
+    (a, a2), (b, b2) = out
+    ma, mb = (a / n)[..., :3].astype(np.float64), (b / n)[..., :3].astype(np.float64)
+    va = np.maximum((a2 / n)[..., :3] - ma ** 2, 0.0)
+    vb = np.maximum((b2 / n)[..., :3] - mb ** 2, 0.0)
+    noisy = (va + vb) > 1e-9 * (1.0 + ma ** 2)
+    assert noisy.sum() > 500
+    z = (ma - mb)[noisy] / np.sqrt((va + vb)[noisy] / n)
+    assert np.mean(z * z) < 1.5
+    for c in range(3):
+        d = ma[..., c].sum() - mb[..., c].sum()
+        assert abs(d) < 4.0 * np.sqrt((va[..., c].sum() + vb[..., c].sum()) / n)
