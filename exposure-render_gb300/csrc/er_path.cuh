@@ -41,6 +41,20 @@ ER_D float lerp_u16(float t, float a, float b)
     return truncf(r);
 }
 
+/* the eight corners read voxel by voxel, clamped to the volume: lookups
+   without corner quads or at the x/y faces (out of line: it is rare, and
+   inlined it would sit in the trackers' hot loops) */
+static __device__ __noinline__ float get_intensity_voxels(const Params& P, int vx, int vy, int vz, float dx, float dy, float dz)
+{
+    const float d00 = lerp_u16(dx, voxel(P, vx, vy, vz), voxel(P, vx + 1, vy, vz));
+    const float d10 = lerp_u16(dx, voxel(P, vx, vy + 1, vz), voxel(P, vx + 1, vy + 1, vz));
+    const float d01 = lerp_u16(dx, voxel(P, vx, vy, vz + 1), voxel(P, vx + 1, vy, vz + 1));
+    const float d11 = lerp_u16(dx, voxel(P, vx, vy + 1, vz + 1), voxel(P, vx + 1, vy + 1, vz + 1));
+    const float d0 = lerp_u16(dy, d00, d10);
+    const float d1 = lerp_u16(dy, d01, d11);
+    return lerp_u16(dz, d0, d1);
+}
+
 /* the trilinear lookup at local voxel coordinates (Lx, Ly, Lz) */
 ER_D float get_intensity_local(const Params& P, float Lx, float Ly, float Lz)
 {
@@ -73,13 +87,7 @@ ER_D float get_intensity_local(const Params& P, float Lx, float Ly, float Lz)
         const float q11 = lerp_u16(dx, (float)(b.y & 0xffffu), (float)(b.y >> 16));
         return lerp_u16(dz, lerp_u16(dy, q00, q10), lerp_u16(dy, q01, q11));
     }
-    const float d00 = lerp_u16(dx, voxel(P, vx, vy, vz), voxel(P, vx + 1, vy, vz));
-    const float d10 = lerp_u16(dx, voxel(P, vx, vy + 1, vz), voxel(P, vx + 1, vy + 1, vz));
-    const float d01 = lerp_u16(dx, voxel(P, vx, vy, vz + 1), voxel(P, vx + 1, vy, vz + 1));
-    const float d11 = lerp_u16(dx, voxel(P, vx, vy + 1, vz + 1), voxel(P, vx + 1, vy + 1, vz + 1));
-    const float d0 = lerp_u16(dy, d00, d10);
-    const float d1 = lerp_u16(dy, d01, d11);
-    return lerp_u16(dz, d0, d1);
+    return get_intensity_voxels(P, vx, vy, vz, dx, dy, dz);
 }
 
 ER_D void local_coords(const Params& P, v3 p, float& Lx, float& Ly, float& Lz)
@@ -350,7 +358,8 @@ ER_D void intersect_volume(const Params& P, const Ray& R, Isect& I)
    (Source/sphere.h:147-150), InsideCylinder radial distance in x/z below
    OuterRadius and |y| below half of Size[2] (Source/cylinder.h:96-99, with
    the height Shape::Update uses, Source/shape.h:100). */
-ER_D bool clipped(const Params& P, v3 p)
+/* out of line: only views with clipping objects call it */
+ER_COLD bool clipped(const Params& P, v3 p)
 {
     for (int i = 0; i < P.clip_count; i++) {
         const Clip& c = P.clips[i];

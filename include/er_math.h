@@ -341,14 +341,17 @@ ER_MATH_FN void er_seed_lanes(uint32_t seed, uint32_t view, uint32_t pixel, uint
 }
 
 /* Stratified sample dimensions (er_render_settings.stratify).  For sample
-   `sample` of `pixel` in `view`, each stratified dimension comes from a
-   rank-1 lattice over the sample index shifted per pixel and dimension by a
-   hash of (seed, view, pixel) (a Cranley-Patterson rotation): the R2
-   sequence (generators 2^32/g and 2^32/g^2, g the plastic number) for the
-   2D dimensions, the golden-ratio sequence for the 1D ones.  Successive
-   samples of a pixel cover each dimension evenly; each sample alone is
-   uniform, so estimates stay unbiased.  Integer arithmetic, 23-bit
-   mantissas in (0, 1): identical on every host and device.
+   `sample` of `pixel` in `view`, the seven stratified dimensions are one
+   point of the 7-dimensional Kronecker sequence R7 over the sample index
+   (generator k = frac(g^-k) * 2^32, k = 1..7, g the positive root of
+   x^8 = x + 1), shifted per pixel and dimension by a hash of (seed, view,
+   pixel) (a Cranley-Patterson rotation).  The generators are distinct, so
+   a pixel's points fill the 7-cube evenly as the samples grow and its
+   estimate converges to the integral; dimensions sharing a generator would
+   keep every point of the pixel on a lower-dimensional torus, and the
+   pixel would converge to the integral along that torus instead.  Each
+   sample alone is uniform, so estimates stay unbiased.  Integer arithmetic,
+   23-bit mantissas in (0, 1): identical on every host and device.
      out[0], out[1]: point on the light (MetroSample light u, v)
      out[2]        : light choice
      out[3], out[4]: BSDF direction
@@ -361,13 +364,13 @@ ER_MATH_FN void er_stratified_sample(uint32_t seed, uint32_t view, uint32_t pixe
     uint32_t h = er_hash32(seed * 0x9e3779b9u + 0x1b873593u);
     h = er_hash32(h ^ (view * 0x85ebca6bu));
     h = er_hash32(h + pixel);
-    out[0] = er_lattice_unit(er_hash32(h ^ 0x3c6ef372u) + sample * 3242174889u);
-    out[1] = er_lattice_unit(er_hash32(h ^ 0xa54ff53au) + sample * 2447445413u);
-    out[2] = er_lattice_unit(er_hash32(h ^ 0x510e527fu) + sample * 2654435769u);
-    out[3] = er_lattice_unit(er_hash32(h ^ 0x9b05688cu) + sample * 3242174889u);
-    out[4] = er_lattice_unit(er_hash32(h ^ 0x1f83d9abu) + sample * 2447445413u);
-    out[5] = er_lattice_unit(er_hash32(h ^ 0x5be0cd19u) + sample * 2654435769u);
-    out[6] = er_lattice_unit(er_hash32(h ^ 0xcbbb9d5du) + sample * 2654435769u);
+    out[0] = er_lattice_unit(er_hash32(h ^ 0x3c6ef372u) + sample * 3915259345u);
+    out[1] = er_lattice_unit(er_hash32(h ^ 0xa54ff53au) + sample * 3569120481u);
+    out[2] = er_lattice_unit(er_hash32(h ^ 0x510e527fu) + sample * 3253582939u);
+    out[3] = er_lattice_unit(er_hash32(h ^ 0x9b05688cu) + sample * 2965941329u);
+    out[4] = er_lattice_unit(er_hash32(h ^ 0x1f83d9abu) + sample * 2703729436u);
+    out[5] = er_lattice_unit(er_hash32(h ^ 0x5be0cd19u) + sample * 2464699080u);
+    out[6] = er_lattice_unit(er_hash32(h ^ 0xcbbb9d5du) + sample * 2246800835u);
 }
 
 #ifdef __cplusplus

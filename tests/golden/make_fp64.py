@@ -3,7 +3,8 @@ scenes.rmse_views() from the FP64 oracle (oracle/_build/liberfp64.so, the C
 restatement evaluated in binary64).
 
 Each image is the mean of N samples per pixel of the unbiased estimator
-(delta-tracked free flight, ratio-tracked shadows, full MIS) from its own
+(delta-tracked free flight, ratio-tracked shadows, full MIS, independent
+random draws) from its own
 random stream (seed 0x5EED64, view 7), rendered as two independent halves;
 the squared tone-mapped difference of the halves / 4 is the reference's own
 noise, stored as noise2.
@@ -36,6 +37,7 @@ def main():
         st = sc.tracer.settings
         st.free_flight = C.FREE_FLIGHT_DELTA
         st.mis = C.MIS_FULL
+        st.stratify = 0          # independent random draws: every pixel converges on its own
         st.majorant_brick = 2
         st.seed = 0x5EED64
         h = OL.SceneHandle(f64, sc)
