@@ -751,6 +751,13 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
     # all-reduced each step: one set of images over all ranks
     for sc in scenes:
         sc.tracer.settings.seed = R.view_seed(1, 0)
+    if args.bricks:
+        # fixed tuning (profiling runs with --no-tune): one majorant brick per volume
+        for sc, b in zip(scenes, (int(x) for x in args.bricks.split(","))):
+            sc.tracer.settings.majorant_brick = b
+    if args.stages is not None:
+        for sc in scenes:
+            sc.tracer.settings.tune_stages = args.stages
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -774,8 +781,8 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
     samples_per_step = sum(cam.film_size[0] * cam.film_size[1] * spp for _, cam, spp in views)
     max_spp = max(spp for _, _, spp in views)
     batch = runtime.Batch(table, flags=C.ER_BATCH_GRAPH)
-    # the tracking stages' persistent-lane mode and empty-space skips, timed
-    # on whole launches of this batch
+    # the tracking stages' persistent-lane mode, timed on whole launches of
+    # this batch
     batch_tune = batch.autotune(sp) if not args.no_tune else None
     if batch_tune:
         # the batch tuner writes the tracers' bricks: keep the Python-side
@@ -1200,6 +1207,8 @@ def main():
     ap.add_argument("--film", type=int, default=0, help="square film edge (smaller profiling cases; 0 = the workload's)")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel (0 = the workload's)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default settings)")
+    ap.add_argument("--bricks", default="", help="c3/c5: majorant brick per volume, comma-separated (with --no-tune)")
+    ap.add_argument("--stages", type=int, default=None, help="c3/c5: tune_stages of every volume's tracer (with --no-tune)")
     ap.add_argument("--no-rmse", action="store_true", help="skip the time-to-RMSE measurement")
     ap.add_argument("--medium", default="tracer", choices=["tracer", "spline"],
                     help="c4/c5 adjoint: the tracer's transfer functions and shading, or the B-spline medium")
