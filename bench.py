@@ -1168,6 +1168,35 @@ def run_medium(args, rank, world, local_rank):
     br_ms = timed(bwd_recompute, 1)
     C.check(lib.er_synchronize())
     samples = film[0] * film[1] * spp
+
+    # end to end, each step: the parameters (density grid, node values) from
+    # pinned host memory, forward, loss gradient, adjoint, both gradients back
+    # into pinned host memory (the optimiser on the host side of the API)
+    h_rho, h_tf = rho.cpu().pin_memory(), tf.cpu().pin_memory()
+    g_rho_h = torch.empty(rho.shape, dtype=torch.float32, pin_memory=True)
+    g_tf_h = torch.empty(tf.shape, dtype=torch.float32, pin_memory=True)
+    d_rho, d_tf = torch.empty_like(rho), torch.empty_like(tf)
+
+    def e2e_step():
+        d_rho.copy_(h_rho, non_blocking=True)
+        d_tf.copy_(h_tf, non_blocking=True)
+        smp, s = m.render_samples(d_rho, d_tf, spp)
+        d = 2.0 * (s / spp - target) / spp / target.numel()
+        g = m.adjoint(d_rho, d_tf, spp, d, smp)
+        g_rho_h.copy_(g[0], non_blocking=True)
+        g_tf_h.copy_(g[1], non_blocking=True)
+        torch.cuda.synchronize()
+
+    e2e_step()
+    e2e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_s = R.max_over_ranks(time.perf_counter() - t0, dist)
+    e2e = {"value": R.whole_job_rate(samples * e2e_steps, e2e_s, world) / 1e6, "unit": "Msamples/s (forward + adjoint)",
+           "h2d_bytes_per_step": int(h_rho.numel() * 4 + h_tf.numel() * 4),
+           "d2h_bytes_per_step": int(g_rho_h.numel() * 4 + g_tf_h.numel() * 4),
+           "ms_per_step": e2e_s / e2e_steps * 1e3}
     loss = float(((state["s"] / spp - target) ** 2).mean())
     if rank != 0:
         return
@@ -1184,12 +1213,15 @@ def run_medium(args, rank, world, local_rank):
                    "parallelism": "independent replicas (own seeds)" if world > 1 else "single"},
         "forward_ms": f_ms, "adjoint_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
         "adjoint_recompute_ms": br_ms, "adjoint_recompute_over_forward": br_ms / f_ms,
+        "e2e": e2e,
         "loss": loss, "grad_norm": {"density": float(state["g"][0].norm()), "opacity": float(state["g"][1].norm())},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         # per window of 2^21 items: forward count, jobs, shadow, gather (+ one reduce per step);
-        # adjoint count, jobs, shadow, primary replay, shadow replay
-        "gpu_launches": args.steps * (9 * (-(-spp // max(1, (1 << 21) // (film[0] * film[1])))) + 1),
+        # adjoint primary replay and shadow replay (one window: against the forward's kept jobs;
+        # several: count, jobs and shadow again per window)
+        "gpu_launches": args.steps * ((6 if spp * film[0] * film[1] <= (1 << 21) else 9)
+                                      * (-(-spp // max(1, (1 << 21) // (film[0] * film[1])))) + 1),
     }
     print(json.dumps(line), flush=True)
     r.close()
