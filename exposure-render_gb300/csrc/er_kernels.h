@@ -131,6 +131,8 @@ struct WavefrontBuffers {
     int pt_shadow;       /* the persistent-lane shadow stage runs (every view delta-tracks) */
     int skip_primary;    /* the free-flight stage compiles the empty-space skip */
     int skip_shadow;     /* the shadow stage compiles the empty-space skip */
+    int refill_eighths;  /* persistent stages refill a warp when fewer than this many eighths of its
+                            tracking lanes still track (1..7) */
     int sort_shade;      /* a view's shader switch mixes BRDF and phase events: the shade stage runs as
                             k_wf_classify + k_wf_shade_sorted (records must be allocated) */
 };

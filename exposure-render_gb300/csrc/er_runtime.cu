@@ -104,6 +104,19 @@ uint64_t fnv1a(uint64_t h, const void* data, size_t n)
 /* items of one wavefront window: 8M samples, 1.5 GB of queues */
 constexpr size_t kWindowCap = (size_t)8 << 20;
 
+/* the persistent stages' refill threshold in eighths of a warp's tracking
+   lanes: 3, or ER_PT_REFILL (1..7) for measurements */
+int refill_eighths()
+{
+    static int v = 0;
+    if (!v) {
+        const char* e = getenv("ER_PT_REFILL");
+        const int r = e ? atoi(e) : 3;
+        v = (r >= 1 && r <= 7) ? r : 3;
+    }
+    return v;
+}
+
 /* queues of the wavefront stages, grown to the largest plan seen */
 struct WfQueues {
     DevBuf<float4> results, events, jobs, partial, records;
@@ -122,6 +135,7 @@ struct WfQueues {
         B.partial = partial.p;
         B.records = nullptr;
         B.sort_shade = 0;
+        B.refill_eighths = refill_eighths();
         B.counters = counters.p;
         B.tune_primary = 4;
         B.tune_shadow = 4;

@@ -171,11 +171,9 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
 }
 
 /* persistent stages: a warp stops tracking to refill when fewer than
-   ER_PT_REFILL_EIGHTHS / 8 of the lanes that were tracking still are
-   (C3 batch: 3/8 and 4/8 give 1249 and 1240 Msamples/s, 6/8 1138, 7/8 978) */
-#ifndef ER_PT_REFILL_EIGHTHS
-#define ER_PT_REFILL_EIGHTHS 3
-#endif
+   refill / 8 of the lanes that were tracking still are (a launch argument,
+   WavefrontBuffers::refill_eighths; C3 batch: 3/8 and 4/8 give 1249 and
+   1240 Msamples/s, 6/8 1138, 7/8 978) */
 
 /* queue slot among the lanes that are here together (persistent stages,
    where lanes reach their queue pushes at different loop trips) */
@@ -204,7 +202,7 @@ template <int MINB, bool ONE, bool OBJ, bool SKIP>
 __global__ void __launch_bounds__(256, MINB) k_wf_primary_pt(const WfView* __restrict__ views, const WfSegment* __restrict__ segs,
                                                               int nseg, const WfView one, const WfSegment one_seg, uint32_t items,
                                                               float4* __restrict__ results, float4* __restrict__ events,
-                                                              uint32_t* __restrict__ n_events, uint32_t* __restrict__ fetch)
+                                                              uint32_t* __restrict__ n_events, uint32_t* __restrict__ fetch, int refill)
 {
     const int lane = threadIdx.x & 31;
     uint32_t i = 0;
@@ -256,7 +254,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary_pt(const WfView* __res
         const int n_work = __popc(__ballot_sync(0xffffffffu, tracking && !k.done));
         while (tracking && !k.done) {
             delta_step<SKIP>(P, R, rng, k);
-            if (k.done || 8 * __popc(__activemask()) < ER_PT_REFILL_EIGHTHS * n_work) break;
+            if (k.done || 8 * __popc(__activemask()) < refill * n_work) break;
         }
         if (!tracking || !k.done) continue;
         /* the sample's nearest event: volume, visible lights, objects */
@@ -732,7 +730,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_shadow(const WfView* __restric
 template <int MINB, bool ONE, bool OBJ, bool SKIP>
 __global__ void __launch_bounds__(256, MINB) k_wf_shadow_pt(const WfView* __restrict__ views, const WfView one,
                                                              const float4* __restrict__ jobs, const uint32_t* __restrict__ n_jobs,
-                                                             float4* __restrict__ results, uint32_t* __restrict__ fetch)
+                                                             float4* __restrict__ results, uint32_t* __restrict__ fetch, int refill)
 {
     const uint32_t n = *n_jobs;
     const int lane = threadIdx.x & 31;
@@ -791,7 +789,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_shadow_pt(const WfView* __rest
         const int n_work = __popc(__ballot_sync(0xffffffffu, seg_phase && !k.done));
         while (seg_phase && !k.done) {
             ratio_step<SKIP>(P, R, rng, k);
-            if (k.done || 8 * __popc(__activemask()) < ER_PT_REFILL_EIGHTHS * n_work) break;
+            if (k.done || 8 * __popc(__activemask()) < refill * n_work) break;
         }
         if (seg_phase && k.done) {
             const float4* j = jobs + (size_t)j_i * 6;
@@ -985,7 +983,7 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         const uint32_t g1 = (items + 255) / 256 < (uint32_t)sm * 64 ? (items + 255) / 256 : (uint32_t)sm * 64;
         cudaEvent_t t0 = stage_begin(s);
 #define ER_PRIMARY(M, O, K) k_wf_primary<M, ONE, O, K><<<g1, 256, 0, s>>>(d_views, dseg, nseg, one, one_seg, items, B.results, B.events, B.counters)
-#define ER_PRIMARY_PT(M, O, K) k_wf_primary_pt<M, ONE, O, K><<<sm * M, 256, 0, s>>>(d_views, dseg, nseg, one, one_seg, items, B.results, B.events, B.counters, B.counters + 2)
+#define ER_PRIMARY_PT(M, O, K) k_wf_primary_pt<M, ONE, O, K><<<sm * M, 256, 0, s>>>(d_views, dseg, nseg, one, one_seg, items, B.results, B.events, B.counters, B.counters + 2, B.refill_eighths)
         if (B.pt_primary) {
             /* delta tracking: persistent lanes, one resident wave */
             if (B.objects) ER_PRIMARY_PT(4, true, true);
@@ -1047,7 +1045,7 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         stage_end(t0, 1, s);
         t0 = stage_begin(s);
 #define ER_SHADOW(M, O, K) k_wf_shadow<M, ONE, O, K><<<sm * 8, 256, 0, s>>>(d_views, one, B.jobs, B.counters + 1, B.results)
-#define ER_SHADOW_PT(M, O, K) k_wf_shadow_pt<M, ONE, O, K><<<sm * M, 256, 0, s>>>(d_views, one, B.jobs, B.counters + 1, B.results, B.counters + 3)
+#define ER_SHADOW_PT(M, O, K) k_wf_shadow_pt<M, ONE, O, K><<<sm * M, 256, 0, s>>>(d_views, one, B.jobs, B.counters + 1, B.results, B.counters + 3, B.refill_eighths)
         if (B.pt_shadow) {
             /* ratio-tracked shadows: persistent lanes, one resident wave */
             if (B.objects) ER_SHADOW_PT(4, true, true);
