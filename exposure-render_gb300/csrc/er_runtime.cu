@@ -105,14 +105,16 @@ uint64_t fnv1a(uint64_t h, const void* data, size_t n)
 constexpr size_t kWindowCap = (size_t)8 << 20;
 
 /* the persistent stages' refill threshold in eighths of a warp's tracking
-   lanes: 3, or ER_PT_REFILL (1..7) for measurements */
+   lanes: 2, or ER_PT_REFILL (1..7) for measurements (with the empty-space
+   jump and tight bricks, C2 / C3 at 2, 3, 4, 5 eighths: 1336 / 2322, 1333 /
+   2266, 1317 / 2183, 1278 / 2051 Msamples/s) */
 int refill_eighths()
 {
     static int v = 0;
     if (!v) {
         const char* e = getenv("ER_PT_REFILL");
-        const int r = e ? atoi(e) : 3;
-        v = (r >= 1 && r <= 7) ? r : 3;
+        const int r = e ? atoi(e) : 2;
+        v = (r >= 1 && r <= 7) ? r : 2;
     }
     return v;
 }

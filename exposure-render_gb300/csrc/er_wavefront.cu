@@ -172,8 +172,8 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
 
 /* persistent stages: a warp stops tracking to refill when fewer than
    refill / 8 of the lanes that were tracking still are (a launch argument,
-   WavefrontBuffers::refill_eighths; C3 batch: 3/8 and 4/8 give 1249 and
-   1240 Msamples/s, 6/8 1138, 7/8 978) */
+   WavefrontBuffers::refill_eighths, 2 by default; measured in er_runtime.cu
+   refill_eighths) */
 
 /* queue slot among the lanes that are here together (persistent stages,
    where lanes reach their queue pushes at different loop trips) */
