@@ -73,14 +73,17 @@ def describe_shading(scene):
 class ClockSampler:
     """nvidia-smi samples during the timed region."""
 
+    QUERY = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
     def __init__(self, index=0):
         self.index = index
         self.proc = None
         self.lines = []
+        self.after = False
 
     def __enter__(self):
-        q = "clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
-            "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+        q = self.QUERY
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
                                           "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
@@ -101,6 +104,16 @@ class ClockSampler:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
+            if not self.lines:
+                # the timed region ended before nvidia-smi's first sample (a
+                # region of a few ms): one query right after it
+                try:
+                    out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=20)
+                    self.lines = [x.strip() for x in out.stdout.splitlines() if x.strip()]
+                    self.after = bool(self.lines)
+                except (OSError, subprocess.TimeoutExpired):
+                    pass
 
     def summary(self):
         sm, mx, reasons = [], [], set()
@@ -119,7 +132,10 @@ class ClockSampler:
                     reasons.add(n)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+        if self.after:
+            out["when"] = "right after the timed region, which ended before nvidia-smi's first sample"
+        return out
 
 
 def measured_peaks():
