@@ -1738,7 +1738,7 @@ ER_API er_status er_batch_autotune(int32_t batch_id, void* stream, int32_t* tune
     rs = er_batch_set_stages(batch_id, best);
     if (rs != ER_OK) return done(rs);
     /* last the occupancy variants of the tracking stages under that mode */
-    const int pairs[][2] = {{4, 4}, {3, 3}, {3, 4}, {4, 3}, {2, 3}, {2, 2}};
+    const int pairs[][2] = {{4, 4}, {3, 3}, {3, 4}, {4, 3}, {2, 3}, {2, 2}, {6, 4}, {4, 6}, {6, 6}};
     int best_p = b->tune_primary, best_s = b->tune_shadow;
     for (const auto& pr : pairs) {
         if (pr[0] == best_p && pr[1] == best_s) continue;
@@ -1831,11 +1831,11 @@ ER_API er_status er_autotune_tracer(int32_t tracer_id, int32_t probe_spp, er_tun
         s.tune_stages = r.tune_stages;
         if (wavefront) {
             /* occupancy pairs, with persistent-lane tracking stages or not (delta tracking) */
-            const int variants[][2] = {{4, 4}, {3, 3}, {3, 4}, {4, 3}, {2, 3}, {3, 2}, {2, 2}, {2, 4}};
-            const int modes_delta[] = {ER_PERSISTENT_SHADOW, ER_PERSISTENT_BOTH, ER_PERSISTENT_NONE};
+            const int variants[][2] = {{4, 4}, {3, 3}, {3, 4}, {4, 3}, {2, 3}, {3, 2}, {2, 2}, {2, 4}, {6, 4}, {4, 6}, {6, 6}};
+            const int modes_delta[] = {ER_PERSISTENT_SHADOW, ER_PERSISTENT_BOTH, ER_PERSISTENT_NONE, ER_PERSISTENT_PRIMARY};
             const int modes_march[] = {ER_PERSISTENT_SHADOW};
             const int* modes = delta ? modes_delta : modes_march;
-            const int n_modes = delta ? 3 : 1;
+            const int n_modes = delta ? 4 : 1;
             for (int mi = 0; mi < n_modes; mi++) {
                 s.tune_stages = modes[mi];
                 for (const auto& vv : variants) {

@@ -959,9 +959,10 @@ int sm_count()
     return sm > 0 ? sm : 132;
 }
 
-/* occupancy variants of the persistent and empty-space-skipping stages: 2,
-   3 or 4 resident blocks per SM (other values run 4) */
-int narrow_minb(int m) { return (m == 2 || m == 3) ? m : 4; }
+/* occupancy variants of the delta-tracking stages (persistent or per-thread,
+   all with the empty-space jump): 2, 3, 4 or 6 resident blocks per SM (other
+   values run 4) */
+int narrow_minb(int m) { return (m == 2 || m == 3 || m == 6) ? m : 4; }
 
 template <bool ONE>
 cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const WfView& one, const WavefrontPlan& plan,
@@ -987,17 +988,13 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         if (B.pt_primary) {
             /* delta tracking: persistent lanes, one resident wave */
             if (B.objects) ER_PRIMARY_PT(4, true, true);
-            else if (B.skip_primary) {
+            else {
+                /* persistent lanes run only with delta tracking, which always jumps */
                 switch (narrow_minb(B.tune_primary)) {
                 case 2: ER_PRIMARY_PT(2, false, true); break;
                 case 3: ER_PRIMARY_PT(3, false, true); break;
+                case 6: ER_PRIMARY_PT(6, false, true); break;
                 default: ER_PRIMARY_PT(4, false, true); break;
-                }
-            } else {
-                switch (narrow_minb(B.tune_primary)) {
-                case 2: ER_PRIMARY_PT(2, false, false); break;
-                case 3: ER_PRIMARY_PT(3, false, false); break;
-                default: ER_PRIMARY_PT(4, false, false); break;
                 }
             }
         } else if (B.objects) ER_PRIMARY(4, true, true);
@@ -1005,6 +1002,7 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
             switch (narrow_minb(B.tune_primary)) {
             case 2: ER_PRIMARY(2, false, true); break;
             case 3: ER_PRIMARY(3, false, true); break;
+            case 6: ER_PRIMARY(6, false, true); break;
             default: ER_PRIMARY(4, false, true); break;
             }
         } else {
@@ -1049,17 +1047,13 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
         if (B.pt_shadow) {
             /* ratio-tracked shadows: persistent lanes, one resident wave */
             if (B.objects) ER_SHADOW_PT(4, true, true);
-            else if (B.skip_shadow) {
+            else {
+                /* persistent lanes run only with delta tracking, which always jumps */
                 switch (narrow_minb(B.tune_shadow)) {
                 case 2: ER_SHADOW_PT(2, false, true); break;
                 case 3: ER_SHADOW_PT(3, false, true); break;
+                case 6: ER_SHADOW_PT(6, false, true); break;
                 default: ER_SHADOW_PT(4, false, true); break;
-                }
-            } else {
-                switch (narrow_minb(B.tune_shadow)) {
-                case 2: ER_SHADOW_PT(2, false, false); break;
-                case 3: ER_SHADOW_PT(3, false, false); break;
-                default: ER_SHADOW_PT(4, false, false); break;
                 }
             }
         } else if (B.objects) ER_SHADOW(4, true, true);
@@ -1067,6 +1061,7 @@ cudaError_t launch_windows(const WfView* d_views, const WfSegment* d_segs, const
             switch (narrow_minb(B.tune_shadow)) {
             case 2: ER_SHADOW(2, false, true); break;
             case 3: ER_SHADOW(3, false, true); break;
+            case 6: ER_SHADOW(6, false, true); break;
             default: ER_SHADOW(4, false, true); break;
             }
         } else {

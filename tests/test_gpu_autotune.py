@@ -54,11 +54,11 @@ def test_autotune_delta_sweep_and_cache(torch, lib, runtime, oracle, cache):
         assert first["majorant_brick"] in (1, 2, 4, 8, 16)
         assert first["tune_primary"] in (2, 3, 4, 6, 8) and first["tune_shadow"] in (2, 3, 4, 6, 8)
         assert first["tune_shade"] in (2, 3, 4, 6)
-        assert first["tune_stages"] & 3 in (C.PERSISTENT_SHADOW, C.PERSISTENT_BOTH, C.PERSISTENT_NONE)
+        assert first["tune_stages"] & 3 in (C.PERSISTENT_SHADOW, C.PERSISTENT_BOTH, C.PERSISTENT_NONE, C.PERSISTENT_PRIMARY)
         assert first["tune_stages"] & ~(3 | C.TUNE_NO_SKIP) == 0
-        # five brick sizes (the empty-space jump always on), occupancy pairs under three persistent-lane
-        # modes, shade variants
-        assert first["candidates"] == 5 + 3 * 8 + 4 and not first["from_cache"] and first["msamples_per_s"] > 0
+        # five brick sizes (the empty-space jump always on), eleven occupancy pairs under the four
+        # persistent-lane modes, four shade variants
+        assert first["candidates"] == 5 + 4 * 11 + 4 and not first["from_cache"] and first["msamples_per_s"] > 0
         assert cache.exists() and len(cache.read_text().splitlines()) == 1
         again = r.autotune(2)
         assert again["from_cache"] and again["candidates"] == 0
@@ -85,7 +85,7 @@ def test_autotune_march_skips_bricks(torch, lib, runtime, cache):
     r = runtime.Renderer(sc, lib)
     try:
         res = r.autotune(1)
-        assert res["candidates"] == 1 + 8 + 4      # the brick does not matter to the march
+        assert res["candidates"] == 1 + 11 + 4     # the brick does not matter to the march
         assert res["majorant_brick"] == 8
     finally:
         r.close()

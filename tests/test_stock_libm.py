@@ -11,7 +11,7 @@ crossing, a light pick) because an elementary function differed in its
 last bits: it shows as a different number of random draws, i.e. different
 RNG lane states after the frame (each draw advances both MWC lanes one
 step, Source/rng.h:35-51).  Pixels without a flip must agree to 1e-4
-relative (the benchmark spec's FP32 tolerance); flips are counted and each is
+relative (the FP32 tolerance of this path's parity); flips are counted and each is
 traced to the draw counts of both builds."""
 import os
 
