@@ -2214,6 +2214,44 @@ void ER_OR(intersect_volume_box)(or_scene* s, int32_t n, const float* r8, float*
     }
 }
 
+/* The majorant-brick walk of the trackers along rays (r8: origin,
+   direction, MinT, MaxT), with the empty-space jump or brick by brick
+   (jump = 0): per ray, up to `cap` records (t in, t out, bx, by, bz) of the
+   non-empty bricks it crosses, in order; counts[2 i] = records,
+   counts[2 i + 1] = DDA iterations.  Test infrastructure for the jump. */
+void ER_OR(dda_walk)(or_scene* s, int32_t n, const float* r8, int32_t jump, int32_t cap, float* out, int32_t* counts)
+{
+    for (int i = 0; i < n; i++) {
+        ray_t R;
+        R.O = V3(r8[8 * i], r8[8 * i + 1], r8[8 * i + 2]);
+        R.D = V3(r8[8 * i + 3], r8[8 * i + 4], r8[8 * i + 5]);
+        R.MinT = r8[8 * i + 6]; R.MaxT = r8[8 * i + 7];
+        int nrec = 0, iters = 0;
+        isect_t Int; isect_invalid(&Int);
+        intersect_box(&R, s->minp, vscale(s->size, 0.5f), &Int);
+        const float t0 = smax(Int.near_t, R.MinT);
+        const float t1 = smin(Int.far_t, R.MaxT);
+        if (Int.valid && t0 < t1 && s->majorant) {
+            dda_t d;
+            dda_init(s, &R, t0, t1, &d);
+            while (!d.done && iters < (1 << 20)) {
+                iters++;
+                const float e = dda_exit(&d);
+                const float mu = s->majorant[((size_t)d.b[2] * (size_t)s->nb[1] + (size_t)d.b[1]) * (size_t)s->nb[0] + (size_t)d.b[0]];
+                if (mu > 0.0f && nrec < cap) {
+                    float* o = out + ((size_t)i * cap + nrec) * 5;
+                    o[0] = d.t; o[1] = e; o[2] = (float)d.b[0]; o[3] = (float)d.b[1]; o[4] = (float)d.b[2];
+                    nrec++;
+                }
+                if (jump && mu <= -2.0f) dda_jump(s, &d, (int)(-mu));
+                else dda_advance(s, &d, e);
+            }
+        }
+        counts[2 * i] = nrec;
+        counts[2 * i + 1] = iters;
+    }
+}
+
 void ER_OR(concentric_sample_disk)(int32_t n, const float* u2, float* out2)
 {
     for (int i = 0; i < n; i++) {

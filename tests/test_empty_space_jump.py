@@ -4,6 +4,7 @@ volume that is empty but for two small boxes, the majorant reads per
 sample stay far below the bricks a ray crosses, and the image matches the
 binary64 build (which jumps the same way) within noise."""
 import numpy as np
+import pytest
 
 import oracle_lib as OL
 
@@ -98,3 +99,46 @@ def test_majorant_brick_size_does_not_change_the_image():
     for c in range(3):
         d = ma[..., c].sum() - mb[..., c].sum()
         assert abs(d) < 4.0 * np.sqrt((va[..., c].sum() + vb[..., c].sum()) / n)
+
+
+@pytest.mark.parametrize("brick", [1, 2, 4])
+def test_jump_crosses_the_same_non_empty_bricks(oracle, brick):
+    """Along 3000 random rays through the box, the walk with the empty-space
+    jump meets the same non-empty bricks, in the same order and over the
+    same ray segments (to float rounding of the face times), as the walk
+    brick by brick, in fewer DDA iterations: the jump never steps over a
+    brick whose majorant is positive."""
+    sc = sparse_scene()
+    sc.tracer.settings.majorant_brick = brick
+    h = OL.SceneHandle(oracle, sc)
+    try:
+        vf = np.zeros(13, dtype=np.float32)
+        oracle.volume_frame(h.h, OL.ptr(vf))
+        lo, size = vf[0:3].astype(np.float64), vf[10:13].astype(np.float64)
+        rng = np.random.default_rng(21 + brick)
+        n, cap = 3000, 256
+        target = lo + rng.uniform(0.0, 1.0, size=(n, 3)) * size
+        d = rng.normal(size=(n, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        origin = target - 2.0 * float(size.max()) * d
+        rays = np.zeros((n, 8), dtype=np.float32)
+        rays[:, 0:3], rays[:, 3:6], rays[:, 6], rays[:, 7] = origin, d, 0.0, 1e6
+        walks = []
+        for jump in (0, 1):
+            out = np.zeros((n, cap, 5), dtype=np.float32)
+            counts = np.zeros((n, 2), dtype=np.int32)
+            oracle.dda_walk(h.h, n, OL.ptr(rays), jump, cap, OL.ptr(out), OL.ptr(counts))
+            walks.append((out, counts))
+    finally:
+        h.close()
+    (a, ca), (b, cb) = walks
+    assert (ca[:, 0] < cap).all() and ca[:, 0].sum() > 1000          # the rays meet the boxes
+    assert cb[:, 1].sum() < 0.5 * ca[:, 1].sum()                      # far fewer iterations
+    scale = float(size.max()) * 4.0
+    for i in range(n):
+        sa = [r for r in a[i, :ca[i, 0]] if r[1] - r[0] > 1e-5 * scale]
+        sb = [r for r in b[i, :cb[i, 0]] if r[1] - r[0] > 1e-5 * scale]
+        assert len(sa) == len(sb), i
+        for ra, rb in zip(sa, sb):
+            assert np.array_equal(ra[2:], rb[2:]), i
+            assert np.allclose(ra[:2], rb[:2], rtol=1e-5, atol=1e-5 * scale), i
