@@ -2252,6 +2252,20 @@ void ER_OR(dda_walk)(or_scene* s, int32_t n, const float* r8, int32_t jump, int3
     }
 }
 
+/* For points p (3 floats each) given with a brick index b3 (3 ints each):
+   out2 = (the extinction a tracker in that brick looks up at p, the brick's
+   majorant).  Test infrastructure for the majorant bound. */
+void ER_OR(brick_bound)(or_scene* s, int32_t n, const float* p, const int32_t* b3, float* out2)
+{
+    for (int i = 0; i < n; i++) {
+        dda_t d;
+        memset(&d, 0, sizeof(d));
+        d.b[0] = b3[3 * i]; d.b[1] = b3[3 * i + 1]; d.b[2] = b3[3 * i + 2];
+        out2[2 * i] = sigma_in_brick(s, V3(p[3 * i], p[3 * i + 1], p[3 * i + 2]), &d);
+        out2[2 * i + 1] = s->majorant[((size_t)d.b[2] * (size_t)s->nb[1] + (size_t)d.b[1]) * (size_t)s->nb[0] + (size_t)d.b[0]];
+    }
+}
+
 void ER_OR(concentric_sample_disk)(int32_t n, const float* u2, float* out2)
 {
     for (int i = 0; i < n; i++) {

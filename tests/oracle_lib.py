@@ -78,6 +78,7 @@ class Oracle:
             f("math_eval", None, [c_int32, c_int32, c_void_p, c_void_p, c_void_p])
             f("majorant_grid", None, [c_void_p, c_void_p, c_int32, c_void_p, c_int32, c_float, c_void_p])
             f("dda_walk", None, [c_void_p, c_int32, c_void_p, c_int32, c_int32, c_void_p, c_void_p])
+            f("brick_bound", None, [c_void_p, c_int32, c_void_p, c_void_p, c_void_p])
 
     @staticmethod
     def _real_c(prefix):

@@ -142,3 +142,49 @@ def test_jump_crosses_the_same_non_empty_bricks(oracle, brick):
         for ra, rb in zip(sa, sb):
             assert np.array_equal(ra[2:], rb[2:]), i
             assert np.allclose(ra[:2], rb[:2], rtol=1e-5, atol=1e-5 * scale), i
+
+
+@pytest.mark.parametrize("brick", [1, 2, 3, 8])
+def test_majorant_bounds_every_tracker_lookup(oracle, brick):
+    """The extinction a tracker looks up at any point of a brick (local
+    coordinates clamped to the brick, here also points a little outside it,
+    as float rounding can place them) never exceeds the brick's majorant, and
+    is zero in empty bricks: a rough random volume, a transfer function that
+    rises and falls steeply, and a constant block where a blend rounding one
+    intensity below the corners' minimum reads a higher extinction."""
+    rng = np.random.default_rng(brick)
+    vol = rng.integers(0, 3000, size=(23, 19, 21)).astype(np.uint16)
+    vol[-12:, -12:, -12:] = 0                             # an empty corner (a whole 8^3 brick's footprint)
+    # a constant block just above a falling edge of the transfer function, at
+    # the origin: with a full-precision weight t (local coordinates below 1),
+    # a blend (1 - t) a + t a rounds below a for about 4% of t, and the
+    # truncation then reads the intensity one below, where the opacity is higher
+    vol[:7, :7, :7] = 501
+    lights, textures = S.c1_lights()
+    t = S.c1_tracer((16, 16))
+    t.opacity = C.make_plf([(0.0, 0.0), (499.0, 0.0), (500.0, 0.9), (501.0, 0.05), (1200.0, 0.5), (1201.0, 0.0),
+                            (2000.0, 0.0), (2999.5, 1.0)])
+    sc = S.Scene("rough", vol, tracer=t, lights=lights, textures=textures)
+    s = sc.tracer.settings
+    s.free_flight, s.majorant_brick = 1, brick
+    h = OL.SceneHandle(oracle, sc)
+    try:
+        vf = np.zeros(13, dtype=np.float32)
+        oracle.volume_frame(h.h, OL.ptr(vf))
+        res = np.array([21, 19, 23], dtype=np.float64)     # x, y, z
+        nb = np.ceil(res / brick).astype(np.int64)
+        n = 200000
+        b = np.stack([rng.integers(0, nb[a], size=n) for a in range(3)], axis=1)
+        # points up to 0.3 brick outside their brick: the clamp must keep every blend in the footprint
+        L = (b + rng.uniform(-0.3, 1.3, size=(n, 3))) * brick
+        L = np.minimum(L, res)
+        p = (vf[0:3].astype(np.float64) + L / (vf[3:6].astype(np.float64) * res)).astype(np.float32)
+        out = np.zeros((n, 2), dtype=np.float32)
+        oracle.brick_bound(h.h, n, OL.ptr(np.ascontiguousarray(p)), OL.ptr(np.ascontiguousarray(b.astype(np.int32))), OL.ptr(out))
+    finally:
+        h.close()
+    sig, mu = out[:, 0], out[:, 1]
+    full = mu > 0.0
+    assert full.sum() > 1000 and (~full).sum() > 100
+    assert (sig[full] <= mu[full]).all(), float((sig[full] - mu[full]).max())
+    assert (sig[~full] == 0.0).all()
