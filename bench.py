@@ -328,9 +328,10 @@ def film_convergence(lib, torch, r, patches, ref_patch, ref_spp, target=1e-2, bu
     configuration of `patches` then renders from view 0 along FILM_SCHEDULE
     until its RMSE reaches `target` (or `budget_s` of rendering is spent).
     `film`: (W, H) of the bound tracer's camera when it differs from the
-    scene's.  `unbiased`: the configurations with the reference's
-    expectation, whose samples-to-target come from a fit of the whole curve
-    (the others, such as the biased fixed-step march, from the crossing)."""
+    scene's.  Samples-to-target is where the measured curve crosses the
+    target (log-log interpolation between the bracketing points);
+    `unbiased` names the configurations with the reference's expectation,
+    for which a fit of the whole curve is reported beside it."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import convergence as CV
     W, H = film if film else (r.width, r.height)
@@ -385,15 +386,12 @@ def film_convergence(lib, torch, r, patches, ref_patch, ref_spp, target=1e-2, bu
         crossing = CV.spp_to_rmse(spps, errs, target)
         out[label] = {"spp": spps, "rmse": errs, "spp_to_target": crossing}
         if label in unbiased:
-            # an estimator with the reference's expectation converges as
-            # rmse^2 = var / n: every schedule point from 32 spp on implies
-            # n (rmse / target)^2; their geometric mean is far less noisy than
-            # the crossing of two points when rare bright samples dominate
+            # a cross-check for an estimator with the reference's expectation,
+            # which converges as rmse^2 = var / n: every schedule point from
+            # 32 spp on implies n (rmse / target)^2; their geometric mean
             implied = [n_ * (e_ / target) ** 2 for n_, e_ in zip(spps, errs) if n_ >= 32 and e_ > 0]
             if implied:
-                out[label]["spp_to_target"] = float(np.exp(np.mean(np.log(implied))))
-                out[label]["spp_to_target_crossing"] = crossing
-                out[label]["method"] = "geometric mean of n (rmse_n / target)^2 over the points n >= 32"
+                out[label]["spp_to_target_fit"] = float(np.exp(np.mean(np.log(implied))))
         del acc
     apply(saved)
     return out
@@ -407,7 +405,7 @@ def film_rmse_summary(fc, fast_value, plain_value, npix, target=1e-2):
     f, p = fc["fast"]["spp_to_target"], fc["plain"]["spp_to_target"]
     out = {"target": target, "reference": fc["reference"],
            "fast": {"spp": f, "seconds": f * npix / (fast_value * 1e6) if f else None, "curve": [fc["fast"]["spp"], fc["fast"]["rmse"]],
-                    "spp_crossing": fc["fast"].get("spp_to_target_crossing"), "method": fc["fast"].get("method", "crossing")},
+                    "spp_fit": fc["fast"].get("spp_to_target_fit")},
            "plain": {"spp": p, "seconds": p * npix / (plain_value * 1e6) if p else None,
                      "curve": [fc["plain"]["spp"], fc["plain"]["rmse"]]}}
     if f and p:
@@ -446,8 +444,8 @@ def batched_rmse_summary(conv, value, plain_value, target=1e-2):
         if "reference" in c and isinstance(c["reference"], dict):
             per[name]["film"] = c["reference"]["film"]
             per[name]["curves"] = {k: [c[k]["spp"], c[k]["rmse"]] for k in ("fast", "plain")}
-            if "spp_to_target_crossing" in c["fast"]:
-                per[name]["fast_spp_crossing"] = c["fast"]["spp_to_target_crossing"]
+            if "spp_to_target_fit" in c["fast"]:
+                per[name]["fast_spp_fit"] = c["fast"]["spp_to_target_fit"]
         if f and p:
             ratios.append(p / f)
     out = {"target": target, "views": per, "throughput_ratio": value / plain_value}
