@@ -119,6 +119,18 @@ int refill_eighths()
     return v;
 }
 
+/* lanes of the wavefront's tracking stages in 8x4 pixel tiles (1) or row
+   by row (0): ER_TILE_ORDER, for measurements; row by row by default */
+int tile_order()
+{
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("ER_TILE_ORDER");
+        v = (e && atoi(e) == 1) ? 1 : 0;
+    }
+    return v;
+}
+
 /* queues of the wavefront stages, grown to the largest plan seen */
 struct WfQueues {
     DevBuf<float4> results, events, jobs, partial, records;
@@ -561,6 +573,7 @@ er_status build(TracerItem& t)
     ER_CUDA(er_launch_shade_table(t.tfs.p, t.shade_tab.p, n, st));
     P.shade_tab = t.shade_tab.p;
     P.free_flight = s.free_flight;
+    P.tile_order = tile_order();
     if (s.free_flight == ER_FREE_FLIGHT_DELTA) {
         int nb[3];
         for (int i = 0; i < 3; i++) nb[i] = (v.res[i] + brick - 1) / brick;

@@ -66,6 +66,20 @@ ER_D const WfView& view_of(const WfView* __restrict__ views, const WfView& one, 
     return views[v];
 }
 
+/* the pixel of slot j of a sample row: row by row, or (tile_order) in 8x4
+   tiles, row by row of tiles, so that a warp's 32 lanes trace an 8x4
+   block of neighbouring pixels; a bijection of [0, W H), so the reduce
+   stage maps the slots back (slot_pixel) */
+ER_D uint32_t slot_pixel(const Params& P, uint32_t j)
+{
+    const int W = P.film[0], H = P.film[1];
+    if (!P.tile_order || (W & 7) || (H & 3)) return j;
+    const uint32_t t = j >> 5, u = j & 31u;
+    const uint32_t tw = (uint32_t)W >> 3;
+    const uint32_t x = (t % tw) * 8u + (u & 7u), y = (t / tw) * 4u + (u >> 3);
+    return y * (uint32_t)W + x;
+}
+
 /* segment of a window holding window-local item i (segments are sorted by offset) */
 ER_D int find_segment(const WfSegment* __restrict__ segs, int nseg, uint32_t i)
 {
@@ -115,7 +129,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary(const WfView* __restri
             const uint32_t local = i - sg.offset;
             const uint32_t npix = (uint32_t)(P.film[0] * P.film[1]);
             const int s = sg.s0 + (int)(local / npix);
-            const int pix = (int)(local % npix);
+            const int pix = (int)slot_pixel(P, local % npix);
             const int x = pix % P.film[0], y = pix / P.film[0];
             er_seed_lanes(P.seed, V.view_id, (uint32_t)pix, V.first + (uint32_t)s, &rng.s0, &rng.s1);
             ms.large_step(rng);
@@ -237,7 +251,7 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary_pt(const WfView* __res
             const uint32_t local = i - sg.offset;
             const uint32_t npix = (uint32_t)(P.film[0] * P.film[1]);
             const int s = sg.s0 + (int)(local / npix);
-            const int pix = (int)(local % npix);
+            const int pix = (int)slot_pixel(P, local % npix);
             er_seed_lanes(P.seed, V.view_id, (uint32_t)pix, V.first + (uint32_t)s, &rng.s0, &rng.s1);
             Metro ms;
             ms.large_step(rng);
@@ -301,10 +315,10 @@ __global__ void __launch_bounds__(256, MINB) k_wf_primary_pt(const WfView* __res
             const uint32_t npix = (uint32_t)(P.film[0] * P.film[1]);
             Rng r0;
             const uint32_t sidx = V.first + (uint32_t)(sg.s0 + (int)(local / npix));
-            er_seed_lanes(P.seed, V.view_id, local % npix, sidx, &r0.s0, &r0.s1);
+            er_seed_lanes(P.seed, V.view_id, slot_pixel(P, local % npix), sidx, &r0.s0, &r0.s1);
             Metro ms;
             ms.large_step(r0);
-            ms.stratify(P, V.view_id, local % npix, sidx);
+            ms.stratify(P, V.view_id, slot_pixel(P, local % npix), sidx);
             const bool obj = OBJ && SE.type == 2;
             float4* e = events + (size_t)slot * 5;
             e[0] = make_float4(u2f(i), u2f(rng.s0), u2f(rng.s1), ms.light_num);
@@ -836,21 +850,22 @@ __global__ void k_wf_reduce(const WfView* __restrict__ views, const WfSegment* _
     const WfSegment sg = ONE ? one_seg : segs[blockIdx.y];
     const WfView& V = view_of<ONE>(views, one, sg.view);
     const int npix = V.P.film[0] * V.P.film[1];
-    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= npix) return;
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= npix) return;
     float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
     if (sg.s0 > 0) {
-        const float4 p = partial_in[pix];
+        const float4 p = partial_in[slot];
         a0 = p.x; a1 = p.y; a2 = p.z; a3 = p.w;
     }
     for (int s = sg.s0; s < sg.s1; s++) {
-        const float4 o = results[(size_t)sg.offset + (size_t)(s - sg.s0) * npix + pix];
+        const float4 o = results[(size_t)sg.offset + (size_t)(s - sg.s0) * npix + slot];
         a0 += o.x; a1 += o.y; a2 += o.z; a3 += o.w;
     }
     if (sg.s1 < V.spp) {
-        partial_out[pix] = make_float4(a0, a1, a2, a3);
+        partial_out[slot] = make_float4(a0, a1, a2, a3);
         return;
     }
+    const uint32_t pix = slot_pixel(V.P, (uint32_t)slot);
     float4 r = make_float4(a0, a1, a2, a3);
     if (V.accumulate) {
         const float4 q = V.sum[pix];
