@@ -112,7 +112,8 @@ struct Params {
                                 0: quads x fastest over the whole volume */
     unsigned long long qb_slab;  /* bricked quads: entries per z-slab of bricks (nbx * nby * 512) */
     int tile_order;          /* wavefront: the samples of a sample row go to lanes in 8x4 pixel tiles
-                                (films with width % 8 == 0 and height % 4 == 0), else row by row */
+                                (films with width % 8 == 0 and height % 4 == 0; the default), else row
+                                by row */
     int res[3];
     float minp[3];
     float inv_size[3];

@@ -119,14 +119,15 @@ int refill_eighths()
     return v;
 }
 
-/* lanes of the wavefront's tracking stages in 8x4 pixel tiles (1) or row
-   by row (0): ER_TILE_ORDER, for measurements; row by row by default */
+/* lanes of the wavefront's tracking stages in 8x4 pixel tiles (the default;
+   C2 1346 -> 1475, C3 2231 -> 2341 Msamples/s, the free-flight stage 17% and
+   7% faster) or row by row (ER_TILE_ORDER=0, for measurements) */
 int tile_order()
 {
     static int v = -1;
     if (v < 0) {
         const char* e = getenv("ER_TILE_ORDER");
-        v = (e && atoi(e) == 1) ? 1 : 0;
+        v = (e && atoi(e) == 0) ? 0 : 1;
     }
     return v;
 }
