@@ -121,13 +121,15 @@ int refill_eighths()
 
 /* lanes of the wavefront's tracking stages in 8x4 pixel tiles (the default;
    C2 1346 -> 1475, C3 2231 -> 2341 Msamples/s, the free-flight stage 17% and
-   7% faster) or row by row (ER_TILE_ORDER=0, for measurements) */
+   7% faster), or for measurements (ER_TILE_ORDER) row by row (0), 4x8 (2)
+   or 16x2 (3) tiles */
 int tile_order()
 {
     static int v = -1;
     if (v < 0) {
         const char* e = getenv("ER_TILE_ORDER");
-        v = (e && atoi(e) == 0) ? 0 : 1;
+        const int r = e ? atoi(e) : 1;
+        v = (r >= 0 && r <= 3) ? r : 1;
     }
     return v;
 }

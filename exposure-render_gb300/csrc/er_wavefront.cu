@@ -66,17 +66,19 @@ ER_D const WfView& view_of(const WfView* __restrict__ views, const WfView& one, 
     return views[v];
 }
 
-/* the pixel of slot j of a sample row: row by row, or (tile_order) in 8x4
-   tiles, row by row of tiles, so that a warp's 32 lanes trace an 8x4
-   block of neighbouring pixels; a bijection of [0, W H), so the reduce
-   stage maps the slots back (slot_pixel) */
+/* the pixel of slot j of a sample row: row by row, or (tile_order) in
+   tiles of 32 pixels, row by row of tiles, so that a warp's 32 lanes trace a
+   block of neighbouring pixels (tile_order 1: 8x4, 2: 4x8, 3: 16x2); a
+   bijection of [0, W H), so the reduce stage maps the slots back */
 ER_D uint32_t slot_pixel(const Params& P, uint32_t j)
 {
     const int W = P.film[0], H = P.film[1];
-    if (!P.tile_order || (W & 7) || (H & 3)) return j;
+    const int lw = P.tile_order == 1 ? 3 : (P.tile_order == 2 ? 2 : 4);     /* log2 of the tile width */
+    const uint32_t tx = 1u << lw, ty = 32u >> lw;
+    if (!P.tile_order || ((uint32_t)W & (tx - 1u)) || ((uint32_t)H & (ty - 1u))) return j;
     const uint32_t t = j >> 5, u = j & 31u;
-    const uint32_t tw = (uint32_t)W >> 3;
-    const uint32_t x = (t % tw) * 8u + (u & 7u), y = (t / tw) * 4u + (u >> 3);
+    const uint32_t tw = (uint32_t)W >> lw;
+    const uint32_t x = (t % tw) * tx + (u & (tx - 1u)), y = (t / tw) * ty + (u >> lw);
     return y * (uint32_t)W + x;
 }
 
