@@ -111,9 +111,9 @@ struct Params {
     int qb_nbx;              /* quads in 8^3 bricks (brick-major, x fastest inside a brick): bricks along x;
                                 0: quads x fastest over the whole volume */
     unsigned long long qb_slab;  /* bricked quads: entries per z-slab of bricks (nbx * nby * 512) */
-    int tile_order;          /* wavefront: the samples of a sample row go to lanes in 8x4 pixel tiles
-                                (films with width % 8 == 0 and height % 4 == 0; the default), else row
-                                by row */
+    int tile_order;          /* wavefront: the samples of a sample row go to lanes in tiles of 32
+                                pixels (1: 8x4, 2: 4x8, the default, 3: 16x2; films whose sides are
+                                multiples of the tile's), else (0) row by row */
     int res[3];
     float minp[3];
     float inv_size[3];

@@ -119,17 +119,17 @@ int refill_eighths()
     return v;
 }
 
-/* lanes of the wavefront's tracking stages in 8x4 pixel tiles (the default;
-   C2 1346 -> 1475, C3 2231 -> 2341 Msamples/s, the free-flight stage 17% and
-   7% faster), or for measurements (ER_TILE_ORDER) row by row (0), 4x8 (2)
+/* lanes of the wavefront's tracking stages in 4x8 pixel tiles (the default;
+   C2 row order / 8x4 / 4x8 / 16x2: 1346 / 1463-1475 / 1499 / 1405
+   Msamples/s), or for measurements (ER_TILE_ORDER) row by row (0), 8x4 (1)
    or 16x2 (3) tiles */
 int tile_order()
 {
     static int v = -1;
     if (v < 0) {
         const char* e = getenv("ER_TILE_ORDER");
-        const int r = e ? atoi(e) : 1;
-        v = (r >= 0 && r <= 3) ? r : 1;
+        const int r = e ? atoi(e) : 2;
+        v = (r >= 0 && r <= 3) ? r : 2;
     }
     return v;
 }
