@@ -891,9 +891,11 @@ def run_batched(args, rank, world, local_rank, wl="c3"):
     # GPU render of the unbiased estimator
     conv, film_conv = None, None
     if world == 1 and not args.no_rmse and wl == "c5":
-        # c5: no FP64 oracle image of the 1024x1024x512 volume (the oracle
-        # would need minutes per 128^2 view); its first view at 2048^2 against
-        # the converged GPU render of the unbiased estimator
+        # c5: its first view on a 128^2 film against the FP64 oracle's
+        # converged image (tests/golden/fp64_c5v0.npz), and at 2048^2
+        # against the converged GPU render of the unbiased estimator
+        conv = convergence(lib, runtime, torch, ["c5v0"],
+                           {"fast": {"free_flight": 1, "stratify": 1}, "plain": {"free_flight": 0, "stratify": 0}})
         r = rs[0]
         cam = views[0][1]
         saved = C.er_tracer_desc.from_buffer_copy(r.tracer_desc)

@@ -445,9 +445,10 @@ def rmse_views(film=128, names=None) -> list:
     """(name, Scene) of the views whose converged images the FP64 oracle
     provides: the c1 scene with the BRDF at every volume event (the
     reference's live shading) and with the isotropic phase function (c1p,
-    the c1 workload's shading), the first view of each c3 volume, and c2 -
-    all at a film of `film`^2 with each workload's camera and settings.
-    `names` restricts the list (and the volumes generated)."""
+    the c1 workload's shading), the first view of each c3 volume, c2, and -
+    only when named, as its volume is 1 GiB - the first c5 view (c5v0); all
+    at a film of `film`^2 with each workload's camera and settings.  `names`
+    restricts the list (and the volumes generated)."""
     want = set(names) if names else {"c1", "c1p", "c3v0", "c3v1", "c3v2", "c2"}
     out = []
     if "c1" in want:
@@ -466,6 +467,13 @@ def rmse_views(film=128, names=None) -> list:
             out.append((f"c3v{k}", sc))
     if "c2" in want:
         out.append(("c2", scene_c2(res=512, film=(film, film))))
+    if "c5v0" in want:
+        sc = scene_c5(film=(film, film))
+        sc.name = "c5v0"
+        cam = C.er_camera_desc.from_buffer_copy(c5_views()[0][1])
+        cam.film_size[0] = cam.film_size[1] = film
+        sc.tracer.camera = cam
+        out.append(("c5v0", sc))
     return out
 
 

@@ -9,7 +9,7 @@ random stream (seed 0x5EED64, view 7), rendered as two independent halves;
 the squared tone-mapped difference of the halves / 4 is the reference's own
 noise, stored as noise2.
 
-    python tests/golden/make_fp64.py [spp]
+    python tests/golden/make_fp64.py [spp [view ...]]     (c5v0 only when named)
 """
 import os
 import sys
@@ -31,9 +31,7 @@ def main():
     names = sys.argv[2:] if len(sys.argv) > 2 else None
     f64 = OL.load_fp64()
     nthreads = os.cpu_count() or 1
-    for name, sc in S.rmse_views():
-        if names and name not in names:
-            continue
+    for name, sc in S.rmse_views(names=names or None):
         st = sc.tracer.settings
         st.free_flight = C.FREE_FLIGHT_DELTA
         st.mis = C.MIS_FULL

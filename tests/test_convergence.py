@@ -32,7 +32,7 @@ def test_tonemap_matches_oracle_bytes():
     assert np.all(np.abs(np.floor(255.0 * tm) - rgba[:, :3]) <= 1)
 
 
-@pytest.mark.parametrize("name", ["c1", "c3v0", "c3v1", "c3v2", "c2"])
+@pytest.mark.parametrize("name", ["c1", "c1p", "c3v0", "c3v1", "c3v2", "c2", "c5v0"])
 def test_fp64_reference_fixture(name):
     p = os.path.join(CV.GOLDEN, f"fp64_{name}.npz")
     assert os.path.exists(p), "run tests/golden/make_fp64.py"
